@@ -1,0 +1,245 @@
+/*
+ * rpgo_gb300 — C ABI of the GB300-native Kimera-RPGO robust back-end.
+ *
+ * Plain C, plain pointers and sizes. Every compute call runs on CUDA device 0
+ * of the calling process (one GPU, sm_103a); there is no CPU fallback: if the
+ * device or the kernels are unavailable, calls fail with RPGO_ERR_CUDA.
+ *
+ * Pose layout (row-major, doubles):
+ *   3D (Pose3): 12 values  R00 R01 R02 R10 R11 R12 R20 R21 R22 tx ty tz
+ *   2D (Pose2):  4 values  cos(theta) sin(theta) x y
+ * Tangent order follows GTSAM: Pose3 [omega; v], Pose2 [v_x, v_y, omega].
+ * Covariance / square-root information blocks are dim x dim row-major with
+ * dim = 6 (3D) or 3 (2D). sqrt_information is the upper-triangular R with
+ * R^T R = information; the solver whitens residuals with it, PCM reads the
+ * covariance (as the reference reads noiseModel()->covariance()).
+ * Keys are 64-bit gtsam::Symbol values: (char << 56) | index.
+ */
+#ifndef RPGO_GB300_H
+#define RPGO_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+enum {
+  RPGO_OK = 0,
+  RPGO_ERR_ARG = 1,        /* bad argument (null pointer, bad enum, size) */
+  RPGO_ERR_CUDA = 2,       /* CUDA runtime / kernel failure */
+  RPGO_ERR_KEY = 3,        /* value key already present, or missing key */
+  RPGO_ERR_SOLVER = 4,     /* linear system not positive definite (GN) */
+  RPGO_ERR_UNSUPPORTED = 5 /* feature outside the implemented path */
+};
+
+/* --------------------------------------------------------------- enumerants
+ * Mirror of include/KimeraRPGO/SolverParams.h:13-27 (Solver,
+ * OutlierRemovalMethod, Verbosity). */
+enum { RPGO_SOLVER_LM = 0, RPGO_SOLVER_GN = 1 };
+enum {
+  RPGO_OUTLIER_NONE = 0,
+  RPGO_OUTLIER_PCM2D = 1,
+  RPGO_OUTLIER_PCM3D = 2,
+  RPGO_OUTLIER_PCM_SIMPLE2D = 3,
+  RPGO_OUTLIER_PCM_SIMPLE3D = 4
+};
+enum { RPGO_VERBOSITY_UPDATE = 0, RPGO_VERBOSITY_QUIET = 1, RPGO_VERBOSITY_VERBOSE = 2 };
+enum { RPGO_GNC_COST = 0, RPGO_GNC_PROBABILITY = 1 };
+enum { RPGO_FACTOR_BETWEEN = 0, RPGO_FACTOR_PRIOR = 1 };
+
+/* Flat mirror of RobustSolverParams (include/KimeraRPGO/SolverParams.h:80-299)
+ * with PcmParams (33-56) and GncParams (58-78) inlined. */
+typedef struct rpgo_params {
+  int32_t solver;            /* RPGO_SOLVER_* */
+  int32_t outlier_removal;   /* RPGO_OUTLIER_* */
+  int32_t verbosity;         /* RPGO_VERBOSITY_* */
+  int32_t dim;               /* 2 or 3; required when outlier_removal == NONE */
+  /* PcmParams */
+  double odom_threshold, lc_threshold;
+  double odom_trans_threshold, odom_rot_threshold;
+  double dist_trans_threshold, dist_rot_threshold;
+  int32_t incremental;
+  /* GncParams */
+  int32_t use_gnc;
+  int32_t gnc_threshold_mode; /* RPGO_GNC_* */
+  double gnc_inlier_threshold;
+  int32_t gnc_max_iterations;
+  double gnc_mu_step, gnc_relative_cost_tol, gnc_weights_tol;
+  int32_t gnc_fix_prev_inliers, gnc_bias_odom;
+  /* additional */
+  int32_t lm_diagonal_damping;
+} rpgo_params;
+
+/* A batch of factors (structure of arrays). For priors key_back is ignored. */
+typedef struct rpgo_factor_batch {
+  int64_t count;
+  const int32_t* kind;             /* RPGO_FACTOR_* */
+  const uint64_t* key_front;
+  const uint64_t* key_back;
+  const double* measured;          /* count x pose stride (12 or 4) */
+  const double* covariance;        /* count x dim x dim */
+  const double* sqrt_information;  /* count x dim x dim */
+} rpgo_factor_batch;
+
+typedef struct rpgo_value_batch {
+  int64_t count;
+  const uint64_t* key;
+  const double* pose;              /* count x pose stride */
+} rpgo_value_batch;
+
+typedef struct rpgo_counts {
+  int64_t num_factors;        /* size of the graph to optimise (getFactorsUnsafe) */
+  int64_t num_values;         /* calculateEstimate().size() */
+  int64_t num_lc;             /* getNumLC */
+  int64_t num_lc_inliers;     /* getNumLCInliers */
+  int64_t num_odom;           /* odometry factors kept by PCM */
+  int64_t num_special;        /* non-between factors (priors) */
+  int64_t num_gnc_weights;    /* getGncWeights().size() */
+  int64_t last_do_optimize;   /* value removeOutliers / addAndCheckIfOptimize returned in the last update */
+} rpgo_counts;
+
+typedef struct rpgo_timing {
+  double pcm_ms;              /* classification, trajectory, odometry + pairwise checks, clique */
+  double solve_ms;            /* GNC / LM / GN */
+  int64_t pair_checks;        /* pairwise consistency tests run */
+  int64_t lm_iterations;      /* accepted LM/GN iterations summed over the GNC schedule */
+  int64_t linear_solves;      /* damped systems solved */
+  int64_t gnc_iterations;     /* outer GNC iterations */
+  int64_t cg_iterations;      /* preconditioned CG iterations */
+  int64_t kernel_launches;    /* kernels of this library launched by the last update */
+} rpgo_timing;
+
+typedef struct rpgo_solver rpgo_solver; /* opaque */
+
+/* ------------------------------------------------------------------ params
+ * RobustSolverParams::RobustSolverParams (SolverParams.h:82-94) defaults. */
+void rpgo_params_default(rpgo_params* p);
+/* SolverParams.h:97-100 */
+void rpgo_params_set_no_rejection(rpgo_params* p, int32_t verbosity);
+/* SolverParams.h:119-126 / 134-141 */
+void rpgo_params_set_pcm2d(rpgo_params* p, double odom_threshold, double lc_threshold, int32_t verbosity);
+void rpgo_params_set_pcm3d(rpgo_params* p, double odom_threshold, double lc_threshold, int32_t verbosity);
+/* SolverParams.h:148-209 (four-threshold overloads; the two-threshold
+ * overloads pass the same pair twice) */
+void rpgo_params_set_pcm_simple2d(rpgo_params* p, double trans_odom, double rot_odom, double trans_pcm,
+                                  double rot_pcm, int32_t verbosity);
+void rpgo_params_set_pcm_simple3d(rpgo_params* p, double trans_odom, double rot_odom, double trans_pcm,
+                                  double rot_pcm, int32_t verbosity);
+/* SolverParams.h:213-250 */
+void rpgo_params_set_gnc_probability(rpgo_params* p, double alpha, int32_t max_iterations, double mu_step,
+                                     double rel_cost_tol, double weight_tol, int32_t fix_prev_inliers,
+                                     int32_t bias_odom);
+void rpgo_params_set_gnc_cost(rpgo_params* p, double cost, int32_t max_iterations, double mu_step,
+                              double rel_cost_tol, double weight_tol, int32_t fix_prev_inliers,
+                              int32_t bias_odom);
+
+/* ------------------------------------------------------------------ solver
+ * RobustSolver::RobustSolver (src/RobustSolver.cpp:29-103). Returns NULL on a
+ * bad parameter set (the reference calls exit(EXIT_FAILURE)) or when no CUDA
+ * device is usable. */
+rpgo_solver* rpgo_create(const rpgo_params* p);
+void rpgo_destroy(rpgo_solver* s);
+
+/* RobustSolver::update (src/RobustSolver.cpp:337-369): PCM outlier rejection
+ * (Pcm::removeOutliers, include/KimeraRPGO/outlier/Pcm.h:148-281) then, if
+ * something changed and optimize_graph != 0, the GNC / LM / GN solve
+ * (RobustSolver::optimize, src/RobustSolver.cpp:115-306). */
+int rpgo_update(rpgo_solver* s, const rpgo_factor_batch* factors, const rpgo_value_batch* values,
+                int32_t optimize_graph);
+/* RobustSolver::forceUpdate (src/RobustSolver.cpp:308-335) */
+int rpgo_force_update(rpgo_solver* s, const rpgo_factor_batch* factors, const rpgo_value_batch* values);
+
+/* README.md:114-118 loadGraph / addGraph, written as update() wrappers:
+ * loadGraph(nfg, values, prior) = update(nfg + prior, values);
+ * addGraph(nfg, values, between) = update(nfg + between, values). The extra
+ * factor is a batch of one appended after `factors`. */
+int rpgo_load_graph(rpgo_solver* s, const rpgo_factor_batch* factors, const rpgo_value_batch* values,
+                    const rpgo_factor_batch* prior);
+int rpgo_add_graph(rpgo_solver* s, const rpgo_factor_batch* factors, const rpgo_value_batch* values,
+                   const rpgo_factor_batch* between);
+
+/* getters (RobustSolver.h:40-47, 110-117; GenericSolver.h:38-41) */
+int rpgo_get_counts(const rpgo_solver* s, rpgo_counts* out);
+/* calculateEstimate(): keys ascending; arrays sized by counts.num_values */
+int rpgo_get_estimate(const rpgo_solver* s, uint64_t* keys, double* poses, int64_t capacity);
+/* getGncWeights(): sized by counts.num_gnc_weights */
+int rpgo_get_gnc_weights(const rpgo_solver* s, double* weights, int64_t capacity);
+/* getFactorsUnsafe(): the graph handed to the optimiser, in its order */
+int rpgo_get_factors(const rpgo_solver* s, int32_t* kind, uint64_t* key_front, uint64_t* key_back,
+                     double* measured, int64_t capacity);
+/* Test hook: the bit-packed symmetric adjacency of loop-closure group `group`
+ * (groups in the order buildGraphToOptimize visits them, Pcm.h:977-1005),
+ * n x ceil(n/32) uint32 words, bit j of row i set when closures i and j are
+ * pairwise consistent. Returns the group size in *n. */
+int rpgo_get_adjacency(const rpgo_solver* s, int32_t group, uint32_t* words, int64_t capacity, int64_t* n);
+int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* out);
+/* RobustSolver::saveData (src/RobustSolver.cpp:448-465): result.g2o and
+ * gnc_weights.csv in `folder`. */
+int rpgo_save_data(const rpgo_solver* s, const char* folder);
+
+/* ------------------------------------------------------------ stage kernels
+ * Device-resident entry points of the hot path, one per reference function
+ * family, for callers that keep the graph in GPU memory. All pointers are
+ * device pointers; `stream` is a cudaStream_t (0 = legacy default stream).
+ * Trajectory entries are addressed by slot (int32); slot layout:
+ *   pose: stride 12 (3D) or 4 (2D) doubles; cov: dim*dim doubles;
+ *   node: int32 (PcmSimple); rot_info: uint8.
+ */
+
+/* Odometry chain composition, Pcm::updateOdom (Pcm.h:516-557) applied in
+ * order for `count` odometry factors: traj[dst[k]] = traj[src[k]] o delta[k].
+ * mode 0: PoseWithCovariance, 1: PoseWithNode. */
+int rpgo_trajectory_scan_dev(int32_t dim, int32_t mode, int64_t count, const int32_t* src, const int32_t* dst,
+                             const double* delta_pose, const double* delta_cov, double* traj_pose, double* traj_cov,
+                             int32_t* traj_node, uint8_t* traj_rot_info, void* stream);
+
+/* Odometry consistency, Pcm::isOdomConsistent + checkOdomConsistent
+ * (Pcm.h:564-629) for `count` closures i -> j with measurement z:
+ * ok[k] = 1 when consistent. mode 0: Mahalanobis against th0; mode 1:
+ * average translation/rotation norms against th0/th1. */
+int rpgo_odometry_check_dev(int32_t dim, int32_t mode, int64_t count, const int32_t* slot_i, const int32_t* slot_j,
+                            const double* z_pose, const double* z_cov, const double* traj_pose,
+                            const double* traj_cov, const int32_t* traj_node, const uint8_t* traj_rot_info,
+                            double th0, double th1, uint8_t* ok, void* stream);
+
+/* Pairwise consistency, Pcm::incrementAdjMatrix + areLoopsConsistent
+ * (Pcm.h:670-768) for rows [row_begin, n) of an n-closure group: for every
+ * i < j with j >= row_begin, closure i = (a_i -> b_i, z_i) is tested against
+ * closure j = (c_j -> d_j, z_j) (c/d swapped when `flip` of i and j differ),
+ * and bits (i, j), (j, i) of `adj` (n rows of `words` uint32) are set or
+ * cleared. Rows and columns below row_begin in the upper-left block are left
+ * as they are. */
+int rpgo_pairwise_adjacency_dev(int32_t dim, int32_t mode, int32_t n, int32_t row_begin, const int32_t* slot_a,
+                                const int32_t* slot_b, const uint8_t* flip, const double* z_pose,
+                                const double* z_cov, const double* traj_pose, const double* traj_cov,
+                                const int32_t* traj_node, const uint8_t* traj_rot_info, double th0, double th1,
+                                uint32_t* adj, int32_t words, void* stream);
+
+/* Greedy max clique, findMaxCliqueHeu / findMaxCliqueHeuIncremental
+ * (src/utils/GraphUtils.cpp:19-44, findCliqueHeu.cpp:32-209) on the
+ * bit-packed adjacency (device): candidates first..n-1, running best seeded
+ * with `seed` (-1 for the full search). Writes the size to *size_out (host)
+ * and the first *size_out entries of the winning work buffer to clique_out
+ * (host, capacity n); *size_out equals `seed` when nothing improved. */
+int rpgo_max_clique_heu_dev(int32_t n, const uint32_t* adj, int32_t words, int32_t first, int32_t seed,
+                            int32_t* clique_out, int32_t* size_out, void* stream);
+
+/* ------------------------------------------------------------- host copies
+ * The same stages on host arrays (copies in, copies out), for tests and for
+ * callers without device memory management. */
+int rpgo_pairwise_adjacency(int32_t dim, int32_t mode, int32_t n, const int32_t* slot_a, const int32_t* slot_b,
+                            const uint8_t* flip, const double* z_pose, const double* z_cov, int32_t num_slots,
+                            const double* traj_pose, const double* traj_cov, const int32_t* traj_node,
+                            const uint8_t* traj_rot_info, double th0, double th1, uint32_t* adj);
+int rpgo_max_clique_heu(int32_t n, const uint32_t* adj, int32_t first, int32_t seed, int32_t* clique_out,
+                        int32_t* size_out);
+
+/* Library / device information (name of the loaded device, SM count). */
+int rpgo_device_info(char* name, int32_t name_capacity, int32_t* sm_count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RPGO_GB300_H */

@@ -1,0 +1,406 @@
+// CPU FP64 oracle — TEST INFRASTRUCTURE ONLY (ctypes entry points).
+//
+// RobustSolver restatement: src/RobustSolver.cpp:29-103 (constructor),
+// 105-113 (known inliers), 115-306 (optimize), 337-369 (update);
+// src/GenericSolver.cpp:37-65 (updateValues, addAndCheckIfOptimize).
+// The structs of the public C ABI header are reused for the argument layout.
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <memory>
+#include <numeric>
+#include <set>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+
+#include "../include/rpgo_gb300.h"
+#include "oracle_solver.hpp"
+
+using namespace oracle;
+
+namespace {
+
+struct SolverBase {
+  virtual ~SolverBase() = default;
+  virtual int update(const rpgo_factor_batch* f, const rpgo_value_batch* v, int opt) = 0;
+  virtual void counts(rpgo_counts* c) const = 0;
+  virtual int estimate(uint64_t* keys, double* poses, int64_t cap) const = 0;
+  virtual int weights(double* w, int64_t cap) const = 0;
+  virtual int factors(int32_t* kind, uint64_t* k1, uint64_t* k2, double* meas, int64_t cap) const = 0;
+  virtual int adjacency(int32_t group, uint32_t* words, int64_t cap, int64_t* n) const = 0;
+  virtual void stats(int64_t* lm_iters, int64_t* solves, int64_t* gnc_iters) const = 0;
+};
+
+template <class S, class U>
+struct RobustSolverO final : SolverBase {
+  using L = typename S::L;
+  using Pose = typename S::Pose;
+  static constexpr int d = S::d;
+  rpgo_params p;
+  std::map<uint64_t, Pose> values;
+  std::vector<Factor<L>> nfg;
+  std::unique_ptr<Pcm<L, U>> pcm;
+  std::vector<double> gnc_weights;
+  size_t gnc_num_inliers = 0, latest_num_lc = 0;
+  int64_t lm_iters = 0, solves = 0, gnc_iters = 0;
+  bool last_do_opt = false;
+
+  explicit RobustSolverO(const rpgo_params& prm, bool with_pcm) : p(prm) {
+    if (with_pcm) {
+      PcmParamsO pp;
+      pp.odom_threshold = p.odom_threshold;
+      pp.lc_threshold = p.lc_threshold;
+      pp.odom_trans_threshold = p.odom_trans_threshold;
+      pp.odom_rot_threshold = p.odom_rot_threshold;
+      pp.dist_trans_threshold = p.dist_trans_threshold;
+      pp.dist_rot_threshold = p.dist_rot_threshold;
+      pp.incremental = p.incremental != 0;
+      pcm.reset(new Pcm<L, U>(pp));
+    }
+  }
+  std::vector<Factor<L>> convert(const rpgo_factor_batch* f) const {
+    std::vector<Factor<L>> out;
+    if (!f) return out;
+    for (int64_t k = 0; k < f->count; ++k) {
+      Factor<L> x;
+      x.kind = f->kind[k];
+      x.k1 = f->key_front[k];
+      x.k2 = (x.kind == 0) ? f->key_back[k] : f->key_front[k];
+      x.measured = L::load(f->measured + k * L::stride);
+      std::memcpy(x.cov, f->covariance + k * d * d, sizeof(double) * d * d);
+      std::memcpy(x.sqrt_info, f->sqrt_information + k * d * d, sizeof(double) * d * d);
+      out.push_back(x);
+    }
+    return out;
+  }
+  int update(const rpgo_factor_batch* fb, const rpgo_value_batch* vb, int optimize_graph) override {
+    try {
+      return update_impl(fb, vb, optimize_graph);
+    } catch (const std::out_of_range&) {
+      return RPGO_ERR_KEY;
+    }
+  }
+  int update_impl(const rpgo_factor_batch* fb, const rpgo_value_batch* vb, int optimize_graph) {
+    auto nf = convert(fb);
+    std::set<uint64_t> new_keys;
+    if (vb) {
+      for (int64_t k = 0; k < vb->count; ++k) {
+        if (values.count(vb->key[k]) || new_keys.count(vb->key[k])) return RPGO_ERR_KEY;
+        new_keys.insert(vb->key[k]);
+      }
+      for (int64_t k = 0; k < vb->count; ++k) values[vb->key[k]] = L::load(vb->pose + k * L::stride);
+    }
+    bool do_opt;
+    if (pcm) {
+      do_opt = pcm->remove_outliers(nf, new_keys, values, &nfg);
+    } else {
+      nfg.insert(nfg.end(), nf.begin(), nf.end());
+      do_opt = true;
+      if (nf.size() == 1 && nf[0].kind == 0 && new_keys.size() == 1) do_opt = false;
+      if (nf.empty() && new_keys.empty()) do_opt = false;
+    }
+    last_do_opt = do_opt;
+    for (const auto& f : nfg) {
+      if (!values.count(f.k1) || !values.count(f.k2)) return RPGO_ERR_KEY;
+    }
+    if (do_opt && optimize_graph) return optimize();
+    return RPGO_OK;
+  }
+  int optimize() {
+    LmParamsO lp;
+    lp.gauss_newton = (p.solver == RPGO_SOLVER_GN);
+    lp.diagonal_damping = p.lm_diagonal_damping != 0;
+    std::vector<Factor<L>> full = nfg;
+    std::map<uint64_t, Pose> result;
+    SolveStats st;
+    const size_t num_lc = pcm ? pcm->total_lc : 0;
+    if (p.use_gnc && pcm && !(p.gnc_fix_prev_inliers && num_lc == latest_num_lc)) {
+      GncParamsO gp;
+      gp.threshold_mode = p.gnc_threshold_mode;
+      gp.threshold = p.gnc_inlier_threshold;
+      gp.max_iterations = p.gnc_max_iterations;
+      gp.mu_step = p.gnc_mu_step;
+      gp.rel_cost_tol = p.gnc_relative_cost_tol;
+      gp.weights_tol = p.gnc_weights_tol;
+      const size_t n_known = pcm->nfg_odom.size() + pcm->nfg_special.size();
+      std::vector<double> init;
+      if (p.gnc_bias_odom) {
+        init.assign(full.size(), 0.0);
+        for (size_t i = 0; i < n_known; ++i) init[i] = 1.0;
+      }
+      auto r = gnc_tls<S>(full, values, n_known, gp, lp, p.gnc_bias_odom ? &init : nullptr);
+      result = r.values;
+      st = r.stats;
+      gnc_iters += r.outer_iterations;
+      gnc_weights.assign(r.weights.begin(), r.weights.begin() + nfg.size());
+      const double sum = std::accumulate(gnc_weights.begin(), gnc_weights.end(), 0.0);
+      gnc_num_inliers = static_cast<size_t>(sum) - n_known;
+    } else {
+      if (p.gnc_fix_prev_inliers && pcm) {
+        const size_t prev_k = gnc_weights.size() - std::min(latest_num_lc, gnc_weights.size());
+        const size_t k = pcm->nfg_odom.size() + pcm->nfg_special.size();
+        full.assign(nfg.begin(), nfg.begin() + std::min(k, nfg.size()));
+        for (size_t i = 0; i < latest_num_lc; ++i)
+          if (prev_k + i < gnc_weights.size() && gnc_weights[prev_k + i] > 0.5 && k + i < nfg.size())
+            full.push_back(nfg[k + i]);
+      }
+      NLS<S> nls;
+      nls.graph = &full;
+      result = nls.optimize(values, lp, &st);
+      if (st.failed) return RPGO_ERR_SOLVER;
+      const size_t tail = std::min(latest_num_lc, gnc_weights.size());
+      std::vector<double> lcw(gnc_weights.end() - tail, gnc_weights.end());
+      gnc_weights.assign(nfg.size(), 1.0);
+      const size_t t2 = std::min(tail, gnc_weights.size());
+      for (size_t i = 0; i < t2; ++i) gnc_weights[gnc_weights.size() - t2 + i] = lcw[lcw.size() - t2 + i];
+    }
+    lm_iters += st.iterations;
+    solves += st.linear_solves;
+    for (auto& kv : result)
+      if (values.count(kv.first)) values[kv.first] = kv.second;
+    if (pcm) latest_num_lc = pcm->total_lc;
+    return RPGO_OK;
+  }
+  void counts(rpgo_counts* c) const override {
+    c->num_factors = (int64_t)nfg.size();
+    c->num_values = (int64_t)values.size();
+    c->num_lc = pcm ? (int64_t)pcm->total_lc : 0;
+    c->num_lc_inliers = p.use_gnc ? (int64_t)gnc_num_inliers : (pcm ? (int64_t)pcm->total_good_lc : 0);
+    c->num_odom = pcm ? (int64_t)pcm->nfg_odom.size() : 0;
+    c->num_special = pcm ? (int64_t)pcm->nfg_special.size() : 0;
+    c->num_gnc_weights = (int64_t)gnc_weights.size();
+    c->last_do_optimize = last_do_opt ? 1 : 0;
+  }
+  int estimate(uint64_t* keys, double* poses, int64_t cap) const override {
+    if ((int64_t)values.size() > cap) return RPGO_ERR_ARG;
+    int64_t i = 0;
+    for (auto& kv : values) {
+      keys[i] = kv.first;
+      L::store(kv.second, poses + i * L::stride);
+      ++i;
+    }
+    return RPGO_OK;
+  }
+  int weights(double* w, int64_t cap) const override {
+    if ((int64_t)gnc_weights.size() > cap) return RPGO_ERR_ARG;
+    for (size_t i = 0; i < gnc_weights.size(); ++i) w[i] = gnc_weights[i];
+    return RPGO_OK;
+  }
+  int factors(int32_t* kind, uint64_t* k1, uint64_t* k2, double* meas, int64_t cap) const override {
+    if ((int64_t)nfg.size() > cap) return RPGO_ERR_ARG;
+    for (size_t i = 0; i < nfg.size(); ++i) {
+      kind[i] = nfg[i].kind;
+      k1[i] = nfg[i].k1;
+      k2[i] = nfg[i].k2;
+      if (meas) L::store(nfg[i].measured, meas + i * L::stride);
+    }
+    return RPGO_OK;
+  }
+  int adjacency(int32_t group, uint32_t* words, int64_t cap, int64_t* n) const override {
+    if (!pcm) return RPGO_ERR_UNSUPPORTED;
+    int32_t gi = 0;
+    for (auto& kv : pcm->loop_closures) {
+      if (gi++ != group) continue;
+      const auto& g = kv.second;
+      *n = g.n;
+      if (!words) return RPGO_OK;
+      if ((int64_t)g.bits.size() > cap) return RPGO_ERR_ARG;
+      for (size_t i = 0; i < g.bits.size(); ++i) words[i] = g.bits[i];
+      return RPGO_OK;
+    }
+    return RPGO_ERR_ARG;
+  }
+  void stats(int64_t* a, int64_t* b, int64_t* c) const override {
+    *a = lm_iters;
+    *b = solves;
+    *c = gnc_iters;
+  }
+};
+
+template <class L>
+void load_pwc(const double* pose, const double* cov, int rot_info, PWC<L>* x) {
+  x->pose = L::load(pose);
+  std::memcpy(x->cov, cov, sizeof(double) * L::dim * L::dim);
+  x->rot_info = rot_info != 0;
+}
+template <class L>
+void store_pwc(const PWC<L>& x, double* pose, double* cov, int* rot_info) {
+  L::store(x.pose, pose);
+  std::memcpy(cov, x.cov, sizeof(double) * L::dim * L::dim);
+  if (rot_info) *rot_info = x.rot_info ? 1 : 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+void* oracle_create(const rpgo_params* p) {
+  const int m = p->outlier_removal;
+  const int dim = (m == RPGO_OUTLIER_PCM2D || m == RPGO_OUTLIER_PCM_SIMPLE2D) ? 2
+                  : (m == RPGO_OUTLIER_NONE) ? p->dim : 3;
+  SolverBase* s = nullptr;
+  switch (m) {
+    case RPGO_OUTLIER_NONE:
+      if (dim == 2) s = new RobustSolverO<Sol2, PWC<Lie2>>(*p, false);
+      else if (dim == 3) s = new RobustSolverO<Sol3, PWC<Lie3>>(*p, false);
+      break;
+    case RPGO_OUTLIER_PCM2D: s = new RobustSolverO<Sol2, PWC<Lie2>>(*p, true); break;
+    case RPGO_OUTLIER_PCM3D: s = new RobustSolverO<Sol3, PWC<Lie3>>(*p, true); break;
+    case RPGO_OUTLIER_PCM_SIMPLE2D: s = new RobustSolverO<Sol2, PWN<Lie2>>(*p, true); break;
+    case RPGO_OUTLIER_PCM_SIMPLE3D: s = new RobustSolverO<Sol3, PWN<Lie3>>(*p, true); break;
+    default: break;
+  }
+  return s;
+}
+void oracle_destroy(void* s) { delete static_cast<SolverBase*>(s); }
+int oracle_update(void* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, int32_t opt) {
+  return static_cast<SolverBase*>(s)->update(f, v, opt);
+}
+int oracle_get_counts(void* s, rpgo_counts* c) {
+  static_cast<SolverBase*>(s)->counts(c);
+  return 0;
+}
+int oracle_get_estimate(void* s, uint64_t* k, double* p, int64_t cap) {
+  return static_cast<SolverBase*>(s)->estimate(k, p, cap);
+}
+int oracle_get_gnc_weights(void* s, double* w, int64_t cap) { return static_cast<SolverBase*>(s)->weights(w, cap); }
+int oracle_get_factors(void* s, int32_t* kind, uint64_t* k1, uint64_t* k2, double* meas, int64_t cap) {
+  return static_cast<SolverBase*>(s)->factors(kind, k1, k2, meas, cap);
+}
+int oracle_get_adjacency(void* s, int32_t g, uint32_t* w, int64_t cap, int64_t* n) {
+  return static_cast<SolverBase*>(s)->adjacency(g, w, cap, n);
+}
+int oracle_get_stats(void* s, int64_t* lm, int64_t* solves, int64_t* gnc) {
+  static_cast<SolverBase*>(s)->stats(lm, solves, gnc);
+  return 0;
+}
+
+// ---- geometry known-answer hooks (GeometryUtils.h)
+// op: 0 compose, 1 between, 2 inverse (b ignored)
+int oracle_pwc_op(int dim, int op, const double* pa, const double* ca, int ria, const double* pb, const double* cb,
+                  int rib, double* pout, double* cout, int* riout) {
+  if (dim == 3) {
+    PWC<Lie3> a, b, r;
+    load_pwc(pa, ca, ria, &a);
+    if (op != 2) load_pwc(pb, cb, rib, &b);
+    r = op == 0 ? a.compose(b) : op == 1 ? a.between(b) : a.inverse();
+    store_pwc(r, pout, cout, riout);
+  } else {
+    PWC<Lie2> a, b, r;
+    load_pwc(pa, ca, ria, &a);
+    if (op != 2) load_pwc(pb, cb, rib, &b);
+    r = op == 0 ? a.compose(b) : op == 1 ? a.between(b) : a.inverse();
+    store_pwc(r, pout, cout, riout);
+  }
+  return 0;
+}
+double oracle_pwc_mahalanobis(int dim, const double* pose, const double* cov, int rot_info) {
+  if (dim == 3) {
+    PWC<Lie3> a;
+    load_pwc(pose, cov, rot_info, &a);
+    return a.mahalanobis_norm();
+  }
+  PWC<Lie2> a;
+  load_pwc(pose, cov, rot_info, &a);
+  return a.mahalanobis_norm();
+}
+// PoseWithNode norms: out[0] = avg_trans_norm, out[1] = avg_rot_norm
+int oracle_pwn_norms(int dim, const double* pose, int node, int rot_info, double* out) {
+  if (dim == 3) {
+    PWN<Lie3> a;
+    a.pose = Lie3::load(pose);
+    a.node = node;
+    a.rot_info = rot_info != 0;
+    out[0] = a.avg_trans_norm();
+    out[1] = a.avg_rot_norm();
+  } else {
+    PWN<Lie2> a;
+    a.pose = Lie2::load(pose);
+    a.node = node;
+    a.rot_info = rot_info != 0;
+    out[0] = a.avg_trans_norm();
+    out[1] = a.avg_rot_norm();
+  }
+  return 0;
+}
+int oracle_logmap(int dim, const double* pose, double* xi) {
+  if (dim == 3) p3_logmap(Lie3::load(pose), xi);
+  else p2_logmap(Lie2::load(pose), xi);
+  return 0;
+}
+double oracle_atan2(double y, double x) { return r_atan2(y, x); }
+double oracle_chi2inv(double alpha, int k) { return chi2inv(alpha, k); }
+
+// Pairwise adjacency of n closures against a trajectory given by slots
+// (the stage restated without the solver state). mode 0 PoseWithCovariance,
+// 1 PoseWithNode. adj: n x ceil(n/32) words (cleared here).
+int oracle_pairwise_adjacency(int dim, int mode, int n, const int32_t* slot_a, const int32_t* slot_b,
+                              const uint8_t* flip, const double* z_pose, const double* z_cov,
+                              const double* traj_pose, const double* traj_cov, const int32_t* traj_node,
+                              const uint8_t* traj_rot, double th0, double th1, uint32_t* adj) {
+  const int words = (n + 31) / 32;
+  std::memset(adj, 0, sizeof(uint32_t) * (size_t)n * words);
+  auto body = [&](auto lie, auto kind) {
+    using L = decltype(lie);
+    constexpr bool simple = decltype(kind)::value;
+    constexpr int dd = L::dim;
+    auto traj = [&](int s) {
+      if constexpr (simple) {
+        PWN<L> x;
+        x.pose = L::load(traj_pose + (size_t)s * L::stride);
+        x.node = traj_node[s];
+        x.rot_info = traj_rot[s] != 0;
+        return x;
+      } else {
+        PWC<L> x;
+        x.pose = L::load(traj_pose + (size_t)s * L::stride);
+        std::memcpy(x.cov, traj_cov + (size_t)s * dd * dd, sizeof(double) * dd * dd);
+        x.rot_info = traj_rot[s] != 0;
+        return x;
+      }
+    };
+    using U = decltype(traj(0));
+    for (int j = 1; j < n; ++j)
+      for (int i = 0; i < j; ++i) {
+        U zab = U::from_factor(L::load(z_pose + (size_t)i * L::stride), z_cov + (size_t)i * dd * dd);
+        U zcd = U::from_factor(L::load(z_pose + (size_t)j * L::stride), z_cov + (size_t)j * dd * dd);
+        int sa = slot_a[i], sb = slot_b[i], sc = slot_a[j], sd = slot_b[j];
+        if (flip[i] != flip[j]) std::swap(sc, sd);
+        U a_odom_c = traj(sa).between(traj(sc));
+        U b_odom_d = traj(sb).between(traj(sd));
+        U loop = a_odom_c.compose(zcd).inverse().compose(zab).compose(b_odom_d);
+        bool ok;
+        if constexpr (simple) ok = loop.avg_trans_norm() < th0 && loop.avg_rot_norm() < th1;
+        else ok = loop.mahalanobis_norm() < th0;
+        if (ok) {
+          adj[(size_t)i * words + (j >> 5)] |= 1u << (j & 31);
+          adj[(size_t)j * words + (i >> 5)] |= 1u << (i & 31);
+        }
+      }
+  };
+  if (dim == 3) {
+    if (mode == 0) body(Lie3{}, std::false_type{});
+    else body(Lie3{}, std::true_type{});
+  } else {
+    if (mode == 0) body(Lie2{}, std::false_type{});
+    else body(Lie2{}, std::true_type{});
+  }
+  return 0;
+}
+
+// Greedy max clique on a bit-packed adjacency (n x ceil(n/32) words).
+int oracle_max_clique_heu(int n, const uint32_t* adj, int first, int seed, int32_t* clique_out, int32_t* size_out) {
+  const int words = (n + 31) / 32;
+  std::vector<uint32_t> bits(adj, adj + (size_t)n * words);
+  Csr g = csr_from_bits(bits, n, words);
+  std::vector<int> best;
+  int sz = fmc_heuristic(g, first, seed, &best);
+  *size_out = sz;
+  for (int i = 0; i < sz && i < (int)best.size(); ++i) clique_out[i] = best[i];
+  return 0;
+}
+
+}  // extern "C"

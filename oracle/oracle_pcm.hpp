@@ -1,0 +1,519 @@
+// CPU FP64 oracle — TEST INFRASTRUCTURE ONLY.
+//
+// Restatement of Kimera-RPGO's PCM outlier rejection:
+//   include/KimeraRPGO/outlier/Pcm.h:148-281   removeOutliers (classification)
+//   include/KimeraRPGO/outlier/Pcm.h:414-502   parseAndIncrementAdjMatrix
+//   include/KimeraRPGO/outlier/Pcm.h:516-557   updateOdom
+//   include/KimeraRPGO/outlier/Pcm.h:564-629   odometry consistency check
+//   include/KimeraRPGO/outlier/Pcm.h:638-718   pairwise loop consistency check
+//   include/KimeraRPGO/outlier/Pcm.h:725-768   incrementAdjMatrix
+//   include/KimeraRPGO/outlier/Pcm.h:851-1005  findInliers[Incremental], buildGraphToOptimize
+//   include/KimeraRPGO/utils/GraphUtils.h:37-58 Trajectory::getBetween
+//   include/KimeraRPGO/max_clique_finder/graphIO.cpp:188-257 dense -> CSR
+//   include/KimeraRPGO/max_clique_finder/findCliqueHeu.cpp:32-209 greedy clique
+//   src/utils/GraphUtils.cpp:19-44 findMaxCliqueHeu[Incremental]
+// Landmarks (special symbols), multi-robot frame alignment and the edit API
+// (remove / ignore / revive) are outside the restated path.
+#pragma once
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <map>
+#include <unordered_map>
+#include <vector>
+
+#include "oracle_math.hpp"
+
+namespace oracle {
+
+// ---------------------------------------------------------------- Lie traits
+struct Lie3 {
+  using Pose = P3;
+  static constexpr int dim = 6, rdim = 3, tdim = 3, stride = 12;
+  static Pose identity() { return p3_identity(); }
+  static Pose compose(const Pose& a, const Pose& b) { return p3_compose(a, b); }
+  static Pose inverse(const Pose& a) { return p3_inverse(a); }
+  static Pose between(const Pose& a, const Pose& b) { return p3_between(a, b); }
+  static void congruence(const Pose& T, const double* S, double* C) { p3_congruence(T, S, C); }
+  static void logmap(const Pose& T, double* xi) { p3_logmap(T, xi); }
+  static double rot_trace(const double* cov) { return (cov[0] + cov[7]) + cov[14]; }
+  static Pose load(const double* p) {
+    Pose q;
+    for (int i = 0; i < 9; ++i) q.R[i] = p[i];
+    for (int i = 0; i < 3; ++i) q.t[i] = p[9 + i];
+    return q;
+  }
+  static void store(const Pose& q, double* p) {
+    for (int i = 0; i < 9; ++i) p[i] = q.R[i];
+    for (int i = 0; i < 3; ++i) p[9 + i] = q.t[i];
+  }
+};
+struct Lie2 {
+  using Pose = P2;
+  static constexpr int dim = 3, rdim = 1, tdim = 2, stride = 4;
+  static Pose identity() { return p2_identity(); }
+  static Pose compose(const Pose& a, const Pose& b) { return p2_compose(a, b); }
+  static Pose inverse(const Pose& a) { return p2_inverse(a); }
+  static Pose between(const Pose& a, const Pose& b) { return p2_between(a, b); }
+  static void congruence(const Pose& T, const double* S, double* C) { p2_congruence(T, S, C); }
+  static void logmap(const Pose& T, double* xi) { p2_logmap(T, xi); }
+  static double rot_trace(const double* cov) { return cov[0]; }
+  static Pose load(const double* p) { return P2{p[0], p[1], p[2], p[3]}; }
+  static void store(const Pose& q, double* p) {
+    p[0] = q.c; p[1] = q.s; p[2] = q.x; p[3] = q.y;
+  }
+};
+
+// ---------------------------------------------------------------- PoseWithCovariance
+template <class L>
+struct PWC {
+  typename L::Pose pose = L::identity();
+  double cov[L::dim * L::dim] = {0};
+  bool rot_info = true;
+
+  // GeometryUtils.h:91-115
+  static PWC from_factor(const typename L::Pose& measured, const double* covariance) {
+    PWC out;
+    out.pose = measured;
+    constexpr int n = L::dim;
+    for (int i = 0; i < n * n; ++i) out.cov[i] = covariance[i];
+    out.rot_info = true;
+    if (std::isnan(L::rot_trace(covariance))) {
+      out.rot_info = false;
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+          out.cov[n * i + j] = (i >= L::rdim && j >= L::rdim) ? covariance[n * i + j] : 0.0;
+    }
+    return out;
+  }
+  // GeometryUtils.h:119-129
+  PWC compose(const PWC& other) const {
+    PWC out;
+    constexpr int n = L::dim;
+    out.pose = L::compose(pose, other.pose);
+    double C[n * n];
+    L::congruence(L::inverse(other.pose), cov, C);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j <= i; ++j) {
+        const double v = C[n * i + j] + other.cov[n * i + j];
+        out.cov[n * i + j] = v;
+        out.cov[n * j + i] = v;
+      }
+    out.rot_info = rot_info && other.rot_info;
+    return out;
+  }
+  // GeometryUtils.h:133-139 (the covariance is deliberately not transformed)
+  PWC inverse() const {
+    PWC out;
+    out.pose = L::inverse(pose);
+    for (int i = 0; i < L::dim * L::dim; ++i) out.cov[i] = cov[i];
+    out.rot_info = rot_info;
+    return out;
+  }
+  // GeometryUtils.h:143-170
+  PWC between(const PWC& other) const {
+    PWC out;
+    constexpr int n = L::dim;
+    const typename L::Pose res = L::between(pose, other.pose);
+    out.pose = res;
+    double C[n * n], Lf[n * n];
+    L::congruence(L::inverse(res), cov, C);
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j <= i; ++j) {
+        const double v = other.cov[n * i + j] - C[n * i + j];
+        out.cov[n * i + j] = v;
+        out.cov[n * j + i] = v;
+      }
+    if (!chol_lower(out.cov, n, Lf)) {
+      const typename L::Pose res2 = L::between(other.pose, pose);
+      L::congruence(L::inverse(res2), other.cov, C);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j <= i; ++j) {
+          const double v = cov[n * i + j] - C[n * i + j];
+          out.cov[n * i + j] = v;
+          out.cov[n * j + i] = v;
+        }
+    }
+    out.rot_info = rot_info && other.rot_info;
+    return out;
+  }
+  // GeometryUtils.h:172-186
+  double mahalanobis_norm() const {
+    constexpr int n = L::dim;
+    double xi[n];
+    L::logmap(pose, xi);
+    if (!rot_info) {
+      constexpr int m = L::tdim, r = L::rdim;
+      double B[m * m];
+      for (int i = 0; i < m; ++i)
+        for (int j = 0; j < m; ++j) B[m * i + j] = cov[n * (r + i) + (r + j)];
+      return std::sqrt(quad_inv(B, m, xi + r));
+    }
+    return std::sqrt(quad_inv(cov, n, xi));
+  }
+};
+
+// ---------------------------------------------------------------- PoseWithNode
+template <class L>
+struct PWN {
+  typename L::Pose pose = L::identity();
+  int node = 0;
+  bool rot_info = true;
+
+  // GeometryUtils.h:221-234
+  static PWN from_factor(const typename L::Pose& measured, const double* covariance) {
+    PWN out;
+    out.pose = measured;
+    out.rot_info = !std::isnan(L::rot_trace(covariance));
+    out.node = 1;
+    return out;
+  }
+  PWN compose(const PWN& other) const {
+    PWN out;
+    out.pose = L::compose(pose, other.pose);
+    out.node = node + other.node;
+    out.rot_info = rot_info && other.rot_info;
+    return out;
+  }
+  PWN inverse() const {
+    PWN out;
+    out.pose = L::inverse(pose);
+    out.node = node;
+    out.rot_info = rot_info;
+    return out;
+  }
+  PWN between(const PWN& other) const {
+    PWN out;
+    out.pose = L::between(pose, other.pose);
+    out.node = std::abs(other.node - node);
+    out.rot_info = rot_info && other.rot_info;
+    return out;
+  }
+  static double norm_slice(const double* v, int m) {
+    double acc = v[0] * v[0];
+    for (int i = 1; i < m; ++i) acc = fmad(v[i], v[i], acc);
+    return std::sqrt(acc);
+  }
+  // GeometryUtils.h:274-288 (Pose2: tail(2) is (v_y, omega), head(1) is v_x)
+  double avg_trans_norm() const {
+    double xi[L::dim];
+    L::logmap(pose, xi);
+    return norm_slice(xi + L::rdim, L::tdim) / static_cast<double>(node);
+  }
+  double avg_rot_norm() const {
+    if (!rot_info) return 0.0;
+    double xi[L::dim];
+    L::logmap(pose, xi);
+    return norm_slice(xi, L::rdim) / static_cast<double>(node);
+  }
+};
+
+static inline char key_chr(uint64_t k) { return static_cast<char>(static_cast<unsigned char>(k >> 56)); }
+static inline uint64_t symbol(char c, uint64_t idx) {
+  return (static_cast<uint64_t>(static_cast<unsigned char>(c)) << 56) | idx;
+}
+
+// ---------------------------------------------------------------- Trajectory
+template <class U>
+struct Trajectory {
+  std::map<uint64_t, U> poses;
+  // GraphUtils.h:37-58 (std::map::operator[] inserts a default entry)
+  U getBetween(uint64_t ka, uint64_t kb) {
+    if (key_chr(ka) == key_chr(kb)) return poses[ka].between(poses[kb]);
+    const uint64_t a0 = symbol(key_chr(ka), 0), b0 = symbol(key_chr(kb), 0);
+    U pa = poses[a0].between(poses[ka]);
+    U pb = poses[b0].between(poses[kb]);
+    U pab = poses[a0].between(poses[b0]);
+    U r = pa.inverse().compose(pab);
+    return r.compose(pb);
+  }
+};
+
+// ---------------------------------------------------------------- max clique (FMC heuristic)
+// CSR exactly as CGraphIO::ReadEigenAdjacencyMatrix builds it: neighbour
+// lists in ascending order, diagonal ignored.
+struct Csr {
+  std::vector<int> off, adj;
+  int max_deg = -1;
+};
+static inline Csr csr_from_bits(const std::vector<uint32_t>& bits, int n, int words) {
+  Csr g;
+  g.off.assign(n + 1, 0);
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < n; ++j)
+      if (j != i && ((bits[(size_t)i * words + (j >> 5)] >> (j & 31)) & 1u)) g.adj.push_back(j);
+    g.off[i + 1] = (int)g.adj.size();
+  }
+  for (int i = 0; i < n; ++i) g.max_deg = std::max(g.max_deg, g.off[i + 1] - g.off[i]);
+  return g;
+}
+
+// findCliqueHeu.cpp:32-117 and 119-209: candidates first..n-1, running best
+// seeded with max_clq; the winning work buffer is returned whole, so its
+// first max_clq slots may hold stale (non-clique) vertices.
+static inline int fmc_heuristic(const Csr& g, int first, int max_clq, std::vector<int>* best) {
+  const int n = (int)g.off.size() - 1;
+  auto deg = [&](int v) { return g.off[v + 1] - g.off[v]; };
+  std::vector<int> S(std::max(g.max_deg, 0) + 1, 0), S1(std::max(g.max_deg, 0) + 1, 0);
+  for (int v = first; v < n; ++v) {
+    if (max_clq > deg(v)) continue;
+    int npos = 0;
+    S[npos++] = v;
+    for (int e = g.off[v]; e < g.off[v + 1]; ++e)
+      if (max_clq <= deg(g.adj[e])) S[npos++] = g.adj[e];
+    int icc = 0;
+    while (npos > 0) {
+      ++icc;
+      const int m = S[npos - 1];
+      int n1 = 0;
+      for (int a = 0; a < npos; ++a) {
+        for (int e = g.off[m]; e < g.off[m + 1]; ++e) {
+          if (S[a] == g.adj[e] && max_clq <= deg(g.adj[e])) {
+            S1[n1++] = S[a];
+            break;
+          }
+        }
+      }
+      for (int a = 0; a < n1; ++a) S[a] = S1[a];
+      npos = n1;
+    }
+    if (max_clq < icc) {
+      *best = S;
+      max_clq = icc;
+    }
+  }
+  return max_clq;
+}
+
+// ---------------------------------------------------------------- factor records
+template <class L>
+struct Factor {
+  int kind = 0;  // 0 between, 1 prior
+  uint64_t k1 = 0, k2 = 0;
+  typename L::Pose measured = L::identity();
+  double cov[L::dim * L::dim] = {0};
+  double sqrt_info[L::dim * L::dim] = {0};
+};
+
+// ObservationId (TypeUtils.h:44-58) with the same symmetric equality and
+// hash (TypeUtils.h:80-88), so std::unordered_map iterates in the same
+// order as the reference's.
+struct ObsId {
+  char id1, id2;
+  bool operator==(const ObsId& o) const {
+    return (id1 == o.id1 && id2 == o.id2) || (id2 == o.id1 && id1 == o.id2);
+  }
+};
+struct ObsIdHash {
+  size_t operator()(const ObsId& id) const {
+    std::hash<char> h;
+    return h(id.id1) + h(id.id2) + h(id.id1) * h(id.id2);
+  }
+};
+
+template <class L>
+struct Group {
+  std::vector<Factor<L>> factors;
+  std::vector<Factor<L>> consistent;
+  int n = 0, words = 0;
+  std::vector<uint32_t> bits;  // n x words, symmetric
+  void grow(int new_n) {
+    const int nw = (new_n + 31) / 32;
+    std::vector<uint32_t> nb((size_t)new_n * nw, 0u);
+    for (int i = 0; i < n; ++i)
+      for (int w = 0; w < words; ++w) nb[(size_t)i * nw + w] = bits[(size_t)i * words + w];
+    bits.swap(nb);
+    n = new_n;
+    words = nw;
+  }
+  void set(int i, int j) {
+    bits[(size_t)i * words + (j >> 5)] |= 1u << (j & 31);
+    bits[(size_t)j * words + (i >> 5)] |= 1u << (i & 31);
+  }
+};
+
+struct PcmParamsO {
+  double odom_threshold = 10.0, lc_threshold = 5.0;
+  double odom_trans_threshold = 0.05, odom_rot_threshold = 0.005;
+  double dist_trans_threshold = 0.01, dist_rot_threshold = 0.001;
+  bool incremental = false;
+};
+
+// U = PWC<L> (Pcm2D/Pcm3D) or PWN<L> (PcmSimple2D/PcmSimple3D)
+template <class L, class U>
+struct Pcm {
+  static constexpr bool kSimple = !std::is_same<U, PWC<L>>::value;
+  PcmParamsO params;
+  bool odom_check = true, lc_check = true;
+  std::vector<Factor<L>> nfg_odom, nfg_special;
+  std::unordered_map<ObsId, Group<L>, ObsIdHash> loop_closures;
+  std::unordered_map<char, Trajectory<U>> trajectories;
+  size_t total_lc = 0, total_good_lc = 0;
+  bool warned_missing = false;
+
+  explicit Pcm(const PcmParamsO& p) : params(p) {
+    if (p.odom_threshold < 0 || p.odom_rot_threshold < 0 || p.odom_trans_threshold < 0) odom_check = false;
+    if (p.lc_threshold < 0 || p.dist_rot_threshold < 0 || p.dist_trans_threshold < 0) lc_check = false;
+  }
+
+  bool check_odom(const U& r) const {
+    if constexpr (kSimple) {
+      return r.avg_trans_norm() < params.odom_trans_threshold && r.avg_rot_norm() < params.odom_rot_threshold;
+    } else {
+      return r.mahalanobis_norm() < params.odom_threshold;
+    }
+  }
+  bool check_loop(const U& r) const {
+    if constexpr (kSimple) {
+      return r.avg_trans_norm() < params.dist_trans_threshold && r.avg_rot_norm() < params.dist_rot_threshold;
+    } else {
+      return r.mahalanobis_norm() < params.lc_threshold;
+    }
+  }
+  // Pcm.h:604-629
+  bool is_odom_consistent(const Factor<L>& f) {
+    if (!odom_check) return true;
+    U pij = trajectories[key_chr(f.k1)].getBetween(f.k1, f.k2);
+    U pji = U::from_factor(f.measured, f.cov).inverse();
+    return check_odom(pij.compose(pji));
+  }
+  // Pcm.h:670-718
+  bool are_loops_consistent(const Factor<L>& ab, const Factor<L>& cd) {
+    if (!lc_check) return true;
+    uint64_t ka = ab.k1, kb = ab.k2, kc = cd.k1, kd = cd.k2;
+    U a_lc_b = U::from_factor(ab.measured, ab.cov);
+    U c_lc_d = U::from_factor(cd.measured, cd.cov);
+    if (key_chr(ka) != key_chr(kc)) std::swap(kc, kd);
+    U a_odom_c = trajectories[key_chr(ka)].getBetween(ka, kc);
+    U b_odom_d = trajectories[key_chr(kb)].getBetween(kb, kd);
+    U a_path_d = a_odom_c.compose(c_lc_d);
+    U d_path_b = a_path_d.inverse().compose(a_lc_b);
+    U loop = d_path_b.compose(b_odom_d);
+    return check_loop(loop);
+  }
+  // Pcm.h:516-557
+  template <class ValuesMap>
+  void update_odom(const Factor<L>& f, const ValuesMap& values) {
+    nfg_odom.push_back(f);
+    const char prefix = key_chr(f.k2);
+    U delta = U::from_factor(f.measured, f.cov);
+    if (trajectories.find(prefix) == trajectories.end()) {
+      U init;
+      init.pose = values.at(f.k1);
+      trajectories[prefix].poses[f.k1] = init;
+    }
+    U prev = trajectories[prefix].poses[f.k1];
+    trajectories[prefix].poses[f.k2] = prev.compose(delta);
+  }
+  // Pcm.h:725-768 for every new member of the group against all earlier ones
+  void increment_adjacency(Group<L>& g, int old_n) {
+    g.grow((int)g.factors.size());
+    for (int j = old_n; j < g.n; ++j)
+      for (int i = 0; i < j; ++i)
+        if (are_loops_consistent(g.factors[i], g.factors[j])) g.set(i, j);
+  }
+
+  template <class ValuesMap>
+  void parse_and_increment(const std::vector<Factor<L>>& lcs, const ValuesMap& values,
+                           std::unordered_map<ObsId, size_t, ObsIdHash>* num_new) {
+    // the reference grows each group one closure at a time; doing all checks
+    // of a batch after the appends gives the same matrix because the pair
+    // test depends only on the two closures and the (fixed) trajectories.
+    std::unordered_map<ObsId, int, ObsIdHash> old_sizes;
+    std::vector<ObsId> touched;
+    for (const auto& f : lcs) {
+      if (!values.count(f.k1) || !values.count(f.k2)) continue;
+      const char c1 = key_chr(f.k1), c2 = key_chr(f.k2);
+      bool ok = true;
+      if (c1 == c2) ok = is_odom_consistent(f);
+      if (!ok) continue;
+      ObsId id{c1, c2};
+      auto it = num_new->find(id);
+      if (it == num_new->end()) num_new->insert({id, 1});
+      else it->second++;
+      Group<L>& g = loop_closures[id];
+      if (!old_sizes.count(id)) {
+        old_sizes[id] = (int)g.factors.size();
+        touched.push_back(id);
+      }
+      g.factors.push_back(f);
+      ++total_lc;
+    }
+    if (lc_check)
+      for (const auto& id : touched) increment_adjacency(loop_closures[id], old_sizes[id]);
+  }
+
+  void find_inliers() {
+    total_good_lc = 0;
+    for (auto& kv : loop_closures) {
+      Group<L>& g = kv.second;
+      size_t num;
+      if (lc_check) {
+        g.consistent.clear();
+        Csr csr = csr_from_bits(g.bits, g.n, g.words);
+        std::vector<int> idx;
+        num = (size_t)fmc_heuristic(csr, 0, -1, &idx);
+        for (size_t i = 0; i < num; ++i) g.consistent.push_back(g.factors[idx[i]]);
+      } else {
+        g.consistent = g.factors;
+        num = g.factors.size();
+      }
+      total_good_lc += num;
+    }
+  }
+  void find_inliers_incremental(const std::unordered_map<ObsId, size_t, ObsIdHash>& num_new) {
+    total_good_lc = 0;
+    for (const auto& kv : num_new) {
+      Group<L>& g = loop_closures[kv.first];
+      const size_t prev = g.consistent.size();
+      Csr csr = csr_from_bits(g.bits, g.n, g.words);
+      std::vector<int> idx;
+      const int first = (int)csr.off.size() - (int)kv.second - 1;
+      int num = fmc_heuristic(csr, first, (int)prev, &idx);
+      if ((size_t)num > prev) {
+        g.consistent.clear();
+        for (int i = 0; i < num; ++i) g.consistent.push_back(g.factors[idx[i]]);
+      }
+    }
+    for (const auto& kv : loop_closures) total_good_lc += kv.second.consistent.size();
+  }
+  std::vector<Factor<L>> build_graph() const {
+    std::vector<Factor<L>> out(nfg_odom);
+    out.insert(out.end(), nfg_special.begin(), nfg_special.end());
+    for (const auto& kv : loop_closures) out.insert(out.end(), kv.second.consistent.begin(), kv.second.consistent.end());
+    return out;
+  }
+
+  // Pcm.h:148-281. values: the solver's value map, already extended by the
+  // caller with new_values. Returns do_optimize.
+  template <class ValuesMap, class KeySet>
+  bool remove_outliers(const std::vector<Factor<L>>& new_factors, const KeySet& new_keys, const ValuesMap& values,
+                       std::vector<Factor<L>>* out_graph) {
+    if (new_factors.empty()) return false;
+    bool do_optimize = false;
+    std::vector<Factor<L>> lcs;
+    for (const auto& f : new_factors) {
+      if (f.kind == 0) {
+        if (f.k1 + 1 == f.k2 && new_keys.count(f.k2)) {
+          update_odom(f, values);
+        } else if (f.k1 != f.k2) {
+          lcs.push_back(f);
+        }
+      } else {
+        nfg_special.push_back(f);
+        do_optimize = true;
+      }
+    }
+    if (!lcs.empty()) {
+      std::unordered_map<ObsId, size_t, ObsIdHash> num_new;
+      parse_and_increment(lcs, values, &num_new);
+      if (params.incremental) find_inliers_incremental(num_new);
+      else find_inliers();
+      do_optimize = true;
+    }
+    *out_graph = build_graph();
+    return do_optimize;
+  }
+};
+
+}  // namespace oracle

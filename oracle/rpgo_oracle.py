@@ -1,0 +1,235 @@
+"""ctypes front-end of the CPU FP64 oracle — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, the smoke check and bench.py's CPU-baseline leg load this
+module; the product path never does. The shared library is built from
+oracle/*.cpp by oracle/Makefile into oracle/_build/liboracle.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("solver", C.c_int32), ("outlier_removal", C.c_int32), ("verbosity", C.c_int32), ("dim", C.c_int32),
+        ("odom_threshold", C.c_double), ("lc_threshold", C.c_double),
+        ("odom_trans_threshold", C.c_double), ("odom_rot_threshold", C.c_double),
+        ("dist_trans_threshold", C.c_double), ("dist_rot_threshold", C.c_double),
+        ("incremental", C.c_int32),
+        ("use_gnc", C.c_int32), ("gnc_threshold_mode", C.c_int32), ("gnc_inlier_threshold", C.c_double),
+        ("gnc_max_iterations", C.c_int32), ("gnc_mu_step", C.c_double), ("gnc_relative_cost_tol", C.c_double),
+        ("gnc_weights_tol", C.c_double), ("gnc_fix_prev_inliers", C.c_int32), ("gnc_bias_odom", C.c_int32),
+        ("lm_diagonal_damping", C.c_int32),
+    ]
+
+
+class FactorBatch(C.Structure):
+    _fields_ = [("count", C.c_int64), ("kind", C.c_void_p), ("key_front", C.c_void_p), ("key_back", C.c_void_p),
+                ("measured", C.c_void_p), ("covariance", C.c_void_p), ("sqrt_information", C.c_void_p)]
+
+
+class ValueBatch(C.Structure):
+    _fields_ = [("count", C.c_int64), ("key", C.c_void_p), ("pose", C.c_void_p)]
+
+
+class Counts(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("num_factors", "num_values", "num_lc", "num_lc_inliers", "num_odom",
+                                          "num_special", "num_gnc_weights", "last_do_optimize")]
+
+
+def build(force: bool = False) -> str:
+    if force or not os.path.exists(_LIB_PATH):
+        subprocess.check_call(["make", "-s", "-C", _HERE])
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        _lib = C.CDLL(_LIB_PATH)
+        _lib.oracle_create.restype = C.c_void_p
+        _lib.oracle_create.argtypes = [C.POINTER(Params)]
+        _lib.oracle_destroy.argtypes = [C.c_void_p]
+        _lib.oracle_update.argtypes = [C.c_void_p, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.c_int32]
+        _lib.oracle_get_counts.argtypes = [C.c_void_p, C.POINTER(Counts)]
+        _lib.oracle_get_estimate.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        _lib.oracle_get_gnc_weights.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+        _lib.oracle_get_factors.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        _lib.oracle_get_adjacency.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64,
+                                              C.POINTER(C.c_int64)]
+        _lib.oracle_get_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                          C.POINTER(C.c_int64)]
+        _lib.oracle_pwc_op.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                       C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]
+        _lib.oracle_pwc_mahalanobis.restype = C.c_double
+        _lib.oracle_pwc_mahalanobis.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_int]
+        _lib.oracle_pwn_norms.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p]
+        _lib.oracle_logmap.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+        _lib.oracle_atan2.restype = C.c_double
+        _lib.oracle_atan2.argtypes = [C.c_double, C.c_double]
+        _lib.oracle_chi2inv.restype = C.c_double
+        _lib.oracle_chi2inv.argtypes = [C.c_double, C.c_int]
+        _lib.oracle_pairwise_adjacency.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 9 + [
+            C.c_double, C.c_double, C.c_void_p]
+        _lib.oracle_max_clique_heu.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None and a.size else None
+
+
+def params_struct(p) -> Params:
+    """Accepts any object with the rpgo_params field names (e.g. the product's
+    RobustSolverParams mirror)."""
+    s = Params()
+    for name, _ in Params._fields_:
+        setattr(s, name, getattr(p, name))
+    return s
+
+
+class _Batch:
+    def __init__(self, g):
+        self.a = g.arrays()
+        a = self.a
+        self.f = FactorBatch(len(a["kind"]), _ptr(a["kind"]), _ptr(a["key1"]), _ptr(a["key2"]), _ptr(a["measured"]),
+                             _ptr(a["cov"]), _ptr(a["sqrt_info"]))
+        self.v = ValueBatch(len(a["value_keys"]), _ptr(a["value_keys"]), _ptr(a["value_poses"]))
+
+
+class OracleSolver:
+    """RobustSolver restated on the CPU (same call shape as the product)."""
+
+    def __init__(self, params):
+        self.dim = 2 if params.outlier_removal in (1, 3) or (params.outlier_removal == 0 and params.dim == 2) else 3
+        self._p = params_struct(params)
+        self.h = lib().oracle_create(C.byref(self._p))
+        if not self.h:
+            raise ValueError("bad parameters")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oracle_destroy(self.h)
+            self.h = None
+
+    def update(self, graph, optimize_graph: bool = True) -> int:
+        b = _Batch(graph)
+        return lib().oracle_update(self.h, C.byref(b.f), C.byref(b.v), int(optimize_graph))
+
+    def counts(self) -> Counts:
+        c = Counts()
+        lib().oracle_get_counts(self.h, C.byref(c))
+        return c
+
+    def size(self) -> int:
+        return self.counts().num_factors
+
+    def estimate(self):
+        n = self.counts().num_values
+        st = 12 if self.dim == 3 else 4
+        keys = np.zeros(n, dtype=np.uint64)
+        poses = np.zeros((n, st))
+        rc = lib().oracle_get_estimate(self.h, _ptr(keys), _ptr(poses), n)
+        assert rc == 0
+        return keys, poses
+
+    def gnc_weights(self):
+        n = self.counts().num_gnc_weights
+        w = np.zeros(n)
+        lib().oracle_get_gnc_weights(self.h, _ptr(w), n)
+        return w
+
+    def factors(self):
+        n = self.counts().num_factors
+        st = 12 if self.dim == 3 else 4
+        kind = np.zeros(n, dtype=np.int32)
+        k1 = np.zeros(n, dtype=np.uint64)
+        k2 = np.zeros(n, dtype=np.uint64)
+        meas = np.zeros((n, st))
+        lib().oracle_get_factors(self.h, _ptr(kind), _ptr(k1), _ptr(k2), _ptr(meas), n)
+        return kind, k1, k2, meas
+
+    def adjacency(self, group: int = 0):
+        n = C.c_int64(0)
+        rc = lib().oracle_get_adjacency(self.h, group, None, 0, C.byref(n))
+        if rc != 0:
+            return None
+        words = (n.value + 31) // 32
+        out = np.zeros(n.value * words, dtype=np.uint32)
+        lib().oracle_get_adjacency(self.h, group, _ptr(out), out.size, C.byref(n))
+        return out.reshape(n.value, words)
+
+    def stats(self):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        lib().oracle_get_stats(self.h, C.byref(a), C.byref(b), C.byref(c))
+        return dict(lm_iterations=a.value, linear_solves=b.value, gnc_iterations=c.value)
+
+
+# ------------------------------------------------------------------ math hooks
+def pwc_op(dim, op, pa, ca, ria=1, pb=None, cb=None, rib=1):
+    st, d = (12, 6) if dim == 3 else (4, 3)
+    pa = np.ascontiguousarray(pa, dtype=np.float64)
+    ca = np.ascontiguousarray(ca, dtype=np.float64)
+    pb = np.ascontiguousarray(pb if pb is not None else pa, dtype=np.float64)
+    cb = np.ascontiguousarray(cb if cb is not None else ca, dtype=np.float64)
+    po = np.zeros(st)
+    co = np.zeros((d, d))
+    ri = C.c_int(0)
+    lib().oracle_pwc_op(dim, op, _ptr(pa), _ptr(ca), ria, _ptr(pb), _ptr(cb), rib, _ptr(po), _ptr(co), C.byref(ri))
+    return po, co, ri.value
+
+
+def pwc_mahalanobis(dim, pose, cov, rot_info=1) -> float:
+    pose = np.ascontiguousarray(pose, dtype=np.float64)
+    cov = np.ascontiguousarray(cov, dtype=np.float64)
+    return lib().oracle_pwc_mahalanobis(dim, _ptr(pose), _ptr(cov), rot_info)
+
+
+def pwn_norms(dim, pose, node, rot_info=1):
+    pose = np.ascontiguousarray(pose, dtype=np.float64)
+    out = np.zeros(2)
+    lib().oracle_pwn_norms(dim, _ptr(pose), node, rot_info, _ptr(out))
+    return float(out[0]), float(out[1])
+
+
+def logmap(dim, pose):
+    pose = np.ascontiguousarray(pose, dtype=np.float64)
+    xi = np.zeros(6 if dim == 3 else 3)
+    lib().oracle_logmap(dim, _ptr(pose), _ptr(xi))
+    return xi
+
+
+def atan2(y, x) -> float:
+    return lib().oracle_atan2(float(y), float(x))
+
+
+def chi2inv(alpha, k) -> float:
+    return lib().oracle_chi2inv(float(alpha), int(k))
+
+
+def pairwise_adjacency(dim, mode, slot_a, slot_b, flip, z_pose, z_cov, traj_pose, traj_cov, traj_node, traj_rot,
+                       th0, th1):
+    n = len(slot_a)
+    words = (n + 31) // 32
+    adj = np.zeros((n, words), dtype=np.uint32)
+    args = [np.ascontiguousarray(x) for x in (slot_a, slot_b, flip, z_pose, z_cov, traj_pose, traj_cov, traj_node,
+                                              traj_rot)]
+    lib().oracle_pairwise_adjacency(dim, mode, n, *[_ptr(a) for a in args], float(th0), float(th1), _ptr(adj))
+    return adj
+
+
+def max_clique_heu(adj_words: np.ndarray, n: int, first: int = 0, seed: int = -1):
+    adj = np.ascontiguousarray(adj_words, dtype=np.uint32)
+    out = np.zeros(max(n, 1), dtype=np.int32)
+    size = np.zeros(1, dtype=np.int32)
+    lib().oracle_max_clique_heu(n, _ptr(adj), first, seed, _ptr(out), _ptr(size))
+    return int(size[0]), out[: max(int(size[0]), 0)].copy()
