@@ -238,6 +238,8 @@ int rpgo_max_clique_heu(int32_t n, const uint32_t* adj, int32_t first, int32_t s
 
 /* Library / device information (name of the loaded device, SM count). */
 int rpgo_device_info(char* name, int32_t name_capacity, int32_t* sm_count);
+/* Number of CUDA kernels this library has launched in this process. */
+int64_t rpgo_kernel_launch_count(void);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,628 @@
+// extern "C" boundary of the library (include/rpgo_gb300.h).
+//
+// rpgo_solver mirrors KimeraRPGO::RobustSolver (include/KimeraRPGO/RobustSolver.h,
+// src/RobustSolver.cpp) and GenericSolver (src/GenericSolver.cpp): it owns
+// the values and the graph to optimise, hands new factors to the PCM plugin
+// (pcm_engine.cpp) and runs the GPU GNC / LM / GN solve (solver.cpp). Where
+// the reference calls exit() or lets an exception escape, a status code is
+// returned instead.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <numeric>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../../include/rpgo_gb300.h"
+#include "pcm_engine.hpp"
+#include "solver.hpp"
+
+using namespace rpgo;
+
+struct rpgo_solver {
+  rpgo_params p;
+  int dim = 3, stride = 12, d = 6;
+  cudaStream_t st = nullptr;
+  Values values;
+  std::vector<FactorRec> nfg;
+  std::unique_ptr<PcmEngine> pcm;
+  std::vector<double> gnc_weights;
+  size_t gnc_num_inliers = 0, latest_num_lc = 0;
+  bool last_do_optimize = false;
+  rpgo_timing timing{};
+};
+
+namespace {
+
+double ms_since(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+std::vector<FactorRec> convert(const rpgo_solver* s, const rpgo_factor_batch* f) {
+  std::vector<FactorRec> out;
+  if (!f) return out;
+  out.resize((size_t)f->count);
+  for (int64_t k = 0; k < f->count; ++k) {
+    FactorRec& r = out[k];
+    r.kind = f->kind[k];
+    r.k1 = f->key_front[k];
+    r.k2 = (r.kind == RPGO_FACTOR_BETWEEN) ? f->key_back[k] : f->key_front[k];
+    std::memcpy(r.meas, f->measured + k * s->stride, sizeof(double) * s->stride);
+    std::memcpy(r.cov, f->covariance + k * s->d * s->d, sizeof(double) * s->d * s->d);
+    std::memcpy(r.sqrt_info, f->sqrt_information + k * s->d * s->d, sizeof(double) * s->d * s->d);
+  }
+  return out;
+}
+
+// RobustSolver::optimize (src/RobustSolver.cpp:115-306)
+int optimize(rpgo_solver* s) {
+  LmParams lp;
+  lp.gauss_newton = s->p.solver == RPGO_SOLVER_GN;
+  lp.diagonal_damping = s->p.lm_diagonal_damping != 0;
+  std::vector<FactorRec> full = s->nfg;
+  NlsStats st;
+  const size_t num_lc = s->pcm ? s->pcm->num_lc() : 0;
+  Values result;
+  if (s->p.use_gnc && s->pcm && !(s->p.gnc_fix_prev_inliers && num_lc == s->latest_num_lc)) {
+    GncConfig g;
+    g.threshold_mode = s->p.gnc_threshold_mode;
+    g.threshold = s->p.gnc_inlier_threshold;
+    g.max_iterations = s->p.gnc_max_iterations;
+    g.mu_step = s->p.gnc_mu_step;
+    g.rel_cost_tol = s->p.gnc_relative_cost_tol;
+    g.weights_tol = s->p.gnc_weights_tol;
+    const size_t n_known = s->pcm->num_odom() + s->pcm->num_special();
+    std::vector<double> init;
+    if (s->p.gnc_bias_odom) {
+      init.assign(full.size(), 0.0);
+      for (size_t i = 0; i < n_known && i < init.size(); ++i) init[i] = 1.0;
+    }
+    GpuNls nls(s->dim, full, s->values, s->st);
+    std::vector<double> w;
+    gnc_tls(nls, n_known, g, lp, s->p.gnc_bias_odom ? &init : nullptr, &w, &st);
+    nls.result(&result);
+    s->gnc_weights.assign(w.begin(), w.begin() + std::min(w.size(), s->nfg.size()));
+    const double sum = std::accumulate(s->gnc_weights.begin(), s->gnc_weights.end(), 0.0);
+    s->gnc_num_inliers = static_cast<size_t>(sum) - n_known;
+  } else {
+    if (s->p.gnc_fix_prev_inliers && s->pcm) {
+      const size_t prev_k = s->gnc_weights.size() - std::min(s->latest_num_lc, s->gnc_weights.size());
+      const size_t k = s->pcm->num_odom() + s->pcm->num_special();
+      full.assign(s->nfg.begin(), s->nfg.begin() + std::min(k, s->nfg.size()));
+      for (size_t i = 0; i < s->latest_num_lc; ++i)
+        if (prev_k + i < s->gnc_weights.size() && s->gnc_weights[prev_k + i] > 0.5 && k + i < s->nfg.size())
+          full.push_back(s->nfg[k + i]);
+    }
+    GpuNls nls(s->dim, full, s->values, s->st);
+    nls.optimize(lp, &st);
+    if (st.failed) return RPGO_ERR_SOLVER;
+    nls.result(&result);
+    const size_t tail = std::min(s->latest_num_lc, s->gnc_weights.size());
+    std::vector<double> lcw(s->gnc_weights.end() - tail, s->gnc_weights.end());
+    s->gnc_weights.assign(s->nfg.size(), 1.0);
+    const size_t t2 = std::min(tail, s->gnc_weights.size());
+    for (size_t i = 0; i < t2; ++i) s->gnc_weights[s->gnc_weights.size() - t2 + i] = lcw[lcw.size() - t2 + i];
+  }
+  s->timing.lm_iterations += st.iterations;
+  s->timing.linear_solves += st.linear_solves;
+  s->timing.cg_iterations += st.cg_iterations;
+  s->timing.gnc_iterations += st.gnc_iterations;
+  // GenericSolver::updateValues (src/GenericSolver.cpp:37-45)
+  for (auto& kv : result) {
+    auto it = s->values.find(kv.first);
+    if (it != s->values.end()) it->second = kv.second;
+  }
+  if (s->pcm) s->latest_num_lc = s->pcm->num_lc();
+  return RPGO_OK;
+}
+
+int update_impl(rpgo_solver* s, const rpgo_factor_batch* fb, const rpgo_value_batch* vb, int optimize_graph,
+                bool force) {
+  auto nf = convert(s, fb);
+  std::set<uint64_t> new_keys;
+  if (vb) {
+    for (int64_t k = 0; k < vb->count; ++k) {
+      if (s->values.count(vb->key[k]) || new_keys.count(vb->key[k])) return RPGO_ERR_KEY;
+      new_keys.insert(vb->key[k]);
+    }
+    for (int64_t k = 0; k < vb->count; ++k)
+      s->values[vb->key[k]] = std::vector<double>(vb->pose + k * s->stride, vb->pose + (k + 1) * s->stride);
+  }
+  cudaEvent_t e0, e1, e2;
+  RPGO_CUDA(cudaEventCreate(&e0));
+  RPGO_CUDA(cudaEventCreate(&e1));
+  RPGO_CUDA(cudaEventCreate(&e2));
+  const int64_t launches0 = launch_counter().load();
+  const int64_t pairs0 = s->pcm ? s->pcm->stats().pair_checks : 0;
+  RPGO_CUDA(cudaEventRecord(e0, s->st));
+  bool do_opt;
+  if (s->pcm) {
+    do_opt = s->pcm->remove_outliers(nf, new_keys, s->values, &s->nfg);
+  } else {
+    // GenericSolver::addAndCheckIfOptimize (src/GenericSolver.cpp:47-65)
+    s->nfg.insert(s->nfg.end(), nf.begin(), nf.end());
+    do_opt = true;
+    if (nf.size() == 1 && nf[0].kind == RPGO_FACTOR_BETWEEN && new_keys.size() == 1) do_opt = false;
+    if (nf.empty() && new_keys.empty()) do_opt = false;
+  }
+  s->last_do_optimize = do_opt;
+  RPGO_CUDA(cudaEventRecord(e1, s->st));
+  for (const auto& f : s->nfg)
+    if (!s->values.count(f.k1) || !s->values.count(f.k2)) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      cudaEventDestroy(e2);
+      return RPGO_ERR_KEY;
+    }
+  int rc = RPGO_OK;
+  if ((do_opt && optimize_graph) || force) rc = optimize(s);
+  RPGO_CUDA(cudaEventRecord(e2, s->st));
+  RPGO_CUDA(cudaEventSynchronize(e2));
+  s->timing.pcm_ms = ms_since(e0, e1);
+  s->timing.solve_ms = ms_since(e1, e2);
+  s->timing.pair_checks = (s->pcm ? s->pcm->stats().pair_checks : 0) - pairs0;
+  s->timing.kernel_launches = launch_counter().load() - launches0;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  return rc;
+}
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const CudaError& e) {
+    std::fprintf(stderr, "rpgo_gb300: %s\n", e.what());
+    return RPGO_ERR_CUDA;
+  } catch (const std::out_of_range&) {
+    return RPGO_ERR_KEY;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "rpgo_gb300: %s\n", e.what());
+    return RPGO_ERR_ARG;
+  }
+}
+
+int device_ready() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) return 0;
+  return 1;
+}
+
+std::vector<FactorRec> concat(const rpgo_solver* s, const rpgo_factor_batch* a, const rpgo_factor_batch* b) {
+  auto x = convert(s, a);
+  auto y = convert(s, b);
+  x.insert(x.end(), y.begin(), y.end());
+  return x;
+}
+
+}  // namespace
+
+extern "C" {
+
+void rpgo_params_default(rpgo_params* p) {
+  std::memset(p, 0, sizeof(*p));
+  p->solver = RPGO_SOLVER_LM;
+  p->outlier_removal = RPGO_OUTLIER_PCM3D;
+  p->verbosity = RPGO_VERBOSITY_UPDATE;
+  p->dim = 3;
+  p->odom_threshold = 10.0;
+  p->lc_threshold = 5.0;
+  p->odom_trans_threshold = 0.05;
+  p->odom_rot_threshold = 0.005;
+  p->dist_trans_threshold = 0.01;
+  p->dist_rot_threshold = 0.001;
+  p->incremental = 0;
+  p->use_gnc = 0;
+  p->gnc_threshold_mode = RPGO_GNC_PROBABILITY;
+  p->gnc_inlier_threshold = 0.9;
+  p->gnc_max_iterations = 100;
+  p->gnc_mu_step = 1.4;
+  p->gnc_relative_cost_tol = 1e-5;
+  p->gnc_weights_tol = 1e-4;
+  p->gnc_fix_prev_inliers = 0;
+  p->gnc_bias_odom = 0;
+  p->lm_diagonal_damping = 1;
+}
+void rpgo_params_set_no_rejection(rpgo_params* p, int32_t v) {
+  p->outlier_removal = RPGO_OUTLIER_NONE;
+  p->verbosity = v;
+}
+void rpgo_params_set_pcm2d(rpgo_params* p, double o, double l, int32_t v) {
+  p->outlier_removal = RPGO_OUTLIER_PCM2D;
+  p->dim = 2;
+  p->odom_threshold = o;
+  p->lc_threshold = l;
+  p->verbosity = v;
+}
+void rpgo_params_set_pcm3d(rpgo_params* p, double o, double l, int32_t v) {
+  p->outlier_removal = RPGO_OUTLIER_PCM3D;
+  p->dim = 3;
+  p->odom_threshold = o;
+  p->lc_threshold = l;
+  p->verbosity = v;
+}
+void rpgo_params_set_pcm_simple2d(rpgo_params* p, double to, double ro, double tp, double rp, int32_t v) {
+  p->outlier_removal = RPGO_OUTLIER_PCM_SIMPLE2D;
+  p->dim = 2;
+  p->odom_trans_threshold = to;
+  p->odom_rot_threshold = ro;
+  p->dist_trans_threshold = tp;
+  p->dist_rot_threshold = rp;
+  p->verbosity = v;
+}
+void rpgo_params_set_pcm_simple3d(rpgo_params* p, double to, double ro, double tp, double rp, int32_t v) {
+  p->outlier_removal = RPGO_OUTLIER_PCM_SIMPLE3D;
+  p->dim = 3;
+  p->odom_trans_threshold = to;
+  p->odom_rot_threshold = ro;
+  p->dist_trans_threshold = tp;
+  p->dist_rot_threshold = rp;
+  p->verbosity = v;
+}
+static void set_gnc(rpgo_params* p, int mode, double t, int32_t it, double mu, double rc, double wt, int32_t fix,
+                    int32_t bias) {
+  p->use_gnc = 1;
+  p->gnc_threshold_mode = mode;
+  p->gnc_inlier_threshold = t;
+  p->gnc_max_iterations = it;
+  p->gnc_mu_step = mu;
+  p->gnc_relative_cost_tol = rc;
+  p->gnc_weights_tol = wt;
+  p->gnc_fix_prev_inliers = fix;
+  p->gnc_bias_odom = bias;
+}
+void rpgo_params_set_gnc_probability(rpgo_params* p, double a, int32_t it, double mu, double rc, double wt,
+                                     int32_t fix, int32_t bias) {
+  set_gnc(p, RPGO_GNC_PROBABILITY, a, it, mu, rc, wt, fix, bias);
+}
+void rpgo_params_set_gnc_cost(rpgo_params* p, double c, int32_t it, double mu, double rc, double wt, int32_t fix,
+                              int32_t bias) {
+  set_gnc(p, RPGO_GNC_COST, c, it, mu, rc, wt, fix, bias);
+}
+
+rpgo_solver* rpgo_create(const rpgo_params* p) {
+  if (!p) return nullptr;
+  const int m = p->outlier_removal;
+  if (m < RPGO_OUTLIER_NONE || m > RPGO_OUTLIER_PCM_SIMPLE3D) return nullptr;
+  if (p->solver != RPGO_SOLVER_LM && p->solver != RPGO_SOLVER_GN) return nullptr;
+  int dim = (m == RPGO_OUTLIER_PCM2D || m == RPGO_OUTLIER_PCM_SIMPLE2D) ? 2 : (m == RPGO_OUTLIER_NONE ? p->dim : 3);
+  if (dim != 2 && dim != 3) return nullptr;
+  if (!device_ready()) return nullptr;
+  auto s = std::make_unique<rpgo_solver>();
+  s->p = *p;
+  s->dim = dim;
+  s->stride = dim == 3 ? 12 : 4;
+  s->d = dim == 3 ? 6 : 3;
+  try {
+    RPGO_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+    if (m != RPGO_OUTLIER_NONE) {
+      PcmConfig c;
+      c.dim = dim;
+      c.mode = (m == RPGO_OUTLIER_PCM_SIMPLE2D || m == RPGO_OUTLIER_PCM_SIMPLE3D) ? 1 : 0;
+      c.odom_threshold = p->odom_threshold;
+      c.lc_threshold = p->lc_threshold;
+      c.odom_trans_threshold = p->odom_trans_threshold;
+      c.odom_rot_threshold = p->odom_rot_threshold;
+      c.dist_trans_threshold = p->dist_trans_threshold;
+      c.dist_rot_threshold = p->dist_rot_threshold;
+      c.incremental = p->incremental != 0;
+      s->pcm = std::make_unique<PcmEngine>(c, s->st);
+    }
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "rpgo_gb300: %s\n", e.what());
+    return nullptr;
+  }
+  return s.release();
+}
+
+void rpgo_destroy(rpgo_solver* s) {
+  if (!s) return;
+  cudaStream_t st = s->st;
+  s->pcm.reset();
+  delete s;
+  if (st) cudaStreamDestroy(st);
+}
+
+int rpgo_update(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, int32_t optimize_graph) {
+  if (!s) return RPGO_ERR_ARG;
+  return guarded([&] { return update_impl(s, f, v, optimize_graph, false); });
+}
+int rpgo_force_update(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v) {
+  if (!s) return RPGO_ERR_ARG;
+  return guarded([&] { return update_impl(s, f, v, 1, true); });
+}
+
+static int update_with_extra(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v,
+                             const rpgo_factor_batch* extra) {
+  if (!s) return RPGO_ERR_ARG;
+  return guarded([&] {
+    auto all = concat(s, f, extra);
+    std::vector<int32_t> kind(all.size());
+    std::vector<uint64_t> k1(all.size()), k2(all.size());
+    std::vector<double> meas(all.size() * s->stride), cov(all.size() * s->d * s->d), R(all.size() * s->d * s->d);
+    for (size_t i = 0; i < all.size(); ++i) {
+      kind[i] = all[i].kind;
+      k1[i] = all[i].k1;
+      k2[i] = all[i].k2;
+      std::memcpy(&meas[i * s->stride], all[i].meas, sizeof(double) * s->stride);
+      std::memcpy(&cov[i * s->d * s->d], all[i].cov, sizeof(double) * s->d * s->d);
+      std::memcpy(&R[i * s->d * s->d], all[i].sqrt_info, sizeof(double) * s->d * s->d);
+    }
+    rpgo_factor_batch b{(int64_t)all.size(), kind.data(), k1.data(), k2.data(), meas.data(), cov.data(), R.data()};
+    return update_impl(s, &b, v, 1, false);
+  });
+}
+int rpgo_load_graph(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v,
+                    const rpgo_factor_batch* prior) {
+  return update_with_extra(s, f, v, prior);
+}
+int rpgo_add_graph(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v,
+                   const rpgo_factor_batch* between) {
+  return update_with_extra(s, f, v, between);
+}
+
+int rpgo_get_counts(const rpgo_solver* s, rpgo_counts* c) {
+  if (!s || !c) return RPGO_ERR_ARG;
+  c->num_factors = (int64_t)s->nfg.size();
+  c->num_values = (int64_t)s->values.size();
+  c->num_lc = s->pcm ? (int64_t)s->pcm->num_lc() : 0;
+  c->num_lc_inliers = s->p.use_gnc ? (int64_t)s->gnc_num_inliers : (s->pcm ? (int64_t)s->pcm->num_lc_inliers() : 0);
+  c->num_odom = s->pcm ? (int64_t)s->pcm->num_odom() : 0;
+  c->num_special = s->pcm ? (int64_t)s->pcm->num_special() : 0;
+  c->num_gnc_weights = (int64_t)s->gnc_weights.size();
+  c->last_do_optimize = s->last_do_optimize ? 1 : 0;
+  return RPGO_OK;
+}
+int rpgo_get_estimate(const rpgo_solver* s, uint64_t* keys, double* poses, int64_t cap) {
+  if (!s || (int64_t)s->values.size() > cap) return RPGO_ERR_ARG;
+  int64_t i = 0;
+  for (const auto& kv : s->values) {
+    keys[i] = kv.first;
+    std::memcpy(poses + i * s->stride, kv.second.data(), sizeof(double) * s->stride);
+    ++i;
+  }
+  return RPGO_OK;
+}
+int rpgo_get_gnc_weights(const rpgo_solver* s, double* w, int64_t cap) {
+  if (!s || (int64_t)s->gnc_weights.size() > cap) return RPGO_ERR_ARG;
+  std::memcpy(w, s->gnc_weights.data(), sizeof(double) * s->gnc_weights.size());
+  return RPGO_OK;
+}
+int rpgo_get_factors(const rpgo_solver* s, int32_t* kind, uint64_t* k1, uint64_t* k2, double* meas, int64_t cap) {
+  if (!s || (int64_t)s->nfg.size() > cap) return RPGO_ERR_ARG;
+  for (size_t i = 0; i < s->nfg.size(); ++i) {
+    if (kind) kind[i] = s->nfg[i].kind;
+    if (k1) k1[i] = s->nfg[i].k1;
+    if (k2) k2[i] = s->nfg[i].k2;
+    if (meas) std::memcpy(meas + i * s->stride, s->nfg[i].meas, sizeof(double) * s->stride);
+  }
+  return RPGO_OK;
+}
+int rpgo_get_adjacency(const rpgo_solver* s, int32_t group, uint32_t* words, int64_t cap, int64_t* n) {
+  if (!s || !n) return RPGO_ERR_ARG;
+  if (!s->pcm) return RPGO_ERR_UNSUPPORTED;
+  return guarded([&] {
+    std::vector<uint32_t> w;
+    int nn = 0;
+    if (!s->pcm->adjacency(group, &w, &nn)) return (int)RPGO_ERR_ARG;
+    *n = nn;
+    if (!words) return (int)RPGO_OK;
+    if ((int64_t)w.size() > cap) return (int)RPGO_ERR_ARG;
+    std::memcpy(words, w.data(), w.size() * sizeof(uint32_t));
+    return (int)RPGO_OK;
+  });
+}
+int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* t) {
+  if (!s || !t) return RPGO_ERR_ARG;
+  *t = s->timing;
+  return RPGO_OK;
+}
+
+int rpgo_save_data(const rpgo_solver* s, const char* folder) {
+  if (!s || !folder) return RPGO_ERR_ARG;
+  // writeG2o (src/Logger.cpp:64-164) and gnc_weights.csv (src/RobustSolver.cpp:448-465)
+  const std::string base(folder);
+  std::ofstream g2o(base + "/result.g2o");
+  if (!g2o) return RPGO_ERR_ARG;
+  auto quat = [](const double* R, double q[4]) {
+    const double tr = R[0] + R[4] + R[8];
+    if (tr > 0) {
+      const double w = std::sqrt(tr + 1.0) * 2;
+      q[0] = 0.25 * w; q[1] = (R[7] - R[5]) / w; q[2] = (R[2] - R[6]) / w; q[3] = (R[3] - R[1]) / w;
+    } else if (R[0] > R[4] && R[0] > R[8]) {
+      const double w = std::sqrt(1.0 + R[0] - R[4] - R[8]) * 2;
+      q[0] = (R[7] - R[5]) / w; q[1] = 0.25 * w; q[2] = (R[1] + R[3]) / w; q[3] = (R[2] + R[6]) / w;
+    } else if (R[4] > R[8]) {
+      const double w = std::sqrt(1.0 + R[4] - R[0] - R[8]) * 2;
+      q[0] = (R[2] - R[6]) / w; q[1] = (R[1] + R[3]) / w; q[2] = 0.25 * w; q[3] = (R[5] + R[7]) / w;
+    } else {
+      const double w = std::sqrt(1.0 + R[8] - R[0] - R[4]) * 2;
+      q[0] = (R[3] - R[1]) / w; q[1] = (R[2] + R[6]) / w; q[2] = (R[5] + R[7]) / w; q[3] = 0.25 * w;
+    }
+  };
+  for (const auto& kv : s->values) {
+    const double* p = kv.second.data();
+    if (s->dim == 2) {
+      g2o << "VERTEX_SE2 " << kv.first << " " << p[2] << " " << p[3] << " " << std::atan2(p[1], p[0]) << "\n";
+    } else {
+      double q[4];
+      quat(p, q);
+      g2o << "VERTEX_SE3:QUAT " << kv.first << " " << p[9] << " " << p[10] << " " << p[11] << " " << q[1] << " "
+          << q[2] << " " << q[3] << " " << q[0] << "\n";
+    }
+  }
+  for (const auto& f : s->nfg) {
+    if (f.kind != RPGO_FACTOR_BETWEEN) continue;
+    const int d = s->d;
+    double info[36];
+    for (int i = 0; i < d; ++i)
+      for (int j = 0; j < d; ++j) {
+        double acc = 0.0;
+        for (int k = 0; k < d; ++k) acc += f.sqrt_info[d * k + i] * f.sqrt_info[d * k + j];
+        info[d * i + j] = acc;
+      }
+    const double* m = f.meas;
+    if (s->dim == 2) {
+      g2o << "EDGE_SE2 " << f.k1 << " " << f.k2 << " " << m[2] << " " << m[3] << " " << std::atan2(m[1], m[0]);
+      for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j) g2o << " " << info[3 * i + j];
+    } else {
+      double q[4];
+      quat(m, q);
+      g2o << "EDGE_SE3:QUAT " << f.k1 << " " << f.k2 << " " << m[9] << " " << m[10] << " " << m[11] << " " << q[1]
+          << " " << q[2] << " " << q[3] << " " << q[0];
+      // diagonal blocks swapped to [t; R], off-diagonal blocks copied in place (Logger.cpp:148-152)
+      double gi[36];
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+          const bool di = i < 3, dj = j < 3;
+          int si = i, sj = j;
+          if (di && dj) { si = i + 3; sj = j + 3; }
+          else if (!di && !dj) { si = i - 3; sj = j - 3; }
+          gi[6 * i + j] = info[6 * si + sj];
+        }
+      for (int i = 0; i < 6; ++i)
+        for (int j = i; j < 6; ++j) g2o << " " << gi[6 * i + j];
+    }
+    g2o << "\n";
+  }
+  if (s->p.use_gnc) {
+    std::ofstream w(base + "/gnc_weights.csv");
+    w.precision(17);
+    for (size_t i = 0; i < s->gnc_weights.size(); ++i) w << s->gnc_weights[i] << (i + 1 < s->gnc_weights.size() ? "\n" : "");
+  }
+  return RPGO_OK;
+}
+
+// ------------------------------------------------------------------ stage entry points (device pointers)
+int rpgo_trajectory_scan_dev(int32_t dim, int32_t mode, int64_t count, const int32_t* src, const int32_t* dst,
+                             const double* delta_pose, const double* delta_cov, double* traj_pose, double* traj_cov,
+                             int32_t* traj_node, uint8_t* traj_rot_info, void* stream) {
+  if ((dim != 2 && dim != 3) || (mode != 0 && mode != 1) || count < 0) return RPGO_ERR_ARG;
+  return guarded([&] {
+    DeviceBuffer<double> rec, cov;
+    DeviceBuffer<uint8_t> rot;
+    TrajView tv{traj_pose, traj_cov, traj_node, traj_rot_info};
+    launch_traj_scan(dim, mode, count, src, dst, delta_pose, delta_cov, tv, rec, cov, rot, (cudaStream_t)stream);
+    RPGO_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return (int)RPGO_OK;
+  });
+}
+int rpgo_odometry_check_dev(int32_t dim, int32_t mode, int64_t count, const int32_t* si, const int32_t* sj,
+                            const double* zp, const double* zc, const double* tp, const double* tc, const int32_t* tn,
+                            const uint8_t* tr, double th0, double th1, uint8_t* ok, void* stream) {
+  if ((dim != 2 && dim != 3) || (mode != 0 && mode != 1) || count < 0) return RPGO_ERR_ARG;
+  return guarded([&] {
+    TrajView tv{const_cast<double*>(tp), const_cast<double*>(tc), const_cast<int32_t*>(tn),
+                const_cast<uint8_t*>(tr)};
+    launch_odom_check(dim, mode, count, si, sj, zp, zc, tv, th0, th1, ok, (cudaStream_t)stream);
+    RPGO_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return (int)RPGO_OK;
+  });
+}
+int rpgo_pairwise_adjacency_dev(int32_t dim, int32_t mode, int32_t n, int32_t row_begin, const int32_t* sa,
+                                const int32_t* sb, const uint8_t* flip, const double* zp, const double* zc,
+                                const double* tp, const double* tc, const int32_t* tn, const uint8_t* tr, double th0,
+                                double th1, uint32_t* adj, int32_t words, void* stream) {
+  if ((dim != 2 && dim != 3) || (mode != 0 && mode != 1) || n < 0 || row_begin < 0 || row_begin > n ||
+      words < (n + 31) / 32)
+    return RPGO_ERR_ARG;
+  return guarded([&] {
+    TrajView tv{const_cast<double*>(tp), const_cast<double*>(tc), const_cast<int32_t*>(tn),
+                const_cast<uint8_t*>(tr)};
+    DeviceBuffer<uint32_t> lower((size_t)(n - row_begin) * words + 1);
+    launch_pairwise(dim, mode, n, row_begin, sa, sb, flip, zp, zc, tv, th0, th1, adj, words, lower.get(),
+                    (cudaStream_t)stream);
+    RPGO_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return (int)RPGO_OK;
+  });
+}
+int rpgo_max_clique_heu_dev(int32_t n, const uint32_t* adj, int32_t words, int32_t first, int32_t seed,
+                            int32_t* clique_out, int32_t* size_out, void* stream) {
+  if (n < 0 || words < (n + 31) / 32 || !size_out) return RPGO_ERR_ARG;
+  return guarded([&] {
+    CliqueWorkspace ws;
+    std::vector<int32_t> cl;
+    const int sz = max_clique_heu(n, adj, words, first, seed, &cl, ws, (cudaStream_t)stream);
+    *size_out = sz;
+    if (clique_out)
+      for (size_t i = 0; i < cl.size(); ++i) clique_out[i] = cl[i];
+    return (int)RPGO_OK;
+  });
+}
+
+// ------------------------------------------------------------------ stage entry points (host arrays)
+int rpgo_pairwise_adjacency(int32_t dim, int32_t mode, int32_t n, const int32_t* sa, const int32_t* sb,
+                            const uint8_t* flip, const double* zp, const double* zc, int32_t num_slots,
+                            const double* tp, const double* tc, const int32_t* tn, const uint8_t* tr, double th0,
+                            double th1, uint32_t* adj) {
+  if ((dim != 2 && dim != 3) || (mode != 0 && mode != 1) || n < 0 || num_slots < 0) return RPGO_ERR_ARG;
+  if (!device_ready()) return RPGO_ERR_CUDA;
+  return guarded([&] {
+    const int stride = dim == 3 ? 12 : 4, d = dim == 3 ? 6 : 3;
+    const int words = (n + 31) / 32;
+    cudaStream_t st = 0;
+    DeviceBuffer<int32_t> dsa, dsb, dtn;
+    DeviceBuffer<uint8_t> dfl, dtr;
+    DeviceBuffer<double> dzp, dzc, dtp, dtc;
+    DeviceBuffer<uint32_t> dadj((size_t)n * words + 1), lower((size_t)n * words + 1);
+    dsa.upload(sa, n, st);
+    dsb.upload(sb, n, st);
+    dfl.upload(flip, n, st);
+    dzp.upload(zp, (size_t)n * stride, st);
+    dzc.upload(zc, (size_t)n * d * d, st);
+    dtp.upload(tp, (size_t)num_slots * stride, st);
+    if (mode == 0) dtc.upload(tc, (size_t)num_slots * d * d, st);
+    else dtn.upload(tn, num_slots, st);
+    dtr.upload(tr, num_slots, st);
+    dadj.zero(st);
+    TrajView tv{dtp.get(), dtc.get(), dtn.get(), dtr.get()};
+    launch_pairwise(dim, mode, n, 0, dsa.get(), dsb.get(), dfl.get(), dzp.get(), dzc.get(), tv, th0, th1,
+                    dadj.get(), words, lower.get(), st);
+    dadj.download(adj, (size_t)n * words, st);
+    RPGO_CUDA(cudaStreamSynchronize(st));
+    return (int)RPGO_OK;
+  });
+}
+int rpgo_max_clique_heu(int32_t n, const uint32_t* adj, int32_t first, int32_t seed, int32_t* clique_out,
+                        int32_t* size_out) {
+  if (n < 0 || !size_out) return RPGO_ERR_ARG;
+  if (!device_ready()) return RPGO_ERR_CUDA;
+  return guarded([&] {
+    const int words = (n + 31) / 32;
+    cudaStream_t st = 0;
+    DeviceBuffer<uint32_t> dadj;
+    dadj.upload(adj, (size_t)n * words, st);
+    CliqueWorkspace ws;
+    std::vector<int32_t> cl;
+    const int sz = max_clique_heu(n, dadj.get(), words, first, seed, &cl, ws, st);
+    *size_out = sz;
+    if (clique_out)
+      for (size_t i = 0; i < cl.size(); ++i) clique_out[i] = cl[i];
+    return (int)RPGO_OK;
+  });
+}
+
+int rpgo_device_info(char* name, int32_t cap, int32_t* sm_count) {
+  if (!device_ready()) return RPGO_ERR_CUDA;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, 0) != cudaSuccess) return RPGO_ERR_CUDA;
+  if (name && cap > 0) {
+    std::strncpy(name, prop.name, (size_t)cap - 1);
+    name[cap - 1] = 0;
+  }
+  if (sm_count) *sm_count = prop.multiProcessorCount;
+  return RPGO_OK;
+}
+
+int64_t rpgo_kernel_launch_count(void) { return launch_counter().load(); }
+
+}  // extern "C"

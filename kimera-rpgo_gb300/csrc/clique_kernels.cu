@@ -1,0 +1,230 @@
+// Greedy max clique on a bit-packed adjacency (sm_103a).
+//
+// Exact replica of FMC::maxCliqueHeu / maxCliqueHeuIncremental
+// (include/KimeraRPGO/max_clique_finder/findCliqueHeu.cpp:32-209) as called by
+// findMaxCliqueHeu[Incremental] (src/utils/GraphUtils.cpp:19-44):
+//  * candidate v is skipped when the running best exceeds deg(v);
+//  * its work list is [v] followed by its neighbours u (ascending) with
+//    deg(u) >= best;
+//  * every round takes the last list element m and keeps, in order, the
+//    elements adjacent to m (with deg >= best); the number of rounds is the
+//    candidate's score;
+//  * a candidate that beats the running best copies the whole work buffer.
+// Because every kept element after the first is a neighbour of v and the list
+// stays sorted, the list is [v] + a set B, m = max(B) and B' = B & N(m): each
+// round is one AND of bit rows plus a population count. The buffer slot p > 0
+// ends up holding the p-th smallest element of the last round's B with at
+// least p elements, so a round that shrinks B from n_r to n_{r+1} elements
+// writes its n_r - n_{r+1} largest elements to slots (n_{r+1}, n_r].
+//
+// The running best makes candidates depend on each other only through the
+// pruning threshold, so a window of candidates is scored concurrently with
+// the threshold at the window start; the host takes the first candidate that
+// improves and restarts the window after it (later results used a stale
+// threshold). A candidate that can no longer beat the threshold
+// (rounds + |B| + 1 <= best) stops early: it could not change the result.
+#include "pcm_kernels.hpp"
+
+namespace rpgo {
+namespace {
+
+__global__ void k_degrees(int n, const uint32_t* __restrict__ adj, int words, int32_t* __restrict__ deg) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  int c = 0;
+  for (int w = lane; w < words; w += 32) {
+    uint32_t x = adj[(size_t)warp * words + w];
+    if (32 * w + 32 > n) x &= (32 * w >= n) ? 0u : ((1u << (n - 32 * w)) - 1u);  // ignore padding bits
+    if (w == (warp >> 5)) x &= ~(1u << (warp & 31));                               // and the diagonal
+    c += __popc(x);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if (lane == 0) deg[warp] = c;
+}
+
+__device__ __forceinline__ int warp_sum(int v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ int warp_max(int v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// One warp per candidate of the window [v0, v0 + count).
+// result[s]: -1 pruned (deg < best), -2 cannot beat best, else icc.
+// sets: per slot 2*words (double buffer); bufs: per slot buf_len ints.
+__global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int words, const int32_t* __restrict__ deg,
+                                int v0, int count, int best, int32_t* __restrict__ result,
+                                uint32_t* __restrict__ sets, int32_t* __restrict__ bufs, int buf_len) {
+  const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (slot >= count) return;
+  const int v = v0 + slot;
+  if (best > deg[v]) {
+    if (lane == 0) result[slot] = -1;
+    return;
+  }
+  uint32_t* cur = sets + (size_t)slot * 2 * words;
+  uint32_t* nxt = cur + words;
+  int32_t* buf = bufs + (size_t)slot * buf_len;
+  // B0 = N(v) restricted to deg >= best
+  int cnt = 0, top = -1;
+  for (int w = lane; w < words; w += 32) {
+    uint32_t x = adj[(size_t)v * words + w];
+    uint32_t keep = 0;
+    while (x) {
+      const int b = __ffs(x) - 1;
+      x &= x - 1;
+      const int u = 32 * w + b;
+      if (u < n && u != v && best <= deg[u]) keep |= 1u << b;
+    }
+    cur[w] = keep;
+    cnt += __popc(keep);
+    if (keep) top = w;
+  }
+  int nr = warp_sum(cnt);
+  top = warp_max(top);
+  if (lane == 0) buf[0] = v;
+  int r = 0;
+  __syncwarp();
+  while (true) {
+    if (nr == 0) {
+      if (lane == 0) result[slot] = r + 1;
+      return;
+    }
+    if (r + nr + 1 <= best) {
+      if (lane == 0) result[slot] = -2;
+      return;
+    }
+    // m = highest element of B: top word's highest bit
+    int m;
+    {
+      // find the highest nonzero word at or below `top`
+      int hw = -1;
+      for (int base = top - (top % 32); base >= 0 && hw < 0; base -= 32) {
+        const int w = base + lane;
+        const uint32_t x = (w <= top && w < words) ? cur[w] : 0u;
+        const unsigned msk = __ballot_sync(0xffffffffu, x != 0u);
+        if (msk) {
+          const int l = 31 - __clz(msk);
+          hw = base + l;
+        }
+      }
+      if (hw < 0) {  // cannot happen when nr > 0; never index below the set
+        if (lane == 0) result[slot] = -3;
+        return;
+      }
+      top = hw;
+      const uint32_t xw = cur[hw];
+      m = 32 * hw + (31 - __clz(xw));
+    }
+    // B' = B & N(m) over words [0, top]
+    int c2 = 0, top2 = -1;
+    for (int w = lane; w <= top; w += 32) {
+      uint32_t x = cur[w] & adj[(size_t)m * words + w];
+      if (w == (m >> 5)) x &= ~(1u << (m & 31));  // m is never its own neighbour: every round shrinks B
+      nxt[w] = x;
+      c2 += __popc(x);
+      if (x) top2 = w;
+    }
+    const int n_next = warp_sum(c2);
+    top2 = warp_max(top2);
+    __syncwarp();
+    // slots (n_next, nr] <- the nr - n_next largest elements of B, ascending
+    int need = nr - n_next;
+    int pos = nr;  // slot of the next element taken from the top
+    for (int base = top; base >= 0 && need > 0; base -= 32) {
+      const int w = base - lane;  // lane 0 takes the highest word of the chunk
+      const uint32_t x = (w >= 0) ? cur[w] : 0u;
+      const int pc = __popc(x);
+      // exclusive prefix from the top (lane 0 first)
+      int incl = pc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+      }
+      const int excl = incl - pc;
+      if (excl < need) {
+        // emit elements of this word from its top bit down
+        uint32_t y = x;
+        int q = excl;
+        while (y && q < need) {
+          const int b = 31 - __clz(y);
+          y &= ~(1u << b);
+          buf[pos - q] = 32 * w + b;
+          ++q;
+        }
+      }
+      const int total = __shfl_sync(0xffffffffu, incl, 31);
+      need -= total;
+      pos -= total;
+    }
+    __syncwarp();
+    uint32_t* t = cur;
+    cur = nxt;
+    nxt = t;
+    nr = n_next;
+    top = top2 < 0 ? 0 : top2;
+    ++r;
+  }
+}
+
+}  // namespace
+
+int max_clique_heu(int n, const uint32_t* adj, int words, int first, int seed, std::vector<int32_t>* clique,
+                   CliqueWorkspace& ws, cudaStream_t st) {
+  clique->clear();
+  if (n <= 0) return seed;
+  ws.deg.resize(n);
+  {
+    const int tb = 256;
+    k_degrees<<<div_up((int64_t)n * 32, tb), tb, 0, st>>>(n, adj, words, ws.deg.get());
+    RPGO_LAUNCHED();
+  }
+  const int W = 2048;
+  const int buf_len = n + 1;
+  ws.result.resize(W);
+  ws.sets.resize((size_t)W * 2 * words);
+  ws.buffers.resize((size_t)W * buf_len);
+  ws.h_result.resize(W);
+  int best = seed;
+  int best_slot_v = -1;
+  std::vector<int32_t> best_buf;
+  int v = std::max(first, 0);
+  while (v < n) {
+    const int count = std::min(W, n - v);
+    const int tb = 256;
+    k_clique_window<<<div_up((int64_t)count * 32, tb), tb, 0, st>>>(n, adj, words, ws.deg.get(), v, count, best,
+                                                                    ws.result.get(), ws.sets.get(),
+                                                                    ws.buffers.get(), buf_len);
+    RPGO_LAUNCHED();
+    ws.result.download(ws.h_result.data(), count, st);
+    RPGO_CUDA(cudaStreamSynchronize(st));
+    int improved = -1;
+    for (int s = 0; s < count; ++s)
+      if (ws.h_result[s] > best) {
+        improved = s;
+        break;
+      }
+    if (improved < 0) {
+      v += count;
+      continue;
+    }
+    best = ws.h_result[improved];
+    best_slot_v = v + improved;
+    best_buf.resize(best);
+    RPGO_CUDA(cudaMemcpyAsync(best_buf.data(), ws.buffers.get() + (size_t)improved * buf_len,
+                              sizeof(int32_t) * best, cudaMemcpyDeviceToHost, st));
+    RPGO_CUDA(cudaStreamSynchronize(st));
+    v = v + improved + 1;
+  }
+  (void)best_slot_v;
+  *clique = best_buf;
+  return best;
+}
+
+}  // namespace rpgo

@@ -1,0 +1,104 @@
+// Shared CUDA plumbing for the rpgo_gb300 library: error handling, device
+// buffers, launch accounting.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace rpgo {
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string& s) : std::runtime_error(s) {}
+};
+
+inline void cuda_check(cudaError_t e, const char* what, const char* file, int line) {
+  if (e != cudaSuccess) {
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s failed at %s:%d: %s", what, file, line, cudaGetErrorString(e));
+    throw CudaError(buf);
+  }
+}
+#define RPGO_CUDA(x) ::rpgo::cuda_check((x), #x, __FILE__, __LINE__)
+#define RPGO_LAUNCHED() ::rpgo::note_launch(cudaGetLastError(), __FILE__, __LINE__)
+
+// Count of kernels this library has launched (process-wide).
+std::atomic<int64_t>& launch_counter();
+inline void note_launch(cudaError_t e, const char* file, int line) {
+  cuda_check(e, "kernel launch", file, line);
+  launch_counter().fetch_add(1, std::memory_order_relaxed);
+}
+
+template <class T>
+class DeviceBuffer {
+ public:
+  DeviceBuffer() = default;
+  explicit DeviceBuffer(size_t n) { resize(n); }
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+  DeviceBuffer(DeviceBuffer&& o) noexcept : p_(o.p_), n_(o.n_), cap_(o.cap_) { o.p_ = nullptr; o.n_ = o.cap_ = 0; }
+  DeviceBuffer& operator=(DeviceBuffer&& o) noexcept {
+    if (this != &o) {
+      release();
+      p_ = o.p_; n_ = o.n_; cap_ = o.cap_;
+      o.p_ = nullptr; o.n_ = o.cap_ = 0;
+    }
+    return *this;
+  }
+  ~DeviceBuffer() { release(); }
+  // resize without preserving contents
+  void resize(size_t n) {
+    if (n > cap_) {
+      release();
+      size_t c = n < 16 ? 16 : n;
+      RPGO_CUDA(cudaMalloc(&p_, c * sizeof(T)));
+      cap_ = c;
+    }
+    n_ = n;
+  }
+  // grow keeping the first n_ elements (capacity doubles)
+  void grow(size_t n, cudaStream_t st) {
+    if (n > cap_) {
+      size_t c = cap_ ? cap_ : 16;
+      while (c < n) c *= 2;
+      T* q = nullptr;
+      RPGO_CUDA(cudaMalloc(&q, c * sizeof(T)));
+      if (p_ && n_) RPGO_CUDA(cudaMemcpyAsync(q, p_, n_ * sizeof(T), cudaMemcpyDeviceToDevice, st));
+      RPGO_CUDA(cudaStreamSynchronize(st));
+      release();
+      p_ = q;
+      cap_ = c;
+    }
+    n_ = n;
+  }
+  void upload(const T* h, size_t n, cudaStream_t st) {
+    resize(n);
+    if (n) RPGO_CUDA(cudaMemcpyAsync(p_, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
+  }
+  void upload(const std::vector<T>& h, cudaStream_t st) { upload(h.data(), h.size(), st); }
+  void download(T* h, size_t n, cudaStream_t st) const {
+    if (n) RPGO_CUDA(cudaMemcpyAsync(h, p_, n * sizeof(T), cudaMemcpyDeviceToHost, st));
+  }
+  void zero(cudaStream_t st) {
+    if (n_) RPGO_CUDA(cudaMemsetAsync(p_, 0, n_ * sizeof(T), st));
+  }
+  T* get() const { return p_; }
+  size_t size() const { return n_; }
+
+ private:
+  void release() {
+    if (p_) cudaFree(p_);
+    p_ = nullptr;
+    n_ = cap_ = 0;
+  }
+  T* p_ = nullptr;
+  size_t n_ = 0, cap_ = 0;
+};
+
+inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+}  // namespace rpgo

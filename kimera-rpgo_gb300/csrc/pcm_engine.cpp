@@ -1,0 +1,325 @@
+// Pcm<poseT, T>::removeOutliers and friends over device data; see
+// pcm_engine.hpp. Reference lines are cited per method.
+#include "pcm_engine.hpp"
+
+#include <algorithm>
+#include <cstring>
+#include <stdexcept>
+
+namespace rpgo {
+
+PcmEngine::PcmEngine(const PcmConfig& cfg, cudaStream_t st) : cfg_(cfg), st_(st) {
+  stride_ = cfg.dim == 3 ? 12 : 4;
+  d_ = cfg.dim == 3 ? 6 : 3;
+  // Pcm.h:74-82: a negative threshold disables the check
+  if (cfg.odom_threshold < 0 || cfg.odom_rot_threshold < 0 || cfg.odom_trans_threshold < 0) odom_check_ = false;
+  if (cfg.lc_threshold < 0 || cfg.dist_rot_threshold < 0 || cfg.dist_trans_threshold < 0) lc_check_ = false;
+}
+
+int32_t PcmEngine::slot(uint64_t key) {
+  auto it = slots_.find(key);
+  if (it != slots_.end()) return it->second;
+  const int32_t s = num_slots_++;
+  slots_.emplace(key, s);
+  pending_default_.push_back(s);
+  return s;
+}
+
+void PcmEngine::ensure_traj_capacity(size_t n) {
+  if (n <= traj_cap_) return;
+  size_t c = traj_cap_ ? traj_cap_ : 1024;
+  while (c < n) c *= 2;
+  const size_t old = traj_cap_;
+  auto grow = [&](auto& buf, size_t per) {
+    buf.grow(c * per, st_);
+    (void)old;
+  };
+  grow(traj_pose_, stride_);
+  grow(traj_cov_, (size_t)d_ * d_);
+  grow(traj_node_, 1);
+  grow(traj_rot_, 1);
+  traj_cap_ = c;
+}
+
+TrajView PcmEngine::view() const {
+  return TrajView{traj_pose_.get(), traj_cov_.get(), traj_node_.get(), traj_rot_.get()};
+}
+
+// std::map::operator[] default entries: identity pose, zero covariance,
+// node 0, rotation_info true (GeometryUtils.h:67-73, 203-206); the first pose
+// of a new robot prefix takes its value with zero covariance (Pcm.h:534-542).
+void PcmEngine::flush_slots() {
+  ensure_traj_capacity((size_t)num_slots_);
+  if (!pending_default_.empty()) {
+    const int32_t lo = *std::min_element(pending_default_.begin(), pending_default_.end());
+    const int32_t hi = *std::max_element(pending_default_.begin(), pending_default_.end()) + 1;
+    const size_t cnt = (size_t)(hi - lo);
+    std::vector<double> pose(cnt * stride_, 0.0), cov(cnt * d_ * d_, 0.0);
+    std::vector<int32_t> node(cnt, 0);
+    std::vector<uint8_t> rot(cnt, 1);
+    for (size_t i = 0; i < cnt; ++i) {
+      double* p = &pose[i * stride_];
+      if (cfg_.dim == 3) {
+        p[0] = p[4] = p[8] = 1.0;
+      } else {
+        p[0] = 1.0;
+      }
+    }
+    RPGO_CUDA(cudaMemcpyAsync(traj_pose_.get() + (size_t)lo * stride_, pose.data(), pose.size() * sizeof(double),
+                              cudaMemcpyHostToDevice, st_));
+    RPGO_CUDA(cudaMemcpyAsync(traj_cov_.get() + (size_t)lo * d_ * d_, cov.data(), cov.size() * sizeof(double),
+                              cudaMemcpyHostToDevice, st_));
+    RPGO_CUDA(cudaMemcpyAsync(traj_node_.get() + lo, node.data(), node.size() * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, st_));
+    RPGO_CUDA(cudaMemcpyAsync(traj_rot_.get() + lo, rot.data(), rot.size(), cudaMemcpyHostToDevice, st_));
+    RPGO_CUDA(cudaStreamSynchronize(st_));
+    pending_default_.clear();
+  }
+  for (auto& pi : pending_init_) {
+    const int32_t s = pi.first;
+    std::vector<double> cov((size_t)d_ * d_, 0.0);
+    int32_t node = 0;
+    uint8_t rot = 1;
+    RPGO_CUDA(cudaMemcpyAsync(traj_pose_.get() + (size_t)s * stride_, pi.second.data(), stride_ * sizeof(double),
+                              cudaMemcpyHostToDevice, st_));
+    RPGO_CUDA(cudaMemcpyAsync(traj_cov_.get() + (size_t)s * d_ * d_, cov.data(), cov.size() * sizeof(double),
+                              cudaMemcpyHostToDevice, st_));
+    RPGO_CUDA(cudaMemcpyAsync(traj_node_.get() + s, &node, sizeof(node), cudaMemcpyHostToDevice, st_));
+    RPGO_CUDA(cudaMemcpyAsync(traj_rot_.get() + s, &rot, 1, cudaMemcpyHostToDevice, st_));
+    RPGO_CUDA(cudaStreamSynchronize(st_));
+  }
+  pending_init_.clear();
+}
+
+void PcmEngine::run_pairwise(Group& g, int old_n) {
+  const int n = (int)g.factors.size();
+  if (n <= old_n) return;
+  // upload the new closures' records
+  g.sa.grow(n, st_);
+  g.sb.grow(n, st_);
+  g.flip.grow(n, st_);
+  g.zp.grow((size_t)n * stride_, st_);
+  g.zc.grow((size_t)n * d_ * d_, st_);
+  const int add = n - old_n;
+  RPGO_CUDA(cudaMemcpyAsync(g.sa.get() + old_n, g.h_sa.data() + old_n, add * sizeof(int32_t),
+                            cudaMemcpyHostToDevice, st_));
+  RPGO_CUDA(cudaMemcpyAsync(g.sb.get() + old_n, g.h_sb.data() + old_n, add * sizeof(int32_t),
+                            cudaMemcpyHostToDevice, st_));
+  RPGO_CUDA(cudaMemcpyAsync(g.flip.get() + old_n, g.h_flip.data() + old_n, add, cudaMemcpyHostToDevice, st_));
+  RPGO_CUDA(cudaMemcpyAsync(g.zp.get() + (size_t)old_n * stride_, g.h_zp.data() + (size_t)old_n * stride_,
+                            (size_t)add * stride_ * sizeof(double), cudaMemcpyHostToDevice, st_));
+  RPGO_CUDA(cudaMemcpyAsync(g.zc.get() + (size_t)old_n * d_ * d_, g.h_zc.data() + (size_t)old_n * d_ * d_,
+                            (size_t)add * d_ * d_ * sizeof(double), cudaMemcpyHostToDevice, st_));
+  // adjacency capacity: row_cap rows of row_cap/32 words, zero padded
+  if (n > g.row_cap) {
+    int cap = g.row_cap ? g.row_cap : 64;
+    while (cap < n) cap *= 2;
+    const int words = cap / 32;
+    DeviceBuffer<uint32_t> nb((size_t)cap * words);
+    nb.zero(st_);
+    if (g.n > 0)
+      RPGO_CUDA(cudaMemcpy2DAsync(nb.get(), (size_t)words * 4, g.adj.get(), (size_t)g.words * 4,
+                                  (size_t)g.words * 4, g.n, cudaMemcpyDeviceToDevice, st_));
+    g.adj = std::move(nb);
+    g.row_cap = cap;
+    g.words = words;
+  }
+  lower_scratch_.resize((size_t)(n - old_n) * g.words);
+  const double th0 = cfg_.mode == 0 ? cfg_.lc_threshold : cfg_.dist_trans_threshold;
+  const double th1 = cfg_.mode == 0 ? 0.0 : cfg_.dist_rot_threshold;
+  launch_pairwise(cfg_.dim, cfg_.mode, n, old_n, g.sa.get(), g.sb.get(), g.flip.get(), g.zp.get(), g.zc.get(),
+                  view(), th0, th1, g.adj.get(), g.words, lower_scratch_.get(), st_);
+  stats_.pair_checks += (int64_t)n * (n - 1) / 2 - (int64_t)old_n * (old_n - 1) / 2;
+  g.n = n;
+}
+
+// Pcm.h:851-899
+void PcmEngine::find_inliers() {
+  total_good_lc_ = 0;
+  for (auto& kv : groups_) {
+    Group& g = kv.second;
+    size_t num;
+    if (lc_check_) {
+      std::vector<int32_t> clique;
+      const int sz = max_clique_heu(g.n, g.adj.get(), g.words, 0, -1, &clique, clique_ws_, st_);
+      g.consistent.assign(clique.begin(), clique.begin() + std::max(sz, 0));
+      num = (size_t)std::max(sz, 0);
+    } else {
+      g.consistent.resize(g.factors.size());
+      for (size_t i = 0; i < g.factors.size(); ++i) g.consistent[i] = (int32_t)i;
+      num = g.factors.size();
+    }
+    total_good_lc_ += num;
+  }
+}
+
+// Pcm.h:906-970 with findMaxCliqueHeuIncremental (GraphUtils.cpp:30-44)
+void PcmEngine::find_inliers_incremental(const std::unordered_map<ObsId, size_t, ObsIdHash>& num_new) {
+  total_good_lc_ = 0;
+  for (const auto& kv : num_new) {
+    Group& g = groups_[kv.first];
+    const int prev = (int)g.consistent.size();
+    std::vector<int32_t> clique;
+    int sz;
+    if (lc_check_) {
+      const int first = g.n - (int)kv.second;
+      sz = max_clique_heu(g.n, g.adj.get(), g.words, first, prev, &clique, clique_ws_, st_);
+    } else {
+      // the adjacency stays the 1x1 zero matrix of a fresh Measurements
+      // (TypeUtils.h:16-33): only a first, lone closure can be taken
+      sz = prev;
+      if (kv.second == 1 && prev < 1) {
+        sz = 1;
+        clique.assign(1, 0);
+      }
+    }
+    if (sz > prev) g.consistent.assign(clique.begin(), clique.begin() + sz);
+  }
+  for (const auto& kv : groups_) total_good_lc_ += kv.second.consistent.size();
+}
+
+bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const std::set<uint64_t>& new_keys,
+                                const Values& values, std::vector<FactorRec>* out) {
+  if (new_factors.empty()) return false;
+  bool do_optimize = false;
+  // ---- classification (Pcm.h:164-240)
+  std::vector<int32_t> src, dst;
+  std::vector<double> dpose, dcov;
+  std::vector<const FactorRec*> lcs;
+  for (const auto& f : new_factors) {
+    if (f.kind == 0) {
+      if (f.k1 + 1 == f.k2 && new_keys.count(f.k2)) {
+        // updateOdom (Pcm.h:516-557)
+        nfg_odom_.push_back(f);
+        const char prefix = key_chr(f.k2);
+        if (!prefix_exists_.count(prefix)) {
+          prefix_exists_.insert(prefix);
+          const int32_t s0 = slot(f.k1);
+          pending_init_.emplace_back(s0, values.at(f.k1));
+        }
+        src.push_back(slot(f.k1));
+        dst.push_back(slot(f.k2));
+        dpose.insert(dpose.end(), f.meas, f.meas + stride_);
+        dcov.insert(dcov.end(), f.cov, f.cov + d_ * d_);
+      } else if (f.k1 != f.k2) {
+        lcs.push_back(&f);
+      }
+    } else {
+      nfg_special_.push_back(f);
+      do_optimize = true;
+    }
+  }
+  if (!src.empty()) {
+    flush_slots();
+    d_src_.upload(src, st_);
+    d_dst_.upload(dst, st_);
+    d_dpose_.upload(dpose, st_);
+    d_dcov_.upload(dcov, st_);
+    launch_traj_scan(cfg_.dim, cfg_.mode, (int64_t)src.size(), d_src_.get(), d_dst_.get(), d_dpose_.get(),
+                     d_dcov_.get(), view(), scratch_rec_, scratch_cov_, scratch_rot_, st_);
+  }
+  if (!lcs.empty()) {
+    // ---- odometry consistency of intra-robot closures (Pcm.h:455-465, 604-629)
+    std::vector<int32_t> ci, cj, owner;
+    std::vector<double> zp, zc;
+    for (size_t k = 0; k < lcs.size(); ++k) {
+      const FactorRec& f = *lcs[k];
+      if (!values.count(f.k1) || !values.count(f.k2)) continue;
+      if (key_chr(f.k1) != key_chr(f.k2) || !odom_check_) continue;
+      prefix_exists_.insert(key_chr(f.k1));
+      ci.push_back(slot(f.k1));
+      cj.push_back(slot(f.k2));
+      owner.push_back((int32_t)k);
+      zp.insert(zp.end(), f.meas, f.meas + stride_);
+      zc.insert(zc.end(), f.cov, f.cov + d_ * d_);
+    }
+    std::vector<uint8_t> passed(lcs.size(), 1);
+    if (!ci.empty()) {
+      flush_slots();
+      DeviceBuffer<int32_t> di, dj;
+      DeviceBuffer<double> dzp, dzc;
+      di.upload(ci, st_);
+      dj.upload(cj, st_);
+      dzp.upload(zp, st_);
+      dzc.upload(zc, st_);
+      d_ok_.resize(ci.size());
+      const double th0 = cfg_.mode == 0 ? cfg_.odom_threshold : cfg_.odom_trans_threshold;
+      const double th1 = cfg_.mode == 0 ? 0.0 : cfg_.odom_rot_threshold;
+      launch_odom_check(cfg_.dim, cfg_.mode, (int64_t)ci.size(), di.get(), dj.get(), dzp.get(), dzc.get(), view(),
+                        th0, th1, d_ok_.get(), st_);
+      std::vector<uint8_t> ok(ci.size());
+      d_ok_.download(ok.data(), ok.size(), st_);
+      RPGO_CUDA(cudaStreamSynchronize(st_));
+      for (size_t q = 0; q < ci.size(); ++q) passed[owner[q]] = ok[q];
+      stats_.odom_checks += (int64_t)ci.size();
+    }
+    // ---- grouping (Pcm.h:466-486)
+    std::unordered_map<ObsId, size_t, ObsIdHash> num_new;
+    std::vector<std::pair<ObsId, int>> touched;
+    for (size_t k = 0; k < lcs.size(); ++k) {
+      const FactorRec& f = *lcs[k];
+      if (!values.count(f.k1) || !values.count(f.k2)) continue;
+      if (!passed[k]) continue;
+      const ObsId id{key_chr(f.k1), key_chr(f.k2)};
+      num_new[id]++;
+      auto it = groups_.find(id);
+      if (it == groups_.end()) {
+        it = groups_.emplace(id, Group()).first;
+        it->second.key = id;
+      }
+      Group& g = it->second;
+      bool seen = false;
+      for (auto& t : touched)
+        if (t.first == id) seen = true;
+      if (!seen) touched.emplace_back(id, (int)g.factors.size());
+      g.factors.push_back(f);
+      g.h_sa.push_back(slot(f.k1));
+      g.h_sb.push_back(slot(f.k2));
+      g.h_flip.push_back(key_chr(f.k1) != g.key.id1 ? 1 : 0);
+      g.h_zp.insert(g.h_zp.end(), f.meas, f.meas + stride_);
+      g.h_zc.insert(g.h_zc.end(), f.cov, f.cov + d_ * d_);
+      ++total_lc_;
+    }
+    if (lc_check_) {
+      flush_slots();
+      for (auto& t : touched) {
+        Group& g = groups_[t.first];
+        if (g.factors.size() >= 2) {
+          // areLoopsConsistent reads both robots' trajectories (Pcm.h:699-710)
+          prefix_exists_.insert(g.key.id1);
+          prefix_exists_.insert(g.key.id2);
+        }
+        run_pairwise(g, t.second);
+      }
+    }
+    if (cfg_.incremental) find_inliers_incremental(num_new);
+    else find_inliers();
+    do_optimize = true;
+  }
+  // ---- buildGraphToOptimize (Pcm.h:977-1005)
+  out->clear();
+  out->insert(out->end(), nfg_odom_.begin(), nfg_odom_.end());
+  out->insert(out->end(), nfg_special_.begin(), nfg_special_.end());
+  for (const auto& kv : groups_)
+    for (int32_t idx : kv.second.consistent) out->push_back(kv.second.factors[idx]);
+  return do_optimize;
+}
+
+bool PcmEngine::adjacency(int gi, std::vector<uint32_t>* words, int* n) const {
+  int k = 0;
+  for (const auto& kv : groups_) {
+    if (k++ != gi) continue;
+    const Group& g = kv.second;
+    *n = g.n;
+    const int w = (g.n + 31) / 32;
+    words->assign((size_t)g.n * w, 0u);
+    if (g.n == 0) return true;
+    RPGO_CUDA(cudaMemcpy2DAsync(words->data(), (size_t)w * 4, g.adj.get(), (size_t)g.words * 4, (size_t)w * 4, g.n,
+                                cudaMemcpyDeviceToHost, st_));
+    RPGO_CUDA(cudaStreamSynchronize(st_));
+    return true;
+  }
+  return false;
+}
+
+}  // namespace rpgo

@@ -1,0 +1,126 @@
+// Host side of PCM outlier rejection: the Pcm<poseT, T> plugin
+// (include/KimeraRPGO/outlier/Pcm.h) driving the device kernels.
+//
+// Bookkeeping stays on the host exactly as the reference keeps it (factor
+// classification, groups keyed by ObservationId in a std::unordered_map with
+// the reference's hash so that groups are visited in the same order, the
+// prefix-trajectory side effects of std::map::operator[]); the trajectories,
+// the odometry check, the pairwise test, the adjacency and the clique run on
+// the GPU.
+#pragma once
+#include <cstdint>
+#include <functional>
+#include <map>
+#include <set>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#include "pcm_kernels.hpp"
+
+namespace rpgo {
+
+struct FactorRec {
+  int32_t kind = 0;  // 0 between, 1 prior
+  uint64_t k1 = 0, k2 = 0;
+  double meas[12] = {0};
+  double cov[36] = {0};
+  double sqrt_info[36] = {0};
+};
+
+using Values = std::map<uint64_t, std::vector<double>>;
+
+inline char key_chr(uint64_t k) { return static_cast<char>(static_cast<unsigned char>(k >> 56)); }
+
+// ObservationId (TypeUtils.h:44-58) and its hash (TypeUtils.h:80-88)
+struct ObsId {
+  char id1, id2;
+  bool operator==(const ObsId& o) const {
+    return (id1 == o.id1 && id2 == o.id2) || (id2 == o.id1 && id1 == o.id2);
+  }
+};
+struct ObsIdHash {
+  size_t operator()(const ObsId& id) const {
+    std::hash<char> h;
+    return h(id.id1) + h(id.id2) + h(id.id1) * h(id.id2);
+  }
+};
+
+struct PcmConfig {
+  int dim = 3;   // 2 or 3
+  int mode = 0;  // 0 Pcm (PoseWithCovariance), 1 PcmSimple (PoseWithNode)
+  double odom_threshold = 10.0, lc_threshold = 5.0;
+  double odom_trans_threshold = 0.05, odom_rot_threshold = 0.005;
+  double dist_trans_threshold = 0.01, dist_rot_threshold = 0.001;
+  bool incremental = false;
+};
+
+struct PcmStats {
+  int64_t pair_checks = 0;
+  int64_t odom_checks = 0;
+};
+
+class PcmEngine {
+ public:
+  PcmEngine(const PcmConfig& cfg, cudaStream_t st);
+  // Pcm::removeOutliers. `values` already holds new_values. Returns
+  // do_optimize; *out is the graph to optimise (odometry, special, inliers).
+  bool remove_outliers(const std::vector<FactorRec>& new_factors, const std::set<uint64_t>& new_keys,
+                       const Values& values, std::vector<FactorRec>* out);
+
+  size_t num_lc() const { return total_lc_; }
+  size_t num_lc_inliers() const { return total_good_lc_; }
+  size_t num_odom() const { return nfg_odom_.size(); }
+  size_t num_special() const { return nfg_special_.size(); }
+  // adjacency of the g-th group in visiting order (host copy, n x words)
+  bool adjacency(int g, std::vector<uint32_t>* words, int* n) const;
+  const PcmStats& stats() const { return stats_; }
+
+ private:
+  struct Group {
+    std::vector<FactorRec> factors;
+    std::vector<int32_t> consistent;  // indices into factors (clique buffer order, duplicates kept)
+    int n = 0, words = 0, row_cap = 0;
+    DeviceBuffer<uint32_t> adj;  // row_cap x words
+    std::vector<int32_t> h_sa, h_sb;
+    std::vector<uint8_t> h_flip;
+    std::vector<double> h_zp, h_zc;
+    DeviceBuffer<int32_t> sa, sb;
+    DeviceBuffer<uint8_t> flip;
+    DeviceBuffer<double> zp, zc;
+    ObsId key{0, 0};
+  };
+  int32_t slot(uint64_t key);  // trajectory slot, default-initialised when new
+  void flush_slots();          // upload defaults / initial poses of new slots
+  void ensure_traj_capacity(size_t n);
+  TrajView view() const;
+  void run_pairwise(Group& g, int old_n);
+  void find_inliers();
+  void find_inliers_incremental(const std::unordered_map<ObsId, size_t, ObsIdHash>& num_new);
+
+  PcmConfig cfg_;
+  bool odom_check_ = true, lc_check_ = true;
+  cudaStream_t st_;
+  int stride_, d_;
+  std::unordered_map<uint64_t, int32_t> slots_;
+  int32_t num_slots_ = 0;
+  size_t traj_cap_ = 0;
+  std::vector<std::pair<int32_t, std::vector<double>>> pending_init_;  // slot -> pose (cov zero)
+  std::vector<int32_t> pending_default_;
+  DeviceBuffer<double> traj_pose_, traj_cov_;
+  DeviceBuffer<int32_t> traj_node_;
+  DeviceBuffer<uint8_t> traj_rot_;
+  std::unordered_set<char> prefix_exists_;
+  std::vector<FactorRec> nfg_odom_, nfg_special_;
+  std::unordered_map<ObsId, Group, ObsIdHash> groups_;
+  size_t total_lc_ = 0, total_good_lc_ = 0;
+  // scratch
+  DeviceBuffer<int32_t> d_src_, d_dst_;
+  DeviceBuffer<double> d_dpose_, d_dcov_, scratch_rec_, scratch_cov_;
+  DeviceBuffer<uint8_t> scratch_rot_, d_ok_;
+  DeviceBuffer<uint32_t> lower_scratch_;
+  CliqueWorkspace clique_ws_;
+  PcmStats stats_;
+};
+
+}  // namespace rpgo

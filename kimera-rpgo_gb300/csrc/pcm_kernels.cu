@@ -1,0 +1,549 @@
+// PCM outlier-rejection kernels (sm_103a).
+//
+//  K0 trajectory scan   Pcm::updateOdom (Pcm.h:516-557): the odometry chain
+//                       T_k = T_{k-1} o Delta_k with the covariance
+//                       Ad(Delta^-1) S Ad(Delta^-1)^T + S_Delta, sequential in
+//                       factor order (one warp; lanes split each 6x6 update).
+//  K1 odometry check    Pcm::isOdomConsistent / checkOdomConsistent
+//                       (Pcm.h:564-629), one thread per loop closure.
+//  K2 pairwise check    Pcm::areLoopsConsistent / checkLoopConsistent /
+//                       incrementAdjMatrix (Pcm.h:638-768): one thread per
+//                       closure pair (i < j), 32 consecutive i per warp, the
+//                       verdicts packed into 32-bit adjacency words with one
+//                       warp ballot; a second kernel mirrors the lower
+//                       triangle into the upper one with warp bit transposes.
+// All arithmetic is the exact FP64 sequence of pcm_math.cuh.
+#include "pcm_kernels.hpp"
+#include "pcm_math.cuh"
+
+namespace rpgo {
+namespace {
+
+using namespace pm;
+
+// ------------------------------------------------------------------ uncertain poses
+template <int DIM>
+struct Lie;
+template <>
+struct Lie<3> {
+  using Pose = P3;
+  static constexpr int d = 6, rd = 3, td = 3, stride = 12;
+  __device__ static void load(const double* s, Pose& p) { p3_load(s, p); }
+  __device__ static void store(const Pose& p, double* s) { p3_store(p, s); }
+  __device__ static void compose(const Pose& a, const Pose& b, Pose& c) { p3_compose(a, b, c); }
+  __device__ static void inverse(const Pose& a, Pose& c) { p3_inverse(a, c); }
+  __device__ static void between(const Pose& a, const Pose& b, Pose& c) { p3_between(a, b, c); }
+  __device__ static void congruence(const Pose& T, const double* S, double* C) { p3_congruence(T, S, C); }
+  __device__ static void logmap(const Pose& T, double* xi) { p3_logmap(T, xi); }
+  __device__ static double rot_trace(const double* c) { return add(add(c[0], c[7]), c[14]); }
+};
+template <>
+struct Lie<2> {
+  using Pose = P2;
+  static constexpr int d = 3, rd = 1, td = 2, stride = 4;
+  __device__ static void load(const double* s, Pose& p) { p2_load(s, p); }
+  __device__ static void store(const Pose& p, double* s) { p2_store(p, s); }
+  __device__ static void compose(const Pose& a, const Pose& b, Pose& c) { p2_compose(a, b, c); }
+  __device__ static void inverse(const Pose& a, Pose& c) { p2_inverse(a, c); }
+  __device__ static void between(const Pose& a, const Pose& b, Pose& c) { p2_between(a, b, c); }
+  __device__ static void congruence(const Pose& T, const double* S, double* C) { p2_congruence(T, S, C); }
+  __device__ static void logmap(const Pose& T, double* xi) { p2_logmap(T, xi); }
+  __device__ static double rot_trace(const double* c) { return c[0]; }
+};
+
+// PoseWithCovariance (GeometryUtils.h:56-187)
+template <int DIM>
+struct PWC {
+  using L = Lie<DIM>;
+  static constexpr int d = L::d;
+  typename L::Pose pose;
+  double cov[d * d];
+  bool rot;
+
+  __device__ void from_factor(const double* zp, const double* zc) {
+    L::load(zp, pose);
+    rot = !isnan(L::rot_trace(zc));
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+#pragma unroll
+      for (int j = 0; j < d; ++j) cov[d * i + j] = (rot || (i >= L::rd && j >= L::rd)) ? zc[d * i + j] : 0.0;
+  }
+  __device__ void from_traj(const TrajView& t, int s) {
+    L::load(t.pose + (size_t)s * L::stride, pose);
+#pragma unroll
+    for (int i = 0; i < d * d; ++i) cov[i] = t.cov[(size_t)s * d * d + i];
+    rot = t.rot[s] != 0;
+  }
+  // this o other (GeometryUtils.h:119-129)
+  __device__ void compose(const PWC& other, PWC& out) const {
+    typename L::Pose inv;
+    L::compose(pose, other.pose, out.pose);
+    L::inverse(other.pose, inv);
+    double C[d * d];
+    L::congruence(inv, cov, C);
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+#pragma unroll
+      for (int j = 0; j <= i; ++j) {
+        const double v = add(C[d * i + j], other.cov[d * i + j]);
+        out.cov[d * i + j] = v;
+        out.cov[d * j + i] = v;
+      }
+    out.rot = rot && other.rot;
+  }
+  // GeometryUtils.h:133-139
+  __device__ void inverse_inplace() {
+    typename L::Pose p;
+    L::inverse(pose, p);
+    pose = p;
+  }
+  // this^-1 o other with the LLT fallback (GeometryUtils.h:143-170)
+  __device__ void between(const PWC& other, PWC& out) const {
+    typename L::Pose res, inv;
+    L::between(pose, other.pose, res);
+    L::inverse(res, inv);
+    double C[d * d];
+    L::congruence(inv, cov, C);
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+#pragma unroll
+      for (int j = 0; j <= i; ++j) {
+        const double v = sub(other.cov[d * i + j], C[d * i + j]);
+        out.cov[d * i + j] = v;
+        out.cov[d * j + i] = v;
+      }
+    if (!chol_ok<d>(out.cov)) {
+      typename L::Pose res2, inv2;
+      L::between(other.pose, pose, res2);
+      L::inverse(res2, inv2);
+      L::congruence(inv2, other.cov, C);
+#pragma unroll
+      for (int i = 0; i < d; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j) {
+          const double v = sub(cov[d * i + j], C[d * i + j]);
+          out.cov[d * i + j] = v;
+          out.cov[d * j + i] = v;
+        }
+    }
+    out.pose = res;
+    out.rot = rot && other.rot;
+  }
+  __device__ double mahalanobis() const {
+    double xi[d];
+    L::logmap(pose, xi);
+    if (!rot) {
+      constexpr int m = L::td, r = L::rd;
+      double B[m * m];
+#pragma unroll
+      for (int i = 0; i < m; ++i)
+#pragma unroll
+        for (int j = 0; j < m; ++j) B[m * i + j] = cov[d * (r + i) + (r + j)];
+      return sqrtd(quad_inv<m>(B, xi + r));
+    }
+    return sqrtd(quad_inv<d>(cov, xi));
+  }
+};
+
+// PoseWithNode (GeometryUtils.h:193-289)
+template <int DIM>
+struct PWN {
+  using L = Lie<DIM>;
+  static constexpr int d = L::d;
+  typename L::Pose pose;
+  int node;
+  bool rot;
+  __device__ void from_factor(const double* zp, const double* zc) {
+    L::load(zp, pose);
+    rot = !isnan(L::rot_trace(zc));
+    node = 1;
+  }
+  __device__ void from_traj(const TrajView& t, int s) {
+    L::load(t.pose + (size_t)s * L::stride, pose);
+    node = t.node[s];
+    rot = t.rot[s] != 0;
+  }
+  __device__ void compose(const PWN& o, PWN& out) const {
+    L::compose(pose, o.pose, out.pose);
+    out.node = node + o.node;
+    out.rot = rot && o.rot;
+  }
+  __device__ void inverse_inplace() {
+    typename L::Pose p;
+    L::inverse(pose, p);
+    pose = p;
+  }
+  __device__ void between(const PWN& o, PWN& out) const {
+    L::between(pose, o.pose, out.pose);
+    out.node = abs(o.node - node);
+    out.rot = rot && o.rot;
+  }
+  __device__ static double norm_slice(const double* v, int m) {
+    double acc = mul(v[0], v[0]);
+    for (int i = 1; i < m; ++i) acc = fmad(v[i], v[i], acc);
+    return sqrtd(acc);
+  }
+  __device__ void norms(double& trans, double& rotn) const {
+    double xi[d];
+    L::logmap(pose, xi);
+    trans = dvd(norm_slice(xi + L::rd, L::td), (double)node);
+    rotn = rot ? dvd(norm_slice(xi, L::rd), (double)node) : 0.0;
+  }
+};
+
+template <class U>
+__device__ __forceinline__ bool check_mahal(const U& u, double th0, double) {
+  return u.mahalanobis() < th0;
+}
+template <int DIM>
+__device__ __forceinline__ bool check_u(const PWC<DIM>& u, double th0, double) {
+  return u.mahalanobis() < th0;
+}
+template <int DIM>
+__device__ __forceinline__ bool check_u(const PWN<DIM>& u, double th0, double th1) {
+  double t, r;
+  u.norms(t, r);
+  return t < th0 && r < th1;
+}
+
+// ------------------------------------------------------------------ K0
+// Exact per-element pieces of PWC::compose for one lane.
+__device__ __forceinline__ double p3_compose_elem(const double* A, const double* B, int e) {
+  // A, B: 12-double pose records (R row-major, t)
+  if (e < 9) {
+    const int i = e / 3, j = e % 3;
+    return dot3e(A[3 * i], A[3 * i + 1], A[3 * i + 2], B[j], B[3 + j], B[6 + j]);
+  }
+  const int i = e - 9;
+  double acc = fmad(A[3 * i], B[9], A[9 + i]);
+  acc = fmad(A[3 * i + 1], B[10], acc);
+  return fmad(A[3 * i + 2], B[11], acc);
+}
+__device__ __forceinline__ double p2_compose_elem(const double* A, const double* B, int e) {
+  // (c, s, x, y)
+  switch (e) {
+    case 0: return fmad(A[0], B[0], -mul(A[1], B[1]));
+    case 1: return fmad(A[1], B[0], mul(A[0], B[1]));
+    case 2: return add(A[2], fmad(A[0], B[2], -mul(A[1], B[3])));
+    default: return add(A[3], fmad(A[1], B[2], mul(A[0], B[3])));
+  }
+}
+
+// Per-odometry-factor constants: the measurement as an uncertain pose
+// (GeometryUtils.h:91-115) and the pieces of Ad(Delta^-1).
+template <int DIM>
+__global__ void k_odom_prep(int64_t count, const double* __restrict__ dpose, const double* __restrict__ dcov,
+                            double* __restrict__ inv_rec, double* __restrict__ cov_out, uint8_t* __restrict__ rot_out) {
+  using L = Lie<DIM>;
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  PWC<DIM> z;
+  z.from_factor(dpose + k * L::stride, dcov + k * L::d * L::d);
+  for (int i = 0; i < L::d * L::d; ++i) cov_out[k * L::d * L::d + i] = z.cov[i];
+  rot_out[k] = z.rot ? 1 : 0;
+  typename L::Pose inv;
+  L::inverse(z.pose, inv);
+  if constexpr (DIM == 3) {
+    double K[9];
+    p3_adjoint_K(inv, K);
+    double* r = inv_rec + k * 21;
+    for (int i = 0; i < 9; ++i) r[i] = inv.R[i];
+    for (int i = 0; i < 9; ++i) r[9 + i] = K[i];
+    for (int i = 0; i < 3; ++i) r[18 + i] = inv.t[i];
+  } else {
+    double A[9];
+    p2_adjoint(inv, A);
+    double* r = inv_rec + k * 9;
+    for (int i = 0; i < 9; ++i) r[i] = A[i];
+  }
+}
+
+// One warp walks the odometry list in order.
+template <int DIM, int MODE>
+__global__ void __launch_bounds__(32) k_traj_scan(int64_t count, const int32_t* __restrict__ src,
+                                                  const int32_t* __restrict__ dst, const double* __restrict__ dpose,
+                                                  const double* __restrict__ inv_rec,
+                                                  const double* __restrict__ dcov_p,
+                                                  const uint8_t* __restrict__ drot, TrajView tr) {
+  using L = Lie<DIM>;
+  constexpr int d = L::d, st = L::stride, dd = d * d;
+  constexpr int REC = (DIM == 3) ? 21 : 9;
+  __shared__ double prev_pose[12], prev_cov[36], M[36], newp[12], rec[21], dpz[12], dc[36];
+  __shared__ int prev_node;
+  __shared__ uint8_t prev_rot;
+  const int lane = threadIdx.x;
+  int32_t last_dst = -1;
+  for (int64_t k = 0; k < count; ++k) {
+    const int32_t s = src[k], t = dst[k];
+    // load previous state (unless it is the pose just written) and the step constants
+    if (s != last_dst) {
+      for (int e = lane; e < st; e += 32) prev_pose[e] = tr.pose[(size_t)s * st + e];
+      if (MODE == 0)
+        for (int e = lane; e < dd; e += 32) prev_cov[e] = tr.cov[(size_t)s * dd + e];
+      if (lane == 0) {
+        prev_rot = tr.rot[s];
+        if (MODE == 1) prev_node = tr.node[s];
+      }
+    }
+    for (int e = lane; e < st; e += 32) dpz[e] = dpose[k * st + e];
+    if (MODE == 0) {
+      for (int e = lane; e < REC; e += 32) rec[e] = inv_rec[k * REC + e];
+      for (int e = lane; e < dd; e += 32) dc[e] = dcov_p[k * dd + e];
+    }
+    __syncwarp();
+    // phase 1: M = Ad(Delta^-1) S_prev (items [0, dd)) and the new pose
+    {
+      constexpr int nm = (MODE == 0) ? dd : 0;
+      for (int e = lane; e < nm + st; e += 32) {
+        if (e < nm) {
+          const int i = e / d, kk = e % d;
+          if constexpr (DIM == 3) M[e] = p3_M_elem(rec, rec + 9, prev_cov, i, kk);
+          else M[e] = p2_M_elem(rec, prev_cov, i, kk);
+        } else {
+          const int pl = e - nm;
+          if constexpr (DIM == 3) newp[pl] = p3_compose_elem(prev_pose, dpz, pl);
+          else newp[pl] = p2_compose_elem(prev_pose, dpz, pl);
+        }
+      }
+    }
+    __syncwarp();
+    // phase 2: lower triangle of M Ad^T + S_Delta
+    if (MODE == 0) {
+      constexpr int ntri = d * (d + 1) / 2;
+      double v = 0.0;
+      int ii = 0, jj = 0;
+      if (lane < ntri) {
+        int idx = lane;
+        ii = 0;
+        while (idx > ii) { idx -= ii + 1; ++ii; }
+        jj = idx;
+        double c;
+        if constexpr (DIM == 3) c = p3_C_elem(rec, rec + 9, M + 6 * ii, jj);
+        else c = p2_C_elem(rec, M + 3 * ii, jj);
+        v = add(c, dc[d * ii + jj]);
+      }
+      __syncwarp();
+      if (lane < ntri) {
+        prev_cov[d * ii + jj] = v;
+        prev_cov[d * jj + ii] = v;
+      }
+    }
+    for (int e = lane; e < st; e += 32) prev_pose[e] = newp[e];
+    if (lane == 0) {
+      prev_rot = (prev_rot && (MODE == 0 ? drot[k] : drot[k])) ? 1 : 0;
+      if (MODE == 1) prev_node = prev_node + 1;
+    }
+    __syncwarp();
+    for (int e = lane; e < st; e += 32) tr.pose[(size_t)t * st + e] = prev_pose[e];
+    if (MODE == 0)
+      for (int e = lane; e < dd; e += 32) tr.cov[(size_t)t * dd + e] = prev_cov[e];
+    if (lane == 0) {
+      tr.rot[t] = prev_rot;
+      if (MODE == 1) tr.node[t] = prev_node;
+    }
+    last_dst = t;
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------ K1
+template <int DIM, class U>
+__global__ void k_odom_check(int64_t count, const int32_t* __restrict__ si, const int32_t* __restrict__ sj,
+                             const double* __restrict__ zp, const double* __restrict__ zc, TrajView tr, double th0,
+                             double th1, uint8_t* __restrict__ ok) {
+  using L = Lie<DIM>;
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  U a, b, pij, z, res;
+  a.from_traj(tr, si[k]);
+  b.from_traj(tr, sj[k]);
+  a.between(b, pij);
+  z.from_factor(zp + k * L::stride, zc + k * L::d * L::d);
+  z.inverse_inplace();
+  pij.compose(z, res);
+  ok[k] = check_u<DIM>(res, th0, th1) ? 1 : 0;
+}
+
+// ------------------------------------------------------------------ K2
+template <int DIM, class U>
+__device__ __forceinline__ bool pair_consistent(int i, int j, const int32_t* __restrict__ sa,
+                                                const int32_t* __restrict__ sb, const uint8_t* __restrict__ flip,
+                                                const double* __restrict__ zp, const double* __restrict__ zc,
+                                                const TrajView& tr, double th0, double th1) {
+  using L = Lie<DIM>;
+  int a = sa[i], b = sb[i], c = sa[j], dd = sb[j];
+  if (flip[i] != flip[j]) {
+    const int t = c;
+    c = dd;
+    dd = t;
+  }
+  U A, B, Ta, Tc, Zj, Zi, P, Q, loop;
+  Ta.from_traj(tr, a);
+  Tc.from_traj(tr, c);
+  Ta.between(Tc, A);
+  Ta.from_traj(tr, b);
+  Tc.from_traj(tr, dd);
+  Ta.between(Tc, B);
+  Zj.from_factor(zp + (size_t)j * L::stride, zc + (size_t)j * L::d * L::d);
+  A.compose(Zj, P);
+  P.inverse_inplace();
+  Zi.from_factor(zp + (size_t)i * L::stride, zc + (size_t)i * L::d * L::d);
+  P.compose(Zi, Q);
+  Q.compose(B, loop);
+  return check_u<DIM>(loop, th0, th1);
+}
+
+// block (32, ROWS): lane -> column i = 32*bx + lane, row j = row_begin + ROWS*by + ty.
+// lower[(j - row_begin) * words + bx] receives bits i < j.
+template <int DIM, class U, int ROWS>
+__global__ void __launch_bounds__(32 * ROWS) k_pairwise(int n, int row_begin, const int32_t* __restrict__ sa,
+                                                        const int32_t* __restrict__ sb,
+                                                        const uint8_t* __restrict__ flip,
+                                                        const double* __restrict__ zp,
+                                                        const double* __restrict__ zc, TrajView tr, double th0,
+                                                        double th1, uint32_t* __restrict__ lower, int words) {
+  const int lane = threadIdx.x;
+  const int j = row_begin + ROWS * blockIdx.y + threadIdx.y;
+  const int i0 = 32 * blockIdx.x;
+  if (j >= n || i0 >= j) return;  // whole warp: tile above the diagonal or past the end
+  const int i = i0 + lane;
+  bool ok = false;
+  if (i < j) ok = pair_consistent<DIM, U>(i, j, sa, sb, flip, zp, zc, tr, th0, th1);
+  const unsigned bits = __ballot_sync(0xffffffffu, ok);
+  if (lane == 0) lower[(size_t)(j - row_begin) * words + blockIdx.x] = bits;
+}
+
+// Mirror: adj[r][c] for c < r from lower rows (r >= row_begin) or the old
+// matrix (r < row_begin); for c > r from lower[c][r] (c >= row_begin) or the
+// old matrix. One warp per 32x32 block, lane = row within the block.
+__global__ void k_symmetrize(int n, int row_begin, const uint32_t* __restrict__ lower, uint32_t* __restrict__ adj,
+                             int words) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nb = (n + 31) / 32;
+  if (warp >= nb * nb) return;
+  const int bi = warp / nb, bj = warp % nb;
+  const int r = 32 * bi + lane;
+  // transpose source: word (rows c = 32*bj + lane) column block bi of lower
+  const int c_src = 32 * bj + lane;
+  uint32_t src = 0;
+  if (c_src < n && c_src >= row_begin) src = lower[(size_t)(c_src - row_begin) * words + bi];
+  uint32_t tr_word = 0;
+#pragma unroll 4
+  for (int b = 0; b < 32; ++b) {
+    const uint32_t col = __ballot_sync(0xffffffffu, (src >> b) & 1u);
+    if (b == lane) tr_word = col;  // bits over c of row 32*bi + b
+  }
+  if (r >= n) return;
+  const uint32_t old = (r < row_begin) ? adj[(size_t)r * words + bj] : 0u;
+  uint32_t out = 0;
+  // column mask helpers within block bj
+  const int c0 = 32 * bj;
+  uint32_t lt = 0, gt = 0, valid = 0;
+  for (int b = 0; b < 32; ++b) {
+    const int c = c0 + b;
+    if (c >= n) break;
+    valid |= 1u << b;
+    if (c < r) lt |= 1u << b;
+    if (c > r) gt |= 1u << b;
+  }
+  // lower part
+  if (r >= row_begin) out |= lower[(size_t)(r - row_begin) * words + bj] & lt;
+  else out |= old & lt;
+  // upper part: new columns from the transpose, old columns from the old matrix
+  uint32_t newcols = 0;
+  for (int b = 0; b < 32; ++b)
+    if (c0 + b >= row_begin && c0 + b < n) newcols |= 1u << b;
+  out |= tr_word & gt & newcols;
+  out |= old & gt & ~newcols;
+  adj[(size_t)r * words + bj] = out & valid;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+void launch_traj_scan(int dim, int mode, int64_t count, const int32_t* src, const int32_t* dst,
+                      const double* dpose, const double* dcov, TrajView tr, DeviceBuffer<double>& scratch_rec,
+                      DeviceBuffer<double>& scratch_cov, DeviceBuffer<uint8_t>& scratch_rot, cudaStream_t st) {
+  if (count <= 0) return;
+  const int d = dim == 3 ? 6 : 3;
+  scratch_rec.resize((size_t)count * (dim == 3 ? 21 : 9));
+  scratch_cov.resize((size_t)count * d * d);
+  scratch_rot.resize((size_t)count);
+  const int tb = 128;
+  if (dim == 3) k_odom_prep<3><<<div_up(count, tb), tb, 0, st>>>(count, dpose, dcov, scratch_rec.get(),
+                                                                   scratch_cov.get(), scratch_rot.get());
+  else k_odom_prep<2><<<div_up(count, tb), tb, 0, st>>>(count, dpose, dcov, scratch_rec.get(), scratch_cov.get(),
+                                                        scratch_rot.get());
+  RPGO_LAUNCHED();
+  if (dim == 3) {
+    if (mode == 0) k_traj_scan<3, 0><<<1, 32, 0, st>>>(count, src, dst, dpose, scratch_rec.get(), scratch_cov.get(),
+                                                       scratch_rot.get(), tr);
+    else k_traj_scan<3, 1><<<1, 32, 0, st>>>(count, src, dst, dpose, scratch_rec.get(), scratch_cov.get(),
+                                             scratch_rot.get(), tr);
+  } else {
+    if (mode == 0) k_traj_scan<2, 0><<<1, 32, 0, st>>>(count, src, dst, dpose, scratch_rec.get(), scratch_cov.get(),
+                                                       scratch_rot.get(), tr);
+    else k_traj_scan<2, 1><<<1, 32, 0, st>>>(count, src, dst, dpose, scratch_rec.get(), scratch_cov.get(),
+                                             scratch_rot.get(), tr);
+  }
+  RPGO_LAUNCHED();
+}
+
+void launch_odom_check(int dim, int mode, int64_t count, const int32_t* si, const int32_t* sj, const double* zp,
+                       const double* zc, TrajView tr, double th0, double th1, uint8_t* ok, cudaStream_t st) {
+  if (count <= 0) return;
+  const int tb = 64;
+  const int g = div_up(count, tb);
+  if (dim == 3) {
+    if (mode == 0) k_odom_check<3, PWC<3>><<<g, tb, 0, st>>>(count, si, sj, zp, zc, tr, th0, th1, ok);
+    else k_odom_check<3, PWN<3>><<<g, tb, 0, st>>>(count, si, sj, zp, zc, tr, th0, th1, ok);
+  } else {
+    if (mode == 0) k_odom_check<2, PWC<2>><<<g, tb, 0, st>>>(count, si, sj, zp, zc, tr, th0, th1, ok);
+    else k_odom_check<2, PWN<2>><<<g, tb, 0, st>>>(count, si, sj, zp, zc, tr, th0, th1, ok);
+  }
+  RPGO_LAUNCHED();
+}
+
+void launch_pairwise(int dim, int mode, int n, int row_begin, const int32_t* sa, const int32_t* sb,
+                     const uint8_t* flip, const double* zp, const double* zc, TrajView tr, double th0, double th1,
+                     uint32_t* adj, int words, uint32_t* lower_scratch, cudaStream_t st) {
+  if (n <= 0 || row_begin >= n) return;
+  constexpr int ROWS = 4;
+  const int rows = n - row_begin;
+  dim3 block(32, ROWS), grid(div_up(n, 32), div_up(rows, ROWS));
+  if (n > 1) {
+    if (dim == 3) {
+      if (mode == 0)
+        k_pairwise<3, PWC<3>, ROWS><<<grid, block, 0, st>>>(n, row_begin, sa, sb, flip, zp, zc, tr, th0, th1,
+                                                            lower_scratch, words);
+      else
+        k_pairwise<3, PWN<3>, ROWS><<<grid, block, 0, st>>>(n, row_begin, sa, sb, flip, zp, zc, tr, th0, th1,
+                                                            lower_scratch, words);
+    } else {
+      if (mode == 0)
+        k_pairwise<2, PWC<2>, ROWS><<<grid, block, 0, st>>>(n, row_begin, sa, sb, flip, zp, zc, tr, th0, th1,
+                                                            lower_scratch, words);
+      else
+        k_pairwise<2, PWN<2>, ROWS><<<grid, block, 0, st>>>(n, row_begin, sa, sb, flip, zp, zc, tr, th0, th1,
+                                                            lower_scratch, words);
+    }
+    RPGO_LAUNCHED();
+  }
+  // rows whose tiles were all skipped (j < 32*bx) keep stale words; the
+  // ballot writes only tiles with i0 < j, so clear the rest first: the
+  // mirror kernel reads only words bx <= j/32, all of which were written
+  // except word j/32 when 32*(j/32) >= j, i.e. j a multiple of 32 -> handled
+  // by masking with c < r in the mirror.
+  const int nb = div_up(n, 32);
+  const int warps = nb * nb;
+  k_symmetrize<<<div_up((int64_t)warps * 32, 256), 256, 0, st>>>(n, row_begin, lower_scratch, adj, words);
+  RPGO_LAUNCHED();
+}
+
+std::atomic<int64_t>& launch_counter() {
+  static std::atomic<int64_t> c{0};
+  return c;
+}
+
+}  // namespace rpgo

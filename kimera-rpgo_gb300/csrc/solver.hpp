@@ -1,0 +1,62 @@
+// Host control of the GPU nonlinear least-squares solve: GTSAM's
+// LevenbergMarquardtOptimizer / GaussNewtonOptimizer and GncOptimizer<TLS>
+// semantics (as RobustSolver::optimize uses them, src/RobustSolver.cpp:115-306)
+// over the device kernels of solver_kernels.cu. Only scalars (costs, the
+// linearised cost change, convergence flags) cross to the host per iteration.
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include "pcm_engine.hpp"
+#include "solver_kernels.hpp"
+
+namespace rpgo {
+
+struct LmParams {
+  bool gauss_newton = false;
+  bool diagonal_damping = true;
+  int max_iterations = 100;
+  double rel_tol = 1e-5, abs_tol = 1e-5, error_tol = 0.0;
+  double lambda_initial = 1e-5, lambda_factor = 10.0, lambda_upper = 1e5, lambda_lower = 0.0;
+  double min_model_fidelity = 1e-3;
+};
+
+struct GncConfig {
+  int threshold_mode = 1;  // 0 cost, 1 probability
+  double threshold = 0.9;
+  int max_iterations = 100;
+  double mu_step = 1.4, rel_cost_tol = 1e-5, weights_tol = 1e-4;
+};
+
+struct NlsStats {
+  int64_t iterations = 0, linear_solves = 0, cg_iterations = 0, gnc_iterations = 0;
+  bool failed = false;
+};
+
+class GpuNls {
+ public:
+  GpuNls(int dim, const std::vector<FactorRec>& graph, const Values& values, cudaStream_t st);
+  void set_weights(const std::vector<double>& w);
+  // LM / GN from the initial values; result left in dev().x
+  void optimize(const LmParams& p, NlsStats* st);
+  double error_at_result();
+  void result(Values* out) const;
+  SolverDev& dev() { return s_; }
+  cudaStream_t stream() const { return st_; }
+  const std::vector<uint64_t>& keys() const { return keys_; }
+
+ private:
+  int dim_;
+  cudaStream_t st_;
+  SolverDev s_;
+  std::vector<uint64_t> keys_;
+};
+
+double chi2inv(double alpha, int dof);
+
+// GncOptimizer<GncParams<LM or GN>> with the TLS loss; known inliers are the
+// first n_known factors. init_weights (optional) as in setWeights.
+void gnc_tls(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp,
+             const std::vector<double>* init_weights, std::vector<double>* weights_out, NlsStats* st);
+
+}  // namespace rpgo

@@ -1,0 +1,1020 @@
+// Nonlinear least-squares kernels of the robust solve (sm_103a).
+//
+//  K4 linearise      one thread per factor: FP64 residual and exact Jacobians
+//                    (BetweenFactor / PriorFactor as GTSAM evaluates them),
+//                    whitened by sqrt(w) R; FP64 gradient blocks, FP32 Hessian
+//                    blocks (J_i^T J_i, J_j^T J_j, J_i^T J_j).
+//  assemble          one thread per variable, fixed factor order (no atomics,
+//                    run-to-run deterministic): diagonal blocks, gradient, the
+//                    odometry-chain preconditioner blocks and the damping
+//                    diagonal clamp(diag H, 1e-6, 1e32) (LM diagonalDamping).
+//  K5 linear solve   one persistent CTA: block cyclic reduction factorisation
+//                    of the odometry-chain (block tridiagonal) preconditioner,
+//                    preconditioned CG on (H + lambda D) in FP32, and FP64
+//                    iterative refinement of the step on the FP64 residual;
+//                    also the linearised cost change -g.d - d^T H d / 2 (FP64).
+//  retract / error   X <- X Expmap(delta); per-factor 0.5 w |R e|^2 (FP64).
+//  K6 GNC weights    TLS weights of GncOptimizer::calculateWeights (FP64).
+#include <algorithm>
+#include <cmath>
+
+#include "solver_kernels.hpp"
+#include "solver_math.cuh"
+
+namespace rpgo {
+namespace {
+
+using namespace sm;
+
+constexpr int kCta = 1024;
+
+// ------------------------------------------------------------------ errors
+template <int DIM>
+__global__ void k_factor_err(int F, const int32_t* __restrict__ kind, const int32_t* __restrict__ vi,
+                             const int32_t* __restrict__ vj, const double* __restrict__ z,
+                             const double* __restrict__ R, const double* __restrict__ x,
+                             const double* __restrict__ w, double* __restrict__ ferr) {
+  using L = SLie<DIM>;
+  constexpr int d = L::d, st = L::stride;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= F) return;
+  typename L::Pose Xi, Z, rel;
+  L::load(x + (size_t)vi[f] * st, Xi);
+  L::load(z + (size_t)f * st, Z);
+  double e[d];
+  if (kind[f] == 0) {
+    typename L::Pose Xj, h;
+    L::load(x + (size_t)vj[f] * st, Xj);
+    L::between(Xi, Xj, h);
+    L::between(Z, h, rel);
+  } else {
+    L::between(Xi, Z, rel);
+  }
+  L::logmap(rel, e);
+  const double* Rf = R + (size_t)f * d * d;
+  double s = 0.0;
+#pragma unroll
+  for (int i = 0; i < d; ++i) {
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * e[k];
+    s += acc * acc;
+  }
+  ferr[f] = 0.5 * (w ? w[f] : 1.0) * s;
+}
+
+__global__ void k_sum_partial(int n, const double* __restrict__ in, double* __restrict__ out) {
+  __shared__ double sh[256];
+  double v = 0.0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v += in[i];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = 128; s; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+
+double device_sum(const double* in, int n, DeviceBuffer<double>& red, cudaStream_t st) {
+  if (n <= 0) return 0.0;
+  const int blocks = std::min(256, div_up(n, 256));
+  red.resize(blocks + 1);
+  k_sum_partial<<<blocks, 256, 0, st>>>(n, in, red.get());
+  RPGO_LAUNCHED();
+  k_sum_partial<<<1, 256, 0, st>>>(blocks, red.get(), red.get() + blocks);
+  RPGO_LAUNCHED();
+  double h = 0.0;
+  RPGO_CUDA(cudaMemcpyAsync(&h, red.get() + blocks, sizeof(double), cudaMemcpyDeviceToHost, st));
+  RPGO_CUDA(cudaStreamSynchronize(st));
+  return h;
+}
+
+// ------------------------------------------------------------------ K4
+template <int DIM>
+__global__ void k_linearize(int F, const int32_t* __restrict__ kind, const int32_t* __restrict__ vi,
+                            const int32_t* __restrict__ vj, const double* __restrict__ z,
+                            const double* __restrict__ R, const double* __restrict__ x,
+                            const double* __restrict__ w, float* __restrict__ fH, double* __restrict__ fg) {
+  using L = SLie<DIM>;
+  constexpr int d = L::d, st = L::stride, dd = d * d;
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= F) return;
+  const bool between = kind[f] == 0;
+  typename L::Pose Xi, Z, rel, h;
+  L::load(x + (size_t)vi[f] * st, Xi);
+  L::load(z + (size_t)f * st, Z);
+  double e[d], D[dd];
+  if (between) {
+    typename L::Pose Xj;
+    L::load(x + (size_t)vj[f] * st, Xj);
+    L::between(Xi, Xj, h);
+    L::between(Z, h, rel);
+    L::logmap(rel, e);
+    L::dlog(e, D);
+  } else {
+    L::between(Xi, Z, rel);
+    L::logmap(rel, e);
+#pragma unroll
+    for (int i = 0; i < d; ++i) e[i] = -e[i];
+  }
+  const double sw = sqrt(w[f]);
+  const double* Rf = R + (size_t)f * dd;
+  double r[d];
+#pragma unroll
+  for (int i = 0; i < d; ++i) {
+    double acc = 0.0;
+#pragma unroll
+    for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * e[k];
+    r[i] = sw * acc;
+  }
+  float Ai[dd], Aj[dd];
+  double gi[d], gj[d];
+  if (between) {
+    // J_i = -D Ad(h^-1), J_j = D
+    typename L::Pose hinv;
+    L::inverse(h, hinv);
+    double Ad[dd], Ji[dd];
+    L::adjoint(hinv, Ad);
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+#pragma unroll
+      for (int j = 0; j < d; ++j) {
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < d; ++k) acc += D[d * i + k] * Ad[d * k + j];
+        Ji[d * i + j] = -acc;
+      }
+    double A[dd];
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+#pragma unroll
+      for (int j = 0; j < d; ++j) {
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * Ji[d * k + j];
+        A[d * i + j] = sw * acc;
+      }
+#pragma unroll
+    for (int j = 0; j < d; ++j) {
+      double acc = 0.0;
+#pragma unroll
+      for (int i = 0; i < d; ++i) acc += A[d * i + j] * r[i];
+      gi[j] = acc;
+    }
+#pragma unroll
+    for (int i = 0; i < dd; ++i) Ai[i] = (float)A[i];
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+#pragma unroll
+      for (int j = 0; j < d; ++j) {
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * D[d * k + j];
+        A[d * i + j] = sw * acc;
+      }
+#pragma unroll
+    for (int j = 0; j < d; ++j) {
+      double acc = 0.0;
+#pragma unroll
+      for (int i = 0; i < d; ++i) acc += A[d * i + j] * r[i];
+      gj[j] = acc;
+    }
+#pragma unroll
+    for (int i = 0; i < dd; ++i) Aj[i] = (float)A[i];
+  } else {
+#pragma unroll
+    for (int i = 0; i < dd; ++i) Ai[i] = (float)(sw * Rf[i]);
+#pragma unroll
+    for (int j = 0; j < d; ++j) {
+      double acc = 0.0;
+#pragma unroll
+      for (int i = 0; i < d; ++i) acc += sw * Rf[d * i + j] * r[i];
+      gi[j] = acc;
+      gj[j] = 0.0;
+    }
+#pragma unroll
+    for (int i = 0; i < dd; ++i) Aj[i] = 0.0f;
+  }
+  float* out = fH + (size_t)f * 3 * dd;
+#pragma unroll
+  for (int a = 0; a < d; ++a)
+#pragma unroll
+    for (int b = 0; b < d; ++b) {
+      float hii = 0.f, hjj = 0.f, hij = 0.f;
+#pragma unroll
+      for (int q = 0; q < d; ++q) {
+        hii = fmaf(Ai[d * q + a], Ai[d * q + b], hii);
+        hjj = fmaf(Aj[d * q + a], Aj[d * q + b], hjj);
+        hij = fmaf(Ai[d * q + a], Aj[d * q + b], hij);
+      }
+      out[d * a + b] = hii;
+      out[dd + d * a + b] = hjj;
+      out[2 * dd + d * a + b] = hij;
+    }
+  double* og = fg + (size_t)f * 2 * d;
+#pragma unroll
+  for (int j = 0; j < d; ++j) {
+    og[j] = gi[j];
+    og[d + j] = gj[j];
+  }
+}
+
+template <int D>
+__global__ void k_assemble(int N, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc_fac,
+                           const int8_t* __restrict__ inc_role, const int32_t* __restrict__ kind,
+                           const int32_t* __restrict__ vi, const int32_t* __restrict__ vj,
+                           const uint8_t* __restrict__ tree, const uint8_t* __restrict__ has_tree,
+                           const float* __restrict__ fH, const double* __restrict__ fg, float* __restrict__ Hd,
+                           float* __restrict__ Md, float* __restrict__ Mu, double* __restrict__ g,
+                           double* __restrict__ dampD, int diag_damping) {
+  constexpr int dd = D * D;
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= N) return;
+  float H[dd], M[dd], U[dd];
+  double gv[D];
+#pragma unroll
+  for (int i = 0; i < dd; ++i) H[i] = M[i] = U[i] = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) gv[i] = 0.0;
+  for (int k = inc_ptr[v]; k < inc_ptr[v + 1]; ++k) {
+    const int f = inc_fac[k];
+    const int role = inc_role[k];
+    const float* blk = fH + (size_t)f * 3 * dd + (role == 1 ? dd : 0);
+    const bool in_m = kind[f] == 1 || tree[f];
+#pragma unroll
+    for (int i = 0; i < dd; ++i) {
+      const float b = blk[i];
+      H[i] += b;
+      if (in_m) M[i] += b;
+    }
+    const double* gg = fg + (size_t)f * 2 * D + role * D;
+#pragma unroll
+    for (int i = 0; i < D; ++i) gv[i] += gg[i];
+    if (tree[f]) {
+      const int other = role == 0 ? vj[f] : vi[f];
+      if (other == v + 1) {
+        const float* hij = fH + (size_t)f * 3 * dd + 2 * dd;
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int b = 0; b < D; ++b) U[D * a + b] += (role == 0) ? hij[D * a + b] : hij[D * b + a];
+      }
+    }
+  }
+  if (!has_tree[v]) {
+#pragma unroll
+    for (int i = 0; i < dd; ++i) M[i] = H[i];
+  }
+#pragma unroll
+  for (int i = 0; i < dd; ++i) {
+    Hd[(size_t)v * dd + i] = H[i];
+    Md[(size_t)v * dd + i] = M[i];
+    Mu[(size_t)v * dd + i] = U[i];
+  }
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    g[(size_t)v * D + i] = gv[i];
+    const double h = (double)H[D * i + i];
+    dampD[(size_t)v * D + i] = diag_damping ? fmin(fmax(h, 1e-6), 1e32) : 1.0;
+  }
+}
+
+// ------------------------------------------------------------------ small dense (FP32)
+template <int D>
+__device__ bool chol_f(const float* A, float* L) {
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      float acc = A[D * i + j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) acc -= L[D * i + k] * L[D * j + k];
+      if (i == j) {
+        if (!(acc > 0.f)) return false;
+        L[D * i + i] = sqrtf(acc);
+      } else {
+        L[D * i + j] = acc / L[D * j + j];
+      }
+    }
+  return true;
+}
+// SPD inverse; on a non-positive pivot, retries with a diagonal shift and
+// finally falls back to the inverse diagonal.
+template <int D>
+__device__ void spd_inv_f(const float* A, float* Ai) {
+  float L[D * D], B[D * D];
+#pragma unroll
+  for (int i = 0; i < D * D; ++i) {
+    B[i] = A[i];
+    L[i] = 0.f;
+  }
+  bool ok = chol_f<D>(B, L);
+  if (!ok) {
+    float tr = 0.f;
+#pragma unroll
+    for (int i = 0; i < D; ++i) tr += fabsf(A[D * i + i]);
+    const float eps = 1e-5f * (tr / D) + 1e-30f;
+#pragma unroll
+    for (int i = 0; i < D; ++i) B[D * i + i] += eps;
+    ok = chol_f<D>(B, L);
+  }
+  if (!ok) {
+#pragma unroll
+    for (int i = 0; i < D * D; ++i) Ai[i] = 0.f;
+#pragma unroll
+    for (int i = 0; i < D; ++i) Ai[D * i + i] = 1.f / fmaxf(fabsf(A[D * i + i]), 1e-30f);
+    return;
+  }
+  // Linv (lower)
+  float Li[D * D];
+#pragma unroll
+  for (int i = 0; i < D * D; ++i) Li[i] = 0.f;
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    Li[D * j + j] = 1.f / L[D * j + j];
+#pragma unroll
+    for (int i = j + 1; i < D; ++i) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = j; k < i; ++k) acc -= L[D * i + k] * Li[D * k + j];
+      Li[D * i + j] = acc / L[D * i + i];
+    }
+  }
+  // A^-1 = Li^T Li
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = i; k < D; ++k) acc += Li[D * k + i] * Li[D * k + j];
+      Ai[D * i + j] = acc;
+      Ai[D * j + i] = acc;
+    }
+}
+template <int D>
+__device__ __forceinline__ void mm_f(const float* A, const float* B, float* C, bool at = false, bool bt = false) {
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float acc = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) acc += (at ? A[D * k + i] : A[D * i + k]) * (bt ? B[D * j + k] : B[D * k + j]);
+      C[D * i + j] = acc;
+    }
+}
+
+// ------------------------------------------------------------------ block reductions (one CTA)
+__device__ __forceinline__ double cta_sum(double v, double* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : 0.0;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[32] = v;
+  }
+  __syncthreads();
+  const double r = sh[32];
+  __syncthreads();
+  return r;
+}
+
+// ------------------------------------------------------------------ K5 preconditioner factorisation
+template <int D>
+__global__ void __launch_bounds__(kCta) k_bcr_factor(int N, int levels, const int32_t* __restrict__ lvl_off,
+                                                     const int32_t* __restrict__ lvl_n, const float* __restrict__ Md,
+                                                     const float* __restrict__ Mu,
+                                                     const double* __restrict__ dampD, double lambda,
+                                                     float* __restrict__ bD, float* __restrict__ bDinv,
+                                                     float* __restrict__ bU, float* __restrict__ bFL,
+                                                     float* __restrict__ bFR) {
+  constexpr int dd = D * D;
+  for (int v = threadIdx.x; v < N; v += blockDim.x) {
+#pragma unroll
+    for (int i = 0; i < dd; ++i) {
+      bD[(size_t)v * dd + i] = Md[(size_t)v * dd + i];
+      bU[(size_t)v * dd + i] = (v + 1 < N) ? Mu[(size_t)v * dd + i] : 0.f;
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) bD[(size_t)v * dd + D * a + a] += (float)(lambda * dampD[(size_t)v * D + a]);
+  }
+  __syncthreads();
+  for (int l = 0; l < levels; ++l) {
+    const int base = lvl_off[l], n = lvl_n[l];
+    if (n == 1) {
+      if (threadIdx.x == 0) spd_inv_f<D>(bD + (size_t)base * dd, bDinv + (size_t)base * dd);
+      break;
+    }
+    for (int o = 1 + 2 * threadIdx.x; o < n; o += 2 * blockDim.x)
+      spd_inv_f<D>(bD + (size_t)(base + o) * dd, bDinv + (size_t)(base + o) * dd);
+    __syncthreads();
+    const int nbase = lvl_off[l + 1];
+    for (int i = 2 * threadIdx.x; i < n; i += 2 * blockDim.x) {
+      float FL[dd], FR[dd], Dn[dd], T[dd];
+      const float* Di = bD + (size_t)(base + i) * dd;
+#pragma unroll
+      for (int q = 0; q < dd; ++q) Dn[q] = Di[q];
+      if (i >= 1) {
+        const float* Ul = bU + (size_t)(base + i - 1) * dd;  // couples i-1, i
+        mm_f<D>(Ul, bDinv + (size_t)(base + i - 1) * dd, FL, true, false);  // U^T Dinv
+        mm_f<D>(FL, Ul, T);                                                // FL U
+#pragma unroll
+        for (int q = 0; q < dd; ++q) Dn[q] -= T[q];
+      } else {
+#pragma unroll
+        for (int q = 0; q < dd; ++q) FL[q] = 0.f;
+      }
+      float Un[dd];
+#pragma unroll
+      for (int q = 0; q < dd; ++q) Un[q] = 0.f;
+      if (i + 1 < n) {
+        const float* Ur = bU + (size_t)(base + i) * dd;  // couples i, i+1
+        mm_f<D>(Ur, bDinv + (size_t)(base + i + 1) * dd, FR);  // U Dinv
+        mm_f<D>(FR, Ur, T, false, true);                          // FR U^T
+#pragma unroll
+        for (int q = 0; q < dd; ++q) Dn[q] -= T[q];
+        if (i + 2 < n) {
+          mm_f<D>(FR, bU + (size_t)(base + i + 1) * dd, T);  // FR U_{i+1}
+#pragma unroll
+          for (int q = 0; q < dd; ++q) Un[q] = -T[q];
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < dd; ++q) FR[q] = 0.f;
+      }
+      // symmetrise the Schur complement
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int b = 0; b < a; ++b) {
+          const float s = 0.5f * (Dn[D * a + b] + Dn[D * b + a]);
+          Dn[D * a + b] = s;
+          Dn[D * b + a] = s;
+        }
+#pragma unroll
+      for (int q = 0; q < dd; ++q) {
+        bFL[(size_t)(base + i) * dd + q] = FL[q];
+        bFR[(size_t)(base + i) * dd + q] = FR[q];
+        bD[(size_t)(nbase + i / 2) * dd + q] = Dn[q];
+        bU[(size_t)(nbase + i / 2) * dd + q] = Un[q];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// z = M^-1 r by block cyclic reduction (forward reduction, coarse solve, back substitution)
+template <int D>
+__device__ void bcr_apply(int levels, const int32_t* lvl_off, const int32_t* lvl_n, const float* bDinv,
+                          const float* bFL, const float* bFR, float* bb, float* bx, const float* r, float* z) {
+  constexpr int dd = D * D;
+  const int n0 = lvl_n[0];
+  for (int q = threadIdx.x; q < n0 * D; q += blockDim.x) bb[q] = r[q];
+  __syncthreads();
+  int l = 0;
+  for (; l < levels && lvl_n[l] > 1; ++l) {
+    const int base = lvl_off[l], n = lvl_n[l], nbase = lvl_off[l + 1];
+    for (int i = 2 * threadIdx.x; i < n; i += 2 * blockDim.x) {
+      float out[D];
+      const float* bi = bb + (size_t)(base + i) * D;
+#pragma unroll
+      for (int a = 0; a < D; ++a) out[a] = bi[a];
+      if (i >= 1) {
+        const float* F = bFL + (size_t)(base + i) * dd;
+        const float* bl = bb + (size_t)(base + i - 1) * D;
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int c = 0; c < D; ++c) out[a] -= F[D * a + c] * bl[c];
+      }
+      if (i + 1 < n) {
+        const float* F = bFR + (size_t)(base + i) * dd;
+        const float* br = bb + (size_t)(base + i + 1) * D;
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int c = 0; c < D; ++c) out[a] -= F[D * a + c] * br[c];
+      }
+#pragma unroll
+      for (int a = 0; a < D; ++a) bb[(size_t)(nbase + i / 2) * D + a] = out[a];
+    }
+    __syncthreads();
+  }
+  // coarsest level: one node
+  {
+    const int base = lvl_off[l];
+    if (threadIdx.x < D) {
+      const int a = threadIdx.x;
+      float acc = 0.f;
+      const float* Di = bDinv + (size_t)base * dd;
+      for (int c = 0; c < D; ++c) acc += Di[D * a + c] * bb[(size_t)base * D + c];
+      bx[(size_t)base * D + a] = acc;
+    }
+  }
+  __syncthreads();
+  for (--l; l >= 0; --l) {
+    const int base = lvl_off[l], n = lvl_n[l], nbase = lvl_off[l + 1];
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      float* xi = bx + (size_t)(base + i) * D;
+      if ((i & 1) == 0) {
+        const float* src = bx + (size_t)(nbase + i / 2) * D;
+#pragma unroll
+        for (int a = 0; a < D; ++a) xi[a] = src[a];
+      } else {
+        const float* Di = bDinv + (size_t)(base + i) * dd;
+        const float* bi = bb + (size_t)(base + i) * D;
+        float out[D];
+#pragma unroll
+        for (int a = 0; a < D; ++a) {
+          float acc = 0.f;
+#pragma unroll
+          for (int c = 0; c < D; ++c) acc += Di[D * a + c] * bi[c];
+          out[a] = acc;
+        }
+        // - FR(i-1)^T x_{i-1}
+        {
+          const float* F = bFR + (size_t)(base + i - 1) * dd;
+          const float* xl = bx + (size_t)(nbase + (i - 1) / 2) * D;
+#pragma unroll
+          for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int c = 0; c < D; ++c) out[a] -= F[D * c + a] * xl[c];
+        }
+        if (i + 1 < n) {
+          const float* F = bFL + (size_t)(base + i + 1) * dd;
+          const float* xr = bx + (size_t)(nbase + (i + 1) / 2) * D;
+#pragma unroll
+          for (int a = 0; a < D; ++a)
+#pragma unroll
+            for (int c = 0; c < D; ++c) out[a] -= F[D * c + a] * xr[c];
+        }
+#pragma unroll
+        for (int a = 0; a < D; ++a) xi[a] = out[a];
+      }
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < n0 * D; q += blockDim.x) z[q] = bx[q];
+  __syncthreads();
+}
+
+struct CsrView {
+  const float* Hd;
+  const float* fH;
+  const int32_t* row_ptr;
+  const int32_t* col;
+  const int32_t* blk;
+  const int8_t* btr;
+  const double* dampD;
+};
+
+// y = (H + lam D) p, FP32
+template <int D>
+__device__ void spmv_f(int N, const CsrView& A, double lam, const float* p, float* y) {
+  constexpr int dd = D * D;
+  for (int v = threadIdx.x; v < N; v += blockDim.x) {
+    float acc[D];
+    const float* H = A.Hd + (size_t)v * dd;
+    const float* pv = p + (size_t)v * D;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      float s = (float)(lam * A.dampD[(size_t)v * D + a]) * pv[a];
+#pragma unroll
+      for (int c = 0; c < D; ++c) s += H[D * a + c] * pv[c];
+      acc[a] = s;
+    }
+    for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
+      const float* B = A.fH + (size_t)A.blk[k] * 3 * dd + 2 * dd;
+      const float* pc = p + (size_t)A.col[k] * D;
+      if (A.btr[k]) {
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int c = 0; c < D; ++c) acc[a] += B[D * c + a] * pc[c];
+      } else {
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int c = 0; c < D; ++c) acc[a] += B[D * a + c] * pc[c];
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) y[(size_t)v * D + a] = acc[a];
+  }
+  __syncthreads();
+}
+// y = (H + lam D) p, FP64 accumulation over the FP32 blocks
+template <int D>
+__device__ void spmv_d(int N, const CsrView& A, double lam, const double* p, double* y) {
+  constexpr int dd = D * D;
+  for (int v = threadIdx.x; v < N; v += blockDim.x) {
+    double acc[D];
+    const float* H = A.Hd + (size_t)v * dd;
+    const double* pv = p + (size_t)v * D;
+#pragma unroll
+    for (int a = 0; a < D; ++a) {
+      double s = lam * A.dampD[(size_t)v * D + a] * pv[a];
+#pragma unroll
+      for (int c = 0; c < D; ++c) s += (double)H[D * a + c] * pv[c];
+      acc[a] = s;
+    }
+    for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
+      const float* B = A.fH + (size_t)A.blk[k] * 3 * dd + 2 * dd;
+      const double* pc = p + (size_t)A.col[k] * D;
+      if (A.btr[k]) {
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int c = 0; c < D; ++c) acc[a] += (double)B[D * c + a] * pc[c];
+      } else {
+#pragma unroll
+        for (int a = 0; a < D; ++a)
+#pragma unroll
+          for (int c = 0; c < D; ++c) acc[a] += (double)B[D * a + c] * pc[c];
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < D; ++a) y[(size_t)v * D + a] = acc[a];
+  }
+  __syncthreads();
+}
+
+struct PcgParams {
+  double tol32;     // relative residual of one FP32 PCG sweep
+  double tol64;     // relative FP64 residual of the refined step
+  int max_cg;       // CG iterations per sweep
+  int max_sweeps;   // refinement sweeps
+};
+
+// Solve (H + lam D) delta = -g; out[0] lin_change, [1] ok, [2] CG iterations, [3] rel residual
+template <int D>
+__global__ void __launch_bounds__(kCta) k_pcg(int N, CsrView A, double lam, const double* __restrict__ g,
+                                              int levels, const int32_t* __restrict__ lvl_off,
+                                              const int32_t* __restrict__ lvl_n, const float* __restrict__ bDinv,
+                                              const float* __restrict__ bFL, const float* __restrict__ bFR,
+                                              float* __restrict__ bb, float* __restrict__ bx, float* __restrict__ cr,
+                                              float* __restrict__ cz, float* __restrict__ cp,
+                                              float* __restrict__ cq, float* __restrict__ cx,
+                                              double* __restrict__ res64, double* __restrict__ tmp64,
+                                              double* __restrict__ delta, PcgParams prm, double* __restrict__ out) {
+  __shared__ double sh[40];
+  const int n = N * D;
+  // rhs norm
+  double loc = 0.0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    delta[q] = 0.0;
+    loc += g[q] * g[q];
+  }
+  const double rhs_norm = sqrt(cta_sum(loc, sh));
+  int total_cg = 0;
+  int ok = 1;
+  double rel = 0.0;
+  if (rhs_norm > 0.0) {
+    for (int sweep = 0; sweep < prm.max_sweeps; ++sweep) {
+      // res64 = -g - A delta
+      spmv_d<D>(N, A, lam, delta, tmp64);
+      loc = 0.0;
+      for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const double r = -g[q] - tmp64[q];
+        res64[q] = r;
+        loc += r * r;
+      }
+      const double rn = sqrt(cta_sum(loc, sh));
+      rel = rn / rhs_norm;
+      if (rel <= prm.tol64) break;
+      // FP32 PCG on A c = res64
+      for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        cr[q] = (float)res64[q];
+        cx[q] = 0.f;
+      }
+      __syncthreads();
+      bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
+      loc = 0.0;
+      double lb = 0.0;
+      for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        cp[q] = cz[q];
+        loc += (double)cr[q] * cz[q];
+        lb += (double)cr[q] * cr[q];
+      }
+      double rz = cta_sum(loc, sh);
+      const double bn = sqrt(cta_sum(lb, sh));
+      for (int it = 0; it < prm.max_cg; ++it) {
+        spmv_f<D>(N, A, lam, cp, cq);
+        loc = 0.0;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) loc += (double)cp[q] * cq[q];
+        const double pq = cta_sum(loc, sh);
+        ++total_cg;
+        if (!(pq > 0.0) || !(rz > 0.0)) {
+          if (it == 0) ok = 0;
+          break;
+        }
+        const float alpha = (float)(rz / pq);
+        loc = 0.0;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) {
+          cx[q] += alpha * cp[q];
+          const float r = cr[q] - alpha * cq[q];
+          cr[q] = r;
+          loc += (double)r * r;
+        }
+        const double rr = sqrt(cta_sum(loc, sh));
+        if (rr <= prm.tol32 * bn) break;
+        bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
+        loc = 0.0;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) loc += (double)cr[q] * cz[q];
+        const double rz_new = cta_sum(loc, sh);
+        const float beta = (float)(rz_new / rz);
+        rz = rz_new;
+        for (int q = threadIdx.x; q < n; q += blockDim.x) cp[q] = cz[q] + beta * cp[q];
+        __syncthreads();
+      }
+      if (!ok) break;
+      for (int q = threadIdx.x; q < n; q += blockDim.x) delta[q] += (double)cx[q];
+      __syncthreads();
+    }
+  }
+  // linearised cost change with the undamped H
+  spmv_d<D>(N, A, 0.0, delta, tmp64);
+  double gd = 0.0, dhd = 0.0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    gd += g[q] * delta[q];
+    dhd += delta[q] * tmp64[q];
+  }
+  gd = cta_sum(gd, sh);
+  dhd = cta_sum(dhd, sh);
+  if (threadIdx.x == 0) {
+    out[0] = -gd - 0.5 * dhd;
+    out[1] = ok;
+    out[2] = total_cg;
+    out[3] = rel;
+  }
+}
+
+template <int DIM>
+__global__ void k_retract(int N, const double* __restrict__ x, const double* __restrict__ delta,
+                          double* __restrict__ xnew) {
+  using L = SLie<DIM>;
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= N) return;
+  typename L::Pose X, E, Y;
+  L::load(x + (size_t)v * L::stride, X);
+  L::exp(delta + (size_t)v * L::d, E);
+  L::compose(X, E, Y);
+  L::store(Y, xnew + (size_t)v * L::stride);
+}
+
+// GncOptimizer::calculateWeights, TLS branch (Yang et al. 2020, eq. 14)
+__global__ void k_gnc_weights(int F, int n_known, const double* __restrict__ u2, const double* __restrict__ barc,
+                              double mu, double* __restrict__ w) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= F) return;
+  if (f < n_known) {
+    w[f] = 1.0;
+    return;
+  }
+  const double b = barc[f], u = u2[f];
+  const double ub = (mu + 1.0) / mu * b;
+  const double lb = mu / (mu + 1.0) * b;
+  double wk = sqrt(b * mu * (mu + 1.0) / u) - mu;
+  if (u >= ub || wk < 0.0) wk = 0.0;
+  else if (u <= lb || wk > 1.0) wk = 1.0;
+  w[f] = wk;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ host wrappers
+void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
+                   const std::vector<int32_t>& vj, const std::vector<double>& z, const std::vector<double>& sqrt_info,
+                   const std::vector<double>& x0, int N, cudaStream_t st) {
+  s.dim = dim;
+  s.d = dim == 3 ? 6 : 3;
+  s.stride = dim == 3 ? 12 : 4;
+  s.N = N;
+  s.F = (int)kind.size();
+  const int d = s.d, dd = d * d, F = s.F;
+  std::vector<uint8_t> tree(F, 0), has_tree(N, 0);
+  std::vector<int32_t> deg(N + 1, 0);
+  for (int f = 0; f < F; ++f) {
+    if (kind[f] == 0 && std::abs(vi[f] - vj[f]) == 1) {
+      tree[f] = 1;
+      has_tree[vi[f]] = has_tree[vj[f]] = 1;
+    }
+    deg[vi[f] + 1]++;
+    if (kind[f] == 0 && vj[f] != vi[f]) deg[vj[f] + 1]++;
+  }
+  std::vector<int32_t> inc_ptr(N + 1, 0);
+  for (int v = 0; v < N; ++v) inc_ptr[v + 1] = inc_ptr[v] + deg[v + 1];
+  std::vector<int32_t> inc_fac(inc_ptr[N]), fill(inc_ptr.begin(), inc_ptr.end() - 1);
+  std::vector<int8_t> inc_role(inc_ptr[N]);
+  for (int f = 0; f < F; ++f) {
+    inc_fac[fill[vi[f]]] = f;
+    inc_role[fill[vi[f]]++] = 0;
+    if (kind[f] == 0 && vj[f] != vi[f]) {
+      inc_fac[fill[vj[f]]] = f;
+      inc_role[fill[vj[f]]++] = 1;
+    }
+  }
+  // SpMV rows: off-diagonal blocks of between factors
+  std::vector<int32_t> rdeg(N + 1, 0);
+  for (int f = 0; f < F; ++f)
+    if (kind[f] == 0 && vi[f] != vj[f]) {
+      rdeg[vi[f] + 1]++;
+      rdeg[vj[f] + 1]++;
+    }
+  std::vector<int32_t> row_ptr(N + 1, 0);
+  for (int v = 0; v < N; ++v) row_ptr[v + 1] = row_ptr[v] + rdeg[v + 1];
+  std::vector<int32_t> col(row_ptr[N]), blk(row_ptr[N]), rf(row_ptr.begin(), row_ptr.end() - 1);
+  std::vector<int8_t> btr(row_ptr[N]);
+  for (int f = 0; f < F; ++f)
+    if (kind[f] == 0 && vi[f] != vj[f]) {
+      int k = rf[vi[f]]++;
+      col[k] = vj[f];
+      blk[k] = f;
+      btr[k] = 0;
+      k = rf[vj[f]]++;
+      col[k] = vi[f];
+      blk[k] = f;
+      btr[k] = 1;
+    }
+  s.kind.upload(kind, st);
+  s.vi.upload(vi, st);
+  s.vj.upload(vj, st);
+  s.tree.upload(tree, st);
+  s.var_has_tree.upload(has_tree, st);
+  s.z.upload(z, st);
+  s.sqrt_info.upload(sqrt_info, st);
+  s.inc_ptr.upload(inc_ptr, st);
+  s.inc_fac.upload(inc_fac, st);
+  s.inc_role.upload(inc_role, st);
+  s.row_ptr.upload(row_ptr, st);
+  s.col.upload(col, st);
+  s.blk.upload(blk, st);
+  s.btr.upload(btr, st);
+  s.x0.upload(x0, st);
+  s.x.resize(x0.size());
+  s.xnew.resize(x0.size());
+  s.weights.resize(F);
+  s.fH.resize((size_t)F * 3 * dd);
+  s.fg.resize((size_t)F * 2 * d);
+  s.ferr.resize(F);
+  s.Hd.resize((size_t)N * dd);
+  s.Md.resize((size_t)N * dd);
+  s.Mu.resize((size_t)N * dd);
+  s.g.resize((size_t)N * d);
+  s.dampD.resize((size_t)N * d);
+  s.delta.resize((size_t)N * d);
+  // cyclic reduction levels
+  s.lvl_off.clear();
+  s.lvl_n.clear();
+  int n = N, off = 0;
+  while (true) {
+    s.lvl_off.push_back(off);
+    s.lvl_n.push_back(n);
+    off += n;
+    if (n <= 1) break;
+    n = (n + 1) / 2;
+  }
+  s.levels = (int)s.lvl_n.size();
+  s.d_lvl_off.upload(s.lvl_off, st);
+  s.d_lvl_n.upload(s.lvl_n, st);
+  const size_t nodes = (size_t)off;
+  s.bD.resize(nodes * dd);
+  s.bDinv.resize(nodes * dd);
+  s.bU.resize(nodes * dd);
+  s.bFL.resize(nodes * dd);
+  s.bFR.resize(nodes * dd);
+  s.bb.resize(nodes * d);
+  s.bx.resize(nodes * d);
+  for (auto* b : {&s.cr, &s.cz, &s.cp, &s.cq, &s.cx}) b->resize((size_t)N * d);
+  s.res64.resize((size_t)N * d);
+  s.tmp64.resize((size_t)N * d);
+  s.out.resize(8);
+}
+
+double solver_error(SolverDev& s, const double* x, const double* weights, cudaStream_t st) {
+  if (s.F == 0) return 0.0;
+  const int tb = 128;
+  if (s.dim == 3)
+    k_factor_err<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                    s.sqrt_info.get(), x, weights, s.ferr.get());
+  else
+    k_factor_err<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                    s.sqrt_info.get(), x, weights, s.ferr.get());
+  RPGO_LAUNCHED();
+  return device_sum(s.ferr.get(), s.F, s.red, st);
+}
+
+void solver_factor_errors(SolverDev& s, const double* x, std::vector<double>* out, cudaStream_t st) {
+  out->assign(s.F, 0.0);
+  if (s.F == 0) return;
+  const int tb = 128;
+  if (s.dim == 3)
+    k_factor_err<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                    s.sqrt_info.get(), x, nullptr, s.ferr.get());
+  else
+    k_factor_err<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                    s.sqrt_info.get(), x, nullptr, s.ferr.get());
+  RPGO_LAUNCHED();
+  s.ferr.download(out->data(), s.F, st);
+  RPGO_CUDA(cudaStreamSynchronize(st));
+}
+
+void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
+  const int tb = 128;
+  if (s.F > 0) {
+    if (s.dim == 3)
+      k_linearize<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                     s.sqrt_info.get(), s.x.get(), s.weights.get(), s.fH.get(),
+                                                     s.fg.get());
+    else
+      k_linearize<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                     s.sqrt_info.get(), s.x.get(), s.weights.get(), s.fH.get(),
+                                                     s.fg.get());
+    RPGO_LAUNCHED();
+  }
+  if (s.dim == 3)
+    k_assemble<6><<<div_up(s.N, tb), tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
+                                                  s.kind.get(), s.vi.get(), s.vj.get(), s.tree.get(),
+                                                  s.var_has_tree.get(), s.fH.get(), s.fg.get(), s.Hd.get(),
+                                                  s.Md.get(), s.Mu.get(), s.g.get(), s.dampD.get(),
+                                                  diagonal_damping ? 1 : 0);
+  else
+    k_assemble<3><<<div_up(s.N, tb), tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
+                                                  s.kind.get(), s.vi.get(), s.vj.get(), s.tree.get(),
+                                                  s.var_has_tree.get(), s.fH.get(), s.fg.get(), s.Hd.get(),
+                                                  s.Md.get(), s.Mu.get(), s.g.get(), s.dampD.get(),
+                                                  diagonal_damping ? 1 : 0);
+  RPGO_LAUNCHED();
+}
+
+SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
+  SolveOut o;
+  if (s.N == 0) {
+    o.ok = 1;
+    return o;
+  }
+  CsrView A{s.Hd.get(), s.fH.get(), s.row_ptr.get(), s.col.get(), s.blk.get(), s.btr.get(), s.dampD.get()};
+  PcgParams prm{1e-5, 1e-10, 2000, 6};
+  if (s.dim == 3) {
+    k_bcr_factor<6><<<1, kCta, 0, st>>>(s.N, s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(), s.Md.get(), s.Mu.get(),
+                                        s.dampD.get(), lambda, s.bD.get(), s.bDinv.get(), s.bU.get(), s.bFL.get(),
+                                        s.bFR.get());
+    RPGO_LAUNCHED();
+    k_pcg<6><<<1, kCta, 0, st>>>(s.N, A, lambda, s.g.get(), s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(),
+                                 s.bDinv.get(), s.bFL.get(), s.bFR.get(), s.bb.get(), s.bx.get(), s.cr.get(),
+                                 s.cz.get(), s.cp.get(), s.cq.get(), s.cx.get(), s.res64.get(), s.tmp64.get(),
+                                 s.delta.get(), prm, s.out.get());
+  } else {
+    k_bcr_factor<3><<<1, kCta, 0, st>>>(s.N, s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(), s.Md.get(), s.Mu.get(),
+                                        s.dampD.get(), lambda, s.bD.get(), s.bDinv.get(), s.bU.get(), s.bFL.get(),
+                                        s.bFR.get());
+    RPGO_LAUNCHED();
+    k_pcg<3><<<1, kCta, 0, st>>>(s.N, A, lambda, s.g.get(), s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(),
+                                 s.bDinv.get(), s.bFL.get(), s.bFR.get(), s.bb.get(), s.bx.get(), s.cr.get(),
+                                 s.cz.get(), s.cp.get(), s.cq.get(), s.cx.get(), s.res64.get(), s.tmp64.get(),
+                                 s.delta.get(), prm, s.out.get());
+  }
+  RPGO_LAUNCHED();
+  double h[4];
+  RPGO_CUDA(cudaMemcpyAsync(h, s.out.get(), sizeof(h), cudaMemcpyDeviceToHost, st));
+  RPGO_CUDA(cudaStreamSynchronize(st));
+  o.lin_change = h[0];
+  o.ok = (int)h[1];
+  o.cg_iterations = (int)h[2];
+  o.rel_residual = h[3];
+  return o;
+}
+
+void solver_retract(SolverDev& s, cudaStream_t st) {
+  if (s.N == 0) return;
+  const int tb = 128;
+  if (s.dim == 3) k_retract<3><<<div_up(s.N, tb), tb, 0, st>>>(s.N, s.x.get(), s.delta.get(), s.xnew.get());
+  else k_retract<2><<<div_up(s.N, tb), tb, 0, st>>>(s.N, s.x.get(), s.delta.get(), s.xnew.get());
+  RPGO_LAUNCHED();
+}
+
+void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const std::vector<double>& barc, double mu,
+                        cudaStream_t st) {
+  if (s.F == 0) return;
+  const int tb = 128;
+  if (s.dim == 3)
+    k_factor_err<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                    s.sqrt_info.get(), x, nullptr, s.ferr.get());
+  else
+    k_factor_err<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                    s.sqrt_info.get(), x, nullptr, s.ferr.get());
+  RPGO_LAUNCHED();
+  DeviceBuffer<double> d_barc;
+  d_barc.upload(barc, st);
+  k_gnc_weights<<<div_up(s.F, tb), tb, 0, st>>>(s.F, n_known, s.ferr.get(), d_barc.get(), mu, s.weights.get());
+  RPGO_LAUNCHED();
+  RPGO_CUDA(cudaStreamSynchronize(st));
+}
+
+}  // namespace rpgo

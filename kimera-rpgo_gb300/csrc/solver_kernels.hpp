@@ -1,0 +1,72 @@
+// Launch interface of the nonlinear least-squares kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "common.cuh"
+
+namespace rpgo {
+
+// Device-resident problem: factors, structure, per-iteration buffers.
+struct SolverDev {
+  int dim = 3, d = 6, stride = 12, N = 0, F = 0;
+  // factors
+  DeviceBuffer<int32_t> kind, vi, vj;
+  DeviceBuffer<uint8_t> tree;            // between factor joining consecutive variables
+  DeviceBuffer<double> z, sqrt_info;     // F x stride, F x d*d
+  DeviceBuffer<double> weights;          // F
+  // incidence CSR (per variable: factor, role 0 = i / prior, 1 = j)
+  DeviceBuffer<int32_t> inc_ptr, inc_fac;
+  DeviceBuffer<int8_t> inc_role;
+  DeviceBuffer<uint8_t> var_has_tree;
+  // SpMV CSR of off-diagonal blocks (per row: column, factor, transposed)
+  DeviceBuffer<int32_t> row_ptr, col, blk;
+  DeviceBuffer<int8_t> btr;
+  // linearisation
+  DeviceBuffer<float> fH;      // F x 3 x dd (Hii, Hjj, Hij)
+  DeviceBuffer<double> fg;     // F x 2 x d
+  DeviceBuffer<float> Hd, Md, Mu;  // N x dd, N x dd, N x dd (Mu[v] couples v, v+1)
+  DeviceBuffer<double> g, dampD;   // N x d
+  // values and step
+  DeviceBuffer<double> x0, x, xnew;  // N x stride
+  DeviceBuffer<double> delta;        // N x d
+  DeviceBuffer<double> ferr;         // F (per-factor error)
+  DeviceBuffer<double> red;          // reduction scratch
+  // preconditioner (block cyclic reduction) and CG scratch
+  std::vector<int32_t> lvl_off, lvl_n;
+  DeviceBuffer<int32_t> d_lvl_off, d_lvl_n;
+  DeviceBuffer<float> bD, bDinv, bU, bFL, bFR, bb, bx;  // per level node
+  DeviceBuffer<float> cr, cz, cp, cq, cx;                // N x d
+  DeviceBuffer<double> res64, tmp64;                     // N x d
+  DeviceBuffer<double> out;                              // solve outputs
+  int levels = 0;
+};
+
+struct SolveOut {
+  double lin_change = 0.0;  // -g.delta - 0.5 delta^T H delta
+  int ok = 0;
+  int cg_iterations = 0;
+  double rel_residual = 0.0;
+};
+
+// setup: host arrays -> device (structure is built here)
+void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
+                   const std::vector<int32_t>& vj, const std::vector<double>& z, const std::vector<double>& sqrt_info,
+                   const std::vector<double>& x0, int N, cudaStream_t st);
+// per-factor error 0.5 w |R e|^2 at values `x` (weights null = 1); returns the sum
+double solver_error(SolverDev& s, const double* x, const double* weights, cudaStream_t st);
+// per-factor unweighted errors at x into s.ferr (host copy returned)
+void solver_factor_errors(SolverDev& s, const double* x, std::vector<double>* out, cudaStream_t st);
+// linearise at s.x with s.weights; assembles Hd, g, tree blocks, damping diagonal
+void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st);
+// solve (H + lambda D) delta = -g into s.delta
+SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st);
+// xnew = x (+) delta
+void solver_retract(SolverDev& s, cudaStream_t st);
+// TLS weights (GncOptimizer::calculateWeights) for factors >= n_known
+void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const std::vector<double>& barc, double mu,
+                        cudaStream_t st);
+
+}  // namespace rpgo

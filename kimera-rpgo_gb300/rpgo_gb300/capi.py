@@ -1,0 +1,267 @@
+"""ctypes binding of librpgo_gb300.so (the C ABI of include/rpgo_gb300.h).
+
+The library is the CUDA implementation; there is no Python or CPU fallback.
+Loading fails loudly when the shared library has not been built.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librpgo_gb300.so")
+_lib = None
+
+OK, ERR_ARG, ERR_CUDA, ERR_KEY, ERR_SOLVER, ERR_UNSUPPORTED = range(6)
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("solver", C.c_int32), ("outlier_removal", C.c_int32), ("verbosity", C.c_int32), ("dim", C.c_int32),
+        ("odom_threshold", C.c_double), ("lc_threshold", C.c_double),
+        ("odom_trans_threshold", C.c_double), ("odom_rot_threshold", C.c_double),
+        ("dist_trans_threshold", C.c_double), ("dist_rot_threshold", C.c_double),
+        ("incremental", C.c_int32),
+        ("use_gnc", C.c_int32), ("gnc_threshold_mode", C.c_int32), ("gnc_inlier_threshold", C.c_double),
+        ("gnc_max_iterations", C.c_int32), ("gnc_mu_step", C.c_double), ("gnc_relative_cost_tol", C.c_double),
+        ("gnc_weights_tol", C.c_double), ("gnc_fix_prev_inliers", C.c_int32), ("gnc_bias_odom", C.c_int32),
+        ("lm_diagonal_damping", C.c_int32),
+    ]
+
+
+class FactorBatch(C.Structure):
+    _fields_ = [("count", C.c_int64), ("kind", C.c_void_p), ("key_front", C.c_void_p), ("key_back", C.c_void_p),
+                ("measured", C.c_void_p), ("covariance", C.c_void_p), ("sqrt_information", C.c_void_p)]
+
+
+class ValueBatch(C.Structure):
+    _fields_ = [("count", C.c_int64), ("key", C.c_void_p), ("pose", C.c_void_p)]
+
+
+class Counts(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("num_factors", "num_values", "num_lc", "num_lc_inliers", "num_odom",
+                                          "num_special", "num_gnc_weights", "last_do_optimize")]
+
+
+class Timing(C.Structure):
+    _fields_ = [("pcm_ms", C.c_double), ("solve_ms", C.c_double)] + [
+        (n, C.c_int64) for n in ("pair_checks", "lm_iterations", "linear_solves", "gnc_iterations", "cg_iterations",
+                                 "kernel_launches")]
+
+
+# every exported entry point: name -> (restype, argtypes)
+_P = C.c_void_p
+SIGNATURES = {
+    "rpgo_params_default": (None, [C.POINTER(Params)]),
+    "rpgo_params_set_no_rejection": (None, [C.POINTER(Params), C.c_int32]),
+    "rpgo_params_set_pcm2d": (None, [C.POINTER(Params), C.c_double, C.c_double, C.c_int32]),
+    "rpgo_params_set_pcm3d": (None, [C.POINTER(Params), C.c_double, C.c_double, C.c_int32]),
+    "rpgo_params_set_pcm_simple2d": (None, [C.POINTER(Params)] + [C.c_double] * 4 + [C.c_int32]),
+    "rpgo_params_set_pcm_simple3d": (None, [C.POINTER(Params)] + [C.c_double] * 4 + [C.c_int32]),
+    "rpgo_params_set_gnc_probability": (None, [C.POINTER(Params), C.c_double, C.c_int32, C.c_double, C.c_double,
+                                               C.c_double, C.c_int32, C.c_int32]),
+    "rpgo_params_set_gnc_cost": (None, [C.POINTER(Params), C.c_double, C.c_int32, C.c_double, C.c_double,
+                                        C.c_double, C.c_int32, C.c_int32]),
+    "rpgo_create": (_P, [C.POINTER(Params)]),
+    "rpgo_destroy": (None, [_P]),
+    "rpgo_update": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.c_int32]),
+    "rpgo_force_update": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch)]),
+    "rpgo_load_graph": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.POINTER(FactorBatch)]),
+    "rpgo_add_graph": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.POINTER(FactorBatch)]),
+    "rpgo_get_counts": (C.c_int, [_P, C.POINTER(Counts)]),
+    "rpgo_get_estimate": (C.c_int, [_P, _P, _P, C.c_int64]),
+    "rpgo_get_gnc_weights": (C.c_int, [_P, _P, C.c_int64]),
+    "rpgo_get_factors": (C.c_int, [_P, _P, _P, _P, _P, C.c_int64]),
+    "rpgo_get_adjacency": (C.c_int, [_P, C.c_int32, _P, C.c_int64, C.POINTER(C.c_int64)]),
+    "rpgo_get_timing": (C.c_int, [_P, C.POINTER(Timing)]),
+    "rpgo_save_data": (C.c_int, [_P, C.c_char_p]),
+    "rpgo_trajectory_scan_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [_P]),
+    "rpgo_odometry_check_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [C.c_double, C.c_double,
+                                                                                          _P, _P]),
+    "rpgo_pairwise_adjacency_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [_P] * 9 + [
+        C.c_double, C.c_double, _P, C.c_int32, _P]),
+    "rpgo_max_clique_heu_dev": (C.c_int, [C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P]),
+    "rpgo_pairwise_adjacency": (C.c_int, [C.c_int32, C.c_int32, C.c_int32] + [_P] * 5 + [C.c_int32] + [_P] * 4 + [
+        C.c_double, C.c_double, _P]),
+    "rpgo_max_clique_heu": (C.c_int, [C.c_int32, _P, C.c_int32, C.c_int32, _P, _P]),
+    "rpgo_device_info": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "rpgo_kernel_launch_count": (C.c_int64, []),
+}
+
+
+def load():
+    """Load the CUDA library (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with python kimera-rpgo_gb300/build.py")
+        lib = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data if a is not None and a.size else None
+
+
+def params_struct(p) -> Params:
+    s = Params()
+    for name, _ in Params._fields_:
+        setattr(s, name, getattr(p, name))
+    return s
+
+
+class Batch:
+    """Keeps the numpy arrays alive while the C structs point into them."""
+
+    def __init__(self, g):
+        self.a = g.arrays()
+        a = self.a
+        self.f = FactorBatch(len(a["kind"]), _ptr(a["kind"]), _ptr(a["key1"]), _ptr(a["key2"]), _ptr(a["measured"]),
+                             _ptr(a["cov"]), _ptr(a["sqrt_info"]))
+        self.v = ValueBatch(len(a["value_keys"]), _ptr(a["value_keys"]), _ptr(a["value_poses"]))
+
+
+class RpgoError(RuntimeError):
+    pass
+
+
+class RobustSolver:
+    """KimeraRPGO::RobustSolver on the GPU (include/KimeraRPGO/RobustSolver.h)."""
+
+    def __init__(self, params):
+        self.dim = 2 if params.outlier_removal in (1, 3) or (params.outlier_removal == 0 and params.dim == 2) else 3
+        self._p = params_struct(params)
+        self.use_gnc = bool(params.use_gnc)
+        self.h = load().rpgo_create(C.byref(self._p))
+        if not self.h:
+            raise RpgoError("rpgo_create failed (bad parameters or no CUDA device)")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            load().rpgo_destroy(self.h)
+            self.h = None
+
+    # ---- reference API
+    def update(self, graph, optimize_graph: bool = True) -> int:
+        b = Batch(graph)
+        return load().rpgo_update(self.h, C.byref(b.f), C.byref(b.v), int(optimize_graph))
+
+    def forceUpdate(self, graph) -> int:
+        b = Batch(graph)
+        return load().rpgo_force_update(self.h, C.byref(b.f), C.byref(b.v))
+
+    def loadGraph(self, graph, prior) -> int:
+        b, p = Batch(graph), Batch(prior)
+        return load().rpgo_load_graph(self.h, C.byref(b.f), C.byref(b.v), C.byref(p.f))
+
+    def addGraph(self, graph, between) -> int:
+        b, p = Batch(graph), Batch(between)
+        return load().rpgo_add_graph(self.h, C.byref(b.f), C.byref(b.v), C.byref(p.f))
+
+    def counts(self) -> Counts:
+        c = Counts()
+        load().rpgo_get_counts(self.h, C.byref(c))
+        return c
+
+    def size(self) -> int:
+        return self.counts().num_factors
+
+    def getNumLC(self) -> int:
+        return self.counts().num_lc
+
+    def getNumLCInliers(self) -> int:
+        return self.counts().num_lc_inliers
+
+    def estimate(self):
+        n = self.counts().num_values
+        st = 12 if self.dim == 3 else 4
+        keys = np.zeros(n, dtype=np.uint64)
+        poses = np.zeros((n, st))
+        rc = load().rpgo_get_estimate(self.h, _ptr(keys), _ptr(poses), n)
+        if rc:
+            raise RpgoError(f"rpgo_get_estimate: {rc}")
+        return keys, poses
+
+    calculateEstimate = estimate
+
+    def gnc_weights(self):
+        n = self.counts().num_gnc_weights
+        w = np.zeros(n)
+        load().rpgo_get_gnc_weights(self.h, _ptr(w), n)
+        return w
+
+    getGncWeights = gnc_weights
+
+    def factors(self):
+        n = self.counts().num_factors
+        st = 12 if self.dim == 3 else 4
+        kind = np.zeros(n, dtype=np.int32)
+        k1 = np.zeros(n, dtype=np.uint64)
+        k2 = np.zeros(n, dtype=np.uint64)
+        meas = np.zeros((n, st))
+        load().rpgo_get_factors(self.h, _ptr(kind), _ptr(k1), _ptr(k2), _ptr(meas), n)
+        return kind, k1, k2, meas
+
+    getFactorsUnsafe = factors
+
+    def adjacency(self, group: int = 0):
+        n = C.c_int64(0)
+        if load().rpgo_get_adjacency(self.h, group, None, 0, C.byref(n)) != 0:
+            return None
+        words = (n.value + 31) // 32
+        out = np.zeros(n.value * words, dtype=np.uint32)
+        load().rpgo_get_adjacency(self.h, group, _ptr(out), out.size, C.byref(n))
+        return out.reshape(n.value, words)
+
+    def timing(self) -> Timing:
+        t = Timing()
+        load().rpgo_get_timing(self.h, C.byref(t))
+        return t
+
+    def saveData(self, folder: str) -> int:
+        return load().rpgo_save_data(self.h, folder.encode())
+
+
+# ------------------------------------------------------------------ stage functions (host arrays)
+def pairwise_adjacency(dim, mode, slot_a, slot_b, flip, z_pose, z_cov, traj_pose, traj_cov, traj_node, traj_rot,
+                       th0, th1):
+    n = len(slot_a)
+    words = (n + 31) // 32
+    adj = np.zeros((max(n, 1), max(words, 1)), dtype=np.uint32)
+    arrs = [np.ascontiguousarray(x) for x in (slot_a, slot_b, flip, z_pose, z_cov)]
+    tr = [np.ascontiguousarray(x) for x in (traj_pose, traj_cov, traj_node, traj_rot)]
+    rc = load().rpgo_pairwise_adjacency(dim, mode, n, *[_ptr(a) for a in arrs], len(traj_rot),
+                                        *[_ptr(a) for a in tr], float(th0), float(th1), _ptr(adj))
+    if rc:
+        raise RpgoError(f"rpgo_pairwise_adjacency: {rc}")
+    return adj[:n, :words]
+
+
+def max_clique_heu(adj_words, n, first=0, seed=-1):
+    adj = np.ascontiguousarray(adj_words, dtype=np.uint32)
+    out = np.zeros(max(n, 1), dtype=np.int32)
+    size = np.zeros(1, dtype=np.int32)
+    rc = load().rpgo_max_clique_heu(n, _ptr(adj), first, seed, _ptr(out), _ptr(size))
+    if rc:
+        raise RpgoError(f"rpgo_max_clique_heu: {rc}")
+    return int(size[0]), out[: max(int(size[0]), 0)].copy()
+
+
+def device_info():
+    name = C.create_string_buffer(256)
+    sm = C.c_int32(0)
+    rc = load().rpgo_device_info(name, 256, C.byref(sm))
+    if rc:
+        raise RpgoError("no CUDA device")
+    return name.value.decode(), sm.value
+
+
+def kernel_launch_count() -> int:
+    return int(load().rpgo_kernel_launch_count())
