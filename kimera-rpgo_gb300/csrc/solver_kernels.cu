@@ -95,7 +95,8 @@ template <int DIM>
 __global__ void k_linearize(int F, const int32_t* __restrict__ kind, const int32_t* __restrict__ vi,
                             const int32_t* __restrict__ vj, const double* __restrict__ z,
                             const double* __restrict__ R, const double* __restrict__ x,
-                            const double* __restrict__ w, float* __restrict__ fH, double* __restrict__ fg) {
+                            const double* __restrict__ w, float* __restrict__ fH, double* __restrict__ fH64,
+                            double* __restrict__ fg) {
   using L = SLie<DIM>;
   constexpr int d = L::d, st = L::stride, dd = d * d;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
@@ -128,10 +129,9 @@ __global__ void k_linearize(int F, const int32_t* __restrict__ kind, const int32
     for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * e[k];
     r[i] = sw * acc;
   }
-  float Ai[dd], Aj[dd];
-  double gi[d], gj[d];
+  double Ai[dd], Aj[dd];
   if (between) {
-    // J_i = -D Ad(h^-1), J_j = D
+    // J_i = -D Ad(h^-1), J_j = D; whitened A = sqrt(w) R J
     typename L::Pose hinv;
     L::inverse(h, hinv);
     double Ad[dd], Ji[dd];
@@ -145,79 +145,58 @@ __global__ void k_linearize(int F, const int32_t* __restrict__ kind, const int32
         for (int k = 0; k < d; ++k) acc += D[d * i + k] * Ad[d * k + j];
         Ji[d * i + j] = -acc;
       }
-    double A[dd];
 #pragma unroll
     for (int i = 0; i < d; ++i)
 #pragma unroll
       for (int j = 0; j < d; ++j) {
-        double acc = 0.0;
+        double ai = 0.0, aj = 0.0;
 #pragma unroll
-        for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * Ji[d * k + j];
-        A[d * i + j] = sw * acc;
+        for (int k = 0; k < d; ++k) {
+          ai += Rf[d * i + k] * Ji[d * k + j];
+          aj += Rf[d * i + k] * D[d * k + j];
+        }
+        Ai[d * i + j] = sw * ai;
+        Aj[d * i + j] = sw * aj;
       }
-#pragma unroll
-    for (int j = 0; j < d; ++j) {
-      double acc = 0.0;
-#pragma unroll
-      for (int i = 0; i < d; ++i) acc += A[d * i + j] * r[i];
-      gi[j] = acc;
-    }
-#pragma unroll
-    for (int i = 0; i < dd; ++i) Ai[i] = (float)A[i];
-#pragma unroll
-    for (int i = 0; i < d; ++i)
-#pragma unroll
-      for (int j = 0; j < d; ++j) {
-        double acc = 0.0;
-#pragma unroll
-        for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * D[d * k + j];
-        A[d * i + j] = sw * acc;
-      }
-#pragma unroll
-    for (int j = 0; j < d; ++j) {
-      double acc = 0.0;
-#pragma unroll
-      for (int i = 0; i < d; ++i) acc += A[d * i + j] * r[i];
-      gj[j] = acc;
-    }
-#pragma unroll
-    for (int i = 0; i < dd; ++i) Aj[i] = (float)A[i];
   } else {
 #pragma unroll
-    for (int i = 0; i < dd; ++i) Ai[i] = (float)(sw * Rf[i]);
-#pragma unroll
-    for (int j = 0; j < d; ++j) {
-      double acc = 0.0;
-#pragma unroll
-      for (int i = 0; i < d; ++i) acc += sw * Rf[d * i + j] * r[i];
-      gi[j] = acc;
-      gj[j] = 0.0;
+    for (int i = 0; i < dd; ++i) {
+      Ai[i] = sw * Rf[i];
+      Aj[i] = 0.0;
     }
+  }
+  double* og = fg + (size_t)f * 2 * d;
 #pragma unroll
-    for (int i = 0; i < dd; ++i) Aj[i] = 0.0f;
+  for (int j = 0; j < d; ++j) {
+    double gi = 0.0, gj = 0.0;
+#pragma unroll
+    for (int i = 0; i < d; ++i) {
+      gi += Ai[d * i + j] * r[i];
+      gj += Aj[d * i + j] * r[i];
+    }
+    og[j] = gi;
+    og[d + j] = gj;
   }
   float* out = fH + (size_t)f * 3 * dd;
+  double* out64 = fH64 + (size_t)f * 3 * dd;
 #pragma unroll
   for (int a = 0; a < d; ++a)
 #pragma unroll
     for (int b = 0; b < d; ++b) {
-      float hii = 0.f, hjj = 0.f, hij = 0.f;
+      double hii = 0.0, hjj = 0.0, hij = 0.0;
 #pragma unroll
       for (int q = 0; q < d; ++q) {
-        hii = fmaf(Ai[d * q + a], Ai[d * q + b], hii);
-        hjj = fmaf(Aj[d * q + a], Aj[d * q + b], hjj);
-        hij = fmaf(Ai[d * q + a], Aj[d * q + b], hij);
+        hii += Ai[d * q + a] * Ai[d * q + b];
+        hjj += Aj[d * q + a] * Aj[d * q + b];
+        hij += Ai[d * q + a] * Aj[d * q + b];
       }
-      out[d * a + b] = hii;
-      out[dd + d * a + b] = hjj;
-      out[2 * dd + d * a + b] = hij;
+      out64[d * a + b] = hii;
+      out64[dd + d * a + b] = hjj;
+      out64[2 * dd + d * a + b] = hij;
+      out[d * a + b] = (float)hii;
+      out[dd + d * a + b] = (float)hjj;
+      out[2 * dd + d * a + b] = (float)hij;
     }
-  double* og = fg + (size_t)f * 2 * d;
-#pragma unroll
-  for (int j = 0; j < d; ++j) {
-    og[j] = gi[j];
-    og[d + j] = gj[j];
-  }
 }
 
 template <int D>
@@ -225,26 +204,27 @@ __global__ void k_assemble(int N, const int32_t* __restrict__ inc_ptr, const int
                            const int8_t* __restrict__ inc_role, const int32_t* __restrict__ kind,
                            const int32_t* __restrict__ vi, const int32_t* __restrict__ vj,
                            const uint8_t* __restrict__ tree, const uint8_t* __restrict__ has_tree,
-                           const float* __restrict__ fH, const double* __restrict__ fg, float* __restrict__ Hd,
-                           float* __restrict__ Md, float* __restrict__ Mu, double* __restrict__ g,
-                           double* __restrict__ dampD, int diag_damping) {
+                           const double* __restrict__ fH64, const double* __restrict__ fg,
+                           double* __restrict__ Hd64, float* __restrict__ Hd, float* __restrict__ Md,
+                           float* __restrict__ Mu, double* __restrict__ g, double* __restrict__ dampD,
+                           int diag_damping) {
   constexpr int dd = D * D;
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= N) return;
-  float H[dd], M[dd], U[dd];
+  double H[dd], M[dd], U[dd];
   double gv[D];
 #pragma unroll
-  for (int i = 0; i < dd; ++i) H[i] = M[i] = U[i] = 0.f;
+  for (int i = 0; i < dd; ++i) H[i] = M[i] = U[i] = 0.0;
 #pragma unroll
   for (int i = 0; i < D; ++i) gv[i] = 0.0;
   for (int k = inc_ptr[v]; k < inc_ptr[v + 1]; ++k) {
     const int f = inc_fac[k];
     const int role = inc_role[k];
-    const float* blk = fH + (size_t)f * 3 * dd + (role == 1 ? dd : 0);
+    const double* blk = fH64 + (size_t)f * 3 * dd + (role == 1 ? dd : 0);
     const bool in_m = kind[f] == 1 || tree[f];
 #pragma unroll
     for (int i = 0; i < dd; ++i) {
-      const float b = blk[i];
+      const double b = blk[i];
       H[i] += b;
       if (in_m) M[i] += b;
     }
@@ -254,7 +234,7 @@ __global__ void k_assemble(int N, const int32_t* __restrict__ inc_ptr, const int
     if (tree[f]) {
       const int other = role == 0 ? vj[f] : vi[f];
       if (other == v + 1) {
-        const float* hij = fH + (size_t)f * 3 * dd + 2 * dd;
+        const double* hij = fH64 + (size_t)f * 3 * dd + 2 * dd;
 #pragma unroll
         for (int a = 0; a < D; ++a)
 #pragma unroll
@@ -268,15 +248,15 @@ __global__ void k_assemble(int N, const int32_t* __restrict__ inc_ptr, const int
   }
 #pragma unroll
   for (int i = 0; i < dd; ++i) {
-    Hd[(size_t)v * dd + i] = H[i];
-    Md[(size_t)v * dd + i] = M[i];
-    Mu[(size_t)v * dd + i] = U[i];
+    Hd64[(size_t)v * dd + i] = H[i];
+    Hd[(size_t)v * dd + i] = (float)H[i];
+    Md[(size_t)v * dd + i] = (float)M[i];
+    Mu[(size_t)v * dd + i] = (float)U[i];
   }
 #pragma unroll
   for (int i = 0; i < D; ++i) {
     g[(size_t)v * D + i] = gv[i];
-    const double h = (double)H[D * i + i];
-    dampD[(size_t)v * D + i] = diag_damping ? fmin(fmax(h, 1e-6), 1e32) : 1.0;
+    dampD[(size_t)v * D + i] = diag_damping ? fmin(fmax(H[D * i + i], 1e-6), 1e32) : 1.0;
   }
 }
 
@@ -567,6 +547,8 @@ __device__ void bcr_apply(int levels, const int32_t* lvl_off, const int32_t* lvl
 struct CsrView {
   const float* Hd;
   const float* fH;
+  const double* Hd64;
+  const double* fH64;
   const int32_t* row_ptr;
   const int32_t* col;
   const int32_t* blk;
@@ -609,34 +591,34 @@ __device__ void spmv_f(int N, const CsrView& A, double lam, const float* p, floa
   }
   __syncthreads();
 }
-// y = (H + lam D) p, FP64 accumulation over the FP32 blocks
+// y = (H + lam D) p with the FP64 blocks
 template <int D>
 __device__ void spmv_d(int N, const CsrView& A, double lam, const double* p, double* y) {
   constexpr int dd = D * D;
   for (int v = threadIdx.x; v < N; v += blockDim.x) {
     double acc[D];
-    const float* H = A.Hd + (size_t)v * dd;
+    const double* H = A.Hd64 + (size_t)v * dd;
     const double* pv = p + (size_t)v * D;
 #pragma unroll
     for (int a = 0; a < D; ++a) {
       double s = lam * A.dampD[(size_t)v * D + a] * pv[a];
 #pragma unroll
-      for (int c = 0; c < D; ++c) s += (double)H[D * a + c] * pv[c];
+      for (int c = 0; c < D; ++c) s += H[D * a + c] * pv[c];
       acc[a] = s;
     }
     for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
-      const float* B = A.fH + (size_t)A.blk[k] * 3 * dd + 2 * dd;
+      const double* B = A.fH64 + (size_t)A.blk[k] * 3 * dd + 2 * dd;
       const double* pc = p + (size_t)A.col[k] * D;
       if (A.btr[k]) {
 #pragma unroll
         for (int a = 0; a < D; ++a)
 #pragma unroll
-          for (int c = 0; c < D; ++c) acc[a] += (double)B[D * c + a] * pc[c];
+          for (int c = 0; c < D; ++c) acc[a] += B[D * c + a] * pc[c];
       } else {
 #pragma unroll
         for (int a = 0; a < D; ++a)
 #pragma unroll
-          for (int c = 0; c < D; ++c) acc[a] += (double)B[D * a + c] * pc[c];
+          for (int c = 0; c < D; ++c) acc[a] += B[D * a + c] * pc[c];
       }
     }
 #pragma unroll
@@ -646,111 +628,98 @@ __device__ void spmv_d(int N, const CsrView& A, double lam, const double* p, dou
 }
 
 struct PcgParams {
-  double tol32;     // relative residual of one FP32 PCG sweep
-  double tol64;     // relative FP64 residual of the refined step
-  int max_cg;       // CG iterations per sweep
-  int max_sweeps;   // refinement sweeps
+  double tol;   // relative FP64 residual |b - A delta| / |b|
+  int max_it;   // CG iterations
 };
 
-// Solve (H + lam D) delta = -g; out[0] lin_change, [1] ok, [2] CG iterations, [3] rel residual
+// Solve (H + lam D) delta = -g by flexible preconditioned CG in FP64 (FP64
+// blocks), the block cyclic reduction preconditioner applied in FP32.
+// out[0] lin_change = -g.delta - delta^T H delta / 2 (undamped H),
+// [1] ok, [2] CG iterations, [3] final relative residual.
 template <int D>
 __global__ void __launch_bounds__(kCta) k_pcg(int N, CsrView A, double lam, const double* __restrict__ g,
                                               int levels, const int32_t* __restrict__ lvl_off,
                                               const int32_t* __restrict__ lvl_n, const float* __restrict__ bDinv,
                                               const float* __restrict__ bFL, const float* __restrict__ bFR,
                                               float* __restrict__ bb, float* __restrict__ bx, float* __restrict__ cr,
-                                              float* __restrict__ cz, float* __restrict__ cp,
-                                              float* __restrict__ cq, float* __restrict__ cx,
-                                              double* __restrict__ res64, double* __restrict__ tmp64,
+                                              float* __restrict__ cz, double* __restrict__ r,
+                                              double* __restrict__ z, double* __restrict__ zo,
+                                              double* __restrict__ p, double* __restrict__ q,
                                               double* __restrict__ delta, PcgParams prm, double* __restrict__ out) {
   __shared__ double sh[40];
   const int n = N * D;
-  // rhs norm
   double loc = 0.0;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    delta[q] = 0.0;
-    loc += g[q] * g[q];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    delta[k] = 0.0;
+    r[k] = -g[k];
+    loc += g[k] * g[k];
+    cr[k] = (float)(-g[k]);
   }
-  const double rhs_norm = sqrt(cta_sum(loc, sh));
-  int total_cg = 0;
-  int ok = 1;
+  const double bnorm = sqrt(cta_sum(loc, sh));
+  int it = 0, ok = 1;
   double rel = 0.0;
-  if (rhs_norm > 0.0) {
-    for (int sweep = 0; sweep < prm.max_sweeps; ++sweep) {
-      // res64 = -g - A delta
-      spmv_d<D>(N, A, lam, delta, tmp64);
+  if (bnorm > 0.0) {
+    bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
+    loc = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      z[k] = (double)cz[k];
+      p[k] = z[k];
+      loc += r[k] * z[k];
+    }
+    double rz = cta_sum(loc, sh);
+    for (; it < prm.max_it; ++it) {
+      spmv_d<D>(N, A, lam, p, q);
       loc = 0.0;
-      for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        const double r = -g[q] - tmp64[q];
-        res64[q] = r;
-        loc += r * r;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) loc += p[k] * q[k];
+      const double pq = cta_sum(loc, sh);
+      if (!(pq > 0.0) || !(rz > 0.0)) {
+        if (it == 0) ok = 0;
+        break;
       }
-      const double rn = sqrt(cta_sum(loc, sh));
-      rel = rn / rhs_norm;
-      if (rel <= prm.tol64) break;
-      // FP32 PCG on A c = res64
-      for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        cr[q] = (float)res64[q];
-        cx[q] = 0.f;
+      const double alpha = rz / pq;
+      loc = 0.0;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        delta[k] += alpha * p[k];
+        const double rk = r[k] - alpha * q[k];
+        r[k] = rk;
+        cr[k] = (float)rk;
+        zo[k] = z[k];
+        loc += rk * rk;
       }
-      __syncthreads();
+      rel = sqrt(cta_sum(loc, sh)) / bnorm;
+      if (rel <= prm.tol) {
+        ++it;
+        break;
+      }
       bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
-      loc = 0.0;
-      double lb = 0.0;
-      for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        cp[q] = cz[q];
-        loc += (double)cr[q] * cz[q];
-        lb += (double)cr[q] * cr[q];
+      double rzn = 0.0, rzo = 0.0;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double zk = (double)cz[k];
+        z[k] = zk;
+        rzn += r[k] * zk;
+        rzo += r[k] * zo[k];
       }
-      double rz = cta_sum(loc, sh);
-      const double bn = sqrt(cta_sum(lb, sh));
-      for (int it = 0; it < prm.max_cg; ++it) {
-        spmv_f<D>(N, A, lam, cp, cq);
-        loc = 0.0;
-        for (int q = threadIdx.x; q < n; q += blockDim.x) loc += (double)cp[q] * cq[q];
-        const double pq = cta_sum(loc, sh);
-        ++total_cg;
-        if (!(pq > 0.0) || !(rz > 0.0)) {
-          if (it == 0) ok = 0;
-          break;
-        }
-        const float alpha = (float)(rz / pq);
-        loc = 0.0;
-        for (int q = threadIdx.x; q < n; q += blockDim.x) {
-          cx[q] += alpha * cp[q];
-          const float r = cr[q] - alpha * cq[q];
-          cr[q] = r;
-          loc += (double)r * r;
-        }
-        const double rr = sqrt(cta_sum(loc, sh));
-        if (rr <= prm.tol32 * bn) break;
-        bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
-        loc = 0.0;
-        for (int q = threadIdx.x; q < n; q += blockDim.x) loc += (double)cr[q] * cz[q];
-        const double rz_new = cta_sum(loc, sh);
-        const float beta = (float)(rz_new / rz);
-        rz = rz_new;
-        for (int q = threadIdx.x; q < n; q += blockDim.x) cp[q] = cz[q] + beta * cp[q];
-        __syncthreads();
-      }
-      if (!ok) break;
-      for (int q = threadIdx.x; q < n; q += blockDim.x) delta[q] += (double)cx[q];
+      rzn = cta_sum(rzn, sh);
+      rzo = cta_sum(rzo, sh);
+      const double beta = (rzn - rzo) / rz;  // flexible (Polak-Ribiere) update
+      rz = rzn;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) p[k] = z[k] + beta * p[k];
       __syncthreads();
     }
   }
   // linearised cost change with the undamped H
-  spmv_d<D>(N, A, 0.0, delta, tmp64);
+  spmv_d<D>(N, A, 0.0, delta, q);
   double gd = 0.0, dhd = 0.0;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    gd += g[q] * delta[q];
-    dhd += delta[q] * tmp64[q];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    gd += g[k] * delta[k];
+    dhd += delta[k] * q[k];
   }
   gd = cta_sum(gd, sh);
   dhd = cta_sum(dhd, sh);
   if (threadIdx.x == 0) {
     out[0] = -gd - 0.5 * dhd;
     out[1] = ok;
-    out[2] = total_cg;
+    out[2] = it;
     out[3] = rel;
   }
 }
@@ -861,9 +830,11 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   s.xnew.resize(x0.size());
   s.weights.resize(F);
   s.fH.resize((size_t)F * 3 * dd);
+  s.fH64.resize((size_t)F * 3 * dd);
   s.fg.resize((size_t)F * 2 * d);
   s.ferr.resize(F);
   s.Hd.resize((size_t)N * dd);
+  s.Hd64.resize((size_t)N * dd);
   s.Md.resize((size_t)N * dd);
   s.Mu.resize((size_t)N * dd);
   s.g.resize((size_t)N * d);
@@ -891,9 +862,9 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   s.bFR.resize(nodes * dd);
   s.bb.resize(nodes * d);
   s.bx.resize(nodes * d);
-  for (auto* b : {&s.cr, &s.cz, &s.cp, &s.cq, &s.cx}) b->resize((size_t)N * d);
-  s.res64.resize((size_t)N * d);
-  s.tmp64.resize((size_t)N * d);
+  s.cr.resize((size_t)N * d);
+  s.cz.resize((size_t)N * d);
+  for (auto* b : {&s.r64, &s.z64, &s.zo64, &s.p64, &s.q64}) b->resize((size_t)N * d);
   s.out.resize(8);
 }
 
@@ -931,23 +902,23 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
     if (s.dim == 3)
       k_linearize<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                      s.sqrt_info.get(), s.x.get(), s.weights.get(), s.fH.get(),
-                                                     s.fg.get());
+                                                     s.fH64.get(), s.fg.get());
     else
       k_linearize<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                      s.sqrt_info.get(), s.x.get(), s.weights.get(), s.fH.get(),
-                                                     s.fg.get());
+                                                     s.fH64.get(), s.fg.get());
     RPGO_LAUNCHED();
   }
   if (s.dim == 3)
     k_assemble<6><<<div_up(s.N, tb), tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
                                                   s.kind.get(), s.vi.get(), s.vj.get(), s.tree.get(),
-                                                  s.var_has_tree.get(), s.fH.get(), s.fg.get(), s.Hd.get(),
+                                                  s.var_has_tree.get(), s.fH64.get(), s.fg.get(), s.Hd64.get(), s.Hd.get(),
                                                   s.Md.get(), s.Mu.get(), s.g.get(), s.dampD.get(),
                                                   diagonal_damping ? 1 : 0);
   else
     k_assemble<3><<<div_up(s.N, tb), tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
                                                   s.kind.get(), s.vi.get(), s.vj.get(), s.tree.get(),
-                                                  s.var_has_tree.get(), s.fH.get(), s.fg.get(), s.Hd.get(),
+                                                  s.var_has_tree.get(), s.fH64.get(), s.fg.get(), s.Hd64.get(), s.Hd.get(),
                                                   s.Md.get(), s.Mu.get(), s.g.get(), s.dampD.get(),
                                                   diagonal_damping ? 1 : 0);
   RPGO_LAUNCHED();
@@ -959,8 +930,8 @@ SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
     o.ok = 1;
     return o;
   }
-  CsrView A{s.Hd.get(), s.fH.get(), s.row_ptr.get(), s.col.get(), s.blk.get(), s.btr.get(), s.dampD.get()};
-  PcgParams prm{1e-5, 1e-10, 2000, 6};
+  CsrView A{s.Hd.get(), s.fH.get(), s.Hd64.get(), s.fH64.get(), s.row_ptr.get(), s.col.get(), s.blk.get(), s.btr.get(), s.dampD.get()};
+  PcgParams prm{1e-12, 5000};
   if (s.dim == 3) {
     k_bcr_factor<6><<<1, kCta, 0, st>>>(s.N, s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(), s.Md.get(), s.Mu.get(),
                                         s.dampD.get(), lambda, s.bD.get(), s.bDinv.get(), s.bU.get(), s.bFL.get(),
@@ -968,7 +939,7 @@ SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
     RPGO_LAUNCHED();
     k_pcg<6><<<1, kCta, 0, st>>>(s.N, A, lambda, s.g.get(), s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(),
                                  s.bDinv.get(), s.bFL.get(), s.bFR.get(), s.bb.get(), s.bx.get(), s.cr.get(),
-                                 s.cz.get(), s.cp.get(), s.cq.get(), s.cx.get(), s.res64.get(), s.tmp64.get(),
+                                 s.cz.get(), s.r64.get(), s.z64.get(), s.zo64.get(), s.p64.get(), s.q64.get(),
                                  s.delta.get(), prm, s.out.get());
   } else {
     k_bcr_factor<3><<<1, kCta, 0, st>>>(s.N, s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(), s.Md.get(), s.Mu.get(),
@@ -977,7 +948,7 @@ SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
     RPGO_LAUNCHED();
     k_pcg<3><<<1, kCta, 0, st>>>(s.N, A, lambda, s.g.get(), s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(),
                                  s.bDinv.get(), s.bFL.get(), s.bFR.get(), s.bb.get(), s.bx.get(), s.cr.get(),
-                                 s.cz.get(), s.cp.get(), s.cq.get(), s.cx.get(), s.res64.get(), s.tmp64.get(),
+                                 s.cz.get(), s.r64.get(), s.z64.get(), s.zo64.get(), s.p64.get(), s.q64.get(),
                                  s.delta.get(), prm, s.out.get());
   }
   RPGO_LAUNCHED();

@@ -25,9 +25,11 @@ struct SolverDev {
   DeviceBuffer<int32_t> row_ptr, col, blk;
   DeviceBuffer<int8_t> btr;
   // linearisation
-  DeviceBuffer<float> fH;      // F x 3 x dd (Hii, Hjj, Hij)
+  DeviceBuffer<float> fH;      // F x 3 x dd (Hii, Hjj, Hij), FP32 copy for CG and preconditioner
+  DeviceBuffer<double> fH64;   // the same blocks in FP64 for the refinement residual
   DeviceBuffer<double> fg;     // F x 2 x d
   DeviceBuffer<float> Hd, Md, Mu;  // N x dd, N x dd, N x dd (Mu[v] couples v, v+1)
+  DeviceBuffer<double> Hd64;       // N x dd
   DeviceBuffer<double> g, dampD;   // N x d
   // values and step
   DeviceBuffer<double> x0, x, xnew;  // N x stride
@@ -38,8 +40,8 @@ struct SolverDev {
   std::vector<int32_t> lvl_off, lvl_n;
   DeviceBuffer<int32_t> d_lvl_off, d_lvl_n;
   DeviceBuffer<float> bD, bDinv, bU, bFL, bFR, bb, bx;  // per level node
-  DeviceBuffer<float> cr, cz, cp, cq, cx;                // N x d
-  DeviceBuffer<double> res64, tmp64;                     // N x d
+  DeviceBuffer<float> cr, cz;                           // N x d, preconditioner input / output
+  DeviceBuffer<double> r64, z64, zo64, p64, q64;        // N x d, CG vectors
   DeviceBuffer<double> out;                              // solve outputs
   int levels = 0;
 };
