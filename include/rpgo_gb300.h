@@ -109,6 +109,12 @@ typedef struct rpgo_timing {
   int64_t gnc_iterations;     /* outer GNC iterations */
   int64_t cg_iterations;      /* preconditioned CG iterations */
   int64_t kernel_launches;    /* kernels of this library launched by the last update */
+  /* device time of the dominant kernels (CUDA events on the library's stream) */
+  double pcg_kernel_ms;       /* whole-GPU PCG launches (sum) */
+  int64_t pcg_kernel_launches;
+  double pcg_kernel_bytes;    /* algorithmic bytes those launches move (sum) */
+  double pair_kernel_ms;      /* pairwise consistency launches (sum) */
+  int64_t pair_kernel_launches;
 } rpgo_timing;
 
 typedef struct rpgo_solver rpgo_solver; /* opaque */
@@ -148,6 +154,13 @@ void rpgo_destroy(rpgo_solver* s);
  * (RobustSolver::optimize, src/RobustSolver.cpp:115-306). */
 int rpgo_update(rpgo_solver* s, const rpgo_factor_batch* factors, const rpgo_value_batch* values,
                 int32_t optimize_graph);
+/* rpgo_update for callers that keep the graph in GPU memory: the bulk arrays
+ * (factors->measured, ->covariance, ->sqrt_information and values->pose) are
+ * DEVICE pointers of the calling process's CUDA device 0; the metadata
+ * (kind, key_front, key_back, key) stays on the host. Same semantics as
+ * rpgo_update; the measurements are copied device to device. */
+int rpgo_update_dev(rpgo_solver* s, const rpgo_factor_batch* factors, const rpgo_value_batch* values,
+                    int32_t optimize_graph);
 /* RobustSolver::forceUpdate (src/RobustSolver.cpp:308-335) */
 int rpgo_force_update(rpgo_solver* s, const rpgo_factor_batch* factors, const rpgo_value_batch* values);
 

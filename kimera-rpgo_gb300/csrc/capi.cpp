@@ -28,8 +28,9 @@ struct rpgo_solver {
   rpgo_params p;
   int dim = 3, stride = 12, d = 6;
   cudaStream_t st = nullptr;
-  Values values;
-  std::vector<FactorRec> nfg;
+  std::unique_ptr<ValueStore> values;  // GenericSolver::values_ (device rows)
+  std::unique_ptr<FactorStore> store;  // every factor measurement ever added (device rows)
+  std::vector<FactorRec> nfg;          // GenericSolver::nfg_ (kinds, keys, store rows)
   std::unique_ptr<PcmEngine> pcm;
   std::vector<double> gnc_weights;
   size_t gnc_num_inliers = 0, latest_num_lc = 0;
@@ -45,18 +46,19 @@ double ms_since(cudaEvent_t a, cudaEvent_t b) {
   return ms;
 }
 
-std::vector<FactorRec> convert(const rpgo_solver* s, const rpgo_factor_batch* f) {
+// Append a batch's measurements to the factor store (host or device arrays)
+// and return the factor records.
+std::vector<FactorRec> ingest(rpgo_solver* s, const rpgo_factor_batch* f, bool on_device) {
   std::vector<FactorRec> out;
-  if (!f) return out;
+  if (!f || f->count <= 0) return out;
+  const int64_t first = s->store->append(f->count, f->measured, f->covariance, f->sqrt_information, on_device, s->st);
   out.resize((size_t)f->count);
   for (int64_t k = 0; k < f->count; ++k) {
     FactorRec& r = out[k];
     r.kind = f->kind[k];
     r.k1 = f->key_front[k];
     r.k2 = (r.kind == RPGO_FACTOR_BETWEEN) ? f->key_back[k] : f->key_front[k];
-    std::memcpy(r.meas, f->measured + k * s->stride, sizeof(double) * s->stride);
-    std::memcpy(r.cov, f->covariance + k * s->d * s->d, sizeof(double) * s->d * s->d);
-    std::memcpy(r.sqrt_info, f->sqrt_information + k * s->d * s->d, sizeof(double) * s->d * s->d);
+    r.row = first + k;
   }
   return out;
 }
@@ -69,7 +71,6 @@ int optimize(rpgo_solver* s) {
   std::vector<FactorRec> full = s->nfg;
   NlsStats st;
   const size_t num_lc = s->pcm ? s->pcm->num_lc() : 0;
-  Values result;
   if (s->p.use_gnc && s->pcm && !(s->p.gnc_fix_prev_inliers && num_lc == s->latest_num_lc)) {
     GncConfig g;
     g.threshold_mode = s->p.gnc_threshold_mode;
@@ -84,10 +85,10 @@ int optimize(rpgo_solver* s) {
       init.assign(full.size(), 0.0);
       for (size_t i = 0; i < n_known && i < init.size(); ++i) init[i] = 1.0;
     }
-    GpuNls nls(s->dim, full, s->values, s->st);
+    GpuNls nls(s->dim, full, *s->store, *s->values, s->st);
     std::vector<double> w;
     gnc_tls(nls, n_known, g, lp, s->p.gnc_bias_odom ? &init : nullptr, &w, &st);
-    nls.result(&result);
+    nls.write_back(*s->values);
     s->gnc_weights.assign(w.begin(), w.begin() + std::min(w.size(), s->nfg.size()));
     const double sum = std::accumulate(s->gnc_weights.begin(), s->gnc_weights.end(), 0.0);
     s->gnc_num_inliers = static_cast<size_t>(sum) - n_known;
@@ -100,10 +101,10 @@ int optimize(rpgo_solver* s) {
         if (prev_k + i < s->gnc_weights.size() && s->gnc_weights[prev_k + i] > 0.5 && k + i < s->nfg.size())
           full.push_back(s->nfg[k + i]);
     }
-    GpuNls nls(s->dim, full, s->values, s->st);
+    GpuNls nls(s->dim, full, *s->store, *s->values, s->st);
     nls.optimize(lp, &st);
     if (st.failed) return RPGO_ERR_SOLVER;
-    nls.result(&result);
+    nls.write_back(*s->values);
     const size_t tail = std::min(s->latest_num_lc, s->gnc_weights.size());
     std::vector<double> lcw(s->gnc_weights.end() - tail, s->gnc_weights.end());
     s->gnc_weights.assign(s->nfg.size(), 1.0);
@@ -114,37 +115,34 @@ int optimize(rpgo_solver* s) {
   s->timing.linear_solves += st.linear_solves;
   s->timing.cg_iterations += st.cg_iterations;
   s->timing.gnc_iterations += st.gnc_iterations;
-  // GenericSolver::updateValues (src/GenericSolver.cpp:37-45)
-  for (auto& kv : result) {
-    auto it = s->values.find(kv.first);
-    if (it != s->values.end()) it->second = kv.second;
-  }
   if (s->pcm) s->latest_num_lc = s->pcm->num_lc();
   return RPGO_OK;
 }
 
-int update_impl(rpgo_solver* s, const rpgo_factor_batch* fb, const rpgo_value_batch* vb, int optimize_graph,
-                bool force) {
-  auto nf = convert(s, fb);
+// RobustSolver::update / forceUpdate on prepared factor records; value
+// arrays are host or device pointers.
+int update_impl(rpgo_solver* s, std::vector<FactorRec> nf, const rpgo_value_batch* vb, bool values_on_device,
+                int optimize_graph, bool force) {
   std::set<uint64_t> new_keys;
   if (vb) {
     for (int64_t k = 0; k < vb->count; ++k) {
-      if (s->values.count(vb->key[k]) || new_keys.count(vb->key[k])) return RPGO_ERR_KEY;
+      if (s->values->has(vb->key[k]) || new_keys.count(vb->key[k])) return RPGO_ERR_KEY;
       new_keys.insert(vb->key[k]);
     }
-    for (int64_t k = 0; k < vb->count; ++k)
-      s->values[vb->key[k]] = std::vector<double>(vb->pose + k * s->stride, vb->pose + (k + 1) * s->stride);
+    s->values->append(vb->count, vb->key, vb->pose, values_on_device, s->st);
   }
+  s->timing = rpgo_timing{};  // the figures describe the last update
   cudaEvent_t e0, e1, e2;
   RPGO_CUDA(cudaEventCreate(&e0));
   RPGO_CUDA(cudaEventCreate(&e1));
   RPGO_CUDA(cudaEventCreate(&e2));
   const int64_t launches0 = launch_counter().load();
   const int64_t pairs0 = s->pcm ? s->pcm->stats().pair_checks : 0;
+  const KernelTimes kt0 = kernel_times();
   RPGO_CUDA(cudaEventRecord(e0, s->st));
   bool do_opt;
   if (s->pcm) {
-    do_opt = s->pcm->remove_outliers(nf, new_keys, s->values, &s->nfg);
+    do_opt = s->pcm->remove_outliers(nf, new_keys, *s->values, *s->store, &s->nfg);
   } else {
     // GenericSolver::addAndCheckIfOptimize (src/GenericSolver.cpp:47-65)
     s->nfg.insert(s->nfg.end(), nf.begin(), nf.end());
@@ -154,21 +152,22 @@ int update_impl(rpgo_solver* s, const rpgo_factor_batch* fb, const rpgo_value_ba
   }
   s->last_do_optimize = do_opt;
   RPGO_CUDA(cudaEventRecord(e1, s->st));
-  for (const auto& f : s->nfg)
-    if (!s->values.count(f.k1) || !s->values.count(f.k2)) {
-      cudaEventDestroy(e0);
-      cudaEventDestroy(e1);
-      cudaEventDestroy(e2);
-      return RPGO_ERR_KEY;
-    }
   int rc = RPGO_OK;
-  if ((do_opt && optimize_graph) || force) rc = optimize(s);
+  for (const auto& f : s->nfg)
+    if (!s->values->has(f.k1) || !s->values->has(f.k2)) rc = RPGO_ERR_KEY;
+  if (rc == RPGO_OK && ((do_opt && optimize_graph) || force)) rc = optimize(s);
   RPGO_CUDA(cudaEventRecord(e2, s->st));
   RPGO_CUDA(cudaEventSynchronize(e2));
   s->timing.pcm_ms = ms_since(e0, e1);
   s->timing.solve_ms = ms_since(e1, e2);
   s->timing.pair_checks = (s->pcm ? s->pcm->stats().pair_checks : 0) - pairs0;
   s->timing.kernel_launches = launch_counter().load() - launches0;
+  const KernelTimes& kt = kernel_times();
+  s->timing.pcg_kernel_ms = kt.pcg_ms - kt0.pcg_ms;
+  s->timing.pcg_kernel_launches = kt.pcg_launches - kt0.pcg_launches;
+  s->timing.pcg_kernel_bytes = kt.pcg_bytes - kt0.pcg_bytes;
+  s->timing.pair_kernel_ms = kt.pair_ms - kt0.pair_ms;
+  s->timing.pair_kernel_launches = kt.pair_launches - kt0.pair_launches;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaEventDestroy(e2);
@@ -196,14 +195,94 @@ int device_ready() {
   return 1;
 }
 
-std::vector<FactorRec> concat(const rpgo_solver* s, const rpgo_factor_batch* a, const rpgo_factor_batch* b) {
-  auto x = convert(s, a);
-  auto y = convert(s, b);
-  x.insert(x.end(), y.begin(), y.end());
-  return x;
+}  // namespace
+
+int save_data_impl_(const rpgo_solver* s, const char* folder) {
+  // writeG2o (src/Logger.cpp:64-164) and gnc_weights.csv (src/RobustSolver.cpp:448-465)
+  const std::string base(folder);
+  std::ofstream g2o(base + "/result.g2o");
+  if (!g2o) return RPGO_ERR_ARG;
+  auto quat = [](const double* R, double q[4]) {
+    const double tr = R[0] + R[4] + R[8];
+    if (tr > 0) {
+      const double w = std::sqrt(tr + 1.0) * 2;
+      q[0] = 0.25 * w; q[1] = (R[7] - R[5]) / w; q[2] = (R[2] - R[6]) / w; q[3] = (R[3] - R[1]) / w;
+    } else if (R[0] > R[4] && R[0] > R[8]) {
+      const double w = std::sqrt(1.0 + R[0] - R[4] - R[8]) * 2;
+      q[0] = (R[7] - R[5]) / w; q[1] = 0.25 * w; q[2] = (R[1] + R[3]) / w; q[3] = (R[2] + R[6]) / w;
+    } else if (R[4] > R[8]) {
+      const double w = std::sqrt(1.0 + R[4] - R[0] - R[8]) * 2;
+      q[0] = (R[2] - R[6]) / w; q[1] = (R[1] + R[3]) / w; q[2] = 0.25 * w; q[3] = (R[5] + R[7]) / w;
+    } else {
+      const double w = std::sqrt(1.0 + R[8] - R[0] - R[4]) * 2;
+      q[0] = (R[3] - R[1]) / w; q[1] = (R[2] + R[6]) / w; q[2] = (R[5] + R[7]) / w; q[3] = 0.25 * w;
+    }
+  };
+  std::vector<uint64_t> vkeys;
+  std::vector<double> vposes;
+  s->values->download_sorted(&vkeys, &vposes, s->st);
+  for (size_t vi = 0; vi < vkeys.size(); ++vi) {
+    const double* p = &vposes[vi * s->stride];
+    const uint64_t vkey = vkeys[vi];
+    if (s->dim == 2) {
+      g2o << "VERTEX_SE2 " << vkey << " " << p[2] << " " << p[3] << " " << std::atan2(p[1], p[0]) << "\n";
+    } else {
+      double q[4];
+      quat(p, q);
+      g2o << "VERTEX_SE3:QUAT " << vkey << " " << p[9] << " " << p[10] << " " << p[11] << " " << q[1] << " "
+          << q[2] << " " << q[3] << " " << q[0] << "\n";
+    }
+  }
+  std::vector<int64_t> rows;
+  for (const auto& f : s->nfg) rows.push_back(f.row);
+  std::vector<double> allm, allr;
+  s->store->download_meas(rows, &allm, s->st);
+  s->store->download_sqrt(rows, &allr, s->st);
+  for (size_t fi = 0; fi < s->nfg.size(); ++fi) {
+    const FactorRec& f = s->nfg[fi];
+    if (f.kind != RPGO_FACTOR_BETWEEN) continue;
+    const int d = s->d;
+    const double* sqrt_info = &allr[fi * d * d];
+    double info[36];
+    for (int i = 0; i < d; ++i)
+      for (int j = 0; j < d; ++j) {
+        double acc = 0.0;
+        for (int k = 0; k < d; ++k) acc += sqrt_info[d * k + i] * sqrt_info[d * k + j];
+        info[d * i + j] = acc;
+      }
+    const double* m = &allm[fi * s->stride];
+    if (s->dim == 2) {
+      g2o << "EDGE_SE2 " << f.k1 << " " << f.k2 << " " << m[2] << " " << m[3] << " " << std::atan2(m[1], m[0]);
+      for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j) g2o << " " << info[3 * i + j];
+    } else {
+      double q[4];
+      quat(m, q);
+      g2o << "EDGE_SE3:QUAT " << f.k1 << " " << f.k2 << " " << m[9] << " " << m[10] << " " << m[11] << " " << q[1]
+          << " " << q[2] << " " << q[3] << " " << q[0];
+      // diagonal blocks swapped to [t; R], off-diagonal blocks copied in place (Logger.cpp:148-152)
+      double gi[36];
+      for (int i = 0; i < 6; ++i)
+        for (int j = 0; j < 6; ++j) {
+          const bool di = i < 3, dj = j < 3;
+          int si = i, sj = j;
+          if (di && dj) { si = i + 3; sj = j + 3; }
+          else if (!di && !dj) { si = i - 3; sj = j - 3; }
+          gi[6 * i + j] = info[6 * si + sj];
+        }
+      for (int i = 0; i < 6; ++i)
+        for (int j = i; j < 6; ++j) g2o << " " << gi[6 * i + j];
+    }
+    g2o << "\n";
+  }
+  if (s->p.use_gnc) {
+    std::ofstream w(base + "/gnc_weights.csv");
+    w.precision(17);
+    for (size_t i = 0; i < s->gnc_weights.size(); ++i) w << s->gnc_weights[i] << (i + 1 < s->gnc_weights.size() ? "\n" : "");
+  }
+  return RPGO_OK;
 }
 
-}  // namespace
 
 extern "C" {
 
@@ -303,6 +382,8 @@ rpgo_solver* rpgo_create(const rpgo_params* p) {
   s->d = dim == 3 ? 6 : 3;
   try {
     RPGO_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+    s->values = std::make_unique<ValueStore>(s->stride);
+    s->store = std::make_unique<FactorStore>(s->stride, s->d);
     if (m != RPGO_OUTLIER_NONE) {
       PcmConfig c;
       c.dim = dim;
@@ -327,37 +408,33 @@ void rpgo_destroy(rpgo_solver* s) {
   if (!s) return;
   cudaStream_t st = s->st;
   s->pcm.reset();
+  s->values.reset();
+  s->store.reset();
   delete s;
   if (st) cudaStreamDestroy(st);
 }
 
 int rpgo_update(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, int32_t optimize_graph) {
   if (!s) return RPGO_ERR_ARG;
-  return guarded([&] { return update_impl(s, f, v, optimize_graph, false); });
+  return guarded([&] { return update_impl(s, ingest(s, f, false), v, false, optimize_graph, false); });
+}
+int rpgo_update_dev(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, int32_t optimize_graph) {
+  if (!s) return RPGO_ERR_ARG;
+  return guarded([&] { return update_impl(s, ingest(s, f, true), v, true, optimize_graph, false); });
 }
 int rpgo_force_update(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v) {
   if (!s) return RPGO_ERR_ARG;
-  return guarded([&] { return update_impl(s, f, v, 1, true); });
+  return guarded([&] { return update_impl(s, ingest(s, f, false), v, false, 1, true); });
 }
 
 static int update_with_extra(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v,
                              const rpgo_factor_batch* extra) {
   if (!s) return RPGO_ERR_ARG;
   return guarded([&] {
-    auto all = concat(s, f, extra);
-    std::vector<int32_t> kind(all.size());
-    std::vector<uint64_t> k1(all.size()), k2(all.size());
-    std::vector<double> meas(all.size() * s->stride), cov(all.size() * s->d * s->d), R(all.size() * s->d * s->d);
-    for (size_t i = 0; i < all.size(); ++i) {
-      kind[i] = all[i].kind;
-      k1[i] = all[i].k1;
-      k2[i] = all[i].k2;
-      std::memcpy(&meas[i * s->stride], all[i].meas, sizeof(double) * s->stride);
-      std::memcpy(&cov[i * s->d * s->d], all[i].cov, sizeof(double) * s->d * s->d);
-      std::memcpy(&R[i * s->d * s->d], all[i].sqrt_info, sizeof(double) * s->d * s->d);
-    }
-    rpgo_factor_batch b{(int64_t)all.size(), kind.data(), k1.data(), k2.data(), meas.data(), cov.data(), R.data()};
-    return update_impl(s, &b, v, 1, false);
+    auto all = ingest(s, f, false);
+    auto more = ingest(s, extra, false);
+    all.insert(all.end(), more.begin(), more.end());
+    return update_impl(s, std::move(all), v, false, 1, false);
   });
 }
 int rpgo_load_graph(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v,
@@ -372,7 +449,7 @@ int rpgo_add_graph(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_
 int rpgo_get_counts(const rpgo_solver* s, rpgo_counts* c) {
   if (!s || !c) return RPGO_ERR_ARG;
   c->num_factors = (int64_t)s->nfg.size();
-  c->num_values = (int64_t)s->values.size();
+  c->num_values = (int64_t)s->values->size();
   c->num_lc = s->pcm ? (int64_t)s->pcm->num_lc() : 0;
   c->num_lc_inliers = s->p.use_gnc ? (int64_t)s->gnc_num_inliers : (s->pcm ? (int64_t)s->pcm->num_lc_inliers() : 0);
   c->num_odom = s->pcm ? (int64_t)s->pcm->num_odom() : 0;
@@ -382,14 +459,15 @@ int rpgo_get_counts(const rpgo_solver* s, rpgo_counts* c) {
   return RPGO_OK;
 }
 int rpgo_get_estimate(const rpgo_solver* s, uint64_t* keys, double* poses, int64_t cap) {
-  if (!s || (int64_t)s->values.size() > cap) return RPGO_ERR_ARG;
-  int64_t i = 0;
-  for (const auto& kv : s->values) {
-    keys[i] = kv.first;
-    std::memcpy(poses + i * s->stride, kv.second.data(), sizeof(double) * s->stride);
-    ++i;
-  }
-  return RPGO_OK;
+  if (!s || (int64_t)s->values->size() > cap) return RPGO_ERR_ARG;
+  return guarded([&] {
+    std::vector<uint64_t> k;
+    std::vector<double> p;
+    s->values->download_sorted(&k, &p, s->st);
+    std::memcpy(keys, k.data(), k.size() * sizeof(uint64_t));
+    std::memcpy(poses, p.data(), p.size() * sizeof(double));
+    return (int)RPGO_OK;
+  });
 }
 int rpgo_get_gnc_weights(const rpgo_solver* s, double* w, int64_t cap) {
   if (!s || (int64_t)s->gnc_weights.size() > cap) return RPGO_ERR_ARG;
@@ -398,13 +476,21 @@ int rpgo_get_gnc_weights(const rpgo_solver* s, double* w, int64_t cap) {
 }
 int rpgo_get_factors(const rpgo_solver* s, int32_t* kind, uint64_t* k1, uint64_t* k2, double* meas, int64_t cap) {
   if (!s || (int64_t)s->nfg.size() > cap) return RPGO_ERR_ARG;
-  for (size_t i = 0; i < s->nfg.size(); ++i) {
-    if (kind) kind[i] = s->nfg[i].kind;
-    if (k1) k1[i] = s->nfg[i].k1;
-    if (k2) k2[i] = s->nfg[i].k2;
-    if (meas) std::memcpy(meas + i * s->stride, s->nfg[i].meas, sizeof(double) * s->stride);
-  }
-  return RPGO_OK;
+  return guarded([&] {
+    for (size_t i = 0; i < s->nfg.size(); ++i) {
+      if (kind) kind[i] = s->nfg[i].kind;
+      if (k1) k1[i] = s->nfg[i].k1;
+      if (k2) k2[i] = s->nfg[i].k2;
+    }
+    if (meas) {
+      std::vector<int64_t> rows;
+      for (const auto& f : s->nfg) rows.push_back(f.row);
+      std::vector<double> m;
+      s->store->download_meas(rows, &m, s->st);
+      std::memcpy(meas, m.data(), m.size() * sizeof(double));
+    }
+    return (int)RPGO_OK;
+  });
 }
 int rpgo_get_adjacency(const rpgo_solver* s, int32_t group, uint32_t* words, int64_t cap, int64_t* n) {
   if (!s || !n) return RPGO_ERR_ARG;
@@ -428,80 +514,8 @@ int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* t) {
 
 int rpgo_save_data(const rpgo_solver* s, const char* folder) {
   if (!s || !folder) return RPGO_ERR_ARG;
-  // writeG2o (src/Logger.cpp:64-164) and gnc_weights.csv (src/RobustSolver.cpp:448-465)
-  const std::string base(folder);
-  std::ofstream g2o(base + "/result.g2o");
-  if (!g2o) return RPGO_ERR_ARG;
-  auto quat = [](const double* R, double q[4]) {
-    const double tr = R[0] + R[4] + R[8];
-    if (tr > 0) {
-      const double w = std::sqrt(tr + 1.0) * 2;
-      q[0] = 0.25 * w; q[1] = (R[7] - R[5]) / w; q[2] = (R[2] - R[6]) / w; q[3] = (R[3] - R[1]) / w;
-    } else if (R[0] > R[4] && R[0] > R[8]) {
-      const double w = std::sqrt(1.0 + R[0] - R[4] - R[8]) * 2;
-      q[0] = (R[7] - R[5]) / w; q[1] = 0.25 * w; q[2] = (R[1] + R[3]) / w; q[3] = (R[2] + R[6]) / w;
-    } else if (R[4] > R[8]) {
-      const double w = std::sqrt(1.0 + R[4] - R[0] - R[8]) * 2;
-      q[0] = (R[2] - R[6]) / w; q[1] = (R[1] + R[3]) / w; q[2] = 0.25 * w; q[3] = (R[5] + R[7]) / w;
-    } else {
-      const double w = std::sqrt(1.0 + R[8] - R[0] - R[4]) * 2;
-      q[0] = (R[3] - R[1]) / w; q[1] = (R[2] + R[6]) / w; q[2] = (R[5] + R[7]) / w; q[3] = 0.25 * w;
-    }
-  };
-  for (const auto& kv : s->values) {
-    const double* p = kv.second.data();
-    if (s->dim == 2) {
-      g2o << "VERTEX_SE2 " << kv.first << " " << p[2] << " " << p[3] << " " << std::atan2(p[1], p[0]) << "\n";
-    } else {
-      double q[4];
-      quat(p, q);
-      g2o << "VERTEX_SE3:QUAT " << kv.first << " " << p[9] << " " << p[10] << " " << p[11] << " " << q[1] << " "
-          << q[2] << " " << q[3] << " " << q[0] << "\n";
-    }
-  }
-  for (const auto& f : s->nfg) {
-    if (f.kind != RPGO_FACTOR_BETWEEN) continue;
-    const int d = s->d;
-    double info[36];
-    for (int i = 0; i < d; ++i)
-      for (int j = 0; j < d; ++j) {
-        double acc = 0.0;
-        for (int k = 0; k < d; ++k) acc += f.sqrt_info[d * k + i] * f.sqrt_info[d * k + j];
-        info[d * i + j] = acc;
-      }
-    const double* m = f.meas;
-    if (s->dim == 2) {
-      g2o << "EDGE_SE2 " << f.k1 << " " << f.k2 << " " << m[2] << " " << m[3] << " " << std::atan2(m[1], m[0]);
-      for (int i = 0; i < 3; ++i)
-        for (int j = i; j < 3; ++j) g2o << " " << info[3 * i + j];
-    } else {
-      double q[4];
-      quat(m, q);
-      g2o << "EDGE_SE3:QUAT " << f.k1 << " " << f.k2 << " " << m[9] << " " << m[10] << " " << m[11] << " " << q[1]
-          << " " << q[2] << " " << q[3] << " " << q[0];
-      // diagonal blocks swapped to [t; R], off-diagonal blocks copied in place (Logger.cpp:148-152)
-      double gi[36];
-      for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) {
-          const bool di = i < 3, dj = j < 3;
-          int si = i, sj = j;
-          if (di && dj) { si = i + 3; sj = j + 3; }
-          else if (!di && !dj) { si = i - 3; sj = j - 3; }
-          gi[6 * i + j] = info[6 * si + sj];
-        }
-      for (int i = 0; i < 6; ++i)
-        for (int j = i; j < 6; ++j) g2o << " " << gi[6 * i + j];
-    }
-    g2o << "\n";
-  }
-  if (s->p.use_gnc) {
-    std::ofstream w(base + "/gnc_weights.csv");
-    w.precision(17);
-    for (size_t i = 0; i < s->gnc_weights.size(); ++i) w << s->gnc_weights[i] << (i + 1 < s->gnc_weights.size() ? "\n" : "");
-  }
-  return RPGO_OK;
+  return guarded([&] { return save_data_impl_(s, folder); });
 }
-
 // ------------------------------------------------------------------ stage entry points (device pointers)
 int rpgo_trajectory_scan_dev(int32_t dim, int32_t mode, int64_t count, const int32_t* src, const int32_t* dst,
                              const double* delta_pose, const double* delta_cov, double* traj_pose, double* traj_cov,

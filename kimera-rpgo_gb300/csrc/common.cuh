@@ -28,6 +28,41 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
 
 // Count of kernels this library has launched (process-wide).
 std::atomic<int64_t>& launch_counter();
+
+// Device time of the dominant kernels, measured with CUDA events on the
+// launching stream (process-wide running sums).
+struct KernelTimes {
+  double pcg_ms = 0.0, pcg_bytes = 0.0;
+  int64_t pcg_launches = 0;
+  double pair_ms = 0.0;
+  int64_t pair_launches = 0;
+};
+KernelTimes& kernel_times();
+
+// RAII pair of events around one launch; elapsed() synchronises the end event.
+class EventTimer {
+ public:
+  explicit EventTimer(cudaStream_t st) : st_(st) {
+    cudaEventCreate(&a_);
+    cudaEventCreate(&b_);
+    cudaEventRecord(a_, st_);
+  }
+  ~EventTimer() {
+    cudaEventDestroy(a_);
+    cudaEventDestroy(b_);
+  }
+  double elapsed_ms() {
+    cudaEventRecord(b_, st_);
+    cudaEventSynchronize(b_);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a_, b_);
+    return ms;
+  }
+
+ private:
+  cudaStream_t st_;
+  cudaEvent_t a_, b_;
+};
 inline void note_launch(cudaError_t e, const char* file, int line) {
   cuda_check(e, "kernel launch", file, line);
   launch_counter().fetch_add(1, std::memory_order_relaxed);

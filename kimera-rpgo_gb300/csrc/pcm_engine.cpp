@@ -80,8 +80,8 @@ void PcmEngine::flush_slots() {
     std::vector<double> cov((size_t)d_ * d_, 0.0);
     int32_t node = 0;
     uint8_t rot = 1;
-    RPGO_CUDA(cudaMemcpyAsync(traj_pose_.get() + (size_t)s * stride_, pi.second.data(), stride_ * sizeof(double),
-                              cudaMemcpyHostToDevice, st_));
+    RPGO_CUDA(cudaMemcpyAsync(traj_pose_.get() + (size_t)s * stride_, values_->pose() + (size_t)pi.second * stride_,
+                              stride_ * sizeof(double), cudaMemcpyDeviceToDevice, st_));
     RPGO_CUDA(cudaMemcpyAsync(traj_cov_.get() + (size_t)s * d_ * d_, cov.data(), cov.size() * sizeof(double),
                               cudaMemcpyHostToDevice, st_));
     RPGO_CUDA(cudaMemcpyAsync(traj_node_.get() + s, &node, sizeof(node), cudaMemcpyHostToDevice, st_));
@@ -91,10 +91,10 @@ void PcmEngine::flush_slots() {
   pending_init_.clear();
 }
 
-void PcmEngine::run_pairwise(Group& g, int old_n) {
+void PcmEngine::run_pairwise(Group& g, int old_n, const FactorStore& store) {
   const int n = (int)g.factors.size();
   if (n <= old_n) return;
-  // upload the new closures' records
+  // the new closures' slots (host) and measurements (gathered from the store)
   g.sa.grow(n, st_);
   g.sb.grow(n, st_);
   g.flip.grow(n, st_);
@@ -106,10 +106,9 @@ void PcmEngine::run_pairwise(Group& g, int old_n) {
   RPGO_CUDA(cudaMemcpyAsync(g.sb.get() + old_n, g.h_sb.data() + old_n, add * sizeof(int32_t),
                             cudaMemcpyHostToDevice, st_));
   RPGO_CUDA(cudaMemcpyAsync(g.flip.get() + old_n, g.h_flip.data() + old_n, add, cudaMemcpyHostToDevice, st_));
-  RPGO_CUDA(cudaMemcpyAsync(g.zp.get() + (size_t)old_n * stride_, g.h_zp.data() + (size_t)old_n * stride_,
-                            (size_t)add * stride_ * sizeof(double), cudaMemcpyHostToDevice, st_));
-  RPGO_CUDA(cudaMemcpyAsync(g.zc.get() + (size_t)old_n * d_ * d_, g.h_zc.data() + (size_t)old_n * d_ * d_,
-                            (size_t)add * d_ * d_ * sizeof(double), cudaMemcpyHostToDevice, st_));
+  d_rows_.upload(g.h_row.data() + old_n, add, st_);
+  gather_rows(add, d_rows_.get(), store.meas(), stride_, g.zp.get() + (size_t)old_n * stride_, st_);
+  gather_rows(add, d_rows_.get(), store.cov(), d_ * d_, g.zc.get() + (size_t)old_n * d_ * d_, st_);
   // adjacency capacity: row_cap rows of row_cap/32 words, zero padded
   if (n > g.row_cap) {
     int cap = g.row_cap ? g.row_cap : 64;
@@ -179,12 +178,13 @@ void PcmEngine::find_inliers_incremental(const std::unordered_map<ObsId, size_t,
 }
 
 bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const std::set<uint64_t>& new_keys,
-                                const Values& values, std::vector<FactorRec>* out) {
+                                const ValueStore& values, const FactorStore& store, std::vector<FactorRec>* out) {
+  values_ = &values;
   if (new_factors.empty()) return false;
   bool do_optimize = false;
   // ---- classification (Pcm.h:164-240)
   std::vector<int32_t> src, dst;
-  std::vector<double> dpose, dcov;
+  std::vector<int64_t> orows;
   std::vector<const FactorRec*> lcs;
   for (const auto& f : new_factors) {
     if (f.kind == 0) {
@@ -195,12 +195,11 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
         if (!prefix_exists_.count(prefix)) {
           prefix_exists_.insert(prefix);
           const int32_t s0 = slot(f.k1);
-          pending_init_.emplace_back(s0, values.at(f.k1));
+          pending_init_.emplace_back(s0, values.row(f.k1));
         }
         src.push_back(slot(f.k1));
         dst.push_back(slot(f.k2));
-        dpose.insert(dpose.end(), f.meas, f.meas + stride_);
-        dcov.insert(dcov.end(), f.cov, f.cov + d_ * d_);
+        orows.push_back(f.row);
       } else if (f.k1 != f.k2) {
         lcs.push_back(&f);
       }
@@ -213,35 +212,38 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
     flush_slots();
     d_src_.upload(src, st_);
     d_dst_.upload(dst, st_);
-    d_dpose_.upload(dpose, st_);
-    d_dcov_.upload(dcov, st_);
+    d_rows_.upload(orows, st_);
+    d_dpose_.resize(orows.size() * stride_);
+    d_dcov_.resize(orows.size() * d_ * d_);
+    gather_rows((int64_t)orows.size(), d_rows_.get(), store.meas(), stride_, d_dpose_.get(), st_);
+    gather_rows((int64_t)orows.size(), d_rows_.get(), store.cov(), d_ * d_, d_dcov_.get(), st_);
     launch_traj_scan(cfg_.dim, cfg_.mode, (int64_t)src.size(), d_src_.get(), d_dst_.get(), d_dpose_.get(),
                      d_dcov_.get(), view(), scratch_rec_, scratch_cov_, scratch_rot_, st_);
   }
   if (!lcs.empty()) {
     // ---- odometry consistency of intra-robot closures (Pcm.h:455-465, 604-629)
     std::vector<int32_t> ci, cj, owner;
-    std::vector<double> zp, zc;
+    std::vector<int64_t> crow;
     for (size_t k = 0; k < lcs.size(); ++k) {
       const FactorRec& f = *lcs[k];
-      if (!values.count(f.k1) || !values.count(f.k2)) continue;
+      if (!values.has(f.k1) || !values.has(f.k2)) continue;
       if (key_chr(f.k1) != key_chr(f.k2) || !odom_check_) continue;
       prefix_exists_.insert(key_chr(f.k1));
       ci.push_back(slot(f.k1));
       cj.push_back(slot(f.k2));
       owner.push_back((int32_t)k);
-      zp.insert(zp.end(), f.meas, f.meas + stride_);
-      zc.insert(zc.end(), f.cov, f.cov + d_ * d_);
+      crow.push_back(f.row);
     }
     std::vector<uint8_t> passed(lcs.size(), 1);
     if (!ci.empty()) {
       flush_slots();
       DeviceBuffer<int32_t> di, dj;
-      DeviceBuffer<double> dzp, dzc;
+      DeviceBuffer<double> dzp(crow.size() * stride_), dzc(crow.size() * d_ * d_);
       di.upload(ci, st_);
       dj.upload(cj, st_);
-      dzp.upload(zp, st_);
-      dzc.upload(zc, st_);
+      d_rows_.upload(crow, st_);
+      gather_rows((int64_t)crow.size(), d_rows_.get(), store.meas(), stride_, dzp.get(), st_);
+      gather_rows((int64_t)crow.size(), d_rows_.get(), store.cov(), d_ * d_, dzc.get(), st_);
       d_ok_.resize(ci.size());
       const double th0 = cfg_.mode == 0 ? cfg_.odom_threshold : cfg_.odom_trans_threshold;
       const double th1 = cfg_.mode == 0 ? 0.0 : cfg_.odom_rot_threshold;
@@ -258,7 +260,7 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
     std::vector<std::pair<ObsId, int>> touched;
     for (size_t k = 0; k < lcs.size(); ++k) {
       const FactorRec& f = *lcs[k];
-      if (!values.count(f.k1) || !values.count(f.k2)) continue;
+      if (!values.has(f.k1) || !values.has(f.k2)) continue;
       if (!passed[k]) continue;
       const ObsId id{key_chr(f.k1), key_chr(f.k2)};
       num_new[id]++;
@@ -276,8 +278,7 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
       g.h_sa.push_back(slot(f.k1));
       g.h_sb.push_back(slot(f.k2));
       g.h_flip.push_back(key_chr(f.k1) != g.key.id1 ? 1 : 0);
-      g.h_zp.insert(g.h_zp.end(), f.meas, f.meas + stride_);
-      g.h_zc.insert(g.h_zc.end(), f.cov, f.cov + d_ * d_);
+      g.h_row.push_back(f.row);
       ++total_lc_;
     }
     if (lc_check_) {
@@ -289,7 +290,7 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
           prefix_exists_.insert(g.key.id1);
           prefix_exists_.insert(g.key.id2);
         }
-        run_pairwise(g, t.second);
+        run_pairwise(g, t.second, store);
       }
     }
     if (cfg_.incremental) find_inliers_incremental(num_new);

@@ -17,18 +17,9 @@
 #include <vector>
 
 #include "pcm_kernels.hpp"
+#include "stores.hpp"
 
 namespace rpgo {
-
-struct FactorRec {
-  int32_t kind = 0;  // 0 between, 1 prior
-  uint64_t k1 = 0, k2 = 0;
-  double meas[12] = {0};
-  double cov[36] = {0};
-  double sqrt_info[36] = {0};
-};
-
-using Values = std::map<uint64_t, std::vector<double>>;
 
 inline char key_chr(uint64_t k) { return static_cast<char>(static_cast<unsigned char>(k >> 56)); }
 
@@ -63,10 +54,11 @@ struct PcmStats {
 class PcmEngine {
  public:
   PcmEngine(const PcmConfig& cfg, cudaStream_t st);
-  // Pcm::removeOutliers. `values` already holds new_values. Returns
-  // do_optimize; *out is the graph to optimise (odometry, special, inliers).
+  // Pcm::removeOutliers. `values` already holds new_values; factor rows point
+  // into `store`. Returns do_optimize; *out is the graph to optimise
+  // (odometry, special, inliers).
   bool remove_outliers(const std::vector<FactorRec>& new_factors, const std::set<uint64_t>& new_keys,
-                       const Values& values, std::vector<FactorRec>* out);
+                       const ValueStore& values, const FactorStore& store, std::vector<FactorRec>* out);
 
   size_t num_lc() const { return total_lc_; }
   size_t num_lc_inliers() const { return total_good_lc_; }
@@ -84,7 +76,7 @@ class PcmEngine {
     DeviceBuffer<uint32_t> adj;  // row_cap x words
     std::vector<int32_t> h_sa, h_sb;
     std::vector<uint8_t> h_flip;
-    std::vector<double> h_zp, h_zc;
+    std::vector<int64_t> h_row;  // factor-store rows of the closures
     DeviceBuffer<int32_t> sa, sb;
     DeviceBuffer<uint8_t> flip;
     DeviceBuffer<double> zp, zc;
@@ -94,7 +86,7 @@ class PcmEngine {
   void flush_slots();          // upload defaults / initial poses of new slots
   void ensure_traj_capacity(size_t n);
   TrajView view() const;
-  void run_pairwise(Group& g, int old_n);
+  void run_pairwise(Group& g, int old_n, const FactorStore& store);
   void find_inliers();
   void find_inliers_incremental(const std::unordered_map<ObsId, size_t, ObsIdHash>& num_new);
 
@@ -105,7 +97,8 @@ class PcmEngine {
   std::unordered_map<uint64_t, int32_t> slots_;
   int32_t num_slots_ = 0;
   size_t traj_cap_ = 0;
-  std::vector<std::pair<int32_t, std::vector<double>>> pending_init_;  // slot -> pose (cov zero)
+  std::vector<std::pair<int32_t, int64_t>> pending_init_;  // slot <- value row (cov zero)
+  const ValueStore* values_ = nullptr;
   std::vector<int32_t> pending_default_;
   DeviceBuffer<double> traj_pose_, traj_cov_;
   DeviceBuffer<int32_t> traj_node_;
@@ -116,6 +109,7 @@ class PcmEngine {
   size_t total_lc_ = 0, total_good_lc_ = 0;
   // scratch
   DeviceBuffer<int32_t> d_src_, d_dst_;
+  DeviceBuffer<int64_t> d_rows_;
   DeviceBuffer<double> d_dpose_, d_dcov_, scratch_rec_, scratch_cov_;
   DeviceBuffer<uint8_t> scratch_rot_, d_ok_;
   DeviceBuffer<uint32_t> lower_scratch_;

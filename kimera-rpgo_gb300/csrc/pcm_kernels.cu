@@ -513,6 +513,7 @@ void launch_pairwise(int dim, int mode, int n, int row_begin, const int32_t* sa,
   const int rows = n - row_begin;
   dim3 block(32, ROWS), grid(div_up(n, 32), div_up(rows, ROWS));
   if (n > 1) {
+    EventTimer timer(st);
     if (dim == 3) {
       if (mode == 0)
         k_pairwise<3, PWC<3>, ROWS><<<grid, block, 0, st>>>(n, row_begin, sa, sb, flip, zp, zc, tr, th0, th1,
@@ -529,6 +530,8 @@ void launch_pairwise(int dim, int mode, int n, int row_begin, const int32_t* sa,
                                                             lower_scratch, words);
     }
     RPGO_LAUNCHED();
+    kernel_times().pair_ms += timer.elapsed_ms();
+    kernel_times().pair_launches += 1;
   }
   // rows whose tiles were all skipped (j < 32*bx) keep stale words; the
   // ballot writes only tiles with i0 < j, so clear the rest first: the
@@ -544,6 +547,10 @@ void launch_pairwise(int dim, int mode, int n, int row_begin, const int32_t* sa,
 std::atomic<int64_t>& launch_counter() {
   static std::atomic<int64_t> c{0};
   return c;
+}
+KernelTimes& kernel_times() {
+  static KernelTimes t;
+  return t;
 }
 
 }  // namespace rpgo

@@ -9,44 +9,46 @@
 
 namespace rpgo {
 
-GpuNls::GpuNls(int dim, const std::vector<FactorRec>& graph, const Values& values, cudaStream_t st)
+GpuNls::GpuNls(int dim, const std::vector<FactorRec>& graph, const FactorStore& store, const ValueStore& values,
+               cudaStream_t st)
     : dim_(dim), st_(st) {
   const int stride = dim == 3 ? 12 : 4, d = dim == 3 ? 6 : 3;
   std::map<uint64_t, int> index;
-  std::vector<double> x0;
-  x0.reserve(values.size() * stride);
-  for (const auto& kv : values) {
+  std::vector<int64_t> vrows;
+  vrows.reserve(values.size());
+  for (const auto& kv : values.rows()) {
     index[kv.first] = (int)keys_.size();
     keys_.push_back(kv.first);
-    x0.insert(x0.end(), kv.second.begin(), kv.second.end());
+    vrows.push_back(kv.second);
   }
   const size_t F = graph.size();
   std::vector<int32_t> kind(F), vi(F), vj(F);
-  std::vector<double> z(F * stride), R(F * d * d);
+  std::vector<int64_t> frows(F);
   for (size_t f = 0; f < F; ++f) {
     const FactorRec& r = graph[f];
     kind[f] = r.kind;
     vi[f] = index.at(r.k1);
     vj[f] = r.kind == 0 ? index.at(r.k2) : vi[f];
-    std::memcpy(&z[f * stride], r.meas, sizeof(double) * stride);
-    std::memcpy(&R[f * d * d], r.sqrt_info, sizeof(double) * d * d);
+    frows[f] = r.row;
   }
-  solver_upload(s_, dim, kind, vi, vj, z, R, x0, (int)keys_.size(), st_);
+  solver_upload(s_, dim, kind, vi, vj, (int)keys_.size(), st_);
+  DeviceBuffer<int64_t> fr;
+  fr.upload(frows, st_);
+  value_rows_.upload(vrows, st_);
+  gather_rows((int64_t)F, fr.get(), store.meas(), stride, s_.z.get(), st_);
+  gather_rows((int64_t)F, fr.get(), store.sqrt_info(), d * d, s_.sqrt_info.get(), st_);
+  gather_rows((int64_t)vrows.size(), value_rows_.get(), values.pose(), stride, s_.x0.get(), st_);
   set_weights(std::vector<double>(F, 1.0));
+  RPGO_CUDA(cudaStreamSynchronize(st_));
 }
 
 void GpuNls::set_weights(const std::vector<double>& w) { s_.weights.upload(w, st_); }
 
 double GpuNls::error_at_result() { return solver_error(s_, s_.x.get(), s_.weights.get(), st_); }
 
-void GpuNls::result(Values* out) const {
-  const int stride = dim_ == 3 ? 12 : 4;
-  std::vector<double> x(keys_.size() * stride);
-  s_.x.download(x.data(), x.size(), st_);
+void GpuNls::write_back(ValueStore& values) const {
+  scatter_rows((int64_t)keys_.size(), value_rows_.get(), s_.x.get(), dim_ == 3 ? 12 : 4, values.pose(), st_);
   RPGO_CUDA(cudaStreamSynchronize(st_));
-  out->clear();
-  for (size_t i = 0; i < keys_.size(); ++i)
-    (*out)[keys_[i]] = std::vector<double>(x.begin() + i * stride, x.begin() + (i + 1) * stride);
 }
 
 // NonlinearOptimizer::defaultOptimize with LevenbergMarquardtOptimizer::iterate

@@ -35,12 +35,16 @@ struct NlsStats {
 
 class GpuNls {
  public:
-  GpuNls(int dim, const std::vector<FactorRec>& graph, const Values& values, cudaStream_t st);
+  // structure from the host factor list; measurements, square-root
+  // informations and initial values gathered on the device from the stores
+  GpuNls(int dim, const std::vector<FactorRec>& graph, const FactorStore& store, const ValueStore& values,
+         cudaStream_t st);
   void set_weights(const std::vector<double>& w);
   // LM / GN from the initial values; result left in dev().x
   void optimize(const LmParams& p, NlsStats* st);
   double error_at_result();
-  void result(Values* out) const;
+  // GenericSolver::updateValues: write the result back into the value rows
+  void write_back(ValueStore& values) const;
   SolverDev& dev() { return s_; }
   cudaStream_t stream() const { return st_; }
   const std::vector<uint64_t>& keys() const { return keys_; }
@@ -50,6 +54,7 @@ class GpuNls {
   cudaStream_t st_;
   SolverDev s_;
   std::vector<uint64_t> keys_;
+  DeviceBuffer<int64_t> value_rows_;  // value-store row of each variable (key order)
 };
 
 double chi2inv(double alpha, int dof);

@@ -15,6 +15,8 @@
 //                    also the linearised cost change -g.d - d^T H d / 2 (FP64).
 //  retract / error   X <- X Expmap(delta); per-factor 0.5 w |R e|^2 (FP64).
 //  K6 GNC weights    TLS weights of GncOptimizer::calculateWeights (FP64).
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cmath>
 
@@ -645,17 +647,23 @@ __global__ void __launch_bounds__(kCta) k_pcg(int N, CsrView A, double lam, cons
                                               float* __restrict__ cz, double* __restrict__ r,
                                               double* __restrict__ z, double* __restrict__ zo,
                                               double* __restrict__ p, double* __restrict__ q,
-                                              double* __restrict__ delta, PcgParams prm, double* __restrict__ out) {
+                                              double* __restrict__ delta, PcgParams prm, int warm,
+                                              double* __restrict__ out) {
   __shared__ double sh[40];
   const int n = N * D;
   double loc = 0.0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    delta[k] = 0.0;
-    r[k] = -g[k];
-    loc += g[k] * g[k];
-    cr[k] = (float)(-g[k]);
-  }
+  for (int k = threadIdx.x; k < n; k += blockDim.x) loc += g[k] * g[k];
   const double bnorm = sqrt(cta_sum(loc, sh));
+  if (warm) {
+    spmv_d<D>(N, A, lam, delta, q);
+  }
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    if (!warm) delta[k] = 0.0;
+    const double rk = warm ? (-g[k] - q[k]) : -g[k];
+    r[k] = rk;
+    cr[k] = (float)rk;
+  }
+  __syncthreads();
   int it = 0, ok = 1;
   double rel = 0.0;
   if (bnorm > 0.0) {
@@ -724,6 +732,177 @@ __global__ void __launch_bounds__(kCta) k_pcg(int N, CsrView A, double lam, cons
   }
 }
 
+// FP32 preconditioned CG on (H + lam D) c = rhs (rhs in cr, solution in cx);
+// out[4] iterations, out[5] ok. One CTA: at the sizes of a single pose graph
+// the inner loop is bound by synchronisation, not arithmetic.
+template <int D>
+__global__ void __launch_bounds__(kCta) k_pcg32(int N, CsrView A, double lam, int levels,
+                                                const int32_t* __restrict__ lvl_off, const int32_t* __restrict__ lvl_n,
+                                                const float* __restrict__ bDinv, const float* __restrict__ bFL,
+                                                const float* __restrict__ bFR, float* __restrict__ bb,
+                                                float* __restrict__ bx, float* __restrict__ cr, float* __restrict__ cz,
+                                                float* __restrict__ cp, float* __restrict__ cq, float* __restrict__ cx,
+                                                double tol, int max_it, double* __restrict__ out) {
+  __shared__ double sh[40];
+  const int n = N * D;
+  double lb = 0.0;
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    cx[k] = 0.f;
+    lb += (double)cr[k] * cr[k];
+  }
+  const double bn = sqrt(cta_sum(lb, sh));
+  int it = 0, ok = 1;
+  if (bn > 0.0) {
+    bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
+    double loc = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      cp[k] = cz[k];
+      loc += (double)cr[k] * cz[k];
+    }
+    double rz = cta_sum(loc, sh);
+    for (; it < max_it; ++it) {
+      spmv_f<D>(N, A, lam, cp, cq);
+      loc = 0.0;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) loc += (double)cp[k] * cq[k];
+      const double pq = cta_sum(loc, sh);
+      if (!(pq > 0.0) || !(rz > 0.0)) {
+        if (it == 0) ok = 0;
+        break;
+      }
+      const float alpha = (float)(rz / pq);
+      loc = 0.0;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        cx[k] += alpha * cp[k];
+        const float rk = cr[k] - alpha * cq[k];
+        cr[k] = rk;
+        loc += (double)rk * rk;
+      }
+      if (sqrt(cta_sum(loc, sh)) <= tol * bn) {
+        ++it;
+        break;
+      }
+      bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
+      loc = 0.0;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) loc += (double)cr[k] * cz[k];
+      const double rzn = cta_sum(loc, sh);
+      const float beta = (float)(rzn / rz);
+      rz = rzn;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) cp[k] = cz[k] + beta * cp[k];
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0) {
+    out[4] = it;
+    out[5] = ok;
+  }
+}
+
+// delta += c (FP32 correction), then r64 = -g - (H + lam D) delta with the
+// FP64 blocks; writes rhs32 = r64 and the per-row squared norm. All SMs.
+template <int D>
+__global__ void k_refine_residual(int N, CsrView A, double lam, const double* __restrict__ g,
+                                  const float* __restrict__ c, int add_c, double* __restrict__ delta,
+                                  float* __restrict__ rhs32, double* __restrict__ rowsq) {
+  constexpr int dd = D * D;
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= N) return;
+  (void)dd;
+  // the correction of this row must be applied before any row reads it: done
+  // by a separate launch (k_add_correction); here delta is final.
+  double acc[D];
+  const double* H = A.Hd64 + (size_t)v * dd;
+  const double* pv = delta + (size_t)v * D;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    double sacc = lam * A.dampD[(size_t)v * D + a] * pv[a];
+#pragma unroll
+    for (int q = 0; q < D; ++q) sacc += H[D * a + q] * pv[q];
+    acc[a] = sacc;
+  }
+  for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
+    const double* B = A.fH64 + (size_t)A.blk[k] * 3 * dd + 2 * dd;
+    const double* pc = delta + (size_t)A.col[k] * D;
+    if (A.btr[k]) {
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int q = 0; q < D; ++q) acc[a] += B[D * q + a] * pc[q];
+    } else {
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int q = 0; q < D; ++q) acc[a] += B[D * a + q] * pc[q];
+    }
+  }
+  double sq = 0.0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    const double r = -g[(size_t)v * D + a] - acc[a];
+    rhs32[(size_t)v * D + a] = (float)r;
+    sq += r * r;
+  }
+  rowsq[v] = sq;
+  (void)c;
+  (void)add_c;
+}
+
+__global__ void k_add_correction(int n, const float* __restrict__ c, double* __restrict__ delta) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) delta[k] += (double)c[k];
+}
+
+__global__ void k_init_rhs(int n, const double* __restrict__ g, double* __restrict__ delta, float* __restrict__ rhs32,
+                           double* __restrict__ sq) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) {
+    delta[k] = 0.0;
+    rhs32[k] = (float)(-g[k]);
+    sq[k] = g[k] * g[k];
+  }
+}
+
+// per row: g.delta and delta.(H delta) with the undamped FP64 blocks
+template <int D>
+__global__ void k_lin_terms(int N, CsrView A, const double* __restrict__ g, const double* __restrict__ delta,
+                            double* __restrict__ gd, double* __restrict__ dhd) {
+  constexpr int dd = D * D;
+  const int v = blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= N) return;
+  double acc[D];
+  const double* H = A.Hd64 + (size_t)v * dd;
+  const double* pv = delta + (size_t)v * D;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    double sacc = 0.0;
+#pragma unroll
+    for (int q = 0; q < D; ++q) sacc += H[D * a + q] * pv[q];
+    acc[a] = sacc;
+  }
+  for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
+    const double* B = A.fH64 + (size_t)A.blk[k] * 3 * dd + 2 * dd;
+    const double* pc = delta + (size_t)A.col[k] * D;
+    if (A.btr[k]) {
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int q = 0; q < D; ++q) acc[a] += B[D * q + a] * pc[q];
+    } else {
+#pragma unroll
+      for (int a = 0; a < D; ++a)
+#pragma unroll
+        for (int q = 0; q < D; ++q) acc[a] += B[D * a + q] * pc[q];
+    }
+  }
+  double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+  for (int a = 0; a < D; ++a) {
+    s1 += g[(size_t)v * D + a] * pv[a];
+    s2 += pv[a] * acc[a];
+  }
+  gd[v] = s1;
+  dhd[v] = s2;
+}
+
 template <int DIM>
 __global__ void k_retract(int N, const double* __restrict__ x, const double* __restrict__ delta,
                           double* __restrict__ xnew) {
@@ -759,8 +938,7 @@ __global__ void k_gnc_weights(int F, int n_known, const double* __restrict__ u2,
 
 // ------------------------------------------------------------------ host wrappers
 void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
-                   const std::vector<int32_t>& vj, const std::vector<double>& z, const std::vector<double>& sqrt_info,
-                   const std::vector<double>& x0, int N, cudaStream_t st) {
+                   const std::vector<int32_t>& vj, int N, cudaStream_t st) {
   s.dim = dim;
   s.d = dim == 3 ? 6 : 3;
   s.stride = dim == 3 ? 12 : 4;
@@ -816,8 +994,8 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   s.vj.upload(vj, st);
   s.tree.upload(tree, st);
   s.var_has_tree.upload(has_tree, st);
-  s.z.upload(z, st);
-  s.sqrt_info.upload(sqrt_info, st);
+  s.z.resize((size_t)F * s.stride);
+  s.sqrt_info.resize((size_t)F * dd);
   s.inc_ptr.upload(inc_ptr, st);
   s.inc_fac.upload(inc_fac, st);
   s.inc_role.upload(inc_role, st);
@@ -825,9 +1003,9 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   s.col.upload(col, st);
   s.blk.upload(blk, st);
   s.btr.upload(btr, st);
-  s.x0.upload(x0, st);
-  s.x.resize(x0.size());
-  s.xnew.resize(x0.size());
+  s.x0.resize((size_t)N * s.stride);
+  s.x.resize((size_t)N * s.stride);
+  s.xnew.resize((size_t)N * s.stride);
   s.weights.resize(F);
   s.fH.resize((size_t)F * 3 * dd);
   s.fH64.resize((size_t)F * 3 * dd);
@@ -862,8 +1040,7 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   s.bFR.resize(nodes * dd);
   s.bb.resize(nodes * d);
   s.bx.resize(nodes * d);
-  s.cr.resize((size_t)N * d);
-  s.cz.resize((size_t)N * d);
+  for (auto* b : {&s.cr, &s.cz, &s.cp, &s.cq, &s.cx}) b->resize((size_t)N * d);
   for (auto* b : {&s.r64, &s.z64, &s.zo64, &s.p64, &s.q64}) b->resize((size_t)N * d);
   s.out.resize(8);
 }
@@ -924,37 +1101,429 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
   RPGO_LAUNCHED();
 }
 
+// ------------------------------------------------------------------ K5, whole-GPU form
+// One cooperative launch (one CTA per SM, grid-wide barriers) runs the
+// complete flexible PCG: FP64 vectors and FP64 block SpMV spread over every
+// SM (GB300's FP64 rate per SM is a small fraction of its FP32 rate, so FP64
+// work must use all SMs), the block cyclic reduction preconditioner in FP32
+// with the large levels spread over the grid and the small top levels done by
+// CTA 0 alone. All branch decisions come from grid-reduced values every CTA
+// reads after the same barrier, so every CTA passes the same barriers.
+namespace cg = cooperative_groups;
+
+struct CoopArgs {
+  int N, levels, top;
+  const int32_t* lvl_off;
+  const int32_t* lvl_n;
+  CsrView A;
+  double lam;
+  const double* g;
+  const float* Md;
+  const float* Mu;
+  float *bD, *bDinv, *bU, *bFL, *bFR, *bb, *bx;
+  double *r, *z, *zo, *p, *q, *delta;
+  float* cr;
+  double* part;  // 4 x gridDim.x
+  double tol;
+  int max_it;
+  double* out;
+};
+
+__device__ __forceinline__ double grid_sum(double v, double* part, int slot, double* sh, cg::grid_group& grid) {
+  v = cta_sum(v, sh);
+  if (threadIdx.x == 0) part[slot * gridDim.x + blockIdx.x] = v;
+  grid.sync();
+  double t = 0.0;
+  for (int b = 0; b < (int)gridDim.x; ++b) t += part[slot * gridDim.x + b];  // same order in every CTA
+  return t;
+}
+
+template <int D>
+__device__ void bcr_level_factor_odd(const CoopArgs& a, int l, int t0, int tstride) {
+  constexpr int dd = D * D;
+  const int base = a.lvl_off[l], n = a.lvl_n[l];
+  for (int o = 1 + 2 * t0; o < n; o += 2 * tstride)
+    spd_inv_f<D>(a.bD + (size_t)(base + o) * dd, a.bDinv + (size_t)(base + o) * dd);
+}
+template <int D>
+__device__ void bcr_level_factor_even(const CoopArgs& a, int l, int t0, int tstride) {
+  constexpr int dd = D * D;
+  const int base = a.lvl_off[l], n = a.lvl_n[l], nbase = a.lvl_off[l + 1];
+  for (int i = 2 * t0; i < n; i += 2 * tstride) {
+    float FL[dd], FR[dd], Dn[dd], T[dd], Un[dd];
+    const float* Di = a.bD + (size_t)(base + i) * dd;
+#pragma unroll
+    for (int k = 0; k < dd; ++k) {
+      Dn[k] = Di[k];
+      Un[k] = 0.f;
+      FL[k] = 0.f;
+      FR[k] = 0.f;
+    }
+    if (i >= 1) {
+      const float* Ul = a.bU + (size_t)(base + i - 1) * dd;
+      mm_f<D>(Ul, a.bDinv + (size_t)(base + i - 1) * dd, FL, true, false);
+      mm_f<D>(FL, Ul, T);
+#pragma unroll
+      for (int k = 0; k < dd; ++k) Dn[k] -= T[k];
+    }
+    if (i + 1 < n) {
+      const float* Ur = a.bU + (size_t)(base + i) * dd;
+      mm_f<D>(Ur, a.bDinv + (size_t)(base + i + 1) * dd, FR);
+      mm_f<D>(FR, Ur, T, false, true);
+#pragma unroll
+      for (int k = 0; k < dd; ++k) Dn[k] -= T[k];
+      if (i + 2 < n) {
+        mm_f<D>(FR, a.bU + (size_t)(base + i + 1) * dd, T);
+#pragma unroll
+        for (int k = 0; k < dd; ++k) Un[k] = -T[k];
+      }
+    }
+#pragma unroll
+    for (int x = 0; x < D; ++x)
+#pragma unroll
+      for (int y = 0; y < x; ++y) {
+        const float sv = 0.5f * (Dn[D * x + y] + Dn[D * y + x]);
+        Dn[D * x + y] = sv;
+        Dn[D * y + x] = sv;
+      }
+#pragma unroll
+    for (int k = 0; k < dd; ++k) {
+      a.bFL[(size_t)(base + i) * dd + k] = FL[k];
+      a.bFR[(size_t)(base + i) * dd + k] = FR[k];
+      a.bD[(size_t)(nbase + i / 2) * dd + k] = Dn[k];
+      a.bU[(size_t)(nbase + i / 2) * dd + k] = Un[k];
+    }
+  }
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) k_bcr_factor_coop(CoopArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  constexpr int dd = D * D;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  for (int v = gt; v < a.N; v += gs) {
+#pragma unroll
+    for (int k = 0; k < dd; ++k) {
+      a.bD[(size_t)v * dd + k] = a.Md[(size_t)v * dd + k];
+      a.bU[(size_t)v * dd + k] = (v + 1 < a.N) ? a.Mu[(size_t)v * dd + k] : 0.f;
+    }
+#pragma unroll
+    for (int x = 0; x < D; ++x) a.bD[(size_t)v * dd + D * x + x] += (float)(a.lam * a.A.dampD[(size_t)v * D + x]);
+  }
+  grid.sync();
+  for (int l = 0; l < a.top; ++l) {
+    bcr_level_factor_odd<D>(a, l, gt, gs);
+    grid.sync();
+    bcr_level_factor_even<D>(a, l, gt, gs);
+    grid.sync();
+  }
+  if (blockIdx.x == 0) {
+    for (int l = a.top; l < a.levels; ++l) {
+      const int n = a.lvl_n[l];
+      if (n == 1) {
+        if (threadIdx.x == 0) spd_inv_f<D>(a.bD + (size_t)a.lvl_off[l] * dd, a.bDinv + (size_t)a.lvl_off[l] * dd);
+        break;
+      }
+      bcr_level_factor_odd<D>(a, l, threadIdx.x, blockDim.x);
+      __syncthreads();
+      bcr_level_factor_even<D>(a, l, threadIdx.x, blockDim.x);
+      __syncthreads();
+    }
+  }
+}
+
+template <int D>
+__device__ __forceinline__ float* lvl_b(const CoopArgs& a, int l) {
+  return l == 0 ? a.cr : a.bb + (size_t)a.lvl_off[l] * D;
+}
+template <int D>
+__device__ void bcr_fwd_level(const CoopArgs& a, int l, int t0, int ts) {
+  constexpr int dd = D * D;
+  const int base = a.lvl_off[l], n = a.lvl_n[l];
+  const float* b = lvl_b<D>(a, l);
+  float* bn = lvl_b<D>(a, l + 1);
+  for (int i = 2 * t0; i < n; i += 2 * ts) {
+    float o[D];
+#pragma unroll
+    for (int x = 0; x < D; ++x) o[x] = b[(size_t)i * D + x];
+    if (i >= 1) {
+      const float* F = a.bFL + (size_t)(base + i) * dd;
+#pragma unroll
+      for (int x = 0; x < D; ++x)
+#pragma unroll
+        for (int c = 0; c < D; ++c) o[x] -= F[D * x + c] * b[(size_t)(i - 1) * D + c];
+    }
+    if (i + 1 < n) {
+      const float* F = a.bFR + (size_t)(base + i) * dd;
+#pragma unroll
+      for (int x = 0; x < D; ++x)
+#pragma unroll
+        for (int c = 0; c < D; ++c) o[x] -= F[D * x + c] * b[(size_t)(i + 1) * D + c];
+    }
+#pragma unroll
+    for (int x = 0; x < D; ++x) bn[(size_t)(i / 2) * D + x] = o[x];
+  }
+}
+// backward level l: x_l from x_{l+1}; at level 0 also writes z (FP64)
+template <int D>
+__device__ void bcr_bwd_level(const CoopArgs& a, int l, int t0, int ts) {
+  constexpr int dd = D * D;
+  const int base = a.lvl_off[l], n = a.lvl_n[l], nbase = a.lvl_off[l + 1];
+  const float* b = lvl_b<D>(a, l);
+  for (int i = t0; i < n; i += ts) {
+    float o[D];
+    if ((i & 1) == 0) {
+#pragma unroll
+      for (int x = 0; x < D; ++x) o[x] = a.bx[(size_t)(nbase + i / 2) * D + x];
+    } else {
+      const float* Di = a.bDinv + (size_t)(base + i) * dd;
+#pragma unroll
+      for (int x = 0; x < D; ++x) {
+        float acc = 0.f;
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc += Di[D * x + c] * b[(size_t)i * D + c];
+        o[x] = acc;
+      }
+      {
+        const float* F = a.bFR + (size_t)(base + i - 1) * dd;
+        const float* xl = a.bx + (size_t)(nbase + (i - 1) / 2) * D;
+#pragma unroll
+        for (int x = 0; x < D; ++x)
+#pragma unroll
+          for (int c = 0; c < D; ++c) o[x] -= F[D * c + x] * xl[c];
+      }
+      if (i + 1 < n) {
+        const float* F = a.bFL + (size_t)(base + i + 1) * dd;
+        const float* xr = a.bx + (size_t)(nbase + (i + 1) / 2) * D;
+#pragma unroll
+        for (int x = 0; x < D; ++x)
+#pragma unroll
+          for (int c = 0; c < D; ++c) o[x] -= F[D * c + x] * xr[c];
+      }
+    }
+    if (l == 0) {
+#pragma unroll
+      for (int x = 0; x < D; ++x) a.z[(size_t)i * D + x] = (double)o[x];
+    } else {
+#pragma unroll
+      for (int x = 0; x < D; ++x) a.bx[(size_t)(base + i) * D + x] = o[x];
+    }
+  }
+}
+// z = M^-1 r with r already in a.cr (all CTAs must call)
+template <int D>
+__device__ void precond_grid(const CoopArgs& a, cg::grid_group& grid) {
+  constexpr int dd = D * D;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  for (int l = 0; l < a.top; ++l) {
+    bcr_fwd_level<D>(a, l, gt, gs);
+    grid.sync();
+  }
+  if (blockIdx.x == 0) {
+    int l = a.top;
+    for (; l < a.levels && a.lvl_n[l] > 1; ++l) {
+      bcr_fwd_level<D>(a, l, threadIdx.x, blockDim.x);
+      __syncthreads();
+    }
+    const int base = a.lvl_off[l];
+    const float* bc = lvl_b<D>(a, l);
+    if (threadIdx.x < D) {
+      const int x = threadIdx.x;
+      float acc = 0.f;
+      for (int c = 0; c < D; ++c) acc += a.bDinv[(size_t)base * dd + D * x + c] * bc[c];
+      if (l == 0) a.z[x] = (double)acc;
+      else a.bx[(size_t)base * D + x] = acc;
+    }
+    __syncthreads();
+    for (--l; l >= a.top; --l) {
+      bcr_bwd_level<D>(a, l, threadIdx.x, blockDim.x);
+      __syncthreads();
+    }
+  }
+  grid.sync();
+  for (int l = a.top - 1; l >= 0; --l) {
+    bcr_bwd_level<D>(a, l, gt, gs);
+    grid.sync();
+  }
+}
+
+template <int D>
+__device__ void spmv_grid(const CsrView& A, int N, double lam, const double* p, double* y) {
+  constexpr int dd = D * D;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  for (int v = gt; v < N; v += gs) {
+    double acc[D];
+    const double* H = A.Hd64 + (size_t)v * dd;
+    const double* pv = p + (size_t)v * D;
+#pragma unroll
+    for (int x = 0; x < D; ++x) {
+      double sacc = lam * A.dampD[(size_t)v * D + x] * pv[x];
+#pragma unroll
+      for (int c = 0; c < D; ++c) sacc += H[D * x + c] * pv[c];
+      acc[x] = sacc;
+    }
+    for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
+      const double* B = A.fH64 + (size_t)A.blk[k] * 3 * dd + 2 * dd;
+      const double* pc = p + (size_t)A.col[k] * D;
+      if (A.btr[k]) {
+#pragma unroll
+        for (int x = 0; x < D; ++x)
+#pragma unroll
+          for (int c = 0; c < D; ++c) acc[x] += B[D * c + x] * pc[c];
+      } else {
+#pragma unroll
+        for (int x = 0; x < D; ++x)
+#pragma unroll
+          for (int c = 0; c < D; ++c) acc[x] += B[D * x + c] * pc[c];
+      }
+    }
+#pragma unroll
+    for (int x = 0; x < D; ++x) y[(size_t)v * D + x] = acc[x];
+  }
+}
+
+// out[0] lin_change, [1] ok, [2] iterations, [3] relative residual
+template <int D>
+__global__ void __launch_bounds__(256) k_pcg_coop(CoopArgs a) {
+  cg::grid_group grid = cg::this_grid();
+  __shared__ double sh[40];
+  const int n = a.N * D;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  double loc = 0.0;
+  for (int k = gt; k < n; k += gs) {
+    const double rk = -a.g[k];
+    a.delta[k] = 0.0;
+    a.r[k] = rk;
+    a.cr[k] = (float)rk;
+    loc += rk * rk;
+  }
+  const double bnorm = sqrt(grid_sum(loc, a.part, 0, sh, grid));
+  int it = 0, ok = 1;
+  double rel = 0.0;
+  if (bnorm > 0.0) {
+    precond_grid<D>(a, grid);
+    loc = 0.0;
+    for (int k = gt; k < n; k += gs) {
+      a.p[k] = a.z[k];
+      loc += a.r[k] * a.z[k];
+    }
+    double rz = grid_sum(loc, a.part, 1, sh, grid);  // also orders the p writes
+    for (; it < a.max_it; ++it) {
+      spmv_grid<D>(a.A, a.N, a.lam, a.p, a.q);
+      grid.sync();
+      loc = 0.0;
+      for (int k = gt; k < n; k += gs) loc += a.p[k] * a.q[k];
+      const double pq = grid_sum(loc, a.part, 2, sh, grid);
+      if (!(pq > 0.0) || !(rz > 0.0)) {
+        if (it == 0) ok = 0;
+        break;
+      }
+      const double alpha = rz / pq;
+      loc = 0.0;
+      for (int k = gt; k < n; k += gs) {
+        a.delta[k] += alpha * a.p[k];
+        const double rk = a.r[k] - alpha * a.q[k];
+        a.r[k] = rk;
+        a.cr[k] = (float)rk;
+        a.zo[k] = a.z[k];
+        loc += rk * rk;
+      }
+      rel = sqrt(grid_sum(loc, a.part, 3, sh, grid)) / bnorm;
+      if (rel <= a.tol) {
+        ++it;
+        break;
+      }
+      precond_grid<D>(a, grid);
+      double rzn = 0.0, rzo = 0.0;
+      for (int k = gt; k < n; k += gs) {
+        rzn += a.r[k] * a.z[k];
+        rzo += a.r[k] * a.zo[k];
+      }
+      rzn = grid_sum(rzn, a.part, 0, sh, grid);
+      rzo = grid_sum(rzo, a.part, 1, sh, grid);
+      const double beta = (rzn - rzo) / rz;
+      rz = rzn;
+      for (int k = gt; k < n; k += gs) a.p[k] = a.z[k] + beta * a.p[k];
+      grid.sync();
+    }
+  }
+  // linearised cost change with the undamped H
+  spmv_grid<D>(a.A, a.N, 0.0, a.delta, a.q);
+  grid.sync();
+  double gd = 0.0, dhd = 0.0;
+  for (int k = gt; k < n; k += gs) {
+    gd += a.g[k] * a.delta[k];
+    dhd += a.delta[k] * a.q[k];
+  }
+  gd = grid_sum(gd, a.part, 2, sh, grid);
+  dhd = grid_sum(dhd, a.part, 3, sh, grid);
+  if (gt == 0) {
+    a.out[0] = -gd - 0.5 * dhd;
+    a.out[1] = ok;
+    a.out[2] = it;
+    a.out[3] = rel;
+  }
+}
+
+// (H + lambda D) delta = -g with the whole-GPU flexible PCG (k_pcg_coop).
 SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
   SolveOut o;
   if (s.N == 0) {
     o.ok = 1;
     return o;
   }
-  CsrView A{s.Hd.get(), s.fH.get(), s.Hd64.get(), s.fH64.get(), s.row_ptr.get(), s.col.get(), s.blk.get(), s.btr.get(), s.dampD.get()};
-  PcgParams prm{1e-12, 5000};
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    RPGO_CUDA(cudaGetDevice(&dev));
+    RPGO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int grid = sms, threads = 256;
+  s.part.resize((size_t)4 * grid);
+  CsrView A{s.Hd.get(), s.fH.get(), s.Hd64.get(), s.fH64.get(), s.row_ptr.get(), s.col.get(), s.blk.get(),
+            s.btr.get(), s.dampD.get()};
+  int top = 0;
+  while (top < s.levels - 1 && s.lvl_n[top] > 1024) ++top;
+  CoopArgs a{s.N, s.levels, top, s.d_lvl_off.get(), s.d_lvl_n.get(), A, lambda, s.g.get(), s.Md.get(), s.Mu.get(),
+             s.bD.get(), s.bDinv.get(), s.bU.get(), s.bFL.get(), s.bFR.get(), s.bb.get(), s.bx.get(), s.r64.get(),
+             s.z64.get(), s.zo64.get(), s.p64.get(), s.q64.get(), s.delta.get(), s.cr.get(), s.part.get(), 1e-12,
+             5000, s.out.get()};
+  void* args[] = {&a};
   if (s.dim == 3) {
-    k_bcr_factor<6><<<1, kCta, 0, st>>>(s.N, s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(), s.Md.get(), s.Mu.get(),
-                                        s.dampD.get(), lambda, s.bD.get(), s.bDinv.get(), s.bU.get(), s.bFL.get(),
-                                        s.bFR.get());
-    RPGO_LAUNCHED();
-    k_pcg<6><<<1, kCta, 0, st>>>(s.N, A, lambda, s.g.get(), s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(),
-                                 s.bDinv.get(), s.bFL.get(), s.bFR.get(), s.bb.get(), s.bx.get(), s.cr.get(),
-                                 s.cz.get(), s.r64.get(), s.z64.get(), s.zo64.get(), s.p64.get(), s.q64.get(),
-                                 s.delta.get(), prm, s.out.get());
+    RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_bcr_factor_coop<6>, grid, threads, args, 0, st));
   } else {
-    k_bcr_factor<3><<<1, kCta, 0, st>>>(s.N, s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(), s.Md.get(), s.Mu.get(),
-                                        s.dampD.get(), lambda, s.bD.get(), s.bDinv.get(), s.bU.get(), s.bFL.get(),
-                                        s.bFR.get());
-    RPGO_LAUNCHED();
-    k_pcg<3><<<1, kCta, 0, st>>>(s.N, A, lambda, s.g.get(), s.levels, s.d_lvl_off.get(), s.d_lvl_n.get(),
-                                 s.bDinv.get(), s.bFL.get(), s.bFR.get(), s.bb.get(), s.bx.get(), s.cr.get(),
-                                 s.cz.get(), s.r64.get(), s.z64.get(), s.zo64.get(), s.p64.get(), s.q64.get(),
-                                 s.delta.get(), prm, s.out.get());
+    RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_bcr_factor_coop<3>, grid, threads, args, 0, st));
   }
   RPGO_LAUNCHED();
+  double pcg_ms = 0.0;
+  {
+    EventTimer timer(st);
+    if (s.dim == 3)
+      RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_pcg_coop<6>, grid, threads, args, 0, st));
+    else
+      RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_pcg_coop<3>, grid, threads, args, 0, st));
+    RPGO_LAUNCHED();
+    pcg_ms = timer.elapsed_ms();
+  }
   double h[4];
   RPGO_CUDA(cudaMemcpyAsync(h, s.out.get(), sizeof(h), cudaMemcpyDeviceToHost, st));
   RPGO_CUDA(cudaStreamSynchronize(st));
+  {
+    // algorithmic bytes of one CG iteration: FP64 block SpMV (diagonal and
+    // off-diagonal blocks, indices, vectors), the FP64 vector updates and
+    // dot products, and one FP32 cyclic-reduction apply over all levels
+    const double d = s.d, dd = d * d, Nn = s.N, nnz = (double)s.col.size(), n = Nn * d;
+    double bcr = 0.0;
+    for (int l = 0; l < s.levels; ++l) {
+      const double nl = s.lvl_n[l];
+      bcr += 0.5 * nl * (2 * dd * 4 + 4 * d * 4) + 0.5 * nl * (2 * d * 4) + 0.5 * nl * (3 * dd * 4 + 5 * d * 4);
+    }
+    const double spmv = 8 * dd * (Nn + nnz) + 8 * d * (2 * Nn + nnz) + 9 * nnz;
+    const double vec = 8 * n * 16 + 4 * n;
+    kernel_times().pcg_ms += pcg_ms;
+    kernel_times().pcg_launches += 1;
+    kernel_times().pcg_bytes += (h[2] + 1.0) * (spmv + vec + bcr);
+  }
   o.lin_change = h[0];
   o.ok = (int)h[1];
   o.cg_iterations = (int)h[2];

@@ -40,7 +40,9 @@ struct SolverDev {
   std::vector<int32_t> lvl_off, lvl_n;
   DeviceBuffer<int32_t> d_lvl_off, d_lvl_n;
   DeviceBuffer<float> bD, bDinv, bU, bFL, bFR, bb, bx;  // per level node
-  DeviceBuffer<float> cr, cz;                           // N x d, preconditioner input / output
+  DeviceBuffer<float> cr, cz, cp, cq, cx;               // N x d, FP32 CG vectors
+  DeviceBuffer<double> rowtmp;                          // per-row reduction terms
+  DeviceBuffer<double> part;                            // per-CTA partial sums
   DeviceBuffer<double> r64, z64, zo64, p64, q64;        // N x d, CG vectors
   DeviceBuffer<double> out;                              // solve outputs
   int levels = 0;
@@ -53,10 +55,10 @@ struct SolveOut {
   double rel_residual = 0.0;
 };
 
-// setup: host arrays -> device (structure is built here)
+// setup: builds the structure from the host factor list and sizes every
+// buffer; the caller fills z, sqrt_info and x0 (device gathers)
 void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
-                   const std::vector<int32_t>& vj, const std::vector<double>& z, const std::vector<double>& sqrt_info,
-                   const std::vector<double>& x0, int N, cudaStream_t st);
+                   const std::vector<int32_t>& vj, int N, cudaStream_t st);
 // per-factor error 0.5 w |R e|^2 at values `x` (weights null = 1); returns the sum
 double solver_error(SolverDev& s, const double* x, const double* weights, cudaStream_t st);
 // per-factor unweighted errors at x into s.ferr (host copy returned)

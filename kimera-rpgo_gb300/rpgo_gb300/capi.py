@@ -48,7 +48,9 @@ class Counts(C.Structure):
 class Timing(C.Structure):
     _fields_ = [("pcm_ms", C.c_double), ("solve_ms", C.c_double)] + [
         (n, C.c_int64) for n in ("pair_checks", "lm_iterations", "linear_solves", "gnc_iterations", "cg_iterations",
-                                 "kernel_launches")]
+                                 "kernel_launches")] + [
+        ("pcg_kernel_ms", C.c_double), ("pcg_kernel_launches", C.c_int64), ("pcg_kernel_bytes", C.c_double),
+        ("pair_kernel_ms", C.c_double), ("pair_kernel_launches", C.c_int64)]
 
 
 # every exported entry point: name -> (restype, argtypes)
@@ -67,6 +69,7 @@ SIGNATURES = {
     "rpgo_create": (_P, [C.POINTER(Params)]),
     "rpgo_destroy": (None, [_P]),
     "rpgo_update": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.c_int32]),
+    "rpgo_update_dev": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.c_int32]),
     "rpgo_force_update": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch)]),
     "rpgo_load_graph": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.POINTER(FactorBatch)]),
     "rpgo_add_graph": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.POINTER(FactorBatch)]),
@@ -128,6 +131,27 @@ class Batch:
         self.v = ValueBatch(len(a["value_keys"]), _ptr(a["value_keys"]), _ptr(a["value_poses"]))
 
 
+class DeviceBatch:
+    """A graph whose bulk arrays (measurements, covariances, square-root
+    informations, value poses) sit in GPU memory (torch tensors on cuda:0);
+    kinds and keys stay on the host. For rpgo_update_dev."""
+
+    def __init__(self, g):
+        import torch
+
+        self.a = g.arrays()
+        a = self.a
+        dev = torch.device("cuda", 0)
+        self.t = {k: torch.from_numpy(np.ascontiguousarray(a[k])).to(dev)
+                  for k in ("measured", "cov", "sqrt_info", "value_poses")}
+        torch.cuda.synchronize()
+        tp = lambda k: self.t[k].data_ptr() if self.t[k].numel() else None
+        self.f = FactorBatch(len(a["kind"]), _ptr(a["kind"]), _ptr(a["key1"]), _ptr(a["key2"]), tp("measured"),
+                             tp("cov"), tp("sqrt_info"))
+        self.v = ValueBatch(len(a["value_keys"]), _ptr(a["value_keys"]), tp("value_poses"))
+        self.bytes = sum(int(x.numel()) * 8 for x in self.t.values())
+
+
 class RpgoError(RuntimeError):
     pass
 
@@ -152,6 +176,9 @@ class RobustSolver:
     def update(self, graph, optimize_graph: bool = True) -> int:
         b = Batch(graph)
         return load().rpgo_update(self.h, C.byref(b.f), C.byref(b.v), int(optimize_graph))
+
+    def update_dev(self, dbatch: "DeviceBatch", optimize_graph: bool = True) -> int:
+        return load().rpgo_update_dev(self.h, C.byref(dbatch.f), C.byref(dbatch.v), int(optimize_graph))
 
     def forceUpdate(self, graph) -> int:
         b = Batch(graph)

@@ -306,3 +306,18 @@ def test_kernels_actually_launch():
     assert capi.kernel_launch_count() > before
     t = g.timing()
     assert t.kernel_launches > 0 and t.pair_checks > 0
+
+
+def test_update_dev_matches_host_update():
+    # HBM-resident inputs (rpgo_update_dev) give the same result as host inputs
+    s = synth.walk3d(300, 60, 20, seed=91)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+    a, b = capi.RobustSolver(p), capi.RobustSolver(p)
+    assert a.update(s.graph) == 0
+    db = capi.DeviceBatch(s.graph)
+    assert b.update_dev(db) == 0
+    assert np.array_equal(a.adjacency(0), b.adjacency(0))
+    assert np.array_equal(a.gnc_weights(), b.gnc_weights())
+    ka, pa = a.estimate()
+    kb, pb = b.estimate()
+    assert np.array_equal(ka, kb) and np.array_equal(pa, pb)
