@@ -31,7 +31,8 @@ enum {
   RPGO_ERR_CUDA = 2,       /* CUDA runtime / kernel failure */
   RPGO_ERR_KEY = 3,        /* value key already present, or missing key */
   RPGO_ERR_SOLVER = 4,     /* linear system not positive definite (GN) */
-  RPGO_ERR_UNSUPPORTED = 5 /* feature outside the implemented path */
+  RPGO_ERR_UNSUPPORTED = 5, /* feature outside the implemented path */
+  RPGO_ERR_SIZE = 6         /* size beyond a fixed maximum of the entry point */
 };
 
 /* --------------------------------------------------------------- enumerants
@@ -238,6 +239,24 @@ int rpgo_pairwise_adjacency_dev(int32_t dim, int32_t mode, int32_t n, int32_t ro
  * (host, capacity n); *size_out equals `seed` when nothing improved. */
 int rpgo_max_clique_heu_dev(int32_t n, const uint32_t* adj, int32_t words, int32_t first, int32_t seed,
                             int32_t* clique_out, int32_t* size_out, void* stream);
+
+/* Allocation-free variant of rpgo_max_clique_heu_dev. It has no counterpart
+ * in the reference: it exists for callers that must not allocate GPU memory
+ * (no cudaMalloc / cudaFree, no library allocator) on their call path. Same
+ * arguments, results and error codes, with a fixed maximum size:
+ * n <= RPGO_CLIQUE_NOALLOC_MAX_N and words <= RPGO_CLIQUE_NOALLOC_MAX_WORDS,
+ * else RPGO_ERR_SIZE with a message on stderr. Its device work arrays live in
+ * one file-scope __device__ array of RPGO_CLIQUE_NOALLOC_SCRATCH_BYTES, held
+ * by every device that loads the library until the process exits. The first
+ * call on a device (with that device current) looks up the array's address
+ * with cudaGetSymbolAddress; make that first call before any stream capture.
+ * Every call shares the one array: calls that overlap on the GPU (from
+ * several host threads, or on several streams) race and give wrong results. */
+#define RPGO_CLIQUE_NOALLOC_MAX_N 4096
+#define RPGO_CLIQUE_NOALLOC_MAX_WORDS 128
+#define RPGO_CLIQUE_NOALLOC_SCRATCH_BYTES 2245632
+int rpgo_max_clique_heu_dev_noalloc(int32_t n, const uint32_t* adj, int32_t words, int32_t first, int32_t seed,
+                                    int32_t* clique_out, int32_t* size_out, void* stream);
 
 /* ------------------------------------------------------------- host copies
  * The same stages on host arrays (copies in, copies out), for tests and for

@@ -23,6 +23,9 @@
 // improves and restarts the window after it (later results used a stale
 // threshold). A candidate that can no longer beat the threshold
 // (rounds + |B| + 1 <= best) stops early: it could not change the result.
+#include <mutex>
+
+#include "../../include/rpgo_gb300.h"
 #include "pcm_kernels.hpp"
 
 namespace rpgo {
@@ -228,3 +231,132 @@ int max_clique_heu(int n, const uint32_t* adj, int words, int first, int seed, s
 }
 
 }  // namespace rpgo
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant: the same two kernels and window loop, with every
+// device work array carved out of one file-scope scratch array instead of
+// cudaMalloc'd buffers. Limits: n <= RPGO_CLIQUE_NOALLOC_MAX_N closures,
+// row stride words <= RPGO_CLIQUE_NOALLOC_MAX_WORDS, and a window of
+// kNoAllocWindow candidates (the result does not depend on the window size:
+// the host always continues after the first improving candidate).
+namespace rpgo {
+namespace {
+
+constexpr int kNoAllocWindow = 128;
+constexpr size_t kAlign = 256;
+constexpr size_t align_up(size_t b) { return (b + kAlign - 1) / kAlign * kAlign; }
+// Region offsets (bytes) inside the scratch array.
+constexpr size_t kDegOff = 0;
+constexpr size_t kResultOff = kDegOff + align_up(sizeof(int32_t) * RPGO_CLIQUE_NOALLOC_MAX_N);
+constexpr size_t kSetsOff = kResultOff + align_up(sizeof(int32_t) * kNoAllocWindow);
+constexpr size_t kBufsOff =
+    kSetsOff + align_up(sizeof(uint32_t) * (size_t)kNoAllocWindow * 2 * RPGO_CLIQUE_NOALLOC_MAX_WORDS);
+constexpr size_t kScratchBytes =
+    kBufsOff + align_up(sizeof(int32_t) * (size_t)kNoAllocWindow * (RPGO_CLIQUE_NOALLOC_MAX_N + 1));
+static_assert(kScratchBytes == RPGO_CLIQUE_NOALLOC_SCRATCH_BYTES, "scratch size in the header is stale");
+
+// Held by every device that loads this library, until the process exits.
+// In host code `g_clique_scratch` is only a handle for cudaGetSymbolAddress.
+static __device__ __align__(256) unsigned char g_clique_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+unsigned char* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on the current device; looked up once
+// per device (the first call on a device) with that device current.
+int scratch_for_current_device(unsigned char** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return RPGO_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
+    unsigned char* ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_clique_scratch);
+    if (e != cudaSuccess || !ptr) {
+      std::fprintf(stderr, "rpgo_gb300: cudaGetSymbolAddress(clique scratch) failed: %s\n", cudaGetErrorString(e));
+      return RPGO_ERR_CUDA;
+    }
+    g_scratch_ptr[dev] = ptr;
+  }
+  *out = g_scratch_ptr[dev];
+  return RPGO_OK;
+}
+
+int max_clique_heu_noalloc(int n, const uint32_t* adj, int words, int first, int seed, int32_t* clique_out,
+                           int32_t* size_out, unsigned char* scratch, cudaStream_t st) {
+  int32_t* deg = reinterpret_cast<int32_t*>(scratch + kDegOff);
+  int32_t* result = reinterpret_cast<int32_t*>(scratch + kResultOff);
+  uint32_t* sets = reinterpret_cast<uint32_t*>(scratch + kSetsOff);
+  int32_t* bufs = reinterpret_cast<int32_t*>(scratch + kBufsOff);
+  int best = seed;
+  if (n > 0) {
+    // The array keeps the previous call's contents. Only the window results
+    // are cleared here; deg, the candidate sets and the work buffers are
+    // written by the kernels before they are read.
+    RPGO_CUDA(cudaMemsetAsync(result, 0, sizeof(int32_t) * kNoAllocWindow, st));
+    {
+      const int tb = 256;
+      k_degrees<<<div_up((int64_t)n * 32, tb), tb, 0, st>>>(n, adj, words, deg);
+      RPGO_LAUNCHED();
+    }
+    const int buf_len = n + 1;
+    int32_t h_result[kNoAllocWindow];
+    int v = std::max(first, 0);
+    while (v < n) {
+      const int count = std::min(kNoAllocWindow, n - v);
+      const int tb = 256;
+      k_clique_window<<<div_up((int64_t)count * 32, tb), tb, 0, st>>>(n, adj, words, deg, v, count, best, result,
+                                                                      sets, bufs, buf_len);
+      RPGO_LAUNCHED();
+      RPGO_CUDA(cudaMemcpyAsync(h_result, result, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, st));
+      RPGO_CUDA(cudaStreamSynchronize(st));
+      int improved = -1;
+      for (int s = 0; s < count; ++s)
+        if (h_result[s] > best) {
+          improved = s;
+          break;
+        }
+      if (improved < 0) {
+        v += count;
+        continue;
+      }
+      best = h_result[improved];
+      // The winner's work buffer goes straight to the caller's output; a
+      // later, larger winner overwrites it.
+      if (clique_out) {
+        RPGO_CUDA(cudaMemcpyAsync(clique_out, bufs + (size_t)improved * buf_len, sizeof(int32_t) * best,
+                                  cudaMemcpyDeviceToHost, st));
+        RPGO_CUDA(cudaStreamSynchronize(st));
+      }
+      v = v + improved + 1;
+    }
+  }
+  *size_out = best;
+  return RPGO_OK;
+}
+
+}  // namespace
+}  // namespace rpgo
+
+extern "C" int rpgo_max_clique_heu_dev_noalloc(int32_t n, const uint32_t* adj, int32_t words, int32_t first,
+                                               int32_t seed, int32_t* clique_out, int32_t* size_out,
+                                               void* stream) {
+  if (n < 0 || words < (n + 31) / 32 || !size_out || (n > 0 && !adj)) return RPGO_ERR_ARG;
+  if (n > RPGO_CLIQUE_NOALLOC_MAX_N || words > RPGO_CLIQUE_NOALLOC_MAX_WORDS) {
+    std::fprintf(stderr,
+                 "rpgo_gb300: rpgo_max_clique_heu_dev_noalloc: n = %d, words = %d exceeds the fixed scratch "
+                 "(n <= %d, words <= %d)\n",
+                 (int)n, (int)words, RPGO_CLIQUE_NOALLOC_MAX_N, RPGO_CLIQUE_NOALLOC_MAX_WORDS);
+    return RPGO_ERR_SIZE;
+  }
+  unsigned char* scratch = nullptr;
+  const int rc = rpgo::scratch_for_current_device(&scratch);
+  if (rc != RPGO_OK) return rc;
+  try {
+    return rpgo::max_clique_heu_noalloc(n, adj, words, first, seed, clique_out, size_out, scratch,
+                                        (cudaStream_t)stream);
+  } catch (const rpgo::CudaError& e) {
+    std::fprintf(stderr, "rpgo_gb300: %s\n", e.what());
+    return RPGO_ERR_CUDA;
+  }
+}

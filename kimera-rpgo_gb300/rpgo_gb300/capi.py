@@ -14,7 +14,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "librpgo_gb300.so")
 _lib = None
 
-OK, ERR_ARG, ERR_CUDA, ERR_KEY, ERR_SOLVER, ERR_UNSUPPORTED = range(6)
+OK, ERR_ARG, ERR_CUDA, ERR_KEY, ERR_SOLVER, ERR_UNSUPPORTED, ERR_SIZE = range(7)
+CLIQUE_NOALLOC_MAX_N = 4096
+CLIQUE_NOALLOC_MAX_WORDS = 128
 
 
 class Params(C.Structure):
@@ -86,6 +88,7 @@ SIGNATURES = {
     "rpgo_pairwise_adjacency_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32] + [_P] * 9 + [
         C.c_double, C.c_double, _P, C.c_int32, _P]),
     "rpgo_max_clique_heu_dev": (C.c_int, [C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P]),
+    "rpgo_max_clique_heu_dev_noalloc": (C.c_int, [C.c_int32, _P, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P]),
     "rpgo_pairwise_adjacency": (C.c_int, [C.c_int32, C.c_int32, C.c_int32] + [_P] * 5 + [C.c_int32] + [_P] * 4 + [
         C.c_double, C.c_double, _P]),
     "rpgo_max_clique_heu": (C.c_int, [C.c_int32, _P, C.c_int32, C.c_int32, _P, _P]),
