@@ -31,6 +31,8 @@ for _p in (ROOT, os.path.join(ROOT, "kimera-rpgo_gb300")):
         sys.path.insert(0, _p)
 
 METRIC = "PCM+GNC solve ms and graphs/s vs plain GPU at ATE<=1e-4 m; pair checks/s"
+# nominal FP64 rate of one GB300 (no measured FP64 figure exists for this part)
+FP64_NOMINAL_GFLOPS = 1250.0
 WORKLOAD = "3d random walk, 5000 poses, 1000 inlier + 333 outlier loop closures, PCM3D(10,5) + GNC-TLS(p=0.9)"
 
 
@@ -220,15 +222,27 @@ def run_gb300(args):
     e2e_ms = max_over_ranks(dist, sum(e2e_times) / len(e2e_times))
     last = tims[-1]
     peak, peak_kind = peaks()
-    pcg_launch_ms = sum(t.pcg_kernel_ms for t in tims) / max(1, sum(t.pcg_kernel_launches for t in tims))
-    pcg_launch_bytes = sum(t.pcg_kernel_bytes for t in tims) / max(1, sum(t.pcg_kernel_launches for t in tims))
-    achieved = pcg_launch_bytes / (pcg_launch_ms * 1e-3) / 1e9 if pcg_launch_ms > 0 else 0.0
+    n_chol = sum(t.chol_kernel_launches for t in tims)
+    n_pcg = sum(t.pcg_kernel_launches for t in tims)
+    if n_chol:
+        kname = "k_chol_solve (direct sparse Cholesky solve, FP64)"
+        launch_ms = sum(t.chol_kernel_ms for t in tims) / n_chol
+        launch_bytes = sum(t.chol_kernel_bytes for t in tims) / n_chol
+        launch_flops = sum(t.chol_kernel_flops for t in tims) / n_chol
+        traffic_file = "chol_traffic.json"
+    else:
+        kname = "k_pcg_coop (whole-GPU flexible PCG)"
+        launch_ms = sum(t.pcg_kernel_ms for t in tims) / max(1, n_pcg)
+        launch_bytes = sum(t.pcg_kernel_bytes for t in tims) / max(1, n_pcg)
+        launch_flops = None
+        traffic_file = "pcg_traffic.json"
+    achieved = launch_bytes / (launch_ms * 1e-3) / 1e9 if launch_ms > 0 else 0.0
     pair_ms = sum(t.pair_kernel_ms for t in tims) / max(1, sum(t.pair_kernel_launches for t in tims))
     pair_checks = last.pair_checks
     # accuracy of this run against the CPU FP64 oracle is checked by the
     # test suite; here: agreement of the two legs (HBM-resident vs host)
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "pcg_traffic.json")
+    tpath = os.path.join(ROOT, "profiles", traffic_file)
     if os.path.exists(tpath):
         with open(tpath) as f:
             traffic = json.load(f).get("bytes_per_launch_scaled")
@@ -255,12 +269,18 @@ def run_gb300(args):
         "gnc_iterations": last.gnc_iterations,
         "lm_iterations": last.lm_iterations,
         "cg_iterations": last.cg_iterations,
+        "chol_levels": last.chol_levels,
+        "chol_tail": last.chol_tail,
         "gpu_launches": launches,
         "e2e": {"value": world * 1000.0 / e2e_ms, "unit": "graphs/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"kernel": "k_pcg_coop (whole-GPU flexible PCG)", "bound": "hbm", "achieved": achieved,
+        "roofline": {"kernel": kname, "bound": "hbm", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": traffic, "launch_ms": pcg_launch_ms, "bytes_per_launch": pcg_launch_bytes},
+                     "traffic": traffic, "launch_ms": launch_ms, "bytes_per_launch": launch_bytes,
+                     "launches_per_step": (n_chol or n_pcg) / len(tims),
+                     "fp64_gflops": (launch_flops / (launch_ms * 1e-3) / 1e9) if launch_flops and launch_ms > 0
+                     else None,
+                     "fp64_peak_nominal_gflops": FP64_NOMINAL_GFLOPS},
         "clocks": clocks.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -49,6 +49,9 @@ enum {
 enum { RPGO_VERBOSITY_UPDATE = 0, RPGO_VERBOSITY_QUIET = 1, RPGO_VERBOSITY_VERBOSE = 2 };
 enum { RPGO_GNC_COST = 0, RPGO_GNC_PROBABILITY = 1 };
 enum { RPGO_FACTOR_BETWEEN = 0, RPGO_FACTOR_PRIOR = 1 };
+/* Linear solver of the LM / GN step (GTSAM: NonlinearOptimizerParams::
+ * linearSolverType, left at its default sparse Cholesky by the reference). */
+enum { RPGO_LINEAR_CHOLESKY = 0, RPGO_LINEAR_PCG = 1 };
 
 /* Flat mirror of RobustSolverParams (include/KimeraRPGO/SolverParams.h:80-299)
  * with PcmParams (33-56) and GncParams (58-78) inlined. */
@@ -71,6 +74,7 @@ typedef struct rpgo_params {
   int32_t gnc_fix_prev_inliers, gnc_bias_odom;
   /* additional */
   int32_t lm_diagonal_damping;
+  int32_t linear_solver;      /* RPGO_LINEAR_*: direct sparse Cholesky (default) or PCG */
 } rpgo_params;
 
 /* A batch of factors (structure of arrays). For priors key_back is ignored. */
@@ -114,6 +118,12 @@ typedef struct rpgo_timing {
   double pcg_kernel_ms;       /* whole-GPU PCG launches (sum) */
   int64_t pcg_kernel_launches;
   double pcg_kernel_bytes;    /* algorithmic bytes those launches move (sum) */
+  double chol_kernel_ms;      /* direct (Cholesky) solve launches (sum) */
+  int64_t chol_kernel_launches;
+  double chol_kernel_flops;   /* algorithmic FP64 flops of their factorisations (sum) */
+  double chol_kernel_bytes;   /* algorithmic device-memory bytes of those solves (sum) */
+  int64_t chol_levels;        /* elimination-tree levels of the sparse part (last plan) */
+  int64_t chol_tail;          /* variables in the dense trailing block (last plan) */
   double pair_kernel_ms;      /* pairwise consistency launches (sum) */
   int64_t pair_kernel_launches;
 } rpgo_timing;

@@ -85,7 +85,7 @@ int optimize(rpgo_solver* s) {
       init.assign(full.size(), 0.0);
       for (size_t i = 0; i < n_known && i < init.size(); ++i) init[i] = 1.0;
     }
-    GpuNls nls(s->dim, full, *s->store, *s->values, s->st);
+    GpuNls nls(s->dim, full, *s->store, *s->values, s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
     std::vector<double> w;
     gnc_tls(nls, n_known, g, lp, s->p.gnc_bias_odom ? &init : nullptr, &w, &st);
     nls.write_back(*s->values);
@@ -101,7 +101,7 @@ int optimize(rpgo_solver* s) {
         if (prev_k + i < s->gnc_weights.size() && s->gnc_weights[prev_k + i] > 0.5 && k + i < s->nfg.size())
           full.push_back(s->nfg[k + i]);
     }
-    GpuNls nls(s->dim, full, *s->store, *s->values, s->st);
+    GpuNls nls(s->dim, full, *s->store, *s->values, s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
     nls.optimize(lp, &st);
     if (st.failed) return RPGO_ERR_SOLVER;
     nls.write_back(*s->values);
@@ -166,6 +166,12 @@ int update_impl(rpgo_solver* s, std::vector<FactorRec> nf, const rpgo_value_batc
   s->timing.pcg_kernel_ms = kt.pcg_ms - kt0.pcg_ms;
   s->timing.pcg_kernel_launches = kt.pcg_launches - kt0.pcg_launches;
   s->timing.pcg_kernel_bytes = kt.pcg_bytes - kt0.pcg_bytes;
+  s->timing.chol_kernel_ms = kt.chol_ms - kt0.chol_ms;
+  s->timing.chol_kernel_launches = kt.chol_launches - kt0.chol_launches;
+  s->timing.chol_kernel_flops = kt.chol_flops - kt0.chol_flops;
+  s->timing.chol_kernel_bytes = kt.chol_bytes - kt0.chol_bytes;
+  s->timing.chol_levels = kt.chol_launches > kt0.chol_launches ? kt.chol_levels : 0;
+  s->timing.chol_tail = kt.chol_launches > kt0.chol_launches ? kt.chol_tail : 0;
   s->timing.pair_kernel_ms = kt.pair_ms - kt0.pair_ms;
   s->timing.pair_kernel_launches = kt.pair_launches - kt0.pair_launches;
   cudaEventDestroy(e0);

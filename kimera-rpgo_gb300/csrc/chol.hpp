@@ -1,0 +1,34 @@
+// Direct solve of the damped normal equations (H + lambda D) delta = -g:
+// sparse block Cholesky over the plan of chol_plan.hpp, in FP64, as one
+// cooperative kernel per solve (factorisation, forward and backward
+// substitution, model change).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "chol_plan.hpp"
+#include "common.cuh"
+#include "solver_kernels.hpp"
+
+namespace rpgo {
+
+struct CholDev {
+  CholPlan plan;
+  int levels = 0;
+  DeviceBuffer<int32_t> perm, col_ptr, blk_row, blk_col, lvl_col_ptr, lvl_cols, lvl_blk_ptr, lvl_blks;
+  DeviceBuffer<int32_t> upd_ptr, upd_src, tupd_ptr, tupd_src, a_ptr, a_src, ta_ptr, ta_src;
+  DeviceBuffer<int32_t> row_ptr, row_blk, trow_ptr, trow_blk;
+  DeviceBuffer<double> L;     // sparse blocks (diagonal slots hold the updated diagonal S_jj)
+  DeviceBuffer<double> Ldiag; // Cholesky factors of the sparse diagonal blocks
+  DeviceBuffer<double> M;     // dense tail, column-major, padded to whole tiles
+  DeviceBuffer<double> Ldd;   // Cholesky factors of the tail's diagonal tiles
+  DeviceBuffer<double> y;     // right-hand side / solution in elimination order
+  DeviceBuffer<double> part;  // per-CTA partial sums
+  DeviceBuffer<double> out;   // model change, status
+  DeviceBuffer<int32_t> status;
+  void upload(CholPlan&& p, cudaStream_t st);
+};
+
+// Solve with the factorisation of (H + lambda D); fills s.delta.
+SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st);
+
+}  // namespace rpgo

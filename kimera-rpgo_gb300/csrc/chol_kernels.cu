@@ -1,0 +1,752 @@
+// Sparse block Cholesky solve of (H + lambda D) delta = -g on the GPU (FP64).
+//
+// One cooperative kernel per solve, 256 threads per CTA, one CTA per SM.
+// Phases are separated by grid barriers:
+//  1. init: right-hand side in elimination order, padding of the dense tail;
+//  2. per elimination-tree level of the sparse columns (leaves first), one
+//     barrier each: every column of the level, by one warp (wide levels) or
+//     one CTA (narrow levels): S = H block (+ lambda D on the diagonal) -
+//     sum of L(i,k) L(j,k)^T over each block's update list, L_jj = chol(S_jj),
+//     L_ij = S_ij L_jj^-T, and the column's forward substitution;
+//  3. the dense tail: its blocks from H and the sparse updates, then a
+//     right-looking tiled Cholesky with one barrier per tile column: in phase
+//     k the CTAs of tile column k apply the update of column k-1, factor the
+//     diagonal tile and solve their tile, while all other CTAs apply the
+//     column k-1 update to the trailing tiles; the forward substitution of
+//     tile k-1 runs in the same phase;
+//  4. backward substitution over the tail tiles, then the sparse levels (top
+//     first); scatter to variable order; the linearised cost change with the
+//     undamped H (a fixed-order grid reduction).
+// Every sum runs in an order fixed by the plan, so results do not depend on
+// scheduling. A non-positive (or NaN) pivot sets the status flag; the factor
+// continues with pivot 1 so that every phase still ends, and the host treats
+// the solve as failed (as GTSAM's IndeterminantLinearSystemException).
+#include <cooperative_groups.h>
+
+#include "chol.hpp"
+
+namespace cg = cooperative_groups;
+
+namespace rpgo {
+namespace {
+
+constexpr int kTB = 24;  // dense tail tile (scalars); a multiple of both block sizes
+constexpr int kThreads = 256;
+
+struct CholArgs {
+  int N, ns, T, ntp, n_tiles, levels;
+  const int32_t *perm, *col_ptr, *blk_row, *blk_col, *lvl_col_ptr, *lvl_cols, *lvl_blk_ptr, *lvl_blks;
+  const int32_t *upd_ptr, *upd_src, *tupd_ptr, *tupd_src, *a_ptr, *a_src, *ta_ptr, *ta_src;
+  const int32_t *row_ptr, *row_blk, *trow_ptr, *trow_blk;
+  const double *Hd64, *fH64, *dampD, *g;
+  const int32_t *h_row_ptr, *h_col, *h_blk;
+  const int8_t* h_btr;
+  double lam;
+  double *L, *Ldiag, *M, *Ldd, *y, *delta, *part, *out;
+  int32_t* status;
+};
+
+__device__ __forceinline__ void set_fail(int32_t* status) { atomicExch(status, 1); }
+
+// s0, s1 (the lane's entries e = lane, lane + 32 of a D x D block) -= sum
+// over the update pairs [beg, end) of (L[a] L[b]^T)(r, c), in list order.
+// The 32 lanes load the indices of 32 pairs at once and broadcast them, so
+// the block loads of consecutive pairs do not wait on an index load.
+template <int D>
+__device__ __forceinline__ void sub_pairs_warp(const double* __restrict__ L, const int32_t* __restrict__ src, int beg,
+                                               int end, int lane, double& s0, double& s1) {
+  constexpr int dd = D * D;
+  const int e0 = lane, e1 = lane + 32;
+  const int r0 = e0 / D, c0 = e0 % D, r1 = e1 / D, c1 = e1 % D;
+  for (int base = beg; base < end; base += 32) {
+    const int cnt = min(32, end - base);
+    int ia = 0, ib = 0;
+    if (lane < cnt) {
+      ia = src[2 * (base + lane)];
+      ib = src[2 * (base + lane) + 1];
+    }
+#pragma unroll 4
+    for (int u = 0; u < cnt; ++u) {
+      const int pa = __shfl_sync(0xffffffffu, ia, u), pb = __shfl_sync(0xffffffffu, ib, u);
+      if (e0 < dd) {
+        const double* A = L + (size_t)pa * dd + r0 * D;
+        const double* B = L + (size_t)pb * dd + c0 * D;
+        double acc = 0.0;
+#pragma unroll
+        for (int t = 0; t < D; ++t) acc = fma(A[t], B[t], acc);
+        s0 -= acc;
+      }
+      if (e1 < dd) {
+        const double* A = L + (size_t)pa * dd + r1 * D;
+        const double* B = L + (size_t)pb * dd + c1 * D;
+        double acc = 0.0;
+#pragma unroll
+        for (int t = 0; t < D; ++t) acc = fma(A[t], B[t], acc);
+        s1 -= acc;
+      }
+    }
+  }
+}
+
+// Hessian entry (r, c) of the block at (row var, col var) from the factor
+// off-diagonal blocks in src[beg, end) (2 f + transposed)
+template <int D>
+__device__ __forceinline__ double gather_offdiag(const double* __restrict__ fH64, const int32_t* __restrict__ src,
+                                                 int beg, int end, int r, int c) {
+  constexpr int dd = D * D;
+  double s = 0.0;
+  for (int u = beg; u < end; ++u) {
+    const int32_t x = src[u];
+    const double* H = fH64 + (size_t)(x >> 1) * 3 * dd + 2 * dd;
+    s += (x & 1) ? H[c * D + r] : H[r * D + c];
+  }
+  return s;
+}
+
+template <int D>
+__device__ __forceinline__ double gather_diag(const CholArgs& a, int v, int r, int c) {
+  constexpr int dd = D * D;
+  double s = a.Hd64[(size_t)v * dd + r * D + c];
+  if (r == c) s += a.lam * a.dampD[(size_t)v * D + r];
+  return s;
+}
+
+// In-register Cholesky of a D x D block (lower, row-major); false on a
+// non-positive pivot (which is replaced by 1).
+template <int D>
+__device__ __forceinline__ bool chol_reg(double (&C)[D * D]) {
+  bool ok = true;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    double s = C[c * D + c];
+#pragma unroll
+    for (int t = 0; t < c; ++t) s -= C[c * D + t] * C[c * D + t];
+    if (!(s > 0.0)) {
+      ok = false;
+      s = 1.0;
+    }
+    const double l = sqrt(s);
+    C[c * D + c] = l;
+#pragma unroll
+    for (int r = c + 1; r < D; ++r) {
+      double v = C[r * D + c];
+#pragma unroll
+      for (int t = 0; t < c; ++t) v -= C[r * D + t] * C[c * D + t];
+      C[r * D + c] = v / l;
+    }
+  }
+  return ok;
+}
+
+// S of sparse block p (one warp): H block (+ lambda D on the diagonal)
+// minus its update pairs; written over the block's slot of L
+template <int D>
+__device__ void block_S(const CholArgs& a, int p, int lane) {
+  constexpr int dd = D * D;
+  const int j = a.blk_col[p], i = a.blk_row[p];
+  const int e0 = lane, e1 = lane + 32;
+  double s0 = 0.0, s1 = 0.0;
+  if (i == j) {
+    const int v = a.perm[j];
+    if (e0 < dd) s0 = gather_diag<D>(a, v, e0 / D, e0 % D);
+    if (e1 < dd) s1 = gather_diag<D>(a, v, e1 / D, e1 % D);
+  } else {
+    if (e0 < dd) s0 = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], e0 / D, e0 % D);
+    if (e1 < dd) s1 = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], e1 / D, e1 % D);
+  }
+  sub_pairs_warp<D>(a.L, a.upd_src, a.upd_ptr[p], a.upd_ptr[p + 1], lane, s0, s1);
+  if (e0 < dd) a.L[(size_t)p * dd + e0] = s0;
+  if (e1 < dd) a.L[(size_t)p * dd + e1] = s1;
+}
+
+// L_jj = chol(S_jj) in registers (every calling thread holds it)
+template <int D>
+__device__ __forceinline__ bool diag_factor(const CholArgs& a, int p0, double (&C)[D * D]) {
+  constexpr int dd = D * D;
+#pragma unroll
+  for (int e = 0; e < dd; ++e) C[e] = a.L[(size_t)p0 * dd + e];
+  return chol_reg<D>(C);
+}
+
+// row r of off-diagonal block q: L_qr = S_qr L_jj^-T (task t = block * D + row)
+template <int D>
+__device__ __forceinline__ void scale_row(const CholArgs& a, int p0, int t, const double (&C)[D * D]) {
+  constexpr int dd = D * D;
+  const int q = p0 + 1 + t / D, r = t % D;
+  double* S = a.L + (size_t)q * dd + r * D;
+  double x[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    double v = S[c];
+#pragma unroll
+    for (int k = 0; k < c; ++k) v -= x[k] * C[c * D + k];
+    x[c] = v / C[c * D + c];
+  }
+#pragma unroll
+  for (int c = 0; c < D; ++c) S[c] = x[c];
+}
+
+template <int D>
+__device__ __forceinline__ void store_diag(const CholArgs& a, int j, const double (&C)[D * D], int lane) {
+  constexpr int dd = D * D;
+#pragma unroll
+  for (int e = 0; e < dd; ++e)
+    if (e % 32 == lane) a.Ldiag[(size_t)j * dd + e] = (e / D >= e % D) ? C[e] : 0.0;
+}
+
+template <int D>
+__device__ void sparse_forward(const CholArgs& a, int j, int lane);
+
+// whole sparse column j by one warp: S of its blocks, L_jj, L_ij, and its
+// forward substitution
+template <int D>
+__device__ void column_warp(const CholArgs& a, int j, int lane) {
+  constexpr int dd = D * D;
+  const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
+  for (int p = p0; p < p1; ++p) block_S<D>(a, p, lane);
+  __syncwarp();
+  double C[dd];
+  const bool ok = diag_factor<D>(a, p0, C);
+  if (!ok && lane == 0) set_fail(a.status);
+  store_diag<D>(a, j, C, lane);
+  for (int t = lane; t < (p1 - p0 - 1) * D; t += 32) scale_row<D>(a, p0, t, C);
+  __syncwarp();
+  sparse_forward<D>(a, j, lane);
+}
+
+// whole sparse column j by one CTA (the warps share its blocks)
+template <int D>
+__device__ void column_cta(const CholArgs& a, int j) {
+  constexpr int dd = D * D;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
+  for (int p = p0 + warp; p < p1; p += nwarps) block_S<D>(a, p, lane);
+  __syncthreads();
+  double C[dd];
+  const bool ok = diag_factor<D>(a, p0, C);
+  if (!ok && threadIdx.x == 0) set_fail(a.status);
+  if (warp == 0) store_diag<D>(a, j, C, lane);
+  for (int t = threadIdx.x; t < (p1 - p0 - 1) * D; t += blockDim.x) scale_row<D>(a, p0, t, C);
+  __syncthreads();
+  if (warp == 0) sparse_forward<D>(a, j, lane);
+  __syncthreads();
+}
+
+// forward substitution of sparse column j: y_j = L_jj^-1 (y_j - sum L_jk y_k)
+template <int D>
+__device__ void sparse_forward(const CholArgs& a, int j, int lane) {
+  constexpr int dd = D * D;
+  double b = 0.0;
+  if (lane < D) {
+    b = a.y[(size_t)j * D + lane];
+    for (int u = a.row_ptr[j]; u < a.row_ptr[j + 1]; ++u) {
+      const int q = a.row_blk[u];
+      const double* B = a.L + (size_t)q * dd + lane * D;
+      const double* yk = a.y + (size_t)a.blk_col[q] * D;
+      double acc = 0.0;
+#pragma unroll
+      for (int c = 0; c < D; ++c) acc = fma(B[c], yk[c], acc);
+      b -= acc;
+    }
+  }
+  const double* Lj = a.Ldiag + (size_t)j * dd;
+  double yv = 0.0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    if (lane == c) yv = b / Lj[c * D + c];
+    const double yc = __shfl_sync(0xffffffffu, yv, c);
+    if (lane > c && lane < D) b -= Lj[lane * D + c] * yc;
+  }
+  if (lane < D) a.y[(size_t)j * D + lane] = yv;
+}
+
+// backward substitution of sparse column j: x_j = L_jj^-T (y_j - sum L_ij^T x_i)
+template <int D>
+__device__ void sparse_backward(const CholArgs& a, int j, int lane) {
+  constexpr int dd = D * D;
+  double b = 0.0;
+  if (lane < D) {
+    b = a.y[(size_t)j * D + lane];
+    for (int q = a.col_ptr[j] + 1; q < a.col_ptr[j + 1]; ++q) {
+      const double* B = a.L + (size_t)q * dd;
+      const double* xi = a.y + (size_t)a.blk_row[q] * D;
+      double acc = 0.0;
+#pragma unroll
+      for (int r = 0; r < D; ++r) acc = fma(B[r * D + lane], xi[r], acc);
+      b -= acc;
+    }
+  }
+  const double* Lj = a.Ldiag + (size_t)j * dd;
+  double xv = 0.0;
+#pragma unroll
+  for (int c = D - 1; c >= 0; --c) {
+    if (lane == c) xv = b / Lj[c * D + c];
+    const double xc = __shfl_sync(0xffffffffu, xv, c);
+    if (lane < c) b -= Lj[c * D + lane] * xc;
+  }
+  if (lane < D) a.y[(size_t)j * D + lane] = xv;
+}
+
+__device__ __forceinline__ void tail_coords(int t, int& bi, int& bj) {
+  int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (i * (i + 1) / 2 > t) --i;
+  while ((i + 1) * (i + 2) / 2 <= t) ++i;
+  bi = i;
+  bj = t - i * (i + 1) / 2;
+}
+
+// S of tail block t into the dense tail
+template <int D>
+__device__ void tail_S(const CholArgs& a, int t, int lane) {
+  constexpr int dd = D * D;
+  int bi, bj;
+  tail_coords(t, bi, bj);
+  const int e0 = lane, e1 = lane + 32;
+  double s0 = 0.0, s1 = 0.0;
+  if (bi == bj) {
+    const int v = a.perm[a.ns + bi];
+    if (e0 < dd) s0 = gather_diag<D>(a, v, e0 / D, e0 % D);
+    if (e1 < dd) s1 = gather_diag<D>(a, v, e1 / D, e1 % D);
+  } else {
+    if (e0 < dd) s0 = gather_offdiag<D>(a.fH64, a.ta_src, a.ta_ptr[t], a.ta_ptr[t + 1], e0 / D, e0 % D);
+    if (e1 < dd) s1 = gather_offdiag<D>(a.fH64, a.ta_src, a.ta_ptr[t], a.ta_ptr[t + 1], e1 / D, e1 % D);
+  }
+  sub_pairs_warp<D>(a.L, a.tupd_src, a.tupd_ptr[t], a.tupd_ptr[t + 1], lane, s0, s1);
+  if (e0 < dd) a.M[(size_t)(bj * D + e0 % D) * a.ntp + bi * D + e0 / D] = s0;
+  if (e1 < dd) a.M[(size_t)(bj * D + e1 % D) * a.ntp + bi * D + e1 / D] = s1;
+}
+
+// tail right-hand side: y_t -= sum over sparse blocks in tail block row t
+template <int D>
+__device__ void tail_rhs(const CholArgs& a, int t, int lane) {
+  constexpr int dd = D * D;
+  if (lane >= D) return;
+  double b = 0.0;
+  for (int u = a.trow_ptr[t]; u < a.trow_ptr[t + 1]; ++u) {
+    const int q = a.trow_blk[u];
+    const double* B = a.L + (size_t)q * dd + lane * D;
+    const double* yk = a.y + (size_t)a.blk_col[q] * D;
+    double acc = 0.0;
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc = fma(B[c], yk[c], acc);
+    b += acc;
+  }
+  a.y[(size_t)(a.ns + t) * D + lane] -= b;
+}
+
+struct TileSmem {
+  double A[kTB][kTB + 1];
+  double B[kTB][kTB + 1];
+  double C[kTB][kTB + 1];
+  double E[kTB][kTB + 1];
+  double red[kThreads / kTB + 1][kTB];
+  double v[kTB];
+};
+
+__device__ __forceinline__ double* tile_ptr(const CholArgs& a, int ti, int tj) {
+  return a.M + (size_t)(tj * kTB) * a.ntp + ti * kTB;
+}
+
+__device__ void load_tile(const CholArgs& a, int ti, int tj, double (*S)[kTB + 1]) {
+  const double* P = tile_ptr(a, ti, tj);
+  for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
+    const int r = e % kTB, c = e / kTB;
+    S[r][c] = P[(size_t)c * a.ntp + r];
+  }
+}
+
+// X[r][c] -= sum_t P[r][t] Q[c][t] (lower part only when lower_only)
+__device__ void smem_update(double (*X)[kTB + 1], double (*P)[kTB + 1], double (*Q)[kTB + 1], bool lower_only) {
+  for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
+    const int r = e % kTB, c = e / kTB;
+    if (lower_only && c > r) continue;
+    double acc = 0.0;
+#pragma unroll
+    for (int t = 0; t < kTB; ++t) acc = fma(P[r][t], Q[c][t], acc);
+    X[r][c] -= acc;
+  }
+}
+
+// Cholesky of the lower part of X in place (right-looking)
+__device__ void smem_chol(double (*X)[kTB + 1], int32_t* status) {
+  for (int c = 0; c < kTB; ++c) {
+    if (threadIdx.x == 0) {
+      double piv = X[c][c];
+      if (!(piv > 0.0)) {
+        set_fail(status);
+        piv = 1.0;
+      }
+      X[c][c] = sqrt(piv);
+    }
+    __syncthreads();
+    const double l = X[c][c];
+    for (int r = c + 1 + threadIdx.x; r < kTB; r += blockDim.x) X[r][c] /= l;
+    __syncthreads();
+    const int m = kTB - c - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int r = c + 1 + e % m, q = c + 1 + e / m;
+      if (q <= r) X[r][q] -= X[r][c] * X[q][c];
+    }
+    __syncthreads();
+  }
+}
+
+// phase k, tile column item: tile (i, k), i >= k
+__device__ void tail_column_item(const CholArgs& a, int i, int k, TileSmem& s) {
+  load_tile(a, k, k, s.C);
+  if (k > 0) load_tile(a, k, k - 1, s.B);
+  if (i > k) {
+    load_tile(a, i, k, s.A);
+    if (k > 0) load_tile(a, i, k - 1, s.E);
+  }
+  __syncthreads();
+  if (k > 0) {
+    smem_update(s.C, s.B, s.B, true);
+    if (i > k) smem_update(s.A, s.E, s.B, false);
+  }
+  __syncthreads();
+  smem_chol(s.C, a.status);
+  if (i == k) {
+    double* O = a.Ldd + (size_t)k * kTB * kTB;
+    for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
+      const int r = e / kTB, c = e % kTB;
+      O[e] = (c <= r) ? s.C[r][c] : 0.0;
+    }
+  } else {
+    // row r of the tile: x = A[r] L^-T
+    if (threadIdx.x < kTB) {
+      const int r = threadIdx.x;
+      for (int c = 0; c < kTB; ++c) {
+        double v = s.A[r][c];
+        for (int t = 0; t < c; ++t) v -= s.A[r][t] * s.C[c][t];
+        s.A[r][c] = v / s.C[c][c];
+      }
+    }
+    __syncthreads();
+    double* P = tile_ptr(a, i, k);
+    for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
+      const int r = e % kTB, c = e / kTB;
+      P[(size_t)c * a.ntp + r] = s.A[r][c];
+    }
+  }
+  __syncthreads();
+}
+
+// phase k >= 1, trailing item: tile (i, j), j >= k + 1, updated by column k - 1
+__device__ void tail_trailing_item(const CholArgs& a, int i, int j, int k, TileSmem& s) {
+  load_tile(a, i, k - 1, s.A);
+  load_tile(a, j, k - 1, s.B);
+  __syncthreads();
+  double* P = tile_ptr(a, i, j);
+  for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
+    const int r = e % kTB, c = e / kTB;
+    if (i == j && c > r) continue;
+    double acc = 0.0;
+#pragma unroll
+    for (int t = 0; t < kTB; ++t) acc = fma(s.A[r][t], s.B[c][t], acc);
+    P[(size_t)c * a.ntp + r] -= acc;
+  }
+  __syncthreads();
+}
+
+// forward substitution of tail tile k (left-looking):
+// y_k = Ldd_k^-1 (y_k - sum_{j<k} L(k, j) y_j); yt = tail segment of y
+__device__ void tail_forward_item(const CholArgs& a, double* yt, int k, TileSmem& s) {
+  constexpr int chunks = kThreads / kTB;
+  const int ncol = k * kTB;
+  if (threadIdx.x < chunks * kTB) {
+    const int r = threadIdx.x % kTB, ch = threadIdx.x / kTB;
+    double acc = 0.0;
+    const double* P = a.M + k * kTB + r;
+    for (int c = ch; c < ncol; c += chunks) acc = fma(P[(size_t)c * a.ntp], yt[c], acc);
+    s.red[ch][r] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double b = 0.0;
+    if (lane < kTB) {
+      b = yt[k * kTB + lane];
+      for (int ch = 0; ch < chunks; ++ch) b -= s.red[ch][lane];
+    }
+    const double* Lk = a.Ldd + (size_t)k * kTB * kTB;
+    double yv = 0.0;
+    for (int c = 0; c < kTB; ++c) {
+      if (lane == c) yv = b / Lk[c * kTB + c];
+      const double yc = __shfl_sync(0xffffffffu, yv, c);
+      if (lane > c && lane < kTB) b -= Lk[lane * kTB + c] * yc;
+    }
+    if (lane < kTB) yt[k * kTB + lane] = yv;
+  }
+  __syncthreads();
+}
+
+// backward substitution of tail tile k (left-looking):
+// x_k = Ldd_k^-T (y_k - sum_{i>k} L(i, k)^T x_i), in place over y
+__device__ void tail_backward_item(const CholArgs& a, double* yt, int k, TileSmem& s) {
+  constexpr int chunks = kThreads / kTB;
+  const int r0 = (k + 1) * kTB;
+  if (threadIdx.x < chunks * kTB) {
+    const int c = threadIdx.x % kTB, ch = threadIdx.x / kTB;
+    double acc = 0.0;
+    const double* P = a.M + (size_t)(k * kTB + c) * a.ntp;
+    for (int r = r0 + ch; r < a.ntp; r += chunks) acc = fma(P[r], yt[r], acc);
+    s.red[ch][c] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double b = 0.0;
+    if (lane < kTB) {
+      b = yt[k * kTB + lane];
+      for (int ch = 0; ch < chunks; ++ch) b -= s.red[ch][lane];
+    }
+    const double* Lk = a.Ldd + (size_t)k * kTB * kTB;
+    double xv = 0.0;
+    for (int c = kTB - 1; c >= 0; --c) {
+      if (lane == c) xv = b / Lk[c * kTB + c];
+      const double xc = __shfl_sync(0xffffffffu, xv, c);
+      if (lane < c) b -= Lk[c * kTB + lane] * xc;
+    }
+    if (lane < kTB) yt[k * kTB + lane] = xv;
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ double cta_sum(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int i = 0; i < nw; ++i) t += sh[i];
+  return t;
+}
+
+template <int D>
+__global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
+  constexpr int dd = D * D;
+  cg::grid_group grid = cg::this_grid();
+  __shared__ TileSmem sm;
+  __shared__ double shr[kThreads / 32];
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const int gw = gt >> 5, nw = gs >> 5;
+  const int n = a.N * D, nt = a.T * D;
+  double* yt = a.y + (size_t)a.ns * D;
+
+  // 1. init
+  if (gt == 0) *a.status = 0;
+  for (int k = gt; k < n; k += gs) {
+    const int pos = k / D, r = k % D;
+    a.y[k] = -a.g[(size_t)a.perm[pos] * D + r];
+  }
+  for (int k = nt + gt; k < a.ntp; k += gs) yt[k] = 0.0;
+  {
+    // padded rows / columns of the tail: identity
+    const int pad = a.ntp - nt;
+    for (int e = gt; e < pad * a.ntp; e += gs) {
+      const int c = e / a.ntp, r = e % a.ntp;  // column nt + c, any row; and row nt + c, columns < nt
+      a.M[(size_t)(nt + c) * a.ntp + r] = (r == nt + c) ? 1.0 : 0.0;
+      if (r < nt) a.M[(size_t)r * a.ntp + nt + c] = 0.0;
+    }
+  }
+  grid.sync();
+
+  // 2. sparse levels, one barrier each: a level with at least as many
+  // columns as CTAs gives a column to a warp, a narrower one to a CTA
+  for (int l = 0; l < a.levels; ++l) {
+    const int c0 = a.lvl_col_ptr[l], nc = a.lvl_col_ptr[l + 1] - c0;
+    if (nc >= (int)gridDim.x) {
+      for (int w = gw; w < nc; w += nw) column_warp<D>(a, a.lvl_cols[c0 + w], lane);
+    } else {
+      for (int c = blockIdx.x; c < nc; c += gridDim.x) column_cta<D>(a, a.lvl_cols[c0 + c]);
+    }
+    grid.sync();
+  }
+
+  // 3. dense tail: blocks, then tiles
+  for (int w = gw; w < a.T * (a.T + 1) / 2; w += nw) tail_S<D>(a, w, lane);
+  grid.sync();
+  const int nT = a.n_tiles;
+  for (int k = 0; k <= nT; ++k) {
+    const int ncol = k < nT ? nT - k : 0;
+    const int m = nT - k - 1;  // trailing tile columns k + 1 .. nT - 1
+    const int ntrail = (k >= 1 && m > 0) ? m * (m + 1) / 2 : 0;
+    const int nfwd = k >= 1 ? 1 : 0;
+    const int items = ncol + ntrail + nfwd;
+    for (int it = blockIdx.x; it < items; it += gridDim.x) {
+      if (it < ncol) {
+        tail_column_item(a, k + it, k, sm);
+      } else if (it < ncol + ntrail) {
+        // trailing tile u -> (i, j), k + 1 <= j <= i <= nT - 1
+        const int u = it - ncol;
+        int ii, jj;
+        tail_coords(u, ii, jj);
+        tail_trailing_item(a, k + 1 + ii, k + 1 + jj, k, sm);
+      } else {
+        tail_forward_item(a, yt, k - 1, sm);
+      }
+    }
+    if (k == 0)
+      for (int w = gw; w < a.T; w += nw) tail_rhs<D>(a, w, lane);
+    grid.sync();
+  }
+
+  // 4. backward substitution: tail tiles, then sparse levels (top first)
+  for (int k = nT - 1; k >= 0; --k) {
+    if (blockIdx.x == (unsigned)(k % gridDim.x)) tail_backward_item(a, yt, k, sm);
+    grid.sync();
+  }
+  for (int l = a.levels - 1; l >= 0; --l) {
+    const int c0 = a.lvl_col_ptr[l], c1 = a.lvl_col_ptr[l + 1];
+    for (int w = gw; w < c1 - c0; w += nw) sparse_backward<D>(a, a.lvl_cols[c0 + w], lane);
+    grid.sync();
+  }
+  for (int k = gt; k < n; k += gs) {
+    const int pos = k / D, r = k % D;
+    a.delta[(size_t)a.perm[pos] * D + r] = a.y[k];
+  }
+  grid.sync();
+
+  // model change with the undamped H: -g.delta - delta^T H delta / 2
+  double gd = 0.0, dhd = 0.0;
+  for (int v = gt; v < a.N; v += gs) {
+    double acc[D];
+    const double* H = a.Hd64 + (size_t)v * dd;
+    const double* pv = a.delta + (size_t)v * D;
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      double s = 0.0;
+#pragma unroll
+      for (int c = 0; c < D; ++c) s += H[D * r + c] * pv[c];
+      acc[r] = s;
+    }
+    for (int k = a.h_row_ptr[v]; k < a.h_row_ptr[v + 1]; ++k) {
+      const double* B = a.fH64 + (size_t)a.h_blk[k] * 3 * dd + 2 * dd;
+      const double* pc = a.delta + (size_t)a.h_col[k] * D;
+      if (a.h_btr[k]) {
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+          for (int c = 0; c < D; ++c) acc[r] += B[D * c + r] * pc[c];
+      } else {
+#pragma unroll
+        for (int r = 0; r < D; ++r)
+#pragma unroll
+          for (int c = 0; c < D; ++c) acc[r] += B[D * r + c] * pc[c];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      gd += a.g[(size_t)v * D + r] * pv[r];
+      dhd += pv[r] * acc[r];
+    }
+  }
+  gd = cta_sum(gd, shr);
+  dhd = cta_sum(dhd, shr);
+  if (threadIdx.x == 0) {
+    a.part[2 * blockIdx.x] = gd;
+    a.part[2 * blockIdx.x + 1] = dhd;
+  }
+  grid.sync();
+  if (gt == 0) {
+    double sg = 0.0, sh = 0.0;
+    for (int b = 0; b < (int)gridDim.x; ++b) {
+      sg += a.part[2 * b];
+      sh += a.part[2 * b + 1];
+    }
+    a.out[0] = -sg - 0.5 * sh;
+  }
+}
+
+}  // namespace
+
+void CholDev::upload(CholPlan&& p, cudaStream_t st) {
+  plan = std::move(p);
+  levels = plan.levels();
+  if (plan.tile != kTB) throw std::logic_error("chol plan tile size differs from the kernel's");
+  perm.upload(plan.perm, st);
+  col_ptr.upload(plan.col_ptr, st);
+  blk_row.upload(plan.blk_row, st);
+  blk_col.upload(plan.blk_col, st);
+  lvl_col_ptr.upload(plan.lvl_col_ptr, st);
+  lvl_cols.upload(plan.lvl_cols, st);
+  lvl_blk_ptr.upload(plan.lvl_blk_ptr, st);
+  lvl_blks.upload(plan.lvl_blks, st);
+  upd_ptr.upload(plan.upd_ptr, st);
+  upd_src.upload(plan.upd_src, st);
+  tupd_ptr.upload(plan.tupd_ptr, st);
+  tupd_src.upload(plan.tupd_src, st);
+  a_ptr.upload(plan.a_ptr, st);
+  a_src.upload(plan.a_src, st);
+  ta_ptr.upload(plan.ta_ptr, st);
+  ta_src.upload(plan.ta_src, st);
+  row_ptr.upload(plan.row_ptr, st);
+  row_blk.upload(plan.row_blk, st);
+  trow_ptr.upload(plan.trow_ptr, st);
+  trow_blk.upload(plan.trow_blk, st);
+  const size_t dd = (size_t)plan.d * plan.d, ntp = (size_t)plan.n_tiles * kTB;
+  L.resize(std::max<size_t>(1, plan.blk_row.size() * dd));
+  Ldiag.resize(std::max<size_t>(1, (size_t)plan.n_sparse * dd));
+  M.resize(std::max<size_t>(1, ntp * ntp));
+  Ldd.resize(std::max<size_t>(1, (size_t)plan.n_tiles * kTB * kTB));
+  y.resize((size_t)plan.n_sparse * plan.d + ntp + 1);
+  out.resize(4);
+  status.resize(1);
+}
+
+SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st) {
+  SolveOut o;
+  if (s.N == 0) {
+    o.ok = 1;
+    return o;
+  }
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    RPGO_CUDA(cudaGetDevice(&dev));
+    RPGO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  }
+  const int grid = sms;
+  c.part.resize((size_t)2 * grid);
+  const CholPlan& p = c.plan;
+  CholArgs a{s.N, p.n_sparse, p.T, p.n_tiles * kTB, p.n_tiles, c.levels,
+             c.perm.get(), c.col_ptr.get(), c.blk_row.get(), c.blk_col.get(), c.lvl_col_ptr.get(), c.lvl_cols.get(),
+             c.lvl_blk_ptr.get(), c.lvl_blks.get(), c.upd_ptr.get(), c.upd_src.get(), c.tupd_ptr.get(),
+             c.tupd_src.get(), c.a_ptr.get(), c.a_src.get(), c.ta_ptr.get(), c.ta_src.get(), c.row_ptr.get(),
+             c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
+             s.g.get(), s.row_ptr.get(), s.col.get(), s.blk.get(), s.btr.get(), lambda, c.L.get(), c.Ldiag.get(),
+             c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.status.get()};
+  void* args[] = {&a};
+  double ms = 0.0;
+  {
+    EventTimer timer(st);
+    if (s.dim == 3)
+      RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_chol_solve<6>, grid, kThreads, args, 0, st));
+    else
+      RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_chol_solve<3>, grid, kThreads, args, 0, st));
+    RPGO_LAUNCHED();
+    ms = timer.elapsed_ms();
+  }
+  double h = 0.0;
+  int32_t status = 0;
+  RPGO_CUDA(cudaMemcpyAsync(&h, c.out.get(), sizeof(double), cudaMemcpyDeviceToHost, st));
+  RPGO_CUDA(cudaMemcpyAsync(&status, c.status.get(), sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  RPGO_CUDA(cudaStreamSynchronize(st));
+  kernel_times().chol_ms += ms;
+  kernel_times().chol_launches += 1;
+  kernel_times().chol_flops += p.flops;
+  kernel_times().chol_bytes += p.bytes;
+  kernel_times().chol_levels = c.levels;
+  kernel_times().chol_tail = p.T;
+  o.lin_change = h;
+  o.ok = status == 0 ? 1 : 0;
+  o.cg_iterations = 0;
+  o.rel_residual = 0.0;
+  return o;
+}
+
+}  // namespace rpgo

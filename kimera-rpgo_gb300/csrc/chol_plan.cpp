@@ -1,0 +1,505 @@
+// Symbolic analysis for the direct solve; see chol_plan.hpp.
+#include "chol_plan.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <functional>
+#include <queue>
+#include <stdexcept>
+#include <string>
+#include <utility>
+
+namespace rpgo {
+namespace {
+
+// time model of the solve kernel (per grid-barrier phase, per FP64 flop)
+constexpr double kPhaseUs = 8.0;
+constexpr double kUsPerFlop = 5e-6;
+
+// Elimination game on the variable graph: eliminating u records its current
+// neighbours (the structure of its column of L, as variables) and joins them
+// into a clique.
+struct Elimination {
+  std::vector<std::vector<int32_t>>& adj;
+  std::vector<char> alive;
+  std::vector<int32_t> order;
+  std::vector<std::vector<int32_t>> col_vars;
+  std::vector<int32_t> merged;
+  explicit Elimination(std::vector<std::vector<int32_t>>& a) : adj(a), alive(a.size(), 1), col_vars(a.size()) {
+    order.reserve(a.size());
+  }
+  template <class OnDegree>
+  void eliminate(int u, OnDegree&& on_degree) {
+    alive[u] = 0;
+    order.push_back(u);
+    std::vector<int32_t> nb;
+    nb.swap(adj[u]);
+    for (int w : nb) {
+      // adj[w] <- (adj[w] \ {u}) U (nb \ {w})
+      const std::vector<int32_t>& a = adj[w];
+      merged.clear();
+      merged.reserve(a.size() + nb.size());
+      size_t i = 0, j = 0;
+      while (i < a.size() || j < nb.size()) {
+        int32_t x;
+        if (j >= nb.size() || (i < a.size() && a[i] < nb[j])) x = a[i++];
+        else if (i >= a.size() || nb[j] < a[i]) x = nb[j++];
+        else {
+          x = a[i++];
+          ++j;
+        }
+        if (x != u && x != w) merged.push_back(x);
+      }
+      adj[w].assign(merged.begin(), merged.end());
+      on_degree(w);
+    }
+    col_vars[u] = std::move(nb);
+  }
+};
+
+// Elimination order:
+//  1. the interior of every chain of degree-2 variables (odometry between loop
+//     closures, dangling trajectory ends) by cyclic reduction: alternate chain
+//     variables first, then alternate survivors, ... This costs no more fill
+//     than eliminating the chain from one end and makes the elimination tree
+//     log2(length) deep over the chain instead of length deep;
+//  2. the remaining variables by minimum degree (ties by the smaller index).
+void order_variables(int N, std::vector<std::vector<int32_t>>& adj, std::vector<int32_t>* order,
+                     std::vector<std::vector<int32_t>>* col_vars) {
+  Elimination el(adj);
+  // 1. chains of variables of degree <= 2
+  std::vector<char> in_chain(N, 0), seen(N, 0);
+  for (int u = 0; u < N; ++u) in_chain[u] = adj[u].size() <= 2;
+  std::vector<std::pair<int, int>> keyed;  // (cyclic-reduction level, variable)
+  std::vector<int32_t> path;
+  for (int s = 0; s < N; ++s) {
+    if (!in_chain[s] || seen[s]) continue;
+    // walk to one end of the chain through chain variables
+    int prev = -1, cur = s;
+    while (true) {
+      int nxt = -1;
+      for (int w : adj[cur])
+        if (w != prev && in_chain[w] && w != s) {
+          nxt = w;
+          break;
+        }
+      if (nxt < 0) break;
+      prev = cur;
+      cur = nxt;
+    }
+    // collect the chain from that end
+    path.clear();
+    prev = -1;
+    while (cur >= 0 && !seen[cur]) {
+      seen[cur] = 1;
+      path.push_back(cur);
+      int nxt = -1;
+      for (int w : adj[cur])
+        if (w != prev && in_chain[w] && !seen[w]) {
+          nxt = w;
+          break;
+        }
+      prev = cur;
+      cur = nxt;
+    }
+    for (size_t t = 0; t < path.size(); ++t) {
+      const unsigned pos1 = (unsigned)t + 1;
+      keyed.push_back({__builtin_ctz(pos1), path[t]});
+    }
+  }
+  std::stable_sort(keyed.begin(), keyed.end(),
+                   [](const std::pair<int, int>& a, const std::pair<int, int>& b) { return a.first < b.first; });
+  for (const auto& kv : keyed) el.eliminate(kv.second, [](int) {});
+  // 2. minimum degree on what remains
+  using Entry = std::pair<int32_t, int32_t>;  // (degree, variable)
+  std::priority_queue<Entry, std::vector<Entry>, std::greater<Entry>> pq;
+  for (int u = 0; u < N; ++u)
+    if (el.alive[u]) pq.push({(int32_t)adj[u].size(), u});
+  auto push = [&](int w) { pq.push({(int32_t)adj[w].size(), w}); };
+  while (!pq.empty()) {
+    const Entry e = pq.top();
+    pq.pop();
+    const int u = e.second;
+    if (!el.alive[u] || e.first != (int32_t)adj[u].size()) continue;
+    el.eliminate(u, push);
+  }
+  *order = std::move(el.order);
+  *col_vars = std::move(el.col_vars);
+}
+
+// Nested dissection by breadth-first level structures: a connected set is
+// split at the level of a breadth-first search from a pseudo-peripheral
+// variable whose variables (those with a neighbour in the next level) form
+// the smallest separator that leaves at least a quarter of the set on each
+// side; both halves are ordered recursively, the separator last. Pose graphs
+// whose closures are local (a thick chain) have separators a few variables
+// wide, so the elimination tree stays about log2(N) separators deep where
+// minimum degree, eliminating such a band from one end, makes it about N deep.
+struct NestedDissection {
+  const std::vector<std::vector<int32_t>>& adj;
+  int leaf;
+  std::vector<int32_t> inset, vis, level;
+  int set_id = 0, bfs_id = 0;
+  std::vector<int32_t> out;
+  NestedDissection(const std::vector<std::vector<int32_t>>& a, int lf)
+      : adj(a), leaf(lf), inset(a.size(), 0), vis(a.size(), 0), level(a.size(), 0) {}
+
+  // breadth-first search inside the current set; returns the visit order
+  void bfs(int root, std::vector<int32_t>* q) {
+    ++bfs_id;
+    q->clear();
+    q->push_back(root);
+    vis[root] = bfs_id;
+    level[root] = 0;
+    for (size_t h = 0; h < q->size(); ++h) {
+      const int u = (*q)[h];
+      for (int w : adj[u])
+        if (inset[w] == set_id && vis[w] != bfs_id) {
+          vis[w] = bfs_id;
+          level[w] = level[u] + 1;
+          q->push_back(w);
+        }
+    }
+  }
+
+  void run(std::vector<int32_t> nodes) {
+    if ((int)nodes.size() <= leaf) {
+      std::sort(nodes.begin(), nodes.end());
+      out.insert(out.end(), nodes.begin(), nodes.end());
+      return;
+    }
+    ++set_id;
+    for (int u : nodes) inset[u] = set_id;
+    std::vector<int32_t> q;
+    bfs(nodes[0], &q);
+    if (q.size() < nodes.size()) {
+      // several components: order each on its own
+      std::vector<std::vector<int32_t>> comps;
+      const int sid = set_id;
+      comps.push_back(q);
+      ++bfs_id;
+      const int mark = bfs_id;
+      for (int u : q) vis[u] = mark;
+      for (int u : nodes) {
+        if (vis[u] == mark) continue;
+        set_id = sid;
+        std::vector<int32_t> c;
+        bfs(u, &c);
+        for (int w : c) vis[w] = mark;
+        comps.push_back(std::move(c));
+      }
+      for (auto& c : comps) run(std::move(c));
+      return;
+    }
+    // pseudo-peripheral root: repeat the search from the farthest variable
+    int root = nodes[0], depth = 0;
+    for (int sweep = 0; sweep < 4; ++sweep) {
+      const int far = q.back();
+      if (level[far] <= depth && sweep > 0) break;
+      depth = level[far];
+      root = far;
+      bfs(root, &q);
+    }
+    bfs(root, &q);
+    const int L = level[q.back()] + 1;
+    std::vector<int32_t> cnt(L + 1, 0);
+    for (int u : q) cnt[level[u]]++;
+    const int n = (int)q.size();
+    int best_m = -1, best = 1 << 30, below = 0;
+    for (int m = 0; m < L; ++m) {
+      const int above = n - below - cnt[m];
+      if (m > 0 && m + 1 < L && 4 * below >= n && 4 * above >= n && cnt[m] < best) {
+        best = cnt[m];
+        best_m = m;
+      }
+      below += cnt[m];
+    }
+    if (best_m < 0) {
+      // no balanced level split (a star or a tiny diameter): keep the set whole
+      std::sort(nodes.begin(), nodes.end());
+      out.insert(out.end(), nodes.begin(), nodes.end());
+      return;
+    }
+    std::vector<int32_t> A, B, S;
+    for (int u : q) {
+      const int l = level[u];
+      if (l < best_m) A.push_back(u);
+      else if (l > best_m) B.push_back(u);
+      else {
+        bool touches_next = false;
+        for (int w : adj[u])
+          if (inset[w] == set_id && level[w] == best_m + 1) {
+            touches_next = true;
+            break;
+          }
+        (touches_next ? S : A).push_back(u);
+      }
+    }
+    run(std::move(A));
+    run(std::move(B));
+    std::sort(S.begin(), S.end());
+    out.insert(out.end(), S.begin(), S.end());
+  }
+};
+
+// Symbolic elimination in a given order.
+void eliminate_in_order(std::vector<std::vector<int32_t>>& adj, const std::vector<int32_t>& order,
+                        std::vector<std::vector<int32_t>>* col_vars) {
+  Elimination el(adj);
+  for (int u : order) el.eliminate(u, [](int) {});
+  *col_vars = std::move(el.col_vars);
+}
+
+int find_block(const CholPlan& p, int col, int row) {
+  if (row == col) return p.col_ptr[col];
+  const auto b = p.blk_row.begin() + p.col_ptr[col] + 1, e = p.blk_row.begin() + p.col_ptr[col + 1];
+  const auto it = std::lower_bound(b, e, row);
+  if (it == e || *it != row)
+    throw std::logic_error("chol plan: block (" + std::to_string(row) + ", " + std::to_string(col) +
+                           ") outside the symbolic structure");
+  return (int)(it - p.blk_row.begin());
+}
+
+}  // namespace
+
+CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
+                        const std::vector<int32_t>& vj) {
+  CholPlan p;
+  p.N = N;
+  p.d = d;
+  const size_t F = kind.size();
+  std::vector<std::vector<int32_t>> adj(N);
+  for (size_t f = 0; f < F; ++f)
+    if (kind[f] == 0 && vi[f] != vj[f]) {
+      adj[vi[f]].push_back(vj[f]);
+      adj[vj[f]].push_back(vi[f]);
+    }
+  for (auto& a : adj) {
+    std::sort(a.begin(), a.end());
+    a.erase(std::unique(a.begin(), a.end()), a.end());
+  }
+  // Candidate orders, kept by a model of the solve kernel's time: every
+  // grid-barrier phase (three per sparse level, two per dense tile) costs
+  // about kPhaseUs, every FP64 flop of the factorisation kUsPerFlop.
+  struct Candidate {
+    std::vector<int32_t> perm, pos;
+    std::vector<std::vector<int32_t>> cols;
+    int T = 0;
+    double cost = 0.0;
+  };
+  auto make_candidate = [&](std::vector<int32_t>&& perm, const std::vector<std::vector<int32_t>>& col_vars) {
+    Candidate c;
+    c.perm = std::move(perm);
+    c.pos.assign(N, 0);
+    for (int j = 0; j < N; ++j) c.pos[c.perm[j]] = j;
+    c.cols.assign(N, {});
+    for (int j = 0; j < N; ++j) {
+      for (int v : col_vars[c.perm[j]]) c.cols[j].push_back(c.pos[v]);
+      std::sort(c.cols[j].begin(), c.cols[j].end());
+    }
+    // dense tail: the trailing columns whose structure is complete
+    while (c.T < N && (int)c.cols[N - 1 - c.T].size() == c.T) ++c.T;
+    const int ns = N - c.T;
+    std::vector<int32_t> lvl(ns, 0);
+    int L = 0;
+    double pairs = 0.0;
+    for (int j = 0; j < ns; ++j) {
+      L = std::max(L, lvl[j] + 1);
+      if (!c.cols[j].empty() && c.cols[j][0] < ns) lvl[c.cols[j][0]] = std::max(lvl[c.cols[j][0]], lvl[j] + 1);
+      const double m = (double)c.cols[j].size();
+      pairs += m * (m + 1) / 2;
+    }
+    const double nt = (double)c.T * d, dd3 = (double)d * d * d;
+    const double tiles = std::ceil(nt / p.tile);
+    const double flops = 2.0 * dd3 * pairs + nt * nt * nt / 3.0;
+    c.cost = (3.0 * L + 2.0 * tiles + 4.0) * kPhaseUs + flops * kUsPerFlop;
+    return c;
+  };
+  std::vector<Candidate> cands;
+  {
+    std::vector<std::vector<int32_t>> a = adj, col_vars;
+    std::vector<int32_t> perm;
+    order_variables(N, a, &perm, &col_vars);
+    cands.push_back(make_candidate(std::move(perm), col_vars));
+  }
+  for (int leaf : {4, 32}) {
+    NestedDissection nd(adj, leaf);
+    std::vector<int32_t> all(N);
+    for (int u = 0; u < N; ++u) all[u] = u;
+    nd.run(std::move(all));
+    std::vector<std::vector<int32_t>> a = adj, col_vars;
+    eliminate_in_order(a, nd.out, &col_vars);
+    cands.push_back(make_candidate(std::move(nd.out), col_vars));
+  }
+  size_t best = 0;
+  for (size_t c = 1; c < cands.size(); ++c)
+    if (cands[c].cost < cands[best].cost) best = c;
+  p.perm = std::move(cands[best].perm);
+  p.pos = std::move(cands[best].pos);
+  std::vector<std::vector<int32_t>> cols = std::move(cands[best].cols);
+  const int T = cands[best].T;
+  p.T = T;
+  p.n_sparse = N - T;
+  const int ns = p.n_sparse;
+  p.n_tiles = (T * d + p.tile - 1) / p.tile;
+
+  // sparse blocks
+  p.col_ptr.assign(ns + 1, 0);
+  for (int j = 0; j < ns; ++j) p.col_ptr[j + 1] = p.col_ptr[j] + 1 + (int)cols[j].size();
+  p.blk_row.resize(p.col_ptr[ns]);
+  p.blk_col.resize(p.col_ptr[ns]);
+  for (int j = 0; j < ns; ++j) {
+    int q = p.col_ptr[j];
+    p.blk_row[q] = j;
+    p.blk_col[q] = j;
+    for (int r : cols[j]) {
+      ++q;
+      p.blk_row[q] = r;
+      p.blk_col[q] = j;
+    }
+  }
+  // elimination-tree levels of the sparse columns
+  std::vector<int32_t> lvl(ns, 0);
+  int L = 0;
+  for (int j = 0; j < ns; ++j) {
+    L = std::max(L, lvl[j] + 1);
+    if (!cols[j].empty() && cols[j][0] < ns) lvl[cols[j][0]] = std::max(lvl[cols[j][0]], lvl[j] + 1);
+  }
+  p.lvl_col_ptr.assign(L + 1, 0);
+  p.lvl_blk_ptr.assign(L + 1, 0);
+  for (int j = 0; j < ns; ++j) {
+    p.lvl_col_ptr[lvl[j] + 1] += 1;
+    p.lvl_blk_ptr[lvl[j] + 1] += p.col_ptr[j + 1] - p.col_ptr[j];
+  }
+  for (int l = 0; l < L; ++l) {
+    p.lvl_col_ptr[l + 1] += p.lvl_col_ptr[l];
+    p.lvl_blk_ptr[l + 1] += p.lvl_blk_ptr[l];
+  }
+  p.lvl_cols.resize(ns);
+  p.lvl_blks.resize(p.col_ptr[ns]);
+  {
+    std::vector<int32_t> cc(p.lvl_col_ptr.begin(), p.lvl_col_ptr.end() - 1),
+        bc(p.lvl_blk_ptr.begin(), p.lvl_blk_ptr.end() - 1);
+    for (int j = 0; j < ns; ++j) {
+      p.lvl_cols[cc[lvl[j]]++] = j;
+      for (int q = p.col_ptr[j]; q < p.col_ptr[j + 1]; ++q) p.lvl_blks[bc[lvl[j]]++] = q;
+    }
+  }
+
+  // updates: for each sparse column k and rows ra <= rb of it, target (rb, ra)
+  // -= L(rb, k) L(ra, k)^T; lists are filled in ascending k
+  const int nblk = p.n_blocks(), ntb = p.n_tail_blocks();
+  p.upd_ptr.assign(nblk + 1, 0);
+  p.tupd_ptr.assign(ntb + 1, 0);
+  auto tail_index = [ns](int rb, int ra) {
+    const int bi = rb - ns, bj = ra - ns;
+    return bi * (bi + 1) / 2 + bj;
+  };
+  double pairs = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<int32_t> fill_s, fill_t;
+    if (pass == 1) {
+      for (int q = 0; q < nblk; ++q) p.upd_ptr[q + 1] += p.upd_ptr[q];
+      for (int t = 0; t < ntb; ++t) p.tupd_ptr[t + 1] += p.tupd_ptr[t];
+      p.upd_src.resize((size_t)2 * p.upd_ptr[nblk]);
+      p.tupd_src.resize((size_t)2 * p.tupd_ptr[ntb]);
+      fill_s.assign(p.upd_ptr.begin(), p.upd_ptr.end() - 1);
+      fill_t.assign(p.tupd_ptr.begin(), p.tupd_ptr.end() - 1);
+    }
+    for (int k = 0; k < ns; ++k) {
+      const int b0 = p.col_ptr[k] + 1, m = p.col_ptr[k + 1] - b0;
+      for (int a = 0; a < m; ++a) {
+        const int ra = p.blk_row[b0 + a];
+        for (int b = a; b < m; ++b) {
+          const int rb = p.blk_row[b0 + b];
+          if (ra < ns) {
+            const int tgt = find_block(p, ra, rb);
+            if (pass == 0) {
+              p.upd_ptr[tgt + 1]++;
+            } else {
+              const int s = fill_s[tgt]++;
+              p.upd_src[2 * s] = b0 + b;
+              p.upd_src[2 * s + 1] = b0 + a;
+            }
+          } else {
+            const int tgt = tail_index(rb, ra);
+            if (pass == 0) {
+              p.tupd_ptr[tgt + 1]++;
+            } else {
+              const int s = fill_t[tgt]++;
+              p.tupd_src[2 * s] = b0 + b;
+              p.tupd_src[2 * s + 1] = b0 + a;
+            }
+          }
+          if (pass == 0) pairs += 1.0;
+        }
+      }
+    }
+  }
+
+  // Hessian off-diagonal blocks per target
+  p.a_ptr.assign(nblk + 1, 0);
+  p.ta_ptr.assign(ntb + 1, 0);
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<int32_t> fill_s, fill_t;
+    if (pass == 1) {
+      for (int q = 0; q < nblk; ++q) p.a_ptr[q + 1] += p.a_ptr[q];
+      for (int t = 0; t < ntb; ++t) p.ta_ptr[t + 1] += p.ta_ptr[t];
+      p.a_src.resize(p.a_ptr[nblk]);
+      p.ta_src.resize(p.ta_ptr[ntb]);
+      fill_s.assign(p.a_ptr.begin(), p.a_ptr.end() - 1);
+      fill_t.assign(p.ta_ptr.begin(), p.ta_ptr.end() - 1);
+    }
+    for (size_t f = 0; f < F; ++f) {
+      if (kind[f] != 0 || vi[f] == vj[f]) continue;
+      const int pi = p.pos[vi[f]], pj = p.pos[vj[f]];
+      const int r = std::max(pi, pj), c = std::min(pi, pj);
+      const int32_t src = (int32_t)(2 * f + (pi == r ? 0 : 1));
+      if (c < ns) {
+        const int tgt = find_block(p, c, r);
+        if (pass == 0) p.a_ptr[tgt + 1]++;
+        else p.a_src[fill_s[tgt]++] = src;
+      } else {
+        const int tgt = tail_index(r, c);
+        if (pass == 0) p.ta_ptr[tgt + 1]++;
+        else p.ta_src[fill_t[tgt]++] = src;
+      }
+    }
+  }
+
+  // row lists for the forward solve
+  p.row_ptr.assign(ns + 1, 0);
+  p.trow_ptr.assign(T + 1, 0);
+  for (int q = 0; q < nblk; ++q) {
+    const int r = p.blk_row[q];
+    if (r == p.blk_col[q]) continue;
+    if (r < ns) p.row_ptr[r + 1]++;
+    else p.trow_ptr[r - ns + 1]++;
+  }
+  for (int j = 0; j < ns; ++j) p.row_ptr[j + 1] += p.row_ptr[j];
+  for (int t = 0; t < T; ++t) p.trow_ptr[t + 1] += p.trow_ptr[t];
+  p.row_blk.resize(p.row_ptr[ns]);
+  p.trow_blk.resize(p.trow_ptr[T]);
+  {
+    std::vector<int32_t> fr(p.row_ptr.begin(), p.row_ptr.end() - 1), ft(p.trow_ptr.begin(), p.trow_ptr.end() - 1);
+    for (int q = 0; q < nblk; ++q) {
+      const int r = p.blk_row[q];
+      if (r == p.blk_col[q]) continue;
+      if (r < ns) p.row_blk[fr[r]++] = q;
+      else p.trow_blk[ft[r - ns]++] = q;
+    }
+  }
+  const double dd3 = (double)d * d * d, nt = (double)T * d;
+  p.flops = 2.0 * dd3 * pairs + ns * dd3 / 3.0 + (nblk - ns) * dd3 + nt * nt * nt / 3.0;
+  {
+    const double dd = (double)d * d, nA = (double)p.a_src.size() + p.ta_src.size();
+    const double factor = 8.0 * dd * (nblk + ns) + 8.0 * nt * (nt + 1) / 2.0;  // L (+ diagonal factors)
+    p.bytes = 8.0 * dd * (N + nA)   // Hessian diagonal and off-diagonal blocks
+              + 2.0 * factor        // factor written, then read by its updates
+              + 2.0 * factor        // read by the forward and the backward substitution
+              + 8.0 * d * N * 6.0;  // gradient, damping, rhs / solution, step, model change
+  }
+  return p;
+}
+
+}  // namespace rpgo

@@ -36,6 +36,9 @@ struct KernelTimes {
   int64_t pcg_launches = 0;
   double pair_ms = 0.0;
   int64_t pair_launches = 0;
+  double chol_ms = 0.0, chol_flops = 0.0, chol_bytes = 0.0;
+  int64_t chol_levels = 0, chol_tail = 0;  // of the last plan used
+  int64_t chol_launches = 0;
 };
 KernelTimes& kernel_times();
 

@@ -10,7 +10,7 @@
 namespace rpgo {
 
 GpuNls::GpuNls(int dim, const std::vector<FactorRec>& graph, const FactorStore& store, const ValueStore& values,
-               cudaStream_t st)
+               cudaStream_t st, bool direct)
     : dim_(dim), st_(st) {
   const int stride = dim == 3 ? 12 : 4, d = dim == 3 ? 6 : 3;
   std::map<uint64_t, int> index;
@@ -31,7 +31,7 @@ GpuNls::GpuNls(int dim, const std::vector<FactorRec>& graph, const FactorStore& 
     vj[f] = r.kind == 0 ? index.at(r.k2) : vi[f];
     frows[f] = r.row;
   }
-  solver_upload(s_, dim, kind, vi, vj, (int)keys_.size(), st_);
+  solver_upload(s_, dim, kind, vi, vj, (int)keys_.size(), st_, direct);
   DeviceBuffer<int64_t> fr;
   fr.upload(frows, st_);
   value_rows_.upload(vrows, st_);

@@ -37,8 +37,9 @@ class GpuNls {
  public:
   // structure from the host factor list; measurements, square-root
   // informations and initial values gathered on the device from the stores
+  // direct: sparse Cholesky steps (else whole-GPU PCG)
   GpuNls(int dim, const std::vector<FactorRec>& graph, const FactorStore& store, const ValueStore& values,
-         cudaStream_t st);
+         cudaStream_t st, bool direct = true);
   void set_weights(const std::vector<double>& w);
   // LM / GN from the initial values; result left in dev().x
   void optimize(const LmParams& p, NlsStats* st);

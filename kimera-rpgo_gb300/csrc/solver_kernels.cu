@@ -2,17 +2,21 @@
 //
 //  K4 linearise      one thread per factor: FP64 residual and exact Jacobians
 //                    (BetweenFactor / PriorFactor as GTSAM evaluates them),
-//                    whitened by sqrt(w) R; FP64 gradient blocks, FP32 Hessian
-//                    blocks (J_i^T J_i, J_j^T J_j, J_i^T J_j).
+//                    whitened by sqrt(w) R; FP64 gradient and Hessian blocks
+//                    (J_i^T J_i, J_j^T J_j, J_i^T J_j), plus an FP32 copy of
+//                    the Hessian blocks for the PCG preconditioner.
 //  assemble          one thread per variable, fixed factor order (no atomics,
 //                    run-to-run deterministic): diagonal blocks, gradient, the
 //                    odometry-chain preconditioner blocks and the damping
 //                    diagonal clamp(diag H, 1e-6, 1e32) (LM diagonalDamping).
-//  K5 linear solve   one persistent CTA: block cyclic reduction factorisation
-//                    of the odometry-chain (block tridiagonal) preconditioner,
-//                    preconditioned CG on (H + lambda D) in FP32, and FP64
-//                    iterative refinement of the step on the FP64 residual;
-//                    also the linearised cost change -g.d - d^T H d / 2 (FP64).
+//  K5 linear solve   (H + lambda D) delta = -g. Default: the direct sparse
+//                    Cholesky of chol_kernels.cu (FP64, one cooperative
+//                    kernel per solve). Here: the alternative whole-GPU
+//                    flexible PCG in FP64 (k_pcg_coop) with an FP32 block
+//                    cyclic-reduction preconditioner of the odometry chain,
+//                    used on request or when the factor would not fit the
+//                    memory budget; both also give the linearised cost change
+//                    -g.d - d^T H d / 2 (FP64, undamped H).
 //  retract / error   X <- X Expmap(delta); per-factor 0.5 w |R e|^2 (FP64).
 //  K6 GNC weights    TLS weights of GncOptimizer::calculateWeights (FP64).
 #include <cooperative_groups.h>
@@ -20,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 
+#include "chol.hpp"
 #include "solver_kernels.hpp"
 #include "solver_math.cuh"
 
@@ -29,6 +34,8 @@ namespace {
 using namespace sm;
 
 constexpr int kCta = 1024;
+// device memory the direct solver's factor may take before the PCG path is used
+constexpr double kCholBudgetBytes = 32.0 * (1 << 30);
 
 // ------------------------------------------------------------------ errors
 template <int DIM>
@@ -938,7 +945,7 @@ __global__ void k_gnc_weights(int F, int n_known, const double* __restrict__ u2,
 
 // ------------------------------------------------------------------ host wrappers
 void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
-                   const std::vector<int32_t>& vj, int N, cudaStream_t st) {
+                   const std::vector<int32_t>& vj, int N, cudaStream_t st, bool direct) {
   s.dim = dim;
   s.d = dim == 3 ? 6 : 3;
   s.stride = dim == 3 ? 12 : 4;
@@ -1043,6 +1050,17 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   for (auto* b : {&s.cr, &s.cz, &s.cp, &s.cq, &s.cx}) b->resize((size_t)N * d);
   for (auto* b : {&s.r64, &s.z64, &s.zo64, &s.p64, &s.q64}) b->resize((size_t)N * d);
   s.out.resize(8);
+  s.chol.reset();
+  if (direct && N > 0) {
+    CholPlan plan = make_chol_plan(N, d, kind, vi, vj);
+    const double ntp = (double)plan.n_tiles * plan.tile;
+    const double bytes = 8.0 * dd * (plan.n_blocks() + plan.n_sparse) + 8.0 * ntp * ntp +
+                         4.0 * (plan.upd_src.size() + plan.tupd_src.size());
+    if (bytes <= kCholBudgetBytes) {
+      s.chol = std::make_shared<CholDev>();
+      s.chol->upload(std::move(plan), st);
+    }
+  }
 }
 
 double solver_error(SolverDev& s, const double* x, const double* weights, cudaStream_t st) {
@@ -1467,6 +1485,7 @@ __global__ void __launch_bounds__(256) k_pcg_coop(CoopArgs a) {
 
 // (H + lambda D) delta = -g with the whole-GPU flexible PCG (k_pcg_coop).
 SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
+  if (s.chol) return chol_solve(s, *s.chol, lambda, st);
   SolveOut o;
   if (s.N == 0) {
     o.ok = 1;

@@ -3,11 +3,14 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <memory>
 #include <vector>
 
 #include "common.cuh"
 
 namespace rpgo {
+
+struct CholDev;
 
 // Device-resident problem: factors, structure, per-iteration buffers.
 struct SolverDev {
@@ -46,6 +49,8 @@ struct SolverDev {
   DeviceBuffer<double> r64, z64, zo64, p64, q64;        // N x d, CG vectors
   DeviceBuffer<double> out;                              // solve outputs
   int levels = 0;
+  // direct solver (sparse Cholesky); null when the PCG path solves
+  std::shared_ptr<CholDev> chol;
 };
 
 struct SolveOut {
@@ -57,8 +62,10 @@ struct SolveOut {
 
 // setup: builds the structure from the host factor list and sizes every
 // buffer; the caller fills z, sqrt_info and x0 (device gathers)
+// direct: plan the sparse Cholesky solve (else, or when its factor would
+// exceed the memory budget, the whole-GPU PCG solves the steps)
 void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
-                   const std::vector<int32_t>& vj, int N, cudaStream_t st);
+                   const std::vector<int32_t>& vj, int N, cudaStream_t st, bool direct);
 // per-factor error 0.5 w |R e|^2 at values `x` (weights null = 1); returns the sum
 double solver_error(SolverDev& s, const double* x, const double* weights, cudaStream_t st);
 // per-factor unweighted errors at x into s.ferr (host copy returned)

@@ -29,7 +29,7 @@ class Params(C.Structure):
         ("use_gnc", C.c_int32), ("gnc_threshold_mode", C.c_int32), ("gnc_inlier_threshold", C.c_double),
         ("gnc_max_iterations", C.c_int32), ("gnc_mu_step", C.c_double), ("gnc_relative_cost_tol", C.c_double),
         ("gnc_weights_tol", C.c_double), ("gnc_fix_prev_inliers", C.c_int32), ("gnc_bias_odom", C.c_int32),
-        ("lm_diagonal_damping", C.c_int32),
+        ("lm_diagonal_damping", C.c_int32), ("linear_solver", C.c_int32),
     ]
 
 
@@ -52,6 +52,8 @@ class Timing(C.Structure):
         (n, C.c_int64) for n in ("pair_checks", "lm_iterations", "linear_solves", "gnc_iterations", "cg_iterations",
                                  "kernel_launches")] + [
         ("pcg_kernel_ms", C.c_double), ("pcg_kernel_launches", C.c_int64), ("pcg_kernel_bytes", C.c_double),
+        ("chol_kernel_ms", C.c_double), ("chol_kernel_launches", C.c_int64), ("chol_kernel_flops", C.c_double),
+        ("chol_kernel_bytes", C.c_double), ("chol_levels", C.c_int64), ("chol_tail", C.c_int64),
         ("pair_kernel_ms", C.c_double), ("pair_kernel_launches", C.c_int64)]
 
 

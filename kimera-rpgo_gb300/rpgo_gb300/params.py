@@ -13,6 +13,8 @@ NONE, PCM2D, PCM3D, PCM_SIMPLE2D, PCM_SIMPLE3D = 0, 1, 2, 3, 4
 UPDATE, QUIET, VERBOSE = 0, 1, 2
 # GncParams::GncThresholdMode
 COST, PROBABILITY = 0, 1
+# linear solver of the LM / GN step (GTSAM linearSolverType; the reference keeps the default)
+LINEAR_CHOLESKY, LINEAR_PCG = 0, 1
 
 
 class RobustSolverParams:
@@ -41,6 +43,7 @@ class RobustSolverParams:
         self.gnc_fix_prev_inliers = 0
         self.gnc_bias_odom = 0
         self.lm_diagonal_damping = 1
+        self.linear_solver = LINEAR_CHOLESKY
 
     # SolverParams.h:97-100
     def setNoRejection(self, verbosity=UPDATE, dim=3):
@@ -55,6 +58,11 @@ class RobustSolverParams:
 
     def setLmDiagonalDamping(self, flag: bool):
         self.lm_diagonal_damping = int(bool(flag))
+        return self
+
+    def setLinearSolver(self, kind: int):
+        """LINEAR_CHOLESKY (default, GTSAM's sparse Cholesky) or LINEAR_PCG."""
+        self.linear_solver = int(kind)
         return self
 
     def setSolver(self, solver):

@@ -12,7 +12,7 @@ import pytest
 from oracle import rpgo_oracle as O
 from rpgo_gb300 import capi, synth
 from rpgo_gb300.graph import Graph, diagonal_sigmas, isotropic_variance, pose2, pose3, symbol
-from rpgo_gb300.params import QUIET, RobustSolverParams
+from rpgo_gb300.params import LINEAR_CHOLESKY, LINEAR_PCG, QUIET, RobustSolverParams
 from scenarios import PCM_SCENARIOS, load_graph_scenarios, run_scenario
 
 pytestmark = pytest.mark.gpu
@@ -263,10 +263,22 @@ def _pose_close(po, pg, dim):
     assert np.max(np.abs(pg - po) / scale) <= POSE_RTOL, float(np.max(np.abs(pg - po) / scale))
 
 
+LINEAR = [LINEAR_CHOLESKY, LINEAR_PCG]
+
+
+def _check_linear_path(g, linear):
+    t = g.timing()
+    if linear == LINEAR_CHOLESKY:
+        assert t.chol_kernel_launches > 0 and t.pcg_kernel_launches == 0
+    else:
+        assert t.pcg_kernel_launches > 0 and t.chol_kernel_launches == 0
+
+
+@pytest.mark.parametrize("linear", LINEAR)
 @pytest.mark.parametrize("gnc", [False, True])
-def test_solver_3d_matches_oracle(gnc):
+def test_solver_3d_matches_oracle(gnc, linear):
     s = synth.walk3d(400, 80, 25, seed=51)
-    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setLinearSolver(linear)
     if gnc:
         p.setGncInlierCostThresholdsAtProbability(0.9)
     o, g = O.OracleSolver(p), capi.RobustSolver(p)
@@ -275,27 +287,43 @@ def test_solver_3d_matches_oracle(gnc):
     kg, pg = g.estimate()
     assert np.array_equal(ko, kg)
     _pose_close(po, pg, 3)
+    _check_linear_path(g, linear)
     if gnc:
         wo, wg = o.gnc_weights(), g.gnc_weights()
         assert np.array_equal(np.round(wo), np.round(wg))
         assert o.counts().num_lc_inliers == g.counts().num_lc_inliers
 
 
-def test_solver_2d_matches_oracle():
+@pytest.mark.parametrize("linear", LINEAR)
+def test_solver_2d_matches_oracle(linear):
     s = synth.grid2d(300, 60, 15, seed=61)
-    p = RobustSolverParams().setPcm2DParams(3.0, 3.0, QUIET)
+    p = RobustSolverParams().setPcm2DParams(3.0, 3.0, QUIET).setLinearSolver(linear)
     o, g = O.OracleSolver(p), capi.RobustSolver(p)
     assert o.update(s.graph) == 0 and g.update(s.graph) == 0
     _pose_close(o.estimate()[1], g.estimate()[1], 2)
+    _check_linear_path(g, linear)
 
 
-def test_gauss_newton_matches_oracle():
+@pytest.mark.parametrize("linear", LINEAR)
+def test_gauss_newton_matches_oracle(linear):
     s = synth.walk3d(300, 50, 0, seed=71)
-    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setLinearSolver(linear)
     p.solver = 1
     o, g = O.OracleSolver(p), capi.RobustSolver(p)
     assert o.update(s.graph) == 0 and g.update(s.graph) == 0
     _pose_close(o.estimate()[1], g.estimate()[1], 3)
+    _check_linear_path(g, linear)
+
+
+def test_direct_solve_larger_graph_matches_oracle():
+    # 2,000 poses with many closures: a dense trailing block of several tiles
+    s = synth.walk3d(2000, 500, 100, seed=53)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+    o, g = O.OracleSolver(p), capi.RobustSolver(p)
+    assert o.update(s.graph) == 0 and g.update(s.graph) == 0
+    _pose_close(o.estimate()[1], g.estimate()[1], 3)
+    assert np.array_equal(np.round(o.gnc_weights()), np.round(g.gnc_weights()))
+    _check_linear_path(g, LINEAR_CHOLESKY)
 
 
 def test_kernels_actually_launch():
