@@ -3,11 +3,12 @@
 // One cooperative kernel per solve, 256 threads per CTA, one CTA per SM.
 // Phases are separated by grid barriers:
 //  1. init: right-hand side in elimination order, padding of the dense tail;
-//  2. per elimination-tree level of the sparse columns (leaves first), one
-//     barrier each: every column of the level, by one warp (wide levels) or
-//     one CTA (narrow levels): S = H block (+ lambda D on the diagonal) -
-//     sum of L(i,k) L(j,k)^T over each block's update list, L_jj = chol(S_jj),
-//     L_ij = S_ij L_jj^-T, and the column's forward substitution;
+//  2. per elimination-tree level of the sparse columns (leaves first):
+//     (A) the level's tasks over all warps: for every block, its Hessian
+//         block minus chunks of its L(i,k) L(j,k)^T updates, and chunks of
+//         every column's forward-substitution row sum;
+//     (B) every column by one warp: S_jj from the partial sums, L_jj =
+//         chol(S_jj), L_ij = S_ij L_jj^-T, and y_j;
 //  3. the dense tail: its blocks from H and the sparse updates, then a
 //     right-looking tiled Cholesky with one barrier per tile column: in phase
 //     k the CTAs of tile column k apply the update of column k-1, factor the
@@ -17,6 +18,12 @@
 //  4. backward substitution over the tail tiles, then the sparse levels (top
 //     first); scatter to variable order; the linearised cost change with the
 //     undamped H (a fixed-order grid reduction).
+// FP64 on this part has a dependent-operation latency of about 33 ns for an
+// FMA and about 300 ns for a divide or square root, so the kernel is written
+// for instruction-level parallelism: split accumulators, right-looking
+// triangular solves (independent updates), and one reciprocal square root
+// per pivot; the factors keep the reciprocal of each pivot on their diagonal
+// and every solve multiplies by it.
 // Every sum runs in an order fixed by the plan, so results do not depend on
 // scheduling. A non-positive (or NaN) pivot sets the status flag; the factor
 // continues with pivot 1 so that every phase still ends, and the host treats
@@ -35,29 +42,42 @@ constexpr int kThreads = 256;
 
 struct CholArgs {
   int N, ns, T, ntp, n_tiles, levels;
-  const int32_t *perm, *col_ptr, *blk_row, *blk_col, *lvl_col_ptr, *lvl_cols, *lvl_blk_ptr, *lvl_blks;
+  const int32_t *perm, *col_ptr, *blk_row, *blk_col, *lvl_col_ptr, *lvl_cols, *lvl_task_ptr, *tasks, *btask, *ftask;
   const int32_t *upd_ptr, *upd_src, *tupd_ptr, *tupd_src, *a_ptr, *a_src, *ta_ptr, *ta_src;
   const int32_t *row_ptr, *row_blk, *trow_ptr, *trow_blk;
   const double *Hd64, *fH64, *dampD, *g;
   const int32_t *h_row_ptr, *h_col, *h_blk;
   const int8_t* h_btr;
   double lam;
-  double *L, *Ldiag, *M, *Ldd, *y, *delta, *part, *out;
+  double *L, *Ldiag, *M, *Ldd, *y, *delta, *part, *out, *Spart;
   int32_t* status;
 };
 
 __device__ __forceinline__ void set_fail(int32_t* status) { atomicExch(status, 1); }
 
+// dot product of length D with two accumulators (even / odd terms)
+template <int D>
+__device__ __forceinline__ double dot_ilp(const double* __restrict__ a, const double* __restrict__ b) {
+  double e = 0.0, o = 0.0;
+#pragma unroll
+  for (int t = 0; t < D; t += 2) e = fma(a[t], b[t], e);
+#pragma unroll
+  for (int t = 1; t < D; t += 2) o = fma(a[t], b[t], o);
+  return e + o;
+}
+
 // s0, s1 (the lane's entries e = lane, lane + 32 of a D x D block) -= sum
-// over the update pairs [beg, end) of (L[a] L[b]^T)(r, c), in list order.
-// The 32 lanes load the indices of 32 pairs at once and broadcast them, so
-// the block loads of consecutive pairs do not wait on an index load.
+// over the update pairs [beg, end) of (L[a] L[b]^T)(r, c). The 32 lanes load
+// the indices of 32 pairs at once and broadcast them, so the block loads of
+// consecutive pairs do not wait on an index load; four partial sums (pair
+// index mod 4) keep four products in flight.
 template <int D>
 __device__ __forceinline__ void sub_pairs_warp(const double* __restrict__ L, const int32_t* __restrict__ src, int beg,
                                                int end, int lane, double& s0, double& s1) {
   constexpr int dd = D * D;
   const int e0 = lane, e1 = lane + 32;
   const int r0 = e0 / D, c0 = e0 % D, r1 = e1 / D, c1 = e1 % D;
+  double q0[4] = {0.0, 0.0, 0.0, 0.0}, q1[4] = {0.0, 0.0, 0.0, 0.0};
   for (int base = beg; base < end; base += 32) {
     const int cnt = min(32, end - base);
     int ia = 0, ib = 0;
@@ -65,27 +85,23 @@ __device__ __forceinline__ void sub_pairs_warp(const double* __restrict__ L, con
       ia = src[2 * (base + lane)];
       ib = src[2 * (base + lane) + 1];
     }
-#pragma unroll 4
-    for (int u = 0; u < cnt; ++u) {
-      const int pa = __shfl_sync(0xffffffffu, ia, u), pb = __shfl_sync(0xffffffffu, ib, u);
-      if (e0 < dd) {
-        const double* A = L + (size_t)pa * dd + r0 * D;
-        const double* B = L + (size_t)pb * dd + c0 * D;
-        double acc = 0.0;
+    int u = 0;
+    for (; u + 4 <= cnt; u += 4) {
 #pragma unroll
-        for (int t = 0; t < D; ++t) acc = fma(A[t], B[t], acc);
-        s0 -= acc;
-      }
-      if (e1 < dd) {
-        const double* A = L + (size_t)pa * dd + r1 * D;
-        const double* B = L + (size_t)pb * dd + c1 * D;
-        double acc = 0.0;
-#pragma unroll
-        for (int t = 0; t < D; ++t) acc = fma(A[t], B[t], acc);
-        s1 -= acc;
+      for (int k = 0; k < 4; ++k) {
+        const int pa = __shfl_sync(0xffffffffu, ia, u + k), pb = __shfl_sync(0xffffffffu, ib, u + k);
+        if (e0 < dd) q0[k] += dot_ilp<D>(L + (size_t)pa * dd + r0 * D, L + (size_t)pb * dd + c0 * D);
+        if (e1 < dd) q1[k] += dot_ilp<D>(L + (size_t)pa * dd + r1 * D, L + (size_t)pb * dd + c1 * D);
       }
     }
+    for (; u < cnt; ++u) {
+      const int pa = __shfl_sync(0xffffffffu, ia, u), pb = __shfl_sync(0xffffffffu, ib, u);
+      if (e0 < dd) q0[0] += dot_ilp<D>(L + (size_t)pa * dd + r0 * D, L + (size_t)pb * dd + c0 * D);
+      if (e1 < dd) q1[0] += dot_ilp<D>(L + (size_t)pa * dd + r1 * D, L + (size_t)pb * dd + c1 * D);
+    }
   }
+  s0 -= (q0[0] + q0[1]) + (q0[2] + q0[3]);
+  s1 -= (q1[0] + q1[1]) + (q1[2] + q1[3]);
 }
 
 // Hessian entry (r, c) of the block at (row var, col var) from the factor
@@ -111,180 +127,230 @@ __device__ __forceinline__ double gather_diag(const CholArgs& a, int v, int r, i
   return s;
 }
 
-// In-register Cholesky of a D x D block (lower, row-major); false on a
-// non-positive pivot (which is replaced by 1).
+// In-register Cholesky of a D x D block (lower, row-major) with the
+// reciprocal of each pivot stored on the diagonal; false on a non-positive
+// (or NaN) pivot, which is replaced by 1.
 template <int D>
 __device__ __forceinline__ bool chol_reg(double (&C)[D * D]) {
   bool ok = true;
 #pragma unroll
   for (int c = 0; c < D; ++c) {
-    double s = C[c * D + c];
+    double e = C[c * D + c], o = 0.0;
 #pragma unroll
-    for (int t = 0; t < c; ++t) s -= C[c * D + t] * C[c * D + t];
+    for (int t = 0; t < c; t += 2) e = fma(-C[c * D + t], C[c * D + t], e);
+#pragma unroll
+    for (int t = 1; t < c; t += 2) o = fma(-C[c * D + t], C[c * D + t], o);
+    double s = e + o;
     if (!(s > 0.0)) {
       ok = false;
       s = 1.0;
     }
-    const double l = sqrt(s);
-    C[c * D + c] = l;
+    const double il = rsqrt(s);
+    C[c * D + c] = il;
 #pragma unroll
     for (int r = c + 1; r < D; ++r) {
-      double v = C[r * D + c];
+      double e2 = C[r * D + c], o2 = 0.0;
 #pragma unroll
-      for (int t = 0; t < c; ++t) v -= C[r * D + t] * C[c * D + t];
-      C[r * D + c] = v / l;
+      for (int t = 0; t < c; t += 2) e2 = fma(-C[r * D + t], C[c * D + t], e2);
+#pragma unroll
+      for (int t = 1; t < c; t += 2) o2 = fma(-C[r * D + t], C[c * D + t], o2);
+      C[r * D + c] = (e2 + o2) * il;
     }
   }
   return ok;
 }
 
-// S of sparse block p (one warp): H block (+ lambda D on the diagonal)
-// minus its update pairs; written over the block's slot of L
+constexpr unsigned kFull = 0xffffffffu;
+
+// Sparse levels use lane groups: a warp holds 32 / D groups of D lanes and
+// lane r of a group owns row r of every D x D block, so one warp-wide FP64
+// instruction serves several groups. (The FP64 pipe of this part retires two
+// lanes per cycle per SM: a warp instruction costs the same whether or not
+// its lanes do useful work.)
+
+// phase A, one warp per task: the groups take the task's entries in turn,
+// then their sums are added in group order into lanes 0 .. D-1.
+//  block task (kind 0 / 1): Spart[t] = (kind 1: H block of id, + lambda D on
+//    a diagonal block) - sum over its pairs (a, b) of L[a] L[b]^T;
+//  row task (kind 2): Spart[t][r] = sum over its row entries (block q,
+//    column k) of (L[q] y_k)[r].
 template <int D>
-__device__ void block_S(const CholArgs& a, int p, int lane) {
-  constexpr int dd = D * D;
-  const int j = a.blk_col[p], i = a.blk_row[p];
-  const int e0 = lane, e1 = lane + 32;
-  double s0 = 0.0, s1 = 0.0;
-  if (i == j) {
-    const int v = a.perm[j];
-    if (e0 < dd) s0 = gather_diag<D>(a, v, e0 / D, e0 % D);
-    if (e1 < dd) s1 = gather_diag<D>(a, v, e1 / D, e1 % D);
-  } else {
-    if (e0 < dd) s0 = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], e0 / D, e0 % D);
-    if (e1 < dd) s1 = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], e1 / D, e1 % D);
+__device__ void run_task(const CholArgs& a, int t, int lane) {
+  constexpr int G = 32 / D, dd = D * D;
+  const int g = lane / D, r = lane % D;
+  const int4 tk = reinterpret_cast<const int4*>(a.tasks)[t];
+  double acc[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) acc[c] = 0.0;
+  if (tk.w < 2) {
+    const int p = tk.x;
+    if (tk.w == 1 && g == 0) {
+      const int j = a.blk_col[p], i = a.blk_row[p];
+      if (i == j) {
+        const int v = a.perm[j];
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc[c] = gather_diag<D>(a, v, r, c);
+      } else {
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc[c] = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], r, c);
+      }
+    }
+    if (g < G) {
+      for (int u = tk.y + g; u < tk.z; u += G) {
+        const int pa = a.upd_src[2 * u], pb = a.upd_src[2 * u + 1];
+        const double* A = a.L + (size_t)pa * dd + r * D;
+        const double* B = a.L + (size_t)pb * dd;
+        double ar[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) ar[k] = A[k];
+#pragma unroll
+        for (int c = 0; c < D; ++c) acc[c] -= dot_ilp<D>(ar, B + c * D);
+      }
+    }
+  } else if (g < G) {
+    for (int u = tk.y + g; u < tk.z; u += G)
+      acc[0] += dot_ilp<D>(a.L + (size_t)a.row_blk[2 * u] * dd + r * D, a.y + (size_t)a.row_blk[2 * u + 1] * D);
   }
-  sub_pairs_warp<D>(a.L, a.upd_src, a.upd_ptr[p], a.upd_ptr[p + 1], lane, s0, s1);
-  if (e0 < dd) a.L[(size_t)p * dd + e0] = s0;
-  if (e1 < dd) a.L[(size_t)p * dd + e1] = s1;
-}
-
-// L_jj = chol(S_jj) in registers (every calling thread holds it)
-template <int D>
-__device__ __forceinline__ bool diag_factor(const CholArgs& a, int p0, double (&C)[D * D]) {
-  constexpr int dd = D * D;
+  const int nval = tk.w < 2 ? D : 1;  // warp-uniform
+  for (int c = 0; c < nval; ++c) {
+    double sum = acc[0];
 #pragma unroll
-  for (int e = 0; e < dd; ++e) C[e] = a.L[(size_t)p0 * dd + e];
-  return chol_reg<D>(C);
-}
-
-// row r of off-diagonal block q: L_qr = S_qr L_jj^-T (task t = block * D + row)
-template <int D>
-__device__ __forceinline__ void scale_row(const CholArgs& a, int p0, int t, const double (&C)[D * D]) {
-  constexpr int dd = D * D;
-  const int q = p0 + 1 + t / D, r = t % D;
-  double* S = a.L + (size_t)q * dd + r * D;
-  double x[D];
+    for (int k = 0; k < D; ++k)
+      if (k == c) sum = acc[k];
+    double tot = sum;
 #pragma unroll
-  for (int c = 0; c < D; ++c) {
-    double v = S[c];
-#pragma unroll
-    for (int k = 0; k < c; ++k) v -= x[k] * C[c * D + k];
-    x[c] = v / C[c * D + c];
+    for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, sum, (r + k * D) & 31);
+    if (lane < D) a.Spart[(size_t)t * dd + lane * D + c] = tot;
   }
-#pragma unroll
-  for (int c = 0; c < D; ++c) S[c] = x[c];
 }
 
+// sum of the task partials of block p (row r) into s
 template <int D>
-__device__ __forceinline__ void store_diag(const CholArgs& a, int j, const double (&C)[D * D], int lane) {
+__device__ __forceinline__ void sum_partials(const CholArgs& a, int p, int r, double (&s)[D]) {
   constexpr int dd = D * D;
+  const int t0 = a.btask[2 * p], nt = a.btask[2 * p + 1];
 #pragma unroll
-  for (int e = 0; e < dd; ++e)
-    if (e % 32 == lane) a.Ldiag[(size_t)j * dd + e] = (e / D >= e % D) ? C[e] : 0.0;
+  for (int c = 0; c < D; ++c) s[c] = 0.0;
+  for (int t = t0; t < t0 + nt; ++t) {
+    const double* P = a.Spart + (size_t)t * dd + r * D;
+#pragma unroll
+    for (int c = 0; c < D; ++c) s[c] += P[c];
+  }
 }
 
-template <int D>
-__device__ void sparse_forward(const CholArgs& a, int j, int lane);
-
-// whole sparse column j by one warp: S of its blocks, L_jj, L_ij, and its
+// phase B, one warp per column j: every lane group factors the diagonal
+// block (the groups hold identical copies of L_jj, right-looking Cholesky
+// across the group, reciprocal pivots on the diagonal), the groups share the
+// off-diagonal blocks L_ij = S_ij L_jj^-T, and group 0 does the column's
 // forward substitution
 template <int D>
 __device__ void column_warp(const CholArgs& a, int j, int lane) {
-  constexpr int dd = D * D;
+  constexpr int G = 32 / D, dd = D * D;
+  const int g = lane / D, r = lane % D;
+  const bool grp = g < G;
+  const int base = (grp ? g : 0) * D;
   const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
-  for (int p = p0; p < p1; ++p) block_S<D>(a, p, lane);
-  __syncwarp();
-  double C[dd];
-  const bool ok = diag_factor<D>(a, p0, C);
-  if (!ok && lane == 0) set_fail(a.status);
-  store_diag<D>(a, j, C, lane);
-  for (int t = lane; t < (p1 - p0 - 1) * D; t += 32) scale_row<D>(a, p0, t, C);
-  __syncwarp();
-  sparse_forward<D>(a, j, lane);
-}
-
-// whole sparse column j by one CTA (the warps share its blocks)
-template <int D>
-__device__ void column_cta(const CholArgs& a, int j) {
-  constexpr int dd = D * D;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-  const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
-  for (int p = p0 + warp; p < p1; p += nwarps) block_S<D>(a, p, lane);
-  __syncthreads();
-  double C[dd];
-  const bool ok = diag_factor<D>(a, p0, C);
-  if (!ok && threadIdx.x == 0) set_fail(a.status);
-  if (warp == 0) store_diag<D>(a, j, C, lane);
-  for (int t = threadIdx.x; t < (p1 - p0 - 1) * D; t += blockDim.x) scale_row<D>(a, p0, t, C);
-  __syncthreads();
-  if (warp == 0) sparse_forward<D>(a, j, lane);
-  __syncthreads();
-}
-
-// forward substitution of sparse column j: y_j = L_jj^-1 (y_j - sum L_jk y_k)
-template <int D>
-__device__ void sparse_forward(const CholArgs& a, int j, int lane) {
-  constexpr int dd = D * D;
-  double b = 0.0;
-  if (lane < D) {
-    b = a.y[(size_t)j * D + lane];
-    for (int u = a.row_ptr[j]; u < a.row_ptr[j + 1]; ++u) {
-      const int q = a.row_blk[u];
-      const double* B = a.L + (size_t)q * dd + lane * D;
-      const double* yk = a.y + (size_t)a.blk_col[q] * D;
-      double acc = 0.0;
+  double C[D];
+  sum_partials<D>(a, p0, r, C);
+  bool ok = true;
 #pragma unroll
-      for (int c = 0; c < D; ++c) acc = fma(B[c], yk[c], acc);
-      b -= acc;
+  for (int c = 0; c < D; ++c) {
+    if (r == c) {
+      double piv = C[c];
+      if (!(piv > 0.0)) {
+        ok = false;
+        piv = 1.0;
+      }
+      C[c] = rsqrt(piv);
+    }
+    const double ilc = __shfl_sync(kFull, C[c], base + c);
+    if (r > c) C[c] *= ilc;
+#pragma unroll
+    for (int q = c + 1; q < D; ++q) {
+      const double lqc = __shfl_sync(kFull, C[c], base + q);
+      if (r >= q) C[q] = fma(-C[c], lqc, C[q]);
     }
   }
-  const double* Lj = a.Ldiag + (size_t)j * dd;
+  const bool bad = __any_sync(kFull, !ok && g == 0);
+  if (lane == 0 && bad) set_fail(a.status);
+  double Lf[dd];
+#pragma unroll
+  for (int q = 0; q < D; ++q)
+#pragma unroll
+    for (int c = 0; c <= q; ++c) Lf[q * D + c] = __shfl_sync(kFull, C[c], base + q);
+  if (g == 0) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) a.Ldiag[(size_t)j * dd + r * D + c] = (c <= r) ? C[c] : 0.0;
+  }
+  if (grp) {
+    for (int p = p0 + 1 + g; p < p1; p += G) {
+      double sv[D];
+      sum_partials<D>(a, p, r, sv);
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        const double x = sv[c] * Lf[c * D + c];
+        sv[c] = x;
+#pragma unroll
+        for (int k = c + 1; k < D; ++k) sv[k] = fma(-x, Lf[k * D + c], sv[k]);
+      }
+#pragma unroll
+      for (int c = 0; c < D; ++c) a.L[(size_t)p * dd + r * D + c] = sv[c];
+    }
+  }
+  // forward substitution: y_j = L_jj^-1 (y_j - row sums)
+  double b = a.y[(size_t)j * D + r];
+  {
+    const int t0 = a.ftask[2 * j], nt = a.ftask[2 * j + 1];
+    double acc = 0.0;
+    for (int t = t0; t < t0 + nt; ++t) acc += a.Spart[(size_t)t * dd + r * D];
+    b -= acc;
+  }
   double yv = 0.0;
 #pragma unroll
   for (int c = 0; c < D; ++c) {
-    if (lane == c) yv = b / Lj[c * D + c];
-    const double yc = __shfl_sync(0xffffffffu, yv, c);
-    if (lane > c && lane < D) b -= Lj[lane * D + c] * yc;
+    if (r == c) yv = b * Lf[c * D + c];
+    const double yc = __shfl_sync(kFull, yv, base + c);
+    if (r > c) b = fma(-C[c], yc, b);
   }
-  if (lane < D) a.y[(size_t)j * D + lane] = yv;
+  if (g == 0) a.y[(size_t)j * D + r] = yv;
 }
 
-// backward substitution of sparse column j: x_j = L_jj^-T (y_j - sum L_ij^T x_i)
+// backward substitution of column j by one warp:
+// x_j = L_jj^-T (y_j - sum L_ij^T x_i), the groups share the blocks
 template <int D>
-__device__ void sparse_backward(const CholArgs& a, int j, int lane) {
-  constexpr int dd = D * D;
-  double b = 0.0;
-  if (lane < D) {
-    b = a.y[(size_t)j * D + lane];
-    for (int q = a.col_ptr[j] + 1; q < a.col_ptr[j + 1]; ++q) {
-      const double* B = a.L + (size_t)q * dd;
+__device__ void backward_warp(const CholArgs& a, int j, int lane) {
+  constexpr int G = 32 / D, dd = D * D;
+  const int g = lane / D, r = lane % D;
+  const int base = (g < G ? g : 0) * D;
+  double acc = 0.0;
+  if (g < G) {
+    const int q1 = a.col_ptr[j + 1];
+    for (int q = a.col_ptr[j] + 1 + g; q < q1; q += G) {
+      const double* B = a.L + (size_t)q * dd + r;
       const double* xi = a.y + (size_t)a.blk_row[q] * D;
-      double acc = 0.0;
+      double e = 0.0, o = 0.0;
 #pragma unroll
-      for (int r = 0; r < D; ++r) acc = fma(B[r * D + lane], xi[r], acc);
-      b -= acc;
+      for (int k = 0; k < D; k += 2) e = fma(B[k * D], xi[k], e);
+#pragma unroll
+      for (int k = 1; k < D; k += 2) o = fma(B[k * D], xi[k], o);
+      acc += e + o;
     }
   }
-  const double* Lj = a.Ldiag + (size_t)j * dd;
+  double tot = acc;
+#pragma unroll
+  for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, acc, (r + k * D) & 31);
+  double b = a.y[(size_t)j * D + r] - tot;
+  double Lc[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) Lc[c] = a.Ldiag[(size_t)j * dd + c * D + r];
   double xv = 0.0;
 #pragma unroll
   for (int c = D - 1; c >= 0; --c) {
-    if (lane == c) xv = b / Lj[c * D + c];
-    const double xc = __shfl_sync(0xffffffffu, xv, c);
-    if (lane < c) b -= Lj[c * D + lane] * xc;
+    if (r == c) xv = b * Lc[c];
+    const double xc = __shfl_sync(kFull, xv, base + c);
+    if (r < c) b = fma(-Lc[c], xc, b);
   }
-  if (lane < D) a.y[(size_t)j * D + lane] = xv;
+  if (g == 0) a.y[(size_t)j * D + r] = xv;
 }
 
 __device__ __forceinline__ void tail_coords(int t, int& bi, int& bj) {
@@ -316,22 +382,20 @@ __device__ void tail_S(const CholArgs& a, int t, int lane) {
   if (e1 < dd) a.M[(size_t)(bj * D + e1 % D) * a.ntp + bi * D + e1 / D] = s1;
 }
 
-// tail right-hand side: y_t -= sum over sparse blocks in tail block row t
+// tail right-hand side: y_t -= sum over the sparse blocks in tail block row t
+// (trow_blk holds (block, column) pairs)
 template <int D>
 __device__ void tail_rhs(const CholArgs& a, int t, int lane) {
   constexpr int dd = D * D;
   if (lane >= D) return;
-  double b = 0.0;
-  for (int u = a.trow_ptr[t]; u < a.trow_ptr[t + 1]; ++u) {
-    const int q = a.trow_blk[u];
-    const double* B = a.L + (size_t)q * dd + lane * D;
-    const double* yk = a.y + (size_t)a.blk_col[q] * D;
-    double acc = 0.0;
-#pragma unroll
-    for (int c = 0; c < D; ++c) acc = fma(B[c], yk[c], acc);
-    b += acc;
+  double acc0 = 0.0, acc1 = 0.0;
+  const int u1 = a.trow_ptr[t + 1];
+  for (int u = a.trow_ptr[t]; u < u1; ++u) {
+    const double v = dot_ilp<D>(a.L + (size_t)a.trow_blk[2 * u] * dd + lane * D, a.y + (size_t)a.trow_blk[2 * u + 1] * D);
+    if (u & 1) acc1 += v;
+    else acc0 += v;
   }
-  a.y[(size_t)(a.ns + t) * D + lane] -= b;
+  a.y[(size_t)(a.ns + t) * D + lane] -= acc0 + acc1;
 }
 
 struct TileSmem {
@@ -355,19 +419,24 @@ __device__ void load_tile(const CholArgs& a, int ti, int tj, double (*S)[kTB + 1
   }
 }
 
+__device__ __forceinline__ double tile_dot(const double* __restrict__ p, const double* __restrict__ q) {
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+  for (int t = 0; t < kTB; ++t) acc[t & 3] = fma(p[t], q[t], acc[t & 3]);
+  return (acc[0] + acc[1]) + (acc[2] + acc[3]);
+}
+
 // X[r][c] -= sum_t P[r][t] Q[c][t] (lower part only when lower_only)
 __device__ void smem_update(double (*X)[kTB + 1], double (*P)[kTB + 1], double (*Q)[kTB + 1], bool lower_only) {
   for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
     const int r = e % kTB, c = e / kTB;
     if (lower_only && c > r) continue;
-    double acc = 0.0;
-#pragma unroll
-    for (int t = 0; t < kTB; ++t) acc = fma(P[r][t], Q[c][t], acc);
-    X[r][c] -= acc;
+    X[r][c] -= tile_dot(P[r], Q[c]);
   }
 }
 
-// Cholesky of the lower part of X in place (right-looking)
+// Cholesky of the lower part of X in place (right-looking); the diagonal
+// keeps the reciprocal of each pivot
 __device__ void smem_chol(double (*X)[kTB + 1], int32_t* status) {
   for (int c = 0; c < kTB; ++c) {
     if (threadIdx.x == 0) {
@@ -376,16 +445,16 @@ __device__ void smem_chol(double (*X)[kTB + 1], int32_t* status) {
         set_fail(status);
         piv = 1.0;
       }
-      X[c][c] = sqrt(piv);
+      X[c][c] = rsqrt(piv);
     }
     __syncthreads();
-    const double l = X[c][c];
-    for (int r = c + 1 + threadIdx.x; r < kTB; r += blockDim.x) X[r][c] /= l;
+    const double il = X[c][c];
+    for (int r = c + 1 + threadIdx.x; r < kTB; r += blockDim.x) X[r][c] *= il;
     __syncthreads();
     const int m = kTB - c - 1;
     for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
       const int r = c + 1 + e % m, q = c + 1 + e / m;
-      if (q <= r) X[r][q] -= X[r][c] * X[q][c];
+      if (q <= r) X[r][q] = fma(-X[r][c], X[q][c], X[r][q]);
     }
     __syncthreads();
   }
@@ -413,13 +482,13 @@ __device__ void tail_column_item(const CholArgs& a, int i, int k, TileSmem& s) {
       O[e] = (c <= r) ? s.C[r][c] : 0.0;
     }
   } else {
-    // row r of the tile: x = A[r] L^-T
+    // row r of the tile: x = A[r] L^-T, right-looking (independent updates)
     if (threadIdx.x < kTB) {
       const int r = threadIdx.x;
       for (int c = 0; c < kTB; ++c) {
-        double v = s.A[r][c];
-        for (int t = 0; t < c; ++t) v -= s.A[r][t] * s.C[c][t];
-        s.A[r][c] = v / s.C[c][c];
+        const double x = s.A[r][c] * s.C[c][c];
+        s.A[r][c] = x;
+        for (int k = c + 1; k < kTB; ++k) s.A[r][k] = fma(-x, s.C[k][c], s.A[r][k]);
       }
     }
     __syncthreads();
@@ -441,10 +510,7 @@ __device__ void tail_trailing_item(const CholArgs& a, int i, int j, int k, TileS
   for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
     const int r = e % kTB, c = e / kTB;
     if (i == j && c > r) continue;
-    double acc = 0.0;
-#pragma unroll
-    for (int t = 0; t < kTB; ++t) acc = fma(s.A[r][t], s.B[c][t], acc);
-    P[(size_t)c * a.ntp + r] -= acc;
+    P[(size_t)c * a.ntp + r] -= tile_dot(s.A[r], s.B[c]);
   }
   __syncthreads();
 }
@@ -456,10 +522,15 @@ __device__ void tail_forward_item(const CholArgs& a, double* yt, int k, TileSmem
   const int ncol = k * kTB;
   if (threadIdx.x < chunks * kTB) {
     const int r = threadIdx.x % kTB, ch = threadIdx.x / kTB;
-    double acc = 0.0;
+    double acc0 = 0.0, acc1 = 0.0;
     const double* P = a.M + k * kTB + r;
-    for (int c = ch; c < ncol; c += chunks) acc = fma(P[(size_t)c * a.ntp], yt[c], acc);
-    s.red[ch][r] = acc;
+    int c = ch;
+    for (; c + chunks < ncol; c += 2 * chunks) {
+      acc0 = fma(P[(size_t)c * a.ntp], yt[c], acc0);
+      acc1 = fma(P[(size_t)(c + chunks) * a.ntp], yt[c + chunks], acc1);
+    }
+    if (c < ncol) acc0 = fma(P[(size_t)c * a.ntp], yt[c], acc0);
+    s.red[ch][r] = acc0 + acc1;
   }
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -472,9 +543,9 @@ __device__ void tail_forward_item(const CholArgs& a, double* yt, int k, TileSmem
     const double* Lk = a.Ldd + (size_t)k * kTB * kTB;
     double yv = 0.0;
     for (int c = 0; c < kTB; ++c) {
-      if (lane == c) yv = b / Lk[c * kTB + c];
+      if (lane == c) yv = b * Lk[c * kTB + c];
       const double yc = __shfl_sync(0xffffffffu, yv, c);
-      if (lane > c && lane < kTB) b -= Lk[lane * kTB + c] * yc;
+      if (lane > c && lane < kTB) b = fma(-Lk[lane * kTB + c], yc, b);
     }
     if (lane < kTB) yt[k * kTB + lane] = yv;
   }
@@ -488,10 +559,15 @@ __device__ void tail_backward_item(const CholArgs& a, double* yt, int k, TileSme
   const int r0 = (k + 1) * kTB;
   if (threadIdx.x < chunks * kTB) {
     const int c = threadIdx.x % kTB, ch = threadIdx.x / kTB;
-    double acc = 0.0;
+    double acc0 = 0.0, acc1 = 0.0;
     const double* P = a.M + (size_t)(k * kTB + c) * a.ntp;
-    for (int r = r0 + ch; r < a.ntp; r += chunks) acc = fma(P[r], yt[r], acc);
-    s.red[ch][c] = acc;
+    int r = r0 + ch;
+    for (; r + chunks < a.ntp; r += 2 * chunks) {
+      acc0 = fma(P[r], yt[r], acc0);
+      acc1 = fma(P[r + chunks], yt[r + chunks], acc1);
+    }
+    if (r < a.ntp) acc0 = fma(P[r], yt[r], acc0);
+    s.red[ch][c] = acc0 + acc1;
   }
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -504,9 +580,9 @@ __device__ void tail_backward_item(const CholArgs& a, double* yt, int k, TileSme
     const double* Lk = a.Ldd + (size_t)k * kTB * kTB;
     double xv = 0.0;
     for (int c = kTB - 1; c >= 0; --c) {
-      if (lane == c) xv = b / Lk[c * kTB + c];
+      if (lane == c) xv = b * Lk[c * kTB + c];
       const double xc = __shfl_sync(0xffffffffu, xv, c);
-      if (lane < c) b -= Lk[c * kTB + lane] * xc;
+      if (lane < c) b = fma(-Lk[c * kTB + lane], xc, b);
     }
     if (lane < kTB) yt[k * kTB + lane] = xv;
   }
@@ -555,15 +631,14 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   }
   grid.sync();
 
-  // 2. sparse levels, one barrier each: a level with at least as many
-  // columns as CTAs gives a column to a warp, a narrower one to a CTA
+  // 2. sparse levels: (A) the level's tasks over all warps, (B) its
+  // columns, one warp each; one barrier after each
   for (int l = 0; l < a.levels; ++l) {
+    const int t0 = a.lvl_task_ptr[l], t1 = a.lvl_task_ptr[l + 1];
+    for (int t = t0 + gw; t < t1; t += nw) run_task<D>(a, t, lane);
+    grid.sync();
     const int c0 = a.lvl_col_ptr[l], nc = a.lvl_col_ptr[l + 1] - c0;
-    if (nc >= (int)gridDim.x) {
-      for (int w = gw; w < nc; w += nw) column_warp<D>(a, a.lvl_cols[c0 + w], lane);
-    } else {
-      for (int c = blockIdx.x; c < nc; c += gridDim.x) column_cta<D>(a, a.lvl_cols[c0 + c]);
-    }
+    for (int w = gw; w < nc; w += nw) column_warp<D>(a, a.lvl_cols[c0 + w], lane);
     grid.sync();
   }
 
@@ -601,8 +676,8 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
     grid.sync();
   }
   for (int l = a.levels - 1; l >= 0; --l) {
-    const int c0 = a.lvl_col_ptr[l], c1 = a.lvl_col_ptr[l + 1];
-    for (int w = gw; w < c1 - c0; w += nw) sparse_backward<D>(a, a.lvl_cols[c0 + w], lane);
+    const int c0 = a.lvl_col_ptr[l], nc = a.lvl_col_ptr[l + 1] - c0;
+    for (int w = gw; w < nc; w += nw) backward_warp<D>(a, a.lvl_cols[c0 + w], lane);
     grid.sync();
   }
   for (int k = gt; k < n; k += gs) {
@@ -611,39 +686,33 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   }
   grid.sync();
 
-  // model change with the undamped H: -g.delta - delta^T H delta / 2
+  // model change with the undamped H: -g.delta - delta^T H delta / 2;
+  // consecutive variables go to different CTAs (the FP64 work spreads over
+  // every SM), partial sums are added in a fixed order
   double gd = 0.0, dhd = 0.0;
-  for (int v = gt; v < a.N; v += gs) {
+  for (int k = threadIdx.x;; k += blockDim.x) {
+    const int v = blockIdx.x + (int)gridDim.x * k;
+    if (v >= a.N) break;
     double acc[D];
     const double* H = a.Hd64 + (size_t)v * dd;
     const double* pv = a.delta + (size_t)v * D;
 #pragma unroll
-    for (int r = 0; r < D; ++r) {
-      double s = 0.0;
-#pragma unroll
-      for (int c = 0; c < D; ++c) s += H[D * r + c] * pv[c];
-      acc[r] = s;
-    }
-    for (int k = a.h_row_ptr[v]; k < a.h_row_ptr[v + 1]; ++k) {
-      const double* B = a.fH64 + (size_t)a.h_blk[k] * 3 * dd + 2 * dd;
-      const double* pc = a.delta + (size_t)a.h_col[k] * D;
-      if (a.h_btr[k]) {
+    for (int r = 0; r < D; ++r) acc[r] = dot_ilp<D>(H + D * r, pv);
+    for (int k2 = a.h_row_ptr[v]; k2 < a.h_row_ptr[v + 1]; ++k2) {
+      const double* B = a.fH64 + (size_t)a.h_blk[k2] * 3 * dd + 2 * dd;
+      const double* pc = a.delta + (size_t)a.h_col[k2] * D;
+      if (a.h_btr[k2]) {
 #pragma unroll
         for (int r = 0; r < D; ++r)
 #pragma unroll
-          for (int c = 0; c < D; ++c) acc[r] += B[D * c + r] * pc[c];
+          for (int c = 0; c < D; ++c) acc[r] = fma(B[D * c + r], pc[c], acc[r]);
       } else {
 #pragma unroll
-        for (int r = 0; r < D; ++r)
-#pragma unroll
-          for (int c = 0; c < D; ++c) acc[r] += B[D * r + c] * pc[c];
+        for (int r = 0; r < D; ++r) acc[r] += dot_ilp<D>(B + D * r, pc);
       }
     }
-#pragma unroll
-    for (int r = 0; r < D; ++r) {
-      gd += a.g[(size_t)v * D + r] * pv[r];
-      dhd += pv[r] * acc[r];
-    }
+    gd += dot_ilp<D>(a.g + (size_t)v * D, pv);
+    dhd += dot_ilp<D>(pv, acc);
   }
   gd = cta_sum(gd, shr);
   dhd = cta_sum(dhd, shr);
@@ -652,13 +721,18 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
     a.part[2 * blockIdx.x + 1] = dhd;
   }
   grid.sync();
-  if (gt == 0) {
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
     double sg = 0.0, sh = 0.0;
-    for (int b = 0; b < (int)gridDim.x; ++b) {
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
       sg += a.part[2 * b];
       sh += a.part[2 * b + 1];
     }
-    a.out[0] = -sg - 0.5 * sh;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      sg += __shfl_xor_sync(kFull, sg, o);
+      sh += __shfl_xor_sync(kFull, sh, o);
+    }
+    if (threadIdx.x == 0) a.out[0] = -sg - 0.5 * sh;
   }
 }
 
@@ -674,8 +748,11 @@ void CholDev::upload(CholPlan&& p, cudaStream_t st) {
   blk_col.upload(plan.blk_col, st);
   lvl_col_ptr.upload(plan.lvl_col_ptr, st);
   lvl_cols.upload(plan.lvl_cols, st);
-  lvl_blk_ptr.upload(plan.lvl_blk_ptr, st);
-  lvl_blks.upload(plan.lvl_blks, st);
+  lvl_task_ptr.upload(plan.lvl_task_ptr, st);
+  tasks.upload(plan.tasks, st);
+  btask.upload(plan.btask, st);
+  ftask.upload(plan.ftask, st);
+  Spart.resize(std::max<size_t>(1, plan.tasks.size() / 4 * (size_t)plan.d * plan.d));
   upd_ptr.upload(plan.upd_ptr, st);
   upd_src.upload(plan.upd_src, st);
   tupd_ptr.upload(plan.tupd_ptr, st);
@@ -715,11 +792,12 @@ SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st) {
   const CholPlan& p = c.plan;
   CholArgs a{s.N, p.n_sparse, p.T, p.n_tiles * kTB, p.n_tiles, c.levels,
              c.perm.get(), c.col_ptr.get(), c.blk_row.get(), c.blk_col.get(), c.lvl_col_ptr.get(), c.lvl_cols.get(),
-             c.lvl_blk_ptr.get(), c.lvl_blks.get(), c.upd_ptr.get(), c.upd_src.get(), c.tupd_ptr.get(),
+             c.lvl_task_ptr.get(), c.tasks.get(), c.btask.get(), c.ftask.get(), c.upd_ptr.get(), c.upd_src.get(), c.tupd_ptr.get(),
              c.tupd_src.get(), c.a_ptr.get(), c.a_src.get(), c.ta_ptr.get(), c.ta_src.get(), c.row_ptr.get(),
              c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
              s.g.get(), s.row_ptr.get(), s.col.get(), s.blk.get(), s.btr.get(), lambda, c.L.get(), c.Ldiag.get(),
-             c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.status.get()};
+             c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.Spart.get(),
+             c.status.get()};
   void* args[] = {&a};
   double ms = 0.0;
   {

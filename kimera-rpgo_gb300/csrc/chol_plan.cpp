@@ -366,24 +366,12 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
     if (!cols[j].empty() && cols[j][0] < ns) lvl[cols[j][0]] = std::max(lvl[cols[j][0]], lvl[j] + 1);
   }
   p.lvl_col_ptr.assign(L + 1, 0);
-  p.lvl_blk_ptr.assign(L + 1, 0);
-  for (int j = 0; j < ns; ++j) {
-    p.lvl_col_ptr[lvl[j] + 1] += 1;
-    p.lvl_blk_ptr[lvl[j] + 1] += p.col_ptr[j + 1] - p.col_ptr[j];
-  }
-  for (int l = 0; l < L; ++l) {
-    p.lvl_col_ptr[l + 1] += p.lvl_col_ptr[l];
-    p.lvl_blk_ptr[l + 1] += p.lvl_blk_ptr[l];
-  }
+  for (int j = 0; j < ns; ++j) p.lvl_col_ptr[lvl[j] + 1] += 1;
+  for (int l = 0; l < L; ++l) p.lvl_col_ptr[l + 1] += p.lvl_col_ptr[l];
   p.lvl_cols.resize(ns);
-  p.lvl_blks.resize(p.col_ptr[ns]);
   {
-    std::vector<int32_t> cc(p.lvl_col_ptr.begin(), p.lvl_col_ptr.end() - 1),
-        bc(p.lvl_blk_ptr.begin(), p.lvl_blk_ptr.end() - 1);
-    for (int j = 0; j < ns; ++j) {
-      p.lvl_cols[cc[lvl[j]]++] = j;
-      for (int q = p.col_ptr[j]; q < p.col_ptr[j + 1]; ++q) p.lvl_blks[bc[lvl[j]]++] = q;
-    }
+    std::vector<int32_t> cc(p.lvl_col_ptr.begin(), p.lvl_col_ptr.end() - 1);
+    for (int j = 0; j < ns; ++j) p.lvl_cols[cc[lvl[j]]++] = j;
   }
 
   // updates: for each sparse column k and rows ra <= rb of it, target (rb, ra)
@@ -478,15 +466,56 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
   }
   for (int j = 0; j < ns; ++j) p.row_ptr[j + 1] += p.row_ptr[j];
   for (int t = 0; t < T; ++t) p.trow_ptr[t + 1] += p.trow_ptr[t];
-  p.row_blk.resize(p.row_ptr[ns]);
-  p.trow_blk.resize(p.trow_ptr[T]);
+  p.row_blk.resize((size_t)2 * p.row_ptr[ns]);
+  p.trow_blk.resize((size_t)2 * p.trow_ptr[T]);
   {
     std::vector<int32_t> fr(p.row_ptr.begin(), p.row_ptr.end() - 1), ft(p.trow_ptr.begin(), p.trow_ptr.end() - 1);
     for (int q = 0; q < nblk; ++q) {
       const int r = p.blk_row[q];
       if (r == p.blk_col[q]) continue;
-      if (r < ns) p.row_blk[fr[r]++] = q;
-      else p.trow_blk[ft[r - ns]++] = q;
+      if (r < ns) {
+        const int u = fr[r]++;
+        p.row_blk[2 * u] = q;
+        p.row_blk[2 * u + 1] = p.blk_col[q];
+      } else {
+        const int u = ft[r - ns]++;
+        p.trow_blk[2 * u] = q;
+        p.trow_blk[2 * u + 1] = p.blk_col[q];
+      }
+    }
+  }
+  // tasks, level by level: every block of a level's columns (its Hessian
+  // block and update chunks), then the row sums of the level's columns
+  p.chunk = 2 * (32 / d);
+  p.row_chunk = 4 * (32 / d);
+  p.lvl_task_ptr.assign(L + 1, 0);
+  p.btask.assign((size_t)2 * nblk, 0);
+  p.ftask.assign((size_t)2 * ns, 0);
+  p.tasks.clear();
+  {
+    int nt = 0;
+    for (int l = 0; l < L; ++l) {
+      for (int w = p.lvl_col_ptr[l]; w < p.lvl_col_ptr[l + 1]; ++w) {
+        const int j = p.lvl_cols[w];
+        for (int q = p.col_ptr[j]; q < p.col_ptr[j + 1]; ++q) {
+          p.btask[2 * q] = nt;
+          int u = p.upd_ptr[q];
+          do {
+            const int e = std::min(u + p.chunk, p.upd_ptr[q + 1]);
+            p.tasks.insert(p.tasks.end(), {q, u, e, u == p.upd_ptr[q] ? 1 : 0});
+            ++nt;
+            u = e;
+          } while (u < p.upd_ptr[q + 1]);
+          p.btask[2 * q + 1] = nt - p.btask[2 * q];
+        }
+        p.ftask[2 * j] = nt;
+        for (int u = p.row_ptr[j]; u < p.row_ptr[j + 1]; u += p.row_chunk) {
+          p.tasks.insert(p.tasks.end(), {j, u, std::min(u + p.row_chunk, p.row_ptr[j + 1]), 2});
+          ++nt;
+        }
+        p.ftask[2 * j + 1] = nt - p.ftask[2 * j];
+      }
+      p.lvl_task_ptr[l + 1] = nt;
     }
   }
   const double dd3 = (double)d * d * d, nt = (double)T * d;

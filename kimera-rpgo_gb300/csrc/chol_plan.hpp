@@ -35,7 +35,16 @@ struct CholPlan {
   std::vector<int32_t> blk_col;  // column position of each block
   // elimination-tree levels of the sparse columns (leaves first)
   std::vector<int32_t> lvl_col_ptr, lvl_cols;  // columns per level
-  std::vector<int32_t> lvl_blk_ptr, lvl_blks;  // blocks of those columns, per level
+  // Tasks of the sparse levels, 4 ints each (id, first, end, kind):
+  //  kind 0 / 1: block id's update list [first, end) cut into chunks of at
+  //    most `chunk` pairs (kind 1 on the block's first chunk, which also
+  //    carries the Hessian block);
+  //  kind 2: the forward-substitution row sum of column id over its row
+  //    list entries [first, end) (chunks of at most `row_chunk`).
+  // Tasks of one level are contiguous (lvl_task_ptr); so are the tasks of
+  // one block (btask: first, count) and of one column's row (ftask).
+  int chunk = 10, row_chunk = 20;
+  std::vector<int32_t> lvl_task_ptr, tasks, btask, ftask;
   // updates: target -= sum over (a, b) of L[a] * L[b]^T, as flat pairs
   std::vector<int32_t> upd_ptr, upd_src;    // sparse targets (per block)
   std::vector<int32_t> tupd_ptr, tupd_src;  // tail targets (lower blocks bi >= bj, index bi*(bi+1)/2 + bj)
@@ -43,7 +52,8 @@ struct CholPlan {
   std::vector<int32_t> a_ptr, a_src;    // sparse targets
   std::vector<int32_t> ta_ptr, ta_src;  // tail targets
   // forward solve: per sparse row j, its off-diagonal blocks (j, k), k < j;
-  // per tail block row t, the sparse blocks in that row
+  // per tail block row t, the sparse blocks in that row; both as (block,
+  // column) pairs
   std::vector<int32_t> row_ptr, row_blk;
   std::vector<int32_t> trow_ptr, trow_blk;
   int levels() const { return (int)lvl_col_ptr.size() - 1; }

@@ -67,12 +67,34 @@ struct Emu {
       }
     }
   }
+  std::vector<double> Spart;  // task partial sums
+  void run_task(int t) {
+    const int* tk = &p.tasks[4 * (size_t)t];
+    if (tk[3] < 2) {
+      const int q = tk[0], j = p.blk_col[q], i = p.blk_row[q];
+      for (int e = 0; e < dd; ++e) {
+        const int r = e / d, c = e % d;
+        double s = 0.0;
+        if (tk[3] == 1)
+          s = i == j ? diag_entry(p.perm[j], r, c) : offdiag_entry(p.a_src, p.a_ptr[q], p.a_ptr[q + 1], r, c);
+        Spart[(size_t)t * dd + e] = pairs(p.upd_src, tk[1], tk[2], r, c, s);
+      }
+    } else {
+      for (int r = 0; r < d; ++r) {
+        double b = 0.0;
+        for (int u = tk[1]; u < tk[2]; ++u) {
+          const int q = p.row_blk[2 * u], k = p.row_blk[2 * u + 1];
+          for (int c = 0; c < d; ++c) b += L[(size_t)q * dd + r * d + c] * y[(size_t)k * d + c];
+        }
+        Spart[(size_t)t * dd + r * d] = b;
+      }
+    }
+  }
   void sparse_S(int q) {
-    const int j = p.blk_col[q], i = p.blk_row[q];
     for (int e = 0; e < dd; ++e) {
-      const int r = e / d, c = e % d;
-      double s = i == j ? diag_entry(p.perm[j], r, c) : offdiag_entry(p.a_src, p.a_ptr[q], p.a_ptr[q + 1], r, c);
-      L[(size_t)q * dd + e] = pairs(p.upd_src, p.upd_ptr[q], p.upd_ptr[q + 1], r, c, s);
+      double s = 0.0;
+      for (int t = p.btask[2 * q]; t < p.btask[2 * q] + p.btask[2 * q + 1]; ++t) s += Spart[(size_t)t * dd + e];
+      L[(size_t)q * dd + e] = s;
     }
   }
   void sparse_scale(int q) {
@@ -97,10 +119,7 @@ struct Emu {
     std::vector<double> b(d);
     for (int r = 0; r < d; ++r) {
       b[r] = y[(size_t)j * d + r];
-      for (int u = p.row_ptr[j]; u < p.row_ptr[j + 1]; ++u) {
-        const int q = p.row_blk[u];
-        for (int c = 0; c < d; ++c) b[r] -= L[(size_t)q * dd + r * d + c] * y[(size_t)p.blk_col[q] * d + c];
-      }
+      for (int t = p.ftask[2 * j]; t < p.ftask[2 * j] + p.ftask[2 * j + 1]; ++t) b[r] -= Spart[(size_t)t * dd + r * d];
     }
     const double* Lj = &Ldiag[(size_t)j * dd];
     for (int c = 0; c < d; ++c) {
@@ -144,8 +163,8 @@ struct Emu {
     for (int r = 0; r < d; ++r) {
       double b = 0.0;
       for (int u = p.trow_ptr[t]; u < p.trow_ptr[t + 1]; ++u) {
-        const int q = p.trow_blk[u];
-        for (int c = 0; c < d; ++c) b += L[(size_t)q * dd + r * d + c] * y[(size_t)p.blk_col[q] * d + c];
+        const int q = p.trow_blk[2 * u], k = p.trow_blk[2 * u + 1];
+        for (int c = 0; c < d; ++c) b += L[(size_t)q * dd + r * d + c] * y[(size_t)k * d + c];
       }
       y[(size_t)(p.n_sparse + t) * d + r] -= b;
     }
@@ -276,7 +295,10 @@ extern "C" int chol_emulate(int N, int d, int F, const int32_t* kind, const int3
     }
   // 2. sparse levels
   const int levels = p.levels();
-  for (int l = 0; l < levels; ++l)
+  e.Spart.assign(p.tasks.size() / 4 * (size_t)dd, 0.0);
+  for (int l = 0; l < levels; ++l) {
+    // (A) the level's update tasks, (B) its columns
+    for (int t = p.lvl_task_ptr[l]; t < p.lvl_task_ptr[l + 1]; ++t) e.run_task(t);
     for (int w = p.lvl_col_ptr[l]; w < p.lvl_col_ptr[l + 1]; ++w) {
       // one column: S of its blocks, L_jj and L_ij, its forward substitution
       const int j = p.lvl_cols[w];
@@ -284,6 +306,7 @@ extern "C" int chol_emulate(int N, int d, int F, const int32_t* kind, const int3
       for (int q = p.col_ptr[j]; q < p.col_ptr[j + 1]; ++q) e.sparse_scale(q);
       e.sparse_forward(j);
     }
+  }
   // 3. tail
   for (int t = 0; t < p.n_tail_blocks(); ++t) e.tail_S(t);
   double* yt = e.y.data() + (size_t)ns * d;
