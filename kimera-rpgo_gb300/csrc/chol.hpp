@@ -16,14 +16,15 @@ struct CholDev {
   int levels = 0;
   DeviceBuffer<int32_t> perm, col_ptr, blk_row, blk_col, lvl_col_ptr, lvl_cols, lvl_task_ptr, tasks, btask, ftask;
   DeviceBuffer<int32_t> upd_ptr, upd_src, tupd_ptr, tupd_src, a_ptr, a_src, ta_ptr, ta_src;
-  DeviceBuffer<int32_t> row_ptr, row_blk, trow_ptr, trow_blk;
+  DeviceBuffer<int32_t> row_ptr, row_blk, trow_ptr, trow_blk, ttasks, ttask_ptr;
   DeviceBuffer<double> L;     // sparse blocks of L (off-diagonal; the diagonal slots are unused)
   DeviceBuffer<double> Ldiag; // factors of the sparse diagonal blocks (reciprocal pivots on the diagonal)
   DeviceBuffer<double> M;     // dense tail, column-major, padded to whole tiles
   DeviceBuffer<double> Ldd;   // factors of the tail's diagonal tiles (reciprocal pivots on the diagonal)
   DeviceBuffer<double> y;     // right-hand side / solution in elimination order
   DeviceBuffer<double> part;  // per-CTA partial sums
-  DeviceBuffer<double> Spart; // update-task partial sums (D x D per task)
+  DeviceBuffer<double> Spart; // level-task partial sums (D x D per task)
+  DeviceBuffer<double> Tpart; // tail row task sums (D per task)
   DeviceBuffer<double> out;   // model change, status
   DeviceBuffer<int32_t> status;
   void upload(CholPlan&& p, cudaStream_t st);

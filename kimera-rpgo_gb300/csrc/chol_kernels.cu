@@ -16,8 +16,8 @@
 //     column k-1 update to the trailing tiles; the forward substitution of
 //     tile k-1 runs in the same phase;
 //  4. backward substitution over the tail tiles, then the sparse levels (top
-//     first); scatter to variable order; the linearised cost change with the
-//     undamped H (a fixed-order grid reduction).
+//     first); scatter to variable order together with the linearised cost
+//     change of the undamped system (a fixed-order grid reduction).
 // FP64 on this part has a dependent-operation latency of about 33 ns for an
 // FMA and about 300 ns for a divide or square root, so the kernel is written
 // for instruction-level parallelism: split accumulators, right-looking
@@ -44,12 +44,10 @@ struct CholArgs {
   int N, ns, T, ntp, n_tiles, levels;
   const int32_t *perm, *col_ptr, *blk_row, *blk_col, *lvl_col_ptr, *lvl_cols, *lvl_task_ptr, *tasks, *btask, *ftask;
   const int32_t *upd_ptr, *upd_src, *tupd_ptr, *tupd_src, *a_ptr, *a_src, *ta_ptr, *ta_src;
-  const int32_t *row_ptr, *row_blk, *trow_ptr, *trow_blk;
+  const int32_t *row_ptr, *row_blk, *trow_ptr, *trow_blk, *ttasks, *ttask_ptr;
   const double *Hd64, *fH64, *dampD, *g;
-  const int32_t *h_row_ptr, *h_col, *h_blk;
-  const int8_t* h_btr;
   double lam;
-  double *L, *Ldiag, *M, *Ldd, *y, *delta, *part, *out, *Spart;
+  double *L, *Ldiag, *M, *Ldd, *y, *delta, *part, *out, *Spart, *Tpart;
   int32_t* status;
 };
 
@@ -382,20 +380,30 @@ __device__ void tail_S(const CholArgs& a, int t, int lane) {
   if (e1 < dd) a.M[(size_t)(bj * D + e1 % D) * a.ntp + bi * D + e1 / D] = s1;
 }
 
-// tail right-hand side: y_t -= sum over the sparse blocks in tail block row t
-// (trow_blk holds (block, column) pairs)
+// tail row task u (one warp, lane groups take the entries in turn):
+// Tpart[u][r] = sum over its entries (block q, column k) of (L[q] y_k)[r]
+template <int D>
+__device__ void tail_row_task(const CholArgs& a, int u, int lane) {
+  constexpr int G = 32 / D, dd = D * D;
+  const int g = lane / D, r = lane % D;
+  const int beg = a.ttasks[3 * u + 1], end = a.ttasks[3 * u + 2];
+  double acc = 0.0;
+  if (g < G)
+    for (int e = beg + g; e < end; e += G)
+      acc += dot_ilp<D>(a.L + (size_t)a.trow_blk[2 * e] * dd + r * D, a.y + (size_t)a.trow_blk[2 * e + 1] * D);
+  double tot = acc;
+#pragma unroll
+  for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, acc, (r + k * D) & 31);
+  if (lane < D) a.Tpart[(size_t)u * D + lane] = tot;
+}
+
+// tail right-hand side: y_t -= the row task sums of tail block row t
 template <int D>
 __device__ void tail_rhs(const CholArgs& a, int t, int lane) {
-  constexpr int dd = D * D;
   if (lane >= D) return;
-  double acc0 = 0.0, acc1 = 0.0;
-  const int u1 = a.trow_ptr[t + 1];
-  for (int u = a.trow_ptr[t]; u < u1; ++u) {
-    const double v = dot_ilp<D>(a.L + (size_t)a.trow_blk[2 * u] * dd + lane * D, a.y + (size_t)a.trow_blk[2 * u + 1] * D);
-    if (u & 1) acc1 += v;
-    else acc0 += v;
-  }
-  a.y[(size_t)(a.ns + t) * D + lane] -= acc0 + acc1;
+  double acc = 0.0;
+  for (int u = a.ttask_ptr[t]; u < a.ttask_ptr[t + 1]; ++u) acc += a.Tpart[(size_t)u * D + lane];
+  a.y[(size_t)(a.ns + t) * D + lane] -= acc;
 }
 
 struct TileSmem {
@@ -643,7 +651,13 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   }
 
   // 3. dense tail: blocks, then tiles
-  for (int w = gw; w < a.T * (a.T + 1) / 2; w += nw) tail_S<D>(a, w, lane);
+  {
+    const int nts = a.T * (a.T + 1) / 2, ntr = a.ttask_ptr[a.T];
+    for (int w = gw; w < nts + ntr; w += nw) {
+      if (w < nts) tail_S<D>(a, w, lane);
+      else tail_row_task<D>(a, w - nts, lane);
+    }
+  }
   grid.sync();
   const int nT = a.n_tiles;
   for (int k = 0; k <= nT; ++k) {
@@ -680,59 +694,37 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
     for (int w = gw; w < nc; w += nw) backward_warp<D>(a, a.lvl_cols[c0 + w], lane);
     grid.sync();
   }
+  // scatter to variable order, with the linearised cost change of the
+  // undamped system: since (H + lambda D) delta = -g, -g.delta - delta^T H
+  // delta / 2 = -g.delta / 2 + lambda delta^T D delta / 2
+  double gd = 0.0, dq = 0.0;
   for (int k = gt; k < n; k += gs) {
     const int pos = k / D, r = k % D;
-    a.delta[(size_t)a.perm[pos] * D + r] = a.y[k];
-  }
-  grid.sync();
-
-  // model change with the undamped H: -g.delta - delta^T H delta / 2;
-  // consecutive variables go to different CTAs (the FP64 work spreads over
-  // every SM), partial sums are added in a fixed order
-  double gd = 0.0, dhd = 0.0;
-  for (int k = threadIdx.x;; k += blockDim.x) {
-    const int v = blockIdx.x + (int)gridDim.x * k;
-    if (v >= a.N) break;
-    double acc[D];
-    const double* H = a.Hd64 + (size_t)v * dd;
-    const double* pv = a.delta + (size_t)v * D;
-#pragma unroll
-    for (int r = 0; r < D; ++r) acc[r] = dot_ilp<D>(H + D * r, pv);
-    for (int k2 = a.h_row_ptr[v]; k2 < a.h_row_ptr[v + 1]; ++k2) {
-      const double* B = a.fH64 + (size_t)a.h_blk[k2] * 3 * dd + 2 * dd;
-      const double* pc = a.delta + (size_t)a.h_col[k2] * D;
-      if (a.h_btr[k2]) {
-#pragma unroll
-        for (int r = 0; r < D; ++r)
-#pragma unroll
-          for (int c = 0; c < D; ++c) acc[r] = fma(B[D * c + r], pc[c], acc[r]);
-      } else {
-#pragma unroll
-        for (int r = 0; r < D; ++r) acc[r] += dot_ilp<D>(B + D * r, pc);
-      }
-    }
-    gd += dot_ilp<D>(a.g + (size_t)v * D, pv);
-    dhd += dot_ilp<D>(pv, acc);
+    const size_t vi = (size_t)a.perm[pos] * D + r;
+    const double x = a.y[k];
+    a.delta[vi] = x;
+    gd = fma(a.g[vi], x, gd);
+    dq = fma(a.dampD[vi] * x, x, dq);
   }
   gd = cta_sum(gd, shr);
-  dhd = cta_sum(dhd, shr);
+  dq = cta_sum(dq, shr);
   if (threadIdx.x == 0) {
     a.part[2 * blockIdx.x] = gd;
-    a.part[2 * blockIdx.x + 1] = dhd;
+    a.part[2 * blockIdx.x + 1] = dq;
   }
   grid.sync();
   if (blockIdx.x == 0 && threadIdx.x < 32) {
-    double sg = 0.0, sh = 0.0;
+    double sg = 0.0, sq = 0.0;
     for (int b = threadIdx.x; b < (int)gridDim.x; b += 32) {
       sg += a.part[2 * b];
-      sh += a.part[2 * b + 1];
+      sq += a.part[2 * b + 1];
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
       sg += __shfl_xor_sync(kFull, sg, o);
-      sh += __shfl_xor_sync(kFull, sh, o);
+      sq += __shfl_xor_sync(kFull, sq, o);
     }
-    if (threadIdx.x == 0) a.out[0] = -sg - 0.5 * sh;
+    if (threadIdx.x == 0) a.out[0] = -0.5 * sg + 0.5 * a.lam * sq;
   }
 }
 
@@ -765,6 +757,9 @@ void CholDev::upload(CholPlan&& p, cudaStream_t st) {
   row_blk.upload(plan.row_blk, st);
   trow_ptr.upload(plan.trow_ptr, st);
   trow_blk.upload(plan.trow_blk, st);
+  ttasks.upload(plan.ttasks, st);
+  ttask_ptr.upload(plan.ttask_ptr, st);
+  Tpart.resize(std::max<size_t>(1, plan.ttasks.size() / 3 * (size_t)plan.d));
   const size_t dd = (size_t)plan.d * plan.d, ntp = (size_t)plan.n_tiles * kTB;
   L.resize(std::max<size_t>(1, plan.blk_row.size() * dd));
   Ldiag.resize(std::max<size_t>(1, (size_t)plan.n_sparse * dd));
@@ -794,9 +789,9 @@ SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st) {
              c.perm.get(), c.col_ptr.get(), c.blk_row.get(), c.blk_col.get(), c.lvl_col_ptr.get(), c.lvl_cols.get(),
              c.lvl_task_ptr.get(), c.tasks.get(), c.btask.get(), c.ftask.get(), c.upd_ptr.get(), c.upd_src.get(), c.tupd_ptr.get(),
              c.tupd_src.get(), c.a_ptr.get(), c.a_src.get(), c.ta_ptr.get(), c.ta_src.get(), c.row_ptr.get(),
-             c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
-             s.g.get(), s.row_ptr.get(), s.col.get(), s.blk.get(), s.btr.get(), lambda, c.L.get(), c.Ldiag.get(),
-             c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.Spart.get(),
+             c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), c.ttasks.get(), c.ttask_ptr.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
+             s.g.get(), lambda, c.L.get(), c.Ldiag.get(),
+             c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.Spart.get(), c.Tpart.get(),
              c.status.get()};
   void* args[] = {&a};
   double ms = 0.0;

@@ -486,7 +486,7 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
   }
   // tasks, level by level: every block of a level's columns (its Hessian
   // block and update chunks), then the row sums of the level's columns
-  p.chunk = 2 * (32 / d);
+  p.chunk = 32 / d;
   p.row_chunk = 4 * (32 / d);
   p.lvl_task_ptr.assign(L + 1, 0);
   p.btask.assign((size_t)2 * nblk, 0);
@@ -517,6 +517,13 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
       }
       p.lvl_task_ptr[l + 1] = nt;
     }
+  }
+  p.ttask_ptr.assign(T + 1, 0);
+  p.ttasks.clear();
+  for (int t = 0; t < T; ++t) {
+    for (int u = p.trow_ptr[t]; u < p.trow_ptr[t + 1]; u += p.row_chunk)
+      p.ttasks.insert(p.ttasks.end(), {t, u, std::min(u + p.row_chunk, p.trow_ptr[t + 1])});
+    p.ttask_ptr[t + 1] = (int)p.ttasks.size() / 3;
   }
   const double dd3 = (double)d * d * d, nt = (double)T * d;
   p.flops = 2.0 * dd3 * pairs + ns * dd3 / 3.0 + (nblk - ns) * dd3 + nt * nt * nt / 3.0;

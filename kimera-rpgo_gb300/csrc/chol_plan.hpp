@@ -43,8 +43,12 @@ struct CholPlan {
   //    list entries [first, end) (chunks of at most `row_chunk`).
   // Tasks of one level are contiguous (lvl_task_ptr); so are the tasks of
   // one block (btask: first, count) and of one column's row (ftask).
-  int chunk = 10, row_chunk = 20;
+  int chunk = 5, row_chunk = 20;
   std::vector<int32_t> lvl_task_ptr, tasks, btask, ftask;
+  // tail row tasks: the sparse part of tail block row t, [first, end) of
+  // trow_blk, in chunks of at most row_chunk (3 ints each: row, first, end);
+  // the tasks of row t are [ttask_ptr[t], ttask_ptr[t + 1])
+  std::vector<int32_t> ttasks, ttask_ptr;
   // updates: target -= sum over (a, b) of L[a] * L[b]^T, as flat pairs
   std::vector<int32_t> upd_ptr, upd_src;    // sparse targets (per block)
   std::vector<int32_t> tupd_ptr, tupd_src;  // tail targets (lower blocks bi >= bj, index bi*(bi+1)/2 + bj)

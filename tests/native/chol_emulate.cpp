@@ -162,7 +162,8 @@ struct Emu {
   void tail_rhs(int t) {
     for (int r = 0; r < d; ++r) {
       double b = 0.0;
-      for (int u = p.trow_ptr[t]; u < p.trow_ptr[t + 1]; ++u) {
+      for (int w = p.ttask_ptr[t]; w < p.ttask_ptr[t + 1]; ++w)
+      for (int u = p.ttasks[3 * w + 1]; u < p.ttasks[3 * w + 2]; ++u) {
         const int q = p.trow_blk[2 * u], k = p.trow_blk[2 * u + 1];
         for (int c = 0; c < d; ++c) b += L[(size_t)q * dd + r * d + c] * y[(size_t)k * d + c];
       }
