@@ -175,50 +175,55 @@ constexpr unsigned kFull = 0xffffffffu;
 template <int D>
 __device__ void run_task(const CholArgs& a, int t, int lane) {
   constexpr int G = 32 / D, dd = D * D;
+  constexpr int NC = D == 6 ? 3 : D;  // output columns of one block task
   const int g = lane / D, r = lane % D;
   const int4 tk = reinterpret_cast<const int4*>(a.tasks)[t];
-  double acc[D];
+  const int kind = tk.w & 3, slot = tk.w >> 3;
+  if (kind < 2) {
+    const int p = tk.x, c0 = ((tk.w >> 2) & 1) * NC;
+    double acc[NC];
 #pragma unroll
-  for (int c = 0; c < D; ++c) acc[c] = 0.0;
-  if (tk.w < 2) {
-    const int p = tk.x;
-    if (tk.w == 1 && g == 0) {
+    for (int c = 0; c < NC; ++c) acc[c] = 0.0;
+    if (kind == 1 && g == 0) {
       const int j = a.blk_col[p], i = a.blk_row[p];
       if (i == j) {
         const int v = a.perm[j];
 #pragma unroll
-        for (int c = 0; c < D; ++c) acc[c] = gather_diag<D>(a, v, r, c);
+        for (int c = 0; c < NC; ++c) acc[c] = gather_diag<D>(a, v, r, c0 + c);
       } else {
 #pragma unroll
-        for (int c = 0; c < D; ++c) acc[c] = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], r, c);
+        for (int c = 0; c < NC; ++c)
+          acc[c] = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], r, c0 + c);
       }
     }
     if (g < G) {
       for (int u = tk.y + g; u < tk.z; u += G) {
         const int pa = a.upd_src[2 * u], pb = a.upd_src[2 * u + 1];
         const double* A = a.L + (size_t)pa * dd + r * D;
-        const double* B = a.L + (size_t)pb * dd;
+        const double* B = a.L + (size_t)pb * dd + c0 * D;
         double ar[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) ar[k] = A[k];
 #pragma unroll
-        for (int c = 0; c < D; ++c) acc[c] -= dot_ilp<D>(ar, B + c * D);
+        for (int c = 0; c < NC; ++c) acc[c] -= dot_ilp<D>(ar, B + c * D);
       }
     }
-  } else if (g < G) {
-    for (int u = tk.y + g; u < tk.z; u += G)
-      acc[0] += dot_ilp<D>(a.L + (size_t)a.row_blk[2 * u] * dd + r * D, a.y + (size_t)a.row_blk[2 * u + 1] * D);
-  }
-  const int nval = tk.w < 2 ? D : 1;  // warp-uniform
-  for (int c = 0; c < nval; ++c) {
-    double sum = acc[0];
 #pragma unroll
-    for (int k = 0; k < D; ++k)
-      if (k == c) sum = acc[k];
-    double tot = sum;
+    for (int c = 0; c < NC; ++c) {
+      double tot = acc[c];
 #pragma unroll
-    for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, sum, (r + k * D) & 31);
-    if (lane < D) a.Spart[(size_t)t * dd + lane * D + c] = tot;
+      for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, acc[c], (r + k * D) & 31);
+      if (lane < D) a.Spart[(size_t)slot * dd + lane * D + c0 + c] = tot;
+    }
+  } else {
+    double acc = 0.0;
+    if (g < G)
+      for (int u = tk.y + g; u < tk.z; u += G)
+        acc += dot_ilp<D>(a.L + (size_t)a.row_blk[2 * u] * dd + r * D, a.y + (size_t)a.row_blk[2 * u + 1] * D);
+    double tot = acc;
+#pragma unroll
+    for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, acc, (r + k * D) & 31);
+    if (lane < D) a.Spart[(size_t)slot * dd + lane * D] = tot;
   }
 }
 
@@ -744,7 +749,7 @@ void CholDev::upload(CholPlan&& p, cudaStream_t st) {
   tasks.upload(plan.tasks, st);
   btask.upload(plan.btask, st);
   ftask.upload(plan.ftask, st);
-  Spart.resize(std::max<size_t>(1, plan.tasks.size() / 4 * (size_t)plan.d * plan.d));
+  Spart.resize(std::max<size_t>(1, (size_t)plan.n_slots * plan.d * plan.d));
   upd_ptr.upload(plan.upd_ptr, st);
   upd_src.upload(plan.upd_src, st);
   tupd_ptr.upload(plan.tupd_ptr, st);

@@ -493,30 +493,33 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
   p.ftask.assign((size_t)2 * ns, 0);
   p.tasks.clear();
   {
-    int nt = 0;
+    const int halves = d == 6 ? 2 : 1;
+    int slot = 0;
     for (int l = 0; l < L; ++l) {
       for (int w = p.lvl_col_ptr[l]; w < p.lvl_col_ptr[l + 1]; ++w) {
         const int j = p.lvl_cols[w];
         for (int q = p.col_ptr[j]; q < p.col_ptr[j + 1]; ++q) {
-          p.btask[2 * q] = nt;
+          p.btask[2 * q] = slot;
           int u = p.upd_ptr[q];
           do {
             const int e = std::min(u + p.chunk, p.upd_ptr[q + 1]);
-            p.tasks.insert(p.tasks.end(), {q, u, e, u == p.upd_ptr[q] ? 1 : 0});
-            ++nt;
+            const int kind = u == p.upd_ptr[q] ? 1 : 0;
+            for (int h = 0; h < halves; ++h) p.tasks.insert(p.tasks.end(), {q, u, e, kind | h << 2 | slot << 3});
+            ++slot;
             u = e;
           } while (u < p.upd_ptr[q + 1]);
-          p.btask[2 * q + 1] = nt - p.btask[2 * q];
+          p.btask[2 * q + 1] = slot - p.btask[2 * q];
         }
-        p.ftask[2 * j] = nt;
+        p.ftask[2 * j] = slot;
         for (int u = p.row_ptr[j]; u < p.row_ptr[j + 1]; u += p.row_chunk) {
-          p.tasks.insert(p.tasks.end(), {j, u, std::min(u + p.row_chunk, p.row_ptr[j + 1]), 2});
-          ++nt;
+          p.tasks.insert(p.tasks.end(), {j, u, std::min(u + p.row_chunk, p.row_ptr[j + 1]), 2 | slot << 3});
+          ++slot;
         }
-        p.ftask[2 * j + 1] = nt - p.ftask[2 * j];
+        p.ftask[2 * j + 1] = slot - p.ftask[2 * j];
       }
-      p.lvl_task_ptr[l + 1] = nt;
+      p.lvl_task_ptr[l + 1] = (int)p.tasks.size() / 4;
     }
+    p.n_slots = slot;
   }
   p.ttask_ptr.assign(T + 1, 0);
   p.ttasks.clear();

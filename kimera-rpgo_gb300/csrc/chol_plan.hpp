@@ -35,15 +35,17 @@ struct CholPlan {
   std::vector<int32_t> blk_col;  // column position of each block
   // elimination-tree levels of the sparse columns (leaves first)
   std::vector<int32_t> lvl_col_ptr, lvl_cols;  // columns per level
-  // Tasks of the sparse levels, 4 ints each (id, first, end, kind):
+  // Tasks of the sparse levels, 4 ints each (id, first, end, code), code =
+  // kind | half << 2 | slot << 3; each writes partial sums to its slot:
   //  kind 0 / 1: block id's update list [first, end) cut into chunks of at
   //    most `chunk` pairs (kind 1 on the block's first chunk, which also
-  //    carries the Hessian block);
+  //    carries the Hessian block); for 6x6 blocks every chunk is two tasks,
+  //    output columns 0-2 (half 0) and 3-5 (half 1), sharing one slot;
   //  kind 2: the forward-substitution row sum of column id over its row
   //    list entries [first, end) (chunks of at most `row_chunk`).
-  // Tasks of one level are contiguous (lvl_task_ptr); so are the tasks of
-  // one block (btask: first, count) and of one column's row (ftask).
-  int chunk = 5, row_chunk = 20;
+  // Tasks of one level are contiguous (lvl_task_ptr); the slots of one block
+  // (btask: first, count) and of one column's row sum (ftask) are too.
+  int chunk = 5, row_chunk = 20, n_slots = 0;
   std::vector<int32_t> lvl_task_ptr, tasks, btask, ftask;
   // tail row tasks: the sparse part of tail block row t, [first, end) of
   // trow_blk, in chunks of at most row_chunk (3 ints each: row, first, end);

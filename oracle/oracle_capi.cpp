@@ -4,6 +4,7 @@
 // 105-113 (known inliers), 115-306 (optimize), 337-369 (update);
 // src/GenericSolver.cpp:37-65 (updateValues, addAndCheckIfOptimize).
 // The structs of the public C ABI header are reused for the argument layout.
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -32,6 +33,8 @@ struct SolverBase {
   virtual int factors(int32_t* kind, uint64_t* k1, uint64_t* k2, double* meas, int64_t cap) const = 0;
   virtual int adjacency(int32_t group, uint32_t* words, int64_t cap, int64_t* n) const = 0;
   virtual void stats(int64_t* lm_iters, int64_t* solves, int64_t* gnc_iters) const = 0;
+  // wall-clock seconds spent in outlier rejection and in the solve (sums)
+  double pcm_seconds = 0.0, solve_seconds = 0.0;
 };
 
 template <class S, class U>
@@ -95,7 +98,9 @@ struct RobustSolverO final : SolverBase {
     }
     bool do_opt;
     if (pcm) {
+      const auto t0 = std::chrono::steady_clock::now();
       do_opt = pcm->remove_outliers(nf, new_keys, values, &nfg);
+      this->pcm_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     } else {
       nfg.insert(nfg.end(), nf.begin(), nf.end());
       do_opt = true;
@@ -106,7 +111,12 @@ struct RobustSolverO final : SolverBase {
     for (const auto& f : nfg) {
       if (!values.count(f.k1) || !values.count(f.k2)) return RPGO_ERR_KEY;
     }
-    if (do_opt && optimize_graph) return optimize();
+    if (do_opt && optimize_graph) {
+      const auto t0 = std::chrono::steady_clock::now();
+      const int rc = optimize();
+      this->solve_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      return rc;
+    }
     return RPGO_OK;
   }
   int optimize() {
@@ -275,6 +285,11 @@ int oracle_get_adjacency(void* s, int32_t g, uint32_t* w, int64_t cap, int64_t* 
 }
 int oracle_get_stats(void* s, int64_t* lm, int64_t* solves, int64_t* gnc) {
   static_cast<SolverBase*>(s)->stats(lm, solves, gnc);
+  return 0;
+}
+int oracle_get_times(void* s, double* pcm_seconds, double* solve_seconds) {
+  *pcm_seconds = static_cast<SolverBase*>(s)->pcm_seconds;
+  *solve_seconds = static_cast<SolverBase*>(s)->solve_seconds;
   return 0;
 }
 

@@ -68,6 +68,7 @@ def lib():
                                               C.POINTER(C.c_int64)]
         _lib.oracle_get_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                           C.POINTER(C.c_int64)]
+        _lib.oracle_get_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib.oracle_pwc_op.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                        C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]
         _lib.oracle_pwc_mahalanobis.restype = C.c_double
@@ -171,7 +172,10 @@ class OracleSolver:
     def stats(self):
         a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
         lib().oracle_get_stats(self.h, C.byref(a), C.byref(b), C.byref(c))
-        return dict(lm_iterations=a.value, linear_solves=b.value, gnc_iterations=c.value)
+        p, s = C.c_double(), C.c_double()
+        lib().oracle_get_times(self.h, C.byref(p), C.byref(s))
+        return dict(lm_iterations=a.value, linear_solves=b.value, gnc_iterations=c.value, pcm_seconds=p.value,
+                    solve_seconds=s.value)
 
 
 # ------------------------------------------------------------------ math hooks

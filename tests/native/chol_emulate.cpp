@@ -70,15 +70,17 @@ struct Emu {
   std::vector<double> Spart;  // task partial sums
   void run_task(int t) {
     const int* tk = &p.tasks[4 * (size_t)t];
-    if (tk[3] < 2) {
+    const int kind = tk[3] & 3, slot = tk[3] >> 3;
+    if (kind < 2) {
       const int q = tk[0], j = p.blk_col[q], i = p.blk_row[q];
-      for (int e = 0; e < dd; ++e) {
-        const int r = e / d, c = e % d;
-        double s = 0.0;
-        if (tk[3] == 1)
-          s = i == j ? diag_entry(p.perm[j], r, c) : offdiag_entry(p.a_src, p.a_ptr[q], p.a_ptr[q + 1], r, c);
-        Spart[(size_t)t * dd + e] = pairs(p.upd_src, tk[1], tk[2], r, c, s);
-      }
+      const int nc = d == 6 ? 3 : d, c0 = ((tk[3] >> 2) & 1) * nc;
+      for (int r = 0; r < d; ++r)
+        for (int c = c0; c < c0 + nc; ++c) {
+          double s = 0.0;
+          if (kind == 1)
+            s = i == j ? diag_entry(p.perm[j], r, c) : offdiag_entry(p.a_src, p.a_ptr[q], p.a_ptr[q + 1], r, c);
+          Spart[(size_t)slot * dd + r * d + c] = pairs(p.upd_src, tk[1], tk[2], r, c, s);
+        }
     } else {
       for (int r = 0; r < d; ++r) {
         double b = 0.0;
@@ -86,7 +88,7 @@ struct Emu {
           const int q = p.row_blk[2 * u], k = p.row_blk[2 * u + 1];
           for (int c = 0; c < d; ++c) b += L[(size_t)q * dd + r * d + c] * y[(size_t)k * d + c];
         }
-        Spart[(size_t)t * dd + r * d] = b;
+        Spart[(size_t)slot * dd + r * d] = b;
       }
     }
   }
@@ -296,7 +298,7 @@ extern "C" int chol_emulate(int N, int d, int F, const int32_t* kind, const int3
     }
   // 2. sparse levels
   const int levels = p.levels();
-  e.Spart.assign(p.tasks.size() / 4 * (size_t)dd, 0.0);
+  e.Spart.assign((size_t)p.n_slots * dd, 0.0);
   for (int l = 0; l < levels; ++l) {
     // (A) the level's update tasks, (B) its columns
     for (int t = p.lvl_task_ptr[l]; t < p.lvl_task_ptr[l + 1]; ++t) e.run_task(t);
