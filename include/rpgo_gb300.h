@@ -75,7 +75,22 @@ typedef struct rpgo_params {
   /* additional */
   int32_t lm_diagonal_damping;
   int32_t linear_solver;      /* RPGO_LINEAR_*: direct sparse Cholesky (default) or PCG */
+  /* GNC warm start (no counterpart in the reference; off by default, which
+   * keeps GncOptimizer's plain mu continuation): RPGO_WARM_* */
+  int32_t gnc_warm_start;
+  double gnc_warm_mu;         /* mu of the first TLS weight update of the warm schedule */
 } rpgo_params;
+
+/* gnc_warm_start values.
+ * OFF: the plain GNC-TLS schedule (GncOptimizer, src/RobustSolver.cpp:133-171).
+ * ON: predicted inlier probabilities (the installed closure model, or the
+ *   probabilities given by rpgo_set_warm_start_probs) pick the first inlier
+ *   set, the mu continuation starts at gnc_warm_mu, each LM run starts from the
+ *   previous estimate, and the result is accepted only when its weights are
+ *   binary and agree with the TLS rule at the final estimate; otherwise the
+ *   plain schedule runs from the start (counted in rpgo_timing.warm_fallbacks).
+ * RECORD: the plain schedule, recording the closure features (training data). */
+enum { RPGO_WARM_OFF = 0, RPGO_WARM_ON = 1, RPGO_WARM_RECORD = 2 };
 
 /* A batch of factors (structure of arrays). For priors key_back is ignored. */
 typedef struct rpgo_factor_batch {
@@ -126,6 +141,8 @@ typedef struct rpgo_timing {
   int64_t chol_tail;          /* variables in the dense trailing block (last plan) */
   double pair_kernel_ms;      /* pairwise consistency launches (sum) */
   int64_t pair_kernel_launches;
+  int64_t warm_runs;          /* warm-started GNC schedules run (RPGO_WARM_ON) */
+  int64_t warm_fallbacks;     /* of those, not certified: the plain schedule was rerun */
 } rpgo_timing;
 
 typedef struct rpgo_solver rpgo_solver; /* opaque */
@@ -199,6 +216,13 @@ int rpgo_get_factors(const rpgo_solver* s, int32_t* kind, uint64_t* key_front, u
  * pairwise consistent. Returns the group size in *n. */
 int rpgo_get_adjacency(const rpgo_solver* s, int32_t group, uint32_t* words, int64_t capacity, int64_t* n);
 int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* out);
+/* GNC warm start (no counterpart in the reference): inlier probabilities for
+ * the factors of the next GNC solve, in the order of the graph it optimises
+ * (rpgo_get_factors after the update; odometry and priors first, their
+ * entries are ignored). Used by that solve when gnc_warm_start is
+ * RPGO_WARM_ON and n equals the graph size (else the installed closure model
+ * predicts them), then cleared. */
+int rpgo_set_warm_start_probs(rpgo_solver* s, const double* probs, int64_t n);
 /* RobustSolver::saveData (src/RobustSolver.cpp:448-465): result.g2o and
  * gnc_weights.csv in `folder`. */
 int rpgo_save_data(const rpgo_solver* s, const char* folder);

@@ -36,6 +36,7 @@ struct rpgo_solver {
   size_t gnc_num_inliers = 0, latest_num_lc = 0;
   bool last_do_optimize = false;
   rpgo_timing timing{};
+  std::vector<double> warm_probs;  // rpgo_set_warm_start_probs, consumed by the next GNC solve
 };
 
 namespace {
@@ -87,7 +88,14 @@ int optimize(rpgo_solver* s) {
     }
     GpuNls nls(s->dim, full, *s->store, *s->values, s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
     std::vector<double> w;
-    gnc_tls(nls, n_known, g, lp, s->p.gnc_bias_odom ? &init : nullptr, &w, &st);
+    bool warm_done = false;
+    if (s->p.gnc_warm_start == RPGO_WARM_ON && s->warm_probs.size() == full.size()) {
+      s->timing.warm_runs++;
+      warm_done = gnc_tls_warm(nls, n_known, g, lp, s->warm_probs, s->p.gnc_warm_mu, &w, &st);
+      if (!warm_done) s->timing.warm_fallbacks++;
+    }
+    s->warm_probs.clear();
+    if (!warm_done) gnc_tls(nls, n_known, g, lp, s->p.gnc_bias_odom ? &init : nullptr, &w, &st);
     nls.write_back(*s->values);
     s->gnc_weights.assign(w.begin(), w.begin() + std::min(w.size(), s->nfg.size()));
     const double sum = std::accumulate(s->gnc_weights.begin(), s->gnc_weights.end(), 0.0);
@@ -315,6 +323,9 @@ void rpgo_params_default(rpgo_params* p) {
   p->gnc_fix_prev_inliers = 0;
   p->gnc_bias_odom = 0;
   p->lm_diagonal_damping = 1;
+  p->linear_solver = RPGO_LINEAR_CHOLESKY;
+  p->gnc_warm_start = RPGO_WARM_OFF;
+  p->gnc_warm_mu = 100.0;
 }
 void rpgo_params_set_no_rejection(rpgo_params* p, int32_t v) {
   p->outlier_removal = RPGO_OUTLIER_NONE;
@@ -511,6 +522,11 @@ int rpgo_get_adjacency(const rpgo_solver* s, int32_t group, uint32_t* words, int
     std::memcpy(words, w.data(), w.size() * sizeof(uint32_t));
     return (int)RPGO_OK;
   });
+}
+int rpgo_set_warm_start_probs(rpgo_solver* s, const double* probs, int64_t n) {
+  if (!s || n < 0 || (n > 0 && !probs)) return RPGO_ERR_ARG;
+  s->warm_probs.assign(probs, probs + n);
+  return RPGO_OK;
 }
 int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* t) {
   if (!s || !t) return RPGO_ERR_ARG;

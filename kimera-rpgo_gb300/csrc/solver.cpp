@@ -53,9 +53,10 @@ void GpuNls::write_back(ValueStore& values) const {
 
 // NonlinearOptimizer::defaultOptimize with LevenbergMarquardtOptimizer::iterate
 // or GaussNewtonOptimizer::iterate (GTSAM, restated).
-void GpuNls::optimize(const LmParams& p, NlsStats* st) {
+void GpuNls::optimize(const LmParams& p, NlsStats* st, bool from_current) {
   SolverDev& s = s_;
-  RPGO_CUDA(cudaMemcpyAsync(s.x.get(), s.x0.get(), s.x0.size() * sizeof(double), cudaMemcpyDeviceToDevice, st_));
+  if (!from_current)
+    RPGO_CUDA(cudaMemcpyAsync(s.x.get(), s.x0.get(), s.x0.size() * sizeof(double), cudaMemcpyDeviceToDevice, st_));
   double cur_err = solver_error(s, s.x.get(), s.weights.get(), st_);
   if (cur_err <= p.error_tol || p.max_iterations <= 0) return;
   double lambda = p.lambda_initial;
@@ -197,6 +198,46 @@ void gnc_tls(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp
   s.weights.download(weights.data(), F, stream);
   RPGO_CUDA(cudaStreamSynchronize(stream));
   *weights_out = weights;
+}
+
+bool gnc_tls_warm(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp,
+                  const std::vector<double>& probs, double warm_mu, std::vector<double>* weights_out, NlsStats* st) {
+  SolverDev& s = nls.dev();
+  cudaStream_t stream = nls.stream();
+  const size_t F = (size_t)s.F;
+  std::vector<double> barc(F, g.threshold_mode == 0 ? g.threshold : 0.5 * chi2inv(g.threshold, s.d));
+  std::vector<double> weights(F, 1.0), wnew(F, 1.0);
+  size_t predicted = 0;
+  for (size_t k = n_known; k < F; ++k) {
+    weights[k] = (k < probs.size() && probs[k] >= 0.5) ? 1.0 : 0.0;
+    predicted += weights[k] == 1.0;
+  }
+  const std::vector<double> first = weights;
+  nls.set_weights(weights);
+  nls.optimize(lp, st);
+  double mu = warm_mu;
+  bool fixed_point = F == n_known;
+  for (int it = 0; it < g.max_iterations && !fixed_point; ++it) {
+    st->gnc_iterations++;
+    solver_gnc_weights(s, s.x.get(), (int)n_known, barc, mu, stream);
+    s.weights.download(wnew.data(), F, stream);
+    RPGO_CUDA(cudaStreamSynchronize(stream));
+    bool same = true;
+    for (size_t k = n_known; k < F && same; ++k)
+      if (std::fabs(wnew[k] - std::round(wnew[k])) > g.weights_tol || std::round(wnew[k]) != weights[k]) same = false;
+    if (same) {
+      fixed_point = true;
+      nls.set_weights(weights);
+      break;
+    }
+    weights = wnew;
+    nls.optimize(lp, st, true);
+    mu *= g.mu_step;
+  }
+  size_t kept = 0;
+  for (size_t k = n_known; k < F; ++k) kept += (first[k] == 1.0 && weights[k] == 1.0);
+  *weights_out = weights;
+  return fixed_point && (double)kept >= kWarmKeep * (double)predicted;
 }
 
 }  // namespace rpgo

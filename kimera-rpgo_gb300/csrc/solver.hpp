@@ -41,8 +41,9 @@ class GpuNls {
   GpuNls(int dim, const std::vector<FactorRec>& graph, const FactorStore& store, const ValueStore& values,
          cudaStream_t st, bool direct = true);
   void set_weights(const std::vector<double>& w);
-  // LM / GN from the initial values; result left in dev().x
-  void optimize(const LmParams& p, NlsStats* st);
+  // LM / GN from the initial values (from_current: from the estimate in
+  // dev().x); result left in dev().x
+  void optimize(const LmParams& p, NlsStats* st, bool from_current = false);
   double error_at_result();
   // GenericSolver::updateValues: write the result back into the value rows
   void write_back(ValueStore& values) const;
@@ -64,5 +65,18 @@ double chi2inv(double alpha, int dof);
 // first n_known factors. init_weights (optional) as in setWeights.
 void gnc_tls(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp,
              const std::vector<double>* init_weights, std::vector<double>* weights_out, NlsStats* st);
+
+// Warm-started GNC-TLS (no counterpart in the reference). probs[k]: predicted
+// inlier probability of factor k >= n_known. The predicted inliers
+// (probs >= 0.5) form the first weights; LM from the initial values; then TLS
+// weight updates starting at mu = warm_mu (mu *= mu_step after each), each
+// followed by LM from the previous estimate, until an update reproduces the
+// binary weights of the last solve (a fixed point of the TLS rule). Returns
+// true (certified) when such a fixed point is reached within max_iterations
+// and keeps at least kWarmKeep of the predicted inliers; false tells the
+// caller to run the plain schedule.
+constexpr double kWarmKeep = 0.75;
+bool gnc_tls_warm(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp,
+                  const std::vector<double>& probs, double warm_mu, std::vector<double>* weights_out, NlsStats* st);
 
 }  // namespace rpgo

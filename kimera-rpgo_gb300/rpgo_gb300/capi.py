@@ -30,6 +30,7 @@ class Params(C.Structure):
         ("gnc_max_iterations", C.c_int32), ("gnc_mu_step", C.c_double), ("gnc_relative_cost_tol", C.c_double),
         ("gnc_weights_tol", C.c_double), ("gnc_fix_prev_inliers", C.c_int32), ("gnc_bias_odom", C.c_int32),
         ("lm_diagonal_damping", C.c_int32), ("linear_solver", C.c_int32),
+        ("gnc_warm_start", C.c_int32), ("gnc_warm_mu", C.c_double),
     ]
 
 
@@ -54,7 +55,8 @@ class Timing(C.Structure):
         ("pcg_kernel_ms", C.c_double), ("pcg_kernel_launches", C.c_int64), ("pcg_kernel_bytes", C.c_double),
         ("chol_kernel_ms", C.c_double), ("chol_kernel_launches", C.c_int64), ("chol_kernel_flops", C.c_double),
         ("chol_kernel_bytes", C.c_double), ("chol_levels", C.c_int64), ("chol_tail", C.c_int64),
-        ("pair_kernel_ms", C.c_double), ("pair_kernel_launches", C.c_int64)]
+        ("pair_kernel_ms", C.c_double), ("pair_kernel_launches", C.c_int64),
+        ("warm_runs", C.c_int64), ("warm_fallbacks", C.c_int64)]
 
 
 # every exported entry point: name -> (restype, argtypes)
@@ -83,6 +85,7 @@ SIGNATURES = {
     "rpgo_get_factors": (C.c_int, [_P, _P, _P, _P, _P, C.c_int64]),
     "rpgo_get_adjacency": (C.c_int, [_P, C.c_int32, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "rpgo_get_timing": (C.c_int, [_P, C.POINTER(Timing)]),
+    "rpgo_set_warm_start_probs": (C.c_int, [_P, _P, C.c_int64]),
     "rpgo_save_data": (C.c_int, [_P, C.c_char_p]),
     "rpgo_trajectory_scan_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [_P]),
     "rpgo_odometry_check_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [C.c_double, C.c_double,
@@ -259,6 +262,13 @@ class RobustSolver:
 
     def saveData(self, folder: str) -> int:
         return load().rpgo_save_data(self.h, folder.encode())
+
+    # ---- GNC warm start (no counterpart in the reference)
+    def set_warm_start_probs(self, probs) -> int:
+        """Inlier probabilities for the next warm-started GNC solve, one per
+        factor of the graph it optimises (known inliers are ignored)."""
+        self._warm = np.ascontiguousarray(probs, dtype=np.float64)
+        return load().rpgo_set_warm_start_probs(self.h, _ptr(self._warm), self._warm.size)
 
 
 # ------------------------------------------------------------------ stage functions (host arrays)

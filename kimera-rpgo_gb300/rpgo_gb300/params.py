@@ -15,6 +15,8 @@ UPDATE, QUIET, VERBOSE = 0, 1, 2
 COST, PROBABILITY = 0, 1
 # linear solver of the LM / GN step (GTSAM linearSolverType; the reference keeps the default)
 LINEAR_CHOLESKY, LINEAR_PCG = 0, 1
+# GNC warm start modes (rpgo_params.gnc_warm_start)
+WARM_OFF, WARM_ON, WARM_RECORD = 0, 1, 2
 
 
 class RobustSolverParams:
@@ -44,6 +46,9 @@ class RobustSolverParams:
         self.gnc_bias_odom = 0
         self.lm_diagonal_damping = 1
         self.linear_solver = LINEAR_CHOLESKY
+        # GNC warm start (no counterpart in the reference): off by default
+        self.gnc_warm_start = WARM_OFF
+        self.gnc_warm_mu = 1e2
 
     # SolverParams.h:97-100
     def setNoRejection(self, verbosity=UPDATE, dim=3):
@@ -125,4 +130,12 @@ class RobustSolverParams:
 
     def gncBiasOdom(self):
         self.gnc_bias_odom = 1
+        return self
+
+    def setGncWarmStart(self, mode=WARM_ON, mu=None):
+        """Warm-started GNC schedule (WARM_ON), plain schedule with closure
+        features recorded (WARM_RECORD), or the plain schedule (WARM_OFF)."""
+        self.gnc_warm_start = int(mode)
+        if mu is not None:
+            self.gnc_warm_mu = float(mu)
         return self

@@ -33,6 +33,9 @@ struct SolverBase {
   virtual int factors(int32_t* kind, uint64_t* k1, uint64_t* k2, double* meas, int64_t cap) const = 0;
   virtual int adjacency(int32_t group, uint32_t* words, int64_t cap, int64_t* n) const = 0;
   virtual void stats(int64_t* lm_iters, int64_t* solves, int64_t* gnc_iters) const = 0;
+  virtual void set_warm_probs(const double* p, int64_t n) = 0;
+  virtual int force_optimize() = 0;
+  int64_t warm_runs = 0, warm_fallbacks = 0;
   // wall-clock seconds spent in outlier rejection and in the solve (sums)
   double pcm_seconds = 0.0, solve_seconds = 0.0;
 };
@@ -50,6 +53,7 @@ struct RobustSolverO final : SolverBase {
   size_t gnc_num_inliers = 0, latest_num_lc = 0;
   int64_t lm_iters = 0, solves = 0, gnc_iters = 0;
   bool last_do_opt = false;
+  std::vector<double> warm_probs;  // consumed by the next warm-started GNC solve
 
   explicit RobustSolverO(const rpgo_params& prm, bool with_pcm) : p(prm) {
     if (with_pcm) {
@@ -141,7 +145,24 @@ struct RobustSolverO final : SolverBase {
         init.assign(full.size(), 0.0);
         for (size_t i = 0; i < n_known; ++i) init[i] = 1.0;
       }
-      auto r = gnc_tls<S>(full, values, n_known, gp, lp, p.gnc_bias_odom ? &init : nullptr);
+      GncResult<S> r;
+      bool warm_done = false;
+      if (p.gnc_warm_start == RPGO_WARM_ON && warm_probs.size() == full.size()) {
+        bool certified = false;
+        r = gnc_tls_warm<S>(full, values, n_known, gp, lp, warm_probs, p.gnc_warm_mu, &certified);
+        ++warm_runs;
+        if (certified) warm_done = true;
+        else ++warm_fallbacks;
+        warm_probs.clear();
+      }
+      if (!warm_done) {
+        SolveStats before = r.stats;
+        const int outer_before = r.outer_iterations;
+        r = gnc_tls<S>(full, values, n_known, gp, lp, p.gnc_bias_odom ? &init : nullptr);
+        r.stats.iterations += before.iterations;
+        r.stats.linear_solves += before.linear_solves;
+        r.outer_iterations += outer_before;
+      }
       result = r.values;
       st = r.stats;
       gnc_iters += r.outer_iterations;
@@ -223,6 +244,14 @@ struct RobustSolverO final : SolverBase {
     }
     return RPGO_ERR_ARG;
   }
+  void set_warm_probs(const double* pr, int64_t n) override { warm_probs.assign(pr, pr + n); }
+  // RobustSolver::forceUpdate with no new factors or values: optimize()
+  int force_optimize() override {
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = optimize();
+    this->solve_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+  }
   void stats(int64_t* a, int64_t* b, int64_t* c) const override {
     *a = lm_iters;
     *b = solves;
@@ -285,6 +314,18 @@ int oracle_get_adjacency(void* s, int32_t g, uint32_t* w, int64_t cap, int64_t* 
 }
 int oracle_get_stats(void* s, int64_t* lm, int64_t* solves, int64_t* gnc) {
   static_cast<SolverBase*>(s)->stats(lm, solves, gnc);
+  return 0;
+}
+// warm-started GNC: inlier probabilities of the next solve's factors (graph
+// order; known inliers ignored), and the warm counters
+int oracle_set_warm_probs(void* s, const double* probs, int64_t n) {
+  static_cast<SolverBase*>(s)->set_warm_probs(probs, n);
+  return 0;
+}
+int oracle_force_optimize(void* s) { return static_cast<SolverBase*>(s)->force_optimize(); }
+int oracle_get_warm_stats(void* s, int64_t* runs, int64_t* fallbacks) {
+  *runs = static_cast<SolverBase*>(s)->warm_runs;
+  *fallbacks = static_cast<SolverBase*>(s)->warm_fallbacks;
   return 0;
 }
 int oracle_get_times(void* s, double* pcm_seconds, double* solve_seconds) {

@@ -776,4 +776,75 @@ GncResult<S> gnc_tls(const std::vector<Factor<typename S::L>>& graph, const std:
   return out;
 }
 
+// Warm-started GNC-TLS schedule (no counterpart in the reference; the
+// library's GNC warm start restated for parity). probs[k] is a predicted
+// inlier probability for every factor k >= n_known. Steps:
+//  1. weights: known factors 1, others 1 when probs[k] >= 0.5 else 0;
+//     LM from the initial values with those weights;
+//  2. TLS weight update at mu (first mu = warm_mu, which skips the
+//     continuation from mu ~ 0); when the new weights are binary within
+//     weights_tol and equal to the weights of the last solve, the estimate is
+//     a fixed point of the TLS rule and the schedule ends; otherwise LM from
+//     the previous estimate with the new weights, mu *= mu_step, repeat (at
+//     most max_iterations updates);
+//  3. a fixed point reached from a start that admitted outliers can be a poor
+//     local minimum of the TLS cost, in which most of the predicted inliers
+//     end up rejected; the result is therefore certified only when at least
+//     kWarmKeep of the predicted inliers are inliers at the fixed point.
+// certified = false (no fixed point within max_iterations, or the prediction
+// contradicted) sends the caller back to the plain schedule.
+constexpr double kWarmKeep = 0.75;
+
+template <class S>
+GncResult<S> gnc_tls_warm(const std::vector<Factor<typename S::L>>& graph,
+                          const std::map<uint64_t, typename S::Pose>& init, size_t n_known, const GncParamsO& gp,
+                          const LmParamsO& lp, const std::vector<double>& probs, double warm_mu, bool* certified) {
+  GncResult<S> out;
+  const size_t nf = graph.size();
+  std::vector<double> barc(nf, 1.0);
+  for (size_t k = 0; k < nf; ++k)
+    barc[k] = (gp.threshold_mode == 0) ? gp.threshold : 0.5 * chi2inv(gp.threshold, S::d);
+  std::vector<double> weights(nf, 1.0);
+  size_t predicted = 0;
+  for (size_t k = n_known; k < nf; ++k) {
+    weights[k] = (k < probs.size() && probs[k] >= 0.5) ? 1.0 : 0.0;
+    predicted += weights[k] == 1.0;
+  }
+  const std::vector<double> first = weights;
+  NLS<S> nls;
+  nls.graph = &graph;
+  nls.weights = &weights;
+  auto result = nls.optimize(init, lp, &out.stats);
+  double mu = warm_mu;
+  bool fixed_point = nf == n_known;
+  std::vector<double> wnew(nf, 1.0);
+  for (int it = 0; it < gp.max_iterations && !fixed_point; ++it) {
+    out.outer_iterations = it + 1;
+    bool same = true;
+    for (size_t k = n_known; k < nf; ++k) {
+      const double u2 = factor_error<S>(graph[k], result, 1.0);
+      const double ub = (mu + 1.0) / mu * barc[k];
+      const double lb = mu / (mu + 1.0) * barc[k];
+      double wk = std::sqrt(barc[k] * mu * (mu + 1.0) / u2) - mu;
+      if (u2 >= ub || wk < 0.0) wk = 0.0;
+      else if (u2 <= lb || wk > 1.0) wk = 1.0;
+      wnew[k] = wk;
+      if (std::fabs(wk - std::round(wk)) > gp.weights_tol || std::round(wk) != weights[k]) same = false;
+    }
+    if (same) {
+      fixed_point = true;
+      break;
+    }
+    for (size_t k = n_known; k < nf; ++k) weights[k] = wnew[k];
+    result = nls.optimize(result, lp, &out.stats);
+    mu *= gp.mu_step;
+  }
+  size_t kept = 0;
+  for (size_t k = n_known; k < nf; ++k) kept += (first[k] == 1.0 && weights[k] == 1.0);
+  *certified = fixed_point && (double)kept >= kWarmKeep * (double)predicted;
+  out.values = result;
+  out.weights = weights;
+  return out;
+}
+
 }  // namespace oracle

@@ -27,7 +27,8 @@ class Params(C.Structure):
         ("use_gnc", C.c_int32), ("gnc_threshold_mode", C.c_int32), ("gnc_inlier_threshold", C.c_double),
         ("gnc_max_iterations", C.c_int32), ("gnc_mu_step", C.c_double), ("gnc_relative_cost_tol", C.c_double),
         ("gnc_weights_tol", C.c_double), ("gnc_fix_prev_inliers", C.c_int32), ("gnc_bias_odom", C.c_int32),
-        ("lm_diagonal_damping", C.c_int32),
+        ("lm_diagonal_damping", C.c_int32), ("linear_solver", C.c_int32),
+        ("gnc_warm_start", C.c_int32), ("gnc_warm_mu", C.c_double),
     ]
 
 
@@ -69,6 +70,9 @@ def lib():
         _lib.oracle_get_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                           C.POINTER(C.c_int64)]
         _lib.oracle_get_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        _lib.oracle_set_warm_probs.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
+        _lib.oracle_force_optimize.argtypes = [C.c_void_p]
+        _lib.oracle_get_warm_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         _lib.oracle_pwc_op.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                        C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]
         _lib.oracle_pwc_mahalanobis.restype = C.c_double
@@ -174,8 +178,20 @@ class OracleSolver:
         lib().oracle_get_stats(self.h, C.byref(a), C.byref(b), C.byref(c))
         p, s = C.c_double(), C.c_double()
         lib().oracle_get_times(self.h, C.byref(p), C.byref(s))
+        wr, wf = C.c_int64(), C.c_int64()
+        lib().oracle_get_warm_stats(self.h, C.byref(wr), C.byref(wf))
         return dict(lm_iterations=a.value, linear_solves=b.value, gnc_iterations=c.value, pcm_seconds=p.value,
-                    solve_seconds=s.value)
+                    solve_seconds=s.value, warm_runs=wr.value, warm_fallbacks=wf.value)
+
+    def force_optimize(self) -> int:
+        """forceUpdate() with no new factors: re-run the solve."""
+        return lib().oracle_force_optimize(self.h)
+
+    def set_warm_probs(self, probs):
+        """Inlier probabilities for the next warm-started GNC solve, one per
+        factor of the graph to optimise (known inliers are ignored)."""
+        self._warm = np.ascontiguousarray(probs, dtype=np.float64)
+        lib().oracle_set_warm_probs(self.h, _ptr(self._warm), self._warm.size)
 
 
 # ------------------------------------------------------------------ math hooks

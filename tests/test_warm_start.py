@@ -1,0 +1,117 @@
+"""GNC warm start (no counterpart in the reference).
+
+The warm-started schedule takes predicted inlier probabilities, solves with
+the predicted inlier set, then iterates TLS weight updates from mu = warm_mu
+(LM from the previous estimate each time) until the weights reproduce
+themselves (a fixed point of the TLS rule). It is certified only when that
+fixed point keeps >= 75 % of the predicted inliers; otherwise the plain
+GncOptimizer schedule runs from the start.
+
+CPU (oracle) tests pin the schedule's semantics; GPU tests check the CUDA
+schedule against the oracle's on the same probabilities, through the C ABI.
+"""
+import numpy as np
+import pytest
+
+from oracle import rpgo_oracle as O
+from rpgo_gb300 import synth
+from rpgo_gb300.params import QUIET, WARM_ON, RobustSolverParams
+
+ATE_TOL = 1e-4
+
+
+def _params(warm=False, pcm_off=True):
+    p = RobustSolverParams()
+    if pcm_off:
+        p.setPcm3DParams(-1.0, -1.0, QUIET)  # PCM checks disabled: GNC sees every closure
+    else:
+        p.setPcm3DParams(10.0, 5.0, QUIET)
+    p.setGncInlierCostThresholdsAtProbability(0.9)
+    if warm:
+        p.setGncWarmStart(WARM_ON, 100.0)
+    return p
+
+
+def _graph():
+    return synth.walk3d(400, 80, 40, seed=21)
+
+
+def _plain_oracle(s, pcm_off=True):
+    o = O.OracleSolver(_params(pcm_off=pcm_off))
+    assert o.update(s.graph) == 0
+    c = o.counts()
+    return o, c.num_odom + c.num_special
+
+
+def _warm_oracle(s, probs, pcm_off=True):
+    o = O.OracleSolver(_params(True, pcm_off))
+    assert o.update(s.graph, optimize_graph=False) == 0
+    o.set_warm_probs(probs)
+    assert o.force_optimize() == 0
+    return o
+
+
+def test_oracle_warm_with_plain_labels_reproduces_plain():
+    s = _graph()
+    plain, nk = _plain_oracle(s)
+    w = plain.gnc_weights()
+    assert (w[nk:] < 0.5).sum() >= 40  # every outlier reached GNC and was rejected
+    warm = _warm_oracle(s, w)
+    st, sp = warm.stats(), plain.stats()
+    assert st["warm_runs"] == 1 and st["warm_fallbacks"] == 0
+    assert np.array_equal(np.round(warm.gnc_weights()), np.round(w))
+    assert synth.ate(warm.estimate()[1], plain.estimate()[1], 3) <= ATE_TOL
+    assert st["linear_solves"] * 5 < sp["linear_solves"]
+
+
+def test_oracle_warm_falls_back_on_contradicted_prediction():
+    s = _graph()
+    plain, nk = _plain_oracle(s)
+    w = plain.gnc_weights()
+    bad = np.ones_like(w)  # every closure predicted inlier, outliers included
+    warm = _warm_oracle(s, bad)
+    st = warm.stats()
+    assert st["warm_runs"] == 1 and st["warm_fallbacks"] == 1
+    # the plain schedule reran from the start: identical to plain
+    assert np.array_equal(warm.gnc_weights(), w)
+    assert synth.ate(warm.estimate()[1], plain.estimate()[1], 3) == 0.0
+
+
+def test_oracle_warm_probs_of_wrong_size_run_plain():
+    s = _graph()
+    plain, nk = _plain_oracle(s)
+    warm = _warm_oracle(s, np.ones(3))
+    assert warm.stats()["warm_runs"] == 0
+    assert np.array_equal(warm.gnc_weights(), plain.gnc_weights())
+
+
+# ------------------------------------------------------------------ GPU schedule vs the oracle's
+@pytest.mark.gpu
+def test_gpu_warm_schedule_matches_oracle():
+    from rpgo_gb300 import build, capi
+
+    build()
+    s = _graph()
+    plain, nk = _plain_oracle(s)
+    w = plain.gnc_weights()
+    rng = np.random.default_rng(3)
+    for probs in (w, np.where(rng.random(w.size) < 0.05, 1.0 - w, w), np.ones_like(w)):
+        g = capi.RobustSolver(_params(True))
+        assert g.update(s.graph, optimize_graph=False) == 0
+        kind, k1, k2, _ = g.factors()
+        ok, ok1, ok2, _ = plain.factors()
+        assert np.array_equal(k1, ok1) and np.array_equal(k2, ok2)
+        assert g.set_warm_start_probs(probs) == 0
+        assert g.forceUpdate(_empty()) == 0
+        o = _warm_oracle(s, probs)
+        t, so = g.timing(), o.stats()
+        assert t.warm_runs == 1
+        assert t.warm_fallbacks == so["warm_fallbacks"]
+        assert np.array_equal(np.round(g.gnc_weights()), np.round(o.gnc_weights()))
+        assert synth.ate(g.estimate()[1], o.estimate()[1], 3) <= ATE_TOL
+
+
+def _empty():
+    from rpgo_gb300.graph import Graph
+
+    return Graph(3)
