@@ -227,6 +227,33 @@ int rpgo_set_warm_start_probs(rpgo_solver* s, const double* probs, int64_t n);
  * gnc_weights.csv in `folder`. */
 int rpgo_save_data(const rpgo_solver* s, const char* folder);
 
+/* ------------------------------------------------------------------ batches
+ * Many independent graphs (Monte-Carlo trials, submaps) solved in one call.
+ * No counterpart in the reference, whose RobustSolver solves one graph per
+ * instance: graph g gives exactly what RobustSolver(p).update(factors[g],
+ * values[g]) gives (the same PCM, GNC and LM steps). The graphs run
+ * concurrently on `workers` host threads, each solver on its own CUDA stream
+ * with its cooperative direct solve limited to `coop_ctas` CTAs so that
+ * several solves share the GPU (workers <= 0, coop_ctas <= 0: defaults).
+ * Outputs (caller-allocated, graphs in order):
+ *   poses: sum_g values[g].count x stride doubles; graph g's estimate in
+ *     ascending key order at offset sum_{h<g} values[h].count x stride;
+ *   gnc_weights (optional): sum_g factors[g].count doubles; graph g's
+ *     getGncWeights() at offset sum_{h<g} factors[h].count, its length in
+ *     num_weights[g];
+ *   status: per graph, the rpgo_update status;
+ *   timing (optional): per graph, the rpgo_timing of its update.
+ * Returns RPGO_OK when every graph ran (check status per graph). */
+typedef struct rpgo_batch_out {
+  double* poses;
+  double* gnc_weights;
+  int64_t* num_weights;
+  int32_t* status;
+  rpgo_timing* timing;
+} rpgo_batch_out;
+int rpgo_solve_batch(const rpgo_params* p, int32_t n, const rpgo_factor_batch* factors,
+                     const rpgo_value_batch* values, int32_t workers, int32_t coop_ctas, rpgo_batch_out* out);
+
 /* ------------------------------------------------------------ stage kernels
  * Device-resident entry points of the hot path, one per reference function
  * family, for callers that keep the graph in GPU memory. All pointers are

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <fstream>
 #include <memory>
+#include <mutex>
 #include <numeric>
 #include <set>
 #include <string>
@@ -37,7 +38,12 @@ struct rpgo_solver {
   bool last_do_optimize = false;
   rpgo_timing timing{};
   std::vector<double> warm_probs;  // rpgo_set_warm_start_probs, consumed by the next GNC solve
+  int coop_ctas = 0;                // CTAs of the cooperative direct solve (0: one per SM)
 };
+
+namespace rpgo {
+void set_coop_ctas(rpgo_solver* s, int ctas) { s->coop_ctas = ctas; }
+}  // namespace rpgo
 
 namespace {
 
@@ -87,6 +93,7 @@ int optimize(rpgo_solver* s) {
       for (size_t i = 0; i < n_known && i < init.size(); ++i) init[i] = 1.0;
     }
     GpuNls nls(s->dim, full, *s->store, *s->values, s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
+    nls.dev().coop_ctas = s->coop_ctas;
     std::vector<double> w;
     bool warm_done = false;
     if (s->p.gnc_warm_start == RPGO_WARM_ON && s->warm_probs.size() == full.size()) {
@@ -110,6 +117,7 @@ int optimize(rpgo_solver* s) {
           full.push_back(s->nfg[k + i]);
     }
     GpuNls nls(s->dim, full, *s->store, *s->values, s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
+    nls.dev().coop_ctas = s->coop_ctas;
     nls.optimize(lp, &st);
     if (st.failed) return RPGO_ERR_SOLVER;
     nls.write_back(*s->values);
@@ -144,7 +152,7 @@ int update_impl(rpgo_solver* s, std::vector<FactorRec> nf, const rpgo_value_batc
   RPGO_CUDA(cudaEventCreate(&e0));
   RPGO_CUDA(cudaEventCreate(&e1));
   RPGO_CUDA(cudaEventCreate(&e2));
-  const int64_t launches0 = launch_counter().load();
+  const int64_t launches0 = thread_launch_counter();
   const int64_t pairs0 = s->pcm ? s->pcm->stats().pair_checks : 0;
   const KernelTimes kt0 = kernel_times();
   RPGO_CUDA(cudaEventRecord(e0, s->st));
@@ -169,7 +177,7 @@ int update_impl(rpgo_solver* s, std::vector<FactorRec> nf, const rpgo_value_batc
   s->timing.pcm_ms = ms_since(e0, e1);
   s->timing.solve_ms = ms_since(e1, e2);
   s->timing.pair_checks = (s->pcm ? s->pcm->stats().pair_checks : 0) - pairs0;
-  s->timing.kernel_launches = launch_counter().load() - launches0;
+  s->timing.kernel_launches = thread_launch_counter() - launches0;
   const KernelTimes& kt = kernel_times();
   s->timing.pcg_kernel_ms = kt.pcg_ms - kt0.pcg_ms;
   s->timing.pcg_kernel_launches = kt.pcg_launches - kt0.pcg_launches;
@@ -203,10 +211,25 @@ int guarded(F&& f) {
   }
 }
 
+// The device's default memory pool backs every DeviceBuffer. It keeps up to
+// kPoolKeepBytes of freed memory for reuse instead of returning it to the
+// driver at each synchronisation.
+constexpr uint64_t kPoolKeepBytes = 8ull << 30;
+
 int device_ready() {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) return 0;
-  return 1;
+  static std::once_flag once;
+  static bool pool_ok = false;
+  std::call_once(once, [] {
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = kPoolKeepBytes;
+      pool_ok = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep) == cudaSuccess;
+    }
+  });
+  return pool_ok ? 1 : 0;
 }
 
 }  // namespace
@@ -399,6 +422,7 @@ rpgo_solver* rpgo_create(const rpgo_params* p) {
   s->d = dim == 3 ? 6 : 3;
   try {
     RPGO_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
+    AllocStreamScope scope(s->st);
     s->values = std::make_unique<ValueStore>(s->stride);
     s->store = std::make_unique<FactorStore>(s->stride, s->d);
     if (m != RPGO_OUTLIER_NONE) {
@@ -424,29 +448,36 @@ rpgo_solver* rpgo_create(const rpgo_params* p) {
 void rpgo_destroy(rpgo_solver* s) {
   if (!s) return;
   cudaStream_t st = s->st;
-  s->pcm.reset();
-  s->values.reset();
-  s->store.reset();
-  delete s;
+  {
+    AllocStreamScope scope(st);
+    s->pcm.reset();
+    s->values.reset();
+    s->store.reset();
+    delete s;
+  }
   if (st) cudaStreamDestroy(st);
 }
 
 int rpgo_update(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, int32_t optimize_graph) {
   if (!s) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
   return guarded([&] { return update_impl(s, ingest(s, f, false), v, false, optimize_graph, false); });
 }
 int rpgo_update_dev(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, int32_t optimize_graph) {
   if (!s) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
   return guarded([&] { return update_impl(s, ingest(s, f, true), v, true, optimize_graph, false); });
 }
 int rpgo_force_update(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v) {
   if (!s) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
   return guarded([&] { return update_impl(s, ingest(s, f, false), v, false, 1, true); });
 }
 
 static int update_with_extra(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v,
                              const rpgo_factor_batch* extra) {
   if (!s) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
   return guarded([&] {
     auto all = ingest(s, f, false);
     auto more = ingest(s, extra, false);
@@ -477,6 +508,7 @@ int rpgo_get_counts(const rpgo_solver* s, rpgo_counts* c) {
 }
 int rpgo_get_estimate(const rpgo_solver* s, uint64_t* keys, double* poses, int64_t cap) {
   if (!s || (int64_t)s->values->size() > cap) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
   return guarded([&] {
     std::vector<uint64_t> k;
     std::vector<double> p;
@@ -493,6 +525,7 @@ int rpgo_get_gnc_weights(const rpgo_solver* s, double* w, int64_t cap) {
 }
 int rpgo_get_factors(const rpgo_solver* s, int32_t* kind, uint64_t* k1, uint64_t* k2, double* meas, int64_t cap) {
   if (!s || (int64_t)s->nfg.size() > cap) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
   return guarded([&] {
     for (size_t i = 0; i < s->nfg.size(); ++i) {
       if (kind) kind[i] = s->nfg[i].kind;
@@ -512,6 +545,7 @@ int rpgo_get_factors(const rpgo_solver* s, int32_t* kind, uint64_t* k1, uint64_t
 int rpgo_get_adjacency(const rpgo_solver* s, int32_t group, uint32_t* words, int64_t cap, int64_t* n) {
   if (!s || !n) return RPGO_ERR_ARG;
   if (!s->pcm) return RPGO_ERR_UNSUPPORTED;
+  AllocStreamScope scope(s->st);
   return guarded([&] {
     std::vector<uint32_t> w;
     int nn = 0;
@@ -536,6 +570,7 @@ int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* t) {
 
 int rpgo_save_data(const rpgo_solver* s, const char* folder) {
   if (!s || !folder) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
   return guarded([&] { return save_data_impl_(s, folder); });
 }
 // ------------------------------------------------------------------ stage entry points (device pointers)
@@ -543,6 +578,7 @@ int rpgo_trajectory_scan_dev(int32_t dim, int32_t mode, int64_t count, const int
                              const double* delta_pose, const double* delta_cov, double* traj_pose, double* traj_cov,
                              int32_t* traj_node, uint8_t* traj_rot_info, void* stream) {
   if ((dim != 2 && dim != 3) || (mode != 0 && mode != 1) || count < 0) return RPGO_ERR_ARG;
+  AllocStreamScope scope((cudaStream_t)stream);
   return guarded([&] {
     DeviceBuffer<double> rec, cov;
     DeviceBuffer<uint8_t> rot;
@@ -556,6 +592,7 @@ int rpgo_odometry_check_dev(int32_t dim, int32_t mode, int64_t count, const int3
                             const double* zp, const double* zc, const double* tp, const double* tc, const int32_t* tn,
                             const uint8_t* tr, double th0, double th1, uint8_t* ok, void* stream) {
   if ((dim != 2 && dim != 3) || (mode != 0 && mode != 1) || count < 0) return RPGO_ERR_ARG;
+  AllocStreamScope scope((cudaStream_t)stream);
   return guarded([&] {
     TrajView tv{const_cast<double*>(tp), const_cast<double*>(tc), const_cast<int32_t*>(tn),
                 const_cast<uint8_t*>(tr)};
@@ -571,6 +608,7 @@ int rpgo_pairwise_adjacency_dev(int32_t dim, int32_t mode, int32_t n, int32_t ro
   if ((dim != 2 && dim != 3) || (mode != 0 && mode != 1) || n < 0 || row_begin < 0 || row_begin > n ||
       words < (n + 31) / 32)
     return RPGO_ERR_ARG;
+  AllocStreamScope scope((cudaStream_t)stream);
   return guarded([&] {
     TrajView tv{const_cast<double*>(tp), const_cast<double*>(tc), const_cast<int32_t*>(tn),
                 const_cast<uint8_t*>(tr)};
@@ -584,6 +622,7 @@ int rpgo_pairwise_adjacency_dev(int32_t dim, int32_t mode, int32_t n, int32_t ro
 int rpgo_max_clique_heu_dev(int32_t n, const uint32_t* adj, int32_t words, int32_t first, int32_t seed,
                             int32_t* clique_out, int32_t* size_out, void* stream) {
   if (n < 0 || words < (n + 31) / 32 || !size_out) return RPGO_ERR_ARG;
+  AllocStreamScope scope((cudaStream_t)stream);
   return guarded([&] {
     CliqueWorkspace ws;
     std::vector<int32_t> cl;
@@ -602,6 +641,7 @@ int rpgo_pairwise_adjacency(int32_t dim, int32_t mode, int32_t n, const int32_t*
                             double th1, uint32_t* adj) {
   if ((dim != 2 && dim != 3) || (mode != 0 && mode != 1) || n < 0 || num_slots < 0) return RPGO_ERR_ARG;
   if (!device_ready()) return RPGO_ERR_CUDA;
+  AllocStreamScope scope(nullptr);
   return guarded([&] {
     const int stride = dim == 3 ? 12 : 4, d = dim == 3 ? 6 : 3;
     const int words = (n + 31) / 32;
@@ -632,6 +672,7 @@ int rpgo_max_clique_heu(int32_t n, const uint32_t* adj, int32_t first, int32_t s
                         int32_t* size_out) {
   if (n < 0 || !size_out) return RPGO_ERR_ARG;
   if (!device_ready()) return RPGO_ERR_CUDA;
+  AllocStreamScope scope(nullptr);
   return guarded([&] {
     const int words = (n + 31) / 32;
     cudaStream_t st = 0;

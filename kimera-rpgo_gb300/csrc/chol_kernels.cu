@@ -781,13 +781,8 @@ SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st) {
     o.ok = 1;
     return o;
   }
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    RPGO_CUDA(cudaGetDevice(&dev));
-    RPGO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  }
-  const int grid = sms;
+  const int sms = device_sm_count();
+  const int grid = s.coop_ctas > 0 ? std::min(s.coop_ctas, sms) : sms;
   c.part.resize((size_t)2 * grid);
   const CholPlan& p = c.plan;
   CholArgs a{s.N, p.n_sparse, p.T, p.n_tiles * kTB, p.n_tiles, c.levels,

@@ -26,11 +26,30 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
 #define RPGO_CUDA(x) ::rpgo::cuda_check((x), #x, __FILE__, __LINE__)
 #define RPGO_LAUNCHED() ::rpgo::note_launch(cudaGetLastError(), __FILE__, __LINE__)
 
-// Count of kernels this library has launched (process-wide).
+// Count of kernels this library has launched (process-wide), and by the
+// calling host thread (per-update figures of concurrent solvers stay apart).
 std::atomic<int64_t>& launch_counter();
+int64_t& thread_launch_counter();
+
+// Device memory is stream-ordered (cudaMallocAsync / cudaFreeAsync from the
+// device's default pool): a free never synchronises the device, so solvers on
+// different streams and host threads run concurrently. Every buffer is
+// allocated and freed on the calling thread's allocation stream, which each C
+// ABI entry point sets to the stream its work runs on (AllocStreamScope).
+cudaStream_t& alloc_stream();
+class AllocStreamScope {
+ public:
+  explicit AllocStreamScope(cudaStream_t st) : prev_(alloc_stream()) { alloc_stream() = st; }
+  ~AllocStreamScope() { alloc_stream() = prev_; }
+  AllocStreamScope(const AllocStreamScope&) = delete;
+  AllocStreamScope& operator=(const AllocStreamScope&) = delete;
+
+ private:
+  cudaStream_t prev_;
+};
 
 // Device time of the dominant kernels, measured with CUDA events on the
-// launching stream (process-wide running sums).
+// launching stream (running sums of the calling host thread).
 struct KernelTimes {
   double pcg_ms = 0.0, pcg_bytes = 0.0;
   int64_t pcg_launches = 0;
@@ -69,6 +88,7 @@ class EventTimer {
 inline void note_launch(cudaError_t e, const char* file, int line) {
   cuda_check(e, "kernel launch", file, line);
   launch_counter().fetch_add(1, std::memory_order_relaxed);
+  ++thread_launch_counter();
 }
 
 template <class T>
@@ -78,11 +98,13 @@ class DeviceBuffer {
   explicit DeviceBuffer(size_t n) { resize(n); }
   DeviceBuffer(const DeviceBuffer&) = delete;
   DeviceBuffer& operator=(const DeviceBuffer&) = delete;
-  DeviceBuffer(DeviceBuffer&& o) noexcept : p_(o.p_), n_(o.n_), cap_(o.cap_) { o.p_ = nullptr; o.n_ = o.cap_ = 0; }
+  DeviceBuffer(DeviceBuffer&& o) noexcept : p_(o.p_), n_(o.n_), cap_(o.cap_), st_(o.st_) {
+    o.p_ = nullptr; o.n_ = o.cap_ = 0;
+  }
   DeviceBuffer& operator=(DeviceBuffer&& o) noexcept {
     if (this != &o) {
       release();
-      p_ = o.p_; n_ = o.n_; cap_ = o.cap_;
+      p_ = o.p_; n_ = o.n_; cap_ = o.cap_; st_ = o.st_;
       o.p_ = nullptr; o.n_ = o.cap_ = 0;
     }
     return *this;
@@ -93,22 +115,24 @@ class DeviceBuffer {
     if (n > cap_) {
       release();
       size_t c = n < 16 ? 16 : n;
-      RPGO_CUDA(cudaMalloc(&p_, c * sizeof(T)));
+      RPGO_CUDA(cudaMallocAsync((void**)&p_, c * sizeof(T), alloc_stream()));
+      st_ = alloc_stream();
       cap_ = c;
     }
     n_ = n;
   }
-  // grow keeping the first n_ elements (capacity doubles)
+  // grow keeping the first n_ elements (capacity doubles); st must be the
+  // allocation stream or ordered after it
   void grow(size_t n, cudaStream_t st) {
     if (n > cap_) {
       size_t c = cap_ ? cap_ : 16;
       while (c < n) c *= 2;
       T* q = nullptr;
-      RPGO_CUDA(cudaMalloc(&q, c * sizeof(T)));
+      RPGO_CUDA(cudaMallocAsync((void**)&q, c * sizeof(T), alloc_stream()));
       if (p_ && n_) RPGO_CUDA(cudaMemcpyAsync(q, p_, n_ * sizeof(T), cudaMemcpyDeviceToDevice, st));
-      RPGO_CUDA(cudaStreamSynchronize(st));
       release();
       p_ = q;
+      st_ = alloc_stream();
       cap_ = c;
     }
     n_ = n;
@@ -128,15 +152,29 @@ class DeviceBuffer {
   size_t size() const { return n_; }
 
  private:
+  // freed on the stream the buffer was allocated on: every use of a buffer
+  // is on that stream (or synchronised before the free)
   void release() {
-    if (p_) cudaFree(p_);
+    if (p_) cudaFreeAsync(p_, st_);
     p_ = nullptr;
     n_ = cap_ = 0;
   }
   T* p_ = nullptr;
   size_t n_ = 0, cap_ = 0;
+  cudaStream_t st_ = nullptr;
 };
 
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+// SM count of the current device (looked up once per process).
+inline int device_sm_count() {
+  static const int sms = [] {
+    int dev = 0, n = 0;
+    RPGO_CUDA(cudaGetDevice(&dev));
+    RPGO_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+    return n;
+  }();
+  return sms;
+}
 
 }  // namespace rpgo

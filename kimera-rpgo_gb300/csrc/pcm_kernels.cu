@@ -548,9 +548,17 @@ std::atomic<int64_t>& launch_counter() {
   static std::atomic<int64_t> c{0};
   return c;
 }
+int64_t& thread_launch_counter() {
+  thread_local int64_t c = 0;
+  return c;
+}
 KernelTimes& kernel_times() {
-  static KernelTimes t;
+  thread_local KernelTimes t;
   return t;
+}
+cudaStream_t& alloc_stream() {
+  thread_local cudaStream_t st = nullptr;
+  return st;
 }
 
 }  // namespace rpgo

@@ -1491,12 +1491,7 @@ SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
     o.ok = 1;
     return o;
   }
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    RPGO_CUDA(cudaGetDevice(&dev));
-    RPGO_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  }
+  const int sms = device_sm_count();
   const int grid = sms, threads = 256;
   s.part.resize((size_t)4 * grid);
   CsrView A{s.Hd.get(), s.fH.get(), s.Hd64.get(), s.fH64.get(), s.row_ptr.get(), s.col.get(), s.blk.get(),

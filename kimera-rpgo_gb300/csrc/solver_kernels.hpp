@@ -15,6 +15,7 @@ struct CholDev;
 // Device-resident problem: factors, structure, per-iteration buffers.
 struct SolverDev {
   int dim = 3, d = 6, stride = 12, N = 0, F = 0;
+  int coop_ctas = 0;  // CTAs of the cooperative direct solve (0: one per SM)
   // factors
   DeviceBuffer<int32_t> kind, vi, vj;
   DeviceBuffer<uint8_t> tree;            // between factor joining consecutive variables

@@ -59,6 +59,11 @@ class Timing(C.Structure):
         ("warm_runs", C.c_int64), ("warm_fallbacks", C.c_int64)]
 
 
+class BatchOut(C.Structure):
+    _fields_ = [("poses", C.c_void_p), ("gnc_weights", C.c_void_p), ("num_weights", C.c_void_p),
+                ("status", C.c_void_p), ("timing", C.c_void_p)]
+
+
 # every exported entry point: name -> (restype, argtypes)
 _P = C.c_void_p
 SIGNATURES = {
@@ -86,6 +91,8 @@ SIGNATURES = {
     "rpgo_get_adjacency": (C.c_int, [_P, C.c_int32, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "rpgo_get_timing": (C.c_int, [_P, C.POINTER(Timing)]),
     "rpgo_set_warm_start_probs": (C.c_int, [_P, _P, C.c_int64]),
+    "rpgo_solve_batch": (C.c_int, [C.POINTER(Params), C.c_int32, _P, _P, C.c_int32, C.c_int32,
+                                   C.POINTER(BatchOut)]),
     "rpgo_save_data": (C.c_int, [_P, C.c_char_p]),
     "rpgo_trajectory_scan_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [_P]),
     "rpgo_odometry_check_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [C.c_double, C.c_double,
@@ -272,6 +279,39 @@ class RobustSolver:
 
 
 # ------------------------------------------------------------------ stage functions (host arrays)
+def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0):
+    """rpgo_solve_batch: solve independent graphs concurrently. Returns a
+    list of (status, keys, poses, gnc_weights, timing) per graph, the poses in
+    ascending key order as calculateEstimate() gives them."""
+    n = len(graphs)
+    batches = [Batch(g) for g in graphs]
+    fb = (FactorBatch * max(n, 1))(*[b.f for b in batches])
+    vb = (ValueBatch * max(n, 1))(*[b.v for b in batches])
+    dim = 2 if params.outlier_removal in (1, 3) or (params.outlier_removal == 0 and params.dim == 2) else 3
+    st = 12 if dim == 3 else 4
+    nv = [int(b.v.count) for b in batches]
+    nf = [int(b.f.count) for b in batches]
+    poses = np.zeros((max(sum(nv), 1), st))
+    weights = np.zeros(max(sum(nf), 1))
+    num_w = np.zeros(max(n, 1), dtype=np.int64)
+    status = np.zeros(max(n, 1), dtype=np.int32)
+    timing = (Timing * max(n, 1))()
+    out = BatchOut(_ptr(poses), _ptr(weights), _ptr(num_w), _ptr(status), C.cast(timing, C.c_void_p))
+    p = params_struct(params)
+    rc = load().rpgo_solve_batch(C.byref(p), n, C.cast(fb, C.c_void_p), C.cast(vb, C.c_void_p), int(workers),
+                                 int(coop_ctas), C.byref(out))
+    if rc:
+        raise RpgoError(f"rpgo_solve_batch: {rc}")
+    res, vo, fo = [], 0, 0
+    for g in range(n):
+        keys = np.sort(np.asarray(batches[g].a["value_keys"], dtype=np.uint64))
+        res.append((int(status[g]), keys, poses[vo:vo + nv[g]].copy(), weights[fo:fo + int(num_w[g])].copy(),
+                    timing[g]))
+        vo += nv[g]
+        fo += nf[g]
+    return res
+
+
 def pairwise_adjacency(dim, mode, slot_a, slot_b, flip, z_pose, z_cov, traj_pose, traj_cov, traj_node, traj_rot,
                        th0, th1):
     n = len(slot_a)

@@ -52,6 +52,33 @@ def se3_exp(xi):
     return T
 
 
+def _skew_n(w):
+    K = np.zeros(w.shape[:-1] + (3, 3))
+    K[..., 0, 1], K[..., 0, 2], K[..., 1, 2] = -w[..., 2], w[..., 1], -w[..., 0]
+    K[..., 1, 0], K[..., 2, 0], K[..., 2, 1] = w[..., 2], -w[..., 1], w[..., 0]
+    return K
+
+
+def se3_exp_n(xi):
+    """Batched se3_exp: (..., 6) -> (..., 4, 4)."""
+    w, v = xi[..., :3], xi[..., 3:]
+    th = np.linalg.norm(w, axis=-1)[..., None, None]
+    K = _skew_n(w)
+    K2 = K @ K
+    small = th < 1e-12
+    ths = np.where(small, 1.0, th)
+    A = np.where(small, 1.0, np.sin(ths) / ths)
+    B = np.where(small, 0.0, (1 - np.cos(ths)) / ths ** 2)
+    Bv = np.where(small, 0.5, B)
+    C = np.where(small, 0.0, (ths - np.sin(ths)) / ths ** 3)
+    I = np.eye(3)
+    T = np.zeros(xi.shape[:-1] + (4, 4))
+    T[..., :3, :3] = I + A * K + B * K2
+    T[..., :3, 3] = ((I + Bv * K + C * K2) @ v[..., None])[..., 0]
+    T[..., 3, 3] = 1.0
+    return T
+
+
 def uniform_rotation(rng):
     u1, u2, u3 = rng.random(3)
     q = (math.sqrt(1 - u1) * math.sin(2 * math.pi * u2), math.sqrt(1 - u1) * math.cos(2 * math.pi * u2),
@@ -121,15 +148,15 @@ def walk3d(n_poses=5000, n_inliers=1000, n_outliers=333, seed=2, step=0.5, rot_s
     g = Graph(3)
     k = lambda i: symbol(prefix, i)
     g.insert(k(0), _p(est[0]))
-    odom = []
+    # per step: 3 rotation-increment draws then 6 noise draws (one stream)
+    draws = rng.standard_normal((max(n_poses - 1, 0), 9))
+    D = se3_exp_n(np.concatenate([draws[:, :3] * rot_sigma, np.zeros((len(draws), 3))], axis=1))
+    D[:, :3, 3] = (step, 0, 0)
+    Z = D @ se3_exp_n(draws[:, 3:] * sig)
+    odom = list(Z)
     for i in range(1, n_poses):
-        d = np.eye(4)
-        d[:3, :3] = so3_exp(rng.normal(0, rot_sigma, 3))
-        d[:3, 3] = (step, 0, 0)
-        gt.append(gt[-1] @ d)
-        z = d @ se3_exp(rng.normal(0, 1, 6) * sig)
-        est.append(est[-1] @ z)
-        odom.append(z)
+        gt.append(gt[-1] @ D[i - 1])
+        est.append(est[-1] @ Z[i - 1])
         g.insert(k(i), _p(est[-1]))
     for i, z in enumerate(odom):
         g.add_between(k(i), k(i + 1), _p(z), noise)
@@ -220,6 +247,26 @@ def config_c2():
 def config_c3():
     """3D random walk: 50,000 poses, 20,000 closures with 30% outliers (seed 3)."""
     return walk3d(50000, 14000, 6000, seed=3)
+
+
+def config_c4_sizes(n_graphs=512, seed=4):
+    """Sizes of the batched workload: per graph (poses, inlier closures,
+    outlier closures, seed); poses ~ U[200, 8000], closures 10-30 % of the
+    poses, outlier rate ~ U[0, 0.5] of the closures."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for g in range(n_graphs):
+        n = int(rng.integers(200, 8001))
+        lc = int(round(rng.uniform(0.10, 0.30) * n))
+        no = int(round(rng.uniform(0.0, 0.5) * lc))
+        out.append((n, lc - no, no, seed + g))
+    return out
+
+
+def config_c4(n_graphs=512, seed=4):
+    """Batched workload: independent 3D random walks of the walk3d generator
+    with the sizes of config_c4_sizes."""
+    return [walk3d(n, ni, no, seed=s) for n, ni, no, s in config_c4_sizes(n_graphs, seed)]
 
 
 def ate(est_poses: np.ndarray, ref_poses: np.ndarray, dim: int = 3) -> float:

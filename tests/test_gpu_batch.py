@@ -1,0 +1,68 @@
+"""Batched solve of independent graphs (rpgo_solve_batch) through the C ABI.
+
+Each graph of the batch must give what its own RobustSolver.update gives:
+the same GNC inlier set and the same poses (the batch runs the same kernels,
+concurrently, with the cooperative direct solve on fewer CTAs), and the
+oracle's result for a graph checked against the CPU FP64 oracle.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import rpgo_oracle as O
+from rpgo_gb300 import capi, synth
+from rpgo_gb300.params import QUIET, RobustSolverParams
+
+ATE_TOL = 1e-4
+SIZES = [(200, 30, 10, 41), (350, 60, 20, 42), (500, 80, 30, 43), (300, 40, 0, 44), (450, 70, 35, 45),
+         (250, 30, 25, 46), (600, 90, 10, 47)]
+
+
+def _params():
+    return RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+
+
+def test_batch_argument_checks_need_no_gpu():
+    lib = capi.load()
+    p = capi.params_struct(_params())
+    assert lib.rpgo_solve_batch(C.byref(p), 0, None, None, 0, 0, None) == 0
+    assert lib.rpgo_solve_batch(C.byref(p), -1, None, None, 0, 0, None) != 0
+    assert lib.rpgo_solve_batch(C.byref(p), 2, None, None, 0, 0, None) != 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("workers,ctas", [(3, 0), (7, 8), (1, 0)])
+def test_batch_equals_individual_solves(workers, ctas):
+    from rpgo_gb300 import build
+
+    build()
+    graphs = [synth.walk3d(n, ni, no, seed=s) for n, ni, no, s in SIZES]
+    res = capi.solve_batch(_params(), [s.graph for s in graphs], workers=workers, coop_ctas=ctas)
+    assert len(res) == len(graphs)
+    for s, (status, keys, poses, w, t) in zip(graphs, res):
+        assert status == 0
+        g = capi.RobustSolver(_params())
+        assert g.update(s.graph) == 0
+        k1, p1 = g.estimate()
+        assert np.array_equal(keys, k1)
+        assert np.array_equal(np.round(w), np.round(g.gnc_weights()))
+        assert synth.ate(poses, p1, 3) <= ATE_TOL
+        np.testing.assert_allclose(poses, p1, rtol=1e-6, atol=1e-9)
+        assert t.gnc_iterations > 0 and t.kernel_launches > 0
+
+
+@pytest.mark.gpu
+def test_batch_graph_matches_oracle():
+    from rpgo_gb300 import build
+
+    build()
+    s = synth.walk3d(400, 60, 20, seed=48)
+    (status, keys, poses, w, t), = capi.solve_batch(_params(), [s.graph], workers=1, coop_ctas=16)
+    assert status == 0
+    o = O.OracleSolver(_params())
+    assert o.update(s.graph) == 0
+    ko, po = o.estimate()
+    assert np.array_equal(keys, ko)
+    assert np.array_equal(np.round(w), np.round(o.gnc_weights()))
+    assert synth.ate(poses, po, 3) <= ATE_TOL
