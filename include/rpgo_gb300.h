@@ -223,6 +223,43 @@ int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* out);
  * RPGO_WARM_ON and n equals the graph size (else the installed closure model
  * predicts them), then cleared. */
 int rpgo_set_warm_start_probs(rpgo_solver* s, const double* probs, int64_t n);
+
+/* Closure network of the warm start (no counterpart in the reference): 16
+ * features -> 64 ReLU -> 64 ReLU -> 1, sigmoid; one flat FP32 parameter
+ * array of RPGO_MLP_PARAMS floats:
+ *   [0,16) feature mean, [16,32) 1/std, [32,1056) W1 (64x16, row = unit),
+ *   [1056,1120) b1, [1120,5216) W2 (64x64), [5216,5280) b2,
+ *   [5280,5344) W3, [5344] b3.
+ * The kernels multiply with the weights rounded to BF16 (nearest even) and
+ * accumulate in FP32.
+ * Features of closure (i -> j, Z, R = sqrt information) at the initial
+ * values X: e = Logmap(Z^-1 Xi^-1 Xj), r = R e, c = |r|^2, gap = |i - j|
+ * (0 between robots):
+ *   0-5 log1p|r_k| (2D: 0-2, rest 0), 6 log1p(c), 7 rotation angle of e,
+ *   8 log1p|translation of e|, 9 log1p(gap), 10 log1p(c / max(1, gap)),
+ *   11 PCM degree / (group size - 1), 12 log1p(PCM degree),
+ *   13 neighbours in the PCM consistent set / (set size - 1),
+ *   14 log1p|translation of Z|, 15 rotation angle of Z. */
+#define RPGO_MLP_FEATURES 16
+#define RPGO_MLP_PARAMS 5345
+/* Installs a closure network (host array of RPGO_MLP_PARAMS floats; NULL
+ * removes it). With gnc_warm_start = RPGO_WARM_ON its predictions are the
+ * warm start's inlier probabilities. */
+int rpgo_set_warm_start_model(rpgo_solver* s, const float* params);
+/* Features of the closures of the last GNC solve run with gnc_warm_start ON
+ * or RECORD: *n rows of RPGO_MLP_FEATURES floats in the order of the
+ * graph's closures (factors after the odometry and priors). out may be NULL
+ * to query *n. */
+int rpgo_get_closure_features(const rpgo_solver* s, float* out, int64_t capacity, int64_t* n);
+/* prob[k] = network(features[k]) for k < n (device pointers). */
+int rpgo_mlp_forward_dev(const float* params, int64_t n, const float* features, float* prob, void* stream);
+/* One training step on n labelled closures (device pointers; labels 0/1):
+ * grad (RPGO_MLP_PARAMS floats) receives the gradient of the mean binary
+ * cross-entropy (normalisation slots zero), *loss (host, optional) the loss;
+ * with lr > 0 one Adam step (beta 0.9 / 0.999, eps 1e-8, bias-corrected with
+ * step >= 1) updates params[32:] and the moments adam_m, adam_v. */
+int rpgo_mlp_train_step_dev(float* params, float* adam_m, float* adam_v, int64_t step, float lr, int64_t n,
+                            const float* features, const float* labels, float* grad, double* loss, void* stream);
 /* RobustSolver::saveData (src/RobustSolver.cpp:448-465): result.g2o and
  * gnc_weights.csv in `folder`. */
 int rpgo_save_data(const rpgo_solver* s, const char* folder);

@@ -22,6 +22,7 @@
 #include "../../include/rpgo_gb300.h"
 #include "pcm_engine.hpp"
 #include "solver.hpp"
+#include "warm.hpp"
 
 using namespace rpgo;
 
@@ -39,6 +40,9 @@ struct rpgo_solver {
   rpgo_timing timing{};
   std::vector<double> warm_probs;  // rpgo_set_warm_start_probs, consumed by the next GNC solve
   int coop_ctas = 0;                // CTAs of the cooperative direct solve (0: one per SM)
+  DeviceBuffer<float> model;        // closure network parameters (rpgo_set_warm_start_model)
+  bool has_model = false;
+  std::vector<float> features;      // closure features of the last GNC solve (warm modes)
 };
 
 namespace rpgo {
@@ -70,6 +74,45 @@ std::vector<FactorRec> ingest(rpgo_solver* s, const rpgo_factor_batch* f, bool o
   return out;
 }
 
+// Features of the closures of the graph to optimise (factors n_known..) at
+// the initial values, kept for rpgo_get_closure_features; with an installed
+// closure network and no caller-given probabilities, its predictions become
+// the warm start's inlier probabilities.
+void closure_features_and_probs(rpgo_solver* s, GpuNls& nls, const std::vector<FactorRec>& full, size_t n_known) {
+  const size_t F = full.size();
+  const int64_t nlc = (int64_t)F - (int64_t)n_known;
+  s->features.clear();
+  if (nlc <= 0) return;
+  std::vector<float> pcm_stats;
+  if (s->pcm) s->pcm->closure_stats(&pcm_stats);
+  std::vector<float> aux((size_t)nlc * 4, 0.f);
+  for (int64_t q = 0; q < nlc; ++q) {
+    const FactorRec& f = full[n_known + q];
+    const uint64_t kmask = (1ull << 56) - 1;
+    if (key_chr(f.k1) == key_chr(f.k2)) {
+      const uint64_t a = f.k1 & kmask, b = f.k2 & kmask;
+      aux[q * 4] = (float)(a > b ? a - b : b - a);
+    }
+    if (pcm_stats.size() == (size_t)nlc * 3)
+      for (int c = 0; c < 3; ++c) aux[q * 4 + 1 + c] = pcm_stats[q * 3 + c];
+  }
+  DeviceBuffer<float> daux, dfeat((size_t)nlc * kFeat);
+  daux.upload(aux, s->st);
+  closure_features(nls.dev(), (int)n_known, daux.get(), dfeat.get(), s->st);
+  s->features.resize((size_t)nlc * kFeat);
+  dfeat.download(s->features.data(), s->features.size(), s->st);
+  if (s->p.gnc_warm_start == RPGO_WARM_ON && s->has_model && s->warm_probs.size() != F) {
+    DeviceBuffer<float> dprob((size_t)nlc);
+    mlp_forward(s->model.get(), nlc, dfeat.get(), dprob.get(), s->st);
+    std::vector<float> prob((size_t)nlc);
+    dprob.download(prob.data(), prob.size(), s->st);
+    RPGO_CUDA(cudaStreamSynchronize(s->st));
+    s->warm_probs.assign(F, 1.0);
+    for (int64_t q = 0; q < nlc; ++q) s->warm_probs[n_known + q] = prob[q];
+  }
+  RPGO_CUDA(cudaStreamSynchronize(s->st));
+}
+
 // RobustSolver::optimize (src/RobustSolver.cpp:115-306)
 int optimize(rpgo_solver* s) {
   LmParams lp;
@@ -94,6 +137,8 @@ int optimize(rpgo_solver* s) {
     }
     GpuNls nls(s->dim, full, *s->store, *s->values, s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
     nls.dev().coop_ctas = s->coop_ctas;
+    if (s->p.gnc_warm_start == RPGO_WARM_ON || s->p.gnc_warm_start == RPGO_WARM_RECORD)
+      closure_features_and_probs(s, nls, full, n_known);
     std::vector<double> w;
     bool warm_done = false;
     if (s->p.gnc_warm_start == RPGO_WARM_ON && s->warm_probs.size() == full.size()) {
@@ -561,6 +606,49 @@ int rpgo_set_warm_start_probs(rpgo_solver* s, const double* probs, int64_t n) {
   if (!s || n < 0 || (n > 0 && !probs)) return RPGO_ERR_ARG;
   s->warm_probs.assign(probs, probs + n);
   return RPGO_OK;
+}
+int rpgo_set_warm_start_model(rpgo_solver* s, const float* params) {
+  if (!s) return RPGO_ERR_ARG;
+  if (!params) {
+    s->has_model = false;
+    return RPGO_OK;
+  }
+  AllocStreamScope scope(s->st);
+  return guarded([&] {
+    s->model.upload(params, kMlpParams, s->st);
+    RPGO_CUDA(cudaStreamSynchronize(s->st));
+    s->has_model = true;
+    return (int)RPGO_OK;
+  });
+}
+int rpgo_get_closure_features(const rpgo_solver* s, float* out, int64_t cap, int64_t* n) {
+  if (!s || !n) return RPGO_ERR_ARG;
+  *n = (int64_t)(s->features.size() / kFeat);
+  if (!out) return RPGO_OK;
+  if ((int64_t)s->features.size() > cap * kFeat) return RPGO_ERR_ARG;
+  std::memcpy(out, s->features.data(), sizeof(float) * s->features.size());
+  return RPGO_OK;
+}
+int rpgo_mlp_forward_dev(const float* params, int64_t n, const float* features, float* prob, void* stream) {
+  if (n < 0 || (n > 0 && (!params || !features || !prob))) return RPGO_ERR_ARG;
+  AllocStreamScope scope((cudaStream_t)stream);
+  return guarded([&] {
+    mlp_forward(params, n, features, prob, (cudaStream_t)stream);
+    RPGO_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return (int)RPGO_OK;
+  });
+}
+int rpgo_mlp_train_step_dev(float* params, float* adam_m, float* adam_v, int64_t step, float lr, int64_t n,
+                            const float* features, const float* labels, float* grad, double* loss, void* stream) {
+  if (n < 0 || !params || !grad || (lr > 0.f && (!adam_m || !adam_v || step < 1)) ||
+      (n > 0 && (!features || !labels)))
+    return RPGO_ERR_ARG;
+  AllocStreamScope scope((cudaStream_t)stream);
+  return guarded([&] {
+    const double l = mlp_train_step(params, adam_m, adam_v, step, lr, n, features, labels, grad, (cudaStream_t)stream);
+    if (loss) *loss = l;
+    return (int)RPGO_OK;
+  });
 }
 int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* t) {
   if (!s || !t) return RPGO_ERR_ARG;

@@ -3,8 +3,11 @@
 #include "pcm_engine.hpp"
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <stdexcept>
+
+#include "warm.hpp"
 
 namespace rpgo {
 
@@ -304,6 +307,37 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
   for (const auto& kv : groups_)
     for (int32_t idx : kv.second.consistent) out->push_back(kv.second.factors[idx]);
   return do_optimize;
+}
+
+void PcmEngine::closure_stats(std::vector<float>* out) {
+  out->clear();
+  for (auto& kv : groups_) {
+    Group& g = kv.second;
+    const int count = (int)g.consistent.size();
+    if (count == 0) continue;
+    if (!lc_check_ || g.n == 0 || !g.adj.get()) {
+      out->insert(out->end(), (size_t)count * 3, 0.f);
+      continue;
+    }
+    std::vector<uint32_t> mask((size_t)g.words, 0u);
+    for (int32_t i : g.consistent) mask[(size_t)i >> 5] |= 1u << (i & 31);
+    int members = 0;
+    for (uint32_t w : mask) members += __builtin_popcount(w);
+    DeviceBuffer<uint32_t> dmask;
+    DeviceBuffer<int32_t> drows, ddeg((size_t)count), dsup((size_t)count);
+    dmask.upload(mask, st_);
+    drows.upload(g.consistent, st_);
+    launch_row_stats(g.n, g.adj.get(), g.words, dmask.get(), drows.get(), count, ddeg.get(), dsup.get(), st_);
+    std::vector<int32_t> deg((size_t)count), sup((size_t)count);
+    ddeg.download(deg.data(), deg.size(), st_);
+    dsup.download(sup.data(), sup.size(), st_);
+    RPGO_CUDA(cudaStreamSynchronize(st_));
+    for (int k = 0; k < count; ++k) {
+      out->push_back((float)deg[k] / (float)std::max(1, g.n - 1));
+      out->push_back((float)std::log1p((double)deg[k]));
+      out->push_back((float)sup[k] / (float)std::max(1, members - 1));
+    }
+  }
 }
 
 bool PcmEngine::adjacency(int gi, std::vector<uint32_t>* words, int* n) const {

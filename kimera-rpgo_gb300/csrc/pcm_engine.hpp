@@ -67,6 +67,11 @@ class PcmEngine {
   // adjacency of the g-th group in visiting order (host copy, n x words)
   bool adjacency(int g, std::vector<uint32_t>* words, int* n) const;
   const PcmStats& stats() const { return stats_; }
+  // For each loop closure of the last graph to optimise (its order): degree
+  // in its group's adjacency / (group size - 1), log1p(degree), and the
+  // number of its neighbours among the group's consistent set / (set size -
+  // 1); zeros where the pairwise check is disabled. 3 floats per closure.
+  void closure_stats(std::vector<float>* out);
 
  private:
   struct Group {

@@ -59,6 +59,9 @@ class Timing(C.Structure):
         ("warm_runs", C.c_int64), ("warm_fallbacks", C.c_int64)]
 
 
+MLP_FEATURES, MLP_PARAMS = 16, 5345
+
+
 class BatchOut(C.Structure):
     _fields_ = [("poses", C.c_void_p), ("gnc_weights", C.c_void_p), ("num_weights", C.c_void_p),
                 ("status", C.c_void_p), ("timing", C.c_void_p)]
@@ -91,6 +94,11 @@ SIGNATURES = {
     "rpgo_get_adjacency": (C.c_int, [_P, C.c_int32, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "rpgo_get_timing": (C.c_int, [_P, C.POINTER(Timing)]),
     "rpgo_set_warm_start_probs": (C.c_int, [_P, _P, C.c_int64]),
+    "rpgo_set_warm_start_model": (C.c_int, [_P, _P]),
+    "rpgo_get_closure_features": (C.c_int, [_P, _P, C.c_int64, C.POINTER(C.c_int64)]),
+    "rpgo_mlp_forward_dev": (C.c_int, [_P, C.c_int64, _P, _P, _P]),
+    "rpgo_mlp_train_step_dev": (C.c_int, [_P, _P, _P, C.c_int64, C.c_float, C.c_int64, _P, _P, _P,
+                                          C.POINTER(C.c_double), _P]),
     "rpgo_solve_batch": (C.c_int, [C.POINTER(Params), C.c_int32, _P, _P, C.c_int32, C.c_int32,
                                    C.POINTER(BatchOut)]),
     "rpgo_save_data": (C.c_int, [_P, C.c_char_p]),
@@ -271,6 +279,25 @@ class RobustSolver:
         return load().rpgo_save_data(self.h, folder.encode())
 
     # ---- GNC warm start (no counterpart in the reference)
+    def set_warm_start_model(self, params) -> int:
+        """Install a closure network (MLP_PARAMS floats) for the warm start;
+        None removes it."""
+        if params is None:
+            return load().rpgo_set_warm_start_model(self.h, None)
+        self._model = np.ascontiguousarray(params, dtype=np.float32)
+        assert self._model.size == MLP_PARAMS
+        return load().rpgo_set_warm_start_model(self.h, _ptr(self._model))
+
+    def closure_features(self):
+        """Features of the closures of the last warm-mode GNC solve (rows of
+        MLP_FEATURES floats, graph order)."""
+        n = C.c_int64(0)
+        load().rpgo_get_closure_features(self.h, None, 0, C.byref(n))
+        out = np.zeros((n.value, MLP_FEATURES), dtype=np.float32)
+        if n.value:
+            load().rpgo_get_closure_features(self.h, _ptr(out), n.value, C.byref(n))
+        return out
+
     def set_warm_start_probs(self, probs) -> int:
         """Inlier probabilities for the next warm-started GNC solve, one per
         factor of the graph it optimises (known inliers are ignored)."""

@@ -139,7 +139,13 @@ def _pick_pairs(rng, pos, radius, count, min_gap=2):
 
 
 def walk3d(n_poses=5000, n_inliers=1000, n_outliers=333, seed=2, step=0.5, rot_sigma=0.1, sigma_t=0.02,
-           sigma_r=0.005, radius=3.0, prefix="a", prior_var=1e-4):
+           sigma_r=0.005, radius=3.0, prefix="a", prior_var=1e-4, clustered_outliers=0, cluster=10):
+    """3D random walk. n_outliers closures join uniformly random pose pairs
+    with a random measurement; clustered_outliers more come in groups of
+    `cluster` that all claim the same wrong place: for a random pose pair
+    (a0, b0) and a random rigid offset W, closure k joins a0 + k and b0 + k
+    with the measurement of gt[b0 + k] moved by W (mutually consistent,
+    inconsistent with the trajectory)."""
     rng = np.random.default_rng(seed)
     sig = np.array([sigma_r] * 3 + [sigma_t] * 3)
     noise = diagonal_sigmas(sig)
@@ -177,6 +183,19 @@ def walk3d(n_poses=5000, n_inliers=1000, n_outliers=333, seed=2, step=0.5, rot_s
         z[:3, :3] = uniform_rotation(rng)
         z[:3, 3] = rng.uniform(-10, 10, 3)
         lcs.append((int(a), int(b), z, True))
+    for _ in range(0, clustered_outliers, cluster):
+        while True:
+            a0, b0 = (int(x) for x in rng.integers(0, max(n_poses - cluster, 1), 2))
+            if abs(a0 - b0) >= cluster + 2:
+                break
+        W = np.eye(4)
+        W[:3, :3] = uniform_rotation(rng)
+        W[:3, 3] = rng.uniform(-10, 10, 3)
+        made = len(lcs) - len(pairs) - n_outliers
+        for c in range(min(cluster, clustered_outliers - made)):
+            a, b = a0 + c, b0 + c
+            z = np.linalg.inv(gt[a]) @ W @ gt[b] @ se3_exp(rng.normal(0, 1, 6) * sig)
+            lcs.append((a, b, z, True))
     order = rng.permutation(len(lcs))
     out = []
     for o in order:
@@ -267,6 +286,15 @@ def config_c4(n_graphs=512, seed=4):
     """Batched workload: independent 3D random walks of the walk3d generator
     with the sizes of config_c4_sizes."""
     return [walk3d(n, ni, no, seed=s) for n, ni, no, s in config_c4_sizes(n_graphs, seed)]
+
+
+def config_c5(seed=5, n_poses=20000, n_closures=8000, outlier_frac=0.4):
+    """Warm-start evaluation graph: 3D random walk of 20,000 poses, 40 %
+    outliers, half uniform and half in clusters of 10 mapping to the same
+    wrong place."""
+    n_out = int(round(outlier_frac * n_closures))
+    n_clu = n_out // 2 // 10 * 10
+    return walk3d(n_poses, n_closures - n_out, n_out - n_clu, seed=seed, clustered_outliers=n_clu)
 
 
 def ate(est_poses: np.ndarray, ref_poses: np.ndarray, dim: int = 3) -> float:

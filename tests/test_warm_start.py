@@ -115,3 +115,53 @@ def _empty():
     from rpgo_gb300.graph import Graph
 
     return Graph(3)
+
+
+# ------------------------------------------------------------------ the trained network
+@pytest.mark.gpu
+@pytest.mark.parametrize("pcm_off", [False, True])
+def test_trained_network_gain(pcm_off):
+    """The shipped network against the method without it, on a held-out
+    graph (seed outside the training and evaluation seeds): plain GNC, and
+    the warm schedule started from 'every closure is an inlier'."""
+    from rpgo_gb300 import build, capi, warmstart
+
+    build()
+    model = warmstart.load_model()
+    s = synth.walk3d(800, 120, 40, seed=77, clustered_outliers=40)
+    plain = capi.RobustSolver(_params(False, pcm_off))
+    assert plain.update(s.graph) == 0
+    wp, tp = plain.gnc_weights(), plain.timing()
+    warm = capi.RobustSolver(_params(True, pcm_off))
+    assert warm.set_warm_start_model(model) == 0
+    assert warm.update(s.graph) == 0
+    ww, tw = warm.gnc_weights(), warm.timing()
+    c = plain.counts()
+    nk = c.num_odom + c.num_special
+    agree = float(np.mean(np.round(ww[nk:]) == np.round(wp[nk:])))
+    print(f"pcm_off={pcm_off}: plain {tp.linear_solves} solves / {tp.gnc_iterations} GNC iterations, "
+          f"warm {tw.linear_solves} / {tw.gnc_iterations}, fallbacks {tw.warm_fallbacks}, agreement {agree:.4f}")
+    assert tw.warm_runs == 1 and tw.warm_fallbacks == 0
+    assert tw.linear_solves * 3 < tp.linear_solves
+    assert agree >= 0.85
+    # every closure that plain GNC keeps is kept or rejected near the threshold; no closure that
+    # plain GNC rejects as a gross outlier (true outlier) is kept by the warm start
+    truth = _truth(s, plain)
+    assert not np.any((np.round(ww[nk:]) == 1) & truth[nk:] & (np.round(wp[nk:]) == 0))
+    # without the network: the same schedule from all-ones probabilities
+    ones = capi.RobustSolver(_params(True, pcm_off))
+    assert ones.update(s.graph, optimize_graph=False) == 0
+    assert ones.set_warm_start_probs(np.ones(ones.counts().num_factors)) == 0
+    assert ones.forceUpdate(_empty()) == 0
+    to = ones.timing()
+    print(f"  all-ones start: {to.linear_solves} solves, fallbacks {to.warm_fallbacks}")
+    assert tw.linear_solves <= to.linear_solves
+
+
+def _truth(s, solver):
+    """Per factor of the solver's graph: True for a generated outlier."""
+    a = s.graph.arrays()
+    off = s.n_odom + 1
+    bad = {(int(a["key1"][off + q]), int(a["key2"][off + q])): bool(s.is_outlier[q]) for q in range(s.n_lc)}
+    _, k1, k2, _ = solver.factors()
+    return np.array([bad.get((int(x), int(y)), False) for x, y in zip(k1, k2)])
