@@ -264,6 +264,21 @@ int rpgo_mlp_train_step_dev(float* params, float* adam_m, float* adam_v, int64_t
  * gnc_weights.csv in `folder`. */
 int rpgo_save_data(const rpgo_solver* s, const char* folder);
 
+/* ---------------------------------------------------------------------- g2o
+ * Native reader of the g2o format of Kimera-RPGO's fixtures and results
+ * (GTSAM readG2o / load3D / load2D semantics, as examples/RpgoReadG2o.cpp:
+ * 129-143 use them): VERTEX_SE3:QUAT / EDGE_SE3:QUAT (dim 3; quaternions
+ * normalised, the information reordered from g2o's [t; R] to [R; t]) or
+ * VERTEX_SE2 / EDGE_SE2 (dim 2); noise models as
+ * noiseModel::Gaussian::Information(I, smart = true). rpgo_g2o_view points
+ * batches into the reader's arrays (valid until rpgo_g2o_free); they can be
+ * passed to rpgo_update as they are. The writer is rpgo_save_data
+ * (src/Logger.cpp:64-164 writeG2o). */
+typedef struct rpgo_g2o rpgo_g2o; /* opaque */
+rpgo_g2o* rpgo_g2o_read(const char* path, int32_t dim, int32_t* status);
+int rpgo_g2o_view(const rpgo_g2o* g, rpgo_factor_batch* factors, rpgo_value_batch* values);
+void rpgo_g2o_free(rpgo_g2o* g);
+
 /* ------------------------------------------------------------------ batches
  * Many independent graphs (Monte-Carlo trials, submaps) solved in one call.
  * No counterpart in the reference, whose RobustSolver solves one graph per

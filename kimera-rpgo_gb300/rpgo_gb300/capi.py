@@ -99,6 +99,9 @@ SIGNATURES = {
     "rpgo_mlp_forward_dev": (C.c_int, [_P, C.c_int64, _P, _P, _P]),
     "rpgo_mlp_train_step_dev": (C.c_int, [_P, _P, _P, C.c_int64, C.c_float, C.c_int64, _P, _P, _P,
                                           C.POINTER(C.c_double), _P]),
+    "rpgo_g2o_read": (_P, [C.c_char_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "rpgo_g2o_view": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch)]),
+    "rpgo_g2o_free": (None, [_P]),
     "rpgo_solve_batch": (C.c_int, [C.POINTER(Params), C.c_int32, _P, _P, C.c_int32, C.c_int32,
                                    C.POINTER(BatchOut)]),
     "rpgo_save_data": (C.c_int, [_P, C.c_char_p]),
@@ -306,6 +309,42 @@ class RobustSolver:
 
 
 # ------------------------------------------------------------------ stage functions (host arrays)
+def read_g2o(path: str, dim: int = 3):
+    """rpgo_g2o_read: the graph of a g2o file (factors in file order, then
+    the vertices as values), as a Graph."""
+    from .graph import Graph
+
+    lib = load()
+    st = C.c_int32(0)
+    h = lib.rpgo_g2o_read(path.encode(), int(dim), C.byref(st))
+    if not h:
+        raise RpgoError(f"rpgo_g2o_read({path}): {st.value}")
+    try:
+        f, v = FactorBatch(), ValueBatch()
+        lib.rpgo_g2o_view(h, C.byref(f), C.byref(v))
+        stride, d = (12, 6) if dim == 3 else (4, 3)
+        n, m = int(f.count), int(v.count)
+
+        def arr(ptr, ctype, count):
+            if count == 0:
+                return np.zeros(0)
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ctype)), shape=(count,)).copy()
+
+        g = Graph(dim)
+        g.kind = [int(x) for x in arr(f.kind, C.c_int32, n)]
+        g.key1 = [int(x) for x in arr(f.key_front, C.c_uint64, n)]
+        g.key2 = [int(x) for x in arr(f.key_back, C.c_uint64, n)]
+        meas = arr(f.measured, C.c_double, n * stride).reshape(n, stride)
+        cov = arr(f.covariance, C.c_double, n * d * d).reshape(n, d, d)
+        sq = arr(f.sqrt_information, C.c_double, n * d * d).reshape(n, d, d)
+        g.measured, g.cov, g.sqrt_info = list(meas), list(cov), list(sq)
+        g.value_keys = [int(x) for x in arr(v.key, C.c_uint64, m)]
+        g.value_poses = list(arr(v.pose, C.c_double, m * stride).reshape(m, stride))
+        return g
+    finally:
+        lib.rpgo_g2o_free(h)
+
+
 def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0):
     """rpgo_solve_batch: solve independent graphs concurrently. Returns a
     list of (status, keys, poses, gnc_weights, timing) per graph, the poses in
