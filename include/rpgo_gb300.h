@@ -216,6 +216,26 @@ int rpgo_get_factors(const rpgo_solver* s, int32_t* kind, uint64_t* key_front, u
  * pairwise consistent. Returns the group size in *n. */
 int rpgo_get_adjacency(const rpgo_solver* s, int32_t group, uint32_t* words, int64_t capacity, int64_t* n);
 int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* out);
+/* ---- edit API (src/RobustSolver.cpp:371-446, Pcm.h:299-408). Each edit
+ * then re-optimises like the reference (removePriorFactorsWithPrefix only when
+ * optimize_graph != 0); values are not changed by the edit itself. */
+/* removeLastLoopClosure(prefix_1, prefix_2) when by_id != 0, else
+ * removeLastLoopClosure(): *removed = 0 where the reference returns NULL
+ * (unknown group, no closure left); the removed closure's keys otherwise.
+ * Without outlier rejection the last factor of the graph is removed
+ * (GenericSolver::removeLastFactor). */
+int rpgo_remove_last_loop_closure(rpgo_solver* s, int32_t by_id, char prefix_1, char prefix_2, uint64_t* key_front,
+                                  uint64_t* key_back, int32_t* removed);
+/* ignorePrefix / revivePrefix: closures of groups involving the prefix leave
+ * / rejoin the graph (no-op with a warning without outlier rejection). */
+int rpgo_ignore_prefix(rpgo_solver* s, char prefix);
+int rpgo_revive_prefix(rpgo_solver* s, char prefix);
+/* getIgnoredPrefixes(): *n prefixes in the order they were ignored; out may
+ * be NULL to query *n. */
+int rpgo_get_ignored_prefixes(const rpgo_solver* s, char* out, int32_t capacity, int32_t* n);
+/* removePriorFactorsWithPrefix(prefix, optimize_graph) */
+int rpgo_remove_prior_factors_with_prefix(rpgo_solver* s, char prefix, int32_t optimize_graph);
+
 /* GNC warm start (no counterpart in the reference): inlier probabilities for
  * the factors of the next GNC solve, in the order of the graph it optimises
  * (rpgo_get_factors after the update; odometry and priors first, their

@@ -607,6 +607,90 @@ int rpgo_set_warm_start_probs(rpgo_solver* s, const double* probs, int64_t n) {
   s->warm_probs.assign(probs, probs + n);
   return RPGO_OK;
 }
+// ---- edit API (src/RobustSolver.cpp:371-446)
+static int edit_optimize(rpgo_solver* s) {
+  for (const auto& f : s->nfg)
+    if (!s->values->has(f.k1) || !s->values->has(f.k2)) return RPGO_ERR_KEY;
+  return optimize(s);
+}
+
+int rpgo_remove_last_loop_closure(rpgo_solver* s, int32_t by_id, char prefix_1, char prefix_2, uint64_t* key_front,
+                                  uint64_t* key_back, int32_t* removed) {
+  if (!s || !removed) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
+  return guarded([&] {
+    uint64_t a = 0, b = 0;
+    bool ok;
+    if (s->pcm) {
+      ok = by_id ? s->pcm->remove_last_loop_closure(prefix_1, prefix_2, &a, &b, &s->nfg)
+                 : s->pcm->remove_last_loop_closure(&a, &b, &s->nfg);
+    } else {
+      // GenericSolver::removeLastFactor (src/GenericSolver.cpp:122-128);
+      // an empty graph removes nothing (the reference indexes it)
+      ok = !s->nfg.empty();
+      if (ok) {
+        a = s->nfg.back().k1;
+        b = s->nfg.back().k2;
+        s->nfg.pop_back();
+      }
+    }
+    *removed = ok ? 1 : 0;
+    if (key_front) *key_front = a;
+    if (key_back) *key_back = b;
+    return edit_optimize(s);
+  });
+}
+
+int rpgo_ignore_prefix(rpgo_solver* s, char prefix) {
+  if (!s) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
+  return guarded([&] {
+    if (s->pcm) s->pcm->ignore_prefix(prefix, &s->nfg);
+    else if (s->p.verbosity != RPGO_VERBOSITY_QUIET)
+      std::fprintf(stderr, "rpgo_gb300: 'ignorePrefix' currently not implemented for no outlier rejection case\n");
+    return edit_optimize(s);
+  });
+}
+
+int rpgo_revive_prefix(rpgo_solver* s, char prefix) {
+  if (!s) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
+  return guarded([&] {
+    if (s->pcm) s->pcm->revive_prefix(prefix, &s->nfg);
+    else if (s->p.verbosity != RPGO_VERBOSITY_QUIET)
+      std::fprintf(stderr, "rpgo_gb300: 'revivePrefix' currently not implemented for no outlier rejection case\n");
+    return edit_optimize(s);
+  });
+}
+
+int rpgo_get_ignored_prefixes(const rpgo_solver* s, char* out, int32_t cap, int32_t* n) {
+  if (!s || !n) return RPGO_ERR_ARG;
+  static const std::vector<char> none;
+  const std::vector<char>& v = s->pcm ? s->pcm->ignored_prefixes() : none;
+  *n = (int32_t)v.size();
+  if (!out) return RPGO_OK;
+  if ((int32_t)v.size() > cap) return RPGO_ERR_ARG;
+  for (size_t i = 0; i < v.size(); ++i) out[i] = v[i];
+  return RPGO_OK;
+}
+
+int rpgo_remove_prior_factors_with_prefix(rpgo_solver* s, char prefix, int32_t optimize_graph) {
+  if (!s) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
+  return guarded([&] {
+    if (s->pcm) {
+      s->pcm->remove_priors_with_prefix(prefix, &s->nfg);
+    } else {
+      // GenericSolver::removePriorsWithPrefix (src/GenericSolver.cpp:130-160)
+      std::vector<FactorRec> kept;
+      for (const auto& f : s->nfg)
+        if (f.kind != RPGO_FACTOR_PRIOR || key_chr(f.k1) != prefix) kept.push_back(f);
+      s->nfg.swap(kept);
+    }
+    return optimize_graph ? edit_optimize(s) : (int)RPGO_OK;
+  });
+}
+
 int rpgo_set_warm_start_model(rpgo_solver* s, const float* params) {
   if (!s) return RPGO_ERR_ARG;
   if (!params) {

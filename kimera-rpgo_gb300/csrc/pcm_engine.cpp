@@ -133,6 +133,7 @@ void PcmEngine::run_pairwise(Group& g, int old_n, const FactorStore& store) {
                   view(), th0, th1, g.adj.get(), g.words, lower_scratch_.get(), st_);
   stats_.pair_checks += (int64_t)n * (n - 1) / 2 - (int64_t)old_n * (old_n - 1) / 2;
   g.n = n;
+  g.adj_rows = n;
 }
 
 // Pcm.h:851-899
@@ -144,8 +145,12 @@ void PcmEngine::find_inliers() {
     if (lc_check_) {
       std::vector<int32_t> clique;
       const int sz = max_clique_heu(g.n, g.adj.get(), g.words, 0, -1, &clique, clique_ws_, st_);
-      g.consistent.assign(clique.begin(), clique.begin() + std::max(sz, 0));
-      num = (size_t)std::max(sz, 0);
+      // after a removal that left fewer than two closures the reference keeps
+      // its larger adjacency; indices past the closures are dropped
+      g.consistent.clear();
+      for (int i = 0; i < sz; ++i)
+        if (clique[i] < (int32_t)g.factors.size()) g.consistent.push_back(clique[i]);
+      num = g.consistent.size();
     } else {
       g.consistent.resize(g.factors.size());
       for (size_t i = 0; i < g.factors.size(); ++i) g.consistent[i] = (int32_t)i;
@@ -175,7 +180,11 @@ void PcmEngine::find_inliers_incremental(const std::unordered_map<ObsId, size_t,
         clique.assign(1, 0);
       }
     }
-    if (sz > prev) g.consistent.assign(clique.begin(), clique.begin() + sz);
+    if (sz > prev) {
+      g.consistent.clear();
+      for (int i = 0; i < sz; ++i)
+        if (clique[i] < (int32_t)g.factors.size()) g.consistent.push_back(clique[i]);
+    }
   }
   for (const auto& kv : groups_) total_good_lc_ += kv.second.consistent.size();
 }
@@ -282,6 +291,7 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
       g.h_sb.push_back(slot(f.k2));
       g.h_flip.push_back(key_chr(f.k1) != g.key.id1 ? 1 : 0);
       g.h_row.push_back(f.row);
+      lc_in_order_.push_back(id);
       ++total_lc_;
     }
     if (lc_check_) {
@@ -300,13 +310,101 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
     else find_inliers();
     do_optimize = true;
   }
-  // ---- buildGraphToOptimize (Pcm.h:977-1005)
+  build_graph(out);
+  return do_optimize;
+}
+
+void PcmEngine::build_graph(std::vector<FactorRec>* out) const {
   out->clear();
   out->insert(out->end(), nfg_odom_.begin(), nfg_odom_.end());
   out->insert(out->end(), nfg_special_.begin(), nfg_special_.end());
-  for (const auto& kv : groups_)
+  auto ignored = [this](char c) { return std::find(ignored_.begin(), ignored_.end(), c) != ignored_.end(); };
+  for (const auto& kv : groups_) {
+    if (ignored(kv.first.id1) || ignored(kv.first.id2)) continue;
     for (int32_t idx : kv.second.consistent) out->push_back(kv.second.factors[idx]);
-  return do_optimize;
+  }
+}
+
+void PcmEngine::clique_of(Group& g, int rows) {
+  g.consistent.clear();
+  std::vector<int32_t> clique;
+  int sz = 0;
+  if (lc_check_ && rows > 0 && g.adj.get()) {
+    sz = max_clique_heu(rows, g.adj.get(), g.words, 0, -1, &clique, clique_ws_, st_);
+  } else if (rows > 0) {
+    // the greedy clique of an edgeless graph is its first vertex
+    sz = 1;
+    clique.assign(1, 0);
+  }
+  for (int i = 0; i < sz; ++i)
+    if (clique[i] < (int32_t)g.factors.size()) g.consistent.push_back(clique[i]);
+}
+
+// Pcm.h:299-342. Deviation: a group whose closures are all gone returns
+// false (the reference would index its empty factor list).
+bool PcmEngine::remove_last(const ObsId& id, uint64_t* k1, uint64_t* k2, std::vector<FactorRec>* out) {
+  auto it = groups_.find(id);
+  if (it == groups_.end()) return false;
+  Group& g = it->second;
+  const int num_lc = g.adj_rows;
+  if (num_lc <= 0 || g.factors.empty()) return false;
+  *k1 = g.factors.back().k1;
+  *k2 = g.factors.back().k2;
+  g.factors.pop_back();
+  g.h_sa.pop_back();
+  g.h_sb.pop_back();
+  g.h_flip.pop_back();
+  g.h_row.pop_back();
+  if (g.factors.size() < 2) {
+    g.consistent.clear();
+    for (size_t i = 0; i < g.factors.size(); ++i) g.consistent.push_back((int32_t)i);
+  } else {
+    // adj_matrix.block(0, 0, numLC - 1, numLC - 1): the removed closure's
+    // column is cleared so that the degrees of the kept rows are exact
+    const int m = num_lc - 1;
+    if (g.adj.get() && g.n > m) {
+      launch_clear_columns(g.adj.get(), g.words, m, m, st_);
+      g.n = m;
+    }
+    g.adj_rows = m;
+    clique_of(g, m);
+  }
+  build_graph(out);
+  return true;
+}
+
+bool PcmEngine::remove_last_loop_closure(char prefix_1, char prefix_2, uint64_t* k1, uint64_t* k2,
+                                         std::vector<FactorRec>* out) {
+  return remove_last(ObsId{prefix_1, prefix_2}, k1, k2, out);
+}
+
+// Pcm.h:347-353
+bool PcmEngine::remove_last_loop_closure(uint64_t* k1, uint64_t* k2, std::vector<FactorRec>* out) {
+  if (lc_in_order_.empty()) return false;
+  const ObsId id = lc_in_order_.back();
+  lc_in_order_.pop_back();
+  return remove_last(id, k1, k2, out);
+}
+
+// Pcm.h:357-365
+void PcmEngine::ignore_prefix(char prefix, std::vector<FactorRec>* out) {
+  if (std::find(ignored_.begin(), ignored_.end(), prefix) == ignored_.end()) ignored_.push_back(prefix);
+  build_graph(out);
+}
+
+// Pcm.h:369-376
+void PcmEngine::revive_prefix(char prefix, std::vector<FactorRec>* out) {
+  ignored_.erase(std::remove(ignored_.begin(), ignored_.end(), prefix), ignored_.end());
+  build_graph(out);
+}
+
+// Pcm.h:386-408: priors of keys with this prefix leave the special factors
+void PcmEngine::remove_priors_with_prefix(char prefix, std::vector<FactorRec>* out) {
+  std::vector<FactorRec> kept;
+  for (const auto& f : nfg_special_)
+    if (f.kind != 1 || key_chr(f.k1) != prefix) kept.push_back(f);
+  nfg_special_.swap(kept);
+  build_graph(out);
 }
 
 void PcmEngine::closure_stats(std::vector<float>* out) {

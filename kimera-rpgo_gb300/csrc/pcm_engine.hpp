@@ -73,11 +73,26 @@ class PcmEngine {
   // 1); zeros where the pairwise check is disabled. 3 floats per closure.
   void closure_stats(std::vector<float>* out);
 
+  // ---- edits (Pcm.h:299-408); each leaves the graph to optimise in *out
+  // removeLastLoopClosure(ObservationId): false when the group is unknown or
+  // has no closure left; the removed closure's keys in *k1, *k2
+  bool remove_last_loop_closure(char prefix_1, char prefix_2, uint64_t* k1, uint64_t* k2,
+                                std::vector<FactorRec>* out);
+  // removeLastLoopClosure(): the group of the latest accepted closure
+  bool remove_last_loop_closure(uint64_t* k1, uint64_t* k2, std::vector<FactorRec>* out);
+  void ignore_prefix(char prefix, std::vector<FactorRec>* out);
+  void revive_prefix(char prefix, std::vector<FactorRec>* out);
+  const std::vector<char>& ignored_prefixes() const { return ignored_; }
+  void remove_priors_with_prefix(char prefix, std::vector<FactorRec>* out);
+
  private:
   struct Group {
     std::vector<FactorRec> factors;
     std::vector<int32_t> consistent;  // indices into factors (clique buffer order, duplicates kept)
     int n = 0, words = 0, row_cap = 0;
+    // rows of the reference's adj_matrix: 1 for a fresh Measurements
+    // (TypeUtils.h:16-33), n after each increment, one less per removal
+    int adj_rows = 1;
     DeviceBuffer<uint32_t> adj;  // row_cap x words
     std::vector<int32_t> h_sa, h_sb;
     std::vector<uint8_t> h_flip;
@@ -94,6 +109,12 @@ class PcmEngine {
   void run_pairwise(Group& g, int old_n, const FactorStore& store);
   void find_inliers();
   void find_inliers_incremental(const std::unordered_map<ObsId, size_t, ObsIdHash>& num_new);
+  // Pcm::buildGraphToOptimize (Pcm.h:977-1005), ignored prefixes left out
+  void build_graph(std::vector<FactorRec>* out) const;
+  bool remove_last(const ObsId& id, uint64_t* k1, uint64_t* k2, std::vector<FactorRec>* out);
+  // clique of the first `rows` closures of a group (indices past the
+  // group's closures dropped)
+  void clique_of(Group& g, int rows);
 
   PcmConfig cfg_;
   bool odom_check_ = true, lc_check_ = true;
@@ -111,6 +132,8 @@ class PcmEngine {
   std::unordered_set<char> prefix_exists_;
   std::vector<FactorRec> nfg_odom_, nfg_special_;
   std::unordered_map<ObsId, Group, ObsIdHash> groups_;
+  std::vector<ObsId> lc_in_order_;  // loop_closures_in_order_ (Pcm.h:112)
+  std::vector<char> ignored_;       // ignored_prefixes_ (Pcm.h:117)
   size_t total_lc_ = 0, total_good_lc_ = 0;
   // scratch
   DeviceBuffer<int32_t> d_src_, d_dst_;

@@ -544,6 +544,27 @@ void launch_pairwise(int dim, int mode, int n, int row_begin, const int32_t* sa,
   RPGO_LAUNCHED();
 }
 
+namespace {
+// rows [0, rows): clear every bit of columns >= from
+__global__ void k_clear_columns(uint32_t* __restrict__ adj, int words, int rows, int from) {
+  const int w0 = from >> 5;
+  const int per_row = words - w0;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (per_row <= 0 || t >= (int64_t)rows * per_row) return;
+  const int r = (int)(t / per_row), w = w0 + (int)(t % per_row);
+  uint32_t* word = adj + (size_t)r * words + w;
+  *word = (w == w0) ? (*word & ((1u << (from & 31)) - 1u)) : 0u;
+}
+}  // namespace
+
+void launch_clear_columns(uint32_t* adj, int words, int rows, int from, cudaStream_t st) {
+  const int per_row = words - (from >> 5);
+  if (rows <= 0 || per_row <= 0) return;
+  const int64_t n = (int64_t)rows * per_row;
+  k_clear_columns<<<div_up(n, 256), 256, 0, st>>>(adj, words, rows, from);
+  RPGO_LAUNCHED();
+}
+
 std::atomic<int64_t>& launch_counter() {
   static std::atomic<int64_t> c{0};
   return c;

@@ -26,6 +26,9 @@ void launch_odom_check(int dim, int mode, int64_t count, const int32_t* si, cons
                        const double* zc, TrajView tr, double th0, double th1, uint8_t* ok, cudaStream_t st);
 
 // adj: n rows of `words` uint32; lower_scratch: (n - row_begin) rows of `words`
+// rows [0, rows) of a bit-packed adjacency (row stride `words`): clear the
+// bits of every column >= from
+void launch_clear_columns(uint32_t* adj, int words, int rows, int from, cudaStream_t st);
 void launch_pairwise(int dim, int mode, int n, int row_begin, const int32_t* sa, const int32_t* sb,
                      const uint8_t* flip, const double* zp, const double* zc, TrajView tr, double th0, double th1,
                      uint32_t* adj, int words, uint32_t* lower_scratch, cudaStream_t st);

@@ -94,6 +94,12 @@ SIGNATURES = {
     "rpgo_get_adjacency": (C.c_int, [_P, C.c_int32, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "rpgo_get_timing": (C.c_int, [_P, C.POINTER(Timing)]),
     "rpgo_set_warm_start_probs": (C.c_int, [_P, _P, C.c_int64]),
+    "rpgo_remove_last_loop_closure": (C.c_int, [_P, C.c_int32, C.c_char, C.c_char, C.POINTER(C.c_uint64),
+                                                C.POINTER(C.c_uint64), C.POINTER(C.c_int32)]),
+    "rpgo_ignore_prefix": (C.c_int, [_P, C.c_char]),
+    "rpgo_revive_prefix": (C.c_int, [_P, C.c_char]),
+    "rpgo_get_ignored_prefixes": (C.c_int, [_P, C.c_char_p, C.c_int32, C.POINTER(C.c_int32)]),
+    "rpgo_remove_prior_factors_with_prefix": (C.c_int, [_P, C.c_char, C.c_int32]),
     "rpgo_set_warm_start_model": (C.c_int, [_P, _P]),
     "rpgo_get_closure_features": (C.c_int, [_P, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "rpgo_mlp_forward_dev": (C.c_int, [_P, C.c_int64, _P, _P, _P]),
@@ -280,6 +286,34 @@ class RobustSolver:
 
     def saveData(self, folder: str) -> int:
         return load().rpgo_save_data(self.h, folder.encode())
+
+    # ---- edit API (src/RobustSolver.cpp:371-446)
+    def removeLastLoopClosure(self, prefix_1=None, prefix_2=None):
+        """Returns (from_key, to_key) of the removed closure, or None."""
+        a, b, r = C.c_uint64(), C.c_uint64(), C.c_int32()
+        by_id = prefix_1 is not None
+        p1 = (prefix_1 or "\0").encode()
+        p2 = (prefix_2 or "\0").encode()
+        rc = load().rpgo_remove_last_loop_closure(self.h, int(by_id), p1, p2, C.byref(a), C.byref(b), C.byref(r))
+        if rc:
+            raise RpgoError(f"rpgo_remove_last_loop_closure: {rc}")
+        return (a.value, b.value) if r.value else None
+
+    def ignorePrefix(self, prefix: str) -> int:
+        return load().rpgo_ignore_prefix(self.h, prefix.encode())
+
+    def revivePrefix(self, prefix: str) -> int:
+        return load().rpgo_revive_prefix(self.h, prefix.encode())
+
+    def getIgnoredPrefixes(self):
+        n = C.c_int32()
+        load().rpgo_get_ignored_prefixes(self.h, None, 0, C.byref(n))
+        buf = C.create_string_buffer(max(n.value, 1))
+        load().rpgo_get_ignored_prefixes(self.h, buf, n.value, C.byref(n))
+        return [chr(c) for c in buf.raw[:n.value]]
+
+    def removePriorFactorsWithPrefix(self, prefix: str, optimize_graph: bool = True) -> int:
+        return load().rpgo_remove_prior_factors_with_prefix(self.h, prefix.encode(), int(optimize_graph))
 
     # ---- GNC warm start (no counterpart in the reference)
     def set_warm_start_model(self, params) -> int:

@@ -35,6 +35,11 @@ struct SolverBase {
   virtual void stats(int64_t* lm_iters, int64_t* solves, int64_t* gnc_iters) const = 0;
   virtual void set_warm_probs(const double* p, int64_t n) = 0;
   virtual int force_optimize() = 0;
+  // edit API (src/RobustSolver.cpp:371-446)
+  virtual int remove_last_loop_closure(int by_id, char p1, char p2, uint64_t* k1, uint64_t* k2, int* removed) = 0;
+  virtual int ignore_prefix(char c, bool revive) = 0;
+  virtual int ignored_prefixes(char* out, int cap) const = 0;
+  virtual int remove_priors_with_prefix(char c, int optimize_graph) = 0;
   int64_t warm_runs = 0, warm_fallbacks = 0;
   // wall-clock seconds spent in outlier rejection and in the solve (sums)
   double pcm_seconds = 0.0, solve_seconds = 0.0;
@@ -245,6 +250,53 @@ struct RobustSolverO final : SolverBase {
     return RPGO_ERR_ARG;
   }
   void set_warm_probs(const double* pr, int64_t n) override { warm_probs.assign(pr, pr + n); }
+  int optimize_timed() {
+    for (const auto& f : nfg)
+      if (!values.count(f.k1) || !values.count(f.k2)) return RPGO_ERR_KEY;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = optimize();
+    this->solve_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+  }
+  int remove_last_loop_closure(int by_id, char p1, char p2, uint64_t* k1, uint64_t* k2, int* removed) override {
+    bool ok;
+    if (pcm) {
+      ok = by_id ? pcm->remove_last(ObsId{p1, p2}, k1, k2, &nfg) : pcm->remove_last_in_order(k1, k2, &nfg);
+    } else {
+      ok = !nfg.empty();
+      if (ok) {
+        *k1 = nfg.back().k1;
+        *k2 = nfg.back().k2;
+        nfg.pop_back();
+      }
+    }
+    *removed = ok ? 1 : 0;
+    return optimize_timed();
+  }
+  int ignore_prefix(char c, bool revive) override {
+    if (pcm) {
+      if (revive) pcm->revive_prefix(c, &nfg);
+      else pcm->ignore_prefix(c, &nfg);
+    }
+    return optimize_timed();
+  }
+  int ignored_prefixes(char* out, int cap) const override {
+    if (!pcm) return 0;
+    const int n = (int)pcm->ignored.size();
+    for (int i = 0; i < n && i < cap; ++i) out[i] = pcm->ignored[i];
+    return n;
+  }
+  int remove_priors_with_prefix(char c, int optimize_graph) override {
+    if (pcm) {
+      pcm->remove_priors_with_prefix(c, &nfg);
+    } else {
+      std::vector<Factor<L>> kept;
+      for (const auto& f : nfg)
+        if (f.kind != 1 || key_chr(f.k1) != c) kept.push_back(f);
+      nfg.swap(kept);
+    }
+    return optimize_graph ? optimize_timed() : RPGO_OK;
+  }
   // RobustSolver::forceUpdate with no new factors or values: optimize()
   int force_optimize() override {
     const auto t0 = std::chrono::steady_clock::now();
@@ -323,6 +375,16 @@ int oracle_set_warm_probs(void* s, const double* probs, int64_t n) {
   return 0;
 }
 int oracle_force_optimize(void* s) { return static_cast<SolverBase*>(s)->force_optimize(); }
+int oracle_remove_last_loop_closure(void* s, int by_id, char p1, char p2, uint64_t* k1, uint64_t* k2, int* removed) {
+  return static_cast<SolverBase*>(s)->remove_last_loop_closure(by_id, p1, p2, k1, k2, removed);
+}
+int oracle_ignore_prefix(void* s, char c, int revive) { return static_cast<SolverBase*>(s)->ignore_prefix(c, revive); }
+int oracle_ignored_prefixes(void* s, char* out, int cap) {
+  return static_cast<SolverBase*>(s)->ignored_prefixes(out, cap);
+}
+int oracle_remove_priors_with_prefix(void* s, char c, int optimize_graph) {
+  return static_cast<SolverBase*>(s)->remove_priors_with_prefix(c, optimize_graph);
+}
 int oracle_get_warm_stats(void* s, int64_t* runs, int64_t* fallbacks) {
   *runs = static_cast<SolverBase*>(s)->warm_runs;
   *fallbacks = static_cast<SolverBase*>(s)->warm_fallbacks;

@@ -316,6 +316,7 @@ struct Group {
   std::vector<Factor<L>> factors;
   std::vector<Factor<L>> consistent;
   int n = 0, words = 0;
+  int adj_rows = 1;  // rows of adj_matrix: 1 for a fresh Measurements (TypeUtils.h:16-33)
   std::vector<uint32_t> bits;  // n x words, symmetric
   void grow(int new_n) {
     const int nw = (new_n + 31) / 32;
@@ -329,6 +330,17 @@ struct Group {
   void set(int i, int j) {
     bits[(size_t)i * words + (j >> 5)] |= 1u << (j & 31);
     bits[(size_t)j * words + (i >> 5)] |= 1u << (i & 31);
+  }
+  // adj_matrix.block(0, 0, m, m)
+  void shrink(int m) {
+    const int nw = (m + 31) / 32;
+    std::vector<uint32_t> nb((size_t)m * nw, 0u);
+    for (int i = 0; i < m; ++i)
+      for (int j = 0; j < m; ++j)
+        if (bits[(size_t)i * words + (j >> 5)] >> (j & 31) & 1u) nb[(size_t)i * nw + (j >> 5)] |= 1u << (j & 31);
+    bits.swap(nb);
+    n = m;
+    words = nw;
   }
 };
 
@@ -347,6 +359,8 @@ struct Pcm {
   bool odom_check = true, lc_check = true;
   std::vector<Factor<L>> nfg_odom, nfg_special;
   std::unordered_map<ObsId, Group<L>, ObsIdHash> loop_closures;
+  std::vector<ObsId> in_order;   // loop_closures_in_order_ (Pcm.h:112)
+  std::vector<char> ignored;     // ignored_prefixes_ (Pcm.h:117)
   std::unordered_map<char, Trajectory<U>> trajectories;
   size_t total_lc = 0, total_good_lc = 0;
   bool warned_missing = false;
@@ -408,6 +422,7 @@ struct Pcm {
   // Pcm.h:725-768 for every new member of the group against all earlier ones
   void increment_adjacency(Group<L>& g, int old_n) {
     g.grow((int)g.factors.size());
+    g.adj_rows = g.n;
     for (int j = old_n; j < g.n; ++j)
       for (int i = 0; i < j; ++i)
         if (are_loops_consistent(g.factors[i], g.factors[j])) g.set(i, j);
@@ -437,6 +452,7 @@ struct Pcm {
         touched.push_back(id);
       }
       g.factors.push_back(f);
+      in_order.push_back(id);
       ++total_lc;
     }
     if (lc_check)
@@ -452,8 +468,12 @@ struct Pcm {
         g.consistent.clear();
         Csr csr = csr_from_bits(g.bits, g.n, g.words);
         std::vector<int> idx;
-        num = (size_t)fmc_heuristic(csr, 0, -1, &idx);
-        for (size_t i = 0; i < num; ++i) g.consistent.push_back(g.factors[idx[i]]);
+        const int sz = fmc_heuristic(csr, 0, -1, &idx);
+        // indices past the closures (an adjacency kept larger by a removal)
+        // are dropped; the reference would index past its factor list
+        for (int i = 0; i < sz; ++i)
+          if (idx[i] < (int)g.factors.size()) g.consistent.push_back(g.factors[idx[i]]);
+        num = g.consistent.size();
       } else {
         g.consistent = g.factors;
         num = g.factors.size();
@@ -472,16 +492,78 @@ struct Pcm {
       int num = fmc_heuristic(csr, first, (int)prev, &idx);
       if ((size_t)num > prev) {
         g.consistent.clear();
-        for (int i = 0; i < num; ++i) g.consistent.push_back(g.factors[idx[i]]);
+        for (int i = 0; i < num; ++i)
+          if (idx[i] < (int)g.factors.size()) g.consistent.push_back(g.factors[idx[i]]);
       }
     }
     for (const auto& kv : loop_closures) total_good_lc += kv.second.consistent.size();
   }
+  // Pcm.h:977-1005
   std::vector<Factor<L>> build_graph() const {
     std::vector<Factor<L>> out(nfg_odom);
     out.insert(out.end(), nfg_special.begin(), nfg_special.end());
-    for (const auto& kv : loop_closures) out.insert(out.end(), kv.second.consistent.begin(), kv.second.consistent.end());
+    auto is_ignored = [this](char c) { return std::find(ignored.begin(), ignored.end(), c) != ignored.end(); };
+    for (const auto& kv : loop_closures) {
+      if (is_ignored(kv.first.id1) || is_ignored(kv.first.id2)) continue;
+      out.insert(out.end(), kv.second.consistent.begin(), kv.second.consistent.end());
+    }
     return out;
+  }
+
+  // Pcm.h:299-342 (a group with no closure left returns false; the reference
+  // would index its empty factor list)
+  bool remove_last(const ObsId& id, uint64_t* k1, uint64_t* k2, std::vector<Factor<L>>* out) {
+    auto it = loop_closures.find(id);
+    if (it == loop_closures.end()) return false;
+    Group<L>& g = it->second;
+    const int num_lc = g.adj_rows;
+    if (num_lc <= 0 || g.factors.empty()) return false;
+    *k1 = g.factors.back().k1;
+    *k2 = g.factors.back().k2;
+    g.factors.pop_back();
+    if (g.factors.size() < 2) {
+      g.consistent = g.factors;
+    } else {
+      const int m = num_lc - 1;
+      g.adj_rows = m;
+      g.consistent.clear();
+      if (lc_check && g.n >= m) {
+        g.shrink(m);
+        Csr csr = csr_from_bits(g.bits, g.n, g.words);
+        std::vector<int> idx;
+        const int sz = fmc_heuristic(csr, 0, -1, &idx);
+        for (int i = 0; i < sz; ++i)
+          if (idx[i] < (int)g.factors.size()) g.consistent.push_back(g.factors[idx[i]]);
+      } else if (m > 0) {
+        g.consistent.push_back(g.factors[0]);  // greedy clique of an edgeless graph
+      }
+    }
+    *out = build_graph();
+    return true;
+  }
+  // Pcm.h:347-353
+  bool remove_last_in_order(uint64_t* k1, uint64_t* k2, std::vector<Factor<L>>* out) {
+    if (in_order.empty()) return false;
+    const ObsId id = in_order.back();
+    in_order.pop_back();
+    return remove_last(id, k1, k2, out);
+  }
+  // Pcm.h:357-376
+  void ignore_prefix(char c, std::vector<Factor<L>>* out) {
+    if (std::find(ignored.begin(), ignored.end(), c) == ignored.end()) ignored.push_back(c);
+    *out = build_graph();
+  }
+  void revive_prefix(char c, std::vector<Factor<L>>* out) {
+    ignored.erase(std::remove(ignored.begin(), ignored.end(), c), ignored.end());
+    *out = build_graph();
+  }
+  // Pcm.h:386-408
+  void remove_priors_with_prefix(char c, std::vector<Factor<L>>* out) {
+    std::vector<Factor<L>> kept;
+    for (const auto& f : nfg_special)
+      if (f.kind != 1 || key_chr(f.k1) != c) kept.push_back(f);
+    nfg_special.swap(kept);
+    *out = build_graph();
   }
 
   // Pcm.h:148-281. values: the solver's value map, already extended by the

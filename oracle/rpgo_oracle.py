@@ -72,6 +72,12 @@ def lib():
         _lib.oracle_get_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib.oracle_set_warm_probs.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         _lib.oracle_force_optimize.argtypes = [C.c_void_p]
+        _lib.oracle_remove_last_loop_closure.argtypes = [C.c_void_p, C.c_int, C.c_char, C.c_char,
+                                                         C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                                         C.POINTER(C.c_int)]
+        _lib.oracle_ignore_prefix.argtypes = [C.c_void_p, C.c_char, C.c_int]
+        _lib.oracle_ignored_prefixes.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+        _lib.oracle_remove_priors_with_prefix.argtypes = [C.c_void_p, C.c_char, C.c_int]
         _lib.oracle_get_warm_stats.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         _lib.oracle_pwc_op.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                        C.c_int, C.c_void_p, C.c_void_p, C.POINTER(C.c_int)]
@@ -182,6 +188,29 @@ class OracleSolver:
         lib().oracle_get_warm_stats(self.h, C.byref(wr), C.byref(wf))
         return dict(lm_iterations=a.value, linear_solves=b.value, gnc_iterations=c.value, pcm_seconds=p.value,
                     solve_seconds=s.value, warm_runs=wr.value, warm_fallbacks=wf.value)
+
+    # ---- edit API (src/RobustSolver.cpp:371-446)
+    def removeLastLoopClosure(self, prefix_1=None, prefix_2=None):
+        a, b, r = C.c_uint64(), C.c_uint64(), C.c_int()
+        by_id = prefix_1 is not None
+        rc = lib().oracle_remove_last_loop_closure(self.h, int(by_id), (prefix_1 or "\0").encode(),
+                                                   (prefix_2 or "\0").encode(), C.byref(a), C.byref(b), C.byref(r))
+        assert rc == 0, rc
+        return (a.value, b.value) if r.value else None
+
+    def ignorePrefix(self, prefix: str) -> int:
+        return lib().oracle_ignore_prefix(self.h, prefix.encode(), 0)
+
+    def revivePrefix(self, prefix: str) -> int:
+        return lib().oracle_ignore_prefix(self.h, prefix.encode(), 1)
+
+    def getIgnoredPrefixes(self):
+        buf = C.create_string_buffer(64)
+        n = lib().oracle_ignored_prefixes(self.h, buf, 64)
+        return [chr(c) for c in buf.raw[:n]]
+
+    def removePriorFactorsWithPrefix(self, prefix: str, optimize_graph: bool = True) -> int:
+        return lib().oracle_remove_priors_with_prefix(self.h, prefix.encode(), int(optimize_graph))
 
     def force_optimize(self) -> int:
         """forceUpdate() with no new factors: re-run the solve."""

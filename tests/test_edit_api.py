@@ -1,0 +1,209 @@
+"""The edit API (RobustSolver::removeLastLoopClosure, ignorePrefix,
+revivePrefix, getIgnoredPrefixes, removePriorFactorsWithPrefix;
+src/RobustSolver.cpp:371-446, Pcm.h:299-408), restated from the reference's
+tests as data:
+  tests/testRemoveLastLoopClosure.cpp:110-380  NoOR, Pcm, Pcm_NoObsId
+  tests/testIgnorePrefix.cpp:108-285           IgnoreSinglePrefixA / B
+  tests/testRemovePriorFactors.cpp:24-168      RemovePriorNoOR / Pcm
+Expected sizes, removed edges and poses (gtsam::assert_equal tolerances) are
+the reference's EXPECT lines. The same scenarios run on the CPU oracle (CPU
+suite) and on the CUDA library (GPU suite), and the GPU poses are checked
+against the oracle's after every step.
+"""
+import numpy as np
+import pytest
+
+from oracle import rpgo_oracle as O
+from rpgo_gb300.graph import Graph, isotropic_variance, pose3, symbol
+from rpgo_gb300.params import QUIET, RobustSolverParams
+
+R90 = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+RM90 = R90.T
+R180 = np.diag([-1.0, -1.0, 1.0])  # Rot3(0, 0, 0, 1): quaternion w 0, z 1
+A, B = (lambda i: symbol("a", i)), (lambda i: symbol("b", i))
+
+
+def _test_graph():
+    """buildTestGraph of testRemoveLastLoopClosure.cpp / testIgnorePrefix.cpp."""
+    g = Graph(3)
+    g.insert(A(0), pose3())
+    g.add_prior(A(0), pose3(), isotropic_variance(6, 10e-8))
+    g.insert(B(0), pose3(t=(0, -1, 0)))
+    g.add_prior(B(0), pose3(t=(0, -1, 0)), isotropic_variance(6, 1))
+    odom = pose3(t=(1, 0, 0))
+    for i in range(3):
+        g.insert(A(i + 1), odom)
+        g.insert(B(i + 1), odom)
+        g.add_between(A(i), A(i + 1), odom, isotropic_variance(6, 10))
+        g.add_between(B(i), B(i + 1), odom, isotropic_variance(6, 10))
+    for i in range(3, 5):
+        g.insert(A(i + 1), pose3(R90, (1, 0, 0)))
+        g.add_between(A(i), A(i + 1), pose3(R90, (1, 0, 0)), isotropic_variance(6, 10))
+    for i in range(3, 5):
+        g.insert(B(i + 1), pose3(RM90, (1, 0, 0)))
+        g.add_between(B(i), B(i + 1), pose3(RM90, (1, 0, 0)), isotropic_variance(6, 10))
+    return g
+
+
+def _two_closures():
+    g = Graph(3)
+    noise = isotropic_variance(6, 10e-8)
+    g.add_between(B(0), A(0), pose3(), noise)
+    g.add_between(A(5), A(3), pose3(R180, (1, 0, 0)), noise)
+    return g
+
+
+def _pose_at(solver, key):
+    keys, poses = solver.estimate()
+    return poses[list(keys).index(key)]
+
+
+def _close(p, R, t, tol):
+    return np.allclose(p[:9], np.asarray(R).reshape(9), atol=tol) and np.allclose(p[9:], t, atol=tol)
+
+
+B0_MOVED = (np.eye(3), (0, 0, 0), 10e-6)
+B0_FREE = (np.eye(3), (0, -1, 0), 0.01)
+A5_LOOP = (R180, (4, 0, 0), 10e-6)
+A5_FREE = (R180, (4, 1, 0), 10e-6)
+
+
+def _check(s, nfg, b0, a5, fails, tag):
+    c = s.counts()
+    if c.num_factors != nfg or c.num_values != 12:
+        fails.append(f"{tag}: sizes {c.num_factors}/{c.num_values}")
+    for key, (R, t, tol) in ((B(0), b0), (A(5), a5)):
+        if not _close(_pose_at(s, key), R, t, tol):
+            fails.append(f"{tag}: pose of {key:#x} {_pose_at(s, key)}")
+
+
+def _params(pcm):
+    return RobustSolverParams().setPcm3DParams(100, 100, QUIET) if pcm else RobustSolverParams().setNoRejection(QUIET)
+
+
+def remove_last_loop_closure(make, pcm, by_id):
+    s = make(_params(pcm))
+    fails = []
+    assert s.update(_test_graph()) == 0
+    _check(s, 12, B0_FREE, A5_FREE, fails, "initial")
+    assert s.update(_two_closures()) == 0
+    _check(s, 14, B0_MOVED, A5_LOOP, fails, "closures")
+    e1 = s.removeLastLoopClosure("a", "a") if by_id else s.removeLastLoopClosure()
+    if e1 != (A(5), A(3)):
+        fails.append(f"removed edge 1 {e1}")
+    _check(s, 13, (np.eye(3), (0, 0, 0), 10e-6), A5_FREE, fails, "removed 1")
+    e2 = s.removeLastLoopClosure("a", "b") if by_id else s.removeLastLoopClosure()
+    if e2 != (B(0), A(0)):
+        fails.append(f"removed edge 2 {e2}")
+    _check(s, 12, B0_FREE, A5_FREE, fails, "removed 2")
+    if not by_id:
+        e3 = s.removeLastLoopClosure()
+        if e3 is not None:
+            fails.append(f"removed edge 3 {e3}")
+        _check(s, 12, B0_FREE, A5_FREE, fails, "removed 3")
+    return fails, s
+
+
+def ignore_prefix(make, prefix):
+    s = make(_params(True))
+    fails = []
+    assert s.update(_test_graph()) == 0
+    assert s.update(_two_closures()) == 0
+    _check(s, 14, B0_MOVED, A5_LOOP, fails, "closures")
+    s.ignorePrefix(prefix)
+    if prefix == "a":
+        _check(s, 12, B0_FREE, A5_FREE, fails, "ignored")
+    else:
+        _check(s, 13, B0_FREE, A5_LOOP, fails, "ignored")
+    if s.getIgnoredPrefixes() != [prefix]:
+        fails.append(f"ignored {s.getIgnoredPrefixes()}")
+    s.revivePrefix(prefix)
+    _check(s, 14, (np.eye(3), (0, 0, 0), 0.01), A5_LOOP, fails, "revived")
+    if s.getIgnoredPrefixes() != []:
+        fails.append(f"ignored after revive {s.getIgnoredPrefixes()}")
+    return fails, s
+
+
+def remove_priors(make, pcm):
+    s = make(_params(pcm))
+    noise = isotropic_variance(6, 10e-8)
+    g = Graph(3)
+    g.add_between(A(0), A(1), pose3(), noise)
+    g.insert(A(0), pose3()).insert(A(1), pose3())
+    g.add_between(B(0), B(1), pose3(), noise)
+    g.insert(B(0), pose3()).insert(B(1), pose3())
+    g.add_between(A(1), A(2), pose3(), noise)
+    g.insert(A(2), pose3())
+    g.add_between(A(0), A(2), pose3(), noise)
+    g.add_between(B(0), A(1), pose3(), noise)
+    for k in (A(0), A(1), B(0)):
+        g.add_prior(k, pose3(), noise)
+    assert s.update(g) == 0
+    fails = []
+    for step, (prefix, n) in enumerate(((None, 8), ("a", 6), ("b", 5))):
+        if prefix:
+            assert s.removePriorFactorsWithPrefix(prefix) == 0
+        c = s.counts()
+        if c.num_factors != n or c.num_values != 5:
+            fails.append(f"step {step}: sizes {c.num_factors}/{c.num_values}")
+    return fails, s
+
+
+SCENARIOS = {
+    "RemoveLastLoopClosureNoOR": lambda m: remove_last_loop_closure(m, False, True),
+    "RemoveLastLoopClosurePcm": lambda m: remove_last_loop_closure(m, True, True),
+    "RemoveLastLoopClosurePcm_NoObsId": lambda m: remove_last_loop_closure(m, True, False),
+    "IgnoreSinglePrefixA": lambda m: ignore_prefix(m, "a"),
+    "IgnoreSinglePrefixB": lambda m: ignore_prefix(m, "b"),
+    "RemovePriorNoOR": lambda m: remove_priors(m, False),
+    "RemovePriorPcm": lambda m: remove_priors(m, True),
+}
+
+
+@pytest.mark.parametrize("name", sorted(SCENARIOS))
+def test_oracle_edit_api_reference_tests(name):
+    fails, _ = SCENARIOS[name](O.OracleSolver)
+    assert not fails, fails
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", sorted(SCENARIOS))
+def test_gpu_edit_api_reference_tests(name):
+    from rpgo_gb300 import build, capi
+
+    build()
+    fails, g = SCENARIOS[name](capi.RobustSolver)
+    assert not fails, fails
+    _, o = SCENARIOS[name](O.OracleSolver)
+    kg, pg = g.estimate()
+    ko, po = o.estimate()
+    assert np.array_equal(kg, ko)
+    np.testing.assert_allclose(pg, po, rtol=1e-6, atol=1e-9)
+    assert g.counts().num_factors == o.counts().num_factors
+    assert g.getIgnoredPrefixes() == o.getIgnoredPrefixes()
+
+
+@pytest.mark.gpu
+def test_gpu_remove_closures_from_large_group_matches_oracle():
+    """Several removals from one PCM group (the adjacency shrinks and the
+    clique is recomputed each time), then new closures appended."""
+    from rpgo_gb300 import build, capi, synth
+
+    build()
+    s = synth.walk3d(400, 60, 20, seed=61)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET)
+    g, o = capi.RobustSolver(p), O.OracleSolver(p)
+    assert g.update(s.graph) == 0 and o.update(s.graph) == 0
+    for _ in range(5):
+        assert g.removeLastLoopClosure() == o.removeLastLoopClosure()
+        assert np.array_equal(g.factors()[1], o.factors()[1])
+        assert np.array_equal(g.adjacency(0), o.adjacency(0))
+    more = synth.walk3d(400, 70, 25, seed=61).graph
+    extra = Graph(3)
+    n0 = s.graph.num_factors
+    for i in range(n0, more.num_factors):
+        extra.add_between(more.key1[i], more.key2[i], more.measured[i], (more.cov[i], more.sqrt_info[i]))
+    assert g.update(extra) == 0 and o.update(extra) == 0
+    assert np.array_equal(g.factors()[1], o.factors()[1])
+    assert np.array_equal(g.adjacency(0), o.adjacency(0))
+    np.testing.assert_allclose(g.estimate()[1], o.estimate()[1], rtol=1e-6, atol=1e-9)
