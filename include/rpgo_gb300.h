@@ -53,6 +53,8 @@ enum { RPGO_FACTOR_BETWEEN = 0, RPGO_FACTOR_PRIOR = 1 };
  * linearSolverType, left at its default sparse Cholesky by the reference). */
 enum { RPGO_LINEAR_CHOLESKY = 0, RPGO_LINEAR_PCG = 1 };
 
+#define RPGO_MAX_SPECIAL_SYMBOLS 16
+
 /* Flat mirror of RobustSolverParams (include/KimeraRPGO/SolverParams.h:80-299)
  * with PcmParams (33-56) and GncParams (58-78) inlined. */
 typedef struct rpgo_params {
@@ -79,6 +81,10 @@ typedef struct rpgo_params {
    * keeps GncOptimizer's plain mu continuation): RPGO_WARM_* */
   int32_t gnc_warm_start;
   double gnc_warm_mu;         /* mu of the first TLS weight update of the warm schedule */
+  /* RobustSolverParams::specialSymbols (SolverParams.h:284): key prefixes of
+   * landmarks, whose observations get landmark PCM (Pcm.h:180-220, 775-844) */
+  int32_t num_special_symbols;
+  char special_symbols[RPGO_MAX_SPECIAL_SYMBOLS];
 } rpgo_params;
 
 /* gnc_warm_start values.

@@ -481,6 +481,8 @@ rpgo_solver* rpgo_create(const rpgo_params* p) {
       c.dist_trans_threshold = p->dist_trans_threshold;
       c.dist_rot_threshold = p->dist_rot_threshold;
       c.incremental = p->incremental != 0;
+      for (int i = 0; i < p->num_special_symbols && i < RPGO_MAX_SPECIAL_SYMBOLS; ++i)
+        c.special.push_back(p->special_symbols[i]);
       s->pcm = std::make_unique<PcmEngine>(c, s->st);
     }
   } catch (const std::exception& e) {

@@ -94,6 +94,101 @@ void PcmEngine::flush_slots() {
   pending_init_.clear();
 }
 
+// adjacency capacity: row_cap rows of row_cap/32 words, zero padded
+void PcmEngine::grow_adjacency(Group& g, int n) {
+  if (n <= g.row_cap) return;
+  int cap = g.row_cap ? g.row_cap : 64;
+  while (cap < n) cap *= 2;
+  const int words = cap / 32;
+  DeviceBuffer<uint32_t> nb((size_t)cap * words);
+  nb.zero(st_);
+  if (g.n > 0)
+    RPGO_CUDA(cudaMemcpy2DAsync(nb.get(), (size_t)words * 4, g.adj.get(), (size_t)g.words * 4, (size_t)g.words * 4,
+                                g.n, cudaMemcpyDeviceToDevice, st_));
+  g.adj = std::move(nb);
+  g.row_cap = cap;
+  g.words = words;
+}
+
+bool PcmEngine::is_special(char c) const {
+  return std::find(cfg_.special.begin(), cfg_.special.end(), c) != cfg_.special.end();
+}
+
+int32_t PcmEngine::slot_in(char prefix, uint64_t key) {
+  if (key_chr(key) == prefix) return slot(key);
+  auto it = foreign_slots_.find({prefix, key});
+  if (it != foreign_slots_.end()) return it->second;
+  const int32_t s = num_slots_++;
+  pending_default_.push_back(s);
+  foreign_slots_[{prefix, key}] = s;
+  return s;
+}
+
+void PcmEngine::run_landmark_pairwise(Group& g, uint64_t lk, int old_n, const FactorStore& store) {
+  const int n = (int)g.factors.size();
+  if (n <= old_n) return;
+  g.zp.grow((size_t)n * stride_, st_);
+  g.zc.grow((size_t)n * d_ * d_, st_);
+  const int add = n - old_n;
+  d_rows_.upload(g.h_row.data() + old_n, add, st_);
+  gather_rows(add, d_rows_.get(), store.meas(), stride_, g.zp.get() + (size_t)old_n * stride_, st_);
+  gather_rows(add, d_rows_.get(), store.cov(), d_ * d_, g.zc.get() + (size_t)old_n * d_ * d_, st_);
+  grow_adjacency(g, n);
+  // the new rows and columns start empty
+  launch_clear_columns(g.adj.get(), g.words, old_n, old_n, st_);
+  RPGO_CUDA(cudaMemsetAsync(g.adj.get() + (size_t)old_n * g.words, 0, sizeof(uint32_t) * (size_t)add * g.words, st_));
+  std::vector<int4> desc;
+  std::vector<int2> ij;
+  for (int j = std::max(old_n, 1); j < n; ++j)
+    for (int i = 0; i < j; ++i) {
+      const uint64_t ki = g.factors[i].k1, kj = g.factors[j].k1;
+      if (ki == lk || kj == lk) continue;  // observation stored landmark -> pose: left inconsistent
+      const char p = key_chr(ki);
+      if (key_chr(kj) == p) {
+        desc.push_back(int4{slot(ki), slot(kj), -1, -1});
+      } else {
+        const int32_t a0 = slot(symbol_key(p, 0)), sa = slot(ki);
+        const int32_t b0 = slot_in(p, symbol_key(key_chr(kj), 0)), sb = slot_in(p, kj);
+        desc.push_back(int4{a0, sa, b0, sb});
+      }
+      ij.push_back(int2{i, j});
+    }
+  flush_slots();
+  if (!desc.empty()) {
+    DeviceBuffer<int4> ddesc;
+    DeviceBuffer<int2> dij;
+    ddesc.upload(desc, st_);
+    dij.upload(ij, st_);
+    const double th0 = cfg_.mode == 0 ? cfg_.lc_threshold : cfg_.dist_trans_threshold;
+    const double th1 = cfg_.mode == 0 ? 0.0 : cfg_.dist_rot_threshold;
+    launch_landmark_pairs(cfg_.dim, cfg_.mode, (int)desc.size(), ddesc.get(), dij.get(), g.zp.get(), g.zc.get(),
+                          view(), th0, th1, g.adj.get(), g.words, st_);
+    RPGO_CUDA(cudaStreamSynchronize(st_));
+    stats_.pair_checks += (int64_t)desc.size();
+  }
+  g.n = n;
+  g.adj_rows = n;
+}
+
+// findMaxCliqueHeu over a landmark's adjacency (Pcm.h:878-897): always run,
+// whatever the loop-closure check setting; a fresh landmark's 1 x 1 zero
+// matrix gives its only observation
+size_t PcmEngine::landmark_inliers(Group& g) {
+  g.consistent.clear();
+  const int rows = g.adj_rows;
+  std::vector<int32_t> clique;
+  int sz = 0;
+  if (rows > 0 && g.adj.get() && g.n >= rows) {
+    sz = max_clique_heu(rows, g.adj.get(), g.words, 0, -1, &clique, clique_ws_, st_);
+  } else if (rows > 0) {
+    sz = 1;
+    clique.assign(1, 0);
+  }
+  for (int i = 0; i < sz; ++i)
+    if (clique[i] < (int32_t)g.factors.size()) g.consistent.push_back(clique[i]);
+  return g.consistent.size();
+}
+
 void PcmEngine::run_pairwise(Group& g, int old_n, const FactorStore& store) {
   const int n = (int)g.factors.size();
   if (n <= old_n) return;
@@ -112,20 +207,7 @@ void PcmEngine::run_pairwise(Group& g, int old_n, const FactorStore& store) {
   d_rows_.upload(g.h_row.data() + old_n, add, st_);
   gather_rows(add, d_rows_.get(), store.meas(), stride_, g.zp.get() + (size_t)old_n * stride_, st_);
   gather_rows(add, d_rows_.get(), store.cov(), d_ * d_, g.zc.get() + (size_t)old_n * d_ * d_, st_);
-  // adjacency capacity: row_cap rows of row_cap/32 words, zero padded
-  if (n > g.row_cap) {
-    int cap = g.row_cap ? g.row_cap : 64;
-    while (cap < n) cap *= 2;
-    const int words = cap / 32;
-    DeviceBuffer<uint32_t> nb((size_t)cap * words);
-    nb.zero(st_);
-    if (g.n > 0)
-      RPGO_CUDA(cudaMemcpy2DAsync(nb.get(), (size_t)words * 4, g.adj.get(), (size_t)g.words * 4,
-                                  (size_t)g.words * 4, g.n, cudaMemcpyDeviceToDevice, st_));
-    g.adj = std::move(nb);
-    g.row_cap = cap;
-    g.words = words;
-  }
+  grow_adjacency(g, n);
   lower_scratch_.resize((size_t)(n - old_n) * g.words);
   const double th0 = cfg_.mode == 0 ? cfg_.lc_threshold : cfg_.dist_trans_threshold;
   const double th1 = cfg_.mode == 0 ? 0.0 : cfg_.dist_rot_threshold;
@@ -158,6 +240,7 @@ void PcmEngine::find_inliers() {
     }
     total_good_lc_ += num;
   }
+  for (auto& kv : landmarks_) total_good_lc_ += landmark_inliers(kv.second);
 }
 
 // Pcm.h:906-970 with findMaxCliqueHeuIncremental (GraphUtils.cpp:30-44)
@@ -187,6 +270,7 @@ void PcmEngine::find_inliers_incremental(const std::unordered_map<ObsId, size_t,
     }
   }
   for (const auto& kv : groups_) total_good_lc_ += kv.second.consistent.size();
+  for (auto& kv : landmarks_) total_good_lc_ += landmark_inliers(kv.second);
 }
 
 bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const std::set<uint64_t>& new_keys,
@@ -200,7 +284,23 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
   std::vector<const FactorRec*> lcs;
   for (const auto& f : new_factors) {
     if (f.kind == 0) {
-      if (f.k1 + 1 == f.k2 && new_keys.count(f.k2)) {
+      if (is_special(key_chr(f.k1)) || is_special(key_chr(f.k2))) {
+        if (new_keys.count(f.k1) || new_keys.count(f.k2)) {
+          // first observation of a landmark (Pcm.h:209-220): a fresh
+          // Measurements holding it, replacing any earlier one
+          Group g;
+          g.factors.push_back(f);
+          g.consistent.push_back(0);
+          g.h_sa.push_back(0);
+          g.h_sb.push_back(0);
+          g.h_flip.push_back(0);
+          g.h_row.push_back(f.row);
+          landmarks_[landmark_key(f)] = std::move(g);
+          ++total_lc_;
+        } else if (f.k1 != f.k2) {
+          lcs.push_back(&f);
+        }
+      } else if (f.k1 + 1 == f.k2 && new_keys.count(f.k2)) {
         // updateOdom (Pcm.h:516-557)
         nfg_odom_.push_back(f);
         const char prefix = key_chr(f.k2);
@@ -240,6 +340,7 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
       const FactorRec& f = *lcs[k];
       if (!values.has(f.k1) || !values.has(f.k2)) continue;
       if (key_chr(f.k1) != key_chr(f.k2) || !odom_check_) continue;
+      if (is_special(key_chr(f.k1))) continue;
       prefix_exists_.insert(key_chr(f.k1));
       ci.push_back(slot(f.k1));
       cj.push_back(slot(f.k2));
@@ -270,9 +371,26 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
     // ---- grouping (Pcm.h:466-486)
     std::unordered_map<ObsId, size_t, ObsIdHash> num_new;
     std::vector<std::pair<ObsId, int>> touched;
+    std::vector<std::pair<uint64_t, int>> touched_lm;
     for (size_t k = 0; k < lcs.size(); ++k) {
       const FactorRec& f = *lcs[k];
       if (!values.has(f.k1) || !values.has(f.k2)) continue;
+      if (is_special(key_chr(f.k1)) || is_special(key_chr(f.k2))) {
+        // landmark re-observation (Pcm.h:440-454)
+        const uint64_t lk = landmark_key(f);
+        Group& lg = landmarks_[lk];
+        bool seen = false;
+        for (auto& t : touched_lm)
+          if (t.first == lk) seen = true;
+        if (!seen) touched_lm.emplace_back(lk, (int)lg.factors.size());
+        lg.factors.push_back(f);
+        lg.h_sa.push_back(0);
+        lg.h_sb.push_back(0);
+        lg.h_flip.push_back(0);
+        lg.h_row.push_back(f.row);
+        ++total_lc_;
+        continue;
+      }
       if (!passed[k]) continue;
       const ObsId id{key_chr(f.k1), key_chr(f.k2)};
       num_new[id]++;
@@ -306,6 +424,8 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
         run_pairwise(g, t.second, store);
       }
     }
+    if (!touched_lm.empty()) flush_slots();
+    for (auto& t : touched_lm) run_landmark_pairwise(landmarks_[t.first], t.first, t.second, store);
     if (cfg_.incremental) find_inliers_incremental(num_new);
     else find_inliers();
     do_optimize = true;
@@ -323,6 +443,8 @@ void PcmEngine::build_graph(std::vector<FactorRec>* out) const {
     if (ignored(kv.first.id1) || ignored(kv.first.id2)) continue;
     for (int32_t idx : kv.second.consistent) out->push_back(kv.second.factors[idx]);
   }
+  for (const auto& kv : landmarks_)
+    for (int32_t idx : kv.second.consistent) out->push_back(kv.second.factors[idx]);
 }
 
 void PcmEngine::clique_of(Group& g, int rows) {
@@ -409,10 +531,11 @@ void PcmEngine::remove_priors_with_prefix(char prefix, std::vector<FactorRec>* o
 
 void PcmEngine::closure_stats(std::vector<float>* out) {
   out->clear();
+  auto ignored = [this](char c) { return std::find(ignored_.begin(), ignored_.end(), c) != ignored_.end(); };
   for (auto& kv : groups_) {
     Group& g = kv.second;
     const int count = (int)g.consistent.size();
-    if (count == 0) continue;
+    if (count == 0 || ignored(kv.first.id1) || ignored(kv.first.id2)) continue;
     if (!lc_check_ || g.n == 0 || !g.adj.get()) {
       out->insert(out->end(), (size_t)count * 3, 0.f);
       continue;
@@ -436,6 +559,7 @@ void PcmEngine::closure_stats(std::vector<float>* out) {
       out->push_back((float)sup[k] / (float)std::max(1, members - 1));
     }
   }
+  for (const auto& kv : landmarks_) out->insert(out->end(), kv.second.consistent.size() * 3, 0.f);
 }
 
 bool PcmEngine::adjacency(int gi, std::vector<uint32_t>* words, int* n) const {

@@ -22,6 +22,10 @@
 namespace rpgo {
 
 inline char key_chr(uint64_t k) { return static_cast<char>(static_cast<unsigned char>(k >> 56)); }
+// gtsam::Symbol(c, index) as a key
+inline uint64_t symbol_key(char c, uint64_t index) {
+  return (static_cast<uint64_t>(static_cast<unsigned char>(c)) << 56) | index;
+}
 
 // ObservationId (TypeUtils.h:44-58) and its hash (TypeUtils.h:80-88)
 struct ObsId {
@@ -44,6 +48,7 @@ struct PcmConfig {
   double odom_trans_threshold = 0.05, odom_rot_threshold = 0.005;
   double dist_trans_threshold = 0.01, dist_rot_threshold = 0.001;
   bool incremental = false;
+  std::vector<char> special;  // landmark key prefixes (specialSymbols)
 };
 
 struct PcmStats {
@@ -107,6 +112,15 @@ class PcmEngine {
   void ensure_traj_capacity(size_t n);
   TrajView view() const;
   void run_pairwise(Group& g, int old_n, const FactorStore& store);
+  // Pcm.h:775-844 for the observations [old_n, n) of landmark `lk`
+  void run_landmark_pairwise(Group& g, uint64_t lk, int old_n, const FactorStore& store);
+  void grow_adjacency(Group& g, int n);
+  bool is_special(char c) const;
+  uint64_t landmark_key(const FactorRec& f) const { return is_special(key_chr(f.k1)) ? f.k1 : f.k2; }
+  // trajectory slot of `key` as looked up in robot `prefix`'s trajectory: a
+  // key of another robot is a default entry of that trajectory
+  int32_t slot_in(char prefix, uint64_t key);
+  size_t landmark_inliers(Group& g);
   void find_inliers();
   void find_inliers_incremental(const std::unordered_map<ObsId, size_t, ObsIdHash>& num_new);
   // Pcm::buildGraphToOptimize (Pcm.h:977-1005), ignored prefixes left out
@@ -132,6 +146,8 @@ class PcmEngine {
   std::unordered_set<char> prefix_exists_;
   std::vector<FactorRec> nfg_odom_, nfg_special_;
   std::unordered_map<ObsId, Group, ObsIdHash> groups_;
+  std::unordered_map<uint64_t, Group> landmarks_;  // landmarks_ (Pcm.h), keyed by landmark key
+  std::map<std::pair<char, uint64_t>, int32_t> foreign_slots_;
   std::vector<ObsId> lc_in_order_;  // loop_closures_in_order_ (Pcm.h:112)
   std::vector<char> ignored_;       // ignored_prefixes_ (Pcm.h:117)
   size_t total_lc_ = 0, total_good_lc_ = 0;

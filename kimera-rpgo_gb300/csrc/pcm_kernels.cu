@@ -393,6 +393,51 @@ __device__ __forceinline__ bool pair_consistent(int i, int j, const int32_t* __r
   return check_u<DIM>(loop, th0, th1);
 }
 
+// Landmark pair (Pcm.h:775-844): observations i, j (pose -> landmark) of one
+// landmark. i_odom_j = getBetween(pose_i, pose_j) of pose_i's trajectory
+// (GraphUtils.h:37-58): slots (s.x, s.y) for one robot; for two robots
+// (s.x, s.y, s.z, s.w) = (root a0, pose_i, root b0, pose_j) as looked up in
+// pose_i's trajectory. loop = (i_odom_j o Z_j)^-1 o Z_i.
+template <int DIM, class U>
+__global__ void k_landmark_pairs(int count, const int4* __restrict__ desc, const int2* __restrict__ ij,
+                                 const double* __restrict__ zp, const double* __restrict__ zc, TrajView tr,
+                                 double th0, double th1, uint32_t* __restrict__ adj, int words) {
+  using L = Lie<DIM>;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= count) return;
+  const int4 s = desc[k];
+  const int i = ij[k].x, j = ij[k].y;
+  U iodomj, X, Y;
+  if (s.z < 0) {
+    X.from_traj(tr, s.x);
+    Y.from_traj(tr, s.y);
+    X.between(Y, iodomj);
+  } else {
+    U pa, pb, pab, t;
+    X.from_traj(tr, s.x);
+    Y.from_traj(tr, s.y);
+    X.between(Y, pa);
+    U B0, Kb;
+    B0.from_traj(tr, s.z);
+    Kb.from_traj(tr, s.w);
+    B0.between(Kb, pb);
+    X.between(B0, pab);
+    pa.inverse_inplace();
+    pa.compose(pab, t);
+    t.compose(pb, iodomj);
+  }
+  U zj, zi, path, loop;
+  zj.from_factor(zp + (size_t)j * L::stride, zc + (size_t)j * L::d * L::d);
+  iodomj.compose(zj, path);
+  path.inverse_inplace();
+  zi.from_factor(zp + (size_t)i * L::stride, zc + (size_t)i * L::d * L::d);
+  path.compose(zi, loop);
+  if (check_u<DIM>(loop, th0, th1)) {
+    atomicOr(adj + (size_t)i * words + (j >> 5), 1u << (j & 31));
+    atomicOr(adj + (size_t)j * words + (i >> 5), 1u << (i & 31));
+  }
+}
+
 // block (32, ROWS): lane -> column i = 32*bx + lane, row j = row_begin + ROWS*by + ty.
 // lower[(j - row_begin) * words + bx] receives bits i < j.
 template <int DIM, class U, int ROWS>
@@ -541,6 +586,21 @@ void launch_pairwise(int dim, int mode, int n, int row_begin, const int32_t* sa,
   const int nb = div_up(n, 32);
   const int warps = nb * nb;
   k_symmetrize<<<div_up((int64_t)warps * 32, 256), 256, 0, st>>>(n, row_begin, lower_scratch, adj, words);
+  RPGO_LAUNCHED();
+}
+
+void launch_landmark_pairs(int dim, int mode, int count, const int4* desc, const int2* ij, const double* zp,
+                           const double* zc, TrajView tr, double th0, double th1, uint32_t* adj, int words,
+                           cudaStream_t st) {
+  if (count <= 0) return;
+  const int tb = 128, nb = div_up(count, tb);
+  if (dim == 3) {
+    if (mode == 0) k_landmark_pairs<3, PWC<3>><<<nb, tb, 0, st>>>(count, desc, ij, zp, zc, tr, th0, th1, adj, words);
+    else k_landmark_pairs<3, PWN<3>><<<nb, tb, 0, st>>>(count, desc, ij, zp, zc, tr, th0, th1, adj, words);
+  } else {
+    if (mode == 0) k_landmark_pairs<2, PWC<2>><<<nb, tb, 0, st>>>(count, desc, ij, zp, zc, tr, th0, th1, adj, words);
+    else k_landmark_pairs<2, PWN<2>><<<nb, tb, 0, st>>>(count, desc, ij, zp, zc, tr, th0, th1, adj, words);
+  }
   RPGO_LAUNCHED();
 }
 

@@ -26,6 +26,12 @@ void launch_odom_check(int dim, int mode, int64_t count, const int32_t* si, cons
                        const double* zc, TrajView tr, double th0, double th1, uint8_t* ok, cudaStream_t st);
 
 // adj: n rows of `words` uint32; lower_scratch: (n - row_begin) rows of `words`
+// landmark pair checks (Pcm.h:775-844) of `count` observation pairs
+// (ij: the two observations' rows; desc: trajectory slots, see the kernel);
+// consistent pairs get their two adjacency bits set
+void launch_landmark_pairs(int dim, int mode, int count, const int4* desc, const int2* ij, const double* zp,
+                           const double* zc, TrajView tr, double th0, double th1, uint32_t* adj, int words,
+                           cudaStream_t st);
 // rows [0, rows) of a bit-packed adjacency (row stride `words`): clear the
 // bits of every column >= from
 void launch_clear_columns(uint32_t* adj, int words, int rows, int from, cudaStream_t st);

@@ -31,6 +31,7 @@ class Params(C.Structure):
         ("gnc_weights_tol", C.c_double), ("gnc_fix_prev_inliers", C.c_int32), ("gnc_bias_odom", C.c_int32),
         ("lm_diagonal_damping", C.c_int32), ("linear_solver", C.c_int32),
         ("gnc_warm_start", C.c_int32), ("gnc_warm_mu", C.c_double),
+        ("num_special_symbols", C.c_int32), ("special_symbols", C.c_char * 16),
     ]
 
 

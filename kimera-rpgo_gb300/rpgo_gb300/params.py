@@ -49,6 +49,9 @@ class RobustSolverParams:
         # GNC warm start (no counterpart in the reference): off by default
         self.gnc_warm_start = WARM_OFF
         self.gnc_warm_mu = 1e2
+        # specialSymbols (SolverParams.h:284): landmark key prefixes
+        self.num_special_symbols = 0
+        self.special_symbols = b""
 
     # SolverParams.h:97-100
     def setNoRejection(self, verbosity=UPDATE, dim=3):
@@ -131,6 +134,17 @@ class RobustSolverParams:
     def gncBiasOdom(self):
         self.gnc_bias_odom = 1
         return self
+
+    @property
+    def specialSymbols(self):
+        return [chr(c) for c in self.special_symbols[:self.num_special_symbols]]
+
+    @specialSymbols.setter
+    def specialSymbols(self, symbols):
+        b = "".join(symbols).encode()
+        if len(b) > 16:
+            raise ValueError("at most 16 special symbols")
+        self.special_symbols, self.num_special_symbols = b, len(b)
 
     def setGncWarmStart(self, mode=WARM_ON, mu=None):
         """Warm-started GNC schedule (WARM_ON), plain schedule with closure

@@ -70,6 +70,8 @@ struct RobustSolverO final : SolverBase {
       pp.dist_trans_threshold = p.dist_trans_threshold;
       pp.dist_rot_threshold = p.dist_rot_threshold;
       pp.incremental = p.incremental != 0;
+      for (int i = 0; i < p.num_special_symbols && i < RPGO_MAX_SPECIAL_SYMBOLS; ++i)
+        pp.special.push_back(p.special_symbols[i]);
       pcm.reset(new Pcm<L, U>(pp));
     }
   }

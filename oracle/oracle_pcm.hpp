@@ -349,6 +349,7 @@ struct PcmParamsO {
   double odom_trans_threshold = 0.05, odom_rot_threshold = 0.005;
   double dist_trans_threshold = 0.01, dist_rot_threshold = 0.001;
   bool incremental = false;
+  std::vector<char> special;  // special (landmark) symbols
 };
 
 // U = PWC<L> (Pcm2D/Pcm3D) or PWN<L> (PcmSimple2D/PcmSimple3D)
@@ -359,6 +360,7 @@ struct Pcm {
   bool odom_check = true, lc_check = true;
   std::vector<Factor<L>> nfg_odom, nfg_special;
   std::unordered_map<ObsId, Group<L>, ObsIdHash> loop_closures;
+  std::unordered_map<uint64_t, Group<L>> landmarks;  // landmarks_ (Pcm.h)
   std::vector<ObsId> in_order;   // loop_closures_in_order_ (Pcm.h:112)
   std::vector<char> ignored;     // ignored_prefixes_ (Pcm.h:117)
   std::unordered_map<char, Trajectory<U>> trajectories;
@@ -419,6 +421,43 @@ struct Pcm {
     U prev = trajectories[prefix].poses[f.k1];
     trajectories[prefix].poses[f.k2] = prev.compose(delta);
   }
+  // Pcm.h:506-511
+  bool is_special(char c) const {
+    return std::find(params.special.begin(), params.special.end(), c) != params.special.end();
+  }
+  uint64_t landmark_key(const Factor<L>& f) const { return is_special(key_chr(f.k1)) ? f.k1 : f.k2; }
+  // Pcm.h:775-844 for the newest observation of a landmark. Observations
+  // stored landmark -> pose are warned about and left inconsistent with every
+  // other (the reference abandons the whole matrix update there).
+  void increment_landmark(Group<L>& g, uint64_t lk) {
+    const int num_lc = (int)g.factors.size();
+    g.grow(num_lc);
+    g.adj_rows = num_lc;
+    if (num_lc < 2) return;
+    const Factor<L>& fj = g.factors[num_lc - 1];
+    const U j_pose_l = U::from_factor(fj.measured, fj.cov);
+    for (int i = 0; i < num_lc - 1; ++i) {
+      const Factor<L>& fi = g.factors[i];
+      if (fi.k1 == lk || fj.k1 == lk) continue;
+      const U i_pose_l = U::from_factor(fi.measured, fi.cov);
+      U i_odom_j = trajectories[key_chr(fi.k1)].getBetween(fi.k1, fj.k1);
+      U i_path_l = i_odom_j.compose(j_pose_l);
+      U loop = i_path_l.inverse().compose(i_pose_l);
+      if (check_loop(loop)) g.set(i, num_lc - 1);
+    }
+  }
+  // findMaxCliqueHeu over a landmark's adjacency (Pcm.h:878-897)
+  size_t landmark_inliers(Group<L>& g) {
+    g.consistent.clear();
+    if (g.n < g.adj_rows) g.grow(g.adj_rows);
+    Csr csr = csr_from_bits(g.bits, g.adj_rows, g.words);
+    std::vector<int> idx;
+    const int sz = fmc_heuristic(csr, 0, -1, &idx);
+    for (int i = 0; i < sz; ++i)
+      if (idx[i] < (int)g.factors.size()) g.consistent.push_back(g.factors[idx[i]]);
+    return g.consistent.size();
+  }
+
   // Pcm.h:725-768 for every new member of the group against all earlier ones
   void increment_adjacency(Group<L>& g, int old_n) {
     g.grow((int)g.factors.size());
@@ -439,6 +478,15 @@ struct Pcm {
     for (const auto& f : lcs) {
       if (!values.count(f.k1) || !values.count(f.k2)) continue;
       const char c1 = key_chr(f.k1), c2 = key_chr(f.k2);
+      if (is_special(c1) || is_special(c2)) {
+        // landmark re-observation (Pcm.h:440-454)
+        const uint64_t lk = landmark_key(f);
+        Group<L>& lg = landmarks[lk];
+        lg.factors.push_back(f);
+        ++total_lc;
+        increment_landmark(lg, lk);
+        continue;
+      }
       bool ok = true;
       if (c1 == c2) ok = is_odom_consistent(f);
       if (!ok) continue;
@@ -480,6 +528,7 @@ struct Pcm {
       }
       total_good_lc += num;
     }
+    for (auto& kv : landmarks) total_good_lc += landmark_inliers(kv.second);
   }
   void find_inliers_incremental(const std::unordered_map<ObsId, size_t, ObsIdHash>& num_new) {
     total_good_lc = 0;
@@ -497,6 +546,7 @@ struct Pcm {
       }
     }
     for (const auto& kv : loop_closures) total_good_lc += kv.second.consistent.size();
+    for (auto& kv : landmarks) total_good_lc += landmark_inliers(kv.second);
   }
   // Pcm.h:977-1005
   std::vector<Factor<L>> build_graph() const {
@@ -507,6 +557,7 @@ struct Pcm {
       if (is_ignored(kv.first.id1) || is_ignored(kv.first.id2)) continue;
       out.insert(out.end(), kv.second.consistent.begin(), kv.second.consistent.end());
     }
+    for (const auto& kv : landmarks) out.insert(out.end(), kv.second.consistent.begin(), kv.second.consistent.end());
     return out;
   }
 
@@ -576,7 +627,18 @@ struct Pcm {
     std::vector<Factor<L>> lcs;
     for (const auto& f : new_factors) {
       if (f.kind == 0) {
-        if (f.k1 + 1 == f.k2 && new_keys.count(f.k2)) {
+        if (is_special(key_chr(f.k1)) || is_special(key_chr(f.k2))) {
+          if (new_keys.count(f.k1) || new_keys.count(f.k2)) {
+            // first observation of a landmark (Pcm.h:209-220)
+            Group<L> g;
+            g.factors.push_back(f);
+            g.consistent.push_back(f);
+            landmarks[landmark_key(f)] = g;
+            ++total_lc;
+          } else if (f.k1 != f.k2) {
+            lcs.push_back(f);
+          }
+        } else if (f.k1 + 1 == f.k2 && new_keys.count(f.k2)) {
           update_odom(f, values);
         } else if (f.k1 != f.k2) {
           lcs.push_back(f);
