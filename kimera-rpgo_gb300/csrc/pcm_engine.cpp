@@ -127,12 +127,14 @@ int32_t PcmEngine::slot_in(char prefix, uint64_t key) {
 void PcmEngine::run_landmark_pairwise(Group& g, uint64_t lk, int old_n, const FactorStore& store) {
   const int n = (int)g.factors.size();
   if (n <= old_n) return;
-  g.zp.grow((size_t)n * stride_, st_);
-  g.zc.grow((size_t)n * d_ * d_, st_);
+  // measurements of every observation (a first observation arrives without
+  // a pairwise check, so its row is gathered here); landmark groups are small
   const int add = n - old_n;
-  d_rows_.upload(g.h_row.data() + old_n, add, st_);
-  gather_rows(add, d_rows_.get(), store.meas(), stride_, g.zp.get() + (size_t)old_n * stride_, st_);
-  gather_rows(add, d_rows_.get(), store.cov(), d_ * d_, g.zc.get() + (size_t)old_n * d_ * d_, st_);
+  g.zp.resize((size_t)n * stride_);
+  g.zc.resize((size_t)n * d_ * d_);
+  d_rows_.upload(g.h_row.data(), n, st_);
+  gather_rows(n, d_rows_.get(), store.meas(), stride_, g.zp.get(), st_);
+  gather_rows(n, d_rows_.get(), store.cov(), d_ * d_, g.zc.get(), st_);
   grow_adjacency(g, n);
   // the new rows and columns start empty
   launch_clear_columns(g.adj.get(), g.words, old_n, old_n, st_);
