@@ -85,7 +85,18 @@ typedef struct rpgo_params {
    * landmarks, whose observations get landmark PCM (Pcm.h:180-220, 775-844) */
   int32_t num_special_symbols;
   char special_symbols[RPGO_MAX_SPECIAL_SYMBOLS];
+  /* multirobot_align_method / multirobot_align_gnc_prob
+   * (SolverParams.h:92-93, 264-272): RPGO_ALIGN_* */
+  int32_t multirobot_align_method;
+  double multirobot_align_gnc_prob;
 } rpgo_params;
+
+/* MultiRobotAlignMethod (SolverParams.h:26-31): after PCM, the initial
+ * values of every robot but the one with the smallest prefix are moved by
+ * the robust average (GNC-TLS at multirobot_align_gnc_prob, or L2) of the
+ * frame offsets its inter-robot closures with that robot imply
+ * (Pcm.h:1011-1131). */
+enum { RPGO_ALIGN_NONE = 0, RPGO_ALIGN_L2 = 1, RPGO_ALIGN_GNC = 2 };
 
 /* gnc_warm_start values.
  * OFF: the plain GNC-TLS schedule (GncOptimizer, src/RobustSolver.cpp:133-171).
@@ -167,6 +178,8 @@ void rpgo_params_set_pcm_simple2d(rpgo_params* p, double trans_odom, double rot_
                                   double rot_pcm, int32_t verbosity);
 void rpgo_params_set_pcm_simple3d(rpgo_params* p, double trans_odom, double rot_odom, double trans_pcm,
                                   double rot_pcm, int32_t verbosity);
+/* SolverParams.h:264-272 */
+void rpgo_params_set_multirobot_align(rpgo_params* p, int32_t method, double gnc_probability);
 /* SolverParams.h:213-250 */
 void rpgo_params_set_gnc_probability(rpgo_params* p, double alpha, int32_t max_iterations, double mu_step,
                                      double rel_cost_tol, double weight_tol, int32_t fix_prev_inliers,

@@ -8,10 +8,12 @@
 // returned instead.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <limits>
 #include <memory>
 #include <mutex>
 #include <numeric>
@@ -23,6 +25,7 @@
 #include "pcm_engine.hpp"
 #include "solver.hpp"
 #include "warm.hpp"
+#include "align.hpp"
 
 using namespace rpgo;
 
@@ -111,6 +114,126 @@ void closure_features_and_probs(rpgo_solver* s, GpuNls& nls, const std::vector<F
     for (int64_t q = 0; q < nlc; ++q) s->warm_probs[n_known + q] = prob[q];
   }
   RPGO_CUDA(cudaStreamSynchronize(s->st));
+}
+
+// Pcm::multirobotValueInitialization (Pcm.h:1011-1074) with
+// gncRobustPoseAveraging (1093-1131): robot r0 (smallest prefix) keeps its
+// odometry poses; every other robot's poses are moved by the GNC-TLS (or L2)
+// average of the frame offsets its consistent closures with r0 imply, solved
+// on the GPU as priors on one pose from the identity with GTSAM's default LM
+// parameters. Only the robot's own keys are written (the reference would also
+// move other robots' keys that a cross-robot lookup left in a trajectory).
+void multirobot_align(rpgo_solver* s) {
+  if (!s->pcm || s->p.multirobot_align_method == RPGO_ALIGN_NONE) return;
+  const std::vector<char> order = s->pcm->sorted_robot_order();
+  if (order.size() < 2) return;
+  const int stride = s->stride, d = s->d;
+  std::vector<uint64_t> keys;
+  std::vector<int32_t> slots;
+  auto apply = [&](char r, const double* T_dev) {
+    s->pcm->robot_slots(r, &keys, &slots);
+    std::vector<int32_t> sl;
+    std::vector<int64_t> rows;
+    for (size_t k = 0; k < keys.size(); ++k)
+      if (s->values->has(keys[k])) {
+        sl.push_back(slots[k]);
+        rows.push_back(s->values->row(keys[k]));
+      }
+    if (sl.empty()) return;
+    DeviceBuffer<int32_t> dsl;
+    DeviceBuffer<int64_t> drows;
+    dsl.upload(sl, s->st);
+    drows.upload(rows, s->st);
+    launch_transform_rows(s->dim, (int)sl.size(), T_dev, dsl.get(), s->pcm->traj_pose(), drows.get(),
+                          s->values->pose(), s->st);
+    RPGO_CUDA(cudaStreamSynchronize(s->st));
+  };
+  std::vector<double> ident(stride, 0.0);
+  if (s->dim == 3) ident[0] = ident[4] = ident[8] = 1.0;
+  else ident[0] = 1.0;
+  DeviceBuffer<double> dident;
+  dident.upload(ident, s->st);
+  const char r0 = order[0];
+  apply(r0, dident.get());
+  for (size_t i = 1; i < order.size(); ++i) {
+    const char ri = order[i];
+    std::vector<FactorRec> lcs;
+    if (!s->pcm->group_closures(r0, ri, &lcs)) continue;
+    std::vector<int32_t> front, back;
+    std::vector<uint8_t> swap;
+    std::vector<int64_t> rows;
+    bool ok = true;
+    for (const auto& f : lcs) {
+      uint64_t a = f.k1, b = f.k2;
+      const bool sw = key_chr(a) != r0;
+      if (sw) std::swap(a, b);
+      const int32_t sa = s->pcm->find_slot(a), sb = s->pcm->find_slot(b);
+      if (sa < 0 || sb < 0 || key_chr(a) != r0 || key_chr(b) != ri) {
+        ok = false;
+        break;
+      }
+      front.push_back(sa);
+      back.push_back(sb);
+      swap.push_back(sw ? 1 : 0);
+      rows.push_back(f.row);
+    }
+    if (!ok) continue;
+    const int K = (int)lcs.size();
+    if (K == 0) {  // an empty average stays at its initial value, the identity
+      apply(ri, dident.get());
+      continue;
+    }
+    std::vector<double> meas((size_t)K * stride);
+    if (K > 0) {
+      DeviceBuffer<int32_t> dfr, dbk;
+      DeviceBuffer<uint8_t> dsw;
+      DeviceBuffer<int64_t> drw;
+      DeviceBuffer<double> dout((size_t)K * stride);
+      dfr.upload(front, s->st);
+      dbk.upload(back, s->st);
+      dsw.upload(swap, s->st);
+      drw.upload(rows, s->st);
+      launch_frame_offsets(s->dim, K, dfr.get(), dbk.get(), dsw.get(), drw.get(), s->pcm->traj_pose(),
+                           s->store->meas(), dout.get(), s->st);
+      dout.download(meas.data(), meas.size(), s->st);
+      RPGO_CUDA(cudaStreamSynchronize(s->st));
+    }
+    // priors on one pose: sigmas 0.1 on the first rotation-dimension entries
+    // of the tangent, 0.5 on the rest (Pcm.h:1100-1106)
+    const int rdim = s->dim == 3 ? 3 : 1;
+    std::vector<double> cov((size_t)K * d * d, 0.0), sq((size_t)K * d * d, 0.0);
+    for (int k = 0; k < K; ++k)
+      for (int e = 0; e < d; ++e) {
+        const double sg = e < rdim ? 0.1 : 0.5;
+        cov[(size_t)k * d * d + d * e + e] = sg * sg;
+        sq[(size_t)k * d * d + d * e + e] = 1.0 / sg;
+      }
+    FactorStore fs(stride, d);
+    ValueStore vs(stride);
+    std::vector<FactorRec> graph((size_t)K);
+    if (K > 0) {
+      const int64_t first = fs.append(K, meas.data(), cov.data(), sq.data(), false, s->st);
+      for (int k = 0; k < K; ++k) graph[k] = FactorRec{RPGO_FACTOR_PRIOR, 0, 0, first + k};
+    }
+    const uint64_t key0 = 0;
+    vs.append(1, &key0, ident.data(), false, s->st);
+    GpuNls nls(s->dim, graph, fs, vs, s->st, true);
+    nls.dev().coop_ctas = s->coop_ctas;
+    GncConfig g;
+    if (s->p.multirobot_align_method == RPGO_ALIGN_L2) {
+      g.threshold_mode = RPGO_GNC_COST;
+      g.threshold = std::numeric_limits<double>::max();
+    } else {
+      g.threshold_mode = RPGO_GNC_PROBABILITY;
+      g.threshold = s->p.multirobot_align_gnc_prob;
+    }
+    LmParams lp;
+    lp.diagonal_damping = false;
+    std::vector<double> w;
+    NlsStats nst;
+    gnc_tls(nls, 0, g, lp, nullptr, &w, &nst);
+    apply(ri, nls.dev().x.get());
+  }
 }
 
 // RobustSolver::optimize (src/RobustSolver.cpp:115-306)
@@ -204,6 +327,7 @@ int update_impl(rpgo_solver* s, std::vector<FactorRec> nf, const rpgo_value_batc
   bool do_opt;
   if (s->pcm) {
     do_opt = s->pcm->remove_outliers(nf, new_keys, *s->values, *s->store, &s->nfg);
+    if (!nf.empty()) multirobot_align(s);
   } else {
     // GenericSolver::addAndCheckIfOptimize (src/GenericSolver.cpp:47-65)
     s->nfg.insert(s->nfg.end(), nf.begin(), nf.end());
@@ -394,6 +518,12 @@ void rpgo_params_default(rpgo_params* p) {
   p->linear_solver = RPGO_LINEAR_CHOLESKY;
   p->gnc_warm_start = RPGO_WARM_OFF;
   p->gnc_warm_mu = 100.0;
+  p->multirobot_align_method = RPGO_ALIGN_NONE;
+  p->multirobot_align_gnc_prob = 0.99;
+}
+void rpgo_params_set_multirobot_align(rpgo_params* p, int32_t method, double prob) {
+  p->multirobot_align_method = method;
+  p->multirobot_align_gnc_prob = prob;
 }
 void rpgo_params_set_no_rejection(rpgo_params* p, int32_t v) {
   p->outlier_removal = RPGO_OUTLIER_NONE;
@@ -457,6 +587,7 @@ rpgo_solver* rpgo_create(const rpgo_params* p) {
   const int m = p->outlier_removal;
   if (m < RPGO_OUTLIER_NONE || m > RPGO_OUTLIER_PCM_SIMPLE3D) return nullptr;
   if (p->solver != RPGO_SOLVER_LM && p->solver != RPGO_SOLVER_GN) return nullptr;
+  if (p->multirobot_align_method < RPGO_ALIGN_NONE || p->multirobot_align_method > RPGO_ALIGN_GNC) return nullptr;
   int dim = (m == RPGO_OUTLIER_PCM2D || m == RPGO_OUTLIER_PCM_SIMPLE2D) ? 2 : (m == RPGO_OUTLIER_NONE ? p->dim : 3);
   if (dim != 2 && dim != 3) return nullptr;
   if (!device_ready()) return nullptr;

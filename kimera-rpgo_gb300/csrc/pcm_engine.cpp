@@ -308,6 +308,7 @@ bool PcmEngine::remove_outliers(const std::vector<FactorRec>& new_factors, const
         const char prefix = key_chr(f.k2);
         if (!prefix_exists_.count(prefix)) {
           prefix_exists_.insert(prefix);
+          robot_order_.push_back(prefix);
           const int32_t s0 = slot(f.k1);
           pending_init_.emplace_back(s0, values.row(f.k1));
         }
@@ -562,6 +563,34 @@ void PcmEngine::closure_stats(std::vector<float>* out) {
     }
   }
   for (const auto& kv : landmarks_) out->insert(out->end(), kv.second.consistent.size() * 3, 0.f);
+}
+
+const std::vector<char>& PcmEngine::sorted_robot_order() {
+  std::sort(robot_order_.begin(), robot_order_.end());
+  return robot_order_;
+}
+
+void PcmEngine::robot_slots(char prefix, std::vector<uint64_t>* keys, std::vector<int32_t>* slots) const {
+  keys->clear();
+  slots->clear();
+  for (const auto& kv : slots_)
+    if (key_chr(kv.first) == prefix) {
+      keys->push_back(kv.first);
+      slots->push_back(kv.second);
+    }
+}
+
+int32_t PcmEngine::find_slot(uint64_t key) const {
+  auto it = slots_.find(key);
+  return it == slots_.end() ? -1 : it->second;
+}
+
+bool PcmEngine::group_closures(char a, char b, std::vector<FactorRec>* out) const {
+  out->clear();
+  auto it = groups_.find(ObsId{a, b});
+  if (it == groups_.end()) return false;
+  for (int32_t idx : it->second.consistent) out->push_back(it->second.factors[idx]);
+  return true;
 }
 
 bool PcmEngine::adjacency(int gi, std::vector<uint32_t>* words, int* n) const {

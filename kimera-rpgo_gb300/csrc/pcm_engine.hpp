@@ -90,6 +90,17 @@ class PcmEngine {
   const std::vector<char>& ignored_prefixes() const { return ignored_; }
   void remove_priors_with_prefix(char prefix, std::vector<FactorRec>* out);
 
+  // ---- multi-robot frame alignment inputs (Pcm.h:1011-1074)
+  // robot prefixes in the order their odometry started, sorted in place as
+  // the reference sorts robot_order_
+  const std::vector<char>& sorted_robot_order();
+  // keys of robot `prefix` that its trajectory holds, with their slots
+  void robot_slots(char prefix, std::vector<uint64_t>* keys, std::vector<int32_t>* slots) const;
+  int32_t find_slot(uint64_t key) const;  // -1 when the trajectory has no entry
+  // consistent closures of the group (a, b); false when there is no group
+  bool group_closures(char a, char b, std::vector<FactorRec>* out) const;
+  const double* traj_pose() const { return traj_pose_.get(); }
+
  private:
   struct Group {
     std::vector<FactorRec> factors;
@@ -150,6 +161,7 @@ class PcmEngine {
   std::map<std::pair<char, uint64_t>, int32_t> foreign_slots_;
   std::vector<ObsId> lc_in_order_;  // loop_closures_in_order_ (Pcm.h:112)
   std::vector<char> ignored_;       // ignored_prefixes_ (Pcm.h:117)
+  std::vector<char> robot_order_;   // robot_order_ (Pcm.h:128)
   size_t total_lc_ = 0, total_good_lc_ = 0;
   // scratch
   DeviceBuffer<int32_t> d_src_, d_dst_;

@@ -32,6 +32,7 @@ class Params(C.Structure):
         ("lm_diagonal_damping", C.c_int32), ("linear_solver", C.c_int32),
         ("gnc_warm_start", C.c_int32), ("gnc_warm_mu", C.c_double),
         ("num_special_symbols", C.c_int32), ("special_symbols", C.c_char * 16),
+        ("multirobot_align_method", C.c_int32), ("multirobot_align_gnc_prob", C.c_double),
     ]
 
 
@@ -77,6 +78,7 @@ SIGNATURES = {
     "rpgo_params_set_pcm3d": (None, [C.POINTER(Params), C.c_double, C.c_double, C.c_int32]),
     "rpgo_params_set_pcm_simple2d": (None, [C.POINTER(Params)] + [C.c_double] * 4 + [C.c_int32]),
     "rpgo_params_set_pcm_simple3d": (None, [C.POINTER(Params)] + [C.c_double] * 4 + [C.c_int32]),
+    "rpgo_params_set_multirobot_align": (None, [C.POINTER(Params), C.c_int32, C.c_double]),
     "rpgo_params_set_gnc_probability": (None, [C.POINTER(Params), C.c_double, C.c_int32, C.c_double, C.c_double,
                                                C.c_double, C.c_int32, C.c_int32]),
     "rpgo_params_set_gnc_cost": (None, [C.POINTER(Params), C.c_double, C.c_int32, C.c_double, C.c_double,

@@ -15,6 +15,8 @@ UPDATE, QUIET, VERBOSE = 0, 1, 2
 COST, PROBABILITY = 0, 1
 # linear solver of the LM / GN step (GTSAM linearSolverType; the reference keeps the default)
 LINEAR_CHOLESKY, LINEAR_PCG = 0, 1
+# MultiRobotAlignMethod (SolverParams.h:26-31)
+ALIGN_NONE, ALIGN_L2, ALIGN_GNC = 0, 1, 2
 # GNC warm start modes (rpgo_params.gnc_warm_start)
 WARM_OFF, WARM_ON, WARM_RECORD = 0, 1, 2
 
@@ -52,6 +54,9 @@ class RobustSolverParams:
         # specialSymbols (SolverParams.h:284): landmark key prefixes
         self.num_special_symbols = 0
         self.special_symbols = b""
+        # SolverParams.h:92-93
+        self.multirobot_align_method = ALIGN_NONE
+        self.multirobot_align_gnc_prob = 0.99
 
     # SolverParams.h:97-100
     def setNoRejection(self, verbosity=UPDATE, dim=3):
@@ -133,6 +138,15 @@ class RobustSolverParams:
 
     def gncBiasOdom(self):
         self.gnc_bias_odom = 1
+        return self
+
+    # SolverParams.h:264-272
+    def setMultiRobotAlignMethod(self, method):
+        self.multirobot_align_method = int(method)
+        return self
+
+    def setMultiRobotGncAlignProbability(self, probability):
+        self.multirobot_align_gnc_prob = float(probability)
         return self
 
     @property

@@ -4,11 +4,13 @@
 // 105-113 (known inliers), 115-306 (optimize), 337-369 (update);
 // src/GenericSolver.cpp:37-65 (updateValues, addAndCheckIfOptimize).
 // The structs of the public C ABI header are reused for the argument layout.
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <iomanip>
+#include <limits>
 #include <memory>
 #include <numeric>
 #include <set>
@@ -111,6 +113,7 @@ struct RobustSolverO final : SolverBase {
     if (pcm) {
       const auto t0 = std::chrono::steady_clock::now();
       do_opt = pcm->remove_outliers(nf, new_keys, values, &nfg);
+      if (!nf.empty()) multirobot_align();
       this->pcm_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     } else {
       nfg.insert(nfg.end(), nf.begin(), nf.end());
@@ -129,6 +132,74 @@ struct RobustSolverO final : SolverBase {
       return rc;
     }
     return RPGO_OK;
+  }
+  // Pcm.h:1093-1131: GNC (TLS at probability p, or L2) average of poses
+  // measured as priors on one pose, from the identity; GTSAM's default
+  // LevenbergMarquardtParams (no diagonal damping)
+  Pose pose_average(const std::vector<Pose>& meas) const {
+    std::vector<Factor<L>> graph;
+    for (const Pose& m : meas) {
+      Factor<L> f;
+      f.kind = 1;
+      f.k1 = f.k2 = 0;
+      f.measured = m;
+      for (int i = 0; i < d * d; ++i) f.cov[i] = f.sqrt_info[i] = 0.0;
+      for (int i = 0; i < d; ++i) {
+        const double sg = i < L::rdim ? 0.1 : 0.5;
+        f.cov[d * i + i] = sg * sg;
+        f.sqrt_info[d * i + i] = 1.0 / sg;
+      }
+      graph.push_back(f);
+    }
+    std::map<uint64_t, Pose> init{{0, L::identity()}};
+    GncParamsO gp;
+    if (p.multirobot_align_method == RPGO_ALIGN_L2) {
+      gp.threshold_mode = 0;
+      gp.threshold = std::numeric_limits<double>::max();
+    } else {
+      gp.threshold_mode = 1;
+      gp.threshold = p.multirobot_align_gnc_prob;
+    }
+    LmParamsO lp;
+    lp.diagonal_damping = false;
+    return gnc_tls<S>(graph, init, 0, gp, lp).values.at(0);
+  }
+  // Pcm.h:1011-1074 (robot keys only: the reference would also move other
+  // robots' keys that a cross-robot lookup left in a trajectory)
+  void multirobot_align() {
+    if (p.multirobot_align_method == RPGO_ALIGN_NONE || pcm->robot_order.size() < 2) return;
+    std::sort(pcm->robot_order.begin(), pcm->robot_order.end());
+    const char r0 = pcm->robot_order[0];
+    auto apply = [&](char r, const Pose& T) {
+      for (const auto& kv : pcm->trajectories[r].poses)
+        if (key_chr(kv.first) == r && values.count(kv.first)) values[kv.first] = L::compose(T, kv.second.pose);
+    };
+    apply(r0, L::identity());
+    for (size_t i = 1; i < pcm->robot_order.size(); ++i) {
+      const char ri = pcm->robot_order[i];
+      auto it = pcm->loop_closures.find(ObsId{r0, ri});
+      if (it == pcm->loop_closures.end()) continue;
+      std::vector<Pose> meas;
+      bool ok = true;
+      auto& t0 = pcm->trajectories[r0].poses;
+      auto& ti = pcm->trajectories[ri].poses;
+      for (const auto& f : it->second.consistent) {
+        uint64_t front = f.k1, back = f.k2;
+        Pose z = f.measured;
+        if (key_chr(front) != r0) {
+          std::swap(front, back);
+          z = L::inverse(z);
+        }
+        auto a = t0.find(front);
+        auto b = ti.find(back);
+        if (a == t0.end() || b == ti.end()) {
+          ok = false;
+          break;
+        }
+        meas.push_back(L::compose(L::compose(a->second.pose, z), L::inverse(b->second.pose)));
+      }
+      if (ok) apply(ri, pose_average(meas));
+    }
   }
   int optimize() {
     LmParamsO lp;

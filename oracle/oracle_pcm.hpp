@@ -362,6 +362,7 @@ struct Pcm {
   std::unordered_map<ObsId, Group<L>, ObsIdHash> loop_closures;
   std::unordered_map<uint64_t, Group<L>> landmarks;  // landmarks_ (Pcm.h)
   std::vector<ObsId> in_order;   // loop_closures_in_order_ (Pcm.h:112)
+  std::vector<char> robot_order; // robot_order_ (Pcm.h:128)
   std::vector<char> ignored;     // ignored_prefixes_ (Pcm.h:117)
   std::unordered_map<char, Trajectory<U>> trajectories;
   size_t total_lc = 0, total_good_lc = 0;
@@ -417,6 +418,7 @@ struct Pcm {
       U init;
       init.pose = values.at(f.k1);
       trajectories[prefix].poses[f.k1] = init;
+      robot_order.push_back(prefix);
     }
     U prev = trajectories[prefix].poses[f.k1];
     trajectories[prefix].poses[f.k2] = prev.compose(delta);

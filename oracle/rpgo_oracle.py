@@ -30,6 +30,7 @@ class Params(C.Structure):
         ("lm_diagonal_damping", C.c_int32), ("linear_solver", C.c_int32),
         ("gnc_warm_start", C.c_int32), ("gnc_warm_mu", C.c_double),
         ("num_special_symbols", C.c_int32), ("special_symbols", C.c_char * 16),
+        ("multirobot_align_method", C.c_int32), ("multirobot_align_gnc_prob", C.c_double),
     ]
 
 
