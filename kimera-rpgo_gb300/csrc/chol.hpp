@@ -27,10 +27,17 @@ struct CholDev {
   DeviceBuffer<double> Tpart; // tail row task sums (D per task)
   DeviceBuffer<double> out;   // model change, status
   DeviceBuffer<int32_t> status;
+  cudaEvent_t ev[2] = {nullptr, nullptr};  // around each launch (kernel time)
+  ~CholDev();
   void upload(CholPlan&& p, cudaStream_t st);
 };
 
 // Solve with the factorisation of (H + lambda D); fills s.delta.
 SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st);
+// Enqueue the same solve without waiting: the model change and the status
+// are copied to host[0] and host[1] (page-locked) by the stream; call
+// chol_finish after the stream reached that point.
+void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, double* host);
+SolveOut chol_finish(SolverDev& s, CholDev& c, const double* host);
 
 }  // namespace rpgo

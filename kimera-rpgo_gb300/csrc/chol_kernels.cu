@@ -775,6 +775,72 @@ void CholDev::upload(CholPlan&& p, cudaStream_t st) {
   status.resize(1);
 }
 
+CholDev::~CholDev() {
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+}
+
+namespace {
+__global__ void k_status_to_double(const int32_t* __restrict__ status, double* __restrict__ out) {
+  out[1] = (double)*status;
+}
+}  // namespace
+
+void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, double* host) {
+  if (s.N == 0) {
+    host[0] = 0.0;
+    host[1] = 0.0;
+    return;
+  }
+  if (!c.ev[0]) {
+    RPGO_CUDA(cudaEventCreate(&c.ev[0]));
+    RPGO_CUDA(cudaEventCreate(&c.ev[1]));
+  }
+  const int sms = device_sm_count();
+  const int grid = s.coop_ctas > 0 ? std::min(s.coop_ctas, sms) : sms;
+  c.part.resize((size_t)2 * grid);
+  const CholPlan& p = c.plan;
+  CholArgs a{s.N, p.n_sparse, p.T, p.n_tiles * kTB, p.n_tiles, c.levels,
+             c.perm.get(), c.col_ptr.get(), c.blk_row.get(), c.blk_col.get(), c.lvl_col_ptr.get(), c.lvl_cols.get(),
+             c.lvl_task_ptr.get(), c.tasks.get(), c.btask.get(), c.ftask.get(), c.upd_ptr.get(), c.upd_src.get(), c.tupd_ptr.get(),
+             c.tupd_src.get(), c.a_ptr.get(), c.a_src.get(), c.ta_ptr.get(), c.ta_src.get(), c.row_ptr.get(),
+             c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), c.ttasks.get(), c.ttask_ptr.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
+             s.g.get(), lambda, c.L.get(), c.Ldiag.get(),
+             c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.Spart.get(), c.Tpart.get(),
+             c.status.get()};
+  void* args[] = {&a};
+  RPGO_CUDA(cudaEventRecord(c.ev[0], st));
+  if (s.dim == 3)
+    RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_chol_solve<6>, grid, kThreads, args, 0, st));
+  else
+    RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_chol_solve<3>, grid, kThreads, args, 0, st));
+  RPGO_LAUNCHED();
+  RPGO_CUDA(cudaEventRecord(c.ev[1], st));
+  k_status_to_double<<<1, 1, 0, st>>>(c.status.get(), c.out.get());
+  RPGO_LAUNCHED();
+  RPGO_CUDA(cudaMemcpyAsync(host, c.out.get(), 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+}
+
+SolveOut chol_finish(SolverDev& s, CholDev& c, const double* host) {
+  SolveOut o;
+  if (s.N == 0) {
+    o.ok = 1;
+    return o;
+  }
+  float ms = 0.f;
+  RPGO_CUDA(cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]));
+  const CholPlan& p = c.plan;
+  kernel_times().chol_ms += ms;
+  kernel_times().chol_launches += 1;
+  kernel_times().chol_flops += p.flops;
+  kernel_times().chol_bytes += p.bytes;
+  kernel_times().chol_levels = c.levels;
+  kernel_times().chol_tail = p.T;
+  o.lin_change = host[0];
+  o.ok = host[1] == 0.0 ? 1 : 0;
+  return o;
+}
+
 SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st) {
   SolveOut o;
   if (s.N == 0) {

@@ -164,6 +164,32 @@ class DeviceBuffer {
   cudaStream_t st_ = nullptr;
 };
 
+// A few page-locked host words for device-to-host copies that must not block
+// the host until a later synchronisation (pageable copies synchronise).
+template <class T>
+class PinnedBuffer {
+ public:
+  PinnedBuffer() = default;
+  PinnedBuffer(const PinnedBuffer&) = delete;
+  PinnedBuffer& operator=(const PinnedBuffer&) = delete;
+  ~PinnedBuffer() {
+    if (p_) cudaFreeHost(p_);
+  }
+  T* get(size_t n) {
+    if (n > n_) {
+      if (p_) cudaFreeHost(p_);
+      p_ = nullptr;
+      RPGO_CUDA(cudaMallocHost((void**)&p_, n * sizeof(T)));
+      n_ = n;
+    }
+    return p_;
+  }
+
+ private:
+  T* p_ = nullptr;
+  size_t n_ = 0;
+};
+
 inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
 // SM count of the current device (looked up once per process).

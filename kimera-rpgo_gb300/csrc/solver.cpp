@@ -79,14 +79,12 @@ void GpuNls::optimize(const LmParams& p, NlsStats* st, bool from_current) {
       ++iters;
     } else {
       while (true) {
-        SolveOut o = solver_solve(s, lambda, st_);
+        double nerr = 0.0;
+        SolveOut o = solver_solve_eval(s, lambda, st_, &nerr);
         st->linear_solves++;
         st->cg_iterations += o.cg_iterations;
         bool success = false, stop_search = false;
-        double nerr = 0.0;
         if (o.ok && o.lin_change >= 0.0) {
-          solver_retract(s, st_);
-          nerr = solver_error(s, s.xnew.get(), s.weights.get(), st_);
           const double cost_change = cur_err - nerr;
           if (o.lin_change > std::numeric_limits<double>::epsilon() * cur_err)
             success = (cost_change / o.lin_change) > p.min_model_fidelity;

@@ -1,10 +1,13 @@
 // Nonlinear least-squares kernels of the robust solve (sm_103a).
 //
-//  K4 linearise      one thread per factor: FP64 residual and exact Jacobians
-//                    (BetweenFactor / PriorFactor as GTSAM evaluates them),
-//                    whitened by sqrt(w) R; FP64 gradient and Hessian blocks
-//                    (J_i^T J_i, J_j^T J_j, J_i^T J_j), plus an FP32 copy of
-//                    the Hessian blocks for the PCG preconditioner.
+//  K4 linearise      FP64 residual and exact Jacobians (BetweenFactor /
+//                    PriorFactor as GTSAM evaluates them), whitened by
+//                    sqrt(w) R; FP64 gradient and Hessian blocks (J_i^T J_i,
+//                    J_j^T J_j, J_i^T J_j), plus an FP32 copy of the Hessian
+//                    blocks for the PCG preconditioner. Phase A one thread
+//                    per factor (residual, Logmap derivative, adjoint), phase
+//                    B d lanes per factor (the Jacobian and Hessian products,
+//                    one row each).
 //  assemble          one thread per variable, fixed factor order (no atomics,
 //                    run-to-run deterministic): diagonal blocks, gradient, the
 //                    odometry-chain preconditioner blocks and the damping
@@ -100,28 +103,46 @@ double device_sum(const double* in, int n, DeviceBuffer<double>& red, cudaStream
 }
 
 // ------------------------------------------------------------------ K4
+// Linearisation of every factor at x (weights w): whitened residual
+// r = sqrt(w) R e, Jacobians (between: J_i = -D Ad(h^-1), J_j = D; prior:
+// J = I), gradient blocks A^T r and Hessian blocks Hii, Hjj, Hij in FP64 and
+// an FP32 copy. Two phases, the Jacobian products spread over d lanes per
+// factor. Phase A, one thread per factor: the
+// whitened residual r (times sqrt(w)), D = LogmapDerivative(e) and
+// Ad(h^-1) into a per-factor record [r (d), D (dd), Ad (dd), sqrt(w)];
+// for priors D and Ad are unused. Phase B, d lanes per factor (lane a owns
+// row a): Ji = -D Ad, Ai = sqrt(w) R Ji, Aj = sqrt(w) R D through shared
+// memory, then gradient entry a and row a of Hii, Hjj, Hij.
 template <int DIM>
-__global__ void k_linearize(int F, const int32_t* __restrict__ kind, const int32_t* __restrict__ vi,
-                            const int32_t* __restrict__ vj, const double* __restrict__ z,
-                            const double* __restrict__ R, const double* __restrict__ x,
-                            const double* __restrict__ w, float* __restrict__ fH, double* __restrict__ fH64,
-                            double* __restrict__ fg) {
+__global__ void k_linearize_a(int F, const int32_t* __restrict__ kind, const int32_t* __restrict__ vi,
+                              const int32_t* __restrict__ vj, const double* __restrict__ z,
+                              const double* __restrict__ R, const double* __restrict__ x,
+                              const double* __restrict__ w, double* __restrict__ rec) {
   using L = SLie<DIM>;
-  constexpr int d = L::d, st = L::stride, dd = d * d;
+  constexpr int d = L::d, st = L::stride, dd = d * d, RS = d + 2 * dd + 1;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= F) return;
   const bool between = kind[f] == 0;
   typename L::Pose Xi, Z, rel, h;
   L::load(x + (size_t)vi[f] * st, Xi);
   L::load(z + (size_t)f * st, Z);
-  double e[d], D[dd];
+  double e[d];
+  double* out = rec + (size_t)f * RS;
   if (between) {
-    typename L::Pose Xj;
+    typename L::Pose Xj, hinv;
     L::load(x + (size_t)vj[f] * st, Xj);
     L::between(Xi, Xj, h);
     L::between(Z, h, rel);
     L::logmap(rel, e);
+    double D[dd], Ad[dd];
     L::dlog(e, D);
+    L::inverse(h, hinv);
+    L::adjoint(hinv, Ad);
+#pragma unroll
+    for (int i = 0; i < dd; ++i) {
+      out[d + i] = D[i];
+      out[d + dd + i] = Ad[i];
+    }
   } else {
     L::between(Xi, Z, rel);
     L::logmap(rel, e);
@@ -130,82 +151,100 @@ __global__ void k_linearize(int F, const int32_t* __restrict__ kind, const int32
   }
   const double sw = sqrt(w[f]);
   const double* Rf = R + (size_t)f * dd;
-  double r[d];
 #pragma unroll
   for (int i = 0; i < d; ++i) {
     double acc = 0.0;
 #pragma unroll
     for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * e[k];
-    r[i] = sw * acc;
+    out[i] = sw * acc;
   }
-  double Ai[dd], Aj[dd];
+  out[d + 2 * dd] = sw;
+}
+
+template <int DIM>
+__global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __restrict__ kind,
+                                                     const double* __restrict__ R, const double* __restrict__ rec,
+                                                     float* __restrict__ fH, double* __restrict__ fH64,
+                                                     double* __restrict__ fg) {
+  constexpr int d = (DIM == 3) ? 6 : 3, dd = d * d, RS = d + 2 * dd + 1;
+  constexpr int per_warp = 32 / d;  // factors per warp
+  constexpr int warps = 4;
+  __shared__ double sJ[warps][per_warp][dd], sA[warps][per_warp][dd], sB[warps][per_warp][dd];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int slot = lane / d, a = lane % d;
+  const int f = (blockIdx.x * warps + warp) * per_warp + slot;
+  const bool active = slot < per_warp && f < F;
+  const double* rc = rec + (size_t)(active ? f : 0) * RS;
+  const double* Rf = R + (size_t)(active ? f : 0) * dd;
+  const bool between = active && kind[f] == 0;
+  double* Ji = sJ[warp][active ? slot : 0];
+  double* Ai = sA[warp][active ? slot : 0];
+  double* Aj = sB[warp][active ? slot : 0];
+  const double sw = active ? rc[d + 2 * dd] : 0.0;
   if (between) {
-    // J_i = -D Ad(h^-1), J_j = D; whitened A = sqrt(w) R J
-    typename L::Pose hinv;
-    L::inverse(h, hinv);
-    double Ad[dd], Ji[dd];
-    L::adjoint(hinv, Ad);
+    const double* D = rc + d;
+    const double* Ad = rc + d + dd;
 #pragma unroll
-    for (int i = 0; i < d; ++i)
+    for (int j = 0; j < d; ++j) {
+      double acc = 0.0;
 #pragma unroll
-      for (int j = 0; j < d; ++j) {
-        double acc = 0.0;
-#pragma unroll
-        for (int k = 0; k < d; ++k) acc += D[d * i + k] * Ad[d * k + j];
-        Ji[d * i + j] = -acc;
-      }
-#pragma unroll
-    for (int i = 0; i < d; ++i)
+      for (int k = 0; k < d; ++k) acc += D[d * a + k] * Ad[d * k + j];
+      Ji[d * a + j] = -acc;
+    }
+  }
+  __syncwarp();
+  if (active) {
+    if (between) {
+      const double* D = rc + d;
 #pragma unroll
       for (int j = 0; j < d; ++j) {
         double ai = 0.0, aj = 0.0;
 #pragma unroll
         for (int k = 0; k < d; ++k) {
-          ai += Rf[d * i + k] * Ji[d * k + j];
-          aj += Rf[d * i + k] * D[d * k + j];
+          ai += Rf[d * a + k] * Ji[d * k + j];
+          aj += Rf[d * a + k] * D[d * k + j];
         }
-        Ai[d * i + j] = sw * ai;
-        Aj[d * i + j] = sw * aj;
+        Ai[d * a + j] = sw * ai;
+        Aj[d * a + j] = sw * aj;
       }
-  } else {
+    } else {
 #pragma unroll
-    for (int i = 0; i < dd; ++i) {
-      Ai[i] = sw * Rf[i];
-      Aj[i] = 0.0;
+      for (int j = 0; j < d; ++j) {
+        Ai[d * a + j] = sw * Rf[d * a + j];
+        Aj[d * a + j] = 0.0;
+      }
     }
+  }
+  __syncwarp();
+  if (!active) return;
+  const double* r = rc;
+  double gi = 0.0, gj = 0.0;
+#pragma unroll
+  for (int i = 0; i < d; ++i) {
+    gi += Ai[d * i + a] * r[i];
+    gj += Aj[d * i + a] * r[i];
   }
   double* og = fg + (size_t)f * 2 * d;
-#pragma unroll
-  for (int j = 0; j < d; ++j) {
-    double gi = 0.0, gj = 0.0;
-#pragma unroll
-    for (int i = 0; i < d; ++i) {
-      gi += Ai[d * i + j] * r[i];
-      gj += Aj[d * i + j] * r[i];
-    }
-    og[j] = gi;
-    og[d + j] = gj;
-  }
+  og[a] = gi;
+  og[d + a] = gj;
   float* out = fH + (size_t)f * 3 * dd;
   double* out64 = fH64 + (size_t)f * 3 * dd;
 #pragma unroll
-  for (int a = 0; a < d; ++a)
+  for (int b = 0; b < d; ++b) {
+    double hii = 0.0, hjj = 0.0, hij = 0.0;
 #pragma unroll
-    for (int b = 0; b < d; ++b) {
-      double hii = 0.0, hjj = 0.0, hij = 0.0;
-#pragma unroll
-      for (int q = 0; q < d; ++q) {
-        hii += Ai[d * q + a] * Ai[d * q + b];
-        hjj += Aj[d * q + a] * Aj[d * q + b];
-        hij += Ai[d * q + a] * Aj[d * q + b];
-      }
-      out64[d * a + b] = hii;
-      out64[dd + d * a + b] = hjj;
-      out64[2 * dd + d * a + b] = hij;
-      out[d * a + b] = (float)hii;
-      out[dd + d * a + b] = (float)hjj;
-      out[2 * dd + d * a + b] = (float)hij;
+    for (int q = 0; q < d; ++q) {
+      hii += Ai[d * q + a] * Ai[d * q + b];
+      hjj += Aj[d * q + a] * Aj[d * q + b];
+      hij += Ai[d * q + a] * Aj[d * q + b];
     }
+    out64[d * a + b] = hii;
+    out64[dd + d * a + b] = hjj;
+    out64[2 * dd + d * a + b] = hij;
+    out[d * a + b] = (float)hii;
+    out[dd + d * a + b] = (float)hjj;
+    out[2 * dd + d * a + b] = (float)hij;
+  }
 }
 
 template <int D>
@@ -1094,14 +1133,22 @@ void solver_factor_errors(SolverDev& s, const double* x, std::vector<double>* ou
 void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
   const int tb = 128;
   if (s.F > 0) {
-    if (s.dim == 3)
-      k_linearize<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
-                                                     s.sqrt_info.get(), s.x.get(), s.weights.get(), s.fH.get(),
-                                                     s.fH64.get(), s.fg.get());
-    else
-      k_linearize<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
-                                                     s.sqrt_info.get(), s.x.get(), s.weights.get(), s.fH.get(),
-                                                     s.fH64.get(), s.fg.get());
+    const int d = s.d, rs = d + 2 * d * d + 1;
+    s.lin_rec.resize((size_t)s.F * rs);
+    const int per_block = 4 * (32 / d);  // k_linearize_b: 4 warps of 32/d factors
+    if (s.dim == 3) {
+      k_linearize_a<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                       s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get());
+      RPGO_LAUNCHED();
+      k_linearize_b<3><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
+                                                               s.fH.get(), s.fH64.get(), s.fg.get());
+    } else {
+      k_linearize_a<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                       s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get());
+      RPGO_LAUNCHED();
+      k_linearize_b<2><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
+                                                               s.fH.get(), s.fH64.get(), s.fg.get());
+    }
     RPGO_LAUNCHED();
   }
   if (s.dim == 3)
@@ -1542,6 +1589,44 @@ SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
   o.ok = (int)h[1];
   o.cg_iterations = (int)h[2];
   o.rel_residual = h[3];
+  return o;
+}
+
+SolveOut solver_solve_eval(SolverDev& s, double lambda, cudaStream_t st, double* nerr) {
+  if (!s.chol) {
+    SolveOut o = solver_solve(s, lambda, st);
+    if (o.ok && o.lin_change >= 0.0) {
+      solver_retract(s, st);
+      *nerr = solver_error(s, s.xnew.get(), s.weights.get(), st);
+    }
+    return o;
+  }
+  double* host = s.pin.get(3);
+  chol_enqueue(s, *s.chol, lambda, st, host);
+  // the candidate step and its cost, whatever the solve's outcome (unused
+  // when it failed)
+  solver_retract(s, st);
+  host[2] = 0.0;
+  if (s.F > 0) {
+    const int tb = 128;
+    if (s.dim == 3)
+      k_factor_err<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                      s.sqrt_info.get(), s.xnew.get(), s.weights.get(), s.ferr.get());
+    else
+      k_factor_err<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                      s.sqrt_info.get(), s.xnew.get(), s.weights.get(), s.ferr.get());
+    RPGO_LAUNCHED();
+    const int blocks = std::min(256, div_up(s.F, 256));
+    s.red.resize(blocks + 1);
+    k_sum_partial<<<blocks, 256, 0, st>>>(s.F, s.ferr.get(), s.red.get());
+    RPGO_LAUNCHED();
+    k_sum_partial<<<1, 256, 0, st>>>(blocks, s.red.get(), s.red.get() + blocks);
+    RPGO_LAUNCHED();
+    RPGO_CUDA(cudaMemcpyAsync(host + 2, s.red.get() + blocks, sizeof(double), cudaMemcpyDeviceToHost, st));
+  }
+  RPGO_CUDA(cudaStreamSynchronize(st));
+  SolveOut o = chol_finish(s, *s.chol, host);
+  *nerr = host[2];
   return o;
 }
 

@@ -32,6 +32,7 @@ struct SolverDev {
   DeviceBuffer<float> fH;      // F x 3 x dd (Hii, Hjj, Hij), FP32 copy for CG and preconditioner
   DeviceBuffer<double> fH64;   // the same blocks in FP64 for the refinement residual
   DeviceBuffer<double> fg;     // F x 2 x d
+  DeviceBuffer<double> lin_rec;  // F x (d + 2 dd + 1): linearisation phase-A records
   DeviceBuffer<float> Hd, Md, Mu;  // N x dd, N x dd, N x dd (Mu[v] couples v, v+1)
   DeviceBuffer<double> Hd64;       // N x dd
   DeviceBuffer<double> g, dampD;   // N x d
@@ -52,6 +53,7 @@ struct SolverDev {
   int levels = 0;
   // direct solver (sparse Cholesky); null when the PCG path solves
   std::shared_ptr<CholDev> chol;
+  PinnedBuffer<double> pin;  // host words of solve_eval's single readback
 };
 
 struct SolveOut {
@@ -75,6 +77,10 @@ void solver_factor_errors(SolverDev& s, const double* x, std::vector<double>* ou
 void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st);
 // solve (H + lambda D) delta = -g into s.delta
 SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st);
+// solve, then xnew = x (+) delta and its weighted error *nerr (valid when
+// the solve succeeded with a non-negative model change); with the direct
+// solver the three results come back in one synchronisation
+SolveOut solver_solve_eval(SolverDev& s, double lambda, cudaStream_t st, double* nerr);
 // xnew = x (+) delta
 void solver_retract(SolverDev& s, cudaStream_t st);
 // TLS weights (GncOptimizer::calculateWeights) for factors >= n_known
