@@ -258,7 +258,10 @@ __global__ void k_odom_prep(int64_t count, const double* __restrict__ dpose, con
   }
 }
 
-// One warp walks the odometry list in order.
+// One warp walks the odometry list in order. The step constants of step k+1
+// (odometry pose, Ad(Delta^-1) pieces, covariance, indices) are loaded into
+// registers while step k computes and land in shared memory at its end, so
+// the walk waits on memory only when a chain restarts from an older pose.
 template <int DIM, int MODE>
 __global__ void __launch_bounds__(32) k_traj_scan(int64_t count, const int32_t* __restrict__ src,
                                                   const int32_t* __restrict__ dst, const double* __restrict__ dpose,
@@ -268,14 +271,46 @@ __global__ void __launch_bounds__(32) k_traj_scan(int64_t count, const int32_t* 
   using L = Lie<DIM>;
   constexpr int d = L::d, st = L::stride, dd = d * d;
   constexpr int REC = (DIM == 3) ? 21 : 9;
+  constexpr int NC = st + ((MODE == 0) ? REC + dd : 0);  // step constants
+  constexpr int NQ = (NC + 31) / 32;
   __shared__ double prev_pose[12], prev_cov[36], M[36], newp[12], rec[21], dpz[12], dc[36];
   __shared__ int prev_node;
   __shared__ uint8_t prev_rot;
   const int lane = threadIdx.x;
+  double pre[NQ];
+  int32_t ps = 0, pt = 0;
+  uint8_t prot = 0;
+  auto load_step = [&](int64_t k) {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const int e = lane + 32 * q;
+      if (e < st) pre[q] = dpose[k * st + e];
+      else if (MODE == 0 && e < st + REC) pre[q] = inv_rec[k * REC + (e - st)];
+      else if (MODE == 0 && e < NC) pre[q] = dcov_p[k * dd + (e - st - REC)];
+    }
+    ps = src[k];
+    pt = dst[k];
+    prot = drot[k];
+  };
+  auto store_step = [&]() {
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      const int e = lane + 32 * q;
+      if (e < st) dpz[e] = pre[q];
+      else if (MODE == 0 && e < st + REC) rec[e - st] = pre[q];
+      else if (MODE == 0 && e < NC) dc[e - st - REC] = pre[q];
+    }
+  };
   int32_t last_dst = -1;
+  if (count > 0) {
+    load_step(0);
+    store_step();
+  }
+  int32_t s = ps, t = pt;
+  uint8_t rot_k = prot;
   for (int64_t k = 0; k < count; ++k) {
-    const int32_t s = src[k], t = dst[k];
-    // load previous state (unless it is the pose just written) and the step constants
+    if (k + 1 < count) load_step(k + 1);
+    // load previous state (unless it is the pose just written)
     if (s != last_dst) {
       for (int e = lane; e < st; e += 32) prev_pose[e] = tr.pose[(size_t)s * st + e];
       if (MODE == 0)
@@ -284,11 +319,6 @@ __global__ void __launch_bounds__(32) k_traj_scan(int64_t count, const int32_t* 
         prev_rot = tr.rot[s];
         if (MODE == 1) prev_node = tr.node[s];
       }
-    }
-    for (int e = lane; e < st; e += 32) dpz[e] = dpose[k * st + e];
-    if (MODE == 0) {
-      for (int e = lane; e < REC; e += 32) rec[e] = inv_rec[k * REC + e];
-      for (int e = lane; e < dd; e += 32) dc[e] = dcov_p[k * dd + e];
     }
     __syncwarp();
     // phase 1: M = Ad(Delta^-1) S_prev (items [0, dd)) and the new pose
@@ -330,7 +360,7 @@ __global__ void __launch_bounds__(32) k_traj_scan(int64_t count, const int32_t* 
     }
     for (int e = lane; e < st; e += 32) prev_pose[e] = newp[e];
     if (lane == 0) {
-      prev_rot = (prev_rot && (MODE == 0 ? drot[k] : drot[k])) ? 1 : 0;
+      prev_rot = (prev_rot && rot_k) ? 1 : 0;
       if (MODE == 1) prev_node = prev_node + 1;
     }
     __syncwarp();
@@ -342,6 +372,13 @@ __global__ void __launch_bounds__(32) k_traj_scan(int64_t count, const int32_t* 
       if (MODE == 1) tr.node[t] = prev_node;
     }
     last_dst = t;
+    __syncwarp();
+    if (k + 1 < count) {
+      store_step();
+      s = ps;
+      t = pt;
+      rot_k = prot;
+    }
     __syncwarp();
   }
 }

@@ -308,6 +308,38 @@ __global__ void k_assemble(int N, const int32_t* __restrict__ inc_ptr, const int
   }
 }
 
+// Assembly for the direct solver: one warp per variable, lane e owning the
+// block entries e and e + 32 (and gradient entry e < D); the same sums in the
+// same factor order as k_assemble (identical FP64 results), without the FP32
+// preconditioner blocks, which only the PCG path reads.
+template <int D>
+__global__ void k_assemble_direct(int N, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc_fac,
+                                  const int8_t* __restrict__ inc_role, const double* __restrict__ fH64,
+                                  const double* __restrict__ fg, double* __restrict__ Hd64, double* __restrict__ g,
+                                  double* __restrict__ dampD, int diag_damping) {
+  constexpr int dd = D * D;
+  const int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (v >= N) return;
+  const int e0 = lane, e1 = lane + 32;
+  double h0 = 0.0, h1 = 0.0, gv = 0.0;
+  for (int k = inc_ptr[v]; k < inc_ptr[v + 1]; ++k) {
+    const int f = inc_fac[k];
+    const int role = inc_role[k];
+    const double* blk = fH64 + (size_t)f * 3 * dd + (role == 1 ? dd : 0);
+    if (e0 < dd) h0 += blk[e0];
+    if (e1 < dd) h1 += blk[e1];
+    if (lane < D) gv += fg[(size_t)f * 2 * D + role * D + lane];
+  }
+  if (e0 < dd) Hd64[(size_t)v * dd + e0] = h0;
+  if (e1 < dd) Hd64[(size_t)v * dd + e1] = h1;
+  if (lane < D) g[(size_t)v * D + lane] = gv;
+  // diagonal entries: e = D i + i
+  if (e0 < dd && e0 % (D + 1) == 0)
+    dampD[(size_t)v * D + e0 / (D + 1)] = diag_damping ? fmin(fmax(h0, 1e-6), 1e32) : 1.0;
+  if (e1 < dd && e1 % (D + 1) == 0)
+    dampD[(size_t)v * D + e1 / (D + 1)] = diag_damping ? fmin(fmax(h1, 1e-6), 1e32) : 1.0;
+}
+
 // ------------------------------------------------------------------ small dense (FP32)
 template <int D>
 __device__ bool chol_f(const float* A, float* L) {
@@ -1150,6 +1182,19 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
                                                                s.fH.get(), s.fH64.get(), s.fg.get());
     }
     RPGO_LAUNCHED();
+  }
+  if (s.chol) {
+    const int blocks = div_up((int64_t)s.N * 32, tb);
+    if (s.dim == 3)
+      k_assemble_direct<6><<<blocks, tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
+                                                  s.fH64.get(), s.fg.get(), s.Hd64.get(), s.g.get(), s.dampD.get(),
+                                                  diagonal_damping ? 1 : 0);
+    else
+      k_assemble_direct<3><<<blocks, tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
+                                                  s.fH64.get(), s.fg.get(), s.Hd64.get(), s.g.get(), s.dampD.get(),
+                                                  diagonal_damping ? 1 : 0);
+    RPGO_LAUNCHED();
+    return;
   }
   if (s.dim == 3)
     k_assemble<6><<<div_up(s.N, tb), tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
