@@ -729,7 +729,11 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
       sg += __shfl_xor_sync(kFull, sg, o);
       sq += __shfl_xor_sync(kFull, sq, o);
     }
-    if (threadIdx.x == 0) a.out[0] = -0.5 * sg + 0.5 * a.lam * sq;
+    if (threadIdx.x == 0) {
+      a.out[0] = -0.5 * sg + 0.5 * a.lam * sq;
+      // every block's pivot failures were flagged before the last barrier
+      a.out[1] = (double)atomicAdd(a.status, 0);
+    }
   }
 }
 
@@ -780,12 +784,6 @@ CholDev::~CholDev() {
     if (e) cudaEventDestroy(e);
 }
 
-namespace {
-__global__ void k_status_to_double(const int32_t* __restrict__ status, double* __restrict__ out) {
-  out[1] = (double)*status;
-}
-}  // namespace
-
 void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, double* host) {
   if (s.N == 0) {
     host[0] = 0.0;
@@ -816,8 +814,6 @@ void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, doub
     RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_chol_solve<3>, grid, kThreads, args, 0, st));
   RPGO_LAUNCHED();
   RPGO_CUDA(cudaEventRecord(c.ev[1], st));
-  k_status_to_double<<<1, 1, 0, st>>>(c.status.get(), c.out.get());
-  RPGO_LAUNCHED();
   RPGO_CUDA(cudaMemcpyAsync(host, c.out.get(), 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
 }
 
