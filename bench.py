@@ -127,11 +127,19 @@ def max_over_ranks(dist, x):
     return float(t.item())
 
 
-def make_workload():
+WORKLOADS = {
+    "walk3d_5000": ("3d random walk, 5000 poses, 1000 inlier + 333 outlier loop closures, PCM3D(10,5) + "
+                    "GNC-TLS(p=0.9)", 5000, 1333, 0.25),
+    "walk3d_50000": ("3d random walk, 50000 poses, 14000 inlier + 6000 outlier loop closures (2e8 pair checks), "
+                     "PCM3D(10,5) + GNC-TLS(p=0.9)", 50000, 20000, 0.30),
+}
+
+
+def make_workload(name="walk3d_5000"):
     from rpgo_gb300 import synth
     from rpgo_gb300.params import QUIET, RobustSolverParams
 
-    s = synth.config_c2()
+    s = synth.config_c2() if name == "walk3d_5000" else synth.config_c3()
     p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
     return s, p
 
@@ -146,7 +154,8 @@ def run_gb300(args):
     dist, rank, world, local = dist_setup(args.gpus)
     build()
     capi.load()
-    s, params = make_workload()
+    s, params = make_workload(args.workload)
+    desc, n_poses, n_lc, out_frac = WORKLOADS[args.workload]
     dev_batch = capi.DeviceBatch(s.graph)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
@@ -259,7 +268,7 @@ def run_gb300(args):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded 3d random walk; no public dataset in the reference)",
-        "config": {"workload": WORKLOAD, "graph_poses": 5000, "loop_closures": 1333, "outlier_fraction": 0.25,
+        "config": {"workload": desc, "graph_poses": n_poses, "loop_closures": n_lc, "outlier_fraction": out_frac,
                    "solver": "GNC-TLS over LM", "l2": "flushed between steps (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "solve_ms": sum(solve_ms) / len(solve_ms),
@@ -283,10 +292,10 @@ def run_gb300(args):
                      "fp64_peak_nominal_gflops": FP64_NOMINAL_GFLOPS},
         "clocks": clocks.summary(),
     }
-    if world == 1 and not args.no_extras:
+    if world == 1 and not args.no_extras and args.workload == "walk3d_5000":
         line["warm_start"] = warm_start_leg(args, params, dev_batch, g_ref=g, plain_ms=ms, flush=flush)
         line["batched"] = batched_leg(params)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.workload == "walk3d_5000":
         line["cpu_baseline"] = cpu_baseline(gnc_iters=int(last.gnc_iterations))
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -498,6 +507,53 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch512(args):
+    """The batched workload: 512 graphs (seed 4: 3d random walks of 200-8000
+    poses, closures 10-30 % of the poses, outlier rate U[0, 0.5]) through
+    rpgo_solve_batch; one step = 64 consecutive graphs of the 512 (steps 8
+    cover them all), timed host to host. Every step's graphs are new to the
+    device (their measurements arrive from host memory), so no L2 flush is
+    needed."""
+    import concurrent.futures as cf
+    import multiprocessing
+
+    import torch
+
+    from rpgo_gb300 import build, capi, synth
+    from rpgo_gb300.params import QUIET, RobustSolverParams
+
+    build()
+    capi.load()
+    params = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+    sizes = synth.config_c4_sizes(512)
+    with cf.ProcessPoolExecutor(8, mp_context=multiprocessing.get_context("spawn")) as ex:
+        graphs = list(ex.map(_c4_graph, sizes, chunksize=4))
+    per = 64
+    chunks = [graphs[i:i + per] for i in range(0, 512, per)]
+    for w in range(args.warmup):
+        capi.solve_batch(params, chunks[w % len(chunks)][:16], workers=args.workers)
+    times, n = [], 0
+    with ClockSampler(0) as clocks:
+        for k in range(args.steps):
+            chunk = chunks[k % len(chunks)]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = capi.solve_batch(params, chunk, workers=args.workers)
+            times.append(time.perf_counter() - t0)
+            assert all(r[0] == 0 for r in res)
+            n += len(chunk)
+    sec = sum(times)
+    line = {"metric": METRIC, "value": n / sec, "unit": "graphs/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * sec / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded 3d random walks)",
+            "config": {"workload": "batch of 512 independent graphs (200-8000 poses, closures 10-30 %, outlier rate "
+                                   "U[0, 0.5]); a step = 64 graphs through rpgo_solve_batch",
+                       "graphs_timed": n, "poses_timed": int(sum(sz[0] for sz in sizes[:n])) if n <= 512 else None,
+                       "workers": args.workers, "parallelism": "single GPU, concurrent graphs"},
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -506,11 +562,16 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the warm-start and batched legs")
+    ap.add_argument("--workload", default="walk3d_5000", choices=["walk3d_5000", "walk3d_50000", "batch512"],
+                    help="walk3d_5000: the benchmark graph (default); the others are separate measurements")
+    ap.add_argument("--workers", type=int, default=8, help="host threads of the batch512 workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch512":
+        run_batch512(args)
     else:
         run_gb300(args)
 
