@@ -530,15 +530,20 @@ def run_batch512(args):
         graphs = list(ex.map(_c4_graph, sizes, chunksize=4))
     per = 64
     chunks = [graphs[i:i + per] for i in range(0, 512, per)]
+    tuned = None
+    if args.workers <= 0:
+        # autotune workers and CTA budget on 24 graphs drawn from across the batch
+        w_, c_, tuned = capi.autotune_batch(params, graphs[::21][:24])
+        args.workers, args.coop_ctas = w_, c_
     for w in range(args.warmup):
-        capi.solve_batch(params, chunks[w % len(chunks)][:16], workers=args.workers)
+        capi.solve_batch(params, chunks[w % len(chunks)][:16], workers=args.workers, coop_ctas=args.coop_ctas)
     times, n = [], 0
     with ClockSampler(0) as clocks:
         for k in range(args.steps):
             chunk = chunks[k % len(chunks)]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            res = capi.solve_batch(params, chunk, workers=args.workers)
+            res = capi.solve_batch(params, chunk, workers=args.workers, coop_ctas=args.coop_ctas)
             times.append(time.perf_counter() - t0)
             assert all(r[0] == 0 for r in res)
             n += len(chunk)
@@ -549,7 +554,9 @@ def run_batch512(args):
             "config": {"workload": "batch of 512 independent graphs (200-8000 poses, closures 10-30 %, outlier rate "
                                    "U[0, 0.5]); a step = 64 graphs through rpgo_solve_batch",
                        "graphs_timed": n, "poses_timed": int(sum(sz[0] for sz in sizes[:n])) if n <= 512 else None,
-                       "workers": args.workers, "parallelism": "single GPU, concurrent graphs"},
+                       "workers": args.workers, "coop_ctas": args.coop_ctas,
+                       "autotune_s": {f"{w}x{c}": round(t, 3) for (w, c), t in tuned.items()} if tuned else None,
+                       "parallelism": "single GPU, concurrent graphs"},
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
 
@@ -564,7 +571,9 @@ def main():
     ap.add_argument("--no-extras", action="store_true", help="skip the warm-start and batched legs")
     ap.add_argument("--workload", default="walk3d_5000", choices=["walk3d_5000", "walk3d_50000", "batch512"],
                     help="walk3d_5000: the benchmark graph (default); the others are separate measurements")
-    ap.add_argument("--workers", type=int, default=8, help="host threads of the batch512 workload")
+    ap.add_argument("--workers", type=int, default=0,
+                    help="host threads of the batch512 workload (0: autotuned with the CTA budget)")
+    ap.add_argument("--coop-ctas", dest="coop_ctas", type=int, default=0, help="batch512: CTAs per direct solve")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

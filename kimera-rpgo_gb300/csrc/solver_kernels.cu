@@ -75,6 +75,68 @@ __global__ void k_factor_err(int F, const int32_t* __restrict__ kind, const int3
   ferr[f] = 0.5 * (w ? w[f] : 1.0) * s;
 }
 
+// Per-factor errors at x and their sum in one launch: each block sums its
+// grid-stride share (fixed tree order) into part[block]; the last block to
+// finish (ticket counter, reset for the next launch) adds the partials in
+// block order into *sum, so the result does not depend on scheduling.
+template <int DIM>
+__global__ void __launch_bounds__(256) k_factor_err_sum(int F, const int32_t* __restrict__ kind,
+                                                        const int32_t* __restrict__ vi,
+                                                        const int32_t* __restrict__ vj, const double* __restrict__ z,
+                                                        const double* __restrict__ R, const double* __restrict__ x,
+                                                        const double* __restrict__ w, double* __restrict__ part,
+                                                        unsigned int* __restrict__ ticket, double* __restrict__ sum) {
+  using L = SLie<DIM>;
+  constexpr int d = L::d, st = L::stride;
+  __shared__ double sh[256];
+  __shared__ bool last;
+  double acc = 0.0;
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += gridDim.x * blockDim.x) {
+    typename L::Pose Xi, Z, rel;
+    L::load(x + (size_t)vi[f] * st, Xi);
+    L::load(z + (size_t)f * st, Z);
+    double e[d];
+    if (kind[f] == 0) {
+      typename L::Pose Xj, h;
+      L::load(x + (size_t)vj[f] * st, Xj);
+      L::between(Xi, Xj, h);
+      L::between(Z, h, rel);
+    } else {
+      L::between(Xi, Z, rel);
+    }
+    L::logmap(rel, e);
+    const double* Rf = R + (size_t)f * d * d;
+    double s2 = 0.0;
+#pragma unroll
+    for (int i = 0; i < d; ++i) {
+      double a = 0.0;
+#pragma unroll
+      for (int k = 0; k < d; ++k) a += Rf[d * i + k] * e[k];
+      s2 += a * a;
+    }
+    acc += 0.5 * (w ? w[f] : 1.0) * s2;
+  }
+  sh[threadIdx.x] = acc;
+  __syncthreads();
+  for (int o = 128; o; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = sh[0];
+    __threadfence();
+    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last && threadIdx.x == 0) {
+    __threadfence();
+    double t = 0.0;
+    for (int b = 0; b < (int)gridDim.x; ++b) t += ((volatile double*)part)[b];
+    *sum = t;
+    *ticket = 0u;
+  }
+}
+
 __global__ void k_sum_partial(int n, const double* __restrict__ in, double* __restrict__ out) {
   __shared__ double sh[256];
   double v = 0.0;
@@ -1134,17 +1196,33 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   }
 }
 
+// enqueue k_factor_err_sum: the sum lands in s.red[blocks]
+static double* enqueue_error_sum(SolverDev& s, const double* x, const double* weights, cudaStream_t st) {
+  const int blocks = std::min(256, div_up(s.F, 256));
+  if (s.ticket.size() == 0) {
+    s.ticket.resize(1);
+    s.ticket.zero(st);
+  }
+  s.red.resize(blocks + 1);
+  if (s.dim == 3)
+    k_factor_err_sum<3><<<blocks, 256, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                s.sqrt_info.get(), x, weights, s.red.get(), s.ticket.get(),
+                                                s.red.get() + blocks);
+  else
+    k_factor_err_sum<2><<<blocks, 256, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                s.sqrt_info.get(), x, weights, s.red.get(), s.ticket.get(),
+                                                s.red.get() + blocks);
+  RPGO_LAUNCHED();
+  return s.red.get() + blocks;
+}
+
 double solver_error(SolverDev& s, const double* x, const double* weights, cudaStream_t st) {
   if (s.F == 0) return 0.0;
-  const int tb = 128;
-  if (s.dim == 3)
-    k_factor_err<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
-                                                    s.sqrt_info.get(), x, weights, s.ferr.get());
-  else
-    k_factor_err<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
-                                                    s.sqrt_info.get(), x, weights, s.ferr.get());
-  RPGO_LAUNCHED();
-  return device_sum(s.ferr.get(), s.F, s.red, st);
+  const double* sum = enqueue_error_sum(s, x, weights, st);
+  double h = 0.0;
+  RPGO_CUDA(cudaMemcpyAsync(&h, sum, sizeof(double), cudaMemcpyDeviceToHost, st));
+  RPGO_CUDA(cudaStreamSynchronize(st));
+  return h;
 }
 
 void solver_factor_errors(SolverDev& s, const double* x, std::vector<double>* out, cudaStream_t st) {
@@ -1653,21 +1731,8 @@ SolveOut solver_solve_eval(SolverDev& s, double lambda, cudaStream_t st, double*
   solver_retract(s, st);
   host[2] = 0.0;
   if (s.F > 0) {
-    const int tb = 128;
-    if (s.dim == 3)
-      k_factor_err<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
-                                                      s.sqrt_info.get(), s.xnew.get(), s.weights.get(), s.ferr.get());
-    else
-      k_factor_err<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
-                                                      s.sqrt_info.get(), s.xnew.get(), s.weights.get(), s.ferr.get());
-    RPGO_LAUNCHED();
-    const int blocks = std::min(256, div_up(s.F, 256));
-    s.red.resize(blocks + 1);
-    k_sum_partial<<<blocks, 256, 0, st>>>(s.F, s.ferr.get(), s.red.get());
-    RPGO_LAUNCHED();
-    k_sum_partial<<<1, 256, 0, st>>>(blocks, s.red.get(), s.red.get() + blocks);
-    RPGO_LAUNCHED();
-    RPGO_CUDA(cudaMemcpyAsync(host + 2, s.red.get() + blocks, sizeof(double), cudaMemcpyDeviceToHost, st));
+    const double* sum = enqueue_error_sum(s, s.xnew.get(), s.weights.get(), st);
+    RPGO_CUDA(cudaMemcpyAsync(host + 2, sum, sizeof(double), cudaMemcpyDeviceToHost, st));
   }
   RPGO_CUDA(cudaStreamSynchronize(st));
   SolveOut o = chol_finish(s, *s.chol, host);

@@ -41,6 +41,7 @@ struct SolverDev {
   DeviceBuffer<double> delta;        // N x d
   DeviceBuffer<double> ferr;         // F (per-factor error)
   DeviceBuffer<double> red;          // reduction scratch
+  DeviceBuffer<unsigned int> ticket; // last-block counter of the one-launch error sum
   // preconditioner (block cyclic reduction) and CG scratch
   std::vector<int32_t> lvl_off, lvl_n;
   DeviceBuffer<int32_t> d_lvl_off, d_lvl_n;

@@ -415,6 +415,24 @@ def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0):
     return res
 
 
+def autotune_batch(params, graphs, candidates=((4, 0), (6, 0), (8, 0), (12, 0), (8, 76), (8, 19))):
+    """Pick the (workers, coop_ctas) of rpgo_solve_batch that solves a sample
+    of graphs fastest (wall clock, after one warm-up run of the sample).
+    Returns (workers, coop_ctas, {config: seconds})."""
+    import time
+
+    solve_batch(params, graphs[:2], workers=2)
+    times = {}
+    for w, c in candidates:
+        t0 = time.perf_counter()
+        res = solve_batch(params, graphs, workers=w, coop_ctas=c)
+        times[(w, c)] = time.perf_counter() - t0
+        if any(r[0] != 0 for r in res):
+            raise RpgoError(f"rpgo_solve_batch failed with workers={w}, coop_ctas={c}")
+    best = min(times, key=times.get)
+    return best[0], best[1], times
+
+
 def pairwise_adjacency(dim, mode, slot_a, slot_b, flip, z_pose, z_cov, traj_pose, traj_cov, traj_node, traj_rot,
                        th0, th1):
     n = len(slot_a)
