@@ -415,10 +415,12 @@ def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0):
     return res
 
 
-def autotune_batch(params, graphs, candidates=((4, 0), (6, 0), (8, 0), (12, 0), (8, 76), (8, 19))):
+def autotune_batch(params, graphs, candidates=((8, 0), (4, 0), (6, 0), (12, 0), (8, 76), (8, 19)), margin=0.05):
     """Pick the (workers, coop_ctas) of rpgo_solve_batch that solves a sample
-    of graphs fastest (wall clock, after one warm-up run of the sample).
-    Returns (workers, coop_ctas, {config: seconds})."""
+    of graphs fastest (wall clock, after one warm-up run of the sample); the
+    first candidate is kept unless another is faster by more than `margin`
+    (timing noise on a small sample). Returns (workers, coop_ctas,
+    {config: seconds})."""
     import time
 
     solve_batch(params, graphs[:2], workers=2)
@@ -430,6 +432,8 @@ def autotune_batch(params, graphs, candidates=((4, 0), (6, 0), (8, 0), (12, 0), 
         if any(r[0] != 0 for r in res):
             raise RpgoError(f"rpgo_solve_batch failed with workers={w}, coop_ctas={c}")
     best = min(times, key=times.get)
+    if times[best] > (1.0 - margin) * times[candidates[0]]:
+        best = candidates[0]
     return best[0], best[1], times
 
 
