@@ -2,7 +2,6 @@
 #include "chol_plan.hpp"
 
 #include <algorithm>
-#include <limits>
 #include <cmath>
 #include <functional>
 #include <queue>
@@ -16,11 +15,6 @@ namespace {
 // time model of the solve kernel (per grid-barrier phase, per FP64 flop)
 constexpr double kPhaseUs = 8.0;
 constexpr double kUsPerFlop = 5e-6;
-// extra dense-tail work per pair of tiles (trailing updates of the tiled
-// tail run one tile per CTA)
-constexpr double kTileUs = 0.5;
-// dense-tail lengths tried beyond the structurally complete tail (variables)
-constexpr int kTailExtra[] = {0, 2, 4, 8, 12, 16, 24, 32};
 
 // Elimination game on the variable graph: eliminating u records its current
 // neighbours (the structure of its column of L, as variables) and joins them
@@ -303,35 +297,22 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
       for (int v : col_vars[c.perm[j]]) c.cols[j].push_back(c.pos[v]);
       std::sort(c.cols[j].begin(), c.cols[j].end());
     }
-    // dense tail: at least the trailing columns whose structure is complete;
-    // a longer tail also takes the top of the elimination tree (its columns
-    // only connect to later ones, so any suffix of the order is a valid
-    // tail), trading sparse levels for dense tiles
-    int t_nat = 0;
-    while (t_nat < N && (int)c.cols[N - 1 - t_nat].size() == t_nat) ++t_nat;
-    c.cost = std::numeric_limits<double>::infinity();
-    for (int extra : kTailExtra) {
-      const int T = std::min(N, t_nat + extra);
-      const int ns = N - T;
-      std::vector<int32_t> lvl(ns, 0);
-      int L = 0;
-      double pairs = 0.0;
-      for (int j = 0; j < ns; ++j) {
-        L = std::max(L, lvl[j] + 1);
-        if (!c.cols[j].empty() && c.cols[j][0] < ns) lvl[c.cols[j][0]] = std::max(lvl[c.cols[j][0]], lvl[j] + 1);
-        const double m = (double)c.cols[j].size();
-        pairs += m * (m + 1) / 2;
-      }
-      const double nt = (double)T * d, dd3 = (double)d * d * d;
-      const double tiles = std::ceil(nt / p.tile);
-      const double flops = 2.0 * dd3 * pairs + nt * nt * nt / 3.0;
-      const double cost = (3.0 * L + 2.0 * tiles + 4.0) * kPhaseUs + tiles * tiles * kTileUs + flops * kUsPerFlop;
-      if (cost < c.cost) {
-        c.cost = cost;
-        c.T = T;
-      }
-      if (T == N) break;
+    // dense tail: the trailing columns whose structure is complete
+    while (c.T < N && (int)c.cols[N - 1 - c.T].size() == c.T) ++c.T;
+    const int ns = N - c.T;
+    std::vector<int32_t> lvl(ns, 0);
+    int L = 0;
+    double pairs = 0.0;
+    for (int j = 0; j < ns; ++j) {
+      L = std::max(L, lvl[j] + 1);
+      if (!c.cols[j].empty() && c.cols[j][0] < ns) lvl[c.cols[j][0]] = std::max(lvl[c.cols[j][0]], lvl[j] + 1);
+      const double m = (double)c.cols[j].size();
+      pairs += m * (m + 1) / 2;
     }
+    const double nt = (double)c.T * d, dd3 = (double)d * d * d;
+    const double tiles = std::ceil(nt / p.tile);
+    const double flops = 2.0 * dd3 * pairs + nt * nt * nt / 3.0;
+    c.cost = (3.0 * L + 2.0 * tiles + 4.0) * kPhaseUs + flops * kUsPerFlop;
     return c;
   };
   std::vector<Candidate> cands;
