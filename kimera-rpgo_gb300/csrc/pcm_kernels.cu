@@ -301,6 +301,34 @@ __global__ void __launch_bounds__(32) k_traj_scan(int64_t count, const int32_t* 
       else if (MODE == 0 && e < NC) dc[e - st - REC] = pre[q];
     }
   };
+  // this lane's phase-1 items (e = lane, lane + 32 of [M entries | pose
+  // entries]) and phase-2 entry (ii, jj) of the lower triangle, fixed for
+  // the whole walk
+  constexpr int nm = (MODE == 0) ? dd : 0;
+  int it_i[2], it_k[2], it_pl[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int e = lane + 32 * q;
+    it_i[q] = -1;
+    it_k[q] = 0;
+    it_pl[q] = -1;
+    if (e < nm) {
+      it_i[q] = e / d;
+      it_k[q] = e % d;
+    } else if (e < nm + st) {
+      it_pl[q] = e - nm;
+    }
+  }
+  constexpr int ntri = d * (d + 1) / 2;
+  int tri_i = 0, tri_j = 0;
+  if (lane < ntri) {
+    int idx = lane;
+    while (idx > tri_i) {
+      idx -= tri_i + 1;
+      ++tri_i;
+    }
+    tri_j = idx;
+  }
   int32_t last_dst = -1;
   if (count > 0) {
     load_step(0);
@@ -322,31 +350,22 @@ __global__ void __launch_bounds__(32) k_traj_scan(int64_t count, const int32_t* 
     }
     __syncwarp();
     // phase 1: M = Ad(Delta^-1) S_prev (items [0, dd)) and the new pose
-    {
-      constexpr int nm = (MODE == 0) ? dd : 0;
-      for (int e = lane; e < nm + st; e += 32) {
-        if (e < nm) {
-          const int i = e / d, kk = e % d;
-          if constexpr (DIM == 3) M[e] = p3_M_elem(rec, rec + 9, prev_cov, i, kk);
-          else M[e] = p2_M_elem(rec, prev_cov, i, kk);
-        } else {
-          const int pl = e - nm;
-          if constexpr (DIM == 3) newp[pl] = p3_compose_elem(prev_pose, dpz, pl);
-          else newp[pl] = p2_compose_elem(prev_pose, dpz, pl);
-        }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (it_i[q] >= 0) {
+        if constexpr (DIM == 3) M[lane + 32 * q] = p3_M_elem(rec, rec + 9, prev_cov, it_i[q], it_k[q]);
+        else M[lane + 32 * q] = p2_M_elem(rec, prev_cov, it_i[q], it_k[q]);
+      } else if (it_pl[q] >= 0) {
+        if constexpr (DIM == 3) newp[it_pl[q]] = p3_compose_elem(prev_pose, dpz, it_pl[q]);
+        else newp[it_pl[q]] = p2_compose_elem(prev_pose, dpz, it_pl[q]);
       }
     }
     __syncwarp();
     // phase 2: lower triangle of M Ad^T + S_Delta
     if (MODE == 0) {
-      constexpr int ntri = d * (d + 1) / 2;
       double v = 0.0;
-      int ii = 0, jj = 0;
+      const int ii = tri_i, jj = tri_j;
       if (lane < ntri) {
-        int idx = lane;
-        ii = 0;
-        while (idx > ii) { idx -= ii + 1; ++ii; }
-        jj = idx;
         double c;
         if constexpr (DIM == 3) c = p3_C_elem(rec, rec + 9, M + 6 * ii, jj);
         else c = p2_C_elem(rec, M + 3 * ii, jj);
