@@ -364,27 +364,6 @@ __device__ __forceinline__ void tail_coords(int t, int& bi, int& bj) {
   bj = t - i * (i + 1) / 2;
 }
 
-// S of tail block t into the dense tail
-template <int D>
-__device__ void tail_S(const CholArgs& a, int t, int lane) {
-  constexpr int dd = D * D;
-  int bi, bj;
-  tail_coords(t, bi, bj);
-  const int e0 = lane, e1 = lane + 32;
-  double s0 = 0.0, s1 = 0.0;
-  if (bi == bj) {
-    const int v = a.perm[a.ns + bi];
-    if (e0 < dd) s0 = gather_diag<D>(a, v, e0 / D, e0 % D);
-    if (e1 < dd) s1 = gather_diag<D>(a, v, e1 / D, e1 % D);
-  } else {
-    if (e0 < dd) s0 = gather_offdiag<D>(a.fH64, a.ta_src, a.ta_ptr[t], a.ta_ptr[t + 1], e0 / D, e0 % D);
-    if (e1 < dd) s1 = gather_offdiag<D>(a.fH64, a.ta_src, a.ta_ptr[t], a.ta_ptr[t + 1], e1 / D, e1 % D);
-  }
-  sub_pairs_warp<D>(a.L, a.tupd_src, a.tupd_ptr[t], a.tupd_ptr[t + 1], lane, s0, s1);
-  if (e0 < dd) a.M[(size_t)(bj * D + e0 % D) * a.ntp + bi * D + e0 / D] = s0;
-  if (e1 < dd) a.M[(size_t)(bj * D + e1 % D) * a.ntp + bi * D + e1 / D] = s1;
-}
-
 // tail row task u (one warp, lane groups take the entries in turn):
 // Tpart[u][r] = sum over its entries (block q, column k) of (L[q] y_k)[r]
 template <int D>
@@ -411,6 +390,8 @@ __device__ void tail_rhs(const CholArgs& a, int t, int lane) {
   a.y[(size_t)(a.ns + t) * D + lane] -= acc;
 }
 
+constexpr int kWarps = kThreads / 32;
+
 struct TileSmem {
   double A[kTB][kTB + 1];
   double B[kTB][kTB + 1];
@@ -418,7 +399,51 @@ struct TileSmem {
   double E[kTB][kTB + 1];
   double red[kThreads / kTB + 1][kTB];
   double v[kTB];
+  double part[kWarps * 36 * 5];  // tail block partial sums: (warp, lane group) x D x D, D = 3 or 6
 };
+
+// S of tail block t into the dense tail, by one CTA: the lane groups of all
+// warps take the block's update pairs in turn (group slot k = warp * G +
+// group takes pairs k, k + W G, ...), then thread e < D x D adds entry e of
+// the Hessian block (+ lambda D on the diagonal) and of the slots' partial
+// sums, in slot order.
+template <int D>
+__device__ void tail_block_cta(const CholArgs& a, int t, TileSmem& s) {
+  constexpr int G = 32 / D, dd = D * D;
+  static_assert(kWarps * G * dd <= (int)(sizeof(s.part) / sizeof(double)), "tail partial buffer");
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  const int g = lane / D, r = lane % D;
+  int bi, bj;
+  tail_coords(t, bi, bj);
+  const int beg = a.tupd_ptr[t], end = a.tupd_ptr[t + 1];
+  const int nslots = min(kWarps * G, end - beg);
+  const int slot = wi * G + g;
+  if (g < G && slot < nslots) {
+    double acc[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc[c] = 0.0;
+    for (int u = beg + slot; u < end; u += kWarps * G) {
+      const double* A = a.L + (size_t)a.tupd_src[2 * u] * dd + r * D;
+      const double* B = a.L + (size_t)a.tupd_src[2 * u + 1] * dd;
+      double ar[D];
+#pragma unroll
+      for (int k = 0; k < D; ++k) ar[k] = A[k];
+#pragma unroll
+      for (int c = 0; c < D; ++c) acc[c] -= dot_ilp<D>(ar, B + c * D);
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) s.part[slot * dd + r * D + c] = acc[c];
+  }
+  __syncthreads();
+  if (threadIdx.x < dd) {
+    const int e = threadIdx.x, rr = e / D, cc = e % D;
+    double v = bi == bj ? gather_diag<D>(a, a.perm[a.ns + bi], rr, cc)
+                        : gather_offdiag<D>(a.fH64, a.ta_src, a.ta_ptr[t], a.ta_ptr[t + 1], rr, cc);
+    for (int k = 0; k < nslots; ++k) v += s.part[k * dd + e];
+    a.M[(size_t)(bj * D + cc) * a.ntp + bi * D + rr] = v;
+  }
+  __syncthreads();
+}
 
 __device__ __forceinline__ double* tile_ptr(const CholArgs& a, int ti, int tj) {
   return a.M + (size_t)(tj * kTB) * a.ntp + ti * kTB;
@@ -449,9 +474,10 @@ __device__ void smem_update(double (*X)[kTB + 1], double (*P)[kTB + 1], double (
 }
 
 // Cholesky of the lower part of X in place (right-looking); the diagonal
-// keeps the reciprocal of each pivot
-__device__ void smem_chol(double (*X)[kTB + 1], int32_t* status) {
-  for (int c = 0; c < kTB; ++c) {
+// keeps the reciprocal of each pivot. Columns from `width` on are padding of
+// the last tile (identity: pivot 1, reciprocal 1, no updates) and are skipped.
+__device__ void smem_chol(double (*X)[kTB + 1], int width, int32_t* status) {
+  for (int c = 0; c < width; ++c) {
     if (threadIdx.x == 0) {
       double piv = X[c][c];
       if (!(piv > 0.0)) {
@@ -473,8 +499,8 @@ __device__ void smem_chol(double (*X)[kTB + 1], int32_t* status) {
   }
 }
 
-// phase k, tile column item: tile (i, k), i >= k
-__device__ void tail_column_item(const CholArgs& a, int i, int k, TileSmem& s) {
+// phase k, tile column item: tile (i, k), i >= k; nt = tail size in scalars
+__device__ void tail_column_item(const CholArgs& a, int i, int k, int nt, TileSmem& s) {
   load_tile(a, k, k, s.C);
   if (k > 0) load_tile(a, k, k - 1, s.B);
   if (i > k) {
@@ -487,7 +513,7 @@ __device__ void tail_column_item(const CholArgs& a, int i, int k, TileSmem& s) {
     if (i > k) smem_update(s.A, s.E, s.B, false);
   }
   __syncthreads();
-  smem_chol(s.C, a.status);
+  smem_chol(s.C, min(kTB, nt - k * kTB), a.status);
   if (i == k) {
     double* O = a.Ldd + (size_t)k * kTB * kTB;
     for (int e = threadIdx.x; e < kTB * kTB; e += blockDim.x) {
@@ -622,7 +648,13 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   __shared__ double shr[kThreads / 32];
   const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31;
-  const int gw = gt >> 5, nw = gs >> 5;
+  // Warp-sized work items (tasks, columns) go round-robin over the CTAs, so
+  // that a level with fewer items than SMs puts one item per SM (no two
+  // items share an SM's FP64 pipe), and to warps 1..7 before warp 0: the
+  // warp whose thread 0 takes part in the grid barrier runs the phase after
+  // it about 2.5 us slower (measured on GB300), so it only takes the items
+  // of the widest levels.
+  const int gw = (((threadIdx.x >> 5) + kWarps - 1) % kWarps) * (int)gridDim.x + (int)blockIdx.x, nw = gs >> 5;
   const int n = a.N * D, nt = a.T * D;
   double* yt = a.y + (size_t)a.ns * D;
 
@@ -655,17 +687,30 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
     grid.sync();
   }
 
-  // 3. dense tail: blocks, then tiles
+  // 3. dense tail: its blocks (one CTA each) and the row sums of its
+  // right-hand side (one warp each, on the CTAs after the blocks'), then the
+  // tiles
   {
     const int nts = a.T * (a.T + 1) / 2, ntr = a.ttask_ptr[a.T];
-    for (int w = gw; w < nts + ntr; w += nw) {
-      if (w < nts) tail_S<D>(a, w, lane);
-      else tail_row_task<D>(a, w - nts, lane);
-    }
+    for (int b = blockIdx.x; b < nts; b += gridDim.x) tail_block_cta<D>(a, b, sm);
+    for (int w = gw; w < nts + ntr; w += nw)
+      if (w >= nts) tail_row_task<D>(a, w - nts, lane);
   }
   grid.sync();
   const int nT = a.n_tiles;
-  for (int k = 0; k <= nT; ++k) {
+  if (nT == 1) {
+    // a single tile: one CTA takes the tail's right-hand side, its
+    // factorisation and both substitutions, in one phase
+    if (blockIdx.x == 0) {
+      for (int w = threadIdx.x >> 5; w < a.T; w += kWarps) tail_rhs<D>(a, w, lane);
+      __syncthreads();
+      tail_column_item(a, 0, 0, nt, sm);
+      tail_forward_item(a, yt, 0, sm);
+      tail_backward_item(a, yt, 0, sm);
+    }
+    grid.sync();
+  }
+  for (int k = 0; nT > 1 && k <= nT; ++k) {
     const int ncol = k < nT ? nT - k : 0;
     const int m = nT - k - 1;  // trailing tile columns k + 1 .. nT - 1
     const int ntrail = (k >= 1 && m > 0) ? m * (m + 1) / 2 : 0;
@@ -673,7 +718,7 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
     const int items = ncol + ntrail + nfwd;
     for (int it = blockIdx.x; it < items; it += gridDim.x) {
       if (it < ncol) {
-        tail_column_item(a, k + it, k, sm);
+        tail_column_item(a, k + it, k, nt, sm);
       } else if (it < ncol + ntrail) {
         // trailing tile u -> (i, j), k + 1 <= j <= i <= nT - 1
         const int u = it - ncol;
@@ -689,8 +734,8 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
     grid.sync();
   }
 
-  // 4. backward substitution: tail tiles, then sparse levels (top first)
-  for (int k = nT - 1; k >= 0; --k) {
+  // 4. backward substitution: tail tiles (several), then sparse levels (top first)
+  for (int k = nT - 1; nT > 1 && k >= 0; --k) {
     if (blockIdx.x == (unsigned)(k % gridDim.x)) tail_backward_item(a, yt, k, sm);
     grid.sync();
   }

@@ -178,7 +178,9 @@ def test_gpu_edit_api_reference_tests(name):
     kg, pg = g.estimate()
     ko, po = o.estimate()
     assert np.array_equal(kg, ko)
-    np.testing.assert_allclose(pg, po, rtol=1e-6, atol=1e-9)
+    # the two linear solvers sum in different orders; entries near zero
+    # (translations of ~1e-5 m) differ by ~1e-9 m
+    np.testing.assert_allclose(pg, po, rtol=1e-6, atol=1e-8)
     assert g.counts().num_factors == o.counts().num_factors
     assert g.getIgnoredPrefixes() == o.getIgnoredPrefixes()
 
