@@ -241,20 +241,45 @@ __device__ __forceinline__ void sum_partials(const CholArgs& a, int p, int r, do
   }
 }
 
-// phase B, one warp per column j: every lane group factors the diagonal
-// block (the groups hold identical copies of L_jj, right-looking Cholesky
-// across the group, reciprocal pivots on the diagonal), the groups share the
-// off-diagonal blocks L_ij = S_ij L_jj^-T, and group 0 does the column's
-// forward substitution
+// S_jj, the diagonal block of column j (block p), from its task partials,
+// summed entry-wise: lane e holds entries e and e + 32, so a partial costs two
+// FP64 additions instead of D; every entry is summed from 0 in slot order
+// (the same additions as a row-wise sum). Then moved to the lane-group row
+// layout (lane r of every group gets row r).
 template <int D>
-__device__ void column_warp(const CholArgs& a, int j, int lane) {
-  constexpr int G = 32 / D, dd = D * D;
-  const int g = lane / D, r = lane % D;
-  const bool grp = g < G;
-  const int base = (grp ? g : 0) * D;
-  const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
-  double C[D];
-  sum_partials<D>(a, p0, r, C);
+__device__ __forceinline__ void diag_partials(const CholArgs& a, int p, int lane, int r, double (&C)[D]) {
+  constexpr int dd = D * D;
+  const int t0 = a.btask[2 * p], t1 = t0 + a.btask[2 * p + 1];
+  const bool has0 = lane < dd, has1 = lane + 32 < dd;
+  double e0 = 0.0, e1 = 0.0;
+  for (int t = t0; t < t1; t += 4) {
+    double x[4], y[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const double* P = a.Spart + (size_t)(t + k) * dd;
+      x[k] = (t + k < t1 && has0) ? P[lane] : 0.0;
+      y[k] = (t + k < t1 && has1) ? P[32 + lane] : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (t + k < t1) {
+        e0 += x[k];
+        e1 += y[k];
+      }
+  }
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const int e = r * D + c;
+    const double v0 = __shfl_sync(kFull, e0, e & 31), v1 = __shfl_sync(kFull, e1, e & 31);
+    C[c] = e < 32 ? v0 : v1;
+  }
+}
+
+// In-register Cholesky of S_jj across a lane group (lane r holds row r; the
+// groups hold identical copies), reciprocal pivots on the diagonal; a failed
+// pivot sets the status flag.
+template <int D>
+__device__ __forceinline__ void factor_diag(const CholArgs& a, int lane, int g, int r, int base, double (&C)[D]) {
   bool ok = true;
 #pragma unroll
   for (int c = 0; c < D; ++c) {
@@ -276,6 +301,63 @@ __device__ void column_warp(const CholArgs& a, int j, int lane) {
   }
   const bool bad = __any_sync(kFull, !ok && g == 0);
   if (lane == 0 && bad) set_fail(a.status);
+}
+
+// L_ij = S_ij L_jj^-T for one row r of an off-diagonal block, in place
+// (right-looking), stored to block p
+template <int D>
+__device__ __forceinline__ void solve_offdiag(const CholArgs& a, int p, int r, const double (&Lf)[D * D],
+                                              double (&sv)[D]) {
+  constexpr int dd = D * D;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    const double x = sv[c] * Lf[c * D + c];
+    sv[c] = x;
+#pragma unroll
+    for (int k = c + 1; k < D; ++k) sv[k] = fma(-x, Lf[k * D + c], sv[k]);
+  }
+#pragma unroll
+  for (int c = 0; c < D; ++c) a.L[(size_t)p * dd + r * D + c] = sv[c];
+}
+
+// y_j - the forward-substitution row sums of column j (row r)
+template <int D>
+__device__ __forceinline__ double forward_rhs(const CholArgs& a, int j, int r) {
+  constexpr int dd = D * D;
+  double b = a.y[(size_t)j * D + r];
+  const int t0 = a.ftask[2 * j], nt = a.ftask[2 * j + 1];
+  double acc = 0.0;
+  for (int t = t0; t < t0 + nt; ++t) acc += a.Spart[(size_t)t * dd + r * D];
+  return b - acc;
+}
+
+// y_j = L_jj^-1 b (lane r of a group holds b_r and row r of L_jj)
+template <int D>
+__device__ __forceinline__ void forward_solve(const CholArgs& a, int j, int g, int r, int base, const double (&C)[D],
+                                              double b) {
+  double yv = 0.0;
+#pragma unroll
+  for (int c = 0; c < D; ++c) {
+    if (r == c) yv = b * C[c];
+    const double yc = __shfl_sync(kFull, yv, base + c);
+    if (r > c) b = fma(-C[c], yc, b);
+  }
+  if (g == 0) a.y[(size_t)j * D + r] = yv;
+}
+
+// phase B, one warp per column j: every lane group factors the diagonal
+// block, the groups share the off-diagonal blocks L_ij = S_ij L_jj^-T, and
+// group 0 does the column's forward substitution
+template <int D>
+__device__ void column_warp(const CholArgs& a, int j, int lane) {
+  constexpr int G = 32 / D, dd = D * D;
+  const int g = lane / D, r = lane % D;
+  const bool grp = g < G;
+  const int base = (grp ? g : 0) * D;
+  const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
+  double C[D];
+  diag_partials<D>(a, p0, lane, r, C);
+  factor_diag<D>(a, lane, g, r, base, C);
   double Lf[dd];
 #pragma unroll
   for (int q = 0; q < D; ++q)
@@ -289,33 +371,60 @@ __device__ void column_warp(const CholArgs& a, int j, int lane) {
     for (int p = p0 + 1 + g; p < p1; p += G) {
       double sv[D];
       sum_partials<D>(a, p, r, sv);
-#pragma unroll
-      for (int c = 0; c < D; ++c) {
-        const double x = sv[c] * Lf[c * D + c];
-        sv[c] = x;
-#pragma unroll
-        for (int k = c + 1; k < D; ++k) sv[k] = fma(-x, Lf[k * D + c], sv[k]);
-      }
-#pragma unroll
-      for (int c = 0; c < D; ++c) a.L[(size_t)p * dd + r * D + c] = sv[c];
+      solve_offdiag<D>(a, p, r, Lf, sv);
     }
   }
-  // forward substitution: y_j = L_jj^-1 (y_j - row sums)
-  double b = a.y[(size_t)j * D + r];
-  {
-    const int t0 = a.ftask[2 * j], nt = a.ftask[2 * j + 1];
-    double acc = 0.0;
-    for (int t = t0; t < t0 + nt; ++t) acc += a.Spart[(size_t)t * dd + r * D];
-    b -= acc;
-  }
-  double yv = 0.0;
+  forward_solve<D>(a, j, g, r, base, C, forward_rhs<D>(a, j, r));
+}
+
+__device__ __forceinline__ void team_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+
+// phase B for column j by a team of two warps (tw 0 = lead, 1 = helper) that
+// meet at named barrier `bar`; sh = D x D + D doubles of shared memory. The
+// lead sums and factors the diagonal block, publishes L_jj and does the
+// forward substitution; meanwhile the helper sums the forward row sums and the
+// partials of the off-diagonal blocks, and after the barrier solves those
+// blocks with L_jj. Same operations and order as column_warp.
+template <int D>
+__device__ void column_team(const CholArgs& a, int j, int tw, int lane, int bar, double* sh) {
+  constexpr int G = 32 / D, dd = D * D;
+  const int g = lane / D, r = lane % D;
+  const bool grp = g < G;
+  const int base = (grp ? g : 0) * D;
+  const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
+  if (tw == 0) {
+    double C[D];
+    diag_partials<D>(a, p0, lane, r, C);
+    factor_diag<D>(a, lane, g, r, base, C);
+    if (g == 0) {
 #pragma unroll
-  for (int c = 0; c < D; ++c) {
-    if (r == c) yv = b * Lf[c * D + c];
-    const double yc = __shfl_sync(kFull, yv, base + c);
-    if (r > c) b = fma(-C[c], yc, b);
+      for (int c = 0; c < D; ++c) {
+        const double v = (c <= r) ? C[c] : 0.0;
+        a.Ldiag[(size_t)j * dd + r * D + c] = v;
+        sh[r * D + c] = v;
+      }
+    }
+    team_sync(bar);
+    forward_solve<D>(a, j, g, r, base, C, sh[dd + r]);
+  } else {
+    const double b = forward_rhs<D>(a, j, r);
+    if (g == 0) sh[dd + r] = b;
+    const int pf = p0 + 1 + g;
+    double sv[D];
+    if (grp && pf < p1) sum_partials<D>(a, pf, r, sv);
+    team_sync(bar);
+    double Lf[dd];
+#pragma unroll
+    for (int q = 0; q < D; ++q)
+#pragma unroll
+      for (int c = 0; c <= q; ++c) Lf[q * D + c] = sh[q * D + c];
+    if (grp) {
+      for (int p = pf; p < p1; p += G) {
+        if (p != pf) sum_partials<D>(a, p, r, sv);
+        solve_offdiag<D>(a, p, r, Lf, sv);
+      }
+    }
   }
-  if (g == 0) a.y[(size_t)j * D + r] = yv;
 }
 
 // backward substitution of column j by one warp:
@@ -400,6 +509,7 @@ struct TileSmem {
   double red[kThreads / kTB + 1][kTB];
   double v[kTB];
   double part[kWarps * 36 * 5];  // tail block partial sums: (warp, lane group) x D x D, D = 3 or 6
+  double team[2][36 + 6];        // phase B teams: L_jj and the forward right-hand side
 };
 
 // S of tail block t into the dense tail, by one CTA: the lane groups of all
@@ -683,7 +793,18 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
     for (int t = t0 + gw; t < t1; t += nw) run_task<D>(a, t, lane);
     grid.sync();
     const int c0 = a.lvl_col_ptr[l], nc = a.lvl_col_ptr[l + 1] - c0;
-    for (int w = gw; w < nc; w += nw) column_warp<D>(a, a.lvl_cols[c0 + w], lane);
+    if (nc <= 2 * (int)gridDim.x) {
+      // narrow level: at most two columns per CTA, each by a team of two
+      // warps (warps 1-2 and 3-4, on four different SM sub-partitions)
+      const int wi = threadIdx.x >> 5;
+      if (wi >= 1 && wi <= 4) {
+        const int slot = (wi - 1) >> 1;
+        const int w = slot * (int)gridDim.x + (int)blockIdx.x;
+        if (w < nc) column_team<D>(a, a.lvl_cols[c0 + w], (wi - 1) & 1, lane, 1 + slot, sm.team[slot]);
+      }
+    } else {
+      for (int w = gw; w < nc; w += nw) column_warp<D>(a, a.lvl_cols[c0 + w], lane);
+    }
     grid.sync();
   }
 
