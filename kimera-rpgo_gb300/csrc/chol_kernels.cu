@@ -9,21 +9,25 @@
 //         every column's forward-substitution row sum;
 //     (B) every column by one warp: S_jj from the partial sums, L_jj =
 //         chol(S_jj), L_ij = S_ij L_jj^-T, and y_j;
-//  3. the dense tail: its blocks from H and the sparse updates, then a
-//     right-looking tiled Cholesky with one barrier per tile column: in phase
-//     k the CTAs of tile column k apply the update of column k-1, factor the
-//     diagonal tile and solve their tile, while all other CTAs apply the
-//     column k-1 update to the trailing tiles; the forward substitution of
-//     tile k-1 runs in the same phase;
+//  3. the dense tail: its blocks from H and the sparse updates (one CTA per
+//     block), then a right-looking tiled Cholesky with one barrier per tile
+//     column: in phase k the CTAs of tile column k apply the update of column
+//     k-1, factor the diagonal tile and solve their tile, while all other CTAs
+//     apply the column k-1 update to the trailing tiles; the forward
+//     substitution of tile k-1 runs in the same phase. A tail of one tile is
+//     factored and solved (both substitutions) by one CTA in one phase;
 //  4. backward substitution over the tail tiles, then the sparse levels (top
 //     first); scatter to variable order together with the linearised cost
 //     change of the undamped system (a fixed-order grid reduction).
-// FP64 on this part has a dependent-operation latency of about 33 ns for an
-// FMA and about 300 ns for a divide or square root, so the kernel is written
-// for instruction-level parallelism: split accumulators, right-looking
-// triangular solves (independent updates), and one reciprocal square root
-// per pivot; the factors keep the reciprocal of each pivot on their diagonal
-// and every solve multiplies by it.
+// FP64 on this part retires one warp instruction per ~33 ns per SM
+// sub-partition whether or not it depends on the previous one (a divide or
+// square root costs ~220-300 ns), so the kernel minimises FP64 instructions on
+// each phase's busiest warp: lane groups that serve several blocks per warp
+// instruction, one FMA chain per output, reductions over the active lane
+// groups only, entry-wise partial sums, and one reciprocal square root per
+// pivot (the factors keep the reciprocal of each pivot on their diagonal and
+// every solve multiplies by it). Work items spread one per SM where a level is
+// narrow, and the column work of narrow levels is split over two warps.
 // Every sum runs in an order fixed by the plan, so results do not depend on
 // scheduling. A non-positive (or NaN) pivot sets the status flag; the factor
 // continues with pivot 1 so that every phase still ends, and the host treats
@@ -53,55 +57,6 @@ struct CholArgs {
 
 __device__ __forceinline__ void set_fail(int32_t* status) { atomicExch(status, 1); }
 
-// dot product of length D with two accumulators (even / odd terms)
-template <int D>
-__device__ __forceinline__ double dot_ilp(const double* __restrict__ a, const double* __restrict__ b) {
-  double e = 0.0, o = 0.0;
-#pragma unroll
-  for (int t = 0; t < D; t += 2) e = fma(a[t], b[t], e);
-#pragma unroll
-  for (int t = 1; t < D; t += 2) o = fma(a[t], b[t], o);
-  return e + o;
-}
-
-// s0, s1 (the lane's entries e = lane, lane + 32 of a D x D block) -= sum
-// over the update pairs [beg, end) of (L[a] L[b]^T)(r, c). The 32 lanes load
-// the indices of 32 pairs at once and broadcast them, so the block loads of
-// consecutive pairs do not wait on an index load; four partial sums (pair
-// index mod 4) keep four products in flight.
-template <int D>
-__device__ __forceinline__ void sub_pairs_warp(const double* __restrict__ L, const int32_t* __restrict__ src, int beg,
-                                               int end, int lane, double& s0, double& s1) {
-  constexpr int dd = D * D;
-  const int e0 = lane, e1 = lane + 32;
-  const int r0 = e0 / D, c0 = e0 % D, r1 = e1 / D, c1 = e1 % D;
-  double q0[4] = {0.0, 0.0, 0.0, 0.0}, q1[4] = {0.0, 0.0, 0.0, 0.0};
-  for (int base = beg; base < end; base += 32) {
-    const int cnt = min(32, end - base);
-    int ia = 0, ib = 0;
-    if (lane < cnt) {
-      ia = src[2 * (base + lane)];
-      ib = src[2 * (base + lane) + 1];
-    }
-    int u = 0;
-    for (; u + 4 <= cnt; u += 4) {
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int pa = __shfl_sync(0xffffffffu, ia, u + k), pb = __shfl_sync(0xffffffffu, ib, u + k);
-        if (e0 < dd) q0[k] += dot_ilp<D>(L + (size_t)pa * dd + r0 * D, L + (size_t)pb * dd + c0 * D);
-        if (e1 < dd) q1[k] += dot_ilp<D>(L + (size_t)pa * dd + r1 * D, L + (size_t)pb * dd + c1 * D);
-      }
-    }
-    for (; u < cnt; ++u) {
-      const int pa = __shfl_sync(0xffffffffu, ia, u), pb = __shfl_sync(0xffffffffu, ib, u);
-      if (e0 < dd) q0[0] += dot_ilp<D>(L + (size_t)pa * dd + r0 * D, L + (size_t)pb * dd + c0 * D);
-      if (e1 < dd) q1[0] += dot_ilp<D>(L + (size_t)pa * dd + r1 * D, L + (size_t)pb * dd + c1 * D);
-    }
-  }
-  s0 -= (q0[0] + q0[1]) + (q0[2] + q0[3]);
-  s1 -= (q1[0] + q1[1]) + (q1[2] + q1[3]);
-}
-
 // Hessian entry (r, c) of the block at (row var, col var) from the factor
 // off-diagonal blocks in src[beg, end) (2 f + transposed)
 template <int D>
@@ -125,39 +80,6 @@ __device__ __forceinline__ double gather_diag(const CholArgs& a, int v, int r, i
   return s;
 }
 
-// In-register Cholesky of a D x D block (lower, row-major) with the
-// reciprocal of each pivot stored on the diagonal; false on a non-positive
-// (or NaN) pivot, which is replaced by 1.
-template <int D>
-__device__ __forceinline__ bool chol_reg(double (&C)[D * D]) {
-  bool ok = true;
-#pragma unroll
-  for (int c = 0; c < D; ++c) {
-    double e = C[c * D + c], o = 0.0;
-#pragma unroll
-    for (int t = 0; t < c; t += 2) e = fma(-C[c * D + t], C[c * D + t], e);
-#pragma unroll
-    for (int t = 1; t < c; t += 2) o = fma(-C[c * D + t], C[c * D + t], o);
-    double s = e + o;
-    if (!(s > 0.0)) {
-      ok = false;
-      s = 1.0;
-    }
-    const double il = rsqrt(s);
-    C[c * D + c] = il;
-#pragma unroll
-    for (int r = c + 1; r < D; ++r) {
-      double e2 = C[r * D + c], o2 = 0.0;
-#pragma unroll
-      for (int t = 0; t < c; t += 2) e2 = fma(-C[r * D + t], C[c * D + t], e2);
-#pragma unroll
-      for (int t = 1; t < c; t += 2) o2 = fma(-C[r * D + t], C[c * D + t], o2);
-      C[r * D + c] = (e2 + o2) * il;
-    }
-  }
-  return ok;
-}
-
 constexpr unsigned kFull = 0xffffffffu;
 
 // Sparse levels use lane groups: a warp holds 32 / D groups of D lanes and
@@ -167,7 +89,11 @@ constexpr unsigned kFull = 0xffffffffu;
 // its lanes do useful work.)
 
 // phase A, one warp per task: the groups take the task's entries in turn,
-// then their sums are added in group order into lanes 0 .. D-1.
+// then the sums of the groups that took entries are added in group order into
+// lanes 0 .. D-1. The FP64 pipe retires a warp instruction every ~33 ns
+// whether or not it depends on the previous one, so products accumulate in
+// one FMA chain per output (no split accumulators) and only groups with
+// entries join the sum: the instruction count is the cost.
 //  block task (kind 0 / 1): Spart[t] = (kind 1: H block of id, + lambda D on
 //    a diagonal block) - sum over its pairs (a, b) of L[a] L[b]^T;
 //  row task (kind 2): Spart[t][r] = sum over its row entries (block q,
@@ -205,24 +131,34 @@ __device__ void run_task(const CholArgs& a, int t, int lane) {
 #pragma unroll
         for (int k = 0; k < D; ++k) ar[k] = A[k];
 #pragma unroll
-        for (int c = 0; c < NC; ++c) acc[c] -= dot_ilp<D>(ar, B + c * D);
+        for (int c = 0; c < NC; ++c)
+#pragma unroll
+          for (int k = 0; k < D; ++k) acc[c] = fma(-ar[k], B[c * D + k], acc[c]);
       }
     }
+    const int ng = min(G, max(1, tk.z - tk.y));
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
       double tot = acc[c];
 #pragma unroll
-      for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, acc[c], (r + k * D) & 31);
+      for (int k = 1; k < G; ++k)
+        if (k < ng) tot += __shfl_sync(kFull, acc[c], (r + k * D) & 31);
       if (lane < D) a.Spart[(size_t)slot * dd + lane * D + c0 + c] = tot;
     }
   } else {
     double acc = 0.0;
     if (g < G)
-      for (int u = tk.y + g; u < tk.z; u += G)
-        acc += dot_ilp<D>(a.L + (size_t)a.row_blk[2 * u] * dd + r * D, a.y + (size_t)a.row_blk[2 * u + 1] * D);
+      for (int u = tk.y + g; u < tk.z; u += G) {
+        const double* Lq = a.L + (size_t)a.row_blk[2 * u] * dd + r * D;
+        const double* yk = a.y + (size_t)a.row_blk[2 * u + 1] * D;
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc = fma(Lq[k], yk[k], acc);
+      }
+    const int ng = min(G, max(1, tk.z - tk.y));
     double tot = acc;
 #pragma unroll
-    for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, acc, (r + k * D) & 31);
+    for (int k = 1; k < G; ++k)
+      if (k < ng) tot += __shfl_sync(kFull, acc, (r + k * D) & 31);
     if (lane < D) a.Spart[(size_t)slot * dd + lane * D] = tot;
   }
 }
@@ -435,22 +371,20 @@ __device__ void backward_warp(const CholArgs& a, int j, int lane) {
   const int g = lane / D, r = lane % D;
   const int base = (g < G ? g : 0) * D;
   double acc = 0.0;
+  const int q0 = a.col_ptr[j] + 1, q1 = a.col_ptr[j + 1];
   if (g < G) {
-    const int q1 = a.col_ptr[j + 1];
-    for (int q = a.col_ptr[j] + 1 + g; q < q1; q += G) {
+    for (int q = q0 + g; q < q1; q += G) {
       const double* B = a.L + (size_t)q * dd + r;
       const double* xi = a.y + (size_t)a.blk_row[q] * D;
-      double e = 0.0, o = 0.0;
 #pragma unroll
-      for (int k = 0; k < D; k += 2) e = fma(B[k * D], xi[k], e);
-#pragma unroll
-      for (int k = 1; k < D; k += 2) o = fma(B[k * D], xi[k], o);
-      acc += e + o;
+      for (int k = 0; k < D; ++k) acc = fma(B[k * D], xi[k], acc);
     }
   }
+  const int ng = min(G, q1 - q0);
   double tot = acc;
 #pragma unroll
-  for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, acc, (r + k * D) & 31);
+  for (int k = 1; k < G; ++k)
+    if (k < ng) tot += __shfl_sync(kFull, acc, (r + k * D) & 31);
   double b = a.y[(size_t)j * D + r] - tot;
   double Lc[D];
 #pragma unroll
@@ -482,11 +416,17 @@ __device__ void tail_row_task(const CholArgs& a, int u, int lane) {
   const int beg = a.ttasks[3 * u + 1], end = a.ttasks[3 * u + 2];
   double acc = 0.0;
   if (g < G)
-    for (int e = beg + g; e < end; e += G)
-      acc += dot_ilp<D>(a.L + (size_t)a.trow_blk[2 * e] * dd + r * D, a.y + (size_t)a.trow_blk[2 * e + 1] * D);
+    for (int e = beg + g; e < end; e += G) {
+      const double* Lq = a.L + (size_t)a.trow_blk[2 * e] * dd + r * D;
+      const double* yk = a.y + (size_t)a.trow_blk[2 * e + 1] * D;
+#pragma unroll
+      for (int k = 0; k < D; ++k) acc = fma(Lq[k], yk[k], acc);
+    }
+  const int ng = min(G, max(1, end - beg));
   double tot = acc;
 #pragma unroll
-  for (int k = 1; k < G; ++k) tot += __shfl_sync(kFull, acc, (r + k * D) & 31);
+  for (int k = 1; k < G; ++k)
+    if (k < ng) tot += __shfl_sync(kFull, acc, (r + k * D) & 31);
   if (lane < D) a.Tpart[(size_t)u * D + lane] = tot;
 }
 
@@ -539,7 +479,9 @@ __device__ void tail_block_cta(const CholArgs& a, int t, TileSmem& s) {
 #pragma unroll
       for (int k = 0; k < D; ++k) ar[k] = A[k];
 #pragma unroll
-      for (int c = 0; c < D; ++c) acc[c] -= dot_ilp<D>(ar, B + c * D);
+      for (int c = 0; c < D; ++c)
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc[c] = fma(-ar[k], B[c * D + k], acc[c]);
     }
 #pragma unroll
     for (int c = 0; c < D; ++c) s.part[slot * dd + r * D + c] = acc[c];
