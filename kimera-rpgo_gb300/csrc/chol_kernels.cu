@@ -163,11 +163,17 @@ __device__ void run_task(const CholArgs& a, int t, int lane) {
   }
 }
 
-// sum of the task partials of block p (row r) into s
+// off-diagonal block p (row r) of S into s: the sum of its task partials, or
+// its Hessian block when it has no update pairs (and no task)
 template <int D>
 __device__ __forceinline__ void sum_partials(const CholArgs& a, int p, int r, double (&s)[D]) {
   constexpr int dd = D * D;
   const int t0 = a.btask[2 * p], nt = a.btask[2 * p + 1];
+  if (nt == 0) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) s[c] = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], r, c);
+    return;
+  }
 #pragma unroll
   for (int c = 0; c < D; ++c) s[c] = 0.0;
   for (int t = t0; t < t0 + nt; ++t) {
@@ -180,14 +186,20 @@ __device__ __forceinline__ void sum_partials(const CholArgs& a, int p, int r, do
 // S_jj, the diagonal block of column j (block p), from its task partials,
 // summed entry-wise: lane e holds entries e and e + 32, so a partial costs two
 // FP64 additions instead of D; every entry is summed from 0 in slot order
-// (the same additions as a row-wise sum). Then moved to the lane-group row
+// (the same additions as a row-wise sum). A block without update pairs (no
+// task) is its Hessian block plus lambda D. Then moved to the lane-group row
 // layout (lane r of every group gets row r).
 template <int D>
-__device__ __forceinline__ void diag_partials(const CholArgs& a, int p, int lane, int r, double (&C)[D]) {
+__device__ __forceinline__ void diag_partials(const CholArgs& a, int j, int p, int lane, int r, double (&C)[D]) {
   constexpr int dd = D * D;
   const int t0 = a.btask[2 * p], t1 = t0 + a.btask[2 * p + 1];
   const bool has0 = lane < dd, has1 = lane + 32 < dd;
   double e0 = 0.0, e1 = 0.0;
+  if (t1 == t0) {
+    const int v = a.perm[j];
+    if (has0) e0 = gather_diag<D>(a, v, lane / D, lane % D);
+    if (has1) e1 = gather_diag<D>(a, v, (lane + 32) / D, (lane + 32) % D);
+  }
   for (int t = t0; t < t1; t += 4) {
     double x[4], y[4];
 #pragma unroll
@@ -211,11 +223,11 @@ __device__ __forceinline__ void diag_partials(const CholArgs& a, int p, int lane
   }
 }
 
-// In-register Cholesky of S_jj across a lane group (lane r holds row r; the
-// groups hold identical copies), reciprocal pivots on the diagonal; a failed
-// pivot sets the status flag.
+// In-register Cholesky of S_jj across a lane group (lane r holds row r, the
+// group's lanes start at `base`), reciprocal pivots on the diagonal; a failed
+// pivot of a group whose lanes have `mine` set sets the status flag.
 template <int D>
-__device__ __forceinline__ void factor_diag(const CholArgs& a, int lane, int g, int r, int base, double (&C)[D]) {
+__device__ __forceinline__ void factor_diag(const CholArgs& a, int lane, bool mine, int r, int base, double (&C)[D]) {
   bool ok = true;
 #pragma unroll
   for (int c = 0; c < D; ++c) {
@@ -235,15 +247,15 @@ __device__ __forceinline__ void factor_diag(const CholArgs& a, int lane, int g, 
       if (r >= q) C[q] = fma(-C[c], lqc, C[q]);
     }
   }
-  const bool bad = __any_sync(kFull, !ok && g == 0);
+  const bool bad = __any_sync(kFull, !ok && mine);
   if (lane == 0 && bad) set_fail(a.status);
 }
 
 // L_ij = S_ij L_jj^-T for one row r of an off-diagonal block, in place
-// (right-looking), stored to block p
+// (right-looking), stored to block p when `st`
 template <int D>
 __device__ __forceinline__ void solve_offdiag(const CholArgs& a, int p, int r, const double (&Lf)[D * D],
-                                              double (&sv)[D]) {
+                                              double (&sv)[D], bool st = true) {
   constexpr int dd = D * D;
 #pragma unroll
   for (int c = 0; c < D; ++c) {
@@ -252,8 +264,10 @@ __device__ __forceinline__ void solve_offdiag(const CholArgs& a, int p, int r, c
 #pragma unroll
     for (int k = c + 1; k < D; ++k) sv[k] = fma(-x, Lf[k * D + c], sv[k]);
   }
+  if (st) {
 #pragma unroll
-  for (int c = 0; c < D; ++c) a.L[(size_t)p * dd + r * D + c] = sv[c];
+    for (int c = 0; c < D; ++c) a.L[(size_t)p * dd + r * D + c] = sv[c];
+  }
 }
 
 // y_j - the forward-substitution row sums of column j (row r)
@@ -267,10 +281,11 @@ __device__ __forceinline__ double forward_rhs(const CholArgs& a, int j, int r) {
   return b - acc;
 }
 
-// y_j = L_jj^-1 b (lane r of a group holds b_r and row r of L_jj)
+// y_j = L_jj^-1 b (lane r of a group holds b_r and row r of L_jj), stored
+// by the lanes with `mine` set
 template <int D>
-__device__ __forceinline__ void forward_solve(const CholArgs& a, int j, int g, int r, int base, const double (&C)[D],
-                                              double b) {
+__device__ __forceinline__ void forward_solve(const CholArgs& a, int j, bool mine, int r, int base,
+                                              const double (&C)[D], double b) {
   double yv = 0.0;
 #pragma unroll
   for (int c = 0; c < D; ++c) {
@@ -278,7 +293,7 @@ __device__ __forceinline__ void forward_solve(const CholArgs& a, int j, int g, i
     const double yc = __shfl_sync(kFull, yv, base + c);
     if (r > c) b = fma(-C[c], yc, b);
   }
-  if (g == 0) a.y[(size_t)j * D + r] = yv;
+  if (mine) a.y[(size_t)j * D + r] = yv;
 }
 
 // phase B, one warp per column j: every lane group factors the diagonal
@@ -292,8 +307,8 @@ __device__ void column_warp(const CholArgs& a, int j, int lane) {
   const int base = (grp ? g : 0) * D;
   const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
   double C[D];
-  diag_partials<D>(a, p0, lane, r, C);
-  factor_diag<D>(a, lane, g, r, base, C);
+  diag_partials<D>(a, j, p0, lane, r, C);
+  factor_diag<D>(a, lane, g == 0, r, base, C);
   double Lf[dd];
 #pragma unroll
   for (int q = 0; q < D; ++q)
@@ -310,7 +325,7 @@ __device__ void column_warp(const CholArgs& a, int j, int lane) {
       solve_offdiag<D>(a, p, r, Lf, sv);
     }
   }
-  forward_solve<D>(a, j, g, r, base, C, forward_rhs<D>(a, j, r));
+  forward_solve<D>(a, j, g == 0, r, base, C, forward_rhs<D>(a, j, r));
 }
 
 __device__ __forceinline__ void team_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
@@ -330,8 +345,8 @@ __device__ void column_team(const CholArgs& a, int j, int tw, int lane, int bar,
   const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
   if (tw == 0) {
     double C[D];
-    diag_partials<D>(a, p0, lane, r, C);
-    factor_diag<D>(a, lane, g, r, base, C);
+    diag_partials<D>(a, j, p0, lane, r, C);
+    factor_diag<D>(a, lane, g == 0, r, base, C);
     if (g == 0) {
 #pragma unroll
       for (int c = 0; c < D; ++c) {
@@ -341,7 +356,7 @@ __device__ void column_team(const CholArgs& a, int j, int tw, int lane, int bar,
       }
     }
     team_sync(bar);
-    forward_solve<D>(a, j, g, r, base, C, sh[dd + r]);
+    forward_solve<D>(a, j, g == 0, r, base, C, sh[dd + r]);
   } else {
     const double b = forward_rhs<D>(a, j, r);
     if (g == 0) sh[dd + r] = b;
@@ -397,6 +412,39 @@ __device__ void backward_warp(const CholArgs& a, int j, int lane) {
     if (r < c) b = fma(-Lc[c], xc, b);
   }
   if (g == 0) a.y[(size_t)j * D + r] = xv;
+}
+
+// backward substitution for wide levels: every lane group takes a column of
+// its own (columns w0 + g of the level); lanes without a column (past the
+// level's end, or the spare lanes of a warp) mirror the warp's first column
+// and store nothing
+template <int D>
+__device__ void backward_groups(const CholArgs& a, int c0, int nc, int w0, int lane) {
+  constexpr int G = 32 / D, dd = D * D;
+  const int g = lane / D, r = lane % D;
+  const int w = w0 + (g < G ? g : 0);
+  const bool mine = g < G && w < nc;
+  const int base = (g < G ? g : 0) * D;
+  const int j = a.lvl_cols[c0 + (mine ? w : w0)];
+  double acc = 0.0;
+  for (int q = a.col_ptr[j] + 1; q < a.col_ptr[j + 1]; ++q) {
+    const double* B = a.L + (size_t)q * dd + r;
+    const double* xi = a.y + (size_t)a.blk_row[q] * D;
+#pragma unroll
+    for (int k = 0; k < D; ++k) acc = fma(B[k * D], xi[k], acc);
+  }
+  double b = a.y[(size_t)j * D + r] - acc;
+  double Lc[D];
+#pragma unroll
+  for (int c = 0; c < D; ++c) Lc[c] = a.Ldiag[(size_t)j * dd + c * D + r];
+  double xv = 0.0;
+#pragma unroll
+  for (int c = D - 1; c >= 0; --c) {
+    if (r == c) xv = b * Lc[c];
+    const double xc = __shfl_sync(kFull, xv, base + c);
+    if (r < c) b = fma(-Lc[c], xc, b);
+  }
+  if (mine) a.y[(size_t)j * D + r] = xv;
 }
 
 __device__ __forceinline__ void tail_coords(int t, int& bi, int& bj) {
@@ -732,8 +780,10 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   // columns, one warp each; one barrier after each
   for (int l = 0; l < a.levels; ++l) {
     const int t0 = a.lvl_task_ptr[l], t1 = a.lvl_task_ptr[l + 1];
-    for (int t = t0 + gw; t < t1; t += nw) run_task<D>(a, t, lane);
-    grid.sync();
+    if (t1 > t0) {  // (the leaves' level has none: no updates, no row sums)
+      for (int t = t0 + gw; t < t1; t += nw) run_task<D>(a, t, lane);
+      grid.sync();
+    }
     const int c0 = a.lvl_col_ptr[l], nc = a.lvl_col_ptr[l + 1] - c0;
     if (nc <= 2 * (int)gridDim.x) {
       // narrow level: at most two columns per CTA, each by a team of two
@@ -804,7 +854,14 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   }
   for (int l = a.levels - 1; l >= 0; --l) {
     const int c0 = a.lvl_col_ptr[l], nc = a.lvl_col_ptr[l + 1] - c0;
-    for (int w = gw; w < nc; w += nw) backward_warp<D>(a, a.lvl_cols[c0 + w], lane);
+    if (nc <= (kWarps - 1) * (int)gridDim.x) {
+      for (int w = gw; w < nc; w += nw) backward_warp<D>(a, a.lvl_cols[c0 + w], lane);
+    } else {
+      // more columns than warps 1..7 of the grid: G columns per warp instead
+      // of a second round
+      constexpr int G = 32 / D;
+      for (int w = gw; w * G < nc; w += nw) backward_groups<D>(a, c0, nc, w * G, lane);
+    }
     grid.sync();
   }
   // scatter to variable order, with the linearised cost change of the

@@ -500,6 +500,10 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
         const int j = p.lvl_cols[w];
         for (int q = p.col_ptr[j]; q < p.col_ptr[j + 1]; ++q) {
           p.btask[2 * q] = slot;
+          // the leaves' blocks have no update pairs (and the leaves no row
+          // sums): they get no task, the column's own phase reads its Hessian
+          // blocks directly, and the leaves' level has no task phase
+          if (l == 0) continue;
           int u = p.upd_ptr[q];
           do {
             const int e = std::min(u + p.chunk, p.upd_ptr[q + 1]);

@@ -93,8 +93,11 @@ struct Emu {
     }
   }
   void sparse_S(int q) {
+    const int j = p.blk_col[q], i = p.blk_row[q];
     for (int e = 0; e < dd; ++e) {
       double s = 0.0;
+      if (p.btask[2 * q + 1] == 0)  // no update pairs, no task: the Hessian block itself
+        s = i == j ? diag_entry(p.perm[j], e / d, e % d) : offdiag_entry(p.a_src, p.a_ptr[q], p.a_ptr[q + 1], e / d, e % d);
       for (int t = p.btask[2 * q]; t < p.btask[2 * q] + p.btask[2 * q + 1]; ++t) s += Spart[(size_t)t * dd + e];
       L[(size_t)q * dd + e] = s;
     }
