@@ -3,10 +3,12 @@
 
 #include <algorithm>
 #include <cmath>
+#include <exception>
 #include <functional>
 #include <queue>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <utility>
 
 namespace rpgo {
@@ -135,14 +137,16 @@ void order_variables(int N, std::vector<std::vector<int32_t>>& adj, std::vector<
 // whose closures are local (a thick chain) have separators a few variables
 // wide, so the elimination tree stays about log2(N) separators deep where
 // minimum degree, eliminating such a band from one end, makes it about N deep.
+// One recursion gives the orders for two leaf sizes (`out` for `leaf`, `out2`
+// for the larger `leaf2`): sets above leaf2 split the same way in both.
 struct NestedDissection {
   const std::vector<std::vector<int32_t>>& adj;
-  int leaf;
+  int leaf, leaf2;
   std::vector<int32_t> inset, vis, level;
   int set_id = 0, bfs_id = 0;
-  std::vector<int32_t> out;
-  NestedDissection(const std::vector<std::vector<int32_t>>& a, int lf)
-      : adj(a), leaf(lf), inset(a.size(), 0), vis(a.size(), 0), level(a.size(), 0) {}
+  std::vector<int32_t> out, out2;
+  NestedDissection(const std::vector<std::vector<int32_t>>& a, int lf, int lf2)
+      : adj(a), leaf(lf), leaf2(lf2), inset(a.size(), 0), vis(a.size(), 0), level(a.size(), 0) {}
 
   // breadth-first search inside the current set; returns the visit order
   void bfs(int root, std::vector<int32_t>* q) {
@@ -162,7 +166,14 @@ struct NestedDissection {
     }
   }
 
-  void run(std::vector<int32_t> nodes) {
+  // two: the set is still above leaf2 for the second order
+  void run(std::vector<int32_t> nodes, bool two) {
+    if (two && (int)nodes.size() <= leaf2) {
+      std::vector<int32_t> sorted = nodes;
+      std::sort(sorted.begin(), sorted.end());
+      out2.insert(out2.end(), sorted.begin(), sorted.end());
+      two = false;
+    }
     if ((int)nodes.size() <= leaf) {
       std::sort(nodes.begin(), nodes.end());
       out.insert(out.end(), nodes.begin(), nodes.end());
@@ -188,7 +199,7 @@ struct NestedDissection {
         for (int w : c) vis[w] = mark;
         comps.push_back(std::move(c));
       }
-      for (auto& c : comps) run(std::move(c));
+      for (auto& c : comps) run(std::move(c), two);
       return;
     }
     // pseudo-peripheral root: repeat the search from the farthest variable
@@ -200,7 +211,7 @@ struct NestedDissection {
       root = far;
       bfs(root, &q);
     }
-    bfs(root, &q);
+    // q and level now hold the search from root
     const int L = level[q.back()] + 1;
     std::vector<int32_t> cnt(L + 1, 0);
     for (int u : q) cnt[level[u]]++;
@@ -218,6 +229,7 @@ struct NestedDissection {
       // no balanced level split (a star or a tiny diameter): keep the set whole
       std::sort(nodes.begin(), nodes.end());
       out.insert(out.end(), nodes.begin(), nodes.end());
+      if (two) out2.insert(out2.end(), nodes.begin(), nodes.end());
       return;
     }
     std::vector<int32_t> A, B, S;
@@ -235,10 +247,11 @@ struct NestedDissection {
         (touches_next ? S : A).push_back(u);
       }
     }
-    run(std::move(A));
-    run(std::move(B));
+    run(std::move(A), two);
+    run(std::move(B), two);
     std::sort(S.begin(), S.end());
     out.insert(out.end(), S.begin(), S.end());
+    if (two) out2.insert(out2.end(), S.begin(), S.end());
   }
 };
 
@@ -315,22 +328,54 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
     c.cost = (3.0 * L + 2.0 * tiles + 4.0) * kPhaseUs + flops * kUsPerFlop;
     return c;
   };
-  std::vector<Candidate> cands;
+  // the three candidates are independent: minimum degree and the second
+  // nested-dissection order run on their own threads
+  std::vector<Candidate> cands(3);
+  std::exception_ptr err[2];
+  std::thread t_md([&] {
+    try {
+      std::vector<std::vector<int32_t>> a = adj, col_vars;
+      std::vector<int32_t> perm;
+      order_variables(N, a, &perm, &col_vars);
+      cands[0] = make_candidate(std::move(perm), col_vars);
+    } catch (...) {
+      err[0] = std::current_exception();
+    }
+  });
   {
-    std::vector<std::vector<int32_t>> a = adj, col_vars;
-    std::vector<int32_t> perm;
-    order_variables(N, a, &perm, &col_vars);
-    cands.push_back(make_candidate(std::move(perm), col_vars));
-  }
-  for (int leaf : {4, 32}) {
-    NestedDissection nd(adj, leaf);
+    // nested dissection with leaves of 4 and of 32 variables
+    NestedDissection nd(adj, 4, 32);
     std::vector<int32_t> all(N);
     for (int u = 0; u < N; ++u) all[u] = u;
-    nd.run(std::move(all));
-    std::vector<std::vector<int32_t>> a = adj, col_vars;
-    eliminate_in_order(a, nd.out, &col_vars);
-    cands.push_back(make_candidate(std::move(nd.out), col_vars));
+    try {
+      nd.run(std::move(all), true);
+    } catch (...) {
+      t_md.join();
+      throw;
+    }
+    std::thread t_nd([&] {
+      try {
+        std::vector<std::vector<int32_t>> a = adj, col_vars;
+        eliminate_in_order(a, nd.out2, &col_vars);
+        cands[2] = make_candidate(std::move(nd.out2), col_vars);
+      } catch (...) {
+        err[1] = std::current_exception();
+      }
+    });
+    try {
+      std::vector<std::vector<int32_t>> a = adj, col_vars;
+      eliminate_in_order(a, nd.out, &col_vars);
+      cands[1] = make_candidate(std::move(nd.out), col_vars);
+    } catch (...) {
+      t_nd.join();
+      t_md.join();
+      throw;
+    }
+    t_nd.join();
   }
+  t_md.join();
+  for (auto& e : err)
+    if (e) std::rethrow_exception(e);
   size_t best = 0;
   for (size_t c = 1; c < cands.size(); ++c)
     if (cands[c].cost < cands[best].cost) best = c;

@@ -46,6 +46,17 @@ void GpuNls::set_weights(const std::vector<double>& w) { s_.weights.upload(w, st
 
 double GpuNls::error_at_result() { return solver_error(s_, s_.x.get(), s_.weights.get(), st_); }
 
+double GpuNls::error_at_result(std::vector<double>* w) {
+  w->resize((size_t)s_.F);
+  if (s_.F == 0) return 0.0;
+  double* h = s_.pin.get(1);
+  const double* sum = enqueue_error_sum(s_, s_.x.get(), s_.weights.get(), st_);
+  RPGO_CUDA(cudaMemcpyAsync(h, sum, sizeof(double), cudaMemcpyDeviceToHost, st_));
+  s_.weights.download(w->data(), (size_t)s_.F, st_);
+  RPGO_CUDA(cudaStreamSynchronize(st_));
+  return h[0];
+}
+
 void GpuNls::write_back(ValueStore& values) const {
   scatter_rows((int64_t)keys_.size(), value_rows_.get(), s_.x.get(), dim_ == 3 ? 12 : 4, values.pose(), st_);
   RPGO_CUDA(cudaStreamSynchronize(st_));
@@ -155,6 +166,8 @@ void gnc_tls(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp
   const size_t F = (size_t)s.F;
   const int dof = s.d;
   std::vector<double> barc(F, g.threshold_mode == 0 ? g.threshold : 0.5 * chi2inv(g.threshold, dof));
+  DeviceBuffer<double> barc_dev;
+  barc_dev.upload(barc, stream);
   std::vector<double> weights(F, 1.0);
   if (init_weights) weights = *init_weights;
   nls.set_weights(weights);
@@ -175,13 +188,11 @@ void gnc_tls(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp
   }
   for (int it = 0; it < g.max_iterations; ++it) {
     st->gnc_iterations++;
-    solver_gnc_weights(s, s.x.get(), (int)n_known, barc, mu, stream);
+    solver_gnc_weights(s, s.x.get(), (int)n_known, barc_dev.get(), mu, stream);
     nls.optimize(lp, st);
-    const double cost = nls.error_at_result();
+    const double cost = nls.error_at_result(&weights);
     bool conv = std::fabs(cost - prev_cost) / std::max(prev_cost, 1e-7) < g.rel_cost_tol;
     if (!conv) {
-      s.weights.download(weights.data(), F, stream);
-      RPGO_CUDA(cudaStreamSynchronize(stream));
       conv = true;
       for (size_t k = 0; k < F; ++k)
         if (std::fabs(weights[k] - std::round(weights[k])) > g.weights_tol) {
@@ -204,6 +215,8 @@ bool gnc_tls_warm(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParam
   cudaStream_t stream = nls.stream();
   const size_t F = (size_t)s.F;
   std::vector<double> barc(F, g.threshold_mode == 0 ? g.threshold : 0.5 * chi2inv(g.threshold, s.d));
+  DeviceBuffer<double> barc_dev;
+  barc_dev.upload(barc, stream);
   std::vector<double> weights(F, 1.0), wnew(F, 1.0);
   size_t predicted = 0;
   for (size_t k = n_known; k < F; ++k) {
@@ -217,7 +230,7 @@ bool gnc_tls_warm(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParam
   bool fixed_point = F == n_known;
   for (int it = 0; it < g.max_iterations && !fixed_point; ++it) {
     st->gnc_iterations++;
-    solver_gnc_weights(s, s.x.get(), (int)n_known, barc, mu, stream);
+    solver_gnc_weights(s, s.x.get(), (int)n_known, barc_dev.get(), mu, stream);
     s.weights.download(wnew.data(), F, stream);
     RPGO_CUDA(cudaStreamSynchronize(stream));
     bool same = true;

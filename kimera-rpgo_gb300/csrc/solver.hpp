@@ -45,6 +45,8 @@ class GpuNls {
   // dev().x); result left in dev().x
   void optimize(const LmParams& p, NlsStats* st, bool from_current = false);
   double error_at_result();
+  // the same, with the current weights copied to w in the same wait
+  double error_at_result(std::vector<double>* w);
   // GenericSolver::updateValues: write the result back into the value rows
   void write_back(ValueStore& values) const;
   SolverDev& dev() { return s_; }

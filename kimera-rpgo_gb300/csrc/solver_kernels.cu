@@ -1197,7 +1197,7 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
 }
 
 // enqueue k_factor_err_sum: the sum lands in s.red[blocks]
-static double* enqueue_error_sum(SolverDev& s, const double* x, const double* weights, cudaStream_t st) {
+double* enqueue_error_sum(SolverDev& s, const double* x, const double* weights, cudaStream_t st) {
   const int blocks = std::min(256, div_up(s.F, 256));
   if (s.ticket.size() == 0) {
     s.ticket.resize(1);
@@ -1748,7 +1748,7 @@ void solver_retract(SolverDev& s, cudaStream_t st) {
   RPGO_LAUNCHED();
 }
 
-void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const std::vector<double>& barc, double mu,
+void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const double* barc, double mu,
                         cudaStream_t st) {
   if (s.F == 0) return;
   const int tb = 128;
@@ -1759,11 +1759,8 @@ void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const std::v
     k_factor_err<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                     s.sqrt_info.get(), x, nullptr, s.ferr.get());
   RPGO_LAUNCHED();
-  DeviceBuffer<double> d_barc;
-  d_barc.upload(barc, st);
-  k_gnc_weights<<<div_up(s.F, tb), tb, 0, st>>>(s.F, n_known, s.ferr.get(), d_barc.get(), mu, s.weights.get());
+  k_gnc_weights<<<div_up(s.F, tb), tb, 0, st>>>(s.F, n_known, s.ferr.get(), barc, mu, s.weights.get());
   RPGO_LAUNCHED();
-  RPGO_CUDA(cudaStreamSynchronize(st));
 }
 
 }  // namespace rpgo

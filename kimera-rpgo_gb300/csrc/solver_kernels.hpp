@@ -84,8 +84,13 @@ SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st);
 SolveOut solver_solve_eval(SolverDev& s, double lambda, cudaStream_t st, double* nerr);
 // xnew = x (+) delta
 void solver_retract(SolverDev& s, cudaStream_t st);
-// TLS weights (GncOptimizer::calculateWeights) for factors >= n_known
-void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const std::vector<double>& barc, double mu,
+// enqueue the weighted error of x (one launch); returns the device word that
+// will hold it
+double* enqueue_error_sum(SolverDev& s, const double* x, const double* weights, cudaStream_t st);
+// TLS weights (GncOptimizer::calculateWeights) for factors >= n_known, with
+// the per-factor thresholds barc on the device; enqueued only (the stream
+// orders them before the next solve)
+void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const double* barc, double mu,
                         cudaStream_t st);
 
 }  // namespace rpgo
