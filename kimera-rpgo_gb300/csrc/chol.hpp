@@ -26,12 +26,17 @@ struct CholDev {
   DeviceBuffer<double> Spart; // level-task partial sums (D x D per task)
   DeviceBuffer<double> Tpart; // tail row task sums (D per task)
   DeviceBuffer<double> out;   // model change, status
+  DeviceBuffer<double> Hs;    // H in the block layout of L (per linearisation)
+  DeviceBuffer<double> dampS; // damping diagonal of the diagonal blocks, same layout
   DeviceBuffer<int32_t> status;
   cudaEvent_t ev[2] = {nullptr, nullptr};  // around each launch (kernel time)
   ~CholDev();
   void upload(CholPlan&& p, cudaStream_t st);
 };
 
+// H and the damping diagonal in the block layout of L, from the linearised
+// system (Hd64, fH64, dampD); enqueued after every linearisation.
+void chol_block_hessian(SolverDev& s, CholDev& c, cudaStream_t st);
 // Solve with the factorisation of (H + lambda D); fills s.delta.
 SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st);
 // Enqueue the same solve without waiting: the model change and the status

@@ -52,6 +52,7 @@ struct CholArgs {
   const double *Hd64, *fH64, *dampD, *g;
   double lam;
   double *L, *Ldiag, *M, *Ldd, *y, *delta, *part, *out, *Spart, *Tpart;
+  const double *Hs, *dampS;  // Hessian and damping diagonal in the factor's block layout
   int32_t* status;
 };
 
@@ -80,6 +81,16 @@ __device__ __forceinline__ double gather_diag(const CholArgs& a, int v, int r, i
   return s;
 }
 
+// entry (r, c) of sparse block p of H + lambda D from the block layout
+// (the same values and additions as gather_diag / gather_offdiag)
+template <int D>
+__device__ __forceinline__ double block_H(const CholArgs& a, int p, bool diag, int r, int c) {
+  constexpr int dd = D * D;
+  double s = a.Hs[(size_t)p * dd + r * D + c];
+  if (diag && r == c) s += a.lam * a.dampS[(size_t)p * D + r];
+  return s;
+}
+
 constexpr unsigned kFull = 0xffffffffu;
 
 // Sparse levels use lane groups: a warp holds 32 / D groups of D lanes and
@@ -104,23 +115,16 @@ __device__ void run_task(const CholArgs& a, int t, int lane) {
   constexpr int NC = D == 6 ? 3 : D;  // output columns of one block task
   const int g = lane / D, r = lane % D;
   const int4 tk = reinterpret_cast<const int4*>(a.tasks)[t];
-  const int kind = tk.w & 3, slot = tk.w >> 3;
+  const int kind = tk.w & 3, slot = tk.w >> 4;
   if (kind < 2) {
     const int p = tk.x, c0 = ((tk.w >> 2) & 1) * NC;
     double acc[NC];
 #pragma unroll
     for (int c = 0; c < NC; ++c) acc[c] = 0.0;
     if (kind == 1 && g == 0) {
-      const int j = a.blk_col[p], i = a.blk_row[p];
-      if (i == j) {
-        const int v = a.perm[j];
+      const bool diag = (tk.w >> 3) & 1;
 #pragma unroll
-        for (int c = 0; c < NC; ++c) acc[c] = gather_diag<D>(a, v, r, c0 + c);
-      } else {
-#pragma unroll
-        for (int c = 0; c < NC; ++c)
-          acc[c] = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], r, c0 + c);
-      }
+      for (int c = 0; c < NC; ++c) acc[c] = block_H<D>(a, p, diag, r, c0 + c);
     }
     if (g < G) {
       for (int u = tk.y + g; u < tk.z; u += G) {
@@ -171,7 +175,7 @@ __device__ __forceinline__ void sum_partials(const CholArgs& a, int p, int r, do
   const int t0 = a.btask[2 * p], nt = a.btask[2 * p + 1];
   if (nt == 0) {
 #pragma unroll
-    for (int c = 0; c < D; ++c) s[c] = gather_offdiag<D>(a.fH64, a.a_src, a.a_ptr[p], a.a_ptr[p + 1], r, c);
+    for (int c = 0; c < D; ++c) s[c] = block_H<D>(a, p, false, r, c);
     return;
   }
 #pragma unroll
@@ -196,9 +200,8 @@ __device__ __forceinline__ void diag_partials(const CholArgs& a, int j, int p, i
   const bool has0 = lane < dd, has1 = lane + 32 < dd;
   double e0 = 0.0, e1 = 0.0;
   if (t1 == t0) {
-    const int v = a.perm[j];
-    if (has0) e0 = gather_diag<D>(a, v, lane / D, lane % D);
-    if (has1) e1 = gather_diag<D>(a, v, (lane + 32) / D, (lane + 32) % D);
+    if (has0) e0 = block_H<D>(a, p, true, lane / D, lane % D);
+    if (has1) e1 = block_H<D>(a, p, true, (lane + 32) / D, (lane + 32) % D);
   }
   for (int t = t0; t < t1; t += 4) {
     double x[4], y[4];
@@ -902,6 +905,29 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   }
 }
 
+// H (and the damping diagonal, on diagonal blocks) in the factor's block
+// layout, once per linearisation: thread per block entry; an off-diagonal
+// block sums its factors' blocks in the plan's order (as gather_offdiag).
+template <int D>
+__global__ void k_block_hessian(int nblk, const int32_t* __restrict__ blk_row, const int32_t* __restrict__ blk_col,
+                                const int32_t* __restrict__ perm, const int32_t* __restrict__ a_ptr,
+                                const int32_t* __restrict__ a_src, const double* __restrict__ Hd64,
+                                const double* __restrict__ fH64, const double* __restrict__ dampD,
+                                double* __restrict__ Hs, double* __restrict__ dampS) {
+  constexpr int dd = D * D;
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nblk * dd) return;
+  const int p = (int)(t / dd), e = (int)(t % dd), r = e / D, c = e % D;
+  const int j = blk_col[p];
+  if (blk_row[p] == j) {
+    const int v = perm[j];
+    Hs[t] = Hd64[(size_t)v * dd + e];
+    if (r == c) dampS[(size_t)p * D + r] = dampD[(size_t)v * D + r];
+  } else {
+    Hs[t] = gather_offdiag<D>(fH64, a_src, a_ptr[p], a_ptr[p + 1], r, c);
+  }
+}
+
 }  // namespace
 
 void CholDev::upload(CholPlan&& p, cudaStream_t st) {
@@ -936,6 +962,8 @@ void CholDev::upload(CholPlan&& p, cudaStream_t st) {
   Tpart.resize(std::max<size_t>(1, plan.ttasks.size() / 3 * (size_t)plan.d));
   const size_t dd = (size_t)plan.d * plan.d, ntp = (size_t)plan.n_tiles * kTB;
   L.resize(std::max<size_t>(1, plan.blk_row.size() * dd));
+  Hs.resize(std::max<size_t>(1, plan.blk_row.size() * dd));
+  dampS.resize(std::max<size_t>(1, plan.blk_row.size() * plan.d));
   Ldiag.resize(std::max<size_t>(1, (size_t)plan.n_sparse * dd));
   M.resize(std::max<size_t>(1, ntp * ntp));
   Ldd.resize(std::max<size_t>(1, (size_t)plan.n_tiles * kTB * kTB));
@@ -947,6 +975,22 @@ void CholDev::upload(CholPlan&& p, cudaStream_t st) {
 CholDev::~CholDev() {
   for (auto& e : ev)
     if (e) cudaEventDestroy(e);
+}
+
+void chol_block_hessian(SolverDev& s, CholDev& c, cudaStream_t st) {
+  const int nblk = (int)c.plan.blk_row.size();
+  if (nblk == 0) return;
+  const int tb = 256;
+  const int64_t n = (int64_t)nblk * c.plan.d * c.plan.d;
+  if (s.dim == 3)
+    k_block_hessian<6><<<div_up(n, tb), tb, 0, st>>>(nblk, c.blk_row.get(), c.blk_col.get(), c.perm.get(),
+                                                    c.a_ptr.get(), c.a_src.get(), s.Hd64.get(), s.fH64.get(),
+                                                    s.dampD.get(), c.Hs.get(), c.dampS.get());
+  else
+    k_block_hessian<3><<<div_up(n, tb), tb, 0, st>>>(nblk, c.blk_row.get(), c.blk_col.get(), c.perm.get(),
+                                                    c.a_ptr.get(), c.a_src.get(), s.Hd64.get(), s.fH64.get(),
+                                                    s.dampD.get(), c.Hs.get(), c.dampS.get());
+  RPGO_LAUNCHED();
 }
 
 void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, double* host) {
@@ -970,7 +1014,7 @@ void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, doub
              c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), c.ttasks.get(), c.ttask_ptr.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
              s.g.get(), lambda, c.L.get(), c.Ldiag.get(),
              c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.Spart.get(), c.Tpart.get(),
-             c.status.get()};
+             c.Hs.get(), c.dampS.get(), c.status.get()};
   void* args[] = {&a};
   RPGO_CUDA(cudaEventRecord(c.ev[0], st));
   if (s.dim == 3)
@@ -1019,7 +1063,7 @@ SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st) {
              c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), c.ttasks.get(), c.ttask_ptr.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
              s.g.get(), lambda, c.L.get(), c.Ldiag.get(),
              c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.Spart.get(), c.Tpart.get(),
-             c.status.get()};
+             c.Hs.get(), c.dampS.get(), c.status.get()};
   void* args[] = {&a};
   double ms = 0.0;
   {

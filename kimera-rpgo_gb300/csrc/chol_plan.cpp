@@ -553,7 +553,9 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
           do {
             const int e = std::min(u + p.chunk, p.upd_ptr[q + 1]);
             const int kind = u == p.upd_ptr[q] ? 1 : 0;
-            for (int h = 0; h < halves; ++h) p.tasks.insert(p.tasks.end(), {q, u, e, kind | h << 2 | slot << 3});
+            const int diag = q == p.col_ptr[j] ? 1 : 0;
+            for (int h = 0; h < halves; ++h)
+              p.tasks.insert(p.tasks.end(), {q, u, e, kind | h << 2 | diag << 3 | slot << 4});
             ++slot;
             u = e;
           } while (u < p.upd_ptr[q + 1]);
@@ -561,7 +563,7 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
         }
         p.ftask[2 * j] = slot;
         for (int u = p.row_ptr[j]; u < p.row_ptr[j + 1]; u += p.row_chunk) {
-          p.tasks.insert(p.tasks.end(), {j, u, std::min(u + p.row_chunk, p.row_ptr[j + 1]), 2 | slot << 3});
+          p.tasks.insert(p.tasks.end(), {j, u, std::min(u + p.row_chunk, p.row_ptr[j + 1]), 2 | slot << 4});
           ++slot;
         }
         p.ftask[2 * j + 1] = slot - p.ftask[2 * j];

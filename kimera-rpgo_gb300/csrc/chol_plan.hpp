@@ -36,7 +36,8 @@ struct CholPlan {
   // elimination-tree levels of the sparse columns (leaves first)
   std::vector<int32_t> lvl_col_ptr, lvl_cols;  // columns per level
   // Tasks of the sparse levels, 4 ints each (id, first, end, code), code =
-  // kind | half << 2 | slot << 3; each writes partial sums to its slot:
+  // kind | half << 2 | diagonal block << 3 | slot << 4; each writes partial
+  // sums to its slot:
   //  kind 0 / 1: block id's update list [first, end) cut into chunks of at
   //    most `chunk` pairs (kind 1 on the block's first chunk, which also
   //    carries the Hessian block); for 6x6 blocks every chunk is two tasks,

@@ -1272,6 +1272,7 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
                                                   s.fH64.get(), s.fg.get(), s.Hd64.get(), s.g.get(), s.dampD.get(),
                                                   diagonal_damping ? 1 : 0);
     RPGO_LAUNCHED();
+    chol_block_hessian(s, *s.chol, st);
     return;
   }
   if (s.dim == 3)

@@ -70,7 +70,7 @@ struct Emu {
   std::vector<double> Spart;  // task partial sums
   void run_task(int t) {
     const int* tk = &p.tasks[4 * (size_t)t];
-    const int kind = tk[3] & 3, slot = tk[3] >> 3;
+    const int kind = tk[3] & 3, slot = tk[3] >> 4;
     if (kind < 2) {
       const int q = tk[0], j = p.blk_col[q], i = p.blk_row[q];
       const int nc = d == 6 ? 3 : d, c0 = ((tk[3] >> 2) & 1) * nc;
