@@ -94,25 +94,30 @@ __device__ __forceinline__ void se3_logmap_derivative(const double* xi, double* 
     c = (2.0 * th - 3.0 * s + th * co) / (2.0 * th2 * th2 * th);
     beta = (1.0 - th * s / (2.0 * (1.0 - co))) / th2;
   }
-  double W[9], V[9], WV[9], VW[9], WVW[9], WW[9], T1[9];
+  // Q of the SE(3) Jacobian, with the products of the skew matrices W = [w]x
+  // and V = [r]x in closed form ([a]x[b]x = b a^T - (a.b) I, [a]x[b]x[a]x =
+  // -(a.b)[a]x): WV + VW - WVW = r w^T + w r^T - 2 (w.r) I + (w.r) W;
+  // WWV + VWW - 3 WVW = w (w x r)^T - (w x r) w^T - 2 th2 V + 3 (w.r) W;
+  // WVWW + WWVW = -2 (w.r) WW, with WW = w w^T - th2 I
+  double W[9], V[9], WW[9], T1[9];
   skew(w, W);
   skew(r, V);
-  mat3mul(W, V, WV);
-  mat3mul(V, W, VW);
-  mat3mul(WV, W, WVW);
-  mat3mul(W, W, WW);
-  double Q[9];
-  {
-    double WWV[9], VWW[9], WVWW[9], WWVW[9];
-    mat3mul(WW, V, WWV);
-    mat3mul(VW, W, VWW);
-    mat3mul(WVW, W, WVWW);
-    mat3mul(W, WVW, WWVW);
+  const double wr = w[0] * r[0] + w[1] * r[1] + w[2] * r[2];
+  const double wxr[3] = {w[1] * r[2] - w[2] * r[1], w[2] * r[0] - w[0] * r[2], w[0] * r[1] - w[1] * r[0]};
 #pragma unroll
-    for (int i = 0; i < 9; ++i)
-      Q[i] = -0.5 * V[i] + a * (WV[i] + VW[i] - WVW[i]) + b * (WWV[i] + VWW[i] - 3.0 * WVW[i]) +
-             c * (WVWW[i] + WWVW[i]);
-  }
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) WW[3 * i + j] = w[i] * w[j] - (i == j ? th2 : 0.0);
+  double Q[9];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int k = 3 * i + j;
+      const double ta = r[i] * w[j] + w[i] * r[j] - (i == j ? 2.0 * wr : 0.0) + wr * W[k];
+      const double tb = w[i] * wxr[j] - wxr[i] * w[j] - 2.0 * th2 * V[k] + 3.0 * wr * W[k];
+      Q[k] = -0.5 * V[k] + a * ta + b * tb - 2.0 * c * wr * WW[k];
+    }
   double Ji[9];
 #pragma unroll
   for (int i = 0; i < 9; ++i) Ji[i] = 0.5 * W[i] + beta * WW[i] + ((i % 4 == 0) ? 1.0 : 0.0);
