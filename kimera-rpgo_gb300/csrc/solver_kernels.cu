@@ -79,8 +79,12 @@ __global__ void k_factor_err(int F, const int32_t* __restrict__ kind, const int3
 // grid-stride share (fixed tree order) into part[block]; the last block to
 // finish (ticket counter, reset for the next launch) adds the partials in
 // block order into *sum, so the result does not depend on scheduling.
+// The error sum runs on blocks of two warps, so that its ~F/32 warps spread
+// over the SMs (one per FP64 sub-partition) instead of crowding a few.
+constexpr int kErrThreads = 64;
+
 template <int DIM>
-__global__ void __launch_bounds__(256) k_factor_err_sum(int F, const int32_t* __restrict__ kind,
+__global__ void __launch_bounds__(kErrThreads) k_factor_err_sum(int F, const int32_t* __restrict__ kind,
                                                         const int32_t* __restrict__ vi,
                                                         const int32_t* __restrict__ vj, const double* __restrict__ z,
                                                         const double* __restrict__ R, const double* __restrict__ x,
@@ -88,7 +92,7 @@ __global__ void __launch_bounds__(256) k_factor_err_sum(int F, const int32_t* __
                                                         unsigned int* __restrict__ ticket, double* __restrict__ sum) {
   using L = SLie<DIM>;
   constexpr int d = L::d, st = L::stride;
-  __shared__ double sh[256];
+  __shared__ double sh[kErrThreads];
   __shared__ bool last;
   double acc = 0.0;
   for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < F; f += gridDim.x * blockDim.x) {
@@ -118,7 +122,7 @@ __global__ void __launch_bounds__(256) k_factor_err_sum(int F, const int32_t* __
   }
   sh[threadIdx.x] = acc;
   __syncthreads();
-  for (int o = 128; o; o >>= 1) {
+  for (int o = kErrThreads / 2; o; o >>= 1) {
     if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
     __syncthreads();
   }
@@ -128,12 +132,22 @@ __global__ void __launch_bounds__(256) k_factor_err_sum(int F, const int32_t* __
     last = atomicAdd(ticket, 1u) == gridDim.x - 1;
   }
   __syncthreads();
-  if (last && threadIdx.x == 0) {
+  if (last) {
+    // the last block adds the block sums: thread t takes t, t + 64, ... in
+    // order, then a fixed tree (the same order for the same grid)
     __threadfence();
     double t = 0.0;
-    for (int b = 0; b < (int)gridDim.x; ++b) t += ((volatile double*)part)[b];
-    *sum = t;
-    *ticket = 0u;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += kErrThreads) t += ((volatile double*)part)[b];
+    sh[threadIdx.x] = t;
+    __syncthreads();
+    for (int o = kErrThreads / 2; o; o >>= 1) {
+      if ((int)threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      *sum = sh[0];
+      *ticket = 0u;
+    }
   }
 }
 
@@ -1198,18 +1212,18 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
 
 // enqueue k_factor_err_sum: the sum lands in s.red[blocks]
 double* enqueue_error_sum(SolverDev& s, const double* x, const double* weights, cudaStream_t st) {
-  const int blocks = std::min(256, div_up(s.F, 256));
+  const int blocks = std::min(1024, div_up(s.F, kErrThreads));
   if (s.ticket.size() == 0) {
     s.ticket.resize(1);
     s.ticket.zero(st);
   }
   s.red.resize(blocks + 1);
   if (s.dim == 3)
-    k_factor_err_sum<3><<<blocks, 256, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+    k_factor_err_sum<3><<<blocks, kErrThreads, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                 s.sqrt_info.get(), x, weights, s.red.get(), s.ticket.get(),
                                                 s.red.get() + blocks);
   else
-    k_factor_err_sum<2><<<blocks, 256, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+    k_factor_err_sum<2><<<blocks, kErrThreads, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                 s.sqrt_info.get(), x, weights, s.red.get(), s.ticket.get(),
                                                 s.red.get() + blocks);
   RPGO_LAUNCHED();
