@@ -5,10 +5,13 @@
 //  1. init: right-hand side in elimination order, padding of the dense tail;
 //  2. per elimination-tree level of the sparse columns (leaves first):
 //     (A) the level's tasks over all warps: for every block, its Hessian
-//         block minus chunks of its L(i,k) L(j,k)^T updates, and chunks of
-//         every column's forward-substitution row sum;
-//     (B) every column by one warp: S_jj from the partial sums, L_jj =
-//         chol(S_jj), L_ij = S_ij L_jj^-T, and y_j;
+//         block (read from the block layout Hs that k_block_hessian writes
+//         once per linearisation) minus chunks of its L(i,k) L(j,k)^T
+//         updates, and chunks of every column's forward-substitution row
+//         sum; the leaves have no tasks;
+//     (B) every column by one warp (narrow levels: a team of two warps):
+//         S_jj from the partial sums, L_jj = chol(S_jj), L_ij = S_ij
+//         L_jj^-T, and y_j;
 //  3. the dense tail: its blocks from H and the sparse updates (one CTA per
 //     block), then a right-looking tiled Cholesky with one barrier per tile
 //     column: in phase k the CTAs of tile column k apply the update of column
@@ -780,7 +783,7 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   grid.sync();
 
   // 2. sparse levels: (A) the level's tasks over all warps, (B) its
-  // columns, one warp each; one barrier after each
+  // columns, one warp or a two-warp team each; one barrier after each
   for (int l = 0; l < a.levels; ++l) {
     const int t0 = a.lvl_task_ptr[l], t1 = a.lvl_task_ptr[l + 1];
     if (t1 > t0) {  // (the leaves' level has none: no updates, no row sums)
