@@ -196,7 +196,12 @@ __global__ void k_linearize_a(int F, const int32_t* __restrict__ kind, const int
                               const double* __restrict__ w, double* __restrict__ rec) {
   using L = SLie<DIM>;
   constexpr int d = L::d, st = L::stride, dd = d * d, RS = d + 2 * dd + 1;
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  // two threads per factor (the FP64 chain of one thread is the cost, and
+  // one thread per factor fills only about a quarter of the SM
+  // sub-partitions): both form the residual; role 1 then the log-map
+  // Jacobian, role 0 the whitened residual and the adjoint
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = t >> 1, role = t & 1;
   if (f >= F) return;
   const bool between = kind[f] == 0;
   typename L::Pose Xi, Z, rel, h;
@@ -205,21 +210,26 @@ __global__ void k_linearize_a(int F, const int32_t* __restrict__ kind, const int
   double e[d];
   double* out = rec + (size_t)f * RS;
   if (between) {
-    typename L::Pose Xj, hinv;
+    typename L::Pose Xj;
     L::load(x + (size_t)vj[f] * st, Xj);
     L::between(Xi, Xj, h);
     L::between(Z, h, rel);
     L::logmap(rel, e);
-    double D[dd], Ad[dd];
-    L::dlog(e, D);
+    if (role == 1) {
+      double D[dd];
+      L::dlog(e, D);
+#pragma unroll
+      for (int i = 0; i < dd; ++i) out[d + i] = D[i];
+      return;
+    }
+    typename L::Pose hinv;
+    double Ad[dd];
     L::inverse(h, hinv);
     L::adjoint(hinv, Ad);
 #pragma unroll
-    for (int i = 0; i < dd; ++i) {
-      out[d + i] = D[i];
-      out[d + dd + i] = Ad[i];
-    }
+    for (int i = 0; i < dd; ++i) out[d + dd + i] = Ad[i];
   } else {
+    if (role == 1) return;
     L::between(Xi, Z, rel);
     L::logmap(rel, e);
 #pragma unroll
@@ -1261,13 +1271,13 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
     s.lin_rec.resize((size_t)s.F * rs);
     const int per_block = 4 * (32 / d);  // k_linearize_b: 4 warps of 32/d factors
     if (s.dim == 3) {
-      k_linearize_a<3><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+      k_linearize_a<3><<<div_up(2 * (int64_t)s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                        s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get());
       RPGO_LAUNCHED();
       k_linearize_b<3><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
                                                                s.fH.get(), s.fH64.get(), s.fg.get());
     } else {
-      k_linearize_a<2><<<div_up(s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+      k_linearize_a<2><<<div_up(2 * (int64_t)s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                        s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get());
       RPGO_LAUNCHED();
       k_linearize_b<2><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
