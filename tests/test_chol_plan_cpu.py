@@ -114,3 +114,15 @@ def test_emulated_direct_solve_reports_indefinite_system(emu):
     H[21:24, 21:24] -= 1e6 * np.eye(d)
     x, ref, info = _run(emu, 30, d, (kind, vi, vj, Hd, fH, H, damp, rhs), 0.0)
     assert info[4] == 1
+
+
+def test_plan_is_deterministic(emu):
+    # the plan's candidate orders are computed on several threads; the chosen
+    # plan, and so the emulated solve, must not depend on their timing
+    d = 6
+    edges = _pose_graph(500, 150, 12)
+    sysm = _system(500, d, edges, [0], 12)
+    runs = [_run(emu, 500, d, sysm, 1e-3) for _ in range(4)]
+    for x, _, info in runs[1:]:
+        assert np.array_equal(x, runs[0][0])
+        assert np.array_equal(info, runs[0][2])
