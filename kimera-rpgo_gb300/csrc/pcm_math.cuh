@@ -10,9 +10,9 @@
 // Every result is a fixed sequence of correctly rounded IEEE double
 // operations: products, sums and quotients go through __dmul_rn / __dadd_rn /
 // __dsub_rn / __ddiv_rn / __dsqrt_rn / __fma_rn, which the compiler never
-// fuses or reorders. The sequence is the one documented operation by
-// operation in DESIGN.md ("FP64 operation order"), so a host implementation
-// that follows it with -ffp-contract=off produces the same bits.
+// fuses or reorders. The functions below spell the sequence out operation by
+// operation, so a host implementation that follows it with
+// -ffp-contract=off produces the same bits.
 #pragma once
 #include <cstdint>
 
