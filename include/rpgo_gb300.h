@@ -235,6 +235,29 @@ int rpgo_get_factors(const rpgo_solver* s, int32_t* kind, uint64_t* key_front, u
  * pairwise consistent. Returns the group size in *n. */
 int rpgo_get_adjacency(const rpgo_solver* s, int32_t group, uint32_t* words, int64_t capacity, int64_t* n);
 int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* out);
+
+/* ---- temporary factors and values (GenericSolver.h:46-65,
+ * RobustSolver.cpp:115-121, 169, 208, 264, 295; GenericSolver.cpp:37-45).
+ * They are optimised together with the graph by every later optimisation
+ * (appended after it; under GNC they are not known inliers), never pass
+ * outlier rejection, and are not part of calculateEstimate(); the solve
+ * updates their values. Host pointers. */
+/* updateTempFactorsValues: append (RPGO_ERR_KEY when a value key exists in
+ * the graph's or the temporary values) */
+int rpgo_update_temp_factors_values(rpgo_solver* s, const rpgo_factor_batch* factors,
+                                    const rpgo_value_batch* values);
+/* replaceTempFactorsValues: replace both sets */
+int rpgo_replace_temp_factors_values(rpgo_solver* s, const rpgo_factor_batch* factors,
+                                     const rpgo_value_batch* values);
+/* clearTempFactorsValues */
+int rpgo_clear_temp_factors_values(rpgo_solver* s);
+/* getTempFactorsUnsafe().size() and getTempValues().size() */
+int rpgo_get_temp_sizes(const rpgo_solver* s, int64_t* num_factors, int64_t* num_values);
+/* getTempValues(): keys ascending, poses as rpgo_get_estimate */
+int rpgo_get_temp_values(const rpgo_solver* s, uint64_t* keys, double* poses, int64_t capacity);
+/* getGncTempWeights(): one weight per temporary factor of the last
+ * optimisation (all 1 when it ran without GNC); *n = their number */
+int rpgo_get_gnc_temp_weights(const rpgo_solver* s, double* weights, int64_t capacity, int64_t* n);
 /* ---- edit API (src/RobustSolver.cpp:371-446, Pcm.h:299-408). Each edit
  * then re-optimises like the reference (removePriorFactorsWithPrefix only when
  * optimize_graph != 0); values are not changed by the edit itself. */

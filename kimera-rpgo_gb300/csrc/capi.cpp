@@ -36,6 +36,9 @@ struct rpgo_solver {
   std::unique_ptr<ValueStore> values;  // GenericSolver::values_ (device rows)
   std::unique_ptr<FactorStore> store;  // every factor measurement ever added (device rows)
   std::vector<FactorRec> nfg;          // GenericSolver::nfg_ (kinds, keys, store rows)
+  std::vector<FactorRec> temp_nfg;     // GenericSolver::temp_nfg_ (measurements in `store`)
+  std::unique_ptr<ValueStore> temp_values;  // GenericSolver::temp_values_
+  std::vector<double> gnc_temp_weights;     // RobustSolver::gnc_temp_weights_
   std::unique_ptr<PcmEngine> pcm;
   std::vector<double> gnc_weights;
   size_t gnc_num_inliers = 0, latest_num_lc = 0;
@@ -236,12 +239,49 @@ void multirobot_align(rpgo_solver* s) {
   }
 }
 
+// keys of a value store in row order
+std::vector<uint64_t> keys_by_row(const ValueStore& v) {
+  std::vector<uint64_t> k(v.size());
+  for (const auto& kv : v.rows()) k[(size_t)kv.second] = kv.first;
+  return k;
+}
+
+// The values the optimiser sees (RobustSolver.cpp:117-120: values_ merged
+// with temp_values_): the graph's store itself, or a merged copy whose rows
+// are the graph's rows followed by the temporary ones.
+struct SolveValues {
+  rpgo_solver* s;
+  std::unique_ptr<ValueStore> merged;
+  explicit SolveValues(rpgo_solver* sv) : s(sv) {
+    if (s->temp_values->size() == 0) return;
+    merged = std::make_unique<ValueStore>(s->stride);
+    const std::vector<uint64_t> k0 = keys_by_row(*s->values), k1 = keys_by_row(*s->temp_values);
+    merged->append((int64_t)k0.size(), k0.data(), s->values->pose(), true, s->st);
+    merged->append((int64_t)k1.size(), k1.data(), s->temp_values->pose(), true, s->st);
+  }
+  ValueStore& get() { return merged ? *merged : *s->values; }
+  // GenericSolver::updateValues (src/GenericSolver.cpp:37-45): results back
+  // into the graph's and the temporary values
+  void write_back(GpuNls& nls) {
+    nls.write_back(get());
+    if (!merged) return;
+    const size_t n0 = s->values->size(), n1 = s->temp_values->size(), st = (size_t)s->stride;
+    RPGO_CUDA(cudaMemcpyAsync(s->values->pose(), merged->pose(), n0 * st * sizeof(double), cudaMemcpyDeviceToDevice,
+                              s->st));
+    RPGO_CUDA(cudaMemcpyAsync(s->temp_values->pose(), merged->pose() + n0 * st, n1 * st * sizeof(double),
+                              cudaMemcpyDeviceToDevice, s->st));
+    RPGO_CUDA(cudaStreamSynchronize(s->st));
+  }
+};
+
 // RobustSolver::optimize (src/RobustSolver.cpp:115-306)
 int optimize(rpgo_solver* s) {
   LmParams lp;
   lp.gauss_newton = s->p.solver == RPGO_SOLVER_GN;
   lp.diagonal_damping = s->p.lm_diagonal_damping != 0;
   std::vector<FactorRec> full = s->nfg;
+  full.insert(full.end(), s->temp_nfg.begin(), s->temp_nfg.end());
+  SolveValues sv(s);
   NlsStats st;
   const size_t num_lc = s->pcm ? s->pcm->num_lc() : 0;
   if (s->p.use_gnc && s->pcm && !(s->p.gnc_fix_prev_inliers && num_lc == s->latest_num_lc)) {
@@ -258,7 +298,7 @@ int optimize(rpgo_solver* s) {
       init.assign(full.size(), 0.0);
       for (size_t i = 0; i < n_known && i < init.size(); ++i) init[i] = 1.0;
     }
-    GpuNls nls(s->dim, full, *s->store, *s->values, s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
+    GpuNls nls(s->dim, full, *s->store, sv.get(), s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
     nls.dev().coop_ctas = s->coop_ctas;
     if (s->p.gnc_warm_start == RPGO_WARM_ON || s->p.gnc_warm_start == RPGO_WARM_RECORD)
       closure_features_and_probs(s, nls, full, n_known);
@@ -271,8 +311,9 @@ int optimize(rpgo_solver* s) {
     }
     s->warm_probs.clear();
     if (!warm_done) gnc_tls(nls, n_known, g, lp, s->p.gnc_bias_odom ? &init : nullptr, &w, &st);
-    nls.write_back(*s->values);
+    sv.write_back(nls);
     s->gnc_weights.assign(w.begin(), w.begin() + std::min(w.size(), s->nfg.size()));
+    s->gnc_temp_weights.assign(w.begin() + std::min(w.size(), s->nfg.size()), w.end());
     const double sum = std::accumulate(s->gnc_weights.begin(), s->gnc_weights.end(), 0.0);
     s->gnc_num_inliers = static_cast<size_t>(sum) - n_known;
   } else {
@@ -283,12 +324,14 @@ int optimize(rpgo_solver* s) {
       for (size_t i = 0; i < s->latest_num_lc; ++i)
         if (prev_k + i < s->gnc_weights.size() && s->gnc_weights[prev_k + i] > 0.5 && k + i < s->nfg.size())
           full.push_back(s->nfg[k + i]);
+      full.insert(full.end(), s->temp_nfg.begin(), s->temp_nfg.end());
     }
-    GpuNls nls(s->dim, full, *s->store, *s->values, s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
+    GpuNls nls(s->dim, full, *s->store, sv.get(), s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
     nls.dev().coop_ctas = s->coop_ctas;
     nls.optimize(lp, &st);
     if (st.failed) return RPGO_ERR_SOLVER;
-    nls.write_back(*s->values);
+    sv.write_back(nls);
+    s->gnc_temp_weights.assign(s->temp_nfg.size(), 1.0);
     const size_t tail = std::min(s->latest_num_lc, s->gnc_weights.size());
     std::vector<double> lcw(s->gnc_weights.end() - tail, s->gnc_weights.end());
     s->gnc_weights.assign(s->nfg.size(), 1.0);
@@ -310,7 +353,8 @@ int update_impl(rpgo_solver* s, std::vector<FactorRec> nf, const rpgo_value_batc
   std::set<uint64_t> new_keys;
   if (vb) {
     for (int64_t k = 0; k < vb->count; ++k) {
-      if (s->values->has(vb->key[k]) || new_keys.count(vb->key[k])) return RPGO_ERR_KEY;
+      if (s->values->has(vb->key[k]) || s->temp_values->has(vb->key[k]) || new_keys.count(vb->key[k]))
+        return RPGO_ERR_KEY;
       new_keys.insert(vb->key[k]);
     }
     s->values->append(vb->count, vb->key, vb->pose, values_on_device, s->st);
@@ -340,6 +384,9 @@ int update_impl(rpgo_solver* s, std::vector<FactorRec> nf, const rpgo_value_batc
   int rc = RPGO_OK;
   for (const auto& f : s->nfg)
     if (!s->values->has(f.k1) || !s->values->has(f.k2)) rc = RPGO_ERR_KEY;
+  auto known = [s](uint64_t k) { return s->values->has(k) || s->temp_values->has(k); };
+  for (const auto& f : s->temp_nfg)
+    if (!known(f.k1) || !known(f.k2)) rc = RPGO_ERR_KEY;
   if (rc == RPGO_OK && ((do_opt && optimize_graph) || force)) rc = optimize(s);
   RPGO_CUDA(cudaEventRecord(e2, s->st));
   RPGO_CUDA(cudaEventSynchronize(e2));
@@ -600,6 +647,7 @@ rpgo_solver* rpgo_create(const rpgo_params* p) {
     RPGO_CUDA(cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking));
     AllocStreamScope scope(s->st);
     s->values = std::make_unique<ValueStore>(s->stride);
+    s->temp_values = std::make_unique<ValueStore>(s->stride);
     s->store = std::make_unique<FactorStore>(s->stride, s->d);
     if (m != RPGO_OUTLIER_NONE) {
       PcmConfig c;
@@ -870,6 +918,88 @@ int rpgo_mlp_train_step_dev(float* params, float* adam_m, float* adam_v, int64_t
 int rpgo_get_timing(const rpgo_solver* s, rpgo_timing* t) {
   if (!s || !t) return RPGO_ERR_ARG;
   *t = s->timing;
+  return RPGO_OK;
+}
+
+// GenericSolver::updateTempFactorsValues / replaceTempFactorsValues
+// (include/KimeraRPGO/GenericSolver.h:50-61)
+static int set_temp(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, bool replace) {
+  if (!s) return RPGO_ERR_ARG;
+  if (f && f->count > 0 && (!f->kind || !f->key_front || !f->measured || !f->covariance || !f->sqrt_information))
+    return RPGO_ERR_ARG;
+  if (v && v->count > 0 && (!v->key || !v->pose)) return RPGO_ERR_ARG;
+  if (f)
+    for (int64_t k = 0; k < f->count; ++k)
+      if (f->kind[k] != RPGO_FACTOR_BETWEEN && f->kind[k] != RPGO_FACTOR_PRIOR) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
+  return guarded([&] {
+    std::set<uint64_t> keys;
+    if (v)
+      for (int64_t k = 0; k < v->count; ++k) {
+        const uint64_t key = v->key[k];
+        if (s->values->has(key) || (!replace && s->temp_values->has(key)) || !keys.insert(key).second)
+          return (int)RPGO_ERR_KEY;
+      }
+    if (replace) {
+      s->temp_nfg.clear();
+      s->temp_values = std::make_unique<ValueStore>(s->stride);
+    }
+    std::vector<FactorRec> nf = ingest(s, f, false);
+    s->temp_nfg.insert(s->temp_nfg.end(), nf.begin(), nf.end());
+    if (v && v->count > 0) s->temp_values->append(v->count, v->key, v->pose, false, s->st);
+    RPGO_CUDA(cudaStreamSynchronize(s->st));
+    return (int)RPGO_OK;
+  });
+}
+
+int rpgo_update_temp_factors_values(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v) {
+  return set_temp(s, f, v, false);
+}
+
+int rpgo_replace_temp_factors_values(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value_batch* v) {
+  return set_temp(s, f, v, true);
+}
+
+// GenericSolver::clearTempFactorsValues (GenericSolver.h:62-65)
+int rpgo_clear_temp_factors_values(rpgo_solver* s) {
+  if (!s) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
+  return guarded([&] {
+    s->temp_nfg.clear();
+    s->temp_values = std::make_unique<ValueStore>(s->stride);
+    return (int)RPGO_OK;
+  });
+}
+
+int rpgo_get_temp_sizes(const rpgo_solver* s, int64_t* nf, int64_t* nv) {
+  if (!s) return RPGO_ERR_ARG;
+  if (nf) *nf = (int64_t)s->temp_nfg.size();
+  if (nv) *nv = (int64_t)s->temp_values->size();
+  return RPGO_OK;
+}
+
+// GenericSolver::getTempValues (GenericSolver.h:46)
+int rpgo_get_temp_values(const rpgo_solver* s, uint64_t* keys, double* poses, int64_t cap) {
+  if (!s || (int64_t)s->temp_values->size() > cap) return RPGO_ERR_ARG;
+  AllocStreamScope scope(s->st);
+  return guarded([&] {
+    std::vector<uint64_t> k;
+    std::vector<double> p;
+    s->temp_values->download_sorted(&k, &p, s->st);
+    if (!k.empty()) {
+      std::memcpy(keys, k.data(), k.size() * sizeof(uint64_t));
+      std::memcpy(poses, p.data(), p.size() * sizeof(double));
+    }
+    return (int)RPGO_OK;
+  });
+}
+
+// RobustSolver::getGncTempWeights (include/KimeraRPGO/RobustSolver.h:108)
+int rpgo_get_gnc_temp_weights(const rpgo_solver* s, double* w, int64_t cap, int64_t* n) {
+  if (!s) return RPGO_ERR_ARG;
+  if (n) *n = (int64_t)s->gnc_temp_weights.size();
+  if ((int64_t)s->gnc_temp_weights.size() > cap) return RPGO_ERR_ARG;
+  if (!s->gnc_temp_weights.empty()) std::memcpy(w, s->gnc_temp_weights.data(), sizeof(double) * s->gnc_temp_weights.size());
   return RPGO_OK;
 }
 

@@ -93,6 +93,12 @@ SIGNATURES = {
     "rpgo_get_counts": (C.c_int, [_P, C.POINTER(Counts)]),
     "rpgo_get_estimate": (C.c_int, [_P, _P, _P, C.c_int64]),
     "rpgo_get_gnc_weights": (C.c_int, [_P, _P, C.c_int64]),
+    "rpgo_update_temp_factors_values": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch)]),
+    "rpgo_replace_temp_factors_values": (C.c_int, [_P, C.POINTER(FactorBatch), C.POINTER(ValueBatch)]),
+    "rpgo_clear_temp_factors_values": (C.c_int, [_P]),
+    "rpgo_get_temp_sizes": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "rpgo_get_temp_values": (C.c_int, [_P, _P, _P, C.c_int64]),
+    "rpgo_get_gnc_temp_weights": (C.c_int, [_P, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "rpgo_get_factors": (C.c_int, [_P, _P, _P, _P, _P, C.c_int64]),
     "rpgo_get_adjacency": (C.c_int, [_P, C.c_int32, _P, C.c_int64, C.POINTER(C.c_int64)]),
     "rpgo_get_timing": (C.c_int, [_P, C.POINTER(Timing)]),
@@ -260,6 +266,42 @@ class RobustSolver:
         return w
 
     getGncWeights = gnc_weights
+
+    # temporary factors and values (GenericSolver.h:46-65)
+    def updateTempFactorsValues(self, graph) -> int:
+        b = Batch(graph)
+        return load().rpgo_update_temp_factors_values(self.h, C.byref(b.f), C.byref(b.v))
+
+    def replaceTempFactorsValues(self, graph) -> int:
+        b = Batch(graph)
+        return load().rpgo_replace_temp_factors_values(self.h, C.byref(b.f), C.byref(b.v))
+
+    def clearTempFactorsValues(self) -> int:
+        return load().rpgo_clear_temp_factors_values(self.h)
+
+    def temp_sizes(self):
+        """(getTempFactorsUnsafe().size(), getTempValues().size())"""
+        nf, nv = C.c_int64(), C.c_int64()
+        load().rpgo_get_temp_sizes(self.h, C.byref(nf), C.byref(nv))
+        return nf.value, nv.value
+
+    def getTempValues(self):
+        n = self.temp_sizes()[1]
+        keys = np.zeros(n, dtype=np.uint64)
+        poses = np.zeros((n, 12 if self.dim == 3 else 4))
+        rc = load().rpgo_get_temp_values(self.h, _ptr(keys), _ptr(poses), n)
+        if rc:
+            raise RpgoError(f"rpgo_get_temp_values: {rc}")
+        return keys, poses
+
+    def getGncTempWeights(self):
+        n = C.c_int64()
+        load().rpgo_get_gnc_temp_weights(self.h, None, 0, C.byref(n))
+        w = np.zeros(n.value)
+        rc = load().rpgo_get_gnc_temp_weights(self.h, _ptr(w), n.value, C.byref(n))
+        if rc:
+            raise RpgoError(f"rpgo_get_gnc_temp_weights: {rc}")
+        return w
 
     def factors(self):
         n = self.counts().num_factors

@@ -42,6 +42,12 @@ struct SolverBase {
   virtual int ignore_prefix(char c, bool revive) = 0;
   virtual int ignored_prefixes(char* out, int cap) const = 0;
   virtual int remove_priors_with_prefix(char c, int optimize_graph) = 0;
+  // temporary factors and values (GenericSolver.h:46-65)
+  virtual int set_temp(const rpgo_factor_batch* f, const rpgo_value_batch* v, bool replace) = 0;
+  virtual void clear_temp() = 0;
+  virtual void temp_sizes(int64_t* nf, int64_t* nv) const = 0;
+  virtual int temp_values_out(uint64_t* keys, double* poses, int64_t cap) const = 0;
+  virtual int temp_weights(double* w, int64_t cap, int64_t* n) const = 0;
   int64_t warm_runs = 0, warm_fallbacks = 0;
   // wall-clock seconds spent in outlier rejection and in the solve (sums)
   double pcm_seconds = 0.0, solve_seconds = 0.0;
@@ -57,6 +63,9 @@ struct RobustSolverO final : SolverBase {
   std::vector<Factor<L>> nfg;
   std::unique_ptr<Pcm<L, U>> pcm;
   std::vector<double> gnc_weights;
+  std::map<uint64_t, Pose> temp_values;  // GenericSolver::temp_values_
+  std::vector<Factor<L>> temp_nfg;       // GenericSolver::temp_nfg_
+  std::vector<double> gnc_temp_weights;  // RobustSolver::gnc_temp_weights_
   size_t gnc_num_inliers = 0, latest_num_lc = 0;
   int64_t lm_iters = 0, solves = 0, gnc_iters = 0;
   bool last_do_opt = false;
@@ -104,7 +113,8 @@ struct RobustSolverO final : SolverBase {
     std::set<uint64_t> new_keys;
     if (vb) {
       for (int64_t k = 0; k < vb->count; ++k) {
-        if (values.count(vb->key[k]) || new_keys.count(vb->key[k])) return RPGO_ERR_KEY;
+        if (values.count(vb->key[k]) || temp_values.count(vb->key[k]) || new_keys.count(vb->key[k]))
+          return RPGO_ERR_KEY;
         new_keys.insert(vb->key[k]);
       }
       for (int64_t k = 0; k < vb->count; ++k) values[vb->key[k]] = L::load(vb->pose + k * L::stride);
@@ -125,6 +135,9 @@ struct RobustSolverO final : SolverBase {
     for (const auto& f : nfg) {
       if (!values.count(f.k1) || !values.count(f.k2)) return RPGO_ERR_KEY;
     }
+    auto known = [this](uint64_t k) { return values.count(k) || temp_values.count(k); };
+    for (const auto& f : temp_nfg)
+      if (!known(f.k1) || !known(f.k2)) return RPGO_ERR_KEY;
     if (do_opt && optimize_graph) {
       const auto t0 = std::chrono::steady_clock::now();
       const int rc = optimize();
@@ -206,6 +219,9 @@ struct RobustSolverO final : SolverBase {
     lp.gauss_newton = (p.solver == RPGO_SOLVER_GN);
     lp.diagonal_damping = p.lm_diagonal_damping != 0;
     std::vector<Factor<L>> full = nfg;
+    full.insert(full.end(), temp_nfg.begin(), temp_nfg.end());
+    std::map<uint64_t, Pose> full_values = values;
+    full_values.insert(temp_values.begin(), temp_values.end());
     std::map<uint64_t, Pose> result;
     SolveStats st;
     const size_t num_lc = pcm ? pcm->total_lc : 0;
@@ -227,7 +243,7 @@ struct RobustSolverO final : SolverBase {
       bool warm_done = false;
       if (p.gnc_warm_start == RPGO_WARM_ON && warm_probs.size() == full.size()) {
         bool certified = false;
-        r = gnc_tls_warm<S>(full, values, n_known, gp, lp, warm_probs, p.gnc_warm_mu, &certified);
+        r = gnc_tls_warm<S>(full, full_values, n_known, gp, lp, warm_probs, p.gnc_warm_mu, &certified);
         ++warm_runs;
         if (certified) warm_done = true;
         else ++warm_fallbacks;
@@ -236,7 +252,7 @@ struct RobustSolverO final : SolverBase {
       if (!warm_done) {
         SolveStats before = r.stats;
         const int outer_before = r.outer_iterations;
-        r = gnc_tls<S>(full, values, n_known, gp, lp, p.gnc_bias_odom ? &init : nullptr);
+        r = gnc_tls<S>(full, full_values, n_known, gp, lp, p.gnc_bias_odom ? &init : nullptr);
         r.stats.iterations += before.iterations;
         r.stats.linear_solves += before.linear_solves;
         r.outer_iterations += outer_before;
@@ -245,6 +261,7 @@ struct RobustSolverO final : SolverBase {
       st = r.stats;
       gnc_iters += r.outer_iterations;
       gnc_weights.assign(r.weights.begin(), r.weights.begin() + nfg.size());
+      gnc_temp_weights.assign(r.weights.begin() + nfg.size(), r.weights.end());
       const double sum = std::accumulate(gnc_weights.begin(), gnc_weights.end(), 0.0);
       gnc_num_inliers = static_cast<size_t>(sum) - n_known;
     } else {
@@ -255,21 +272,26 @@ struct RobustSolverO final : SolverBase {
         for (size_t i = 0; i < latest_num_lc; ++i)
           if (prev_k + i < gnc_weights.size() && gnc_weights[prev_k + i] > 0.5 && k + i < nfg.size())
             full.push_back(nfg[k + i]);
+        full.insert(full.end(), temp_nfg.begin(), temp_nfg.end());
       }
       NLS<S> nls;
       nls.graph = &full;
-      result = nls.optimize(values, lp, &st);
+      result = nls.optimize(full_values, lp, &st);
       if (st.failed) return RPGO_ERR_SOLVER;
       const size_t tail = std::min(latest_num_lc, gnc_weights.size());
       std::vector<double> lcw(gnc_weights.end() - tail, gnc_weights.end());
       gnc_weights.assign(nfg.size(), 1.0);
       const size_t t2 = std::min(tail, gnc_weights.size());
       for (size_t i = 0; i < t2; ++i) gnc_weights[gnc_weights.size() - t2 + i] = lcw[lcw.size() - t2 + i];
+      gnc_temp_weights.assign(temp_nfg.size(), 1.0);
     }
     lm_iters += st.iterations;
     solves += st.linear_solves;
-    for (auto& kv : result)
+    // GenericSolver::updateValues (src/GenericSolver.cpp:37-45)
+    for (auto& kv : result) {
       if (values.count(kv.first)) values[kv.first] = kv.second;
+      else if (temp_values.count(kv.first)) temp_values[kv.first] = kv.second;
+    }
     if (pcm) latest_num_lc = pcm->total_lc;
     return RPGO_OK;
   }
@@ -371,6 +393,43 @@ struct RobustSolverO final : SolverBase {
     return optimize_graph ? optimize_timed() : RPGO_OK;
   }
   // RobustSolver::forceUpdate with no new factors or values: optimize()
+  int set_temp(const rpgo_factor_batch* f, const rpgo_value_batch* v, bool replace) override {
+    std::set<uint64_t> keys;
+    if (v)
+      for (int64_t k = 0; k < v->count; ++k)
+        if (values.count(v->key[k]) || (!replace && temp_values.count(v->key[k])) || !keys.insert(v->key[k]).second)
+          return RPGO_ERR_KEY;
+    if (replace) clear_temp();
+    const auto nf = convert(f);
+    temp_nfg.insert(temp_nfg.end(), nf.begin(), nf.end());
+    if (v)
+      for (int64_t k = 0; k < v->count; ++k) temp_values[v->key[k]] = L::load(v->pose + k * L::stride);
+    return RPGO_OK;
+  }
+  void clear_temp() override {
+    temp_nfg.clear();
+    temp_values.clear();
+  }
+  void temp_sizes(int64_t* nf, int64_t* nv) const override {
+    *nf = (int64_t)temp_nfg.size();
+    *nv = (int64_t)temp_values.size();
+  }
+  int temp_values_out(uint64_t* keys, double* poses, int64_t cap) const override {
+    if ((int64_t)temp_values.size() > cap) return RPGO_ERR_ARG;
+    int64_t i = 0;
+    for (const auto& kv : temp_values) {
+      keys[i] = kv.first;
+      L::store(kv.second, poses + i * L::stride);
+      ++i;
+    }
+    return RPGO_OK;
+  }
+  int temp_weights(double* w, int64_t cap, int64_t* n) const override {
+    *n = (int64_t)gnc_temp_weights.size();
+    if (*n > cap) return RPGO_ERR_ARG;
+    std::copy(gnc_temp_weights.begin(), gnc_temp_weights.end(), w);
+    return RPGO_OK;
+  }
   int force_optimize() override {
     const auto t0 = std::chrono::steady_clock::now();
     const int rc = optimize();
@@ -448,6 +507,23 @@ int oracle_set_warm_probs(void* s, const double* probs, int64_t n) {
   return 0;
 }
 int oracle_force_optimize(void* s) { return static_cast<SolverBase*>(s)->force_optimize(); }
+int oracle_set_temp(void* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, int replace) {
+  return static_cast<SolverBase*>(s)->set_temp(f, v, replace != 0);
+}
+int oracle_clear_temp(void* s) {
+  static_cast<SolverBase*>(s)->clear_temp();
+  return RPGO_OK;
+}
+int oracle_temp_sizes(void* s, int64_t* nf, int64_t* nv) {
+  static_cast<SolverBase*>(s)->temp_sizes(nf, nv);
+  return RPGO_OK;
+}
+int oracle_temp_values(void* s, uint64_t* k, double* p, int64_t cap) {
+  return static_cast<SolverBase*>(s)->temp_values_out(k, p, cap);
+}
+int oracle_temp_weights(void* s, double* w, int64_t cap, int64_t* n) {
+  return static_cast<SolverBase*>(s)->temp_weights(w, cap, n);
+}
 int oracle_remove_last_loop_closure(void* s, int by_id, char p1, char p2, uint64_t* k1, uint64_t* k2, int* removed) {
   return static_cast<SolverBase*>(s)->remove_last_loop_closure(by_id, p1, p2, k1, k2, removed);
 }

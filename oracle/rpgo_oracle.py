@@ -49,8 +49,8 @@ class Counts(C.Structure):
 
 
 def build(force: bool = False) -> str:
-    if force or not os.path.exists(_LIB_PATH):
-        subprocess.check_call(["make", "-s", "-C", _HERE])
+    # make rebuilds only when a source is newer than the library
+    subprocess.check_call(["make", "-s", "-C", _HERE] + (["-B"] if force else []))
     return _LIB_PATH
 
 
@@ -74,6 +74,11 @@ def lib():
         _lib.oracle_get_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib.oracle_set_warm_probs.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         _lib.oracle_force_optimize.argtypes = [C.c_void_p]
+        _lib.oracle_set_temp.argtypes = [C.c_void_p, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.c_int]
+        _lib.oracle_clear_temp.argtypes = [C.c_void_p]
+        _lib.oracle_temp_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        _lib.oracle_temp_values.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
+        _lib.oracle_temp_weights.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.POINTER(C.c_int64)]
         _lib.oracle_remove_last_loop_closure.argtypes = [C.c_void_p, C.c_int, C.c_char, C.c_char,
                                                          C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
                                                          C.POINTER(C.c_int)]
@@ -217,6 +222,38 @@ class OracleSolver:
     def force_optimize(self) -> int:
         """forceUpdate() with no new factors: re-run the solve."""
         return lib().oracle_force_optimize(self.h)
+
+    # temporary factors and values (GenericSolver.h:46-65)
+    def updateTempFactorsValues(self, graph) -> int:
+        b = _Batch(graph)
+        return lib().oracle_set_temp(self.h, C.byref(b.f), C.byref(b.v), 0)
+
+    def replaceTempFactorsValues(self, graph) -> int:
+        b = _Batch(graph)
+        return lib().oracle_set_temp(self.h, C.byref(b.f), C.byref(b.v), 1)
+
+    def clearTempFactorsValues(self) -> int:
+        return lib().oracle_clear_temp(self.h)
+
+    def temp_sizes(self):
+        """(getTempFactorsUnsafe().size(), getTempValues().size())"""
+        nf, nv = C.c_int64(), C.c_int64()
+        lib().oracle_temp_sizes(self.h, C.byref(nf), C.byref(nv))
+        return nf.value, nv.value
+
+    def getTempValues(self):
+        n = self.temp_sizes()[1]
+        keys = np.zeros(n, dtype=np.uint64)
+        poses = np.zeros((n, 12 if self.dim == 3 else 4))
+        assert lib().oracle_temp_values(self.h, _ptr(keys), _ptr(poses), n) == 0
+        return keys, poses
+
+    def getGncTempWeights(self):
+        n = C.c_int64()
+        lib().oracle_temp_weights(self.h, None, 0, C.byref(n))
+        w = np.zeros(n.value)
+        assert lib().oracle_temp_weights(self.h, _ptr(w), n.value, C.byref(n)) == 0
+        return w
 
     def set_warm_probs(self, probs):
         """Inlier probabilities for the next warm-started GNC solve, one per
