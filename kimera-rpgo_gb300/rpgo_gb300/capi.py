@@ -258,6 +258,8 @@ class RobustSolver:
         return keys, poses
 
     calculateEstimate = estimate
+    calculateBestEstimate = estimate  # GenericSolver.h:42
+    getLinearizationPoint = estimate  # GenericSolver.h:43
 
     def gnc_weights(self):
         n = self.counts().num_gnc_weights
