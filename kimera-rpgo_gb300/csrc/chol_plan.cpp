@@ -166,8 +166,12 @@ struct NestedDissection {
     }
   }
 
-  // two: the set is still above leaf2 for the second order
-  void run(std::vector<int32_t> nodes, bool two) {
+  // two: the set is still above leaf2 for the second order; the two halves
+  // of a large set in the first kParDepth splits are ordered concurrently
+  // (a second instance on its own thread, its orders inserted before the
+  // other half's: the same orders as one thread's)
+  static constexpr int kParDepth = 2, kParMin = 2048;
+  void run(std::vector<int32_t> nodes, bool two, int split = 0) {
     if (two && (int)nodes.size() <= leaf2) {
       std::vector<int32_t> sorted = nodes;
       std::sort(sorted.begin(), sorted.end());
@@ -199,7 +203,7 @@ struct NestedDissection {
         for (int w : c) vis[w] = mark;
         comps.push_back(std::move(c));
       }
-      for (auto& c : comps) run(std::move(c), two);
+      for (auto& c : comps) run(std::move(c), two, split);
       return;
     }
     // pseudo-peripheral root: repeat the search from the farthest variable
@@ -247,8 +251,31 @@ struct NestedDissection {
         (touches_next ? S : A).push_back(u);
       }
     }
-    run(std::move(A), two);
-    run(std::move(B), two);
+    if (split < kParDepth && (int)(A.size() + B.size()) > kParMin) {
+      NestedDissection other(adj, leaf, leaf2);
+      std::exception_ptr err;
+      std::thread t([&] {
+        try {
+          other.run(std::move(A), two, split + 1);
+        } catch (...) {
+          err = std::current_exception();
+        }
+      });
+      const size_t at = out.size(), at2 = out2.size();
+      try {
+        run(std::move(B), two, split + 1);
+      } catch (...) {
+        t.join();
+        throw;
+      }
+      t.join();
+      if (err) std::rethrow_exception(err);
+      out.insert(out.begin() + at, other.out.begin(), other.out.end());
+      out2.insert(out2.begin() + at2, other.out2.begin(), other.out2.end());
+    } else {
+      run(std::move(A), two, split + 1);
+      run(std::move(B), two, split + 1);
+    }
     std::sort(S.begin(), S.end());
     out.insert(out.end(), S.begin(), S.end());
     if (two) out2.insert(out2.end(), S.begin(), S.end());
