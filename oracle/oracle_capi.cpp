@@ -4,6 +4,7 @@
 // 105-113 (known inliers), 115-306 (optimize), 337-369 (update);
 // src/GenericSolver.cpp:37-65 (updateValues, addAndCheckIfOptimize).
 // The structs of the public C ABI header are reused for the argument layout.
+#include <omp.h>
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -507,6 +508,11 @@ int oracle_set_warm_probs(void* s, const double* probs, int64_t n) {
   return 0;
 }
 int oracle_force_optimize(void* s) { return static_cast<SolverBase*>(s)->force_optimize(); }
+// OpenMP threads of the pair tests (0: keep); returns the current count
+int oracle_set_threads(int n) {
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+}
 int oracle_set_temp(void* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, int replace) {
   return static_cast<SolverBase*>(s)->set_temp(f, v, replace != 0);
 }

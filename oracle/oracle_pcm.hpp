@@ -460,13 +460,21 @@ struct Pcm {
     return g.consistent.size();
   }
 
-  // Pcm.h:725-768 for every new member of the group against all earlier ones
+  // Pcm.h:725-768 for every new member of the group against all earlier ones.
+  // The pair tests are independent: with OpenMP threads, each new row j is
+  // filled by one thread (bits i < j of row j), then one pass mirrors them;
+  // the matrix is the same as the sequential fill's.
   void increment_adjacency(Group<L>& g, int old_n) {
     g.grow((int)g.factors.size());
     g.adj_rows = g.n;
-    for (int j = old_n; j < g.n; ++j)
+    const int n = g.n, words = g.words;
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int j = old_n; j < n; ++j)
       for (int i = 0; i < j; ++i)
-        if (are_loops_consistent(g.factors[i], g.factors[j])) g.set(i, j);
+        if (are_loops_consistent(g.factors[i], g.factors[j])) g.bits[(size_t)j * words + (i >> 5)] |= 1u << (i & 31);
+    for (int i = 0; i < n; ++i)
+      for (int j = std::max(i + 1, old_n); j < n; ++j)
+        if (g.bits[(size_t)j * words + (i >> 5)] >> (i & 31) & 1u) g.bits[(size_t)i * words + (j >> 5)] |= 1u << (j & 31);
   }
 
   template <class ValuesMap>

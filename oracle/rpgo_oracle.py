@@ -74,6 +74,7 @@ def lib():
         _lib.oracle_get_times.argtypes = [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]
         _lib.oracle_set_warm_probs.argtypes = [C.c_void_p, C.c_void_p, C.c_int64]
         _lib.oracle_force_optimize.argtypes = [C.c_void_p]
+        _lib.oracle_set_threads.argtypes = [C.c_int]
         _lib.oracle_set_temp.argtypes = [C.c_void_p, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.c_int]
         _lib.oracle_clear_temp.argtypes = [C.c_void_p]
         _lib.oracle_temp_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
@@ -260,6 +261,11 @@ class OracleSolver:
         factor of the graph to optimise (known inliers are ignored)."""
         self._warm = np.ascontiguousarray(probs, dtype=np.float64)
         lib().oracle_set_warm_probs(self.h, _ptr(self._warm), self._warm.size)
+
+
+def set_threads(n: int = 0) -> int:
+    """OpenMP threads of the oracle's pair tests (0: keep); returns the count."""
+    return lib().oracle_set_threads(int(n))
 
 
 # ------------------------------------------------------------------ math hooks
