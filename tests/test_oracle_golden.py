@@ -233,3 +233,26 @@ def test_load_graph_and_gnc_scenarios_oracle(robot_a, robot_b):
         if fails:
             bad[name] = fails
     assert not bad, bad
+
+
+def test_oracle_pair_tests_same_on_any_thread_count():
+    # the oracle fills new rows of the consistency matrix on OpenMP threads;
+    # the matrix (and so every later result) must not depend on their count
+    from rpgo_gb300 import synth
+    from rpgo_gb300.params import QUIET, RobustSolverParams
+
+    s = synth.walk3d(600, 120, 40, seed=17)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET)
+    before = O.set_threads(0)
+    try:
+        out = []
+        for threads in (1, 4):
+            O.set_threads(threads)
+            o = O.OracleSolver(p)
+            assert o.update(s.graph) == 0
+            out.append((o.adjacency(0), o.factors()[1], o.estimate()[1]))
+        assert np.array_equal(out[0][0], out[1][0])
+        assert np.array_equal(out[0][1], out[1][1])
+        assert np.array_equal(out[0][2], out[1][2])
+    finally:
+        O.set_threads(before)
