@@ -125,3 +125,30 @@ def test_gpu_temporary_factors_match_reference_and_oracle(robot_a):
     fails = scenario(g, lambda: g.forceUpdate(Graph(3)), robot_a, check)
     assert not fails, fails
     assert not mism, mism
+
+
+def test_oracle_temporary_2d_without_gnc():
+    # 2D, PCM without GNC: temporary factors are optimised with the graph,
+    # their weights are all ones (src/RobustSolver.cpp:208), the temporary
+    # value moves with the solve and the graph's own counts do not change
+    from rpgo_gb300 import synth
+    from rpgo_gb300.graph import pose2, pose2_compose
+
+    s = synth.grid2d(60, 10, 2, seed=3)
+    o = O.OracleSolver(RobustSolverParams().setPcm2DParams(3.0, 3.0, QUIET))
+    assert o.update(s.graph) == 0
+    n0 = (o.counts().num_factors, o.counts().num_values)
+    t = Graph(2)
+    t.insert(symbol("z", 0), pose2(0.0, 0.0, 0.0))
+    t.add_between(symbol("a", 5), symbol("z", 0), pose2(0.5, -0.25, 0.1), isotropic_variance(3, 0.01))
+    assert o.updateTempFactorsValues(t) == 0
+    assert o.force_optimize() == 0
+    assert (o.counts().num_factors, o.counts().num_values) == n0
+    assert np.array_equal(o.getGncTempWeights(), [1.0])
+    keys, poses = o.getTempValues()
+    assert list(keys) == [symbol("z", 0)]
+    # the only factor on z0 is the temporary one: z0 = a5 (+) measurement
+    k, est = o.estimate()
+    a5 = est[list(k).index(symbol("a", 5))]
+    np.testing.assert_allclose(poses[0], pose2_compose(a5, pose2(0.5, -0.25, 0.1)), atol=1e-6)
+    assert o.clearTempFactorsValues() == 0 and o.temp_sizes() == (0, 0)
