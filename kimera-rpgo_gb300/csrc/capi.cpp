@@ -929,8 +929,10 @@ static int set_temp(rpgo_solver* s, const rpgo_factor_batch* f, const rpgo_value
     return RPGO_ERR_ARG;
   if (v && v->count > 0 && (!v->key || !v->pose)) return RPGO_ERR_ARG;
   if (f)
-    for (int64_t k = 0; k < f->count; ++k)
+    for (int64_t k = 0; k < f->count; ++k) {
       if (f->kind[k] != RPGO_FACTOR_BETWEEN && f->kind[k] != RPGO_FACTOR_PRIOR) return RPGO_ERR_ARG;
+      if (f->kind[k] == RPGO_FACTOR_BETWEEN && !f->key_back) return RPGO_ERR_ARG;
+    }
   AllocStreamScope scope(s->st);
   return guarded([&] {
     std::set<uint64_t> keys;
