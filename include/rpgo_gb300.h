@@ -425,7 +425,8 @@ int rpgo_max_clique_heu_dev(int32_t n, const uint32_t* adj, int32_t words, int32
  * by every device that loads the library until the process exits. The first
  * call on a device (with that device current) looks up the array's address
  * with cudaGetSymbolAddress; make that first call before any stream capture.
- * Every call shares the one array: calls that overlap on the GPU (from
+ * The address is kept for the process: do not call this entry point again
+ * after a cudaDeviceReset of that device. Every call shares the one array: calls that overlap on the GPU (from
  * several host threads, or on several streams) race and give wrong results. */
 #define RPGO_CLIQUE_NOALLOC_MAX_N 4096
 #define RPGO_CLIQUE_NOALLOC_MAX_WORDS 128
@@ -447,6 +448,11 @@ int rpgo_max_clique_heu(int32_t n, const uint32_t* adj, int32_t first, int32_t s
 int rpgo_device_info(char* name, int32_t name_capacity, int32_t* sm_count);
 /* Number of CUDA kernels this library has launched in this process. */
 int64_t rpgo_kernel_launch_count(void);
+/* Number of device (cudaMallocAsync) and pinned host (cudaMallocHost)
+ * allocations this library's buffers have made in this process; no
+ * counterpart in the reference (it lets a caller check that a call path
+ * allocates nothing). */
+int64_t rpgo_buffer_alloc_count(void);
 
 #ifdef __cplusplus
 }

@@ -1138,5 +1138,6 @@ int rpgo_device_info(char* name, int32_t cap, int32_t* sm_count) {
 }
 
 int64_t rpgo_kernel_launch_count(void) { return launch_counter().load(); }
+int64_t rpgo_buffer_alloc_count(void) { return alloc_counter().load(); }
 
 }  // extern "C"

@@ -264,7 +264,10 @@ std::mutex g_scratch_mu;
 unsigned char* g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of the scratch array on the current device; looked up once
-// per device (the first call on a device) with that device current.
+// per device (the first call on a device) with that device current. The
+// address belongs to the device's primary context: after cudaDeviceReset the
+// cached address is stale, so this entry point must not be used again in that
+// process.
 int scratch_for_current_device(unsigned char** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return RPGO_ERR_CUDA;
@@ -349,14 +352,18 @@ extern "C" int rpgo_max_clique_heu_dev_noalloc(int32_t n, const uint32_t* adj, i
                  (int)n, (int)words, RPGO_CLIQUE_NOALLOC_MAX_N, RPGO_CLIQUE_NOALLOC_MAX_WORDS);
     return RPGO_ERR_SIZE;
   }
-  unsigned char* scratch = nullptr;
-  const int rc = rpgo::scratch_for_current_device(&scratch);
-  if (rc != RPGO_OK) return rc;
   try {
+    unsigned char* scratch = nullptr;
+    const int rc = rpgo::scratch_for_current_device(&scratch);
+    if (rc != RPGO_OK) return rc;
     return rpgo::max_clique_heu_noalloc(n, adj, words, first, seed, clique_out, size_out, scratch,
                                         (cudaStream_t)stream);
   } catch (const rpgo::CudaError& e) {
     std::fprintf(stderr, "rpgo_gb300: %s\n", e.what());
+    return RPGO_ERR_CUDA;
+  } catch (...) {
+    // nothing may cross the C ABI (a failed mutex lock throws std::system_error)
+    std::fprintf(stderr, "rpgo_gb300: rpgo_max_clique_heu_dev_noalloc: unexpected exception\n");
     return RPGO_ERR_CUDA;
   }
 }

@@ -30,6 +30,8 @@ inline void cuda_check(cudaError_t e, const char* what, const char* file, int li
 // calling host thread (per-update figures of concurrent solvers stay apart).
 std::atomic<int64_t>& launch_counter();
 int64_t& thread_launch_counter();
+// device and pinned host allocations made by this library's buffers (process-wide)
+std::atomic<int64_t>& alloc_counter();
 
 // Device memory is stream-ordered (cudaMallocAsync / cudaFreeAsync from the
 // device's default pool): a free never synchronises the device, so solvers on
@@ -115,6 +117,7 @@ class DeviceBuffer {
     if (n > cap_) {
       release();
       size_t c = n < 16 ? 16 : n;
+      alloc_counter().fetch_add(1, std::memory_order_relaxed);
       RPGO_CUDA(cudaMallocAsync((void**)&p_, c * sizeof(T), alloc_stream()));
       st_ = alloc_stream();
       cap_ = c;
@@ -128,6 +131,7 @@ class DeviceBuffer {
       size_t c = cap_ ? cap_ : 16;
       while (c < n) c *= 2;
       T* q = nullptr;
+      alloc_counter().fetch_add(1, std::memory_order_relaxed);
       RPGO_CUDA(cudaMallocAsync((void**)&q, c * sizeof(T), alloc_stream()));
       if (p_ && n_) RPGO_CUDA(cudaMemcpyAsync(q, p_, n_ * sizeof(T), cudaMemcpyDeviceToDevice, st));
       release();
@@ -179,6 +183,7 @@ class PinnedBuffer {
     if (n > n_) {
       if (p_) cudaFreeHost(p_);
       p_ = nullptr;
+      alloc_counter().fetch_add(1, std::memory_order_relaxed);
       RPGO_CUDA(cudaMallocHost((void**)&p_, n * sizeof(T)));
       n_ = n;
     }

@@ -685,6 +685,10 @@ std::atomic<int64_t>& launch_counter() {
   static std::atomic<int64_t> c{0};
   return c;
 }
+std::atomic<int64_t>& alloc_counter() {
+  static std::atomic<int64_t> c{0};
+  return c;
+}
 int64_t& thread_launch_counter() {
   thread_local int64_t c = 0;
   return c;

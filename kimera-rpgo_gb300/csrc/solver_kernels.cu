@@ -36,7 +36,6 @@ namespace {
 
 using namespace sm;
 
-constexpr int kCta = 1024;
 // device memory the direct solver's factor may take before the PCG path is used
 constexpr double kCholBudgetBytes = 32.0 * (1 << 30);
 
@@ -531,185 +530,6 @@ __device__ __forceinline__ double cta_sum(double v, double* sh) {
   return r;
 }
 
-// ------------------------------------------------------------------ K5 preconditioner factorisation
-template <int D>
-__global__ void __launch_bounds__(kCta) k_bcr_factor(int N, int levels, const int32_t* __restrict__ lvl_off,
-                                                     const int32_t* __restrict__ lvl_n, const float* __restrict__ Md,
-                                                     const float* __restrict__ Mu,
-                                                     const double* __restrict__ dampD, double lambda,
-                                                     float* __restrict__ bD, float* __restrict__ bDinv,
-                                                     float* __restrict__ bU, float* __restrict__ bFL,
-                                                     float* __restrict__ bFR) {
-  constexpr int dd = D * D;
-  for (int v = threadIdx.x; v < N; v += blockDim.x) {
-#pragma unroll
-    for (int i = 0; i < dd; ++i) {
-      bD[(size_t)v * dd + i] = Md[(size_t)v * dd + i];
-      bU[(size_t)v * dd + i] = (v + 1 < N) ? Mu[(size_t)v * dd + i] : 0.f;
-    }
-#pragma unroll
-    for (int a = 0; a < D; ++a) bD[(size_t)v * dd + D * a + a] += (float)(lambda * dampD[(size_t)v * D + a]);
-  }
-  __syncthreads();
-  for (int l = 0; l < levels; ++l) {
-    const int base = lvl_off[l], n = lvl_n[l];
-    if (n == 1) {
-      if (threadIdx.x == 0) spd_inv_f<D>(bD + (size_t)base * dd, bDinv + (size_t)base * dd);
-      break;
-    }
-    for (int o = 1 + 2 * threadIdx.x; o < n; o += 2 * blockDim.x)
-      spd_inv_f<D>(bD + (size_t)(base + o) * dd, bDinv + (size_t)(base + o) * dd);
-    __syncthreads();
-    const int nbase = lvl_off[l + 1];
-    for (int i = 2 * threadIdx.x; i < n; i += 2 * blockDim.x) {
-      float FL[dd], FR[dd], Dn[dd], T[dd];
-      const float* Di = bD + (size_t)(base + i) * dd;
-#pragma unroll
-      for (int q = 0; q < dd; ++q) Dn[q] = Di[q];
-      if (i >= 1) {
-        const float* Ul = bU + (size_t)(base + i - 1) * dd;  // couples i-1, i
-        mm_f<D>(Ul, bDinv + (size_t)(base + i - 1) * dd, FL, true, false);  // U^T Dinv
-        mm_f<D>(FL, Ul, T);                                                // FL U
-#pragma unroll
-        for (int q = 0; q < dd; ++q) Dn[q] -= T[q];
-      } else {
-#pragma unroll
-        for (int q = 0; q < dd; ++q) FL[q] = 0.f;
-      }
-      float Un[dd];
-#pragma unroll
-      for (int q = 0; q < dd; ++q) Un[q] = 0.f;
-      if (i + 1 < n) {
-        const float* Ur = bU + (size_t)(base + i) * dd;  // couples i, i+1
-        mm_f<D>(Ur, bDinv + (size_t)(base + i + 1) * dd, FR);  // U Dinv
-        mm_f<D>(FR, Ur, T, false, true);                          // FR U^T
-#pragma unroll
-        for (int q = 0; q < dd; ++q) Dn[q] -= T[q];
-        if (i + 2 < n) {
-          mm_f<D>(FR, bU + (size_t)(base + i + 1) * dd, T);  // FR U_{i+1}
-#pragma unroll
-          for (int q = 0; q < dd; ++q) Un[q] = -T[q];
-        }
-      } else {
-#pragma unroll
-        for (int q = 0; q < dd; ++q) FR[q] = 0.f;
-      }
-      // symmetrise the Schur complement
-#pragma unroll
-      for (int a = 0; a < D; ++a)
-#pragma unroll
-        for (int b = 0; b < a; ++b) {
-          const float s = 0.5f * (Dn[D * a + b] + Dn[D * b + a]);
-          Dn[D * a + b] = s;
-          Dn[D * b + a] = s;
-        }
-#pragma unroll
-      for (int q = 0; q < dd; ++q) {
-        bFL[(size_t)(base + i) * dd + q] = FL[q];
-        bFR[(size_t)(base + i) * dd + q] = FR[q];
-        bD[(size_t)(nbase + i / 2) * dd + q] = Dn[q];
-        bU[(size_t)(nbase + i / 2) * dd + q] = Un[q];
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// z = M^-1 r by block cyclic reduction (forward reduction, coarse solve, back substitution)
-template <int D>
-__device__ void bcr_apply(int levels, const int32_t* lvl_off, const int32_t* lvl_n, const float* bDinv,
-                          const float* bFL, const float* bFR, float* bb, float* bx, const float* r, float* z) {
-  constexpr int dd = D * D;
-  const int n0 = lvl_n[0];
-  for (int q = threadIdx.x; q < n0 * D; q += blockDim.x) bb[q] = r[q];
-  __syncthreads();
-  int l = 0;
-  for (; l < levels && lvl_n[l] > 1; ++l) {
-    const int base = lvl_off[l], n = lvl_n[l], nbase = lvl_off[l + 1];
-    for (int i = 2 * threadIdx.x; i < n; i += 2 * blockDim.x) {
-      float out[D];
-      const float* bi = bb + (size_t)(base + i) * D;
-#pragma unroll
-      for (int a = 0; a < D; ++a) out[a] = bi[a];
-      if (i >= 1) {
-        const float* F = bFL + (size_t)(base + i) * dd;
-        const float* bl = bb + (size_t)(base + i - 1) * D;
-#pragma unroll
-        for (int a = 0; a < D; ++a)
-#pragma unroll
-          for (int c = 0; c < D; ++c) out[a] -= F[D * a + c] * bl[c];
-      }
-      if (i + 1 < n) {
-        const float* F = bFR + (size_t)(base + i) * dd;
-        const float* br = bb + (size_t)(base + i + 1) * D;
-#pragma unroll
-        for (int a = 0; a < D; ++a)
-#pragma unroll
-          for (int c = 0; c < D; ++c) out[a] -= F[D * a + c] * br[c];
-      }
-#pragma unroll
-      for (int a = 0; a < D; ++a) bb[(size_t)(nbase + i / 2) * D + a] = out[a];
-    }
-    __syncthreads();
-  }
-  // coarsest level: one node
-  {
-    const int base = lvl_off[l];
-    if (threadIdx.x < D) {
-      const int a = threadIdx.x;
-      float acc = 0.f;
-      const float* Di = bDinv + (size_t)base * dd;
-      for (int c = 0; c < D; ++c) acc += Di[D * a + c] * bb[(size_t)base * D + c];
-      bx[(size_t)base * D + a] = acc;
-    }
-  }
-  __syncthreads();
-  for (--l; l >= 0; --l) {
-    const int base = lvl_off[l], n = lvl_n[l], nbase = lvl_off[l + 1];
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-      float* xi = bx + (size_t)(base + i) * D;
-      if ((i & 1) == 0) {
-        const float* src = bx + (size_t)(nbase + i / 2) * D;
-#pragma unroll
-        for (int a = 0; a < D; ++a) xi[a] = src[a];
-      } else {
-        const float* Di = bDinv + (size_t)(base + i) * dd;
-        const float* bi = bb + (size_t)(base + i) * D;
-        float out[D];
-#pragma unroll
-        for (int a = 0; a < D; ++a) {
-          float acc = 0.f;
-#pragma unroll
-          for (int c = 0; c < D; ++c) acc += Di[D * a + c] * bi[c];
-          out[a] = acc;
-        }
-        // - FR(i-1)^T x_{i-1}
-        {
-          const float* F = bFR + (size_t)(base + i - 1) * dd;
-          const float* xl = bx + (size_t)(nbase + (i - 1) / 2) * D;
-#pragma unroll
-          for (int a = 0; a < D; ++a)
-#pragma unroll
-            for (int c = 0; c < D; ++c) out[a] -= F[D * c + a] * xl[c];
-        }
-        if (i + 1 < n) {
-          const float* F = bFL + (size_t)(base + i + 1) * dd;
-          const float* xr = bx + (size_t)(nbase + (i + 1) / 2) * D;
-#pragma unroll
-          for (int a = 0; a < D; ++a)
-#pragma unroll
-            for (int c = 0; c < D; ++c) out[a] -= F[D * c + a] * xr[c];
-        }
-#pragma unroll
-        for (int a = 0; a < D; ++a) xi[a] = out[a];
-      }
-    }
-    __syncthreads();
-  }
-  for (int q = threadIdx.x; q < n0 * D; q += blockDim.x) z[q] = bx[q];
-  __syncthreads();
-}
-
 struct CsrView {
   const float* Hd;
   const float* fH;
@@ -721,351 +541,6 @@ struct CsrView {
   const int8_t* btr;
   const double* dampD;
 };
-
-// y = (H + lam D) p, FP32
-template <int D>
-__device__ void spmv_f(int N, const CsrView& A, double lam, const float* p, float* y) {
-  constexpr int dd = D * D;
-  for (int v = threadIdx.x; v < N; v += blockDim.x) {
-    float acc[D];
-    const float* H = A.Hd + (size_t)v * dd;
-    const float* pv = p + (size_t)v * D;
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      float s = (float)(lam * A.dampD[(size_t)v * D + a]) * pv[a];
-#pragma unroll
-      for (int c = 0; c < D; ++c) s += H[D * a + c] * pv[c];
-      acc[a] = s;
-    }
-    for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
-      const float* B = A.fH + (size_t)A.blk[k] * 3 * dd + 2 * dd;
-      const float* pc = p + (size_t)A.col[k] * D;
-      if (A.btr[k]) {
-#pragma unroll
-        for (int a = 0; a < D; ++a)
-#pragma unroll
-          for (int c = 0; c < D; ++c) acc[a] += B[D * c + a] * pc[c];
-      } else {
-#pragma unroll
-        for (int a = 0; a < D; ++a)
-#pragma unroll
-          for (int c = 0; c < D; ++c) acc[a] += B[D * a + c] * pc[c];
-      }
-    }
-#pragma unroll
-    for (int a = 0; a < D; ++a) y[(size_t)v * D + a] = acc[a];
-  }
-  __syncthreads();
-}
-// y = (H + lam D) p with the FP64 blocks
-template <int D>
-__device__ void spmv_d(int N, const CsrView& A, double lam, const double* p, double* y) {
-  constexpr int dd = D * D;
-  for (int v = threadIdx.x; v < N; v += blockDim.x) {
-    double acc[D];
-    const double* H = A.Hd64 + (size_t)v * dd;
-    const double* pv = p + (size_t)v * D;
-#pragma unroll
-    for (int a = 0; a < D; ++a) {
-      double s = lam * A.dampD[(size_t)v * D + a] * pv[a];
-#pragma unroll
-      for (int c = 0; c < D; ++c) s += H[D * a + c] * pv[c];
-      acc[a] = s;
-    }
-    for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
-      const double* B = A.fH64 + (size_t)A.blk[k] * 3 * dd + 2 * dd;
-      const double* pc = p + (size_t)A.col[k] * D;
-      if (A.btr[k]) {
-#pragma unroll
-        for (int a = 0; a < D; ++a)
-#pragma unroll
-          for (int c = 0; c < D; ++c) acc[a] += B[D * c + a] * pc[c];
-      } else {
-#pragma unroll
-        for (int a = 0; a < D; ++a)
-#pragma unroll
-          for (int c = 0; c < D; ++c) acc[a] += B[D * a + c] * pc[c];
-      }
-    }
-#pragma unroll
-    for (int a = 0; a < D; ++a) y[(size_t)v * D + a] = acc[a];
-  }
-  __syncthreads();
-}
-
-struct PcgParams {
-  double tol;   // relative FP64 residual |b - A delta| / |b|
-  int max_it;   // CG iterations
-};
-
-// Solve (H + lam D) delta = -g by flexible preconditioned CG in FP64 (FP64
-// blocks), the block cyclic reduction preconditioner applied in FP32.
-// out[0] lin_change = -g.delta - delta^T H delta / 2 (undamped H),
-// [1] ok, [2] CG iterations, [3] final relative residual.
-template <int D>
-__global__ void __launch_bounds__(kCta) k_pcg(int N, CsrView A, double lam, const double* __restrict__ g,
-                                              int levels, const int32_t* __restrict__ lvl_off,
-                                              const int32_t* __restrict__ lvl_n, const float* __restrict__ bDinv,
-                                              const float* __restrict__ bFL, const float* __restrict__ bFR,
-                                              float* __restrict__ bb, float* __restrict__ bx, float* __restrict__ cr,
-                                              float* __restrict__ cz, double* __restrict__ r,
-                                              double* __restrict__ z, double* __restrict__ zo,
-                                              double* __restrict__ p, double* __restrict__ q,
-                                              double* __restrict__ delta, PcgParams prm, int warm,
-                                              double* __restrict__ out) {
-  __shared__ double sh[40];
-  const int n = N * D;
-  double loc = 0.0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) loc += g[k] * g[k];
-  const double bnorm = sqrt(cta_sum(loc, sh));
-  if (warm) {
-    spmv_d<D>(N, A, lam, delta, q);
-  }
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    if (!warm) delta[k] = 0.0;
-    const double rk = warm ? (-g[k] - q[k]) : -g[k];
-    r[k] = rk;
-    cr[k] = (float)rk;
-  }
-  __syncthreads();
-  int it = 0, ok = 1;
-  double rel = 0.0;
-  if (bnorm > 0.0) {
-    bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
-    loc = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      z[k] = (double)cz[k];
-      p[k] = z[k];
-      loc += r[k] * z[k];
-    }
-    double rz = cta_sum(loc, sh);
-    for (; it < prm.max_it; ++it) {
-      spmv_d<D>(N, A, lam, p, q);
-      loc = 0.0;
-      for (int k = threadIdx.x; k < n; k += blockDim.x) loc += p[k] * q[k];
-      const double pq = cta_sum(loc, sh);
-      if (!(pq > 0.0) || !(rz > 0.0)) {
-        if (it == 0) ok = 0;
-        break;
-      }
-      const double alpha = rz / pq;
-      loc = 0.0;
-      for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        delta[k] += alpha * p[k];
-        const double rk = r[k] - alpha * q[k];
-        r[k] = rk;
-        cr[k] = (float)rk;
-        zo[k] = z[k];
-        loc += rk * rk;
-      }
-      rel = sqrt(cta_sum(loc, sh)) / bnorm;
-      if (rel <= prm.tol) {
-        ++it;
-        break;
-      }
-      bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
-      double rzn = 0.0, rzo = 0.0;
-      for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double zk = (double)cz[k];
-        z[k] = zk;
-        rzn += r[k] * zk;
-        rzo += r[k] * zo[k];
-      }
-      rzn = cta_sum(rzn, sh);
-      rzo = cta_sum(rzo, sh);
-      const double beta = (rzn - rzo) / rz;  // flexible (Polak-Ribiere) update
-      rz = rzn;
-      for (int k = threadIdx.x; k < n; k += blockDim.x) p[k] = z[k] + beta * p[k];
-      __syncthreads();
-    }
-  }
-  // linearised cost change with the undamped H
-  spmv_d<D>(N, A, 0.0, delta, q);
-  double gd = 0.0, dhd = 0.0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    gd += g[k] * delta[k];
-    dhd += delta[k] * q[k];
-  }
-  gd = cta_sum(gd, sh);
-  dhd = cta_sum(dhd, sh);
-  if (threadIdx.x == 0) {
-    out[0] = -gd - 0.5 * dhd;
-    out[1] = ok;
-    out[2] = it;
-    out[3] = rel;
-  }
-}
-
-// FP32 preconditioned CG on (H + lam D) c = rhs (rhs in cr, solution in cx);
-// out[4] iterations, out[5] ok. One CTA: at the sizes of a single pose graph
-// the inner loop is bound by synchronisation, not arithmetic.
-template <int D>
-__global__ void __launch_bounds__(kCta) k_pcg32(int N, CsrView A, double lam, int levels,
-                                                const int32_t* __restrict__ lvl_off, const int32_t* __restrict__ lvl_n,
-                                                const float* __restrict__ bDinv, const float* __restrict__ bFL,
-                                                const float* __restrict__ bFR, float* __restrict__ bb,
-                                                float* __restrict__ bx, float* __restrict__ cr, float* __restrict__ cz,
-                                                float* __restrict__ cp, float* __restrict__ cq, float* __restrict__ cx,
-                                                double tol, int max_it, double* __restrict__ out) {
-  __shared__ double sh[40];
-  const int n = N * D;
-  double lb = 0.0;
-  for (int k = threadIdx.x; k < n; k += blockDim.x) {
-    cx[k] = 0.f;
-    lb += (double)cr[k] * cr[k];
-  }
-  const double bn = sqrt(cta_sum(lb, sh));
-  int it = 0, ok = 1;
-  if (bn > 0.0) {
-    bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
-    double loc = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      cp[k] = cz[k];
-      loc += (double)cr[k] * cz[k];
-    }
-    double rz = cta_sum(loc, sh);
-    for (; it < max_it; ++it) {
-      spmv_f<D>(N, A, lam, cp, cq);
-      loc = 0.0;
-      for (int k = threadIdx.x; k < n; k += blockDim.x) loc += (double)cp[k] * cq[k];
-      const double pq = cta_sum(loc, sh);
-      if (!(pq > 0.0) || !(rz > 0.0)) {
-        if (it == 0) ok = 0;
-        break;
-      }
-      const float alpha = (float)(rz / pq);
-      loc = 0.0;
-      for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        cx[k] += alpha * cp[k];
-        const float rk = cr[k] - alpha * cq[k];
-        cr[k] = rk;
-        loc += (double)rk * rk;
-      }
-      if (sqrt(cta_sum(loc, sh)) <= tol * bn) {
-        ++it;
-        break;
-      }
-      bcr_apply<D>(levels, lvl_off, lvl_n, bDinv, bFL, bFR, bb, bx, cr, cz);
-      loc = 0.0;
-      for (int k = threadIdx.x; k < n; k += blockDim.x) loc += (double)cr[k] * cz[k];
-      const double rzn = cta_sum(loc, sh);
-      const float beta = (float)(rzn / rz);
-      rz = rzn;
-      for (int k = threadIdx.x; k < n; k += blockDim.x) cp[k] = cz[k] + beta * cp[k];
-      __syncthreads();
-    }
-  }
-  if (threadIdx.x == 0) {
-    out[4] = it;
-    out[5] = ok;
-  }
-}
-
-// delta += c (FP32 correction), then r64 = -g - (H + lam D) delta with the
-// FP64 blocks; writes rhs32 = r64 and the per-row squared norm. All SMs.
-template <int D>
-__global__ void k_refine_residual(int N, CsrView A, double lam, const double* __restrict__ g,
-                                  const float* __restrict__ c, int add_c, double* __restrict__ delta,
-                                  float* __restrict__ rhs32, double* __restrict__ rowsq) {
-  constexpr int dd = D * D;
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= N) return;
-  (void)dd;
-  // the correction of this row must be applied before any row reads it: done
-  // by a separate launch (k_add_correction); here delta is final.
-  double acc[D];
-  const double* H = A.Hd64 + (size_t)v * dd;
-  const double* pv = delta + (size_t)v * D;
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    double sacc = lam * A.dampD[(size_t)v * D + a] * pv[a];
-#pragma unroll
-    for (int q = 0; q < D; ++q) sacc += H[D * a + q] * pv[q];
-    acc[a] = sacc;
-  }
-  for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
-    const double* B = A.fH64 + (size_t)A.blk[k] * 3 * dd + 2 * dd;
-    const double* pc = delta + (size_t)A.col[k] * D;
-    if (A.btr[k]) {
-#pragma unroll
-      for (int a = 0; a < D; ++a)
-#pragma unroll
-        for (int q = 0; q < D; ++q) acc[a] += B[D * q + a] * pc[q];
-    } else {
-#pragma unroll
-      for (int a = 0; a < D; ++a)
-#pragma unroll
-        for (int q = 0; q < D; ++q) acc[a] += B[D * a + q] * pc[q];
-    }
-  }
-  double sq = 0.0;
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    const double r = -g[(size_t)v * D + a] - acc[a];
-    rhs32[(size_t)v * D + a] = (float)r;
-    sq += r * r;
-  }
-  rowsq[v] = sq;
-  (void)c;
-  (void)add_c;
-}
-
-__global__ void k_add_correction(int n, const float* __restrict__ c, double* __restrict__ delta) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) delta[k] += (double)c[k];
-}
-
-__global__ void k_init_rhs(int n, const double* __restrict__ g, double* __restrict__ delta, float* __restrict__ rhs32,
-                           double* __restrict__ sq) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) {
-    delta[k] = 0.0;
-    rhs32[k] = (float)(-g[k]);
-    sq[k] = g[k] * g[k];
-  }
-}
-
-// per row: g.delta and delta.(H delta) with the undamped FP64 blocks
-template <int D>
-__global__ void k_lin_terms(int N, CsrView A, const double* __restrict__ g, const double* __restrict__ delta,
-                            double* __restrict__ gd, double* __restrict__ dhd) {
-  constexpr int dd = D * D;
-  const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= N) return;
-  double acc[D];
-  const double* H = A.Hd64 + (size_t)v * dd;
-  const double* pv = delta + (size_t)v * D;
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    double sacc = 0.0;
-#pragma unroll
-    for (int q = 0; q < D; ++q) sacc += H[D * a + q] * pv[q];
-    acc[a] = sacc;
-  }
-  for (int k = A.row_ptr[v]; k < A.row_ptr[v + 1]; ++k) {
-    const double* B = A.fH64 + (size_t)A.blk[k] * 3 * dd + 2 * dd;
-    const double* pc = delta + (size_t)A.col[k] * D;
-    if (A.btr[k]) {
-#pragma unroll
-      for (int a = 0; a < D; ++a)
-#pragma unroll
-        for (int q = 0; q < D; ++q) acc[a] += B[D * q + a] * pc[q];
-    } else {
-#pragma unroll
-      for (int a = 0; a < D; ++a)
-#pragma unroll
-        for (int q = 0; q < D; ++q) acc[a] += B[D * a + q] * pc[q];
-    }
-  }
-  double s1 = 0.0, s2 = 0.0;
-#pragma unroll
-  for (int a = 0; a < D; ++a) {
-    s1 += g[(size_t)v * D + a] * pv[a];
-    s2 += pv[a] * acc[a];
-  }
-  gd[v] = s1;
-  dhd[v] = s2;
-}
 
 template <int DIM>
 __global__ void k_retract(int N, const double* __restrict__ x, const double* __restrict__ delta,

@@ -132,6 +132,7 @@ SIGNATURES = {
     "rpgo_max_clique_heu": (C.c_int, [C.c_int32, _P, C.c_int32, C.c_int32, _P, _P]),
     "rpgo_device_info": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_int32)]),
     "rpgo_kernel_launch_count": (C.c_int64, []),
+    "rpgo_buffer_alloc_count": (C.c_int64, []),
 }
 
 
@@ -516,3 +517,8 @@ def device_info():
 
 def kernel_launch_count() -> int:
     return int(load().rpgo_kernel_launch_count())
+
+
+def buffer_alloc_count() -> int:
+    """Device and pinned host allocations made by the library's buffers."""
+    return int(load().rpgo_buffer_alloc_count())

@@ -49,6 +49,12 @@ struct SolverBase {
   virtual void temp_sizes(int64_t* nf, int64_t* nv) const = 0;
   virtual int temp_values_out(uint64_t* keys, double* poses, int64_t cap) const = 0;
   virtual int temp_weights(double* w, int64_t cap, int64_t* n) const = 0;
+  // checks at large sizes (no reference counterpart): sampled rows of the
+  // first group's consistency matrix, and the solve stage alone on a given
+  // factor list with its first n_known factors as GNC known inliers
+  virtual int pcm_rows(const rpgo_factor_batch* f, const rpgo_value_batch* v, const int32_t* rows, int n_rows,
+                       uint32_t* out, int64_t cap, int64_t* n, int64_t* src, int64_t src_cap, bool lower_only) = 0;
+  virtual int solve_graph(const rpgo_factor_batch* f, const rpgo_value_batch* v, int64_t n_known) = 0;
   int64_t warm_runs = 0, warm_fallbacks = 0;
   // wall-clock seconds spent in outlier rejection and in the solve (sums)
   double pcm_seconds = 0.0, solve_seconds = 0.0;
@@ -98,6 +104,7 @@ struct RobustSolverO final : SolverBase {
       x.measured = L::load(f->measured + k * L::stride);
       std::memcpy(x.cov, f->covariance + k * d * d, sizeof(double) * d * d);
       std::memcpy(x.sqrt_info, f->sqrt_information + k * d * d, sizeof(double) * d * d);
+      x.src = k;
       out.push_back(x);
     }
     return out;
@@ -215,7 +222,7 @@ struct RobustSolverO final : SolverBase {
       if (ok) apply(ri, pose_average(meas));
     }
   }
-  int optimize() {
+  int optimize(int64_t n_known_override = -1) {
     LmParamsO lp;
     lp.gauss_newton = (p.solver == RPGO_SOLVER_GN);
     lp.diagonal_damping = p.lm_diagonal_damping != 0;
@@ -226,7 +233,7 @@ struct RobustSolverO final : SolverBase {
     std::map<uint64_t, Pose> result;
     SolveStats st;
     const size_t num_lc = pcm ? pcm->total_lc : 0;
-    if (p.use_gnc && pcm && !(p.gnc_fix_prev_inliers && num_lc == latest_num_lc)) {
+    if (p.use_gnc && (pcm || n_known_override >= 0) && !(p.gnc_fix_prev_inliers && num_lc == latest_num_lc)) {
       GncParamsO gp;
       gp.threshold_mode = p.gnc_threshold_mode;
       gp.threshold = p.gnc_inlier_threshold;
@@ -234,7 +241,8 @@ struct RobustSolverO final : SolverBase {
       gp.mu_step = p.gnc_mu_step;
       gp.rel_cost_tol = p.gnc_relative_cost_tol;
       gp.weights_tol = p.gnc_weights_tol;
-      const size_t n_known = pcm->nfg_odom.size() + pcm->nfg_special.size();
+      const size_t n_known = n_known_override >= 0 ? (size_t)n_known_override
+                                                   : pcm->nfg_odom.size() + pcm->nfg_special.size();
       std::vector<double> init;
       if (p.gnc_bias_odom) {
         init.assign(full.size(), 0.0);
@@ -434,6 +442,58 @@ struct RobustSolverO final : SolverBase {
   int force_optimize() override {
     const auto t0 = std::chrono::steady_clock::now();
     const int rc = optimize();
+    this->solve_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+  }
+  int pcm_rows(const rpgo_factor_batch* fb, const rpgo_value_batch* vb, const int32_t* rows, int n_rows,
+               uint32_t* out, int64_t cap, int64_t* n, int64_t* src, int64_t src_cap, bool lower_only) override {
+    if (!pcm || !fb || !vb) return RPGO_ERR_UNSUPPORTED;
+    std::set<uint64_t> new_keys;
+    for (int64_t k = 0; k < vb->count; ++k) {
+      if (values.count(vb->key[k]) || !new_keys.insert(vb->key[k]).second) return RPGO_ERR_KEY;
+      values[vb->key[k]] = L::load(vb->pose + k * L::stride);
+    }
+    pcm->defer_lc = true;
+    try {
+      pcm->remove_outliers(convert(fb), new_keys, values, &nfg);
+    } catch (const std::out_of_range&) {
+      return RPGO_ERR_KEY;
+    }
+    if (pcm->loop_closures.empty()) {
+      *n = 0;
+      return RPGO_OK;
+    }
+    auto& g = pcm->loop_closures.begin()->second;
+    *n = (int64_t)g.factors.size();
+    const int words = (int)((g.factors.size() + 31) / 32);
+    std::vector<int> rv;
+    for (int i = 0; i < n_rows; ++i) {
+      if (rows[i] < 0 || rows[i] >= (int)g.factors.size()) return RPGO_ERR_ARG;
+      rv.push_back(rows[i]);
+    }
+    if (src) {
+      if (src_cap < *n) return RPGO_ERR_ARG;
+      for (size_t i = 0; i < g.factors.size(); ++i) src[i] = g.factors[i].src;
+    }
+    if (out) {
+      if (cap < (int64_t)rv.size() * words) return RPGO_ERR_ARG;
+      std::vector<uint32_t> bits;
+      pcm->sample_rows(g, rv, &bits, lower_only);
+      std::copy(bits.begin(), bits.end(), out);
+    }
+    return RPGO_OK;
+  }
+  int solve_graph(const rpgo_factor_batch* fb, const rpgo_value_batch* vb, int64_t n_known) override {
+    if (!fb || !vb || n_known < 0 || n_known > fb->count) return RPGO_ERR_ARG;
+    for (int64_t k = 0; k < vb->count; ++k) {
+      if (values.count(vb->key[k])) return RPGO_ERR_KEY;
+      values[vb->key[k]] = L::load(vb->pose + k * L::stride);
+    }
+    nfg = convert(fb);
+    for (const auto& f : nfg)
+      if (!values.count(f.k1) || !values.count(f.k2)) return RPGO_ERR_KEY;
+    const auto t0 = std::chrono::steady_clock::now();
+    const int rc = optimize(n_known);
     this->solve_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     return rc;
   }
@@ -662,6 +722,42 @@ int oracle_pairwise_adjacency(int dim, int mode, int n, const int32_t* slot_a, c
     else body(Lie2{}, std::true_type{});
   }
   return 0;
+}
+
+// 0: the reference's linear-search greedy clique (default), 1: the
+// membership-stamp form with identical results; returns the previous value
+int oracle_set_clique_impl(int impl) {
+  const int old = g_clique_impl;
+  g_clique_impl = impl;
+  return old;
+}
+// On a fresh solver: classify, odometry-check and group the closures of one
+// batch (no consistency matrix); the first group's size n, the input-batch
+// index of each of its closures (src, n entries) and the requested rows of
+// its consistency matrix (out: n_rows x ceil(n / 32) words; lower_only:
+// columns below the diagonal only)
+int oracle_pcm_rows(void* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, const int32_t* rows,
+                    int32_t n_rows, uint32_t* out, int64_t cap, int64_t* n, int64_t* src, int64_t src_cap,
+                    int lower_only) {
+  return static_cast<SolverBase*>(s)->pcm_rows(f, v, rows, n_rows, out, cap, n, src, src_cap, lower_only != 0);
+}
+// linear-search iterations of the reference's greedy clique on a bit-packed
+// adjacency (n x ceil(n/32) words)
+double oracle_clique_scan_ops(int n, const uint32_t* adj) {
+  const int words = (n + 31) / 32;
+  std::vector<uint32_t> bits(adj, adj + (size_t)n * words);
+  return fmc_scan_ops(csr_from_bits(bits, n, words), 0, -1);
+}
+// iterations cap of every LM / GN run (-1: the solver's own); returns the old
+int oracle_set_lm_max_iterations(int n) {
+  const int old = g_lm_max_iterations;
+  g_lm_max_iterations = n;
+  return old;
+}
+// On a fresh solver: RobustSolver::optimize over the given factor list and
+// values, GNC known inliers = factors [0, n_known)
+int oracle_solve_graph(void* s, const rpgo_factor_batch* f, const rpgo_value_batch* v, int64_t n_known) {
+  return static_cast<SolverBase*>(s)->solve_graph(f, v, n_known);
 }
 
 // Greedy max clique on a bit-packed adjacency (n x ceil(n/32) words).

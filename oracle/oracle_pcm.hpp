@@ -240,8 +240,15 @@ static inline Csr csr_from_bits(const std::vector<uint32_t>& bits, int n, int wo
   Csr g;
   g.off.assign(n + 1, 0);
   for (int i = 0; i < n; ++i) {
-    for (int j = 0; j < n; ++j)
-      if (j != i && ((bits[(size_t)i * words + (j >> 5)] >> (j & 31)) & 1u)) g.adj.push_back(j);
+    // set bits of row i in ascending column order (columns >= n ignored)
+    for (int w = 0; w < words && 32 * w < n; ++w) {
+      uint32_t x = bits[(size_t)i * words + w];
+      while (x) {
+        const int j = 32 * w + __builtin_ctz(x);
+        x &= x - 1u;
+        if (j < n && j != i) g.adj.push_back(j);
+      }
+    }
     g.off[i + 1] = (int)g.adj.size();
   }
   for (int i = 0; i < n; ++i) g.max_deg = std::max(g.max_deg, g.off[i + 1] - g.off[i]);
@@ -250,8 +257,10 @@ static inline Csr csr_from_bits(const std::vector<uint32_t>& bits, int n, int wo
 
 // findCliqueHeu.cpp:32-117 and 119-209: candidates first..n-1, running best
 // seeded with max_clq; the winning work buffer is returned whole, so its
-// first max_clq slots may hold stale (non-clique) vertices.
-static inline int fmc_heuristic(const Csr& g, int first, int max_clq, std::vector<int>* best) {
+// first max_clq slots may hold stale (non-clique) vertices. This is the
+// reference's loop structure, including its linear search of S[a] in the
+// neighbour list of m (the cost the CPU baseline times).
+static inline int fmc_heuristic_scan(const Csr& g, int first, int max_clq, std::vector<int>* best) {
   const int n = (int)g.off.size() - 1;
   auto deg = [&](int v) { return g.off[v + 1] - g.off[v]; };
   std::vector<int> S(std::max(g.max_deg, 0) + 1, 0), S1(std::max(g.max_deg, 0) + 1, 0);
@@ -285,6 +294,100 @@ static inline int fmc_heuristic(const Csr& g, int first, int max_clq, std::vecto
   return max_clq;
 }
 
+// The same heuristic with the linear search replaced by a membership stamp:
+// before each round, every neighbour u of m gets stamp[u] = round id, so
+// "S[a] occurs in N(m)" is one lookup. The scan's `break` on the first match
+// only ends the search, so the kept elements, their order, the round count
+// and every write to S are those of fmc_heuristic_scan: O(|S| + deg(m)) per
+// round instead of O(|S| deg(m)).
+static inline int fmc_heuristic_marked(const Csr& g, int first, int max_clq, std::vector<int>* best) {
+  const int n = (int)g.off.size() - 1;
+  auto deg = [&](int v) { return g.off[v + 1] - g.off[v]; };
+  std::vector<int> S(std::max(g.max_deg, 0) + 1, 0), S1(std::max(g.max_deg, 0) + 1, 0);
+  std::vector<int64_t> stamp(std::max(n, 1), -1);
+  int64_t round_id = 0;
+  for (int v = first; v < n; ++v) {
+    if (max_clq > deg(v)) continue;
+    int npos = 0;
+    S[npos++] = v;
+    for (int e = g.off[v]; e < g.off[v + 1]; ++e)
+      if (max_clq <= deg(g.adj[e])) S[npos++] = g.adj[e];
+    int icc = 0;
+    while (npos > 0) {
+      ++icc;
+      const int m = S[npos - 1];
+      ++round_id;
+      for (int e = g.off[m]; e < g.off[m + 1]; ++e) stamp[g.adj[e]] = round_id;
+      int n1 = 0;
+      for (int a = 0; a < npos; ++a)
+        if (stamp[S[a]] == round_id && max_clq <= deg(S[a])) S1[n1++] = S[a];
+      for (int a = 0; a < n1; ++a) S[a] = S1[a];
+      npos = n1;
+    }
+    if (max_clq < icc) {
+      *best = S;
+      max_clq = icc;
+    }
+  }
+  return max_clq;
+}
+
+// Inner-loop iterations the reference's linear search (fmc_heuristic_scan)
+// performs on g: per round and per element S[a], the entries of N(m) it
+// compares before the match that keeps S[a] (position + 1), or all deg(m)
+// when S[a] is not kept. Same control flow as fmc_heuristic_marked, so it
+// costs O(|S| + deg(m)) per round; used to price the linear search at sizes
+// where running it is out of reach.
+static inline double fmc_scan_ops(const Csr& g, int first, int max_clq) {
+  const int n = (int)g.off.size() - 1;
+  auto deg = [&](int v) { return g.off[v + 1] - g.off[v]; };
+  std::vector<int> S(std::max(g.max_deg, 0) + 1, 0), S1(std::max(g.max_deg, 0) + 1, 0);
+  std::vector<int64_t> stamp(std::max(n, 1), -1);
+  std::vector<int> where(std::max(n, 1), 0);
+  int64_t round_id = 0;
+  double ops = 0.0;
+  for (int v = first; v < n; ++v) {
+    if (max_clq > deg(v)) continue;
+    int npos = 0;
+    S[npos++] = v;
+    for (int e = g.off[v]; e < g.off[v + 1]; ++e)
+      if (max_clq <= deg(g.adj[e])) S[npos++] = g.adj[e];
+    int icc = 0;
+    while (npos > 0) {
+      ++icc;
+      const int m = S[npos - 1];
+      ++round_id;
+      for (int e = g.off[m]; e < g.off[m + 1]; ++e) {
+        stamp[g.adj[e]] = round_id;
+        where[g.adj[e]] = e - g.off[m];
+      }
+      int n1 = 0;
+      int64_t cnt = 0;
+      for (int a = 0; a < npos; ++a) {
+        if (stamp[S[a]] == round_id && max_clq <= deg(S[a])) {
+          S1[n1++] = S[a];
+          cnt += where[S[a]] + 1;
+        } else {
+          cnt += deg(m);
+        }
+      }
+      ops += (double)cnt;
+      for (int a = 0; a < n1; ++a) S[a] = S1[a];
+      npos = n1;
+    }
+    if (max_clq < icc) max_clq = icc;
+  }
+  return ops;
+}
+
+// Which form the oracle runs: 0 = the reference's linear search (default),
+// 1 = the membership-stamp form (identical results, for checks at large sizes).
+inline int g_clique_impl = 0;
+static inline int fmc_heuristic(const Csr& g, int first, int max_clq, std::vector<int>* best) {
+  return g_clique_impl == 1 ? fmc_heuristic_marked(g, first, max_clq, best)
+                            : fmc_heuristic_scan(g, first, max_clq, best);
+}
+
 // ---------------------------------------------------------------- factor records
 template <class L>
 struct Factor {
@@ -293,6 +396,7 @@ struct Factor {
   typename L::Pose measured = L::identity();
   double cov[L::dim * L::dim] = {0};
   double sqrt_info[L::dim * L::dim] = {0};
+  int64_t src = -1;  // index in the input batch (checks only)
 };
 
 // ObservationId (TypeUtils.h:44-58) with the same symmetric equality and
@@ -367,6 +471,9 @@ struct Pcm {
   std::unordered_map<char, Trajectory<U>> trajectories;
   size_t total_lc = 0, total_good_lc = 0;
   bool warned_missing = false;
+  // checks at large sizes: parse, odometry-check and group the closures but
+  // leave the consistency matrix and the clique to sample_rows
+  bool defer_lc = false;
 
   explicit Pcm(const PcmParamsO& p) : params(p) {
     if (p.odom_threshold < 0 || p.odom_rot_threshold < 0 || p.odom_trans_threshold < 0) odom_check = false;
@@ -513,7 +620,7 @@ struct Pcm {
       in_order.push_back(id);
       ++total_lc;
     }
-    if (lc_check)
+    if (lc_check && !defer_lc)
       for (const auto& id : touched) increment_adjacency(loop_closures[id], old_sizes[id]);
   }
 
@@ -627,6 +734,30 @@ struct Pcm {
     *out = build_graph();
   }
 
+  // Rows of a group's consistency matrix as incrementAdjMatrix (Pcm.h:725-768)
+  // fills it: bit (r, c), r != c, is are_loops_consistent(factor min(r, c),
+  // factor max(r, c)). out: rows.size() x ceil(n / 32) words. Words are
+  // independent, so they are spread over the OpenMP threads. lower_only:
+  // columns c < r only (the pairs that new row r adds, as the reference
+  // evaluates them).
+  void sample_rows(Group<L>& g, const std::vector<int>& rows, std::vector<uint32_t>* out, bool lower_only = false) {
+    const int n = (int)g.factors.size(), words = (n + 31) / 32;
+    out->assign(rows.size() * (size_t)words, 0u);
+    const int64_t tasks = (int64_t)rows.size() * words;
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int64_t t = 0; t < tasks; ++t) {
+      const int r = rows[t / words], w = (int)(t % words);
+      uint32_t x = 0u;
+      for (int b = 0; b < 32; ++b) {
+        const int c = 32 * w + b;
+        if (c >= n || c == r || (lower_only && c > r)) continue;
+        const int i = std::min(r, c), j = std::max(r, c);
+        if (are_loops_consistent(g.factors[i], g.factors[j])) x |= 1u << b;
+      }
+      (*out)[t] = x;
+    }
+  }
+
   // Pcm.h:148-281. values: the solver's value map, already extended by the
   // caller with new_values. Returns do_optimize.
   template <class ValuesMap, class KeySet>
@@ -661,8 +792,13 @@ struct Pcm {
     if (!lcs.empty()) {
       std::unordered_map<ObsId, size_t, ObsIdHash> num_new;
       parse_and_increment(lcs, values, &num_new);
-      if (params.incremental) find_inliers_incremental(num_new);
-      else find_inliers();
+      if (defer_lc) {
+        // nothing: sample_rows evaluates the requested rows
+      } else if (params.incremental) {
+        find_inliers_incremental(num_new);
+      } else {
+        find_inliers();
+      }
       do_optimize = true;
     }
     *out_graph = build_graph();

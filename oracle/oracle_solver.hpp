@@ -268,6 +268,14 @@ struct BlockChol {
   std::vector<std::vector<int>> cols;      // per position k: later positions adjacent at elimination
   std::vector<std::vector<double>> L;      // per position k: [L_kk, L_{cols[k][0]},k, ...]
   std::vector<std::vector<int>> upd_slot;  // per k: for pairs (a>=c) of cols[k], slot in column cols[k][c]
+  // Left-looking form of the same updates: per column j, per block slot, the
+  // sources (k, a, q) in ascending k (the order in which the right-looking
+  // loop over k applies them), and the columns grouped by dependency level.
+  struct Upd {
+    int k, a, q;
+  };
+  std::vector<std::vector<std::vector<Upd>>> upd_in;  // [j][slot] -> sources
+  std::vector<int> lvl_ptr, lvl_cols;
 
   void symbolic(int n, int bs, const std::vector<std::pair<int, int>>& edges) {
     N = n;
@@ -278,30 +286,29 @@ struct BlockChol {
         adj[e.first].insert(e.second);
         adj[e.second].insert(e.first);
       }
-    std::vector<char> done(n, 0);
     order.clear();
     pos.assign(n, -1);
     std::vector<std::vector<int>> nb_at(n);
+    // minimum degree, ties to the smallest index: the first element of the
+    // set ordered by (degree, index) is the vertex a scan v = 0..n-1 with a
+    // strict "<" on the degree would pick
+    std::set<std::pair<size_t, int>> queue;
+    for (int v = 0; v < n; ++v) queue.insert({adj[v].size(), v});
     for (int step = 0; step < n; ++step) {
-      int best = -1;
-      size_t bd = std::numeric_limits<size_t>::max();
-      for (int v = 0; v < n; ++v)
-        if (!done[v] && adj[v].size() < bd) {
-          bd = adj[v].size();
-          best = v;
-        }
-      const int v = best;
-      done[v] = 1;
+      const int v = queue.begin()->second;
+      queue.erase(queue.begin());
       pos[v] = step;
       order.push_back(v);
       std::vector<int> nb(adj[v].begin(), adj[v].end());
       nb_at[v] = nb;
+      for (int u : nb) queue.erase({adj[u].size(), u});
       for (int u : nb) adj[u].erase(v);
       for (size_t i = 0; i < nb.size(); ++i)
         for (size_t j = i + 1; j < nb.size(); ++j) {
           adj[nb[i]].insert(nb[j]);
           adj[nb[j]].insert(nb[i]);
         }
+      for (int u : nb) queue.insert({adj[u].size(), u});
       adj[v].clear();
     }
     cols.assign(n, {});
@@ -326,12 +333,29 @@ struct BlockChol {
           }
         }
     }
+    upd_in.assign(n, {});
+    for (int j = 0; j < n; ++j) upd_in[j].assign(cols[j].size() + 1, {});
+    std::vector<int> level(n, 0);
+    for (int k = 0; k < n; ++k) {
+      const auto& c = cols[k];
+      size_t idx = 0;
+      for (size_t a = 0; a < c.size(); ++a)
+        for (size_t q = 0; q <= a; ++q) upd_in[c[q]][upd_slot[k][idx++]].push_back({k, (int)a, (int)q});
+      for (int u : c) level[u] = std::max(level[u], level[k] + 1);
+    }
+    const int nl = n ? *std::max_element(level.begin(), level.end()) + 1 : 0;
+    lvl_ptr.assign(nl + 1, 0);
+    for (int j = 0; j < n; ++j) lvl_ptr[level[j] + 1]++;
+    for (int l = 0; l < nl; ++l) lvl_ptr[l + 1] += lvl_ptr[l];
+    lvl_cols.assign(n, 0);
+    std::vector<int> fill(lvl_ptr.begin(), lvl_ptr.end() - 1);
+    for (int j = 0; j < n; ++j) lvl_cols[fill[level[j]]++] = j;
   }
   // load H (diag blocks per variable, off-diagonal blocks per edge (i,j) meaning H_ij)
   void load(const std::vector<double>& Hd, const std::vector<std::pair<int, int>>& edges,
             const std::vector<double>& He) {
     const int bb = b * b;
-    L.assign(N, {});
+    L.resize(N);  // keeps each column's storage from the previous load
     for (int k = 0; k < N; ++k) L[k].assign((size_t)bb * (cols[k].size() + 1), 0.0);
     for (int v = 0; v < N; ++v)
       for (int i = 0; i < bb; ++i) L[pos[v]][i] += Hd[(size_t)v * bb + i];
@@ -356,52 +380,69 @@ struct BlockChol {
         for (int c = 0; c < b; ++c) dst[r * b + c] += tr ? B[c * b + r] : B[r * b + c];
     }
   }
-  bool factor() {
+  // Column j of the factor, left-looking: every block of column j first
+  // takes its updates -= L(row, k) L(j, k)^T from the earlier columns k in
+  // ascending k (each product summed t = 0..b-1 from 0, then subtracted),
+  // which are the operations and the order of the right-looking loop (column
+  // k applying its updates to all later columns after being factored); then
+  // the diagonal block's Cholesky and the off-diagonal solves. Columns of one
+  // dependency level do not touch each other, so they run on the OpenMP
+  // threads; the factor does not depend on the thread count.
+  bool factor_column(int j) {
     const int bb = b * b;
-    for (int k = 0; k < N; ++k) {
-      double* D = &L[k][0];
-      double Lk[36];
-      // dense Cholesky of the diagonal block (lower)
-      for (int i = 0; i < b; ++i)
-        for (int j = 0; j <= i; ++j) {
-          double acc = D[i * b + j];
-          for (int q = 0; q < j; ++q) acc -= Lk[i * b + q] * Lk[j * b + q];
-          if (i == j) {
-            if (!(acc > 0.0)) return false;
-            Lk[i * b + i] = std::sqrt(acc);
-          } else {
-            Lk[i * b + j] = acc / Lk[j * b + j];
-          }
-        }
-      for (int i = 0; i < b; ++i)
-        for (int j = 0; j < b; ++j) D[i * b + j] = (j <= i) ? Lk[i * b + j] : 0.0;
-      const size_t m = cols[k].size();
-      // L_uk = A_uk Lk^-T  (row-wise forward substitution)
-      for (size_t a = 0; a < m; ++a) {
-        double* B = &L[k][(a + 1) * bb];
+    auto& Lj = L[j];
+    for (size_t s = 0; s < upd_in[j].size(); ++s) {
+      double* T = &Lj[s * bb];
+      for (const Upd& u : upd_in[j][s]) {
+        const double* La = &L[u.k][(size_t)(u.a + 1) * bb];
+        const double* Lq = &L[u.k][(size_t)(u.q + 1) * bb];
         for (int r = 0; r < b; ++r)
-          for (int j = 0; j < b; ++j) {
-            double acc = B[r * b + j];
-            for (int q = 0; q < j; ++q) acc -= B[r * b + q] * Lk[j * b + q];
-            B[r * b + j] = acc / Lk[j * b + j];
+          for (int c = 0; c < b; ++c) {
+            double acc = 0.0;
+            for (int t = 0; t < b; ++t) acc += La[r * b + t] * Lq[c * b + t];
+            T[r * b + c] -= acc;
           }
       }
-      // Schur complement updates into later columns
-      size_t idx = 0;
-      for (size_t a = 0; a < m; ++a)
-        for (size_t q = 0; q <= a; ++q) {
-          const double* La = &L[k][(a + 1) * bb];
-          const double* Lq = &L[k][(q + 1) * bb];
-          double* T = &L[cols[k][q]][(size_t)upd_slot[k][idx++] * bb];
-          for (int r = 0; r < b; ++r)
-            for (int c = 0; c < b; ++c) {
-              double acc = 0.0;
-              for (int t = 0; t < b; ++t) acc += La[r * b + t] * Lq[c * b + t];
-              T[r * b + c] -= acc;
-            }
+    }
+    double* D = &Lj[0];
+    double Lk[36];
+    // dense Cholesky of the diagonal block (lower)
+    for (int i = 0; i < b; ++i)
+      for (int jj = 0; jj <= i; ++jj) {
+        double acc = D[i * b + jj];
+        for (int q = 0; q < jj; ++q) acc -= Lk[i * b + q] * Lk[jj * b + q];
+        if (i == jj) {
+          if (!(acc > 0.0)) return false;
+          Lk[i * b + i] = std::sqrt(acc);
+        } else {
+          Lk[i * b + jj] = acc / Lk[jj * b + jj];
+        }
+      }
+    for (int i = 0; i < b; ++i)
+      for (int jj = 0; jj < b; ++jj) D[i * b + jj] = (jj <= i) ? Lk[i * b + jj] : 0.0;
+    // L_uj = A_uj Lj^-T  (row-wise forward substitution)
+    for (size_t a = 0; a < cols[j].size(); ++a) {
+      double* B = &Lj[(a + 1) * bb];
+      for (int r = 0; r < b; ++r)
+        for (int c = 0; c < b; ++c) {
+          double acc = B[r * b + c];
+          for (int q = 0; q < c; ++q) acc -= B[r * b + q] * Lk[c * b + q];
+          B[r * b + c] = acc / Lk[c * b + c];
         }
     }
     return true;
+  }
+  bool factor() {
+    bool ok = true;
+    for (size_t l = 0; l + 1 < lvl_ptr.size() && ok; ++l) {
+      const int c0 = lvl_ptr[l], c1 = lvl_ptr[l + 1];
+      int bad = 0;
+#pragma omp parallel for schedule(dynamic, 4) reduction(| : bad)
+      for (int t = c0; t < c1; ++t)
+        if (!factor_column(lvl_cols[t])) bad |= 1;
+      ok = bad == 0;
+    }
+    return ok;
   }
   // solve (L L^T) x = rhs, rhs/x indexed by variable
   void solve(const std::vector<double>& rhs, std::vector<double>& x) const {
@@ -498,6 +539,10 @@ struct SolveStats {
   bool failed = false;
 };
 
+// Sampling hook of the CPU timings: when >= 0, every LM / GN run stops after
+// this many iterations (default -1: the solver's own limit).
+inline int g_lm_max_iterations = -1;
+
 template <class S>
 struct NLS {
   using L = typename S::L;
@@ -510,13 +555,23 @@ struct NLS {
   std::vector<uint64_t> keys;
   std::map<uint64_t, int> index;
   std::vector<std::pair<int, int>> edges;  // variable pairs of between factors (per factor)
+  std::vector<int> fi_, fj_;               // variable indices of every factor
+  std::vector<int> edge_fac_;              // factor of each edge
+  std::vector<int> inc_ptr_, inc_;         // per variable: its factors (factor << 1 | role), factor order
+  mutable std::vector<double> lin_part_;   // per-factor linearisation pieces
   BlockChol chol;
   bool symbolic_done = false;
 
   double w(size_t k) const { return weights ? (*weights)[k] : 1.0; }
+  // per-factor terms on the OpenMP threads, summed in factor order (the
+  // same additions as a sequential loop)
   double error(const Values& v) const {
+    const int64_t F = (int64_t)graph->size();
+    std::vector<double> e((size_t)F);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < F; ++k) e[(size_t)k] = factor_error<S>((*graph)[(size_t)k], v, w((size_t)k));
     double s = 0.0;
-    for (size_t k = 0; k < graph->size(); ++k) s += factor_error<S>((*graph)[k], v, w(k));
+    for (int64_t k = 0; k < F; ++k) s += e[(size_t)k];
     return s;
   }
   void setup(const Values& v) {
@@ -527,27 +582,57 @@ struct NLS {
       keys.push_back(kv.first);
     }
     edges.clear();
-    for (auto& f : *graph)
-      if (f.kind == 0) edges.push_back({index.at(f.k1), index.at(f.k2)});
+    edge_fac_.clear();
+    fi_.clear();
+    fj_.clear();
+    for (auto& f : *graph) {
+      fi_.push_back(index.at(f.k1));
+      fj_.push_back(f.kind == 0 ? index.at(f.k2) : fi_.back());
+      if (f.kind == 0) {
+        edges.push_back({fi_.back(), fj_.back()});
+        edge_fac_.push_back((int)(fi_.size() - 1));
+      }
+    }
+    // per variable: (factor << 1 | role) in factor order, role 0 = the i
+    // (or prior) part, 1 = the j part
+    const int nv = (int)keys.size();
+    inc_ptr_.assign(nv + 1, 0);
+    for (size_t k = 0; k < fi_.size(); ++k) {
+      inc_ptr_[fi_[k] + 1]++;
+      if ((*graph)[k].kind == 0) inc_ptr_[fj_[k] + 1]++;
+    }
+    for (int v = 0; v < nv; ++v) inc_ptr_[v + 1] += inc_ptr_[v];
+    inc_.assign(inc_ptr_[nv], 0);
+    std::vector<int> fill(inc_ptr_.begin(), inc_ptr_.end() - 1);
+    for (size_t k = 0; k < fi_.size(); ++k) {
+      inc_[fill[fi_[k]]++] = (int)(k << 1);
+      if ((*graph)[k].kind == 0) inc_[fill[fj_[k]]++] = (int)(k << 1) | 1;
+    }
     if (!symbolic_done) {
       chol.symbolic((int)keys.size(), d, edges);
       symbolic_done = true;
     }
   }
   // H (diag blocks Hd, per-between-factor blocks He), g, and 0.5|b|^2
+  // Per factor (OpenMP threads): its Hessian blocks and gradient pieces;
+  // then added into H and g in factor order, so every sum sees the same
+  // additions in the same order as a sequential pass.
   void linearize(const Values& v, std::vector<double>& Hd, std::vector<double>& He, std::vector<double>& g) const {
     const int n = (int)keys.size();
-    Hd.assign((size_t)n * d * d, 0.0);
-    He.assign(edges.size() * d * d, 0.0);
+    constexpr int dd = d * d, rec = 3 * dd + 2 * d;
+    const int64_t F = (int64_t)graph->size();
+    Hd.assign((size_t)n * dd, 0.0);
+    He.assign(edges.size() * dd, 0.0);
     g.assign((size_t)n * d, 0.0);
-    size_t e = 0;
-    for (size_t k = 0; k < graph->size(); ++k) {
-      const auto& f = (*graph)[k];
-      const int i = index.at(f.k1);
+    std::vector<double>& part = lin_part_;
+    part.resize((size_t)F * rec);
+#pragma omp parallel for schedule(static)
+    for (int64_t k = 0; k < F; ++k) {
+      const auto& f = (*graph)[(size_t)k];
+      double* P = &part[(size_t)k * rec];
       double r[d], Ji[d * d], Jj[d * d];
       if (f.kind == 0) {
-        const int j = index.at(f.k2);
-        linearize_factor<S>(f, v.at(f.k1), v.at(f.k2), w(k), r, Ji, Jj);
+        linearize_factor<S>(f, v.at(f.k1), v.at(f.k2), w((size_t)k), r, Ji, Jj);
         for (int a = 0; a < d; ++a)
           for (int b = 0; b < d; ++b) {
             double hii = 0, hjj = 0, hij = 0;
@@ -556,9 +641,9 @@ struct NLS {
               hjj += Jj[q * d + a] * Jj[q * d + b];
               hij += Ji[q * d + a] * Jj[q * d + b];
             }
-            Hd[(size_t)i * d * d + a * d + b] += hii;
-            Hd[(size_t)j * d * d + a * d + b] += hjj;
-            He[e * d * d + a * d + b] += hij;
+            P[a * d + b] = hii;
+            P[dd + a * d + b] = hjj;
+            P[2 * dd + a * d + b] = hij;
           }
         for (int a = 0; a < d; ++a) {
           double gi = 0, gj = 0;
@@ -566,23 +651,42 @@ struct NLS {
             gi += Ji[q * d + a] * r[q];
             gj += Jj[q * d + a] * r[q];
           }
-          g[(size_t)i * d + a] += gi;
-          g[(size_t)j * d + a] += gj;
+          P[3 * dd + a] = gi;
+          P[3 * dd + d + a] = gj;
         }
-        ++e;
       } else {
-        linearize_factor<S>(f, v.at(f.k1), v.at(f.k1), w(k), r, Ji, nullptr);
+        linearize_factor<S>(f, v.at(f.k1), v.at(f.k1), w((size_t)k), r, Ji, nullptr);
         for (int a = 0; a < d; ++a)
           for (int b = 0; b < d; ++b) {
             double h = 0;
             for (int q = 0; q < d; ++q) h += Ji[q * d + a] * Ji[q * d + b];
-            Hd[(size_t)i * d * d + a * d + b] += h;
+            P[a * d + b] = h;
           }
         for (int a = 0; a < d; ++a) {
           double gi = 0;
           for (int q = 0; q < d; ++q) gi += Ji[q * d + a] * r[q];
-          g[(size_t)i * d + a] += gi;
+          P[3 * dd + a] = gi;
         }
+      }
+    }
+    // He: one factor per edge slot; Hd and g: per variable, its factors'
+    // pieces in factor order (the incidence lists ascend by factor, the i
+    // part before the j part), the additions of a sequential pass
+    const int64_t E = (int64_t)edges.size();
+#pragma omp parallel for schedule(static)
+    for (int64_t e = 0; e < E; ++e) {
+      const double* P = &part[(size_t)edge_fac_[(size_t)e] * rec];
+      for (int t = 0; t < dd; ++t) He[(size_t)e * dd + t] += P[2 * dd + t];
+    }
+#pragma omp parallel for schedule(static)
+    for (int v = 0; v < n; ++v) {
+      double* H = &Hd[(size_t)v * dd];
+      double* gv = &g[(size_t)v * d];
+      for (int u = inc_ptr_[v]; u < inc_ptr_[v + 1]; ++u) {
+        const int k = inc_[u] >> 1, role = inc_[u] & 1;
+        const double* P = &part[(size_t)k * rec];
+        for (int t = 0; t < dd; ++t) H[t] += P[role * dd + t];
+        for (int a = 0; a < d; ++a) gv[a] += P[3 * dd + role * d + a];
       }
     }
   }
@@ -601,13 +705,19 @@ struct NLS {
     return s;
   }
   Values retract(const Values& v, const std::vector<double>& delta) const {
+    std::vector<Pose> nv(keys.size());
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)keys.size(); ++i)
+      nv[(size_t)i] = L::compose(v.at(keys[(size_t)i]), S::exp(&delta[(size_t)i * d]));
     Values out;
-    for (size_t i = 0; i < keys.size(); ++i) out[keys[i]] = L::compose(v.at(keys[i]), S::exp(&delta[i * d]));
+    for (size_t i = 0; i < keys.size(); ++i) out.emplace_hint(out.end(), keys[i], nv[i]);  // keys ascend
     return out;
   }
 
   // GTSAM LevenbergMarquardtOptimizer / GaussNewtonOptimizer restated
-  Values optimize(const Values& init, const LmParamsO& p, SolveStats* st) {
+  Values optimize(const Values& init, const LmParamsO& p_in, SolveStats* st) {
+    LmParamsO p = p_in;
+    if (g_lm_max_iterations >= 0) p.max_iterations = g_lm_max_iterations;
     setup(init);
     Values cur = init;
     double cur_err = error(cur);
@@ -727,8 +837,11 @@ GncResult<S> gnc_tls(const std::vector<Factor<typename S::L>>& graph, const std:
   auto result = nls.optimize(init, lp, &out.stats);
   // mu initialisation from the residuals at the initial values
   double mu = std::numeric_limits<double>::infinity();
+  std::vector<double> r0(nf);
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < (int64_t)nf; ++k) r0[(size_t)k] = factor_error<S>(graph[(size_t)k], init, 1.0);
   for (size_t k = 0; k < nf; ++k) {
-    const double rk = factor_error<S>(graph[k], init, 1.0);
+    const double rk = r0[k];
     if (2.0 * rk - barc[k] > 0.0) mu = std::min(mu, barc[k] / (2.0 * rk - barc[k]));
   }
   if (mu >= 0.0 && mu < 1e-6) mu = 1e-6;
@@ -743,7 +856,9 @@ GncResult<S> gnc_tls(const std::vector<Factor<typename S::L>>& graph, const std:
   }
   for (int it = 0; it < max_outer; ++it) {
     out.outer_iterations = it + 1;
-    for (size_t k = 0; k < nf; ++k) {
+#pragma omp parallel for schedule(static)
+    for (int64_t kk = 0; kk < (int64_t)nf; ++kk) {
+      const size_t k = (size_t)kk;
       if (k < n_known) {
         weights[k] = 1.0;
         continue;

@@ -100,6 +100,14 @@ def lib():
         _lib.oracle_pairwise_adjacency.argtypes = [C.c_int, C.c_int, C.c_int] + [C.c_void_p] * 9 + [
             C.c_double, C.c_double, C.c_void_p]
         _lib.oracle_max_clique_heu.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        _lib.oracle_set_clique_impl.argtypes = [C.c_int]
+        _lib.oracle_pcm_rows.argtypes = [C.c_void_p, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.c_void_p,
+                                         C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.c_void_p,
+                                         C.c_int64, C.c_int]
+        _lib.oracle_clique_scan_ops.restype = C.c_double
+        _lib.oracle_clique_scan_ops.argtypes = [C.c_int, C.c_void_p]
+        _lib.oracle_set_lm_max_iterations.argtypes = [C.c_int]
+        _lib.oracle_solve_graph.argtypes = [C.c_void_p, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.c_int64]
     return _lib
 
 
@@ -256,11 +264,85 @@ class OracleSolver:
         assert lib().oracle_temp_weights(self.h, _ptr(w), n.value, C.byref(n)) == 0
         return w
 
+    def pcm_rows(self, graph, rows, lower_only=False):
+        """On a fresh solver: classify, odometry-check and group the closures
+        of `graph` (one batch) without the consistency matrix; returns (n,
+        src, bits): the first group's size, the index in `graph` of each of
+        its closures (group order), and rows `rows` of its consistency matrix
+        (len(rows) x ceil(n / 32) words), evaluated on the OpenMP threads;
+        lower_only: columns below the diagonal only (each pair once)."""
+        b = _Batch(graph)
+        r = np.ascontiguousarray(rows, dtype=np.int32)
+        nf = max(graph.num_factors, 1)
+        flat = np.zeros(max(len(r), 1) * ((nf + 31) // 32), dtype=np.uint32)
+        src = np.zeros(nf, dtype=np.int64)
+        n = C.c_int64(0)
+        rc = lib().oracle_pcm_rows(self.h, C.byref(b.f), C.byref(b.v), _ptr(r), len(r), _ptr(flat), flat.size,
+                                   C.byref(n), _ptr(src), src.size, int(lower_only))
+        assert rc == 0, rc
+        words = (n.value + 31) // 32
+        bits = flat[:len(r) * words].reshape(len(r), words)
+        return n.value, src[:n.value], bits
+
+    def solve_graph(self, graph, n_known: int) -> int:
+        """On a fresh solver: the solve stage alone (RobustSolver::optimize)
+        over `graph`'s factors and values, with factors [0, n_known) as the
+        GNC known inliers."""
+        b = _Batch(graph)
+        return lib().oracle_solve_graph(self.h, C.byref(b.f), C.byref(b.v), int(n_known))
+
     def set_warm_probs(self, probs):
         """Inlier probabilities for the next warm-started GNC solve, one per
         factor of the graph to optimise (known inliers are ignored)."""
         self._warm = np.ascontiguousarray(probs, dtype=np.float64)
         lib().oracle_set_warm_probs(self.h, _ptr(self._warm), self._warm.size)
+
+
+def set_clique_impl(impl: int) -> int:
+    """0: the reference's linear-search greedy clique (default); 1: the
+    membership-stamp form with identical results (for large checks).
+    Returns the previous setting."""
+    return lib().oracle_set_clique_impl(int(impl))
+
+
+def filtered_graph(graph, kind, key1, key2):
+    """The factor graph a solver's outlier rejection produced, rebuilt from
+    its factor list (kind, key1, key2 in graph order) with the measurements
+    and noise models of the matching factors of the input `graph`. The greedy
+    clique can list a closure twice (stale buffer slots, as in the
+    reference): a repeated factor reuses its input."""
+    from rpgo_gb300.graph import Graph
+
+    src = {}
+    for i in range(graph.num_factors):
+        src.setdefault((int(graph.kind[i]), int(graph.key1[i]), int(graph.key2[i])), []).append(i)
+    g = Graph(graph.dim)
+    used = {}
+    for kd, a, b in zip(kind, key1, key2):
+        key = (int(kd), int(a), int(b))
+        j = src[key][min(used.get(key, 0), len(src[key]) - 1)]
+        used[key] = used.get(key, 0) + 1
+        g.kind.append(graph.kind[j])
+        g.key1.append(graph.key1[j])
+        g.key2.append(graph.key2[j])
+        g.measured.append(graph.measured[j])
+        g.cov.append(graph.cov[j])
+        g.sqrt_info.append(graph.sqrt_info[j])
+    g.value_keys, g.value_poses = list(graph.value_keys), list(graph.value_poses)
+    return g
+
+
+def clique_scan_ops(adj_words: np.ndarray, n: int) -> float:
+    """Inner-loop iterations of the reference's linear-search greedy clique
+    on this adjacency (counted, not run)."""
+    adj = np.ascontiguousarray(adj_words, dtype=np.uint32)
+    return lib().oracle_clique_scan_ops(int(n), _ptr(adj))
+
+
+def set_lm_max_iterations(n: int) -> int:
+    """Cap every LM / GN run at n iterations (-1: the solver's own limit);
+    returns the previous cap. For bounded CPU timing samples."""
+    return lib().oracle_set_lm_max_iterations(int(n))
 
 
 def set_threads(n: int = 0) -> int:

@@ -33,7 +33,9 @@ def convert(src: str, dst: str) -> None:
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path to the Kimera-RPGO source tree>")
+    ref = sys.argv[1]
     here = os.path.dirname(os.path.abspath(__file__))
     for name in ("robot_a", "robot_b"):
         convert(os.path.join(ref, "tests", "data", name + ".g2o"), os.path.join(here, name + ".npz"))

@@ -256,3 +256,159 @@ def test_oracle_pair_tests_same_on_any_thread_count():
         assert np.array_equal(out[0][2], out[1][2])
     finally:
         O.set_threads(before)
+
+
+# ---------------------------------------------------------------- oracle forms used for large checks
+@pytest.mark.parametrize("seed", range(8))
+def test_clique_stamp_form_matches_linear_scan(seed):
+    # the membership-stamp form must reproduce the reference's linear-search
+    # form exactly: size, index list (stale slots included), incremental form
+    rng = np.random.default_rng(200 + seed)
+    n = int(rng.integers(1, 300))
+    p = rng.uniform(0.02, 0.98)
+    iu = np.triu_indices(n, 1)
+    m = rng.random(len(iu[0])) < p
+    adj = _bits(n, list(zip(iu[0][m], iu[1][m])))
+    before = O.set_clique_impl(0)
+    try:
+        ref = O.max_clique_heu(adj, n)
+        ref2 = O.max_clique_heu(adj, n, n // 3, max(1, ref[0] // 2))
+        O.set_clique_impl(1)
+        got = O.max_clique_heu(adj, n)
+        got2 = O.max_clique_heu(adj, n, n // 3, max(1, ref[0] // 2))
+    finally:
+        O.set_clique_impl(before)
+    assert ref[0] == got[0] and np.array_equal(ref[1], got[1])
+    assert ref2[0] == got2[0] and np.array_equal(ref2[1], got2[1])
+
+
+def _oracle_run(p, graph, impl):
+    before = O.set_clique_impl(impl)
+    try:
+        o = O.OracleSolver(p)
+        assert o.update(graph) == 0
+        return o
+    finally:
+        O.set_clique_impl(before)
+
+
+def test_oracle_stamp_clique_same_pcm_result():
+    # whole PCM + solve on the 2D benchmark graph (thresholds 1.0 / 1.0) and a
+    # 3D walk: same factor list and estimate with either clique form
+    from rpgo_gb300 import synth
+    from rpgo_gb300.params import QUIET, RobustSolverParams
+
+    cases = [(synth.config_c1().graph, RobustSolverParams().setPcm2DParams(1.0, 1.0, QUIET)),
+             (synth.walk3d(800, 200, 60, seed=19).graph,
+              RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9))]
+    for graph, p in cases:
+        a, b = _oracle_run(p, graph, 0), _oracle_run(p, graph, 1)
+        for x, y in zip(a.factors()[:3], b.factors()[:3]):
+            assert np.array_equal(x, y)
+        assert np.array_equal(a.estimate()[1], b.estimate()[1])
+        assert np.array_equal(a.gnc_weights(), b.gnc_weights())
+
+
+def test_pcm_rows_equal_full_matrix_rows():
+    from rpgo_gb300 import synth
+    from rpgo_gb300.params import QUIET, RobustSolverParams
+
+    s = synth.walk3d(700, 160, 60, seed=23)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET)
+    o = O.OracleSolver(p)
+    assert o.update(s.graph, False) == 0
+    full = o.adjacency(0)
+    n, src, _ = O.OracleSolver(p).pcm_rows(s.graph, [])
+    assert n == full.shape[0]
+    rows = np.array([0, 1, n // 2, n - 1], dtype=np.int32)
+    n2, src2, bits = O.OracleSolver(p).pcm_rows(s.graph, rows)
+    assert n2 == n and np.array_equal(src, src2)
+    assert np.array_equal(bits, full[rows])
+    # src: group order = arrival order of the closures that passed the odometry check
+    assert np.all(np.diff(src) > 0) and src[0] >= s.n_odom + 1
+
+
+def test_solve_graph_equals_update_solve():
+    # the solve stage alone on the factor list an update produced (known
+    # inliers = odometry + priors) equals that update's solve
+    from rpgo_gb300 import synth
+    from rpgo_gb300.params import QUIET, RobustSolverParams
+
+    s = synth.walk3d(500, 120, 40, seed=29)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+    o = O.OracleSolver(p)
+    assert o.update(s.graph) == 0
+    c = o.counts()
+    kind, k1, k2, _ = o.factors()
+    fg = O.filtered_graph(s.graph, kind, k1, k2)
+    o2 = O.OracleSolver(p)
+    assert o2.solve_graph(fg, c.num_odom + c.num_special) == 0
+    assert np.array_equal(o.estimate()[1], o2.estimate()[1])
+    assert np.array_equal(o.gnc_weights(), o2.gnc_weights())
+    assert o.stats()["linear_solves"] == o2.stats()["linear_solves"]
+
+
+def test_oracle_solve_same_on_any_thread_count():
+    # per-factor linearisation and error terms run on OpenMP threads and are
+    # summed in factor order: the estimate must not depend on the count
+    from rpgo_gb300 import synth
+    from rpgo_gb300.params import QUIET, RobustSolverParams
+
+    s = synth.walk3d(400, 100, 30, seed=31)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+    before = O.set_threads(0)
+    try:
+        out = []
+        for threads in (1, 5):
+            O.set_threads(threads)
+            o = O.OracleSolver(p)
+            assert o.update(s.graph) == 0
+            out.append((o.estimate()[1], o.gnc_weights()))
+        assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    finally:
+        O.set_threads(before)
+
+
+def _scan_ops_python(n, adj):
+    """findCliqueHeu.cpp:32-117 with a counter on the inner linear search."""
+    nb = [[j for j in range(n) if j != i and (adj[i, j >> 5] >> np.uint32(j & 31)) & 1] for i in range(n)]
+    deg = [len(x) for x in nb]
+    S = [0] * ((max(deg) if n else 0) + 1)
+    maxclq, ops = -1, 0
+    for v in range(n):
+        if maxclq > deg[v]:
+            continue
+        pos = 0
+        S[pos] = v
+        pos += 1
+        for u in nb[v]:
+            if maxclq <= deg[u]:
+                S[pos] = u
+                pos += 1
+        icc = 0
+        while pos > 0:
+            icc += 1
+            m = S[pos - 1]
+            S1 = []
+            for a in range(pos):
+                for e, u in enumerate(nb[m]):
+                    ops += 1
+                    if S[a] == u and maxclq <= deg[u]:
+                        S1.append(S[a])
+                        break
+            for a, x in enumerate(S1):
+                S[a] = x
+            pos = len(S1)
+        if maxclq < icc:
+            maxclq = icc
+    return ops
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_clique_scan_op_count(seed):
+    rng = np.random.default_rng(300 + seed)
+    n = int(rng.integers(2, 60))
+    iu = np.triu_indices(n, 1)
+    m = rng.random(len(iu[0])) < rng.uniform(0.2, 0.9)
+    adj = _bits(n, list(zip(iu[0][m], iu[1][m])))
+    assert O.clique_scan_ops(adj, n) == _scan_ops_python(n, adj)

@@ -54,11 +54,17 @@ def test_noalloc_clique_matches_existing_entry_point_on_consecutive_calls():
     for n, words, seed, planted, first, seed_size in cases:
         adj = torch.from_numpy(_adjacency(n, words, seed, planted).view(np.int32)).to(dev)
         torch.cuda.synchronize()
+        allocs_ref = capi.buffer_alloc_count()
         rc_ref, size_ref, clique_ref = _call(lib.rpgo_max_clique_heu_dev, adj, n, words, first, seed_size, stream)
+        # the counter sees the allocating entry point's buffers
+        assert capi.buffer_alloc_count() > allocs_ref
         launches = capi.kernel_launch_count()
+        allocs = capi.buffer_alloc_count()
         rc, size, clique = _call(lib.rpgo_max_clique_heu_dev_noalloc, adj, n, words, first, seed_size, stream)
         assert rc_ref == capi.OK and rc == capi.OK
         assert capi.kernel_launch_count() > launches
+        # the promise itself: no device or pinned buffer was allocated
+        assert capi.buffer_alloc_count() == allocs
         assert size == size_ref >= planted
         assert np.array_equal(clique, clique_ref)
 
