@@ -106,8 +106,14 @@ enum { RPGO_ALIGN_NONE = 0, RPGO_ALIGN_L2 = 1, RPGO_ALIGN_GNC = 2 };
  *   previous estimate, and the result is accepted only when its weights are
  *   binary and agree with the TLS rule at the final estimate; otherwise the
  *   plain schedule runs from the start (counted in rpgo_timing.warm_fallbacks).
- * RECORD: the plain schedule, recording the closure features (training data). */
-enum { RPGO_WARM_OFF = 0, RPGO_WARM_ON = 1, RPGO_WARM_RECORD = 2 };
+ * RECORD: the plain schedule, recording the closure features (training data).
+ * CONTINUATION: plain GNC's mu continuation and TLS weight rule, with two
+ *   changes: the first solve uses the predicted inlier set (probability >= 0.5;
+ *   all ones without a model or probabilities) instead of all ones, and every
+ *   later LM run starts from the previous estimate instead of the initial
+ *   values. No certificate: the result is plain GNC's only as far as the two
+ *   changes leave its decisions unchanged. */
+enum { RPGO_WARM_OFF = 0, RPGO_WARM_ON = 1, RPGO_WARM_RECORD = 2, RPGO_WARM_CONTINUATION = 3 };
 
 /* A batch of factors (structure of arrays). For priors key_back is ignored. */
 typedef struct rpgo_factor_batch {

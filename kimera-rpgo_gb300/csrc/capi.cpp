@@ -107,7 +107,8 @@ void closure_features_and_probs(rpgo_solver* s, GpuNls& nls, const std::vector<F
   closure_features(nls.dev(), (int)n_known, daux.get(), dfeat.get(), s->st);
   s->features.resize((size_t)nlc * kFeat);
   dfeat.download(s->features.data(), s->features.size(), s->st);
-  if (s->p.gnc_warm_start == RPGO_WARM_ON && s->has_model && s->warm_probs.size() != F) {
+  if ((s->p.gnc_warm_start == RPGO_WARM_ON || s->p.gnc_warm_start == RPGO_WARM_CONTINUATION) && s->has_model &&
+      s->warm_probs.size() != F) {
     DeviceBuffer<float> dprob((size_t)nlc);
     mlp_forward(s->model.get(), nlc, dfeat.get(), dprob.get(), s->st);
     std::vector<float> prob((size_t)nlc);
@@ -300,14 +301,25 @@ int optimize(rpgo_solver* s) {
     }
     GpuNls nls(s->dim, full, *s->store, sv.get(), s->st, s->p.linear_solver != RPGO_LINEAR_PCG);
     nls.dev().coop_ctas = s->coop_ctas;
-    if (s->p.gnc_warm_start == RPGO_WARM_ON || s->p.gnc_warm_start == RPGO_WARM_RECORD)
+    const int wm = s->p.gnc_warm_start;
+    if (wm == RPGO_WARM_ON || wm == RPGO_WARM_RECORD || wm == RPGO_WARM_CONTINUATION)
       closure_features_and_probs(s, nls, full, n_known);
     std::vector<double> w;
     bool warm_done = false;
-    if (s->p.gnc_warm_start == RPGO_WARM_ON && s->warm_probs.size() == full.size()) {
+    if (wm == RPGO_WARM_ON && s->warm_probs.size() == full.size()) {
       s->timing.warm_runs++;
       warm_done = gnc_tls_warm(nls, n_known, g, lp, s->warm_probs, s->p.gnc_warm_mu, &w, &st);
       if (!warm_done) s->timing.warm_fallbacks++;
+    }
+    if (wm == RPGO_WARM_CONTINUATION) {
+      // plain continuation; first weights from the prediction, LM from the
+      // previous estimate
+      std::vector<double> first(full.size(), 1.0);
+      if (s->warm_probs.size() == full.size())
+        for (size_t k = n_known; k < full.size(); ++k) first[k] = s->warm_probs[k] >= 0.5 ? 1.0 : 0.0;
+      s->timing.warm_runs++;
+      gnc_tls(nls, n_known, g, lp, &first, &w, &st, true);
+      warm_done = true;
     }
     s->warm_probs.clear();
     if (!warm_done) gnc_tls(nls, n_known, g, lp, s->p.gnc_bias_odom ? &init : nullptr, &w, &st);

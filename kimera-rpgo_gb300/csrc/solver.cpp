@@ -160,7 +160,8 @@ double chi2inv(double alpha, int k) {
 
 // GncOptimizer::optimize (TLS), restated.
 void gnc_tls(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp,
-             const std::vector<double>* init_weights, std::vector<double>* weights_out, NlsStats* st) {
+             const std::vector<double>* init_weights, std::vector<double>* weights_out, NlsStats* st,
+             bool lm_from_previous) {
   SolverDev& s = nls.dev();
   cudaStream_t stream = nls.stream();
   const size_t F = (size_t)s.F;
@@ -189,7 +190,7 @@ void gnc_tls(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp
   for (int it = 0; it < g.max_iterations; ++it) {
     st->gnc_iterations++;
     solver_gnc_weights(s, s.x.get(), (int)n_known, barc_dev.get(), mu, stream);
-    nls.optimize(lp, st);
+    nls.optimize(lp, st, lm_from_previous);
     const double cost = nls.error_at_result(&weights);
     bool conv = std::fabs(cost - prev_cost) / std::max(prev_cost, 1e-7) < g.rel_cost_tol;
     if (!conv) {

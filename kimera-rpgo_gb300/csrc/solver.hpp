@@ -65,8 +65,11 @@ double chi2inv(double alpha, int dof);
 
 // GncOptimizer<GncParams<LM or GN>> with the TLS loss; known inliers are the
 // first n_known factors. init_weights (optional) as in setWeights.
+// lm_from_previous (no counterpart in the reference): every LM run after the
+// first starts from the previous estimate instead of the initial values.
 void gnc_tls(GpuNls& nls, size_t n_known, const GncConfig& g, const LmParams& lp,
-             const std::vector<double>* init_weights, std::vector<double>* weights_out, NlsStats* st);
+             const std::vector<double>* init_weights, std::vector<double>* weights_out, NlsStats* st,
+             bool lm_from_previous = false);
 
 // Warm-started GNC-TLS (no counterpart in the reference). probs[k]: predicted
 // inlier probability of factor k >= n_known. The predicted inliers

@@ -18,7 +18,7 @@ LINEAR_CHOLESKY, LINEAR_PCG = 0, 1
 # MultiRobotAlignMethod (SolverParams.h:26-31)
 ALIGN_NONE, ALIGN_L2, ALIGN_GNC = 0, 1, 2
 # GNC warm start modes (rpgo_params.gnc_warm_start)
-WARM_OFF, WARM_ON, WARM_RECORD = 0, 1, 2
+WARM_OFF, WARM_ON, WARM_RECORD, WARM_CONTINUATION = 0, 1, 2, 3
 
 
 class RobustSolverParams:
@@ -162,7 +162,9 @@ class RobustSolverParams:
 
     def setGncWarmStart(self, mode=WARM_ON, mu=None):
         """Warm-started GNC schedule (WARM_ON), plain schedule with closure
-        features recorded (WARM_RECORD), or the plain schedule (WARM_OFF)."""
+        features recorded (WARM_RECORD), plain mu continuation with the
+        predicted first inlier set and LM from the previous estimate
+        (WARM_CONTINUATION), or the plain schedule (WARM_OFF)."""
         self.gnc_warm_start = int(mode)
         if mu is not None:
             self.gnc_warm_mu = float(mu)

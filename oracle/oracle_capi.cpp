@@ -258,6 +258,17 @@ struct RobustSolverO final : SolverBase {
         else ++warm_fallbacks;
         warm_probs.clear();
       }
+      if (p.gnc_warm_start == RPGO_WARM_CONTINUATION) {
+        // plain continuation, first weights from the prediction (all ones
+        // without one), every later LM from the previous estimate
+        std::vector<double> first(full.size(), 1.0);
+        if (warm_probs.size() == full.size())
+          for (size_t k = n_known; k < full.size(); ++k) first[k] = warm_probs[k] >= 0.5 ? 1.0 : 0.0;
+        warm_probs.clear();
+        ++warm_runs;
+        r = gnc_tls<S>(full, full_values, n_known, gp, lp, &first, -1, true);
+        warm_done = true;
+      }
       if (!warm_done) {
         SolveStats before = r.stats;
         const int outer_before = r.outer_iterations;
@@ -725,7 +736,8 @@ int oracle_pairwise_adjacency(int dim, int mode, int n, const int32_t* slot_a, c
 }
 
 // 0: the reference's linear-search greedy clique (default), 1: the
-// membership-stamp form with identical results; returns the previous value
+// membership-stamp form, 2: the bit-row form (both with identical results);
+// returns the previous value
 int oracle_set_clique_impl(int impl) {
   const int old = g_clique_impl;
   g_clique_impl = impl;
@@ -742,11 +754,17 @@ int oracle_pcm_rows(void* s, const rpgo_factor_batch* f, const rpgo_value_batch*
   return static_cast<SolverBase*>(s)->pcm_rows(f, v, rows, n_rows, out, cap, n, src, src_cap, lower_only != 0);
 }
 // linear-search iterations of the reference's greedy clique on a bit-packed
-// adjacency (n x ceil(n/32) words)
-double oracle_clique_scan_ops(int n, const uint32_t* adj) {
+// adjacency (n x ceil(n/32) words): counted exactly (exact != 0, O(|S| +
+// deg) per round), or estimated on bit rows (positions of the kept elements
+// in the neighbour list to their 64-bit word; OpenMP)
+double oracle_clique_scan_ops(int n, const uint32_t* adj, int exact) {
   const int words = (n + 31) / 32;
   std::vector<uint32_t> bits(adj, adj + (size_t)n * words);
-  return fmc_scan_ops(csr_from_bits(bits, n, words), 0, -1);
+  if (exact) return fmc_scan_ops(csr_from_bits(bits, n, words), 0, -1);
+  std::vector<int> best;
+  double ops = 0.0;
+  fmc_heuristic_bits(BitRows(bits, n, words), 0, -1, &best, &ops);
+  return ops;
 }
 // iterations cap of every LM / GN run (-1: the solver's own); returns the old
 int oracle_set_lm_max_iterations(int n) {
@@ -764,9 +782,8 @@ int oracle_solve_graph(void* s, const rpgo_factor_batch* f, const rpgo_value_bat
 int oracle_max_clique_heu(int n, const uint32_t* adj, int first, int seed, int32_t* clique_out, int32_t* size_out) {
   const int words = (n + 31) / 32;
   std::vector<uint32_t> bits(adj, adj + (size_t)n * words);
-  Csr g = csr_from_bits(bits, n, words);
   std::vector<int> best;
-  int sz = fmc_heuristic(g, first, seed, &best);
+  int sz = fmc_from_bits(bits, n, words, first, seed, &best);
   *size_out = sz;
   for (int i = 0; i < sz && i < (int)best.size(); ++i) clique_out[i] = best[i];
   return 0;

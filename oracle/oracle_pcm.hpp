@@ -380,12 +380,203 @@ static inline double fmc_scan_ops(const Csr& g, int first, int max_clq) {
   return ops;
 }
 
+// The same heuristic on bit rows, for dense matrices. A candidate's list S is
+// kept as v (always first) followed by a bitset of the other members, whose
+// ascending order is the order of the reference's list: the kept elements
+// keep their order, so "S <- elements of S adjacent to m" is S_bits &= N(m)
+// (v stays: m is a neighbour of v; the degree filter of the round is already
+// in S_bits), and m = S[last] is the highest set bit (v once S_bits is
+// empty). The reference's work buffer is rebuilt for a winning candidate:
+// the initial fill writes positions [0, n_0), round r writes [0, n_r), so
+// position p ends with element p of the last list longer than p.
+// Candidates are evaluated in windows on the OpenMP threads with the running
+// best fixed; the first improving candidate of a window (in order) wins and
+// the scan restarts after it, so every decision is the sequential scan's.
+// ops_out (optional): the reference's linear-search inner iterations,
+// estimated per round: a kept element costs its position in N(m) plus one
+// (counted to its 64-bit word, inside the word at the word's mean), any
+// other element all of N(m).
+struct BitRows {
+  int n = 0, w64 = 0;
+  std::vector<uint64_t> row;  // n x w64
+  std::vector<int> deg;
+  BitRows(const std::vector<uint32_t>& bits, int n_, int words) : n(n_), w64((n_ + 63) / 64) {
+    row.assign((size_t)n * w64, 0ull);
+    deg.assign(n, 0);
+    for (int i = 0; i < n; ++i) {
+      uint64_t* r = &row[(size_t)i * w64];
+      for (int w = 0; w < words && 32 * w < n; ++w) r[w >> 1] |= (uint64_t)bits[(size_t)i * words + w] << (32 * (w & 1));
+      if (n % 64) r[w64 - 1] &= (~0ull) >> (64 - n % 64);
+      r[i >> 6] &= ~(1ull << (i & 63));  // the diagonal is not an edge
+      int d = 0;
+      for (int w = 0; w < w64; ++w) d += __builtin_popcountll(r[w]);
+      deg[i] = d;
+    }
+  }
+  const uint64_t* of(int i) const { return &row[(size_t)i * w64]; }
+};
+
+// Rounds of candidate v with running best max_clq (dmask: vertices of degree
+// >= max_clq); S: w64 words of scratch. n_sizes (optional): list length after
+// each round, [0] the initial fill; keep (optional): each round's member set.
+// Returns the round count icc.
+static inline int fmc_bits_candidate(const BitRows& g, int v, const std::vector<uint64_t>& dmask,
+                                     std::vector<uint64_t>& S, std::vector<int>* n_sizes,
+                                     std::vector<std::vector<uint64_t>>* keep, double* ops) {
+  const int W = g.w64;
+  const uint64_t* nv = g.of(v);
+  int cnt = 0, hi = -1;
+  for (int w = 0; w < W; ++w) {
+    S[w] = nv[w] & dmask[w];
+    if (S[w]) {
+      cnt += __builtin_popcountll(S[w]);
+      hi = w;
+    }
+  }
+  if (n_sizes) n_sizes->assign(1, 1 + cnt);
+  if (keep) keep->assign(1, std::vector<uint64_t>(S.begin(), S.end()));
+  int icc = 0;
+  int npos = 1 + cnt;
+  while (npos > 0) {
+    ++icc;
+    if (cnt == 0) {  // m = v, not adjacent to itself: the list empties
+      if (ops) *ops += (double)g.deg[v];
+      npos = 0;
+      if (n_sizes) n_sizes->push_back(0);
+      break;
+    }
+    const int m = 64 * hi + 63 - __builtin_clzll(S[hi]);
+    const uint64_t* nm = g.of(m);
+    int kept = 0, nh = -1;
+    double rank_sum = 0.0;
+    int prefix = 0;
+    for (int w = 0; w <= hi; ++w) {
+      const int pn = __builtin_popcountll(nm[w]);
+      S[w] &= nm[w];
+      if (S[w]) {
+        const int kw = __builtin_popcountll(S[w]);
+        kept += kw;
+        nh = w;
+        if (ops) rank_sum += (double)kw * ((double)prefix + 0.5 * (double)pn);
+      }
+      prefix += pn;
+    }
+    if (ops) {
+      // the search for a kept element stops at its position in N(m), v's
+      // included; the others (m among them) scan all of N(m)
+      int vrank = 0;
+      for (int w = 0; w < (v >> 6); ++w) vrank += __builtin_popcountll(nm[w]);
+      vrank += __builtin_popcountll(nm[v >> 6] & ((1ull << (v & 63)) - 1ull));
+      *ops += rank_sum + (double)kept + (double)(vrank + 1) + (double)(cnt - kept) * (double)g.deg[m];
+    }
+    cnt = kept;
+    hi = nh;
+    npos = 1 + cnt;
+    if (n_sizes) n_sizes->push_back(npos);
+    if (keep) keep->push_back(std::vector<uint64_t>(S.begin(), S.begin() + W));
+  }
+  return icc;
+}
+
+static inline int fmc_heuristic_bits(const BitRows& g, int first, int max_clq, std::vector<int>* best,
+                                     double* ops_out = nullptr) {
+  const int n = g.n, W = g.w64;
+  std::vector<uint64_t> dmask(W, 0ull);
+  auto build_mask = [&](int m) {
+    std::fill(dmask.begin(), dmask.end(), 0ull);
+    for (int i = 0; i < n; ++i)
+      if (m <= g.deg[i]) dmask[i >> 6] |= 1ull << (i & 63);
+  };
+  build_mask(max_clq);
+  double ops = 0.0;
+  int v = std::max(first, 0);
+  const int window = 64;
+  std::vector<int> res(window);
+  std::vector<double> wops(window);
+  while (v < n) {
+    const int cnt = std::min(window, n - v);
+#pragma omp parallel
+    {
+      std::vector<uint64_t> S(W);
+#pragma omp for schedule(dynamic, 1)
+      for (int k = 0; k < cnt; ++k) {
+        const int c = v + k;
+        wops[k] = 0.0;
+        if (max_clq > g.deg[c]) {
+          res[k] = -1;
+          continue;
+        }
+        res[k] = fmc_bits_candidate(g, c, dmask, S, nullptr, nullptr, ops_out ? &wops[k] : nullptr);
+      }
+    }
+    int improved = -1;
+    for (int k = 0; k < cnt; ++k) {
+      if (ops_out) ops += wops[k];
+      if (res[k] > max_clq) {
+        improved = k;
+        break;
+      }
+    }
+    if (improved < 0) {
+      v += cnt;
+      continue;
+    }
+    const int c = v + improved;
+    // the winner again, keeping its rounds, to rebuild its work buffer;
+    // positions [0, icc) lie inside its own initial fill, so no earlier
+    // candidate's writes survive there
+    std::vector<uint64_t> S(W);
+    std::vector<int> sizes;
+    std::vector<std::vector<uint64_t>> rounds;
+    const int icc = fmc_bits_candidate(g, c, dmask, S, &sizes, &rounds, nullptr);
+    std::vector<int> out((size_t)std::max(icc, 0), 0);
+    // list r (0 = the initial fill) is final on positions [sizes[r + 1], sizes[r])
+    for (size_t r = 0; r + 1 < sizes.size(); ++r) {
+      const int lo = sizes[r + 1], hi2 = std::min(sizes[r], icc);
+      if (lo >= hi2) continue;
+      // element p of list r: p = 0 is c, p >= 1 the p-th member in ascending order
+      int p = 0;
+      if (lo == 0) out[p++] = c;
+      p = std::max(p, lo);
+      int rank = 0;
+      const std::vector<uint64_t>& R = rounds[r];
+      for (int w = 0; w < W && p < hi2; ++w) {
+        uint64_t x = R[w];
+        const int pc = __builtin_popcountll(x);
+        if (rank + pc < p) {
+          rank += pc;
+          continue;
+        }
+        while (x && p < hi2) {
+          const int b = __builtin_ctzll(x);
+          x &= x - 1;
+          ++rank;
+          if (rank >= p) out[p++] = 64 * w + b;
+        }
+      }
+    }
+    *best = out;
+    max_clq = icc;
+    build_mask(max_clq);
+    v = c + 1;
+  }
+  if (ops_out) *ops_out = ops;
+  return max_clq;
+}
+
 // Which form the oracle runs: 0 = the reference's linear search (default),
-// 1 = the membership-stamp form (identical results, for checks at large sizes).
+// 1 = the membership-stamp form, 2 = the bit-row form (identical results;
+// 1 and 2 are for checks at large sizes).
 inline int g_clique_impl = 0;
 static inline int fmc_heuristic(const Csr& g, int first, int max_clq, std::vector<int>* best) {
   return g_clique_impl == 1 ? fmc_heuristic_marked(g, first, max_clq, best)
                             : fmc_heuristic_scan(g, first, max_clq, best);
+}
+// the heuristic of a bit-packed matrix (n x words uint32) in the selected form
+static inline int fmc_from_bits(const std::vector<uint32_t>& bits, int n, int words, int first, int max_clq,
+                                std::vector<int>* best) {
+  if (g_clique_impl == 2) return fmc_heuristic_bits(BitRows(bits, n, words), first, max_clq, best);
+  return fmc_heuristic(csr_from_bits(bits, n, words), first, max_clq, best);
 }
 
 // ---------------------------------------------------------------- factor records
@@ -559,9 +750,8 @@ struct Pcm {
   size_t landmark_inliers(Group<L>& g) {
     g.consistent.clear();
     if (g.n < g.adj_rows) g.grow(g.adj_rows);
-    Csr csr = csr_from_bits(g.bits, g.adj_rows, g.words);
     std::vector<int> idx;
-    const int sz = fmc_heuristic(csr, 0, -1, &idx);
+    const int sz = fmc_from_bits(g.bits, g.adj_rows, g.words, 0, -1, &idx);
     for (int i = 0; i < sz; ++i)
       if (idx[i] < (int)g.factors.size()) g.consistent.push_back(g.factors[idx[i]]);
     return g.consistent.size();
@@ -631,9 +821,8 @@ struct Pcm {
       size_t num;
       if (lc_check) {
         g.consistent.clear();
-        Csr csr = csr_from_bits(g.bits, g.n, g.words);
         std::vector<int> idx;
-        const int sz = fmc_heuristic(csr, 0, -1, &idx);
+        const int sz = fmc_from_bits(g.bits, g.n, g.words, 0, -1, &idx);
         // indices past the closures (an adjacency kept larger by a removal)
         // are dropped; the reference would index past its factor list
         for (int i = 0; i < sz; ++i)
@@ -652,10 +841,9 @@ struct Pcm {
     for (const auto& kv : num_new) {
       Group<L>& g = loop_closures[kv.first];
       const size_t prev = g.consistent.size();
-      Csr csr = csr_from_bits(g.bits, g.n, g.words);
       std::vector<int> idx;
-      const int first = (int)csr.off.size() - (int)kv.second - 1;
-      int num = fmc_heuristic(csr, first, (int)prev, &idx);
+      const int first = g.n - (int)kv.second;
+      int num = fmc_from_bits(g.bits, g.n, g.words, first, (int)prev, &idx);
       if ((size_t)num > prev) {
         g.consistent.clear();
         for (int i = 0; i < num; ++i)
@@ -697,9 +885,8 @@ struct Pcm {
       g.consistent.clear();
       if (lc_check && g.n >= m) {
         g.shrink(m);
-        Csr csr = csr_from_bits(g.bits, g.n, g.words);
         std::vector<int> idx;
-        const int sz = fmc_heuristic(csr, 0, -1, &idx);
+        const int sz = fmc_from_bits(g.bits, g.n, g.words, 0, -1, &idx);
         for (int i = 0; i < sz; ++i)
           if (idx[i] < (int)g.factors.size()) g.consistent.push_back(g.factors[idx[i]]);
       } else if (m > 0) {

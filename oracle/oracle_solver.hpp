@@ -823,7 +823,8 @@ struct GncResult {
 template <class S>
 GncResult<S> gnc_tls(const std::vector<Factor<typename S::L>>& graph, const std::map<uint64_t, typename S::Pose>& init,
                      size_t n_known, const GncParamsO& gp, const LmParamsO& lp,
-                     const std::vector<double>* init_weights = nullptr, int max_outer_override = -1) {
+                     const std::vector<double>* init_weights = nullptr, int max_outer_override = -1,
+                     bool lm_from_previous = false) {
   GncResult<S> out;
   const size_t nf = graph.size();
   std::vector<double> barc(nf, 1.0);
@@ -871,7 +872,7 @@ GncResult<S> gnc_tls(const std::vector<Factor<typename S::L>>& graph, const std:
       else if (u2 <= lb || wk > 1.0) wk = 1.0;
       weights[k] = wk;
     }
-    result = nls.optimize(init, lp, &out.stats);
+    result = nls.optimize(lm_from_previous ? result : init, lp, &out.stats);
     const double cost = nls.error(result);
     bool conv = std::fabs(cost - prev_cost) / std::max(prev_cost, 1e-7) < gp.rel_cost_tol;
     if (!conv) {

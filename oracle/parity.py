@@ -47,7 +47,7 @@ def check(graph, params, gpu, rows=256, seed=0, solve=True, threads=0, keep=Fals
     seeded whole rows to evaluate (single-group graphs). Returns a dict of
     booleans, errors and the oracle's wall time per stage (with keep, also
     the oracle solver of the solve stage under "_oracle")."""
-    before_impl = O.set_clique_impl(1)
+    before_impl = O.set_clique_impl(2)
     before_thr = O.set_threads(0)
     if threads:
         O.set_threads(threads)

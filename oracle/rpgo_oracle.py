@@ -105,7 +105,7 @@ def lib():
                                          C.c_int32, C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.c_void_p,
                                          C.c_int64, C.c_int]
         _lib.oracle_clique_scan_ops.restype = C.c_double
-        _lib.oracle_clique_scan_ops.argtypes = [C.c_int, C.c_void_p]
+        _lib.oracle_clique_scan_ops.argtypes = [C.c_int, C.c_void_p, C.c_int]
         _lib.oracle_set_lm_max_iterations.argtypes = [C.c_int]
         _lib.oracle_solve_graph.argtypes = [C.c_void_p, C.POINTER(FactorBatch), C.POINTER(ValueBatch), C.c_int64]
     return _lib
@@ -300,8 +300,9 @@ class OracleSolver:
 
 def set_clique_impl(impl: int) -> int:
     """0: the reference's linear-search greedy clique (default); 1: the
-    membership-stamp form with identical results (for large checks).
-    Returns the previous setting."""
+    membership-stamp form; 2: the bit-row form on the OpenMP threads (both
+    with identical results, for large checks). Returns the previous
+    setting."""
     return lib().oracle_set_clique_impl(int(impl))
 
 
@@ -332,11 +333,13 @@ def filtered_graph(graph, kind, key1, key2):
     return g
 
 
-def clique_scan_ops(adj_words: np.ndarray, n: int) -> float:
+def clique_scan_ops(adj_words: np.ndarray, n: int, exact: bool = True) -> float:
     """Inner-loop iterations of the reference's linear-search greedy clique
-    on this adjacency (counted, not run)."""
+    on this adjacency, not run: counted exactly (O(|S| + deg) per round), or
+    with exact=False estimated on bit rows (each kept element's position in
+    the neighbour list to its 64-bit word; for large dense matrices)."""
     adj = np.ascontiguousarray(adj_words, dtype=np.uint32)
-    return lib().oracle_clique_scan_ops(int(n), _ptr(adj))
+    return lib().oracle_clique_scan_ops(int(n), _ptr(adj), int(bool(exact)))
 
 
 def set_lm_max_iterations(n: int) -> int:

@@ -273,13 +273,14 @@ def test_clique_stamp_form_matches_linear_scan(seed):
     try:
         ref = O.max_clique_heu(adj, n)
         ref2 = O.max_clique_heu(adj, n, n // 3, max(1, ref[0] // 2))
-        O.set_clique_impl(1)
-        got = O.max_clique_heu(adj, n)
-        got2 = O.max_clique_heu(adj, n, n // 3, max(1, ref[0] // 2))
+        for impl in (1, 2):
+            O.set_clique_impl(impl)
+            got = O.max_clique_heu(adj, n)
+            got2 = O.max_clique_heu(adj, n, n // 3, max(1, ref[0] // 2))
+            assert ref[0] == got[0] and np.array_equal(ref[1], got[1]), impl
+            assert ref2[0] == got2[0] and np.array_equal(ref2[1], got2[1]), impl
     finally:
         O.set_clique_impl(before)
-    assert ref[0] == got[0] and np.array_equal(ref[1], got[1])
-    assert ref2[0] == got2[0] and np.array_equal(ref2[1], got2[1])
 
 
 def _oracle_run(p, graph, impl):
@@ -302,11 +303,13 @@ def test_oracle_stamp_clique_same_pcm_result():
              (synth.walk3d(800, 200, 60, seed=19).graph,
               RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9))]
     for graph, p in cases:
-        a, b = _oracle_run(p, graph, 0), _oracle_run(p, graph, 1)
-        for x, y in zip(a.factors()[:3], b.factors()[:3]):
-            assert np.array_equal(x, y)
-        assert np.array_equal(a.estimate()[1], b.estimate()[1])
-        assert np.array_equal(a.gnc_weights(), b.gnc_weights())
+        a = _oracle_run(p, graph, 0)
+        for impl in (1, 2):
+            b = _oracle_run(p, graph, impl)
+            for x, y in zip(a.factors()[:3], b.factors()[:3]):
+                assert np.array_equal(x, y)
+            assert np.array_equal(a.estimate()[1], b.estimate()[1])
+            assert np.array_equal(a.gnc_weights(), b.gnc_weights())
 
 
 def test_pcm_rows_equal_full_matrix_rows():
@@ -412,3 +415,37 @@ def test_clique_scan_op_count(seed):
     m = rng.random(len(iu[0])) < rng.uniform(0.2, 0.9)
     adj = _bits(n, list(zip(iu[0][m], iu[1][m])))
     assert O.clique_scan_ops(adj, n) == _scan_ops_python(n, adj)
+
+
+def test_clique_bit_rows_on_dense_planted_graphs():
+    # dense graphs (the regime of the 50,000-pose benchmark matrix): the
+    # bit-row form equals the linear search, size and index list
+    rng = np.random.default_rng(43)
+    for n, p in ((400, 0.8), (700, 0.95)):
+        dense = np.triu(rng.random((n, n)) < p, 1)
+        members = rng.choice(n, n // 2, replace=False)
+        dense[np.ix_(members, members)] = True
+        iu = np.nonzero(np.triu(dense, 1))
+        adj = _bits(n, list(zip(iu[0], iu[1])))
+        before = O.set_clique_impl(0)
+        try:
+            ref = O.max_clique_heu(adj, n)
+            O.set_clique_impl(2)
+            got = O.max_clique_heu(adj, n)
+        finally:
+            O.set_clique_impl(before)
+        assert ref[0] == got[0] and np.array_equal(ref[1], got[1])
+
+
+def test_clique_scan_op_estimate_near_count():
+    # the bit-row estimate (positions in N(m) to the 64-bit word) against
+    # the exact count on dense random graphs with a planted clique
+    rng = np.random.default_rng(41)
+    for n, p in ((300, 0.6), (500, 0.9)):
+        dense = np.triu(rng.random((n, n)) < p, 1)
+        members = rng.choice(n, n // 3, replace=False)
+        dense[np.ix_(members, members)] = True
+        iu = np.nonzero(np.triu(dense, 1))
+        adj = _bits(n, list(zip(iu[0], iu[1])))
+        exact, est = O.clique_scan_ops(adj, n), O.clique_scan_ops(adj, n, exact=False)
+        assert abs(est - exact) <= 0.02 * exact, (n, exact, est)

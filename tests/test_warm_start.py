@@ -117,6 +117,65 @@ def _empty():
     return Graph(3)
 
 
+# ------------------------------------------------------------------ continuation-preserving schedule
+def _cont_params(pcm_off=True):
+    from rpgo_gb300.params import WARM_CONTINUATION
+
+    p = _params(pcm_off=pcm_off)
+    p.setGncWarmStart(WARM_CONTINUATION)
+    return p
+
+
+def _cont_oracle(s, probs, pcm_off=True):
+    o = O.OracleSolver(_cont_params(pcm_off))
+    assert o.update(s.graph, optimize_graph=False) == 0
+    if probs is not None:
+        o.set_warm_probs(probs)
+    assert o.force_optimize() == 0
+    return o
+
+
+def test_oracle_continuation_schedule_keeps_mu_path():
+    # same mu continuation and weight rule as plain GNC: with all closures
+    # predicted inliers the first solve is plain GNC's, and fewer damped
+    # solves follow (LM from the previous estimate)
+    s = _graph()
+    plain, nk = _plain_oracle(s)
+    ones = np.ones(plain.counts().num_factors)
+    cont = _cont_oracle(s, ones)
+    sp, sc = plain.stats(), cont.stats()
+    assert sc["warm_runs"] == 1 and sc["gnc_iterations"] >= 1
+    assert sc["linear_solves"] < sp["linear_solves"]
+    # probabilities of the wrong size are ignored (first weights all ones)
+    again = _cont_oracle(s, np.ones(3))
+    assert np.array_equal(again.gnc_weights(), cont.gnc_weights())
+    # a predicted outlier set changes the first solve
+    zeros = ones.copy()
+    zeros[nk:] = 0.0
+    other = _cont_oracle(s, zeros)
+    assert other.stats()["linear_solves"] != sc["linear_solves"]
+
+
+@pytest.mark.gpu
+def test_gpu_continuation_schedule_matches_oracle():
+    from rpgo_gb300 import build, capi
+
+    build()
+    s = _graph()
+    plain, nk = _plain_oracle(s)
+    w = plain.gnc_weights()
+    for probs in (w, np.ones_like(w)):
+        g = capi.RobustSolver(_cont_params())
+        assert g.update(s.graph, optimize_graph=False) == 0
+        assert g.set_warm_start_probs(probs) == 0
+        assert g.forceUpdate(_empty()) == 0
+        o = _cont_oracle(s, probs)
+        t, so = g.timing(), o.stats()
+        assert t.warm_runs == 1 and t.gnc_iterations == so["gnc_iterations"]
+        assert np.array_equal(np.round(g.gnc_weights()), np.round(o.gnc_weights()))
+        assert synth.ate(g.estimate()[1], o.estimate()[1], 3) <= ATE_TOL
+
+
 # ------------------------------------------------------------------ the trained network
 @pytest.mark.gpu
 @pytest.mark.parametrize("pcm_off", [False, True])
