@@ -402,6 +402,200 @@ __global__ void __launch_bounds__(32) k_traj_scan(int64_t count, const int32_t* 
   }
 }
 
+// The 3D PoseWithCovariance walk on two warps (64 threads), one output
+// element per thread. Every element of compose (GeometryUtils.h:119-129) is
+// an FMA chain over at most six products, evaluated exactly as p3_M_elem,
+// p3_C_elem and p3_compose_elem do (a chain that starts with a product
+// starts from fma(a0, b0, -0), which equals mul(a0, b0) bit for bit, so the
+// threads run one branch-free chain): warp 0 takes the three-term chains
+// (rows 0-2 of M = Ad(Delta^-1) S, the new pose, the C entries of columns
+// 0-2), warp 1 the six-term chains (rows 3-5 of M, the C entries of columns
+// 3-5), so both warps issue their FP64 chains on their own sub-partitions.
+// Step constants are double-buffered in shared memory: the next step's are
+// loaded while this one computes. Two block barriers per step.
+__global__ void __launch_bounds__(64) k_traj_scan_pwc3(int64_t count, const int32_t* __restrict__ src,
+                                                       const int32_t* __restrict__ dst,
+                                                       const double* __restrict__ dpose,
+                                                       const double* __restrict__ inv_rec,
+                                                       const double* __restrict__ dcov_p,
+                                                       const uint8_t* __restrict__ drot, TrajView tr) {
+  constexpr int st = 12, dd = 36, REC = 21, NC = st + REC + dd;  // 69 step constants
+  __shared__ double prev_pose[12], prev_cov[36], M[36];
+  __shared__ double cst[2][72];  // [0,12) Delta pose, [12,33) Ad(Delta^-1) pieces (R, K, t), [33,69) Sigma_Delta
+  __shared__ uint8_t prev_rot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // ---- this thread's chains (fixed for the whole walk)
+  // phase 1 kind: 0 none, 1 M row < 3, 2 pose R entry, 3 pose t entry, 4 M row >= 3
+  int p1 = 0, mi = 0, mk = 0, pe = 0;
+  if (warp == 0) {
+    if (lane < 18) {
+      p1 = 1;
+      mi = lane / 6;
+      mk = lane % 6;
+    } else if (lane < 27) {
+      p1 = 2;
+      pe = lane - 18;
+    } else if (lane < 30) {
+      p1 = 3;
+      pe = 9 + (lane - 27);
+    }
+  } else if (lane < 18) {
+    p1 = 4;
+    mi = 3 + lane / 6;
+    mk = lane % 6;
+  }
+  // phase 2: lower-triangle entry (ci, cj) of M Ad^T
+  int p2 = 0, ci = 0, cj = 0;
+  if (warp == 0 && lane < 15) {  // columns 0-2: rows cj..5 of each column
+    int idx = lane;
+    cj = 0;
+    while (idx >= 6 - cj) {
+      idx -= 6 - cj;
+      ++cj;
+    }
+    ci = cj + idx;
+    p2 = 1;
+  } else if (warp == 1 && lane < 6) {  // columns 3-5, rows >= column
+    const int tab_i[6] = {3, 4, 5, 4, 5, 5}, tab_j[6] = {3, 3, 3, 4, 4, 5};
+    ci = tab_i[lane];
+    cj = tab_j[lane];
+    p2 = 2;
+  }
+  double pre[2];
+  int32_t ps = 0, pt = 0;
+  uint8_t prot = 0;
+  auto load_step = [&](int64_t k) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int e = tid + 64 * q;
+      if (e < st) pre[q] = dpose[k * st + e];
+      else if (e < st + REC) pre[q] = inv_rec[k * REC + (e - st)];
+      else if (e < NC) pre[q] = dcov_p[k * dd + (e - st - REC)];
+    }
+    ps = src[k];
+    pt = dst[k];
+    prot = drot[k];
+  };
+  auto store_step = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int e = tid + 64 * q;
+      if (e < NC) cst[buf][e] = pre[q];
+    }
+  };
+  int32_t last_dst = -1;
+  if (count > 0) {
+    load_step(0);
+    store_step(0);
+  }
+  __syncthreads();
+  int32_t s = ps, t = pt;
+  uint8_t rot_k = prot;
+  for (int64_t k = 0; k < count; ++k) {
+    const int b = (int)(k & 1);
+    const double* dpz = cst[b];
+    const double* R = cst[b] + 12;
+    const double* K = cst[b] + 21;
+    const double* dc = cst[b] + 33;
+    if (k + 1 < count) load_step(k + 1);
+    if (s != last_dst) {  // the chain continues from an older pose: read it back
+      for (int e = tid; e < st; e += 64) prev_pose[e] = tr.pose[(size_t)s * st + e];
+      for (int e = tid; e < dd; e += 64) prev_cov[e] = tr.cov[(size_t)s * dd + e];
+      if (tid == 0) prev_rot = tr.rot[s];
+      __syncthreads();
+    }
+    // ---- phase 1
+    double newp = 0.0;
+    if (p1 != 0) {
+      double a[6], x[6], c0 = -0.0;
+      int nt = 3;
+      if (p1 == 1) {
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          a[q] = R[3 * mi + q];
+          x[q] = prev_cov[6 * q + mk];
+        }
+      } else if (p1 == 4) {
+        const int r = mi - 3;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          a[q] = K[3 * r + q];
+          x[q] = prev_cov[6 * q + mk];
+          a[3 + q] = R[3 * r + q];
+          x[3 + q] = prev_cov[18 + 6 * q + mk];
+        }
+        nt = 6;
+      } else if (p1 == 2) {
+        const int i = pe / 3, j = pe % 3;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          a[q] = prev_pose[3 * i + q];
+          x[q] = dpz[3 * q + j];
+        }
+      } else {
+        const int i = pe - 9;
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+          a[q] = prev_pose[3 * i + q];
+          x[q] = dpz[9 + q];
+        }
+        c0 = prev_pose[9 + i];
+      }
+      double acc = fmad(a[0], x[0], c0);
+      acc = fmad(a[1], x[1], acc);
+      acc = fmad(a[2], x[2], acc);
+      if (nt == 6) {
+        acc = fmad(a[3], x[3], acc);
+        acc = fmad(a[4], x[4], acc);
+        acc = fmad(a[5], x[5], acc);
+      }
+      if (p1 == 1 || p1 == 4) M[6 * mi + mk] = acc;
+      else newp = acc;
+    }
+    __syncthreads();
+    // ---- phase 2: C = M Ad^T + Sigma_Delta (lower triangle, mirrored), the new pose
+    if (p2 != 0) {
+      const double* m = M + 6 * ci;
+      double acc;
+      if (p2 == 1) {
+        acc = fmad(m[0], R[3 * cj], -0.0);
+        acc = fmad(m[1], R[3 * cj + 1], acc);
+        acc = fmad(m[2], R[3 * cj + 2], acc);
+      } else {
+        const double* kk = K + 3 * (cj - 3);
+        const double* rr = R + 3 * (cj - 3);
+        acc = fmad(m[0], kk[0], -0.0);
+        acc = fmad(m[1], kk[1], acc);
+        acc = fmad(m[2], kk[2], acc);
+        acc = fmad(m[3], rr[0], acc);
+        acc = fmad(m[4], rr[1], acc);
+        acc = fmad(m[5], rr[2], acc);
+      }
+      const double v = add(acc, dc[6 * ci + cj]);
+      prev_cov[6 * ci + cj] = v;
+      prev_cov[6 * cj + ci] = v;
+      tr.cov[(size_t)t * dd + 6 * ci + cj] = v;
+      if (ci != cj) tr.cov[(size_t)t * dd + 6 * cj + ci] = v;
+    }
+    if (p1 == 2 || p1 == 3) {
+      prev_pose[pe] = newp;
+      tr.pose[(size_t)t * st + pe] = newp;
+    }
+    if (tid == 0) {
+      prev_rot = (prev_rot && rot_k) ? 1 : 0;
+      tr.rot[t] = prev_rot;
+    }
+    last_dst = t;
+    if (k + 1 < count) {
+      store_step(b ^ 1);
+      s = ps;
+      t = pt;
+      rot_k = prot;
+    }
+    __syncthreads();
+  }
+}
+
 // ------------------------------------------------------------------ K1
 template <int DIM, class U>
 __global__ void k_odom_check(int64_t count, const int32_t* __restrict__ si, const int32_t* __restrict__ sj,
@@ -578,8 +772,8 @@ void launch_traj_scan(int dim, int mode, int64_t count, const int32_t* src, cons
                                                         scratch_rot.get());
   RPGO_LAUNCHED();
   if (dim == 3) {
-    if (mode == 0) k_traj_scan<3, 0><<<1, 32, 0, st>>>(count, src, dst, dpose, scratch_rec.get(), scratch_cov.get(),
-                                                       scratch_rot.get(), tr);
+    if (mode == 0) k_traj_scan_pwc3<<<1, 64, 0, st>>>(count, src, dst, dpose, scratch_rec.get(), scratch_cov.get(),
+                                                     scratch_rot.get(), tr);
     else k_traj_scan<3, 1><<<1, 32, 0, st>>>(count, src, dst, dpose, scratch_rec.get(), scratch_cov.get(),
                                              scratch_rot.get(), tr);
   } else {
