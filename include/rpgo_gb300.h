@@ -450,6 +450,16 @@ int rpgo_pairwise_adjacency(int32_t dim, int32_t mode, int32_t n, const int32_t*
 int rpgo_max_clique_heu(int32_t n, const uint32_t* adj, int32_t first, int32_t seed, int32_t* clique_out,
                         int32_t* size_out);
 
+/* Fill-in guard of the direct solve (no counterpart in the reference, whose
+ * GTSAM solve always factors): when the symbolic plan of a graph predicts
+ * more than `flops` factorisation flops (default 1e10, about 30 ms per damped
+ * system), the first damped system of each solve is solved by both the
+ * direct sparse Cholesky and the whole-GPU PCG path, the direct result is
+ * kept, and the later systems use the faster path (prefer 0), or always the
+ * direct one (1), or always PCG (2). Both reach a relative residual of 1e-12.
+ * Process-wide; returns the previous threshold. */
+double rpgo_set_direct_solve_guard(double flops, int32_t prefer);
+
 /* Library / device information (name of the loaded device, SM count). */
 int rpgo_device_info(char* name, int32_t name_capacity, int32_t* sm_count);
 /* Number of CUDA kernels this library has launched in this process. */

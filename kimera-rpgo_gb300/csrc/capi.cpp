@@ -1150,6 +1150,9 @@ int rpgo_device_info(char* name, int32_t cap, int32_t* sm_count) {
 }
 
 int64_t rpgo_kernel_launch_count(void) { return launch_counter().load(); }
+double rpgo_set_direct_solve_guard(double flops, int32_t prefer) {
+  return set_direct_solve_guard(flops, prefer < 0 || prefer > 2 ? 0 : prefer);
+}
 int64_t rpgo_buffer_alloc_count(void) { return alloc_counter().load(); }
 
 }  // extern "C"

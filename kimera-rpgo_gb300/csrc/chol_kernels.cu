@@ -46,6 +46,9 @@ namespace {
 
 constexpr int kTB = 24;  // dense tail tile (scalars); a multiple of both block sizes
 constexpr int kThreads = 256;
+// a level's tasks (columns) run one per lane group instead of one per warp
+// when there are at least this many per warp of the grid
+constexpr int kGroupModeItems = 2;
 
 struct CholArgs {
   int N, ns, T, ntp, n_tiles, levels;
@@ -382,6 +385,121 @@ __device__ void column_team(const CholArgs& a, int j, int tw, int lane, int bar,
       }
     }
   }
+}
+
+// phase A on wide levels: every lane group runs a task of its own (the
+// groups of a warp take consecutive tasks), so one warp instruction serves
+// up to G tasks. The operations and their order are run_task's: a block
+// task's first pair continues the chain that starts at its Hessian block
+// (kind 1) or zero, every further pair starts from zero and is added after
+// its chain, in pair order (a task has at most G pairs, as the warp form
+// gives each group one); a row task sums its entries in G interleaved
+// chains (entry u in chain (u - first) mod G) added in chain order.
+template <int D>
+__device__ void run_task_group(const CholArgs& a, int t, bool valid, int r) {
+  constexpr int G = 32 / D, dd = D * D;
+  constexpr int NC = D == 6 ? 3 : D;
+  const int4 tk = reinterpret_cast<const int4*>(a.tasks)[t];
+  const int kind = tk.w & 3, slot = tk.w >> 4;
+  if (kind < 2) {
+    const int p = tk.x, c0 = ((tk.w >> 2) & 1) * NC;
+    double tot[NC];
+    if (kind == 1) {
+      const bool diag = (tk.w >> 3) & 1;
+#pragma unroll
+      for (int c = 0; c < NC; ++c) tot[c] = block_H<D>(a, p, diag, r, c0 + c);
+    } else {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) tot[c] = 0.0;
+    }
+    for (int u = tk.y; u < tk.z; ++u) {
+      const int pa = a.upd_src[2 * u], pb = a.upd_src[2 * u + 1];
+      const double* A = a.L + (size_t)pa * dd + r * D;
+      const double* B = a.L + (size_t)pb * dd + c0 * D;
+      double ar[D];
+#pragma unroll
+      for (int k = 0; k < D; ++k) ar[k] = A[k];
+      if (u == tk.y) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c)
+#pragma unroll
+          for (int k = 0; k < D; ++k) tot[c] = fma(-ar[k], B[c * D + k], tot[c]);
+      } else {
+        double acc[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+          acc[c] = 0.0;
+#pragma unroll
+          for (int k = 0; k < D; ++k) acc[c] = fma(-ar[k], B[c * D + k], acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < NC; ++c) tot[c] += acc[c];
+      }
+    }
+    if (valid) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) a.Spart[(size_t)slot * dd + r * D + c0 + c] = tot[c];
+    }
+  } else {
+    double tot = 0.0;
+    const int n = tk.z - tk.y, ng = min(G, max(1, n));
+    for (int g = 0; g < ng; ++g) {
+      double acc = 0.0;
+      for (int u = tk.y + g; u < tk.z; u += G) {
+        const double* Lq = a.L + (size_t)a.row_blk[2 * u] * dd + r * D;
+        const double* yk = a.y + (size_t)a.row_blk[2 * u + 1] * D;
+#pragma unroll
+        for (int k = 0; k < D; ++k) acc = fma(Lq[k], yk[k], acc);
+      }
+      tot = g == 0 ? acc : tot + acc;
+    }
+    if (valid) a.Spart[(size_t)slot * dd + r * D] = tot;
+  }
+}
+
+// phase B on wide levels: every lane group finalises a column of its own
+// (the groups of a warp take consecutive columns of the level): the
+// operations and their order are column_warp's. Groups without a column
+// (past the level's end, and the spare lanes of a warp) mirror the warp's
+// first column and store nothing, so every lane takes part in the shuffles.
+template <int D>
+__device__ void column_group(const CholArgs& a, int c0, int nc, int w0, int lane) {
+  constexpr int G = 32 / D, dd = D * D;
+  const int g = lane / D, r = lane % D;
+  const int w = w0 + (g < G ? g : 0);
+  const bool mine = g < G && w < nc;
+  const int base = (g < G ? g : 0) * D;
+  const int j = a.lvl_cols[c0 + (mine ? w : w0)];
+  const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
+  // S_jj row r: every entry summed from 0 over the task slots in order, or
+  // the Hessian block plus lambda D when the block has no task
+  double C[D];
+  {
+    const int t0 = a.btask[2 * p0], t1 = t0 + a.btask[2 * p0 + 1];
+#pragma unroll
+    for (int c = 0; c < D; ++c) C[c] = (t1 == t0) ? block_H<D>(a, p0, true, r, c) : 0.0;
+    for (int t = t0; t < t1; ++t) {
+      const double* P = a.Spart + (size_t)t * dd + r * D;
+#pragma unroll
+      for (int c = 0; c < D; ++c) C[c] += P[c];
+    }
+  }
+  factor_diag<D>(a, lane, mine, r, base, C);
+  double Lf[dd];
+#pragma unroll
+  for (int q = 0; q < D; ++q)
+#pragma unroll
+    for (int c = 0; c <= q; ++c) Lf[q * D + c] = __shfl_sync(kFull, C[c], base + q);
+  if (mine) {
+#pragma unroll
+    for (int c = 0; c < D; ++c) a.Ldiag[(size_t)j * dd + r * D + c] = (c <= r) ? C[c] : 0.0;
+    for (int p = p0 + 1; p < p1; ++p) {
+      double sv[D];
+      sum_partials<D>(a, p, r, sv);
+      solve_offdiag<D>(a, p, r, Lf, sv);
+    }
+  }
+  forward_solve<D>(a, j, mine, r, base, C, forward_rhs<D>(a, j, r));
 }
 
 // backward substitution of column j by one warp:
@@ -787,11 +905,26 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   for (int l = 0; l < a.levels; ++l) {
     const int t0 = a.lvl_task_ptr[l], t1 = a.lvl_task_ptr[l + 1];
     if (t1 > t0) {  // (the leaves' level has none: no updates, no row sums)
-      for (int t = t0 + gw; t < t1; t += nw) run_task<D>(a, t, lane);
+      if (t1 - t0 >= kGroupModeItems * nw) {
+        // wide: a task per lane group
+        constexpr int G = 32 / D;
+        const int g = lane / D;
+        for (int w = gw * G; w < t1 - t0; w += nw * G) {
+          const int t = w + (g < G ? g : 0);
+          const bool valid = g < G && t < t1 - t0;
+          run_task_group<D>(a, t0 + (valid ? t : w), valid, lane % D);
+        }
+      } else {
+        for (int t = t0 + gw; t < t1; t += nw) run_task<D>(a, t, lane);
+      }
       grid.sync();
     }
     const int c0 = a.lvl_col_ptr[l], nc = a.lvl_col_ptr[l + 1] - c0;
-    if (nc <= 2 * (int)gridDim.x) {
+    if (nc >= kGroupModeItems * nw) {
+      // wide: a column per lane group
+      constexpr int G = 32 / D;
+      for (int w = gw * G; w < nc; w += nw * G) column_group<D>(a, c0, nc, w, lane);
+    } else if (nc <= 2 * (int)gridDim.x) {
       // narrow level: at most two columns per CTA, each by a team of two
       // warps (warps 1-2 and 3-4, on four different SM sub-partitions)
       const int wi = threadIdx.x >> 5;
@@ -996,6 +1129,25 @@ void chol_block_hessian(SolverDev& s, CholDev& c, cudaStream_t st) {
   RPGO_LAUNCHED();
 }
 
+// CTAs of the cooperative solve: every co-resident CTA (two per SM at 256
+// threads x 128 registers: twice the warps per SM to hide the latency of the
+// wide levels' loads), or the caller's budget
+static int chol_grid(const SolverDev& s) {
+  static const int per_sm[2] = {
+      [] {
+        int n = 0;
+        RPGO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_chol_solve<3>, kThreads, 0));
+        return std::max(1, n);
+      }(),
+      [] {
+        int n = 0;
+        RPGO_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_chol_solve<6>, kThreads, 0));
+        return std::max(1, n);
+      }()};
+  const int most = device_sm_count() * per_sm[s.dim == 3 ? 1 : 0];
+  return s.coop_ctas > 0 ? std::min(s.coop_ctas, most) : most;
+}
+
 void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, double* host) {
   if (s.N == 0) {
     host[0] = 0.0;
@@ -1006,8 +1158,7 @@ void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, doub
     RPGO_CUDA(cudaEventCreate(&c.ev[0]));
     RPGO_CUDA(cudaEventCreate(&c.ev[1]));
   }
-  const int sms = device_sm_count();
-  const int grid = s.coop_ctas > 0 ? std::min(s.coop_ctas, sms) : sms;
+  const int grid = chol_grid(s);
   c.part.resize((size_t)2 * grid);
   const CholPlan& p = c.plan;
   CholArgs a{s.N, p.n_sparse, p.T, p.n_tiles * kTB, p.n_tiles, c.levels,
@@ -1055,8 +1206,7 @@ SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st) {
     o.ok = 1;
     return o;
   }
-  const int sms = device_sm_count();
-  const int grid = s.coop_ctas > 0 ? std::min(s.coop_ctas, sms) : sms;
+  const int grid = chol_grid(s);
   c.part.resize((size_t)2 * grid);
   const CholPlan& p = c.plan;
   CholArgs a{s.N, p.n_sparse, p.T, p.n_tiles * kTB, p.n_tiles, c.levels,

@@ -23,6 +23,9 @@
 // improves and restarts the window after it (later results used a stale
 // threshold). A candidate that can no longer beat the threshold
 // (rounds + |B| + 1 <= best) stops early: it could not change the result.
+// Each round waits on one adjacency row (that of m); the row of B's
+// second-highest element, the next round's m whenever it is adjacent to m
+// (most rounds on dense matrices), is fetched one round ahead.
 #include <mutex>
 
 #include "../../include/rpgo_gb300.h"
@@ -56,6 +59,8 @@ __device__ __forceinline__ int warp_max(int v) {
   for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
+
+constexpr int kRowRegs = 24;  // register words per lane of a prefetched adjacency row (n <= 24,576)
 
 // One warp per candidate of the window [v0, v0 + count).
 // result[s]: -1 pruned (deg < best), -2 cannot beat best, else icc.
@@ -92,6 +97,11 @@ __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int wor
   top = warp_max(top);
   if (lane == 0) buf[0] = v;
   int r = 0;
+  // rows of at most 32 * kRowRegs words are held in registers: the row of
+  // this round's m and the prefetched row of the likely next one
+  const bool regs = words <= 32 * kRowRegs;
+  uint32_t row[kRowRegs], pf[kRowRegs];
+  int pf_m = -1;
   __syncwarp();
   while (true) {
     if (nr == 0) {
@@ -126,12 +136,60 @@ __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int wor
     }
     // B' = B & N(m) over words [0, top]
     int c2 = 0, top2 = -1;
-    for (int w = lane; w <= top; w += 32) {
-      uint32_t x = cur[w] & adj[(size_t)m * words + w];
-      if (w == (m >> 5)) x &= ~(1u << (m & 31));  // m is never its own neighbour: every round shrinks B
-      nxt[w] = x;
-      c2 += __popc(x);
-      if (x) top2 = w;
+    if (regs) {
+      // row of m from the registers when the previous round fetched it
+      if (pf_m != m) {
+#pragma unroll
+        for (int q = 0; q < kRowRegs; ++q) {
+          const int w = lane + 32 * q;
+          row[q] = (w <= top) ? adj[(size_t)m * words + w] : 0u;
+        }
+      } else {
+#pragma unroll
+        for (int q = 0; q < kRowRegs; ++q) row[q] = pf[q];
+      }
+      // fetch the row of B's second-highest element, the next m whenever it
+      // is a neighbour of m (its words up to the current top cover every
+      // later round's, as top only falls); read by the next round
+      uint32_t below = cur[top] & ~(1u << (m & 31));
+      int m2 = below ? 32 * top + (31 - __clz(below)) : -1;
+      if (m2 < 0 && top > 0) {
+        const int w = top - 1 - lane;
+        const uint32_t x = (w >= 0) ? cur[w] : 0u;
+        const unsigned msk = __ballot_sync(0xffffffffu, x != 0u);
+        if (msk) {
+          const int l = __ffs(msk) - 1;  // lowest lane = highest word
+          const uint32_t xl = __shfl_sync(0xffffffffu, x, l);
+          m2 = 32 * (top - 1 - l) + (31 - __clz(xl));
+        }
+      }
+      pf_m = m2;
+      if (m2 >= 0) {
+#pragma unroll
+        for (int q = 0; q < kRowRegs; ++q) {
+          const int w = lane + 32 * q;
+          pf[q] = (w <= top) ? adj[(size_t)m2 * words + w] : 0u;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < kRowRegs; ++q) {
+        const int w = lane + 32 * q;
+        if (w <= top) {
+          uint32_t x = cur[w] & row[q];
+          if (w == (m >> 5)) x &= ~(1u << (m & 31));  // m is never its own neighbour: every round shrinks B
+          nxt[w] = x;
+          c2 += __popc(x);
+          if (x) top2 = w;
+        }
+      }
+    } else {
+      for (int w = lane; w <= top; w += 32) {
+        uint32_t x = cur[w] & adj[(size_t)m * words + w];
+        if (w == (m >> 5)) x &= ~(1u << (m & 31));  // m is never its own neighbour: every round shrinks B
+        nxt[w] = x;
+        c2 += __popc(x);
+        if (x) top2 = w;
+      }
     }
     const int n_next = warp_sum(c2);
     top2 = warp_max(top2);

@@ -25,6 +25,7 @@
 #include <cooperative_groups.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 
 #include "chol.hpp"
@@ -38,6 +39,17 @@ using namespace sm;
 
 // device memory the direct solver's factor may take before the PCG path is used
 constexpr double kCholBudgetBytes = 32.0 * (1 << 30);
+// Fill-in guard: factorisations above this many flops (about 30 ms of the
+// direct kernel) race the two solvers on the first damped system. Measured
+// on GB300, 20,000 poses, GNC alone: 8,000 closures, 40 % outliers half
+// clustered: direct 170 ms / PCG 374 ms per system (5.3e10 flops); 5,600
+// inliers + 2,400 uniform outliers: direct 264 ms / PCG 78 ms (9.2e10).
+std::atomic<double> g_guard_flops{1e10};
+std::atomic<int> g_guard_prefer{0};
+
+bool use_direct(const SolverDev& s) { return s.chol && !s.pcg_chosen; }
+// the PCG path's assembly (FP32 blocks, chain preconditioner) is needed
+bool need_pcg(const SolverDev& s) { return !use_direct(s) || s.race; }
 
 // ------------------------------------------------------------------ errors
 template <int DIM>
@@ -312,7 +324,7 @@ __global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __res
   double* og = fg + (size_t)f * 2 * d;
   og[a] = gi;
   og[d + a] = gj;
-  float* out = fH + (size_t)f * 3 * dd;
+  float* out = fH ? fH + (size_t)f * 3 * dd : nullptr;
   double* out64 = fH64 + (size_t)f * 3 * dd;
 #pragma unroll
   for (int b = 0; b < d; ++b) {
@@ -326,9 +338,11 @@ __global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __res
     out64[d * a + b] = hii;
     out64[dd + d * a + b] = hjj;
     out64[2 * dd + d * a + b] = hij;
-    out[d * a + b] = (float)hii;
-    out[dd + d * a + b] = (float)hjj;
-    out[2 * dd + d * a + b] = (float)hij;
+    if (fH) {  // the FP32 copy feeds only the PCG path's preconditioner and SpMV
+      out[d * a + b] = (float)hii;
+      out[dd + d * a + b] = (float)hjj;
+      out[2 * dd + d * a + b] = (float)hij;
+    }
   }
 }
 
@@ -689,8 +703,11 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
     const double bytes = 8.0 * dd * (plan.n_blocks() + plan.n_sparse) + 8.0 * ntp * ntp +
                          4.0 * (plan.upd_src.size() + plan.tupd_src.size());
     if (bytes <= kCholBudgetBytes) {
+      const double flops = plan.flops;
       s.chol = std::make_shared<CholDev>();
       s.chol->upload(std::move(plan), st);
+      s.race = flops > g_guard_flops.load() ? 1 : 0;
+      s.pcg_chosen = false;
     }
   }
 }
@@ -750,17 +767,19 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
                                                        s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get());
       RPGO_LAUNCHED();
       k_linearize_b<3><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
-                                                               s.fH.get(), s.fH64.get(), s.fg.get());
+                                                               need_pcg(s) ? s.fH.get() : nullptr, s.fH64.get(),
+                                                               s.fg.get());
     } else {
       k_linearize_a<2><<<div_up(2 * (int64_t)s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                        s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get());
       RPGO_LAUNCHED();
       k_linearize_b<2><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
-                                                               s.fH.get(), s.fH64.get(), s.fg.get());
+                                                               need_pcg(s) ? s.fH.get() : nullptr, s.fH64.get(),
+                                                               s.fg.get());
     }
     RPGO_LAUNCHED();
   }
-  if (s.chol) {
+  if (use_direct(s)) {
     const int blocks = div_up((int64_t)s.N * 32, tb);
     if (s.dim == 3)
       k_assemble_direct<6><<<blocks, tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
@@ -772,7 +791,9 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
                                                   diagonal_damping ? 1 : 0);
     RPGO_LAUNCHED();
     chol_block_hessian(s, *s.chol, st);
-    return;
+    if (!s.race) return;
+    // racing: the PCG path's blocks too (same FP64 diagonal, gradient and
+    // damping as k_assemble_direct's)
   }
   if (s.dim == 3)
     k_assemble<6><<<div_up(s.N, tb), tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
@@ -1154,8 +1175,37 @@ __global__ void __launch_bounds__(256) k_pcg_coop(CoopArgs a) {
 }
 
 // (H + lambda D) delta = -g with the whole-GPU flexible PCG (k_pcg_coop).
+double set_direct_solve_guard(double flops, int prefer) {
+  g_guard_prefer.store(prefer);
+  return g_guard_flops.exchange(flops);
+}
+
+// the whole-GPU PCG solve; *ms (optional) receives its kernel time
+SolveOut pcg_solve(SolverDev& s, double lambda, cudaStream_t st, double* ms_out);
+
+// the fill-in guard's race on the first damped system: the PCG path, then
+// the direct solve, whose result this solve keeps (the choice affects the
+// later solves only); the faster path (or the preferred one) stays
+static SolveOut race_solve(SolverDev& s, double lambda, cudaStream_t st) {
+  double pcg_ms = 0.0;
+  const SolveOut op = pcg_solve(s, lambda, st, &pcg_ms);
+  const double before = kernel_times().chol_ms;
+  const SolveOut oc = chol_solve(s, *s.chol, lambda, st);
+  const double chol_ms = kernel_times().chol_ms - before;
+  const int prefer = g_guard_prefer.load();
+  s.pcg_chosen = prefer == 2 || (prefer == 0 && op.ok && pcg_ms < chol_ms);
+  s.race = 0;
+  SolveOut o = oc;
+  o.cg_iterations = op.cg_iterations;
+  return o;
+}
+
 SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
-  if (s.chol) return chol_solve(s, *s.chol, lambda, st);
+  if (use_direct(s)) return s.race ? race_solve(s, lambda, st) : chol_solve(s, *s.chol, lambda, st);
+  return pcg_solve(s, lambda, st, nullptr);
+}
+
+SolveOut pcg_solve(SolverDev& s, double lambda, cudaStream_t st, double* ms_out) {
   SolveOut o;
   if (s.N == 0) {
     o.ok = 1;
@@ -1189,6 +1239,7 @@ SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
     RPGO_LAUNCHED();
     pcg_ms = timer.elapsed_ms();
   }
+  if (ms_out) *ms_out = pcg_ms;
   double h[4];
   RPGO_CUDA(cudaMemcpyAsync(h, s.out.get(), sizeof(h), cudaMemcpyDeviceToHost, st));
   RPGO_CUDA(cudaStreamSynchronize(st));
@@ -1216,7 +1267,7 @@ SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st) {
 }
 
 SolveOut solver_solve_eval(SolverDev& s, double lambda, cudaStream_t st, double* nerr) {
-  if (!s.chol) {
+  if (!use_direct(s) || s.race) {
     SolveOut o = solver_solve(s, lambda, st);
     if (o.ok && o.lin_change >= 0.0) {
       solver_retract(s, st);

@@ -16,6 +16,11 @@ struct CholDev;
 struct SolverDev {
   int dim = 3, d = 6, stride = 12, N = 0, F = 0;
   int coop_ctas = 0;  // CTAs of the cooperative direct solve (0: one per SM)
+  // fill-in guard: a direct plan whose factorisation exceeds the guard's
+  // flops runs its first damped system with both solvers (race = 1) and
+  // keeps the faster (pcg_chosen when the PCG path won)
+  int race = 0;
+  bool pcg_chosen = false;
   // factors
   DeviceBuffer<int32_t> kind, vi, vj;
   DeviceBuffer<uint8_t> tree;            // between factor joining consecutive variables
@@ -78,6 +83,11 @@ void solver_factor_errors(SolverDev& s, const double* x, std::vector<double>* ou
 void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st);
 // solve (H + lambda D) delta = -g into s.delta
 SolveOut solver_solve(SolverDev& s, double lambda, cudaStream_t st);
+// fill-in guard of the direct solve (process-wide): plans of more than
+// `flops` factorisation flops race both solvers on their first damped
+// system; prefer 0 keeps the faster, 1 always the direct solve, 2 always the
+// PCG path (for tests). Returns the previous threshold.
+double set_direct_solve_guard(double flops, int prefer);
 // solve, then xnew = x (+) delta and its weighted error *nerr (valid when
 // the solve succeeded with a non-negative model change); with the direct
 // solver the three results come back in one synchronisation

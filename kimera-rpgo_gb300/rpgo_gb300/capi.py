@@ -133,6 +133,7 @@ SIGNATURES = {
     "rpgo_device_info": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_int32)]),
     "rpgo_kernel_launch_count": (C.c_int64, []),
     "rpgo_buffer_alloc_count": (C.c_int64, []),
+    "rpgo_set_direct_solve_guard": (C.c_double, [C.c_double, C.c_int32]),
 }
 
 
@@ -517,6 +518,13 @@ def device_info():
 
 def kernel_launch_count() -> int:
     return int(load().rpgo_kernel_launch_count())
+
+
+def set_direct_solve_guard(flops: float, prefer: int = 0) -> float:
+    """Fill-in guard of the direct solve: plans above `flops` race the direct
+    and PCG solvers on the first damped system (prefer 0: keep the faster,
+    1: direct, 2: PCG). Returns the previous threshold."""
+    return float(load().rpgo_set_direct_solve_guard(float(flops), int(prefer)))
 
 
 def buffer_alloc_count() -> int:

@@ -349,3 +349,35 @@ def test_update_dev_matches_host_update():
     ka, pa = a.estimate()
     kb, pb = b.estimate()
     assert np.array_equal(ka, kb) and np.array_equal(pa, pb)
+
+
+@pytest.mark.parametrize("prefer", [1, 2])
+def test_fill_in_guard_branches_match_oracle(prefer):
+    # GNC alone on uniform outliers: every outlier joins distant poses and the
+    # factor fills in. A zero guard makes every plan race the two solvers on
+    # its first damped system; both branches (direct kept / PCG kept for the
+    # rest of the schedule) equal the oracle.
+    s = synth.walk3d(800, 160, 120, seed=57)
+    p = RobustSolverParams().setPcm3DParams(-1.0, -1.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+    old = capi.set_direct_solve_guard(0.0, prefer)
+    try:
+        o, g = O.OracleSolver(p), capi.RobustSolver(p)
+        assert o.update(s.graph) == 0 and g.update(s.graph) == 0
+    finally:
+        capi.set_direct_solve_guard(old, 0)
+    t = g.timing()
+    if prefer == 1:
+        assert t.pcg_kernel_launches == 1 and t.chol_kernel_launches == t.linear_solves
+    else:
+        assert t.chol_kernel_launches == 1 and t.pcg_kernel_launches == t.linear_solves
+    assert np.array_equal(np.round(o.gnc_weights()), np.round(g.gnc_weights()))
+    _pose_close(o.estimate()[1], g.estimate()[1], 3)
+
+
+def test_fill_in_guard_off_below_threshold():
+    # the benchmark-sized plans stay far below the default guard: no race
+    s = synth.walk3d(600, 150, 50, seed=58)
+    p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+    g = capi.RobustSolver(p)
+    assert g.update(s.graph) == 0
+    assert g.timing().pcg_kernel_launches == 0
