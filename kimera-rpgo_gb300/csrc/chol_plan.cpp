@@ -2,6 +2,7 @@
 #include "chol_plan.hpp"
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <exception>
 #include <functional>
@@ -444,6 +445,14 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
   {
     std::vector<int32_t> cc(p.lvl_col_ptr.begin(), p.lvl_col_ptr.end() - 1);
     for (int j = 0; j < ns; ++j) p.lvl_cols[cc[lvl[j]]++] = j;
+    // each level's columns by descending block count (consecutive columns go
+    // to the lane groups of one warp on wide levels: similar loops); columns
+    // of a level are independent, so the order changes no result
+    for (int l = 0; l < L; ++l)
+      std::stable_sort(p.lvl_cols.begin() + p.lvl_col_ptr[l], p.lvl_cols.begin() + p.lvl_col_ptr[l + 1],
+                       [&](int32_t a, int32_t b) {
+                         return p.col_ptr[a + 1] - p.col_ptr[a] > p.col_ptr[b + 1] - p.col_ptr[b];
+                       });
   }
 
   // updates: for each sparse column k and rows ra <= rb of it, target (rb, ra)
@@ -572,10 +581,11 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
         const int j = p.lvl_cols[w];
         for (int q = p.col_ptr[j]; q < p.col_ptr[j + 1]; ++q) {
           p.btask[2 * q] = slot;
-          // the leaves' blocks have no update pairs (and the leaves no row
-          // sums): they get no task, the column's own phase reads its Hessian
-          // blocks directly, and the leaves' level has no task phase
-          if (l == 0) continue;
+          // blocks without update pairs (every block of the leaves, which
+          // also have no row sums) get no task: the column's own phase reads
+          // their Hessian blocks directly, and the leaves' level has no task
+          // phase
+          if (l == 0 || p.upd_ptr[q] == p.upd_ptr[q + 1]) continue;
           int u = p.upd_ptr[q];
           do {
             const int e = std::min(u + p.chunk, p.upd_ptr[q + 1]);
@@ -595,7 +605,22 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
         }
         p.ftask[2 * j + 1] = slot - p.ftask[2 * j];
       }
-      p.lvl_task_ptr[l + 1] = (int)p.tasks.size() / 4;
+      // the level's tasks by descending work (a block chunk's pairs weigh
+      // three row entries; the Hessian block of a first chunk one more), so
+      // that the lane groups of a warp, which take consecutive tasks on wide
+      // levels, get similar loops; the order of independent tasks changes no
+      // result
+      const int t0 = p.lvl_task_ptr[l], t1 = (int)p.tasks.size() / 4;
+      std::vector<std::array<int32_t, 4>> lt((size_t)(t1 - t0));
+      for (int t = t0; t < t1; ++t) lt[t - t0] = {p.tasks[4 * t], p.tasks[4 * t + 1], p.tasks[4 * t + 2], p.tasks[4 * t + 3]};
+      auto work = [](const std::array<int32_t, 4>& x) {
+        const int kind = x[3] & 3, n = x[2] - x[1];
+        return kind == 2 ? n : 3 * n + (kind == 1 ? 1 : 0);
+      };
+      std::stable_sort(lt.begin(), lt.end(), [&](const auto& a, const auto& b) { return work(a) > work(b); });
+      for (int t = t0; t < t1; ++t)
+        for (int k = 0; k < 4; ++k) p.tasks[4 * t + k] = lt[t - t0][k];
+      p.lvl_task_ptr[l + 1] = t1;
     }
     p.n_slots = slot;
   }

@@ -41,14 +41,16 @@ struct CholPlan {
   //  kind 0 / 1: block id's update list [first, end) cut into chunks of at
   //    most `chunk` pairs (kind 1 on the block's first chunk, which also
   //    carries the Hessian block); for 6x6 blocks every chunk is two tasks,
-  //    output columns 0-2 (half 0) and 3-5 (half 1), sharing one slot; 
-  //    block of the first level (the leaves, which have no update pairs) has
-  //    no task (btask count 0) and is read from the Hessian when its column
-  //    is finalised;
+  //    output columns 0-2 (half 0) and 3-5 (half 1), sharing one slot; a
+  //    block without update pairs (every block of the first level, the
+  //    leaves) has no task (btask count 0) and is read from the Hessian when
+  //    its column is finalised;
   //  kind 2: the forward-substitution row sum of column id over its row
   //    list entries [first, end) (chunks of at most `row_chunk`).
-  // Tasks of one level are contiguous (lvl_task_ptr); the slots of one block
-  // (btask: first, count) and of one column's row sum (ftask) are too.
+  // Tasks of one level are contiguous (lvl_task_ptr), ordered by descending
+  // work; the slots of one block (btask: first, count) and of one column's
+  // row sum (ftask) are contiguous. Each level's columns (lvl_cols) are
+  // ordered by descending block count.
   int chunk = 5, row_chunk = 20, n_slots = 0;
   std::vector<int32_t> lvl_task_ptr, tasks, btask, ftask;
   // tail row tasks: the sparse part of tail block row t, [first, end) of
