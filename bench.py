@@ -424,6 +424,8 @@ def batched_leg(params, n_graphs=64, workers=8):
     import concurrent.futures as cf
     import multiprocessing
 
+    import numpy as np
+
     from rpgo_gb300 import capi, synth
 
     sizes = synth.config_c4_sizes(512)[:n_graphs]
@@ -434,6 +436,13 @@ def batched_leg(params, n_graphs=64, workers=8):
     res = capi.solve_batch(params, graphs, workers=workers)
     tb = time.perf_counter() - t0
     assert all(r[0] == 0 for r in res)
+    # the lock-step form: one launch per stage over all graphs
+    capi.solve_batch(params, graphs[:workers], joint=True)
+    t0 = time.perf_counter()
+    rj = capi.solve_batch(params, graphs, joint=True)
+    tj = time.perf_counter() - t0
+    assert all(r[0] == 0 for r in rj)
+    same = sum(int(np.array_equal(np.round(a[3]), np.round(b[3]))) for a, b in zip(res, rj))
     t0 = time.perf_counter()
     for gr in graphs:
         assert capi.RobustSolver(params).update(gr) == 0
@@ -441,6 +450,10 @@ def batched_leg(params, n_graphs=64, workers=8):
     return {"value": n_graphs / tb, "unit": "graphs/s", "graphs": n_graphs, "workers": workers,
             "poses": int(sum(x[0] for x in sizes)), "seconds": tb, "one_at_a_time_graphs_per_s": n_graphs / ts,
             "speedup_vs_one_at_a_time": ts / tb,
+            "joint": {"value": n_graphs / tj, "seconds": tj, "rounds_solve_ms": float(rj[0][4].solve_ms),
+                      "linear_solves_max": int(max(r[4].linear_solves for r in rj)),
+                      "linear_solves_sum": int(sum(r[4].linear_solves for r in rj)),
+                      "graphs_with_worker_inlier_set": same},
             "workload": "first 64 graphs of the 512-graph batch (seed 4): 3d random walks of 200-8000 poses, "
                         "closures 10-30 % of the poses, outlier rate U[0, 0.5]; wall clock, host to host"}
 

@@ -373,6 +373,18 @@ typedef struct rpgo_batch_out {
 } rpgo_batch_out;
 int rpgo_solve_batch(const rpgo_params* p, int32_t n, const rpgo_factor_batch* factors,
                      const rpgo_value_batch* values, int32_t workers, int32_t coop_ctas, rpgo_batch_out* out);
+/* The same batch with the solves in lock-step (no counterpart in the
+ * reference): every graph's PCM runs on its own solver as in
+ * rpgo_solve_batch; then the GNC-TLS / LM (or GN) solves of the graphs advance
+ * together, one damped solve per graph per round, and every stage of a round
+ * (linearisation, block Hessian, the direct solve, retraction, errors, TLS
+ * weights) is one launch over all graphs, each graph with its own damping
+ * and decisions. `group`: graphs per lock-step group (0: all). Graphs whose
+ * solve needs the solver's own path (temporary values, a warm start, the PCG
+ * solver) are solved by it. Outputs as rpgo_solve_batch; timing.solve_ms is
+ * the wall time of the graph's group. */
+int rpgo_solve_batch_joint(const rpgo_params* p, int32_t n, const rpgo_factor_batch* factors,
+                           const rpgo_value_batch* values, int32_t group, rpgo_batch_out* out);
 
 /* ------------------------------------------------------------ stage kernels
  * Device-resident entry points of the hot path, one per reference function

@@ -1,6 +1,7 @@
-// Batched solve of independent graphs (rpgo_solve_batch, include/rpgo_gb300.h).
+// Batched solve of independent graphs (rpgo_solve_batch and
+// rpgo_solve_batch_joint, include/rpgo_gb300.h).
 //
-// Each graph is an ordinary rpgo_solver (RobustSolver look-alike) on its own
+// rpgo_solve_batch: each graph is an ordinary rpgo_solver (RobustSolver look-alike) on its own
 // non-blocking stream; `workers` host threads take graphs from a shared
 // counter. The GPU runs the workers' kernels concurrently: the per-graph
 // kernels of PCM (trajectory scan, odometry and pairwise checks, clique) are
@@ -8,13 +9,19 @@
 // to `coop_ctas` CTAs so that several fit on the device at once. Device memory
 // is stream-ordered (no device-wide synchronisation on free), so the workers
 // do not serialise each other.
+//
+// rpgo_solve_batch_joint: every graph's PCM on its own solver (worker
+// threads), then the GNC / LM solves of all graphs in lock-step rounds with
+// one launch per stage over all of them (batch_joint.cpp).
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cstring>
 #include <thread>
 #include <vector>
 
 #include "../../include/rpgo_gb300.h"
+#include "batch_joint.hpp"
 #include "common.cuh"
 
 namespace rpgo {
@@ -27,16 +34,9 @@ constexpr int kDefaultWorkers = 16;
 // co-resident CTAs of the direct solve per SM (256 threads x 128 registers)
 constexpr int kCholCtasPerSm = 2;
 
-void solve_one(const rpgo_params* p, const rpgo_factor_batch& f, const rpgo_value_batch& v, int ctas,
-               double* poses, int64_t stride, double* weights, int64_t* num_weights, int32_t* status,
-               rpgo_timing* timing) {
-  rpgo_solver* s = rpgo_create(p);
-  if (!s) {
-    *status = RPGO_ERR_CUDA;
-    return;
-  }
-  rpgo::set_coop_ctas(s, ctas);
-  int rc = rpgo_update(s, &f, &v, 1);
+// the estimate, weights and timing of solver s into the batch outputs
+int write_outputs(rpgo_solver* s, int rc, const rpgo_factor_batch& f, const rpgo_value_batch& v, double* poses,
+                  int64_t stride, double* weights, int64_t* num_weights, rpgo_timing* timing) {
   if (rc == RPGO_OK) {
     rpgo_counts c;
     rpgo_get_counts(s, &c);
@@ -59,8 +59,42 @@ void solve_one(const rpgo_params* p, const rpgo_factor_batch& f, const rpgo_valu
     }
   }
   if (timing) rpgo_get_timing(s, timing);
-  *status = rc;
+  return rc;
+}
+
+void solve_one(const rpgo_params* p, const rpgo_factor_batch& f, const rpgo_value_batch& v, int ctas,
+               double* poses, int64_t stride, double* weights, int64_t* num_weights, int32_t* status,
+               rpgo_timing* timing) {
+  rpgo_solver* s = rpgo_create(p);
+  if (!s) {
+    *status = RPGO_ERR_CUDA;
+    return;
+  }
+  rpgo::set_coop_ctas(s, ctas);
+  const int rc = rpgo_update(s, &f, &v, 1);
+  *status = write_outputs(s, rc, f, v, poses, stride, weights, num_weights, timing);
   rpgo_destroy(s);
+}
+
+// the batch's pose dimension (all graphs share the parameters)
+int batch_dim(const rpgo_params* p) {
+  const int m = p->outlier_removal;
+  return (m == RPGO_OUTLIER_PCM2D || m == RPGO_OUTLIER_PCM_SIMPLE2D) ? 2 : (m == RPGO_OUTLIER_NONE ? p->dim : 3);
+}
+
+// run work(i) for i in [0, n) on up to `threads` host threads
+template <class Fn>
+void parallel_for(int n, int threads, Fn&& work) {
+  std::atomic<int> next{0};
+  auto loop = [&] {
+    for (int i; (i = next.fetch_add(1)) < n;) work(i);
+  };
+  const int nt = std::max(1, std::min(n, threads));
+  std::vector<std::thread> pool;
+  pool.reserve((size_t)nt - 1);
+  for (int t = 1; t < nt; ++t) pool.emplace_back(loop);
+  loop();
+  for (auto& t : pool) t.join();
 }
 
 }  // namespace
@@ -70,8 +104,7 @@ extern "C" int rpgo_solve_batch(const rpgo_params* p, int32_t n, const rpgo_fact
                                 rpgo_batch_out* out) {
   if (!p || n < 0 || (n > 0 && (!factors || !values || !out || !out->poses || !out->status))) return RPGO_ERR_ARG;
   if (n == 0) return RPGO_OK;
-  const int m = p->outlier_removal;
-  const int dim = (m == RPGO_OUTLIER_PCM2D || m == RPGO_OUTLIER_PCM_SIMPLE2D) ? 2 : (m == RPGO_OUTLIER_NONE ? p->dim : 3);
+  const int dim = batch_dim(p);
   const int64_t stride = dim == 3 ? 12 : 4;
   std::vector<int64_t> voff((size_t)n + 1, 0), foff((size_t)n + 1, 0);
   for (int g = 0; g < n; ++g) {
@@ -102,5 +135,88 @@ extern "C" int rpgo_solve_batch(const rpgo_params* p, int32_t n, const rpgo_fact
   for (int t = 1; t < nw; ++t) pool.emplace_back(work);
   work();
   for (auto& t : pool) t.join();
+  return RPGO_OK;
+}
+
+extern "C" int rpgo_solve_batch_joint(const rpgo_params* p, int32_t n, const rpgo_factor_batch* factors,
+                                      const rpgo_value_batch* values, int32_t group, rpgo_batch_out* out) {
+  if (!p || n < 0 || (n > 0 && (!factors || !values || !out || !out->poses || !out->status))) return RPGO_ERR_ARG;
+  if (n == 0) return RPGO_OK;
+  const int dim = batch_dim(p);
+  const int64_t stride = dim == 3 ? 12 : 4;
+  std::vector<int64_t> voff((size_t)n + 1, 0), foff((size_t)n + 1, 0);
+  for (int g = 0; g < n; ++g) {
+    voff[g + 1] = voff[g] + values[g].count;
+    foff[g + 1] = foff[g] + factors[g].count;
+  }
+  const int threads = kDefaultWorkers;
+  // 1. every graph's PCM (and classification) on its own solver, concurrently
+  std::vector<rpgo_solver*> sv((size_t)n, nullptr);
+  std::vector<int> rc((size_t)n, RPGO_OK), kind((size_t)n, rpgo::kJointNone);
+  std::vector<rpgo::JointProblem> jp((size_t)n);
+  std::vector<double> solve_ms((size_t)n, 0.0);
+  parallel_for(n, threads, [&](int g) {
+    sv[g] = rpgo_create(p);
+    if (!sv[g]) {
+      rc[g] = RPGO_ERR_CUDA;
+      return;
+    }
+    rc[g] = rpgo_update(sv[g], &factors[g], &values[g], 0);
+    if (rc[g] != RPGO_OK) return;
+    try {
+      kind[g] = rpgo::joint_prepare(sv[g], &jp[g]);
+    } catch (...) {
+      rc[g] = RPGO_ERR_CUDA;
+    }
+  });
+  // 2. graphs that need their solver's own path
+  parallel_for(n, threads, [&](int g) {
+    if (rc[g] == RPGO_OK && kind[g] == rpgo::kJointOwn) {
+      try {
+        rc[g] = rpgo::joint_optimize_own(sv[g], &solve_ms[g]);
+      } catch (...) {
+        rc[g] = RPGO_ERR_CUDA;
+      }
+    }
+  });
+  // 3. the rest in lock-step groups
+  std::vector<int> joint;
+  for (int g = 0; g < n; ++g)
+    if (rc[g] == RPGO_OK && kind[g] == rpgo::kJointSolve) joint.push_back(g);
+  const int gsz = group > 0 ? group : std::max(1, (int)joint.size());
+  cudaStream_t st = nullptr;
+  if (!joint.empty() && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+    for (int g : joint) rc[g] = RPGO_ERR_CUDA;
+    joint.clear();
+  }
+  if (!joint.empty()) {
+    for (size_t b0 = 0; b0 < joint.size(); b0 += gsz) {
+      const size_t b1 = std::min(joint.size(), b0 + gsz);
+      std::vector<rpgo::JointProblem*> probs;
+      for (size_t k = b0; k < b1; ++k) probs.push_back(&jp[joint[k]]);
+      try {
+        const auto t0 = std::chrono::steady_clock::now();
+        rpgo::solve_joint(dim, probs, st);
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        for (size_t k = b0; k < b1; ++k) solve_ms[joint[k]] = ms;
+      } catch (...) {
+        for (size_t k = b0; k < b1; ++k) rc[joint[k]] = RPGO_ERR_CUDA;
+      }
+    }
+    cudaStreamDestroy(st);
+  }
+  // 4. bookkeeping and outputs
+  parallel_for(n, threads, [&](int g) {
+    if (!sv[g]) {
+      out->status[g] = rc[g];
+      return;
+    }
+    if (rc[g] == RPGO_OK && kind[g] == rpgo::kJointSolve) rc[g] = rpgo::joint_commit(sv[g], jp[g], solve_ms[g]);
+    out->status[g] = write_outputs(sv[g], rc[g], factors[g], values[g], out->poses + voff[g] * stride, stride,
+                                   out->gnc_weights ? out->gnc_weights + foff[g] : nullptr,
+                                   out->num_weights ? out->num_weights + g : nullptr,
+                                   out->timing ? out->timing + g : nullptr);
+    rpgo_destroy(sv[g]);
+  });
   return RPGO_OK;
 }

@@ -26,6 +26,7 @@
 #include "solver.hpp"
 #include "warm.hpp"
 #include "align.hpp"
+#include "batch_joint.hpp"
 
 using namespace rpgo;
 
@@ -357,6 +358,97 @@ int optimize(rpgo_solver* s) {
   if (s->pcm) s->latest_num_lc = s->pcm->num_lc();
   return RPGO_OK;
 }
+
+}  // namespace
+
+namespace rpgo {
+
+// The problem RobustSolver::optimize would solve now, for the joint batch:
+// kJointSolve with *jp filled, kJointNone when the last update asked for no
+// optimisation, kJointOwn when this solve needs the solver's own path
+// (temporary values, a warm start, the fixed-previous-inliers subset, the
+// PCG solver, an empty graph).
+int joint_prepare(rpgo_solver* s, JointProblem* jp) {
+  if (!s->last_do_optimize) return kJointNone;
+  if (s->temp_values->size() != 0 || s->p.linear_solver == RPGO_LINEAR_PCG) return kJointOwn;
+  std::vector<FactorRec> full = s->nfg;
+  full.insert(full.end(), s->temp_nfg.begin(), s->temp_nfg.end());
+  if (full.empty() || s->values->size() == 0) return kJointOwn;
+  jp->lm = LmParams{};
+  jp->lm.gauss_newton = s->p.solver == RPGO_SOLVER_GN;
+  jp->lm.diagonal_damping = s->p.lm_diagonal_damping != 0;
+  const size_t num_lc = s->pcm ? s->pcm->num_lc() : 0;
+  jp->init_weights.clear();
+  if (s->p.use_gnc && s->pcm && !(s->p.gnc_fix_prev_inliers && num_lc == s->latest_num_lc)) {
+    if (s->p.gnc_warm_start != RPGO_WARM_OFF) return kJointOwn;
+    jp->gnc = true;
+    jp->gnc_cfg.threshold_mode = s->p.gnc_threshold_mode;
+    jp->gnc_cfg.threshold = s->p.gnc_inlier_threshold;
+    jp->gnc_cfg.max_iterations = s->p.gnc_max_iterations;
+    jp->gnc_cfg.mu_step = s->p.gnc_mu_step;
+    jp->gnc_cfg.rel_cost_tol = s->p.gnc_relative_cost_tol;
+    jp->gnc_cfg.weights_tol = s->p.gnc_weights_tol;
+    jp->n_known = s->pcm->num_odom() + s->pcm->num_special();
+    if (s->p.gnc_bias_odom) {
+      jp->init_weights.assign(full.size(), 0.0);
+      for (size_t i = 0; i < jp->n_known && i < full.size(); ++i) jp->init_weights[i] = 1.0;
+    }
+  } else {
+    if (s->p.gnc_fix_prev_inliers && s->pcm) return kJointOwn;
+    jp->gnc = false;
+    jp->n_known = full.size();
+  }
+  jp->graph = std::move(full);
+  jp->store = s->store.get();
+  jp->values = s->values.get();
+  return kJointSolve;
+}
+
+// RobustSolver::optimize's bookkeeping after the joint batch solved *jp
+// (the estimate is already in the solver's values)
+int joint_commit(rpgo_solver* s, const JointProblem& jp, double solve_ms) {
+  const NlsStats& st = jp.stats;
+  if (jp.gnc) {
+    const std::vector<double>& w = jp.weights;
+    s->gnc_weights.assign(w.begin(), w.begin() + std::min(w.size(), s->nfg.size()));
+    s->gnc_temp_weights.assign(w.begin() + std::min(w.size(), s->nfg.size()), w.end());
+    const double sum = std::accumulate(s->gnc_weights.begin(), s->gnc_weights.end(), 0.0);
+    s->gnc_num_inliers = static_cast<size_t>(sum) - jp.n_known;
+  } else {
+    if (st.failed) return RPGO_ERR_SOLVER;
+    s->gnc_temp_weights.assign(s->temp_nfg.size(), 1.0);
+    const size_t tail = std::min(s->latest_num_lc, s->gnc_weights.size());
+    std::vector<double> lcw(s->gnc_weights.end() - tail, s->gnc_weights.end());
+    s->gnc_weights.assign(s->nfg.size(), 1.0);
+    const size_t t2 = std::min(tail, s->gnc_weights.size());
+    for (size_t i = 0; i < t2; ++i) s->gnc_weights[s->gnc_weights.size() - t2 + i] = lcw[lcw.size() - t2 + i];
+  }
+  s->timing.solve_ms = solve_ms;
+  s->timing.lm_iterations += st.iterations;
+  s->timing.linear_solves += st.linear_solves;
+  s->timing.gnc_iterations += st.gnc_iterations;
+  if (s->pcm) s->latest_num_lc = s->pcm->num_lc();
+  return RPGO_OK;
+}
+
+// the solver's own optimisation (joint_prepare answered kJointOwn)
+int joint_optimize_own(rpgo_solver* s, double* solve_ms) {
+  cudaEvent_t e0, e1;
+  RPGO_CUDA(cudaEventCreate(&e0));
+  RPGO_CUDA(cudaEventCreate(&e1));
+  RPGO_CUDA(cudaEventRecord(e0, s->st));
+  const int rc = optimize(s);
+  RPGO_CUDA(cudaEventRecord(e1, s->st));
+  RPGO_CUDA(cudaEventSynchronize(e1));
+  *solve_ms = ms_since(e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return rc;
+}
+
+}  // namespace rpgo
+
+namespace {
 
 // RobustSolver::update / forceUpdate on prepared factor records; value
 // arrays are host or device pointers.

@@ -36,7 +36,8 @@ struct CholDev {
 
 // H and the damping diagonal in the block layout of L, from the linearised
 // system (Hd64, fH64, dampD); enqueued after every linearisation.
-void chol_block_hessian(SolverDev& s, CholDev& c, cudaStream_t st);
+// mask: a joint batch's variable control words (bit 0: graph in this round)
+void chol_block_hessian(SolverDev& s, CholDev& c, cudaStream_t st, const uint8_t* mask = nullptr);
 // Solve with the factorisation of (H + lambda D); fills s.delta.
 SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st);
 // Enqueue the same solve without waiting: the model change and the status
@@ -44,5 +45,11 @@ SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st);
 // chol_finish after the stream reached that point.
 void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, double* host);
 SolveOut chol_finish(SolverDev& s, CholDev& c, const double* host);
+// Joint batch: enqueue one launch that solves every active system of the
+// batch b with its own damping; per-system model change and status land in
+// b.out (2 per system), the steps in s.delta.
+void chol_enqueue_batch(SolverDev& s, CholDev& c, const BatchDev& b, cudaStream_t st);
+// kernel time of the last enqueued launch (after the stream passed it)
+float chol_last_ms(CholDev& c);
 
 }  // namespace rpgo

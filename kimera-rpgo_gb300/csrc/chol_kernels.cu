@@ -60,9 +60,26 @@ struct CholArgs {
   double *L, *Ldiag, *M, *Ldd, *y, *delta, *part, *out, *Spart, *Tpart;
   const double *Hs, *dampS;  // Hessian and damping diagonal in the factor's block layout
   int32_t* status;
+  // Independent systems solved in one launch (a joint batch of graphs; G = 0
+  // for one system). System s owns the positions (and variables) [b_off[s],
+  // b_off[s + 1]); b_sys maps a position to its system. Systems whose b_act
+  // word has bit 0 clear are skipped. Each has its own damping, status and model change.
+  int G;
+  const int32_t *b_sys, *b_off;
+  const uint8_t* b_act;
+  const double* b_lam;
+  int32_t* b_status;
+  double *b_out, *b_term;  // per system (model change, status); per position partials
 };
 
 __device__ __forceinline__ void set_fail(int32_t* status) { atomicExch(status, 1); }
+
+// the system of position j is solved by this launch
+__device__ __forceinline__ bool sys_on(const CholArgs& a, int j) { return a.G == 0 || (a.b_act[a.b_sys[j]] & 1); }
+// status word of the system of position j
+__device__ __forceinline__ int32_t* sys_status(const CholArgs& a, int j) {
+  return a.G == 0 ? a.status : a.b_status + a.b_sys[j];
+}
 
 // Hessian entry (r, c) of the block at (row var, col var) from the factor
 // off-diagonal blocks in src[beg, end) (2 f + transposed)
@@ -93,7 +110,10 @@ template <int D>
 __device__ __forceinline__ double block_H(const CholArgs& a, int p, bool diag, int r, int c) {
   constexpr int dd = D * D;
   double s = a.Hs[(size_t)p * dd + r * D + c];
-  if (diag && r == c) s += a.lam * a.dampS[(size_t)p * D + r];
+  if (diag && r == c) {
+    const double lam = a.G == 0 ? a.lam : a.b_lam[a.b_sys[a.blk_col[p]]];
+    s += lam * a.dampS[(size_t)p * D + r];
+  }
   return s;
 }
 
@@ -122,6 +142,7 @@ __device__ void run_task(const CholArgs& a, int t, int lane) {
   const int g = lane / D, r = lane % D;
   const int4 tk = reinterpret_cast<const int4*>(a.tasks)[t];
   const int kind = tk.w & 3, slot = tk.w >> 4;
+  if (!sys_on(a, kind < 2 ? a.blk_col[tk.x] : tk.x)) return;  // (warp-uniform)
   if (kind < 2) {
     const int p = tk.x, c0 = ((tk.w >> 2) & 1) * NC;
     double acc[NC];
@@ -234,9 +255,10 @@ __device__ __forceinline__ void diag_partials(const CholArgs& a, int j, int p, i
 
 // In-register Cholesky of S_jj across a lane group (lane r holds row r, the
 // group's lanes start at `base`), reciprocal pivots on the diagonal; a failed
-// pivot of a group whose lanes have `mine` set sets the status flag.
+// pivot of a group whose lanes have `mine` set sets *status.
 template <int D>
-__device__ __forceinline__ void factor_diag(const CholArgs& a, int lane, bool mine, int r, int base, double (&C)[D]) {
+__device__ __forceinline__ void factor_diag(const CholArgs& a, int lane, bool mine, int r, int base, double (&C)[D],
+                                            int32_t* status) {
   bool ok = true;
 #pragma unroll
   for (int c = 0; c < D; ++c) {
@@ -256,8 +278,8 @@ __device__ __forceinline__ void factor_diag(const CholArgs& a, int lane, bool mi
       if (r >= q) C[q] = fma(-C[c], lqc, C[q]);
     }
   }
-  const bool bad = __any_sync(kFull, !ok && mine);
-  if (lane == 0 && bad) set_fail(a.status);
+  // the lane whose pivot failed flags its own group's system
+  if (!ok && mine) set_fail(status);
 }
 
 // L_ij = S_ij L_jj^-T for one row r of an off-diagonal block, in place
@@ -314,10 +336,11 @@ __device__ void column_warp(const CholArgs& a, int j, int lane) {
   const int g = lane / D, r = lane % D;
   const bool grp = g < G;
   const int base = (grp ? g : 0) * D;
+  if (!sys_on(a, j)) return;  // (warp-uniform)
   const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
   double C[D];
   diag_partials<D>(a, j, p0, lane, r, C);
-  factor_diag<D>(a, lane, g == 0, r, base, C);
+  factor_diag<D>(a, lane, g == 0, r, base, C, sys_status(a, j));
   double Lf[dd];
 #pragma unroll
   for (int q = 0; q < D; ++q)
@@ -352,10 +375,11 @@ __device__ void column_team(const CholArgs& a, int j, int tw, int lane, int bar,
   const bool grp = g < G;
   const int base = (grp ? g : 0) * D;
   const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
+  if (!sys_on(a, j)) return;  // (both warps of the team: no named barrier)
   if (tw == 0) {
     double C[D];
     diag_partials<D>(a, j, p0, lane, r, C);
-    factor_diag<D>(a, lane, g == 0, r, base, C);
+    factor_diag<D>(a, lane, g == 0, r, base, C, sys_status(a, j));
     if (g == 0) {
 #pragma unroll
       for (int c = 0; c < D; ++c) {
@@ -399,8 +423,11 @@ template <int D>
 __device__ void run_task_group(const CholArgs& a, int t, bool valid, int r) {
   constexpr int G = 32 / D, dd = D * D;
   constexpr int NC = D == 6 ? 3 : D;
-  const int4 tk = reinterpret_cast<const int4*>(a.tasks)[t];
+  int4 tk = reinterpret_cast<const int4*>(a.tasks)[t];
   const int kind = tk.w & 3, slot = tk.w >> 4;
+  // groups without a task of a solved system run empty loops
+  valid = valid && sys_on(a, kind < 2 ? a.blk_col[tk.x] : tk.x);
+  if (!valid) tk.z = tk.y;
   if (kind < 2) {
     const int p = tk.x, c0 = ((tk.w >> 2) & 1) * NC;
     double tot[NC];
@@ -467,15 +494,16 @@ __device__ void column_group(const CholArgs& a, int c0, int nc, int w0, int lane
   constexpr int G = 32 / D, dd = D * D;
   const int g = lane / D, r = lane % D;
   const int w = w0 + (g < G ? g : 0);
-  const bool mine = g < G && w < nc;
+  const int j = a.lvl_cols[c0 + ((g < G && w < nc) ? w : w0)];
+  // groups without a column of a solved system run empty loops
+  const bool mine = g < G && w < nc && sys_on(a, j);
   const int base = (g < G ? g : 0) * D;
-  const int j = a.lvl_cols[c0 + (mine ? w : w0)];
   const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
   // S_jj row r: every entry summed from 0 over the task slots in order, or
   // the Hessian block plus lambda D when the block has no task
   double C[D];
   {
-    const int t0 = a.btask[2 * p0], t1 = t0 + a.btask[2 * p0 + 1];
+    const int t0 = a.btask[2 * p0], t1 = t0 + (mine ? a.btask[2 * p0 + 1] : 0);
 #pragma unroll
     for (int c = 0; c < D; ++c) C[c] = (t1 == t0) ? block_H<D>(a, p0, true, r, c) : 0.0;
     for (int t = t0; t < t1; ++t) {
@@ -484,7 +512,7 @@ __device__ void column_group(const CholArgs& a, int c0, int nc, int w0, int lane
       for (int c = 0; c < D; ++c) C[c] += P[c];
     }
   }
-  factor_diag<D>(a, lane, mine, r, base, C);
+  factor_diag<D>(a, lane, mine, r, base, C, sys_status(a, j));
   double Lf[dd];
 #pragma unroll
   for (int q = 0; q < D; ++q)
@@ -499,7 +527,7 @@ __device__ void column_group(const CholArgs& a, int c0, int nc, int w0, int lane
       solve_offdiag<D>(a, p, r, Lf, sv);
     }
   }
-  forward_solve<D>(a, j, mine, r, base, C, forward_rhs<D>(a, j, r));
+  forward_solve<D>(a, j, mine, r, base, C, mine ? forward_rhs<D>(a, j, r) : 0.0);
 }
 
 // backward substitution of column j by one warp:
@@ -509,6 +537,7 @@ __device__ void backward_warp(const CholArgs& a, int j, int lane) {
   constexpr int G = 32 / D, dd = D * D;
   const int g = lane / D, r = lane % D;
   const int base = (g < G ? g : 0) * D;
+  if (!sys_on(a, j)) return;  // (warp-uniform)
   double acc = 0.0;
   const int q0 = a.col_ptr[j] + 1, q1 = a.col_ptr[j + 1];
   if (g < G) {
@@ -547,11 +576,13 @@ __device__ void backward_groups(const CholArgs& a, int c0, int nc, int w0, int l
   constexpr int G = 32 / D, dd = D * D;
   const int g = lane / D, r = lane % D;
   const int w = w0 + (g < G ? g : 0);
-  const bool mine = g < G && w < nc;
+  const int j = a.lvl_cols[c0 + ((g < G && w < nc) ? w : w0)];
+  // groups without a column of a solved system run an empty loop
+  const bool mine = g < G && w < nc && sys_on(a, j);
   const int base = (g < G ? g : 0) * D;
-  const int j = a.lvl_cols[c0 + (mine ? w : w0)];
   double acc = 0.0;
-  for (int q = a.col_ptr[j] + 1; q < a.col_ptr[j + 1]; ++q) {
+  const int q1 = mine ? a.col_ptr[j + 1] : 0;
+  for (int q = a.col_ptr[j] + 1; q < q1; ++q) {
     const double* B = a.L + (size_t)q * dd + r;
     const double* xi = a.y + (size_t)a.blk_row[q] * D;
 #pragma unroll
@@ -884,6 +915,7 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
 
   // 1. init
   if (gt == 0) *a.status = 0;
+  for (int k = gt; k < a.G; k += gs) a.b_status[k] = 0;
   for (int k = gt; k < n; k += gs) {
     const int pos = k / D, r = k % D;
     a.y[k] = -a.g[(size_t)a.perm[pos] * D + r];
@@ -1006,6 +1038,43 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
   // scatter to variable order, with the linearised cost change of the
   // undamped system: since (H + lambda D) delta = -g, -g.delta - delta^T H
   // delta / 2 = -g.delta / 2 + lambda delta^T D delta / 2
+  if (a.G > 0) {
+    // several systems: per-position partials, then one warp per system adds
+    // its positions in a fixed order (lane-strided chains, then a fixed tree)
+    for (int pos = gt; pos < a.N; pos += gs) {
+      if (!sys_on(a, pos)) continue;
+      double pg = 0.0, pq = 0.0;
+#pragma unroll
+      for (int r = 0; r < D; ++r) {
+        const size_t vi = (size_t)a.perm[pos] * D + r;
+        const double x = a.y[(size_t)pos * D + r];
+        a.delta[vi] = x;
+        pg = fma(a.g[vi], x, pg);
+        pq = fma(a.dampD[vi] * x, x, pq);
+      }
+      a.b_term[2 * pos] = pg;
+      a.b_term[2 * pos + 1] = pq;
+    }
+    grid.sync();
+    for (int sy = gw; sy < a.G; sy += nw) {
+      if (!(a.b_act[sy] & 1)) continue;
+      double sg = 0.0, sq = 0.0;
+      for (int pos = a.b_off[sy] + lane; pos < a.b_off[sy + 1]; pos += 32) {
+        sg += a.b_term[2 * pos];
+        sq += a.b_term[2 * pos + 1];
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        sg += __shfl_xor_sync(kFull, sg, o);
+        sq += __shfl_xor_sync(kFull, sq, o);
+      }
+      if (lane == 0) {
+        a.b_out[2 * sy] = -0.5 * sg + 0.5 * a.b_lam[sy] * sq;
+        a.b_out[2 * sy + 1] = (double)atomicAdd(a.b_status + sy, 0);
+      }
+    }
+    return;
+  }
   double gd = 0.0, dq = 0.0;
   for (int k = gt; k < n; k += gs) {
     const int pos = k / D, r = k % D;
@@ -1049,12 +1118,14 @@ __global__ void k_block_hessian(int nblk, const int32_t* __restrict__ blk_row, c
                                 const int32_t* __restrict__ perm, const int32_t* __restrict__ a_ptr,
                                 const int32_t* __restrict__ a_src, const double* __restrict__ Hd64,
                                 const double* __restrict__ fH64, const double* __restrict__ dampD,
-                                double* __restrict__ Hs, double* __restrict__ dampS) {
+                                double* __restrict__ Hs, double* __restrict__ dampS,
+                                const uint8_t* __restrict__ mask) {
   constexpr int dd = D * D;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= (int64_t)nblk * dd) return;
   const int p = (int)(t / dd), e = (int)(t % dd), r = e / D, c = e % D;
   const int j = blk_col[p];
+  if (mask && !(mask[j] & 1)) return;  // (a joint batch's graph not in this round)
   if (blk_row[p] == j) {
     const int v = perm[j];
     Hs[t] = Hd64[(size_t)v * dd + e];
@@ -1113,7 +1184,7 @@ CholDev::~CholDev() {
     if (e) cudaEventDestroy(e);
 }
 
-void chol_block_hessian(SolverDev& s, CholDev& c, cudaStream_t st) {
+void chol_block_hessian(SolverDev& s, CholDev& c, cudaStream_t st, const uint8_t* mask) {
   const int nblk = (int)c.plan.blk_row.size();
   if (nblk == 0) return;
   const int tb = 256;
@@ -1121,11 +1192,11 @@ void chol_block_hessian(SolverDev& s, CholDev& c, cudaStream_t st) {
   if (s.dim == 3)
     k_block_hessian<6><<<div_up(n, tb), tb, 0, st>>>(nblk, c.blk_row.get(), c.blk_col.get(), c.perm.get(),
                                                     c.a_ptr.get(), c.a_src.get(), s.Hd64.get(), s.fH64.get(),
-                                                    s.dampD.get(), c.Hs.get(), c.dampS.get());
+                                                    s.dampD.get(), c.Hs.get(), c.dampS.get(), mask);
   else
     k_block_hessian<3><<<div_up(n, tb), tb, 0, st>>>(nblk, c.blk_row.get(), c.blk_col.get(), c.perm.get(),
                                                     c.a_ptr.get(), c.a_src.get(), s.Hd64.get(), s.fH64.get(),
-                                                    s.dampD.get(), c.Hs.get(), c.dampS.get());
+                                                    s.dampD.get(), c.Hs.get(), c.dampS.get(), mask);
   RPGO_LAUNCHED();
 }
 
@@ -1148,6 +1219,26 @@ static int chol_grid(const SolverDev& s) {
   return s.coop_ctas > 0 ? std::min(s.coop_ctas, most) : most;
 }
 
+// kernel arguments of one solve (one system; the joint batch adds its own)
+static CholArgs make_args(SolverDev& s, CholDev& c, double lambda) {
+  const CholPlan& p = c.plan;
+  CholArgs a{s.N, p.n_sparse, p.T, p.n_tiles * kTB, p.n_tiles, c.levels,
+             c.perm.get(), c.col_ptr.get(), c.blk_row.get(), c.blk_col.get(), c.lvl_col_ptr.get(), c.lvl_cols.get(),
+             c.lvl_task_ptr.get(), c.tasks.get(), c.btask.get(), c.ftask.get(), c.upd_ptr.get(), c.upd_src.get(), c.tupd_ptr.get(),
+             c.tupd_src.get(), c.a_ptr.get(), c.a_src.get(), c.ta_ptr.get(), c.ta_src.get(), c.row_ptr.get(),
+             c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), c.ttasks.get(), c.ttask_ptr.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
+             s.g.get(), lambda, c.L.get(), c.Ldiag.get(),
+             c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.Spart.get(), c.Tpart.get(),
+             c.Hs.get(), c.dampS.get(), c.status.get()};
+  a.G = 0;
+  a.b_sys = a.b_off = nullptr;
+  a.b_act = nullptr;
+  a.b_lam = nullptr;
+  a.b_status = nullptr;
+  a.b_out = a.b_term = nullptr;
+  return a;
+}
+
 void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, double* host) {
   if (s.N == 0) {
     host[0] = 0.0;
@@ -1160,15 +1251,7 @@ void chol_enqueue(SolverDev& s, CholDev& c, double lambda, cudaStream_t st, doub
   }
   const int grid = chol_grid(s);
   c.part.resize((size_t)2 * grid);
-  const CholPlan& p = c.plan;
-  CholArgs a{s.N, p.n_sparse, p.T, p.n_tiles * kTB, p.n_tiles, c.levels,
-             c.perm.get(), c.col_ptr.get(), c.blk_row.get(), c.blk_col.get(), c.lvl_col_ptr.get(), c.lvl_cols.get(),
-             c.lvl_task_ptr.get(), c.tasks.get(), c.btask.get(), c.ftask.get(), c.upd_ptr.get(), c.upd_src.get(), c.tupd_ptr.get(),
-             c.tupd_src.get(), c.a_ptr.get(), c.a_src.get(), c.ta_ptr.get(), c.ta_src.get(), c.row_ptr.get(),
-             c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), c.ttasks.get(), c.ttask_ptr.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
-             s.g.get(), lambda, c.L.get(), c.Ldiag.get(),
-             c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.Spart.get(), c.Tpart.get(),
-             c.Hs.get(), c.dampS.get(), c.status.get()};
+  CholArgs a = make_args(s, c, lambda);
   void* args[] = {&a};
   RPGO_CUDA(cudaEventRecord(c.ev[0], st));
   if (s.dim == 3)
@@ -1209,14 +1292,7 @@ SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st) {
   const int grid = chol_grid(s);
   c.part.resize((size_t)2 * grid);
   const CholPlan& p = c.plan;
-  CholArgs a{s.N, p.n_sparse, p.T, p.n_tiles * kTB, p.n_tiles, c.levels,
-             c.perm.get(), c.col_ptr.get(), c.blk_row.get(), c.blk_col.get(), c.lvl_col_ptr.get(), c.lvl_cols.get(),
-             c.lvl_task_ptr.get(), c.tasks.get(), c.btask.get(), c.ftask.get(), c.upd_ptr.get(), c.upd_src.get(), c.tupd_ptr.get(),
-             c.tupd_src.get(), c.a_ptr.get(), c.a_src.get(), c.ta_ptr.get(), c.ta_src.get(), c.row_ptr.get(),
-             c.row_blk.get(), c.trow_ptr.get(), c.trow_blk.get(), c.ttasks.get(), c.ttask_ptr.get(), s.Hd64.get(), s.fH64.get(), s.dampD.get(),
-             s.g.get(), lambda, c.L.get(), c.Ldiag.get(),
-             c.M.get(), c.Ldd.get(), c.y.get(), s.delta.get(), c.part.get(), c.out.get(), c.Spart.get(), c.Tpart.get(),
-             c.Hs.get(), c.dampS.get(), c.status.get()};
+  CholArgs a = make_args(s, c, lambda);
   void* args[] = {&a};
   double ms = 0.0;
   {
@@ -1244,6 +1320,39 @@ SolveOut chol_solve(SolverDev& s, CholDev& c, double lambda, cudaStream_t st) {
   o.cg_iterations = 0;
   o.rel_residual = 0.0;
   return o;
+}
+
+void chol_enqueue_batch(SolverDev& s, CholDev& c, const BatchDev& b, cudaStream_t st) {
+  if (s.N == 0 || b.G == 0) return;
+  if (!c.ev[0]) {
+    RPGO_CUDA(cudaEventCreate(&c.ev[0]));
+    RPGO_CUDA(cudaEventCreate(&c.ev[1]));
+  }
+  const int grid = chol_grid(s);
+  c.part.resize((size_t)2 * grid);
+  CholArgs a = make_args(s, c, 0.0);
+  a.G = b.G;
+  a.b_sys = b.vsys.get();
+  a.b_off = b.voff.get();
+  a.b_act = b.ctl.get();
+  a.b_lam = b.lam.get();
+  a.b_status = b.status.get();
+  a.b_out = b.out.get();
+  a.b_term = b.term.get();
+  void* args[] = {&a};
+  RPGO_CUDA(cudaEventRecord(c.ev[0], st));
+  if (s.dim == 3)
+    RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_chol_solve<6>, grid, kThreads, args, 0, st));
+  else
+    RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_chol_solve<3>, grid, kThreads, args, 0, st));
+  RPGO_LAUNCHED();
+  RPGO_CUDA(cudaEventRecord(c.ev[1], st));
+}
+
+float chol_last_ms(CholDev& c) {
+  float ms = 0.f;
+  if (c.ev[0]) RPGO_CUDA(cudaEventElapsedTime(&ms, c.ev[0], c.ev[1]));
+  return ms;
 }
 
 }  // namespace rpgo

@@ -304,7 +304,7 @@ int find_block(const CholPlan& p, int col, int row) {
 }  // namespace
 
 CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
-                        const std::vector<int32_t>& vj) {
+                        const std::vector<int32_t>& vj, bool dense_tail) {
   CholPlan p;
   p.N = N;
   p.d = d;
@@ -339,7 +339,7 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
       std::sort(c.cols[j].begin(), c.cols[j].end());
     }
     // dense tail: the trailing columns whose structure is complete
-    while (c.T < N && (int)c.cols[N - 1 - c.T].size() == c.T) ++c.T;
+    while (dense_tail && c.T < N && (int)c.cols[N - 1 - c.T].size() == c.T) ++c.T;
     const int ns = N - c.T;
     std::vector<int32_t> lvl(ns, 0);
     int L = 0;
@@ -642,6 +642,125 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
               + 8.0 * d * N * 6.0;  // gradient, damping, rhs / solution, step, model change
   }
   return p;
+}
+
+CholPlan merge_chol_plans(const std::vector<CholPlan>& plans, const std::vector<int32_t>& foff) {
+  CholPlan u;
+  const int G = (int)plans.size();
+  if (G == 0) return u;
+  u.d = plans[0].d;
+  u.tile = plans[0].tile;
+  u.chunk = plans[0].chunk;
+  u.row_chunk = plans[0].row_chunk;
+  int L = 0;
+  for (const CholPlan& p : plans) {
+    if (p.T != 0 || p.d != u.d || p.chunk != u.chunk || p.row_chunk != u.row_chunk)
+      throw std::logic_error("merge_chol_plans: plans with dense tails or different block sizes");
+    L = std::max(L, p.levels());
+    u.N += p.N;
+    u.flops += p.flops;
+    u.bytes += p.bytes;
+  }
+  u.n_sparse = u.N;
+  u.T = 0;
+  u.n_tiles = 0;
+  // offsets of each plan's positions, blocks, slots, update pairs, Hessian
+  // sources and row entries in the merged arrays
+  std::vector<int32_t> voff(G + 1, 0), boff(G + 1, 0), soff(G + 1, 0), uoff(G + 1, 0), aoff(G + 1, 0),
+      roff(G + 1, 0);
+  for (int g = 0; g < G; ++g) {
+    const CholPlan& p = plans[g];
+    voff[g + 1] = voff[g] + p.N;
+    boff[g + 1] = boff[g] + p.n_blocks();
+    soff[g + 1] = soff[g] + p.n_slots;
+    uoff[g + 1] = uoff[g] + p.upd_ptr.back();
+    aoff[g + 1] = aoff[g] + p.a_ptr.back();
+    roff[g + 1] = roff[g] + p.row_ptr.back();
+  }
+  u.n_slots = soff[G];
+  const int nb = boff[G];
+  u.perm.resize(u.N);
+  u.pos.resize(u.N);
+  u.col_ptr.assign(u.N + 1, 0);
+  u.blk_row.resize(nb);
+  u.blk_col.resize(nb);
+  u.upd_ptr.assign(nb + 1, 0);
+  u.upd_src.resize((size_t)2 * uoff[G]);
+  u.a_ptr.assign(nb + 1, 0);
+  u.a_src.resize(aoff[G]);
+  u.row_ptr.assign(u.N + 1, 0);
+  u.row_blk.resize((size_t)2 * roff[G]);
+  u.btask.resize((size_t)2 * nb);
+  u.ftask.resize((size_t)2 * u.N);
+  for (int g = 0; g < G; ++g) {
+    const CholPlan& p = plans[g];
+    const int v0 = voff[g], b0 = boff[g], s0 = soff[g], u0 = uoff[g], a0 = aoff[g], r0 = roff[g];
+    for (int j = 0; j < p.N; ++j) {
+      u.perm[v0 + j] = p.perm[j] + v0;
+      u.pos[v0 + j] = p.pos[j] + v0;
+      u.col_ptr[v0 + j + 1] = p.col_ptr[j + 1] + b0;
+      u.row_ptr[v0 + j + 1] = p.row_ptr[j + 1] + r0;
+      u.ftask[2 * (v0 + j)] = p.ftask[2 * j] + s0;
+      u.ftask[2 * (v0 + j) + 1] = p.ftask[2 * j + 1];
+    }
+    for (int q = 0; q < p.n_blocks(); ++q) {
+      u.blk_row[b0 + q] = p.blk_row[q] + v0;
+      u.blk_col[b0 + q] = p.blk_col[q] + v0;
+      u.upd_ptr[b0 + q + 1] = p.upd_ptr[q + 1] + u0;
+      u.a_ptr[b0 + q + 1] = p.a_ptr[q + 1] + a0;
+      u.btask[2 * (b0 + q)] = p.btask[2 * q] + s0;
+      u.btask[2 * (b0 + q) + 1] = p.btask[2 * q + 1];
+    }
+    for (size_t k = 0; k < p.upd_src.size(); ++k) u.upd_src[(size_t)2 * u0 + k] = p.upd_src[k] + b0;
+    // Hessian sources 2 f + transposed: factor f of plan g is factor foff[g] + f
+    for (size_t k = 0; k < p.a_src.size(); ++k) u.a_src[a0 + k] = p.a_src[k] + 2 * foff[g];
+    for (size_t k = 0; k < p.row_blk.size(); k += 2) {
+      u.row_blk[(size_t)2 * r0 + k] = p.row_blk[k] + b0;
+      u.row_blk[(size_t)2 * r0 + k + 1] = p.row_blk[k + 1] + v0;
+    }
+  }
+  // levels: every plan's level l, then the level's columns by descending
+  // block count and its tasks by descending work (as make_chol_plan orders a
+  // level); independent items, so the order changes no result
+  u.lvl_col_ptr.assign(L + 1, 0);
+  u.lvl_task_ptr.assign(L + 1, 0);
+  u.lvl_cols.reserve(u.N);
+  for (int l = 0; l < L; ++l) {
+    const size_t c_begin = u.lvl_cols.size(), t_begin = u.tasks.size() / 4;
+    for (int g = 0; g < G; ++g) {
+      const CholPlan& p = plans[g];
+      if (l >= p.levels()) continue;
+      const int v0 = voff[g], b0 = boff[g], s0 = soff[g], u0 = uoff[g], r0 = roff[g];
+      for (int w = p.lvl_col_ptr[l]; w < p.lvl_col_ptr[l + 1]; ++w) u.lvl_cols.push_back(p.lvl_cols[w] + v0);
+      for (int t = p.lvl_task_ptr[l]; t < p.lvl_task_ptr[l + 1]; ++t) {
+        const int32_t* tk = &p.tasks[4 * (size_t)t];
+        const int kind = tk[3] & 3, low = tk[3] & 15, slot = tk[3] >> 4;
+        if (kind < 2) u.tasks.insert(u.tasks.end(), {tk[0] + b0, tk[1] + u0, tk[2] + u0, low | (slot + s0) << 4});
+        else u.tasks.insert(u.tasks.end(), {tk[0] + v0, tk[1] + r0, tk[2] + r0, low | (slot + s0) << 4});
+      }
+    }
+    std::stable_sort(u.lvl_cols.begin() + c_begin, u.lvl_cols.end(), [&](int32_t a, int32_t b) {
+      return u.col_ptr[a + 1] - u.col_ptr[a] > u.col_ptr[b + 1] - u.col_ptr[b];
+    });
+    const size_t t_end = u.tasks.size() / 4;
+    std::vector<std::array<int32_t, 4>> lt(t_end - t_begin);
+    for (size_t t = t_begin; t < t_end; ++t)
+      lt[t - t_begin] = {u.tasks[4 * t], u.tasks[4 * t + 1], u.tasks[4 * t + 2], u.tasks[4 * t + 3]};
+    auto work = [](const std::array<int32_t, 4>& x) {
+      const int kind = x[3] & 3, n = x[2] - x[1];
+      return kind == 2 ? n : 3 * n + (kind == 1 ? 1 : 0);
+    };
+    std::stable_sort(lt.begin(), lt.end(), [&](const auto& a, const auto& b) { return work(a) > work(b); });
+    for (size_t t = t_begin; t < t_end; ++t)
+      for (int k = 0; k < 4; ++k) u.tasks[4 * t + k] = lt[t - t_begin][k];
+    u.lvl_col_ptr[l + 1] = (int32_t)u.lvl_cols.size();
+    u.lvl_task_ptr[l + 1] = (int32_t)t_end;
+  }
+  u.tupd_ptr.assign(1, 0);
+  u.ta_ptr.assign(1, 0);
+  u.trow_ptr.assign(1, 0);
+  u.ttask_ptr.assign(1, 0);
+  return u;
 }
 
 }  // namespace rpgo

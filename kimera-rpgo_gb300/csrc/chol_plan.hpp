@@ -79,7 +79,16 @@ struct CholPlan {
 };
 
 // kind/vi/vj: the factor list (kind 0 = between vi-vj, 1 = prior on vi).
+// dense_tail false: every column sparse (T = 0), as merge_chol_plans needs.
 CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
-                        const std::vector<int32_t>& vj);
+                        const std::vector<int32_t>& vj, bool dense_tail = true);
+
+// One plan for independent systems (a joint batch of graphs), from their
+// plans without dense tails: plan g's positions and variables follow those
+// of plans 0 .. g-1, as do its blocks, slots and list entries; its factors
+// are foff[g] .. foff[g + 1] - 1 of the merged factor list. Level l holds
+// every plan's level l, ordered as make_chol_plan orders a level. Each
+// system's operations are those of its own plan.
+CholPlan merge_chol_plans(const std::vector<CholPlan>& plans, const std::vector<int32_t>& foff);
 
 }  // namespace rpgo

@@ -56,11 +56,12 @@ template <int DIM>
 __global__ void k_factor_err(int F, const int32_t* __restrict__ kind, const int32_t* __restrict__ vi,
                              const int32_t* __restrict__ vj, const double* __restrict__ z,
                              const double* __restrict__ R, const double* __restrict__ x,
-                             const double* __restrict__ w, double* __restrict__ ferr) {
+                             const double* __restrict__ w, double* __restrict__ ferr,
+                             const uint8_t* __restrict__ mask = nullptr, uint8_t bit = 0) {
   using L = SLie<DIM>;
   constexpr int d = L::d, st = L::stride;
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= F) return;
+  if (f >= F || (mask && !(mask[f] & bit))) return;
   typename L::Pose Xi, Z, rel;
   L::load(x + (size_t)vi[f] * st, Xi);
   L::load(z + (size_t)f * st, Z);
@@ -204,7 +205,8 @@ template <int DIM>
 __global__ void k_linearize_a(int F, const int32_t* __restrict__ kind, const int32_t* __restrict__ vi,
                               const int32_t* __restrict__ vj, const double* __restrict__ z,
                               const double* __restrict__ R, const double* __restrict__ x,
-                              const double* __restrict__ w, double* __restrict__ rec) {
+                              const double* __restrict__ w, double* __restrict__ rec,
+                              const uint8_t* __restrict__ mask) {
   using L = SLie<DIM>;
   constexpr int d = L::d, st = L::stride, dd = d * d, RS = d + 2 * dd + 1;
   // two threads per factor (the FP64 chain of one thread is the cost, and
@@ -213,7 +215,7 @@ __global__ void k_linearize_a(int F, const int32_t* __restrict__ kind, const int
   // Jacobian, role 0 the whitened residual and the adjoint
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int f = t >> 1, role = t & 1;
-  if (f >= F) return;
+  if (f >= F || (mask && !(mask[f] & 1))) return;
   const bool between = kind[f] == 0;
   typename L::Pose Xi, Z, rel, h;
   L::load(x + (size_t)vi[f] * st, Xi);
@@ -262,7 +264,7 @@ template <int DIM>
 __global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __restrict__ kind,
                                                      const double* __restrict__ R, const double* __restrict__ rec,
                                                      float* __restrict__ fH, double* __restrict__ fH64,
-                                                     double* __restrict__ fg) {
+                                                     double* __restrict__ fg, const uint8_t* __restrict__ mask) {
   constexpr int d = (DIM == 3) ? 6 : 3, dd = d * d, RS = d + 2 * dd + 1;
   constexpr int per_warp = 32 / d;  // factors per warp
   constexpr int warps = 4;
@@ -270,7 +272,7 @@ __global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __res
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int slot = lane / d, a = lane % d;
   const int f = (blockIdx.x * warps + warp) * per_warp + slot;
-  const bool active = slot < per_warp && f < F;
+  const bool active = slot < per_warp && f < F && (!mask || (mask[f] & 1));
   const double* rc = rec + (size_t)(active ? f : 0) * RS;
   const double* Rf = R + (size_t)(active ? f : 0) * dd;
   const bool between = active && kind[f] == 0;
@@ -415,10 +417,10 @@ template <int D>
 __global__ void k_assemble_direct(int N, const int32_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc_fac,
                                   const int8_t* __restrict__ inc_role, const double* __restrict__ fH64,
                                   const double* __restrict__ fg, double* __restrict__ Hd64, double* __restrict__ g,
-                                  double* __restrict__ dampD, int diag_damping) {
+                                  double* __restrict__ dampD, int diag_damping, const uint8_t* __restrict__ mask) {
   constexpr int dd = D * D;
   const int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (v >= N) return;
+  if (v >= N || (mask && !(mask[v] & 1))) return;
   const int e0 = lane, e1 = lane + 32;
   double h0 = 0.0, h1 = 0.0, gv = 0.0;
   for (int k = inc_ptr[v]; k < inc_ptr[v + 1]; ++k) {
@@ -558,10 +560,10 @@ struct CsrView {
 
 template <int DIM>
 __global__ void k_retract(int N, const double* __restrict__ x, const double* __restrict__ delta,
-                          double* __restrict__ xnew) {
+                          double* __restrict__ xnew, const uint8_t* __restrict__ mask = nullptr) {
   using L = SLie<DIM>;
   const int v = blockIdx.x * blockDim.x + threadIdx.x;
-  if (v >= N) return;
+  if (v >= N || (mask && !(mask[v] & 1))) return;
   typename L::Pose X, E, Y;
   L::load(x + (size_t)v * L::stride, X);
   L::exp(delta + (size_t)v * L::d, E);
@@ -570,28 +572,70 @@ __global__ void k_retract(int N, const double* __restrict__ x, const double* __r
 }
 
 // GncOptimizer::calculateWeights, TLS branch (Yang et al. 2020, eq. 14)
-__global__ void k_gnc_weights(int F, int n_known, const double* __restrict__ u2, const double* __restrict__ barc,
-                              double mu, double* __restrict__ w) {
-  const int f = blockIdx.x * blockDim.x + threadIdx.x;
-  if (f >= F) return;
-  if (f < n_known) {
-    w[f] = 1.0;
-    return;
-  }
-  const double b = barc[f], u = u2[f];
+__device__ __forceinline__ double tls_weight(double u, double b, double mu) {
   const double ub = (mu + 1.0) / mu * b;
   const double lb = mu / (mu + 1.0) * b;
   double wk = sqrt(b * mu * (mu + 1.0) / u) - mu;
   if (u >= ub || wk < 0.0) wk = 0.0;
   else if (u <= lb || wk > 1.0) wk = 1.0;
-  w[f] = wk;
+  return wk;
+}
+__global__ void k_gnc_weights(int F, int n_known, const double* __restrict__ u2, const double* __restrict__ barc,
+                              double mu, double* __restrict__ w) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= F) return;
+  w[f] = f < n_known ? 1.0 : tls_weight(u2[f], barc[f], mu);
+}
+
+// ------------------------------------------------------------------ joint batch
+// control word of each graph per variable and per factor
+__global__ void k_batch_masks(int N, int F, const int32_t* __restrict__ vsys, const int32_t* __restrict__ fsys,
+                              const uint8_t* __restrict__ ctl, uint8_t* __restrict__ vmask,
+                              uint8_t* __restrict__ fmask) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) vmask[i] = ctl[vsys[i]];
+  if (i < F) fmask[i] = ctl[fsys[i]];
+}
+
+// dst <- src on the rows (stride doubles) of the variables whose control word has `bit`
+__global__ void k_batch_copy(int64_t n, int stride, const uint8_t* __restrict__ vmask, uint8_t bit,
+                             const double* __restrict__ src, double* __restrict__ dst) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= n) return;
+  if (vmask[e / stride] & bit) dst[e] = src[e];
+}
+
+// TLS weights of the factors of graphs with kBatchGnc, each graph with its
+// own mu and known inliers (the first nknown factors of the graph)
+__global__ void k_batch_gnc(int F, const int32_t* __restrict__ fsys, const int32_t* __restrict__ foff,
+                            const int32_t* __restrict__ nknown, const uint8_t* __restrict__ fmask,
+                            const double* __restrict__ u2, const double* __restrict__ barc,
+                            const double* __restrict__ mu, double* __restrict__ w) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= F || !(fmask[f] & kBatchGnc)) return;
+  const int g = fsys[f];
+  w[f] = f - foff[g] < nknown[g] ? 1.0 : tls_weight(u2[f], barc[f], mu[g]);
+}
+
+// per graph: the sum of vals over [off[g], off[g + 1]) for the graphs whose
+// control word has `bit`; one warp per graph, lane-strided chains then a
+// fixed tree (the order depends on the graph only)
+__global__ void k_batch_sums(int G, const int32_t* __restrict__ off, const uint8_t* __restrict__ ctl, uint8_t bit,
+                             const double* __restrict__ vals, double* __restrict__ out) {
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (g >= G || !(ctl[g] & bit)) return;  // (warp-uniform)
+  double acc = 0.0;
+  for (int i = off[g] + lane; i < off[g + 1]; i += 32) acc += vals[i];
+#pragma unroll
+  for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) out[g] = acc;
 }
 
 }  // namespace
 
 // ------------------------------------------------------------------ host wrappers
 void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
-                   const std::vector<int32_t>& vj, int N, cudaStream_t st, bool direct) {
+                   const std::vector<int32_t>& vj, int N, cudaStream_t st, bool direct, CholPlan* given) {
   s.dim = dim;
   s.d = dim == 3 ? 6 : 3;
   s.stride = dim == 3 ? 12 : 4;
@@ -698,7 +742,7 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   s.out.resize(8);
   s.chol.reset();
   if (direct && N > 0) {
-    CholPlan plan = make_chol_plan(N, d, kind, vi, vj);
+    CholPlan plan = given ? std::move(*given) : make_chol_plan(N, d, kind, vi, vj);
     const double ntp = (double)plan.n_tiles * plan.tile;
     const double bytes = 8.0 * dd * (plan.n_blocks() + plan.n_sparse) + 8.0 * ntp * ntp +
                          4.0 * (plan.upd_src.size() + plan.tupd_src.size());
@@ -706,7 +750,7 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
       const double flops = plan.flops;
       s.chol = std::make_shared<CholDev>();
       s.chol->upload(std::move(plan), st);
-      s.race = flops > g_guard_flops.load() ? 1 : 0;
+      s.race = (!given && flops > g_guard_flops.load()) ? 1 : 0;
       s.pcg_chosen = false;
     }
   }
@@ -764,18 +808,18 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
     const int per_block = 4 * (32 / d);  // k_linearize_b: 4 warps of 32/d factors
     if (s.dim == 3) {
       k_linearize_a<3><<<div_up(2 * (int64_t)s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
-                                                       s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get());
+                                                       s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get(), nullptr);
       RPGO_LAUNCHED();
       k_linearize_b<3><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
                                                                need_pcg(s) ? s.fH.get() : nullptr, s.fH64.get(),
-                                                               s.fg.get());
+                                                               s.fg.get(), nullptr);
     } else {
       k_linearize_a<2><<<div_up(2 * (int64_t)s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
-                                                       s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get());
+                                                       s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get(), nullptr);
       RPGO_LAUNCHED();
       k_linearize_b<2><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
                                                                need_pcg(s) ? s.fH.get() : nullptr, s.fH64.get(),
-                                                               s.fg.get());
+                                                               s.fg.get(), nullptr);
     }
     RPGO_LAUNCHED();
   }
@@ -784,11 +828,11 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
     if (s.dim == 3)
       k_assemble_direct<6><<<blocks, tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
                                                   s.fH64.get(), s.fg.get(), s.Hd64.get(), s.g.get(), s.dampD.get(),
-                                                  diagonal_damping ? 1 : 0);
+                                                  diagonal_damping ? 1 : 0, nullptr);
     else
       k_assemble_direct<3><<<blocks, tb, 0, st>>>(s.N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(),
                                                   s.fH64.get(), s.fg.get(), s.Hd64.get(), s.g.get(), s.dampD.get(),
-                                                  diagonal_damping ? 1 : 0);
+                                                  diagonal_damping ? 1 : 0, nullptr);
     RPGO_LAUNCHED();
     chol_block_hessian(s, *s.chol, st);
     if (!s.race) return;
@@ -1312,6 +1356,67 @@ void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const double
   RPGO_LAUNCHED();
   k_gnc_weights<<<div_up(s.F, tb), tb, 0, st>>>(s.F, n_known, s.ferr.get(), barc, mu, s.weights.get());
   RPGO_LAUNCHED();
+}
+
+template <int DIM>
+static void batch_round_t(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st) {
+  constexpr int d = DIM == 3 ? 6 : 3;
+  const int tb = 128, N = s.N, F = s.F, stride = s.stride;
+  k_batch_masks<<<div_up(std::max(N, F), tb), tb, 0, st>>>(N, F, b.vsys.get(), b.fsys.get(), b.ctl.get(),
+                                                          b.vmask.get(), b.fmask.get());
+  RPGO_LAUNCHED();
+  const int64_t nx = (int64_t)N * stride;
+  // accept, GNC weights, reset, error at x: in this order
+  k_batch_copy<<<div_up(nx, 256), 256, 0, st>>>(nx, stride, b.vmask.get(), kBatchAccept, s.xnew.get(), s.x.get());
+  RPGO_LAUNCHED();
+  k_factor_err<DIM><<<div_up(F, tb), tb, 0, st>>>(F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                  s.sqrt_info.get(), s.x.get(), nullptr, s.ferr.get(), b.fmask.get(),
+                                                  kBatchGnc);
+  RPGO_LAUNCHED();
+  k_batch_gnc<<<div_up(F, tb), tb, 0, st>>>(F, b.fsys.get(), b.foff.get(), b.nknown.get(), b.fmask.get(),
+                                            s.ferr.get(), b.barc.get(), b.mu.get(), s.weights.get());
+  RPGO_LAUNCHED();
+  k_batch_copy<<<div_up(nx, 256), 256, 0, st>>>(nx, stride, b.vmask.get(), kBatchReset, s.x0.get(), s.x.get());
+  RPGO_LAUNCHED();
+  k_factor_err<DIM><<<div_up(F, tb), tb, 0, st>>>(F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                  s.sqrt_info.get(), s.x.get(), s.weights.get(), s.ferr.get(),
+                                                  b.fmask.get(), kBatchError);
+  RPGO_LAUNCHED();
+  k_batch_sums<<<div_up((int64_t)b.G * 32, tb), tb, 0, st>>>(b.G, b.foff.get(), b.ctl.get(), kBatchError,
+                                                            s.ferr.get(), b.err.get());
+  RPGO_LAUNCHED();
+  if (!any_active) return;
+  // linearise, solve, retract, error at xnew: the active graphs
+  const int rs = d + 2 * d * d + 1;
+  s.lin_rec.resize((size_t)F * rs);
+  k_linearize_a<DIM><<<div_up(2 * (int64_t)F, tb), tb, 0, st>>>(F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                                s.sqrt_info.get(), s.x.get(), s.weights.get(),
+                                                                s.lin_rec.get(), b.fmask.get());
+  RPGO_LAUNCHED();
+  k_linearize_b<DIM><<<div_up(F, 4 * (32 / d)), 128, 0, st>>>(F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
+                                                              nullptr, s.fH64.get(), s.fg.get(), b.fmask.get());
+  RPGO_LAUNCHED();
+  k_assemble_direct<d><<<div_up((int64_t)N * 32, tb), tb, 0, st>>>(
+      N, s.inc_ptr.get(), s.inc_fac.get(), s.inc_role.get(), s.fH64.get(), s.fg.get(), s.Hd64.get(), s.g.get(),
+      s.dampD.get(), diagonal_damping ? 1 : 0, b.vmask.get());
+  RPGO_LAUNCHED();
+  chol_block_hessian(s, *s.chol, st, b.vmask.get());
+  chol_enqueue_batch(s, *s.chol, b, st);
+  k_retract<DIM><<<div_up(N, tb), tb, 0, st>>>(N, s.x.get(), s.delta.get(), s.xnew.get(), b.vmask.get());
+  RPGO_LAUNCHED();
+  k_factor_err<DIM><<<div_up(F, tb), tb, 0, st>>>(F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+                                                  s.sqrt_info.get(), s.xnew.get(), s.weights.get(), s.ferr.get(),
+                                                  b.fmask.get(), kBatchActive);
+  RPGO_LAUNCHED();
+  k_batch_sums<<<div_up((int64_t)b.G * 32, tb), tb, 0, st>>>(b.G, b.foff.get(), b.ctl.get(), kBatchActive,
+                                                            s.ferr.get(), b.err.get() + b.G);
+  RPGO_LAUNCHED();
+}
+
+void batch_round(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st) {
+  if (!s.chol) throw std::logic_error("joint batch without a direct-solve plan");
+  if (s.dim == 3) batch_round_t<3>(s, b, diagonal_damping, any_active, st);
+  else batch_round_t<2>(s, b, diagonal_damping, any_active, st);
 }
 
 }  // namespace rpgo

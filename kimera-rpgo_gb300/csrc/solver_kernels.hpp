@@ -11,6 +11,34 @@
 namespace rpgo {
 
 struct CholDev;
+struct CholPlan;
+
+// Joint batch: G independent graphs held as one problem whose variables and
+// factors of graph s are contiguous ([voff[s], voff[s + 1]), [foff[s],
+// foff[s + 1])); the elimination positions of graph s are its variables'
+// range too. Each round works on the graphs selected by their control word:
+enum : uint8_t {
+  kBatchActive = 1,   // linearise, solve, retract and evaluate the new error
+  kBatchAccept = 2,   // first: x <- xnew (the last step was accepted)
+  kBatchGnc = 4,      // then: TLS weights from the residuals at x with mu
+  kBatchReset = 8,    // then: x <- x0 (an LM run from the initial values)
+  kBatchError = 16,   // then: the weighted error at x
+};
+struct BatchDev {
+  int G = 0;
+  std::vector<int32_t> h_voff, h_foff;
+  DeviceBuffer<int32_t> vsys, fsys;    // variable / factor -> graph
+  DeviceBuffer<int32_t> voff, foff;    // G + 1 each
+  DeviceBuffer<int32_t> nknown;        // per graph: known inliers (weights fixed at 1)
+  DeviceBuffer<uint8_t> ctl;           // per graph control word (kBatch*)
+  DeviceBuffer<uint8_t> vmask, fmask;  // the control word per variable / factor
+  DeviceBuffer<double> lam, mu;        // per graph damping and GNC parameter
+  DeviceBuffer<double> barc;           // per factor TLS threshold
+  DeviceBuffer<int32_t> status;        // per graph pivot failure
+  DeviceBuffer<double> out;            // per graph: model change, status (direct solve)
+  DeviceBuffer<double> term;           // per variable: model change partials
+  DeviceBuffer<double> err;            // per graph: error at x (kBatchError), at xnew (kBatchActive)
+};
 
 // Device-resident problem: factors, structure, per-iteration buffers.
 struct SolverDev {
@@ -73,8 +101,10 @@ struct SolveOut {
 // buffer; the caller fills z, sqrt_info and x0 (device gathers)
 // direct: plan the sparse Cholesky solve (else, or when its factor would
 // exceed the memory budget, the whole-GPU PCG solves the steps)
+// plan: a prepared plan for the direct solve (the joint batch's merged plan)
 void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, const std::vector<int32_t>& vi,
-                   const std::vector<int32_t>& vj, int N, cudaStream_t st, bool direct);
+                   const std::vector<int32_t>& vj, int N, cudaStream_t st, bool direct,
+                   CholPlan* plan = nullptr);
 // per-factor error 0.5 w |R e|^2 at values `x` (weights null = 1); returns the sum
 double solver_error(SolverDev& s, const double* x, const double* weights, cudaStream_t st);
 // per-factor unweighted errors at x into s.ferr (host copy returned)
@@ -102,5 +132,14 @@ double* enqueue_error_sum(SolverDev& s, const double* x, const double* weights, 
 // orders them before the next solve)
 void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const double* barc, double mu,
                         cudaStream_t st);
+
+// Joint batch rounds (s is the union problem, planned with its own CholPlan
+// from merge_chol_plans). batch_round enqueues, for the graphs selected by
+// the control words in b.ctl (already on the device): the accept / GNC /
+// reset updates of x and the weights, the error at x, then the linearisation,
+// the direct solve with each graph's damping b.lam, the retraction and the
+// error at xnew (any_active: some graph has kBatchActive). Results (b.out,
+// b.err) stay on the device.
+void batch_round(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st);
 
 }  // namespace rpgo

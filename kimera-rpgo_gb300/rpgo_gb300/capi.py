@@ -119,6 +119,7 @@ SIGNATURES = {
     "rpgo_g2o_free": (None, [_P]),
     "rpgo_solve_batch": (C.c_int, [C.POINTER(Params), C.c_int32, _P, _P, C.c_int32, C.c_int32,
                                    C.POINTER(BatchOut)]),
+    "rpgo_solve_batch_joint": (C.c_int, [C.POINTER(Params), C.c_int32, _P, _P, C.c_int32, C.POINTER(BatchOut)]),
     "rpgo_save_data": (C.c_int, [_P, C.c_char_p]),
     "rpgo_trajectory_scan_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [_P]),
     "rpgo_odometry_check_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [C.c_double, C.c_double,
@@ -428,10 +429,11 @@ def read_g2o(path: str, dim: int = 3):
         lib.rpgo_g2o_free(h)
 
 
-def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0):
-    """rpgo_solve_batch: solve independent graphs concurrently. Returns a
-    list of (status, keys, poses, gnc_weights, timing) per graph, the poses in
-    ascending key order as calculateEstimate() gives them."""
+def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0, joint: bool = False, group: int = 0):
+    """rpgo_solve_batch: solve independent graphs concurrently (joint: the
+    lock-step rpgo_solve_batch_joint with `group` graphs per group, 0 = all).
+    Returns a list of (status, keys, poses, gnc_weights, timing) per graph,
+    the poses in ascending key order as calculateEstimate() gives them."""
     n = len(graphs)
     batches = [Batch(g) for g in graphs]
     fb = (FactorBatch * max(n, 1))(*[b.f for b in batches])
@@ -447,10 +449,14 @@ def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0):
     timing = (Timing * max(n, 1))()
     out = BatchOut(_ptr(poses), _ptr(weights), _ptr(num_w), _ptr(status), C.cast(timing, C.c_void_p))
     p = params_struct(params)
-    rc = load().rpgo_solve_batch(C.byref(p), n, C.cast(fb, C.c_void_p), C.cast(vb, C.c_void_p), int(workers),
-                                 int(coop_ctas), C.byref(out))
+    if joint:
+        rc = load().rpgo_solve_batch_joint(C.byref(p), n, C.cast(fb, C.c_void_p), C.cast(vb, C.c_void_p), int(group),
+                                           C.byref(out))
+    else:
+        rc = load().rpgo_solve_batch(C.byref(p), n, C.cast(fb, C.c_void_p), C.cast(vb, C.c_void_p), int(workers),
+                                     int(coop_ctas), C.byref(out))
     if rc:
-        raise RpgoError(f"rpgo_solve_batch: {rc}")
+        raise RpgoError(f"rpgo_solve_batch{'_joint' if joint else ''}: {rc}")
     res, vo, fo = [], 0, 0
     for g in range(n):
         keys = np.sort(np.asarray(batches[g].a["value_keys"], dtype=np.uint64))

@@ -21,6 +21,7 @@ struct Emu {
   int d, dd, ntp;
   const double *Hd, *fH, *damp;
   double lam;
+  const double* lam_v = nullptr;  // per-variable damping (joint batch), else lam
   std::vector<double> L, Ldiag, M, Ldd, y;
   int fail = 0;
   Emu(const CholPlan& pl) : p(pl), d(pl.d), dd(pl.d * pl.d), ntp(pl.n_tiles * pl.tile) {}
@@ -28,7 +29,7 @@ struct Emu {
 
   double diag_entry(int v, int r, int c) {
     double s = Hd[(size_t)v * dd + r * d + c];
-    if (r == c) s += lam * damp[(size_t)v * d + r];
+    if (r == c) s += (lam_v ? lam_v[v] : lam) * damp[(size_t)v * d + r];
     return s;
   }
   double offdiag_entry(const std::vector<int32_t>& src, int beg, int end, int r, int c) {
@@ -276,16 +277,16 @@ struct Emu {
 
 }  // namespace
 
-extern "C" int chol_emulate(int N, int d, int F, const int32_t* kind, const int32_t* vi, const int32_t* vj,
-                            const double* Hd, const double* fH, const double* rhs, double lam, const double* damp,
-                            double* x_out, int32_t* info) {
-  std::vector<int32_t> k(kind, kind + F), a(vi, vi + F), b(vj, vj + F);
-  CholPlan p = rpgo::make_chol_plan(N, d, k, a, b);
+namespace {
+
+int emulate(const CholPlan& p, int N, int d, const double* Hd, const double* fH, const double* rhs, double lam,
+            const double* lam_v, const double* damp, double* x_out, int32_t* info) {
   Emu e(p);
   e.Hd = Hd;
   e.fH = fH;
   e.damp = damp;
   e.lam = lam;
+  e.lam_v = lam_v;
   const int dd = d * d, ns = p.n_sparse, nt = p.T * d, ntp = e.ntp, TB = p.tile;
   e.L.assign((size_t)p.n_blocks() * dd, 0.0);
   e.Ldiag.assign((size_t)ns * dd, 0.0);
@@ -341,4 +342,41 @@ extern "C" int chol_emulate(int N, int d, int F, const int32_t* kind, const int3
   info[3] = nT;
   info[4] = e.fail;
   return 0;
+}
+
+}  // namespace
+
+extern "C" int chol_emulate(int N, int d, int F, const int32_t* kind, const int32_t* vi, const int32_t* vj,
+                            const double* Hd, const double* fH, const double* rhs, double lam, const double* damp,
+                            double* x_out, int32_t* info) {
+  std::vector<int32_t> k(kind, kind + F), a(vi, vi + F), b(vj, vj + F);
+  CholPlan p = rpgo::make_chol_plan(N, d, k, a, b);
+  return emulate(p, N, d, Hd, fH, rhs, lam, nullptr, damp, x_out, info);
+}
+
+// The joint batch's plan: G independent systems (system g: Ns[g] variables
+// and Fs[g] factors, contiguous in the union arrays, indices global), each
+// planned without a dense tail and merged; system g damped by lam_g[g].
+extern "C" int chol_emulate_joint(int G, const int32_t* Ns, const int32_t* Fs, int d, const int32_t* kind,
+                                  const int32_t* vi, const int32_t* vj, const double* Hd, const double* fH,
+                                  const double* rhs, const double* lam_g, const double* damp, double* x_out,
+                                  int32_t* info) {
+  std::vector<CholPlan> plans(G);
+  std::vector<int32_t> foff(G + 1, 0);
+  std::vector<double> lam_v;
+  int v0 = 0;
+  for (int g = 0; g < G; ++g) {
+    const int f0 = foff[g];
+    foff[g + 1] = f0 + Fs[g];
+    std::vector<int32_t> k(kind + f0, kind + f0 + Fs[g]), a(Fs[g]), b(Fs[g]);
+    for (int f = 0; f < Fs[g]; ++f) {
+      a[f] = vi[f0 + f] - v0;
+      b[f] = vj[f0 + f] - v0;
+    }
+    plans[g] = rpgo::make_chol_plan(Ns[g], d, k, a, b, false);
+    lam_v.insert(lam_v.end(), Ns[g], lam_g[g]);
+    v0 += Ns[g];
+  }
+  CholPlan p = rpgo::merge_chol_plans(plans, foff);
+  return emulate(p, v0, d, Hd, fH, rhs, 0.0, lam_v.data(), damp, x_out, info);
 }

@@ -126,3 +126,35 @@ def test_plan_is_deterministic(emu):
     for x, _, info in runs[1:]:
         assert np.array_equal(x, runs[0][0])
         assert np.array_equal(info, runs[0][2])
+
+
+def test_emulated_joint_batch_plan_matches_dense(emu):
+    # the joint batch's merged plan: three graphs of different sizes and
+    # levels, planned without dense tails and merged, each damped with its
+    # own lambda; the emulated solve equals the dense solve of each graph
+    emu.chol_emulate_joint.restype = C.c_int
+    d = 6
+    sizes = [(300, 60, 21), (40, 0, 22), (120, 200, 23)]
+    lams = np.array([1e-3, 0.0, 10.0])
+    parts = [_system(N, d, _pose_graph(N, n_lc, seed), [0], seed) for N, n_lc, seed in sizes]
+    Ns = np.array([N for N, _, _ in sizes], np.int32)
+    Fs = np.array([len(pt[0]) for pt in parts], np.int32)
+    voff = np.concatenate([[0], np.cumsum(Ns)])
+    kind = np.concatenate([pt[0] for pt in parts]).astype(np.int32)
+    vi = np.concatenate([pt[1] + voff[g] for g, pt in enumerate(parts)]).astype(np.int32)
+    vj = np.concatenate([pt[2] + voff[g] for g, pt in enumerate(parts)]).astype(np.int32)
+    Hd = np.ascontiguousarray(np.concatenate([pt[3] for pt in parts]))
+    fH = np.ascontiguousarray(np.concatenate([pt[4] for pt in parts]))
+    damp = np.ascontiguousarray(np.concatenate([pt[6] for pt in parts]))
+    rhs = np.ascontiguousarray(np.concatenate([pt[7] for pt in parts]))
+    x = np.zeros(int(voff[-1]) * d)
+    info = np.zeros(5, np.int32)
+    p = lambda a: np.ascontiguousarray(a).ctypes.data_as(C.c_void_p)
+    emu.chol_emulate_joint(3, p(Ns), p(Fs), d, p(kind), p(vi), p(vj), p(Hd), p(fH), p(rhs), p(lams), p(damp),
+                           x.ctypes.data_as(C.c_void_p), info.ctypes.data_as(C.c_void_p))
+    assert info[4] == 0 and info[1] == 0 and info[0] == voff[-1]
+    for g, pt in enumerate(parts):
+        H, dmp, b = pt[5], pt[6], pt[7]
+        ref = np.linalg.solve(H + lams[g] * np.diag(dmp.reshape(-1)), b)
+        xg = x[voff[g] * d:voff[g + 1] * d]
+        assert np.allclose(xg, ref, rtol=1e-8, atol=1e-10 * np.abs(ref).max()), (g, np.abs(xg - ref).max())

@@ -12,7 +12,7 @@ import pytest
 
 from oracle import rpgo_oracle as O
 from rpgo_gb300 import capi, synth
-from rpgo_gb300.params import QUIET, RobustSolverParams
+from rpgo_gb300.params import GN, QUIET, RobustSolverParams
 
 ATE_TOL = 1e-4
 SIZES = [(200, 30, 10, 41), (350, 60, 20, 42), (500, 80, 30, 43), (300, 40, 0, 44), (450, 70, 35, 45),
@@ -29,6 +29,9 @@ def test_batch_argument_checks_need_no_gpu():
     assert lib.rpgo_solve_batch(C.byref(p), 0, None, None, 0, 0, None) == 0
     assert lib.rpgo_solve_batch(C.byref(p), -1, None, None, 0, 0, None) != 0
     assert lib.rpgo_solve_batch(C.byref(p), 2, None, None, 0, 0, None) != 0
+    assert lib.rpgo_solve_batch_joint(C.byref(p), 0, None, None, 0, None) == 0
+    assert lib.rpgo_solve_batch_joint(C.byref(p), -1, None, None, 0, None) != 0
+    assert lib.rpgo_solve_batch_joint(C.byref(p), 2, None, None, 0, None) != 0
 
 
 @pytest.mark.gpu
@@ -52,17 +55,70 @@ def test_batch_equals_individual_solves(workers, ctas):
         assert t.gnc_iterations > 0 and t.kernel_launches > 0
 
 
+def _check_against_oracle(params, graphs, res):
+    for s, (status, keys, poses, w, t) in zip(graphs, res):
+        assert status == 0
+        o = O.OracleSolver(params)
+        assert o.update(s.graph) == 0
+        ko, po = o.estimate()
+        assert np.array_equal(keys, ko)
+        assert np.array_equal(np.round(w), np.round(o.gnc_weights()))
+        assert synth.ate(poses, po, 3) <= ATE_TOL
+
+
 @pytest.mark.gpu
 def test_batch_graph_matches_oracle():
     from rpgo_gb300 import build
 
     build()
-    s = synth.walk3d(400, 60, 20, seed=48)
-    (status, keys, poses, w, t), = capi.solve_batch(_params(), [s.graph], workers=1, coop_ctas=16)
-    assert status == 0
-    o = O.OracleSolver(_params())
-    assert o.update(s.graph) == 0
-    ko, po = o.estimate()
-    assert np.array_equal(keys, ko)
-    assert np.array_equal(np.round(w), np.round(o.gnc_weights()))
-    assert synth.ate(poses, po, 3) <= ATE_TOL
+    graphs = [synth.walk3d(n, ni, no, seed=s) for n, ni, no, s in [(400, 60, 20, 48), (300, 50, 30, 49),
+                                                                 (550, 90, 20, 50)]]
+    res = capi.solve_batch(_params(), [s.graph for s in graphs], workers=2, coop_ctas=16)
+    _check_against_oracle(_params(), graphs, res)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("group", [0, 3])
+def test_joint_batch_matches_oracle_and_individual_solves(group):
+    # lock-step solves (one launch per stage over all graphs of a group): each
+    # graph's inlier set equals the oracle's and its own update's, poses
+    # within the oracle tolerance and close to its own update's (the error
+    # sums and the dense-tail-free plan round differently)
+    from rpgo_gb300 import build
+
+    build()
+    graphs = [synth.walk3d(n, ni, no, seed=s) for n, ni, no, s in SIZES]
+    res = capi.solve_batch(_params(), [s.graph for s in graphs], joint=True, group=group)
+    _check_against_oracle(_params(), graphs, res)
+    for s, (status, keys, poses, w, t) in zip(graphs, res):
+        g = capi.RobustSolver(_params())
+        assert g.update(s.graph) == 0
+        k1, p1 = g.estimate()
+        assert np.array_equal(keys, k1)
+        assert np.array_equal(np.round(w), np.round(g.gnc_weights()))
+        assert synth.ate(poses, p1, 3) <= ATE_TOL
+        assert t.gnc_iterations == g.timing().gnc_iterations
+        assert t.linear_solves > 0 and t.solve_ms > 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["gn", "lm_only", "bias_odom", "no_closures"])
+def test_joint_batch_modes_match_oracle(mode):
+    # Gauss-Newton under GNC, plain LM without GNC, GNC with odometry-biased
+    # first weights, and graphs whose closures PCM rejects entirely
+    from rpgo_gb300 import build
+
+    build()
+    p = _params()
+    sizes = SIZES[:4]
+    if mode == "gn":
+        p.setSolver(GN)
+    elif mode == "lm_only":
+        p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET)
+    elif mode == "bias_odom":
+        p.gnc_bias_odom = 1
+    else:
+        p = RobustSolverParams().setPcm3DParams(0.0, 0.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+    graphs = [synth.walk3d(n, ni, no, seed=s) for n, ni, no, s in sizes]
+    res = capi.solve_batch(p, [s.graph for s in graphs], joint=True)
+    _check_against_oracle(p, graphs, res)
