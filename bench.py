@@ -728,19 +728,21 @@ def run_batch512(args):
     per = 64
     chunks = [graphs[i:i + per] for i in range(0, 512, per)]
     tuned = None
-    if args.workers <= 0:
-        # autotune workers and CTA budget on 24 graphs drawn from across the batch
-        w_, c_, tuned = capi.autotune_batch(params, graphs[::21][:24])
-        args.workers, args.coop_ctas = w_, c_
+    if args.workers > 0:
+        cfg = {"workers": args.workers, "coop_ctas": args.coop_ctas}
+    else:
+        # autotune the form (worker threads or lock-step groups) and its sizes
+        # on 24 graphs drawn from across the batch
+        cfg, tuned = capi.autotune_batch(params, graphs[::21][:24])
     for w in range(args.warmup):
-        capi.solve_batch(params, chunks[w % len(chunks)][:16], workers=args.workers, coop_ctas=args.coop_ctas)
+        capi.solve_batch(params, chunks[w % len(chunks)][:16], **cfg)
     times, n = [], 0
     with ClockSampler(0) as clocks:
         for k in range(args.steps):
             chunk = chunks[k % len(chunks)]
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            res = capi.solve_batch(params, chunk, workers=args.workers, coop_ctas=args.coop_ctas)
+            res = capi.solve_batch(params, chunk, **cfg)
             times.append(time.perf_counter() - t0)
             assert all(r[0] == 0 for r in res)
             n += len(chunk)
@@ -749,10 +751,10 @@ def run_batch512(args):
             "warmup": args.warmup, "ms_per_step": 1000.0 * sec / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded 3d random walks)",
             "config": {"workload": "batch of 512 independent graphs (200-8000 poses, closures 10-30 %, outlier rate "
-                                   "U[0, 0.5]); a step = 64 graphs through rpgo_solve_batch",
+                                   "U[0, 0.5]); a step = 64 graphs through rpgo_solve_batch or rpgo_solve_batch_joint",
                        "graphs_timed": n, "poses_timed": int(sum(sz[0] for sz in sizes[:n])) if n <= 512 else None,
-                       "workers": args.workers, "coop_ctas": args.coop_ctas,
-                       "autotune_s": {f"{w}x{c}": round(t, 3) for (w, c), t in tuned.items()} if tuned else None,
+                       "batch_form": cfg,
+                       "autotune_s": {k: round(t, 3) for k, t in tuned.items()} if tuned else None,
                        "l2": "not flushed: every step's graphs arrive from host memory",
                        "parallelism": "single GPU, concurrent graphs"},
             "clocks": clocks.summary()}

@@ -379,12 +379,20 @@ int rpgo_solve_batch(const rpgo_params* p, int32_t n, const rpgo_factor_batch* f
  * together, one damped solve per graph per round, and every stage of a round
  * (linearisation, block Hessian, the direct solve, retraction, errors, TLS
  * weights) is one launch over all graphs, each graph with its own damping
- * and decisions. `group`: graphs per lock-step group (0: all). Graphs whose
- * solve needs the solver's own path (temporary values, a warm start, the PCG
- * solver) are solved by it. Outputs as rpgo_solve_batch; timing.solve_ms is
- * the wall time of the graph's group. */
+ * and decisions. Graphs are grouped by size; `streams` groups (0: 4) run
+ * concurrently on their own streams, each group of `group` graphs (0: the
+ * graphs shared evenly over the streams). Graphs whose solve needs the
+ * solver's own path (temporary values, a warm start, the PCG solver) are
+ * solved by it. Outputs as rpgo_solve_batch; timing.solve_ms is the wall
+ * time of the graph's group. */
 int rpgo_solve_batch_joint(const rpgo_params* p, int32_t n, const rpgo_factor_batch* factors,
-                           const rpgo_value_batch* values, int32_t group, rpgo_batch_out* out);
+                           const rpgo_value_batch* values, int32_t group, int32_t streams, rpgo_batch_out* out);
+/* The joint batch replays each round from one captured CUDA graph (on = 1,
+ * the default) or launches its stages one by one (on = 0); process-wide.
+ * Returns the previous setting. */
+int32_t rpgo_set_joint_graphs(int32_t on);
+/* Rounds of joint batches replayed from a captured graph so far (process-wide). */
+int64_t rpgo_joint_graph_rounds(void);
 
 /* ------------------------------------------------------------ stage kernels
  * Device-resident entry points of the hot path, one per reference function

@@ -16,7 +16,9 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cstdio>
 #include <cstring>
+#include <exception>
 #include <thread>
 #include <vector>
 
@@ -31,6 +33,8 @@ void set_coop_ctas(rpgo_solver* s, int ctas);
 namespace {
 
 constexpr int kDefaultWorkers = 16;
+// concurrent lock-step groups of the joint batch
+constexpr int kDefaultJointStreams = 4;
 // co-resident CTAs of the direct solve per SM (256 threads x 128 registers)
 constexpr int kCholCtasPerSm = 2;
 
@@ -139,7 +143,8 @@ extern "C" int rpgo_solve_batch(const rpgo_params* p, int32_t n, const rpgo_fact
 }
 
 extern "C" int rpgo_solve_batch_joint(const rpgo_params* p, int32_t n, const rpgo_factor_batch* factors,
-                                      const rpgo_value_batch* values, int32_t group, rpgo_batch_out* out) {
+                                      const rpgo_value_batch* values, int32_t group, int32_t streams,
+                                      rpgo_batch_out* out) {
   if (!p || n < 0 || (n > 0 && (!factors || !values || !out || !out->poses || !out->status))) return RPGO_ERR_ARG;
   if (n == 0) return RPGO_OK;
   const int dim = batch_dim(p);
@@ -165,7 +170,8 @@ extern "C" int rpgo_solve_batch_joint(const rpgo_params* p, int32_t n, const rpg
     if (rc[g] != RPGO_OK) return;
     try {
       kind[g] = rpgo::joint_prepare(sv[g], &jp[g]);
-    } catch (...) {
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "rpgo_solve_batch_joint: graph %d: %s\n", g, e.what());
       rc[g] = RPGO_ERR_CUDA;
     }
   });
@@ -174,37 +180,51 @@ extern "C" int rpgo_solve_batch_joint(const rpgo_params* p, int32_t n, const rpg
     if (rc[g] == RPGO_OK && kind[g] == rpgo::kJointOwn) {
       try {
         rc[g] = rpgo::joint_optimize_own(sv[g], &solve_ms[g]);
-      } catch (...) {
+      } catch (const std::exception& e) {
+        std::fprintf(stderr, "rpgo_solve_batch_joint: graph %d: %s\n", g, e.what());
         rc[g] = RPGO_ERR_CUDA;
       }
     }
   });
-  // 3. the rest in lock-step groups
+  // 3. the rest in lock-step groups of graphs of similar size (similar
+  // numbers of rounds), several groups concurrently, each on its own stream
+  // and a share of the SMs for its direct solve
   std::vector<int> joint;
   for (int g = 0; g < n; ++g)
     if (rc[g] == RPGO_OK && kind[g] == rpgo::kJointSolve) joint.push_back(g);
-  const int gsz = group > 0 ? group : std::max(1, (int)joint.size());
-  cudaStream_t st = nullptr;
-  if (!joint.empty() && cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+  std::stable_sort(joint.begin(), joint.end(), [&](int a, int b) { return values[a].count > values[b].count; });
+  const int nj = (int)joint.size();
+  const int ns = std::max(1, std::min(nj, streams > 0 ? (int)streams : kDefaultJointStreams));
+  const int gsz = group > 0 ? (int)group : std::max(1, (nj + ns - 1) / ns);
+  const int ngroups = nj > 0 ? (nj + gsz - 1) / gsz : 0;
+  int sms = 0;
+  try {
+    sms = rpgo::device_sm_count();
+  } catch (const rpgo::CudaError&) {
     for (int g : joint) rc[g] = RPGO_ERR_CUDA;
-    joint.clear();
   }
-  if (!joint.empty()) {
-    for (size_t b0 = 0; b0 < joint.size(); b0 += gsz) {
-      const size_t b1 = std::min(joint.size(), b0 + gsz);
-      std::vector<rpgo::JointProblem*> probs;
-      for (size_t k = b0; k < b1; ++k) probs.push_back(&jp[joint[k]]);
-      try {
-        const auto t0 = std::chrono::steady_clock::now();
-        rpgo::solve_joint(dim, probs, st);
-        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-        for (size_t k = b0; k < b1; ++k) solve_ms[joint[k]] = ms;
-      } catch (...) {
-        for (size_t k = b0; k < b1; ++k) rc[joint[k]] = RPGO_ERR_CUDA;
-      }
+  const int conc = std::min(ns, std::max(1, ngroups));
+  const int ctas = conc > 1 ? std::max(1, kCholCtasPerSm * sms / conc) : 0;
+  parallel_for(sms > 0 ? ngroups : 0, conc, [&](int k) {
+    const int b0 = k * gsz, b1 = std::min(nj, b0 + gsz);
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+      for (int i = b0; i < b1; ++i) rc[joint[i]] = RPGO_ERR_CUDA;
+      return;
+    }
+    std::vector<rpgo::JointProblem*> probs;
+    for (int i = b0; i < b1; ++i) probs.push_back(&jp[joint[i]]);
+    try {
+      const auto t0 = std::chrono::steady_clock::now();
+      rpgo::solve_joint(dim, probs, st, ctas);
+      const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      for (int i = b0; i < b1; ++i) solve_ms[joint[i]] = ms;
+    } catch (const std::exception& e) {
+      std::fprintf(stderr, "rpgo_solve_batch_joint: group of %d graphs failed: %s\n", b1 - b0, e.what());
+      for (int i = b0; i < b1; ++i) rc[joint[i]] = RPGO_ERR_CUDA;
     }
     cudaStreamDestroy(st);
-  }
+  });
   // 4. bookkeeping and outputs
   parallel_for(n, threads, [&](int g) {
     if (!sv[g]) {
@@ -220,3 +240,7 @@ extern "C" int rpgo_solve_batch_joint(const rpgo_params* p, int32_t n, const rpg
   });
   return RPGO_OK;
 }
+
+extern "C" int32_t rpgo_set_joint_graphs(int32_t on) { return rpgo::set_joint_graphs(on != 0) ? 1 : 0; }
+
+extern "C" int64_t rpgo_joint_graph_rounds(void) { return rpgo::joint_graph_rounds(); }

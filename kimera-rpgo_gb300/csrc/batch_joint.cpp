@@ -16,6 +16,9 @@ namespace rpgo {
 
 namespace {
 
+std::atomic<bool> g_joint_graphs{true};         // capture the round as a CUDA graph
+std::atomic<int64_t> g_joint_graph_rounds{0};   // rounds replayed from a graph (process-wide)
+
 struct Local {  // one graph in the union's numbering
   std::vector<int32_t> kind, vi, vj;
   std::vector<int64_t> frows, vrows;
@@ -60,12 +63,11 @@ struct Graph {
   bool gnc_pending = false;     // TLS weights at the start of the next round
   bool need_weights = false;    // download this graph's weights after the next round
   std::vector<double> w;        // host copy of the weights of the current GNC stage
-  uint8_t ctl = 0;
 };
 
 }  // namespace
 
-int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st) {
+int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st, int coop_ctas) {
   const int G = (int)probs.size();
   if (G == 0) return 0;
   const int d = dim == 3 ? 6 : 3, stride = dim == 3 ? 12 : 4;
@@ -123,6 +125,7 @@ int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st) {
   CholPlan merged = merge_chol_plans(plans, b.h_foff);
   plans.clear();
   SolverDev u;
+  u.coop_ctas = coop_ctas;
   solver_upload(u, dim, kind, vi, vj, N, st, true, &merged);
   if (!u.chol) throw std::runtime_error("joint batch: the merged factor exceeds the direct solver's memory budget");
   std::vector<DeviceBuffer<int64_t>> vrows(G);
@@ -282,9 +285,77 @@ int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st) {
     outer_end(x);
   };
 
-  for (Graph& x : gs) lm_begin(x);
   int rounds = 0;
-  std::vector<double> wall;
+  // One round's device work: the control words, dampings and mu in, the
+  // stages before the direct solve; the direct solve; the stages after it and
+  // the per-graph results out. The stages before and after are replayed
+  // from two captured CUDA graphs once the buffers have their sizes (after
+  // the first round; the host arrays are page-locked and fixed); the direct
+  // solve, a cooperative launch, is launched on its own between them. If a
+  // capture or instantiation is refused, the stages launch one by one.
+  auto enqueue_pre = [&](bool any_active) {
+    RPGO_CUDA(cudaMemcpyAsync(b.ctl.get(), ctl, G, cudaMemcpyHostToDevice, st));
+    RPGO_CUDA(cudaMemcpyAsync(b.lam.get(), lam, G * sizeof(double), cudaMemcpyHostToDevice, st));
+    RPGO_CUDA(cudaMemcpyAsync(b.mu.get(), mus, G * sizeof(double), cudaMemcpyHostToDevice, st));
+    batch_round_pre(u, b, probs[0]->lm.diagonal_damping, any_active, st);
+  };
+  auto enqueue_post = [&] {
+    batch_round_post(u, b, st);
+    RPGO_CUDA(cudaMemcpyAsync(res, b.err.get(), 2 * G * sizeof(double), cudaMemcpyDeviceToHost, st));
+    RPGO_CUDA(cudaMemcpyAsync(res + 2 * G, b.out.get(), 2 * G * sizeof(double), cudaMemcpyDeviceToHost, st));
+  };
+  cudaGraphExec_t exec_pre = nullptr, exec_post = nullptr;
+  bool use_graph = g_joint_graphs.load();
+  int64_t graph_launches = 0;
+  auto capture = [&](auto&& enqueue) -> cudaGraphExec_t {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t e = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return nullptr;
+    }
+    bool ok = true;
+    try {
+      enqueue();
+    } catch (const CudaError&) {
+      ok = false;
+    }
+    const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+    ok = ok && ec == cudaSuccess && graph != nullptr;
+    if (ok && cudaGraphInstantiate(&e, graph, 0) != cudaSuccess) {
+      ok = false;
+      e = nullptr;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    (void)cudaGetLastError();
+    return ok ? e : nullptr;
+  };
+  auto run_round = [&](bool any_active) {
+    if (any_active && use_graph && rounds >= 1 && !exec_pre) {
+      exec_pre = capture([&] { enqueue_pre(true); });
+      exec_post = exec_pre ? capture(enqueue_post) : nullptr;
+      if (!exec_pre || !exec_post) {
+        use_graph = false;
+        if (exec_pre) cudaGraphExecDestroy(exec_pre);
+        if (exec_post) cudaGraphExecDestroy(exec_post);
+        exec_pre = exec_post = nullptr;
+      }
+    }
+    if (any_active && exec_pre) {
+      RPGO_CUDA(cudaGraphLaunch(exec_pre, st));
+      batch_round_solve(u, b, st);
+      RPGO_CUDA(cudaGraphLaunch(exec_post, st));
+      ++graph_launches;
+    } else {
+      enqueue_pre(any_active);
+      if (any_active) {
+        batch_round_solve(u, b, st);
+        enqueue_post();
+      }
+    }
+  };
+
+  for (Graph& x : gs) lm_begin(x);
   for (;;) {
     bool any_active = false, any_ctl = false, any_w = false;
     for (int g = 0; g < G; ++g) {
@@ -307,16 +378,15 @@ int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st) {
       any_w = any_w || x.need_weights;
     }
     if (!any_ctl) break;
-    RPGO_CUDA(cudaMemcpyAsync(b.ctl.get(), ctl, G, cudaMemcpyHostToDevice, st));
-    RPGO_CUDA(cudaMemcpyAsync(b.lam.get(), lam, G * sizeof(double), cudaMemcpyHostToDevice, st));
-    RPGO_CUDA(cudaMemcpyAsync(b.mu.get(), mus, G * sizeof(double), cudaMemcpyHostToDevice, st));
-    batch_round(u, b, probs[0]->lm.diagonal_damping, any_active, st);
-    RPGO_CUDA(cudaMemcpyAsync(res, b.err.get(), 2 * G * sizeof(double), cudaMemcpyDeviceToHost, st));
-    RPGO_CUDA(cudaMemcpyAsync(res + 2 * G, b.out.get(), 2 * G * sizeof(double), cudaMemcpyDeviceToHost, st));
+    run_round(any_active);
     double* hwp = nullptr;
-    if (any_w) {
+    if (any_w) {  // the weight slices of the graphs that start a GNC stage
       hwp = hw.get(F);
-      RPGO_CUDA(cudaMemcpyAsync(hwp, u.weights.get(), (size_t)F * sizeof(double), cudaMemcpyDeviceToHost, st));
+      for (int g = 0; g < G; ++g)
+        if (gs[g].need_weights)
+          RPGO_CUDA(cudaMemcpyAsync(hwp + b.h_foff[g], u.weights.get() + b.h_foff[g],
+                                    (size_t)(b.h_foff[g + 1] - b.h_foff[g]) * sizeof(double), cudaMemcpyDeviceToHost,
+                                    st));
     }
     RPGO_CUDA(cudaStreamSynchronize(st));
     if (any_active) {
@@ -366,7 +436,13 @@ int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st) {
     probs[g]->weights.assign(wf.begin() + b.h_foff[g], wf.begin() + b.h_foff[g + 1]);
   }
   RPGO_CUDA(cudaStreamSynchronize(st));
+  if (exec_pre) cudaGraphExecDestroy(exec_pre);
+  if (exec_post) cudaGraphExecDestroy(exec_post);
+  g_joint_graph_rounds.fetch_add(graph_launches);
   return rounds;
 }
+
+bool set_joint_graphs(bool on) { return g_joint_graphs.exchange(on); }
+int64_t joint_graph_rounds() { return g_joint_graph_rounds.load(); }
 
 }  // namespace rpgo

@@ -42,9 +42,16 @@ struct JointProblem {
 };
 
 // Solves every problem (same dim, same LM / GNC parameters apart from the
-// known-inlier counts and first weights) in lock-step rounds on stream st.
-// Returns the number of rounds.
-int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st);
+// known-inlier counts and first weights) in lock-step rounds on stream st,
+// the direct solve on coop_ctas CTAs (0: every co-resident CTA). Returns the
+// number of rounds.
+int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st, int coop_ctas = 0);
+
+// Rounds are replayed from one captured CUDA graph (set_joint_graphs(false):
+// launched stage by stage); returns the previous setting.
+bool set_joint_graphs(bool on);
+// rounds replayed from a captured graph so far (process-wide)
+int64_t joint_graph_rounds();
 
 // The solver side (capi.cpp). joint_prepare: the problem that
 // RobustSolver::optimize would solve after the last update (made with

@@ -1359,7 +1359,7 @@ void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const double
 }
 
 template <int DIM>
-static void batch_round_t(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st) {
+static void batch_pre_t(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st) {
   constexpr int d = DIM == 3 ? 6 : 3;
   const int tb = 128, N = s.N, F = s.F, stride = s.stride;
   k_batch_masks<<<div_up(std::max(N, F), tb), tb, 0, st>>>(N, F, b.vsys.get(), b.fsys.get(), b.ctl.get(),
@@ -1401,7 +1401,11 @@ static void batch_round_t(SolverDev& s, BatchDev& b, bool diagonal_damping, bool
       s.dampD.get(), diagonal_damping ? 1 : 0, b.vmask.get());
   RPGO_LAUNCHED();
   chol_block_hessian(s, *s.chol, st, b.vmask.get());
-  chol_enqueue_batch(s, *s.chol, b, st);
+}
+
+template <int DIM>
+static void batch_post_t(SolverDev& s, BatchDev& b, cudaStream_t st) {
+  const int tb = 128, N = s.N, F = s.F;
   k_retract<DIM><<<div_up(N, tb), tb, 0, st>>>(N, s.x.get(), s.delta.get(), s.xnew.get(), b.vmask.get());
   RPGO_LAUNCHED();
   k_factor_err<DIM><<<div_up(F, tb), tb, 0, st>>>(F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
@@ -1413,10 +1417,17 @@ static void batch_round_t(SolverDev& s, BatchDev& b, bool diagonal_damping, bool
   RPGO_LAUNCHED();
 }
 
-void batch_round(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st) {
+void batch_round_pre(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st) {
   if (!s.chol) throw std::logic_error("joint batch without a direct-solve plan");
-  if (s.dim == 3) batch_round_t<3>(s, b, diagonal_damping, any_active, st);
-  else batch_round_t<2>(s, b, diagonal_damping, any_active, st);
+  if (s.dim == 3) batch_pre_t<3>(s, b, diagonal_damping, any_active, st);
+  else batch_pre_t<2>(s, b, diagonal_damping, any_active, st);
+}
+
+void batch_round_solve(SolverDev& s, BatchDev& b, cudaStream_t st) { chol_enqueue_batch(s, *s.chol, b, st); }
+
+void batch_round_post(SolverDev& s, BatchDev& b, cudaStream_t st) {
+  if (s.dim == 3) batch_post_t<3>(s, b, st);
+  else batch_post_t<2>(s, b, st);
 }
 
 }  // namespace rpgo

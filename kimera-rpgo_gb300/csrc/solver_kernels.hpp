@@ -134,12 +134,15 @@ void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const double
                         cudaStream_t st);
 
 // Joint batch rounds (s is the union problem, planned with its own CholPlan
-// from merge_chol_plans). batch_round enqueues, for the graphs selected by
-// the control words in b.ctl (already on the device): the accept / GNC /
-// reset updates of x and the weights, the error at x, then the linearisation,
-// the direct solve with each graph's damping b.lam, the retraction and the
-// error at xnew (any_active: some graph has kBatchActive). Results (b.out,
+// from merge_chol_plans), for the graphs selected by the control words in
+// b.ctl (already on the device). batch_round_pre: the accept / GNC / reset
+// updates of x and the weights, the error at x, then (any_active: some graph
+// has kBatchActive) the linearisation and block Hessian; batch_round_solve:
+// the cooperative direct solve with each graph's damping b.lam;
+// batch_round_post: the retraction and the error at xnew. Results (b.out,
 // b.err) stay on the device.
-void batch_round(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st);
+void batch_round_pre(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st);
+void batch_round_solve(SolverDev& s, BatchDev& b, cudaStream_t st);
+void batch_round_post(SolverDev& s, BatchDev& b, cudaStream_t st);
 
 }  // namespace rpgo

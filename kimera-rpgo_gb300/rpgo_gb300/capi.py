@@ -119,7 +119,10 @@ SIGNATURES = {
     "rpgo_g2o_free": (None, [_P]),
     "rpgo_solve_batch": (C.c_int, [C.POINTER(Params), C.c_int32, _P, _P, C.c_int32, C.c_int32,
                                    C.POINTER(BatchOut)]),
-    "rpgo_solve_batch_joint": (C.c_int, [C.POINTER(Params), C.c_int32, _P, _P, C.c_int32, C.POINTER(BatchOut)]),
+    "rpgo_solve_batch_joint": (C.c_int, [C.POINTER(Params), C.c_int32, _P, _P, C.c_int32, C.c_int32,
+                                         C.POINTER(BatchOut)]),
+    "rpgo_set_joint_graphs": (C.c_int32, [C.c_int32]),
+    "rpgo_joint_graph_rounds": (C.c_int64, []),
     "rpgo_save_data": (C.c_int, [_P, C.c_char_p]),
     "rpgo_trajectory_scan_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [_P]),
     "rpgo_odometry_check_dev": (C.c_int, [C.c_int32, C.c_int32, C.c_int64] + [_P] * 8 + [C.c_double, C.c_double,
@@ -429,9 +432,11 @@ def read_g2o(path: str, dim: int = 3):
         lib.rpgo_g2o_free(h)
 
 
-def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0, joint: bool = False, group: int = 0):
+def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0, joint: bool = False, group: int = 0,
+                streams: int = 0):
     """rpgo_solve_batch: solve independent graphs concurrently (joint: the
-    lock-step rpgo_solve_batch_joint with `group` graphs per group, 0 = all).
+    lock-step rpgo_solve_batch_joint, `streams` concurrent groups of `group`
+    graphs; 0 = defaults).
     Returns a list of (status, keys, poses, gnc_weights, timing) per graph,
     the poses in ascending key order as calculateEstimate() gives them."""
     n = len(graphs)
@@ -451,7 +456,7 @@ def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0, joint: boo
     p = params_struct(params)
     if joint:
         rc = load().rpgo_solve_batch_joint(C.byref(p), n, C.cast(fb, C.c_void_p), C.cast(vb, C.c_void_p), int(group),
-                                           C.byref(out))
+                                           int(streams), C.byref(out))
     else:
         rc = load().rpgo_solve_batch(C.byref(p), n, C.cast(fb, C.c_void_p), C.cast(vb, C.c_void_p), int(workers),
                                      int(coop_ctas), C.byref(out))
@@ -467,26 +472,44 @@ def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0, joint: boo
     return res
 
 
-def autotune_batch(params, graphs, candidates=((8, 0), (4, 0), (6, 0), (12, 0), (8, 76), (8, 19)), margin=0.05):
-    """Pick the (workers, coop_ctas) of rpgo_solve_batch that solves a sample
-    of graphs fastest (wall clock, after one warm-up run of the sample); the
-    first candidate is kept unless another is faster by more than `margin`
-    (timing noise on a small sample). Returns (workers, coop_ctas,
-    {config: seconds})."""
+BATCH_CANDIDATES = (
+    {"workers": 8}, {"workers": 4}, {"workers": 12}, {"workers": 8, "coop_ctas": 76}, {"workers": 8, "coop_ctas": 19},
+    {"joint": True, "streams": 1}, {"joint": True, "streams": 2}, {"joint": True, "streams": 4},
+    {"joint": True, "streams": 8}, {"joint": True, "streams": 4, "group": 4},
+)
+
+
+def _config_name(c):
+    if c.get("joint"):
+        return f"joint_s{c.get('streams', 0)}_g{c.get('group', 0)}"
+    return f"workers{c.get('workers', 0)}_ctas{c.get('coop_ctas', 0)}"
+
+
+def autotune_batch(params, graphs, candidates=BATCH_CANDIDATES, margin=0.05):
+    """Pick the configuration of the batched solve that finishes a sample of
+    graphs fastest (wall clock, after one warm-up run of the sample): the
+    worker form (rpgo_solve_batch: host threads, the CTA budget of each
+    direct solve) or the joint form (rpgo_solve_batch_joint: concurrent
+    lock-step groups, their size and, through the stream count, each group's
+    CTA budget). The first candidate is kept unless another is faster by more
+    than `margin` (timing noise on a small sample). Returns (config,
+    {name: seconds}); config holds solve_batch's keyword arguments."""
     import time
 
     solve_batch(params, graphs[:2], workers=2)
+    solve_batch(params, graphs[:2], joint=True)
     times = {}
-    for w, c in candidates:
+    for c in candidates:
         t0 = time.perf_counter()
-        res = solve_batch(params, graphs, workers=w, coop_ctas=c)
-        times[(w, c)] = time.perf_counter() - t0
+        res = solve_batch(params, graphs, **c)
+        times[_config_name(c)] = time.perf_counter() - t0
         if any(r[0] != 0 for r in res):
-            raise RpgoError(f"rpgo_solve_batch failed with workers={w}, coop_ctas={c}")
-    best = min(times, key=times.get)
-    if times[best] > (1.0 - margin) * times[candidates[0]]:
+            raise RpgoError(f"batched solve failed with {c}")
+    first = _config_name(candidates[0])
+    best = min(candidates, key=lambda c: times[_config_name(c)])
+    if times[_config_name(best)] > (1.0 - margin) * times[first]:
         best = candidates[0]
-    return best[0], best[1], times
+    return dict(best), times
 
 
 def pairwise_adjacency(dim, mode, slot_a, slot_b, flip, z_pose, z_cov, traj_pose, traj_cov, traj_node, traj_rot,

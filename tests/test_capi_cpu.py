@@ -13,7 +13,7 @@ HEADER = os.path.join(ROOT, "include", "rpgo_gb300.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    names = re.findall(r"\b(?:void|int|int64_t|double|rpgo_\w+\s*\*)\s*\*?\s*(rpgo_\w+)\s*\(", text)
+    names = re.findall(r"\b(?:void|int|int32_t|int64_t|double|rpgo_\w+\s*\*)\s*\*?\s*(rpgo_\w+)\s*\(", text)
     return sorted(set(names))
 
 

@@ -29,9 +29,9 @@ def test_batch_argument_checks_need_no_gpu():
     assert lib.rpgo_solve_batch(C.byref(p), 0, None, None, 0, 0, None) == 0
     assert lib.rpgo_solve_batch(C.byref(p), -1, None, None, 0, 0, None) != 0
     assert lib.rpgo_solve_batch(C.byref(p), 2, None, None, 0, 0, None) != 0
-    assert lib.rpgo_solve_batch_joint(C.byref(p), 0, None, None, 0, None) == 0
-    assert lib.rpgo_solve_batch_joint(C.byref(p), -1, None, None, 0, None) != 0
-    assert lib.rpgo_solve_batch_joint(C.byref(p), 2, None, None, 0, None) != 0
+    assert lib.rpgo_solve_batch_joint(C.byref(p), 0, None, None, 0, 0, None) == 0
+    assert lib.rpgo_solve_batch_joint(C.byref(p), -1, None, None, 0, 0, None) != 0
+    assert lib.rpgo_solve_batch_joint(C.byref(p), 2, None, None, 0, 0, None) != 0
 
 
 @pytest.mark.gpu
@@ -78,8 +78,8 @@ def test_batch_graph_matches_oracle():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("group", [0, 3])
-def test_joint_batch_matches_oracle_and_individual_solves(group):
+@pytest.mark.parametrize("group,streams", [(0, 1), (3, 0), (2, 3)])
+def test_joint_batch_matches_oracle_and_individual_solves(group, streams):
     # lock-step solves (one launch per stage over all graphs of a group): each
     # graph's inlier set equals the oracle's and its own update's, poses
     # within the oracle tolerance and close to its own update's (the error
@@ -88,7 +88,7 @@ def test_joint_batch_matches_oracle_and_individual_solves(group):
 
     build()
     graphs = [synth.walk3d(n, ni, no, seed=s) for n, ni, no, s in SIZES]
-    res = capi.solve_batch(_params(), [s.graph for s in graphs], joint=True, group=group)
+    res = capi.solve_batch(_params(), [s.graph for s in graphs], joint=True, group=group, streams=streams)
     _check_against_oracle(_params(), graphs, res)
     for s, (status, keys, poses, w, t) in zip(graphs, res):
         g = capi.RobustSolver(_params())
@@ -122,3 +122,27 @@ def test_joint_batch_modes_match_oracle(mode):
     graphs = [synth.walk3d(n, ni, no, seed=s) for n, ni, no, s in sizes]
     res = capi.solve_batch(p, [s.graph for s in graphs], joint=True)
     _check_against_oracle(p, graphs, res)
+
+
+@pytest.mark.gpu
+def test_joint_batch_graph_replay_equals_stage_launches():
+    # the rounds replayed from one captured CUDA graph run the same kernels
+    # on the same data as stage-by-stage launches: identical results
+    from rpgo_gb300 import build
+
+    build()
+    lib = capi.load()
+    graphs = [synth.walk3d(n, ni, no, seed=s) for n, ni, no, s in SIZES[:4]]
+    r0 = lib.rpgo_joint_graph_rounds()
+    res_g = capi.solve_batch(_params(), [s.graph for s in graphs], joint=True, streams=1)
+    replayed = lib.rpgo_joint_graph_rounds() - r0
+    old = lib.rpgo_set_joint_graphs(0)
+    try:
+        res_s = capi.solve_batch(_params(), [s.graph for s in graphs], joint=True, streams=1)
+    finally:
+        lib.rpgo_set_joint_graphs(old)
+    assert replayed > 0
+    for a, b in zip(res_g, res_s):
+        assert a[0] == 0 and b[0] == 0
+        assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
+        assert a[4].linear_solves == b[4].linear_solves
