@@ -330,6 +330,17 @@ int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st, int
     (void)cudaGetLastError();
     return ok ? e : nullptr;
   };
+  // the set of graphs whose items the direct solve's compacted lists hold
+  std::vector<uint8_t> listed(G, 2);
+  auto recompact = [&] {
+    bool changed = false;
+    for (int g = 0; g < G; ++g) {
+      const uint8_t on = ctl[g] & kBatchActive;
+      if (on != listed[g]) changed = true;
+      listed[g] = on;
+    }
+    return changed;
+  };
   auto run_round = [&](bool any_active) {
     if (any_active && use_graph && rounds >= 1 && !exec_pre) {
       exec_pre = capture([&] { enqueue_pre(true); });
@@ -343,13 +354,13 @@ int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st, int
     }
     if (any_active && exec_pre) {
       RPGO_CUDA(cudaGraphLaunch(exec_pre, st));
-      batch_round_solve(u, b, st);
+      batch_round_solve(u, b, recompact(), st);
       RPGO_CUDA(cudaGraphLaunch(exec_post, st));
       ++graph_launches;
     } else {
       enqueue_pre(any_active);
       if (any_active) {
-        batch_round_solve(u, b, st);
+        batch_round_solve(u, b, recompact(), st);
         enqueue_post();
       }
     }

@@ -49,6 +49,10 @@ SolveOut chol_finish(SolverDev& s, CholDev& c, const double* host);
 // batch b with its own damping; per-system model change and status land in
 // b.out (2 per system), the steps in s.delta.
 void chol_enqueue_batch(SolverDev& s, CholDev& c, const BatchDev& b, cudaStream_t st);
+// Joint batch: compact the plan's level lists to the graphs whose control
+// word (already on the device) has kBatchActive; later chol_enqueue_batch
+// launches use the compacted lists.
+void chol_batch_compact(CholDev& c, BatchDev& b, cudaStream_t st);
 // kernel time of the last enqueued launch (after the stream passed it)
 float chol_last_ms(CholDev& c);
 

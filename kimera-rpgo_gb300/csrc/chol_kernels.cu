@@ -70,12 +70,27 @@ struct CholArgs {
   const double* b_lam;
   int32_t* b_status;
   double *b_out, *b_term;  // per system (model change, status); per position partials
+  // the level lists hold only the solved systems' items (tasks and lvl_cols
+  // compacted per level, in plan order, ending at lvl_task_end / lvl_col_end)
+  int b_compact;
+  const int32_t *lvl_task_end, *lvl_col_end;
 };
+
+// end of level l's tasks and columns (the compacted lists of a joint batch
+// end early)
+__device__ __forceinline__ int task_end(const CholArgs& a, int l) {
+  return a.lvl_task_end ? a.lvl_task_end[l] : a.lvl_task_ptr[l + 1];
+}
+__device__ __forceinline__ int col_end(const CholArgs& a, int l) {
+  return a.lvl_col_end ? a.lvl_col_end[l] : a.lvl_col_ptr[l + 1];
+}
 
 __device__ __forceinline__ void set_fail(int32_t* status) { atomicExch(status, 1); }
 
 // the system of position j is solved by this launch
-__device__ __forceinline__ bool sys_on(const CholArgs& a, int j) { return a.G == 0 || (a.b_act[a.b_sys[j]] & 1); }
+__device__ __forceinline__ bool sys_on(const CholArgs& a, int j) {
+  return a.G == 0 || a.b_compact || (a.b_act[a.b_sys[j]] & 1);
+}
 // status word of the system of position j
 __device__ __forceinline__ int32_t* sys_status(const CholArgs& a, int j) {
   return a.G == 0 ? a.status : a.b_status + a.b_sys[j];
@@ -135,12 +150,31 @@ constexpr unsigned kFull = 0xffffffffu;
 //    a diagonal block) - sum over its pairs (a, b) of L[a] L[b]^T;
 //  row task (kind 2): Spart[t][r] = sum over its row entries (block q,
 //    column k) of (L[q] y_k)[r].
+// The index chain of task t for a warp: the task record and its lane
+// group's first pair (block tasks: the two blocks; row tasks: the block and
+// its column). Plan data, so a narrow level's task phase has it loaded ahead
+// of the barrier before it.
+struct TaskAhead {
+  int4 tk;
+  int u0, u1;
+};
 template <int D>
-__device__ void run_task(const CholArgs& a, int t, int lane) {
+__device__ __forceinline__ void task_ahead(const CholArgs& a, int t, int lane, TaskAhead& x) {
+  constexpr int G = 32 / D;
+  const int g = lane / D;
+  x.tk = reinterpret_cast<const int4*>(a.tasks)[t];
+  const int u = x.tk.y + g;
+  const int32_t* src = (x.tk.w & 3) < 2 ? a.upd_src : a.row_blk;
+  x.u0 = (g < G && u < x.tk.z) ? src[2 * u] : 0;
+  x.u1 = (g < G && u < x.tk.z) ? src[2 * u + 1] : 0;
+}
+
+template <int D>
+__device__ void run_task_core(const CholArgs& a, const TaskAhead& x, int lane) {
   constexpr int G = 32 / D, dd = D * D;
   constexpr int NC = D == 6 ? 3 : D;  // output columns of one block task
   const int g = lane / D, r = lane % D;
-  const int4 tk = reinterpret_cast<const int4*>(a.tasks)[t];
+  const int4 tk = x.tk;
   const int kind = tk.w & 3, slot = tk.w >> 4;
   if (!sys_on(a, kind < 2 ? a.blk_col[tk.x] : tk.x)) return;  // (warp-uniform)
   if (kind < 2) {
@@ -155,7 +189,8 @@ __device__ void run_task(const CholArgs& a, int t, int lane) {
     }
     if (g < G) {
       for (int u = tk.y + g; u < tk.z; u += G) {
-        const int pa = a.upd_src[2 * u], pb = a.upd_src[2 * u + 1];
+        const bool first = u == tk.y + g;
+        const int pa = first ? x.u0 : a.upd_src[2 * u], pb = first ? x.u1 : a.upd_src[2 * u + 1];
         const double* A = a.L + (size_t)pa * dd + r * D;
         const double* B = a.L + (size_t)pb * dd + c0 * D;
         double ar[D];
@@ -180,8 +215,9 @@ __device__ void run_task(const CholArgs& a, int t, int lane) {
     double acc = 0.0;
     if (g < G)
       for (int u = tk.y + g; u < tk.z; u += G) {
-        const double* Lq = a.L + (size_t)a.row_blk[2 * u] * dd + r * D;
-        const double* yk = a.y + (size_t)a.row_blk[2 * u + 1] * D;
+        const bool first = u == tk.y + g;
+        const double* Lq = a.L + (size_t)(first ? x.u0 : a.row_blk[2 * u]) * dd + r * D;
+        const double* yk = a.y + (size_t)(first ? x.u1 : a.row_blk[2 * u + 1]) * D;
 #pragma unroll
         for (int k = 0; k < D; ++k) acc = fma(Lq[k], yk[k], acc);
       }
@@ -194,12 +230,18 @@ __device__ void run_task(const CholArgs& a, int t, int lane) {
   }
 }
 
+template <int D>
+__device__ void run_task(const CholArgs& a, int t, int lane) {
+  TaskAhead x;
+  task_ahead<D>(a, t, lane, x);
+  run_task_core<D>(a, x, lane);
+}
+
 // off-diagonal block p (row r) of S into s: the sum of its task partials, or
 // its Hessian block when it has no update pairs (and no task)
 template <int D>
-__device__ __forceinline__ void sum_partials(const CholArgs& a, int p, int r, double (&s)[D]) {
+__device__ __forceinline__ void sum_partials_r(const CholArgs& a, int p, int t0, int nt, int r, double (&s)[D]) {
   constexpr int dd = D * D;
-  const int t0 = a.btask[2 * p], nt = a.btask[2 * p + 1];
   if (nt == 0) {
 #pragma unroll
     for (int c = 0; c < D; ++c) s[c] = block_H<D>(a, p, false, r, c);
@@ -213,6 +255,10 @@ __device__ __forceinline__ void sum_partials(const CholArgs& a, int p, int r, do
     for (int c = 0; c < D; ++c) s[c] += P[c];
   }
 }
+template <int D>
+__device__ __forceinline__ void sum_partials(const CholArgs& a, int p, int r, double (&s)[D]) {
+  sum_partials_r<D>(a, p, a.btask[2 * p], a.btask[2 * p + 1], r, s);
+}
 
 // S_jj, the diagonal block of column j (block p), from its task partials,
 // summed entry-wise: lane e holds entries e and e + 32, so a partial costs two
@@ -221,9 +267,9 @@ __device__ __forceinline__ void sum_partials(const CholArgs& a, int p, int r, do
 // task) is its Hessian block plus lambda D. Then moved to the lane-group row
 // layout (lane r of every group gets row r).
 template <int D>
-__device__ __forceinline__ void diag_partials(const CholArgs& a, int j, int p, int lane, int r, double (&C)[D]) {
+__device__ __forceinline__ void diag_partials_r(const CholArgs& a, int p, int t0, int t1, int lane, int r,
+                                                double (&C)[D]) {
   constexpr int dd = D * D;
-  const int t0 = a.btask[2 * p], t1 = t0 + a.btask[2 * p + 1];
   const bool has0 = lane < dd, has1 = lane + 32 < dd;
   double e0 = 0.0, e1 = 0.0;
   if (t1 == t0) {
@@ -251,6 +297,11 @@ __device__ __forceinline__ void diag_partials(const CholArgs& a, int j, int p, i
     const double v0 = __shfl_sync(kFull, e0, e & 31), v1 = __shfl_sync(kFull, e1, e & 31);
     C[c] = e < 32 ? v0 : v1;
   }
+}
+template <int D>
+__device__ __forceinline__ void diag_partials(const CholArgs& a, int j, int p, int lane, int r, double (&C)[D]) {
+  const int t0 = a.btask[2 * p];
+  diag_partials_r<D>(a, p, t0, t0 + a.btask[2 * p + 1], lane, r, C);
 }
 
 // In-register Cholesky of S_jj across a lane group (lane r holds row r, the
@@ -303,13 +354,15 @@ __device__ __forceinline__ void solve_offdiag(const CholArgs& a, int p, int r, c
 
 // y_j - the forward-substitution row sums of column j (row r)
 template <int D>
-__device__ __forceinline__ double forward_rhs(const CholArgs& a, int j, int r) {
+__device__ __forceinline__ double forward_rhs_r(const CholArgs& a, double b, int t0, int nt, int r) {
   constexpr int dd = D * D;
-  double b = a.y[(size_t)j * D + r];
-  const int t0 = a.ftask[2 * j], nt = a.ftask[2 * j + 1];
   double acc = 0.0;
   for (int t = t0; t < t0 + nt; ++t) acc += a.Spart[(size_t)t * dd + r * D];
   return b - acc;
+}
+template <int D>
+__device__ __forceinline__ double forward_rhs(const CholArgs& a, int j, int r) {
+  return forward_rhs_r<D>(a, a.y[(size_t)j * D + r], a.ftask[2 * j], a.ftask[2 * j + 1], r);
 }
 
 // y_j = L_jj^-1 b (lane r of a group holds b_r and row r of L_jj), stored
@@ -368,17 +421,43 @@ __device__ __forceinline__ void team_sync(int id) { asm volatile("bar.sync %0, 6
 // forward substitution; meanwhile the helper sums the forward row sums and the
 // partials of the off-diagonal blocks, and after the barrier solves those
 // blocks with L_jj. Same operations and order as column_warp.
+// The index chain of column j's phase-B team up to its first partial sum:
+// block and slot ranges (the lead: the diagonal block's slots; the helper: its
+// lane group's first off-diagonal block's slots and the row sums' slots).
+// Plan data, so it is followed ahead of the level's task-phase barrier.
+struct ColAhead {
+  int j, p0, p1, t0, t1, f0, fn;
+};
 template <int D>
-__device__ void column_team(const CholArgs& a, int j, int tw, int lane, int bar, double* sh) {
+__device__ __forceinline__ void column_ahead(const CholArgs& a, int j, int tw, int lane, ColAhead& c) {
+  const int g = lane / D;
+  c.j = j;
+  c.p0 = a.col_ptr[j];
+  c.p1 = a.col_ptr[j + 1];
+  if (tw == 0) {
+    c.t0 = a.btask[2 * c.p0];
+    c.t1 = c.t0 + a.btask[2 * c.p0 + 1];
+    c.f0 = c.fn = 0;
+  } else {
+    const int pf = c.p0 + 1 + g;
+    c.t0 = (g < 32 / D && pf < c.p1) ? a.btask[2 * pf] : 0;
+    c.t1 = (g < 32 / D && pf < c.p1) ? a.btask[2 * pf + 1] : 0;
+    c.f0 = a.ftask[2 * j];
+    c.fn = a.ftask[2 * j + 1];
+  }
+}
+
+template <int D>
+__device__ void column_team_core(const CholArgs& a, const ColAhead& ca, int tw, int lane, int bar, double* sh) {
   constexpr int G = 32 / D, dd = D * D;
   const int g = lane / D, r = lane % D;
   const bool grp = g < G;
   const int base = (grp ? g : 0) * D;
-  const int p0 = a.col_ptr[j], p1 = a.col_ptr[j + 1];
+  const int j = ca.j, p0 = ca.p0, p1 = ca.p1;
   if (!sys_on(a, j)) return;  // (both warps of the team: no named barrier)
   if (tw == 0) {
     double C[D];
-    diag_partials<D>(a, j, p0, lane, r, C);
+    diag_partials_r<D>(a, p0, ca.t0, ca.t1, lane, r, C);
     factor_diag<D>(a, lane, g == 0, r, base, C, sys_status(a, j));
     if (g == 0) {
 #pragma unroll
@@ -391,11 +470,11 @@ __device__ void column_team(const CholArgs& a, int j, int tw, int lane, int bar,
     team_sync(bar);
     forward_solve<D>(a, j, g == 0, r, base, C, sh[dd + r]);
   } else {
-    const double b = forward_rhs<D>(a, j, r);
+    const double b = forward_rhs_r<D>(a, a.y[(size_t)j * D + r], ca.f0, ca.fn, r);
     if (g == 0) sh[dd + r] = b;
     const int pf = p0 + 1 + g;
     double sv[D];
-    if (grp && pf < p1) sum_partials<D>(a, pf, r, sv);
+    if (grp && pf < p1) sum_partials_r<D>(a, pf, ca.t0, ca.t1, r, sv);
     team_sync(bar);
     double Lf[dd];
 #pragma unroll
@@ -409,6 +488,13 @@ __device__ void column_team(const CholArgs& a, int j, int tw, int lane, int bar,
       }
     }
   }
+}
+
+template <int D>
+__device__ void column_team(const CholArgs& a, int j, int tw, int lane, int bar, double* sh) {
+  ColAhead ca;
+  column_ahead<D>(a, j, tw, lane, ca);
+  column_team_core<D>(a, ca, tw, lane, bar, sh);
 }
 
 // phase A on wide levels: every lane group runs a task of its own (the
@@ -530,22 +616,46 @@ __device__ void column_group(const CholArgs& a, int c0, int nc, int w0, int lane
   forward_solve<D>(a, j, mine, r, base, C, mine ? forward_rhs<D>(a, j, r) : 0.0);
 }
 
+// The index chain of the backward substitution of column j (the column,
+// its block range, the row of its lane group's first block): plan data, so a
+// warp follows it for its column of the next (narrow) level ahead of the
+// barrier, and after the barrier issues every value load of the column at
+// once (its blocks, diagonal factor and y_j are final since the forward pass;
+// only the solutions x_i come from the level above).
+struct BackAhead {
+  int j, q, q1, row;
+};
+template <int D>
+__device__ __forceinline__ void backward_ahead(const CholArgs& a, int j, int lane, BackAhead& p) {
+  constexpr int G = 32 / D;
+  const int g = lane / D;
+  p.j = j;
+  p.q = a.col_ptr[j] + 1 + g;
+  p.q1 = a.col_ptr[j + 1];
+  p.row = (g < G && p.q < p.q1) ? a.blk_row[p.q] : 0;
+}
+
 // backward substitution of column j by one warp:
 // x_j = L_jj^-T (y_j - sum L_ij^T x_i), the groups share the blocks
 template <int D>
-__device__ void backward_warp(const CholArgs& a, int j, int lane) {
+__device__ void backward_warp_core(const CholArgs& a, const BackAhead& p, int lane) {
   constexpr int G = 32 / D, dd = D * D;
   const int g = lane / D, r = lane % D;
   const int base = (g < G ? g : 0) * D;
+  const int j = p.j;
   if (!sys_on(a, j)) return;  // (warp-uniform)
   double acc = 0.0;
-  const int q0 = a.col_ptr[j] + 1, q1 = a.col_ptr[j + 1];
-  if (g < G) {
-    for (int q = q0 + g; q < q1; q += G) {
-      const double* B = a.L + (size_t)q * dd + r;
-      const double* xi = a.y + (size_t)a.blk_row[q] * D;
+  const int q0 = p.q - g, q1 = p.q1;
+  if (g < G && p.q < q1) {
+    const double* B0 = a.L + (size_t)p.q * dd + r;
+    const double* xi = a.y + (size_t)p.row * D;
 #pragma unroll
-      for (int k = 0; k < D; ++k) acc = fma(B[k * D], xi[k], acc);
+    for (int k = 0; k < D; ++k) acc = fma(B0[k * D], xi[k], acc);
+    for (int q = p.q + G; q < q1; q += G) {
+      const double* B = a.L + (size_t)q * dd + r;
+      const double* xq = a.y + (size_t)a.blk_row[q] * D;
+#pragma unroll
+      for (int k = 0; k < D; ++k) acc = fma(B[k * D], xq[k], acc);
     }
   }
   const int ng = min(G, q1 - q0);
@@ -565,6 +675,13 @@ __device__ void backward_warp(const CholArgs& a, int j, int lane) {
     if (r < c) b = fma(-Lc[c], xc, b);
   }
   if (g == 0) a.y[(size_t)j * D + r] = xv;
+}
+
+template <int D>
+__device__ void backward_warp(const CholArgs& a, int j, int lane) {
+  BackAhead p;
+  backward_ahead<D>(a, j, lane, p);
+  backward_warp_core<D>(a, p, lane);
 }
 
 // backward substitution for wide levels: every lane group takes a column of
@@ -653,6 +770,8 @@ struct TileSmem {
   double v[kTB];
   double part[kWarps * 36 * 5];  // tail block partial sums: (warp, lane group) x D x D, D = 3 or 6
   double team[2][36 + 6];        // phase B teams: L_jj and the forward right-hand side
+  ColAhead ahead[4][32];         // phase B teams (warps 1-4): index chains loaded ahead
+  TaskAhead task[kWarps][32];    // narrow task phases: each warp's first task, loaded ahead
 };
 
 // S of tail block t into the dense tail, by one CTA: the lane groups of all
@@ -897,7 +1016,6 @@ __device__ __forceinline__ double cta_sum(double v, double* sh) {
 
 template <int D>
 __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
-  constexpr int dd = D * D;
   cg::grid_group grid = cg::this_grid();
   __shared__ TileSmem sm;
   __shared__ double shr[kThreads / 32];
@@ -934,8 +1052,17 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
 
   // 2. sparse levels: (A) the level's tasks over all warps, (B) its
   // columns, one warp or a two-warp team each; one barrier after each
+  // a narrow level's phase B: at most two columns per CTA, each by a team of
+  // two warps (warps 1-2 and 3-4, on four different SM sub-partitions)
+  const int wi = threadIdx.x >> 5;
+  const int team_slot = (wi - 1) >> 1;
+  const int team_w = team_slot * (int)gridDim.x + (int)blockIdx.x;
+  bool task_ready = false;  // sm.task[wi][lane] holds this warp's first task of level l
   for (int l = 0; l < a.levels; ++l) {
-    const int t0 = a.lvl_task_ptr[l], t1 = a.lvl_task_ptr[l + 1];
+    const int t0 = a.lvl_task_ptr[l], t1 = task_end(a, l);
+    const int c0 = a.lvl_col_ptr[l], nc = col_end(a, l) - c0;
+    const bool narrow = nc < kGroupModeItems * nw && nc <= 2 * (int)gridDim.x;
+    const bool team = narrow && wi >= 1 && wi <= 4 && team_w < nc;
     if (t1 > t0) {  // (the leaves' level has none: no updates, no row sums)
       if (t1 - t0 >= kGroupModeItems * nw) {
         // wide: a task per lane group
@@ -947,26 +1074,40 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
           run_task_group<D>(a, t0 + (valid ? t : w), valid, lane % D);
         }
       } else {
-        for (int t = t0 + gw; t < t1; t += nw) run_task<D>(a, t, lane);
+        for (int t = t0 + gw; t < t1; t += nw) {
+          if (t == t0 + gw && task_ready) run_task_core<D>(a, sm.task[wi][lane], lane);
+          else run_task<D>(a, t, lane);
+        }
       }
+      // the team's index chain for phase B, ahead of the barrier (through
+      // shared memory: held in registers it would raise the kernel's
+      // register count above two CTAs per SM)
+      if (team) column_ahead<D>(a, a.lvl_cols[c0 + team_w], (wi - 1) & 1, lane, sm.ahead[wi - 1][lane]);
       grid.sync();
     }
-    const int c0 = a.lvl_col_ptr[l], nc = a.lvl_col_ptr[l + 1] - c0;
     if (nc >= kGroupModeItems * nw) {
       // wide: a column per lane group
       constexpr int G = 32 / D;
       for (int w = gw * G; w < nc; w += nw * G) column_group<D>(a, c0, nc, w, lane);
-    } else if (nc <= 2 * (int)gridDim.x) {
-      // narrow level: at most two columns per CTA, each by a team of two
-      // warps (warps 1-2 and 3-4, on four different SM sub-partitions)
-      const int wi = threadIdx.x >> 5;
-      if (wi >= 1 && wi <= 4) {
-        const int slot = (wi - 1) >> 1;
-        const int w = slot * (int)gridDim.x + (int)blockIdx.x;
-        if (w < nc) column_team<D>(a, a.lvl_cols[c0 + w], (wi - 1) & 1, lane, 1 + slot, sm.team[slot]);
+    } else if (narrow) {
+      if (team) {
+        ColAhead ca;
+        if (t1 > t0) ca = sm.ahead[wi - 1][lane];
+        else column_ahead<D>(a, a.lvl_cols[c0 + team_w], (wi - 1) & 1, lane, ca);
+        column_team_core<D>(a, ca, (wi - 1) & 1, lane, 1 + team_slot, sm.team[team_slot]);
       }
     } else {
       for (int w = gw; w < nc; w += nw) column_warp<D>(a, a.lvl_cols[c0 + w], lane);
+    }
+    // the warp's first task of the next level (narrow task phases), ahead of
+    // the barrier, through shared memory
+    task_ready = false;
+    if (l + 1 < a.levels) {
+      const int u0 = a.lvl_task_ptr[l + 1], u1 = task_end(a, l + 1);
+      if (u1 > u0 && u1 - u0 < kGroupModeItems * nw && u0 + gw < u1) {
+        task_ahead<D>(a, u0 + gw, lane, sm.task[wi][lane]);
+        task_ready = true;
+      }
     }
     grid.sync();
   }
@@ -1023,15 +1164,29 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
     if (blockIdx.x == (unsigned)(k % gridDim.x)) tail_backward_item(a, yt, k, sm);
     grid.sync();
   }
+  // a narrow level has at most one column per warp (warps 1..7 take them):
+  // the warp's column of the next level is loaded ahead of each barrier
+  BackAhead back;
+  int back_l = -1;  // the level whose column `back` holds
   for (int l = a.levels - 1; l >= 0; --l) {
-    const int c0 = a.lvl_col_ptr[l], nc = a.lvl_col_ptr[l + 1] - c0;
+    const int c0 = a.lvl_col_ptr[l], nc = col_end(a, l) - c0;
     if (nc <= (kWarps - 1) * (int)gridDim.x) {
-      for (int w = gw; w < nc; w += nw) backward_warp<D>(a, a.lvl_cols[c0 + w], lane);
+      if (gw < nc) {
+        if (back_l == l) backward_warp_core<D>(a, back, lane);
+        else backward_warp<D>(a, a.lvl_cols[c0 + gw], lane);
+      }
     } else {
       // more columns than warps 1..7 of the grid: G columns per warp instead
       // of a second round
       constexpr int G = 32 / D;
       for (int w = gw; w * G < nc; w += nw) backward_groups<D>(a, c0, nc, w * G, lane);
+    }
+    if (l > 0) {
+      const int c1 = a.lvl_col_ptr[l - 1], n1 = col_end(a, l - 1) - c1;
+      if (n1 <= (kWarps - 1) * (int)gridDim.x && gw < n1) {
+        backward_ahead<D>(a, a.lvl_cols[c1 + gw], lane, back);
+        back_l = l - 1;
+      }
     }
     grid.sync();
   }
@@ -1111,8 +1266,9 @@ __global__ void __launch_bounds__(kThreads) k_chol_solve(CholArgs a) {
 }
 
 // H (and the damping diagonal, on diagonal blocks) in the factor's block
-// layout, once per linearisation: thread per block entry; an off-diagonal
-// block sums its factors' blocks in the plan's order (as gather_offdiag).
+// layout, once per linearisation: thread per block row; an off-diagonal
+// block sums its factors' blocks in the plan's order (each entry the same
+// additions as gather_offdiag).
 template <int D>
 __global__ void k_block_hessian(int nblk, const int32_t* __restrict__ blk_row, const int32_t* __restrict__ blk_col,
                                 const int32_t* __restrict__ perm, const int32_t* __restrict__ a_ptr,
@@ -1122,17 +1278,113 @@ __global__ void k_block_hessian(int nblk, const int32_t* __restrict__ blk_row, c
                                 const uint8_t* __restrict__ mask) {
   constexpr int dd = D * D;
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (t >= (int64_t)nblk * dd) return;
-  const int p = (int)(t / dd), e = (int)(t % dd), r = e / D, c = e % D;
+  if (t >= (int64_t)nblk * D) return;
+  const int p = (int)(t / D), r = (int)(t % D);
   const int j = blk_col[p];
   if (mask && !(mask[j] & 1)) return;  // (a joint batch's graph not in this round)
+  double* out = Hs + (size_t)p * dd + r * D;
   if (blk_row[p] == j) {
     const int v = perm[j];
-    Hs[t] = Hd64[(size_t)v * dd + e];
-    if (r == c) dampS[(size_t)p * D + r] = dampD[(size_t)v * D + r];
+#pragma unroll
+    for (int c = 0; c < D; ++c) out[c] = Hd64[(size_t)v * dd + r * D + c];
+    dampS[(size_t)p * D + r] = dampD[(size_t)v * D + r];
   } else {
-    Hs[t] = gather_offdiag<D>(fH64, a_src, a_ptr[p], a_ptr[p + 1], r, c);
+    double acc[D];
+#pragma unroll
+    for (int c = 0; c < D; ++c) acc[c] = 0.0;
+    for (int u = a_ptr[p]; u < a_ptr[p + 1]; ++u) {
+      const int32_t x = a_src[u];
+      const double* H = fH64 + (size_t)(x >> 1) * 3 * dd + 2 * dd;
+#pragma unroll
+      for (int c = 0; c < D; ++c) acc[c] += (x & 1) ? H[c * D + r] : H[r * D + c];
+    }
+#pragma unroll
+    for (int c = 0; c < D; ++c) out[c] = acc[c];
   }
+}
+
+// Joint batch: the items (tasks, columns) of the graphs in the round, per
+// level, in plan order. Chunks never straddle a level (chunk table from the
+// plan). Pass 1 counts each chunk's active items; pass 2 places each chunk at
+// its level's start plus the counts of the level's earlier chunks and writes
+// its active items in order (a block-wide scan); pass 3 writes every level's
+// end.
+constexpr int kCompactThreads = 256;
+
+__device__ __forceinline__ bool task_active(const int4& tk, const int32_t* __restrict__ blk_col,
+                                            const int32_t* __restrict__ vsys, const uint8_t* __restrict__ ctl) {
+  const int pos = (tk.w & 3) < 2 ? blk_col[tk.x] : tk.x;
+  return ctl[vsys[pos]] & 1;
+}
+
+// kind 0: tasks (int4 items), 1: columns (int items)
+template <int KIND>
+__global__ void k_compact_count(const int4* __restrict__ chunks, const int4* __restrict__ tasks,
+                                const int32_t* __restrict__ cols, const int32_t* __restrict__ blk_col,
+                                const int32_t* __restrict__ vsys, const uint8_t* __restrict__ ctl,
+                                int32_t* __restrict__ counts) {
+  __shared__ int sh[kCompactThreads / 32];
+  const int4 ch = chunks[blockIdx.x];  // (level, begin, end, first chunk of the level)
+  int c = 0;
+  for (int i = ch.y + threadIdx.x; i < ch.z; i += blockDim.x)
+    c += KIND == 0 ? task_active(tasks[i], blk_col, vsys, ctl) : (ctl[vsys[cols[i]]] & 1);
+  c = __reduce_add_sync(0xffffffffu, c);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = c;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int w = 0; w < kCompactThreads / 32; ++w) t += sh[w];
+    counts[blockIdx.x] = t;
+  }
+}
+
+template <int KIND>
+__global__ void k_compact_scatter(const int4* __restrict__ chunks, const int32_t* __restrict__ lvl_ptr,
+                                  const int4* __restrict__ tasks, const int32_t* __restrict__ cols,
+                                  const int32_t* __restrict__ blk_col, const int32_t* __restrict__ vsys,
+                                  const uint8_t* __restrict__ ctl, const int32_t* __restrict__ counts,
+                                  int4* __restrict__ tasks_c, int32_t* __restrict__ cols_c) {
+  __shared__ int sh[kCompactThreads / 32];
+  __shared__ int base;
+  const int4 ch = chunks[blockIdx.x];
+  if (threadIdx.x == 0) {
+    int o = lvl_ptr[ch.x];
+    for (int k = ch.w; k < (int)blockIdx.x; ++k) o += counts[k];
+    base = o;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i0 = ch.y; i0 < ch.z; i0 += blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    bool on = false;
+    if (i < ch.z) on = KIND == 0 ? task_active(tasks[i], blk_col, vsys, ctl) : (ctl[vsys[cols[i]]] & 1);
+    const unsigned m = __ballot_sync(0xffffffffu, on);
+    if (lane == 0) sh[warp] = __popc(m);
+    __syncthreads();
+    int before = 0, total = 0;
+    for (int w = 0; w < kCompactThreads / 32; ++w) {
+      before += w < warp ? sh[w] : 0;
+      total += sh[w];
+    }
+    if (on) {
+      const int o = base + before + __popc(m & ((1u << lane) - 1u));
+      if (KIND == 0) tasks_c[o] = tasks[i];
+      else cols_c[o] = cols[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) base += total;
+    __syncthreads();
+  }
+}
+
+__global__ void k_compact_ends(int levels, const int32_t* __restrict__ lvl_ptr,
+                               const int32_t* __restrict__ level_chunks, const int32_t* __restrict__ counts,
+                               int32_t* __restrict__ ends) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  if (l >= levels) return;
+  int e = lvl_ptr[l];
+  for (int k = level_chunks[l]; k < level_chunks[l + 1]; ++k) e += counts[k];
+  ends[l] = e;
 }
 
 }  // namespace
@@ -1188,7 +1440,7 @@ void chol_block_hessian(SolverDev& s, CholDev& c, cudaStream_t st, const uint8_t
   const int nblk = (int)c.plan.blk_row.size();
   if (nblk == 0) return;
   const int tb = 256;
-  const int64_t n = (int64_t)nblk * c.plan.d * c.plan.d;
+  const int64_t n = (int64_t)nblk * c.plan.d;
   if (s.dim == 3)
     k_block_hessian<6><<<div_up(n, tb), tb, 0, st>>>(nblk, c.blk_row.get(), c.blk_col.get(), c.perm.get(),
                                                     c.a_ptr.get(), c.a_src.get(), s.Hd64.get(), s.fH64.get(),
@@ -1236,6 +1488,8 @@ static CholArgs make_args(SolverDev& s, CholDev& c, double lambda) {
   a.b_lam = nullptr;
   a.b_status = nullptr;
   a.b_out = a.b_term = nullptr;
+  a.b_compact = 0;
+  a.lvl_task_end = a.lvl_col_end = nullptr;
   return a;
 }
 
@@ -1339,6 +1593,13 @@ void chol_enqueue_batch(SolverDev& s, CholDev& c, const BatchDev& b, cudaStream_
   a.b_status = b.status.get();
   a.b_out = b.out.get();
   a.b_term = b.term.get();
+  if (b.compacted) {
+    a.tasks = reinterpret_cast<const int32_t*>(b.tasks_c.get());
+    a.lvl_cols = b.cols_c.get();
+    a.lvl_task_end = b.task_end.get();
+    a.lvl_col_end = b.col_end.get();
+    a.b_compact = 1;
+  }
   void* args[] = {&a};
   RPGO_CUDA(cudaEventRecord(c.ev[0], st));
   if (s.dim == 3)
@@ -1347,6 +1608,68 @@ void chol_enqueue_batch(SolverDev& s, CholDev& c, const BatchDev& b, cudaStream_
     RPGO_CUDA(cudaLaunchCooperativeKernel((const void*)k_chol_solve<3>, grid, kThreads, args, 0, st));
   RPGO_LAUNCHED();
   RPGO_CUDA(cudaEventRecord(c.ev[1], st));
+}
+
+void chol_batch_compact(CholDev& c, BatchDev& b, cudaStream_t st) {
+  const CholPlan& p = c.plan;
+  const int L = p.levels();
+  if (L == 0) return;
+  constexpr int kChunk = 4096;
+  if (b.n_task_chunks == 0) {
+    // chunk tables: (level, begin, end, the level's first chunk), per level
+    // its first chunk; every level gets at least one (possibly empty) chunk
+    auto tables = [&](const std::vector<int32_t>& ptr, DeviceBuffer<int4>& chunks, DeviceBuffer<int32_t>& level_chunks,
+                      int* n) {
+      std::vector<int4> ch;
+      std::vector<int32_t> lc(L + 1, 0);
+      for (int l = 0; l < L; ++l) {
+        lc[l] = (int)ch.size();
+        const int first = (int)ch.size();
+        int i = ptr[l];
+        do {
+          const int e = std::min(ptr[l + 1], i + kChunk);
+          ch.push_back(make_int4(l, i, e, first));
+          i = e;
+        } while (i < ptr[l + 1]);
+      }
+      lc[L] = (int)ch.size();
+      chunks.upload(ch, st);
+      level_chunks.upload(lc, st);
+      *n = (int)ch.size();
+    };
+    tables(p.lvl_task_ptr, b.task_chunks, b.task_level_chunks, &b.n_task_chunks);
+    tables(p.lvl_col_ptr, b.col_chunks, b.col_level_chunks, &b.n_col_chunks);
+    b.task_counts.resize(b.n_task_chunks);
+    b.col_counts.resize(b.n_col_chunks);
+    b.tasks_c.resize(std::max<size_t>(1, p.tasks.size() / 4));
+    b.cols_c.resize(std::max<size_t>(1, p.lvl_cols.size()));
+    b.task_end.resize(L);
+    b.col_end.resize(L);
+  }
+  const int4* tasks = reinterpret_cast<const int4*>(c.tasks.get());
+  k_compact_count<0><<<b.n_task_chunks, kCompactThreads, 0, st>>>(b.task_chunks.get(), tasks, nullptr,
+                                                                  c.blk_col.get(), b.vsys.get(), b.ctl.get(),
+                                                                  b.task_counts.get());
+  RPGO_LAUNCHED();
+  k_compact_count<1><<<b.n_col_chunks, kCompactThreads, 0, st>>>(b.col_chunks.get(), nullptr, c.lvl_cols.get(),
+                                                                 c.blk_col.get(), b.vsys.get(), b.ctl.get(),
+                                                                 b.col_counts.get());
+  RPGO_LAUNCHED();
+  k_compact_scatter<0><<<b.n_task_chunks, kCompactThreads, 0, st>>>(
+      b.task_chunks.get(), c.lvl_task_ptr.get(), tasks, nullptr, c.blk_col.get(), b.vsys.get(), b.ctl.get(),
+      b.task_counts.get(), b.tasks_c.get(), nullptr);
+  RPGO_LAUNCHED();
+  k_compact_scatter<1><<<b.n_col_chunks, kCompactThreads, 0, st>>>(
+      b.col_chunks.get(), c.lvl_col_ptr.get(), nullptr, c.lvl_cols.get(), c.blk_col.get(), b.vsys.get(),
+      b.ctl.get(), b.col_counts.get(), nullptr, b.cols_c.get());
+  RPGO_LAUNCHED();
+  k_compact_ends<<<div_up(L, 64), 64, 0, st>>>(L, c.lvl_task_ptr.get(), b.task_level_chunks.get(),
+                                               b.task_counts.get(), b.task_end.get());
+  RPGO_LAUNCHED();
+  k_compact_ends<<<div_up(L, 64), 64, 0, st>>>(L, c.lvl_col_ptr.get(), b.col_level_chunks.get(),
+                                               b.col_counts.get(), b.col_end.get());
+  RPGO_LAUNCHED();
+  b.compacted = true;
 }
 
 float chol_last_ms(CholDev& c) {

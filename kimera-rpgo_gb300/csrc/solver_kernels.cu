@@ -1423,7 +1423,10 @@ void batch_round_pre(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_
   else batch_pre_t<2>(s, b, diagonal_damping, any_active, st);
 }
 
-void batch_round_solve(SolverDev& s, BatchDev& b, cudaStream_t st) { chol_enqueue_batch(s, *s.chol, b, st); }
+void batch_round_solve(SolverDev& s, BatchDev& b, bool recompact, cudaStream_t st) {
+  if (recompact) chol_batch_compact(*s.chol, b, st);
+  chol_enqueue_batch(s, *s.chol, b, st);
+}
 
 void batch_round_post(SolverDev& s, BatchDev& b, cudaStream_t st) {
   if (s.dim == 3) batch_post_t<3>(s, b, st);

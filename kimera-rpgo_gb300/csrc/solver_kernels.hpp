@@ -38,6 +38,12 @@ struct BatchDev {
   DeviceBuffer<double> out;            // per graph: model change, status (direct solve)
   DeviceBuffer<double> term;           // per variable: model change partials
   DeviceBuffer<double> err;            // per graph: error at x (kBatchError), at xnew (kBatchActive)
+  // the direct solve's level lists compacted to the graphs in the round
+  // (rebuilt when that set changes; chunk tables fixed by the merged plan)
+  bool compacted = false;
+  DeviceBuffer<int4> task_chunks, col_chunks, tasks_c;
+  DeviceBuffer<int32_t> task_level_chunks, col_level_chunks, task_counts, col_counts, task_end, col_end, cols_c;
+  int n_task_chunks = 0, n_col_chunks = 0;
 };
 
 // Device-resident problem: factors, structure, per-iteration buffers.
@@ -138,11 +144,13 @@ void solver_gnc_weights(SolverDev& s, const double* x, int n_known, const double
 // b.ctl (already on the device). batch_round_pre: the accept / GNC / reset
 // updates of x and the weights, the error at x, then (any_active: some graph
 // has kBatchActive) the linearisation and block Hessian; batch_round_solve:
-// the cooperative direct solve with each graph's damping b.lam;
+// the cooperative direct solve with each graph's damping b.lam (recompact:
+// the set of graphs in the round changed, the level lists are compacted
+// again first);
 // batch_round_post: the retraction and the error at xnew. Results (b.out,
 // b.err) stay on the device.
 void batch_round_pre(SolverDev& s, BatchDev& b, bool diagonal_damping, bool any_active, cudaStream_t st);
-void batch_round_solve(SolverDev& s, BatchDev& b, cudaStream_t st);
+void batch_round_solve(SolverDev& s, BatchDev& b, bool recompact, cudaStream_t st);
 void batch_round_post(SolverDev& s, BatchDev& b, cudaStream_t st);
 
 }  // namespace rpgo
