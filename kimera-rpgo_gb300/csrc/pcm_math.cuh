@@ -320,61 +320,59 @@ __device__ __forceinline__ void p2_logmap(const P2& T, double xi[3]) {
 }
 
 // ------------------------------------------------------------------ SPD helpers
-// Cholesky decision as Eigen's LLT: fails when a pivot is <= 0 (NaN passes).
+// Positive-definiteness test of a symmetric matrix as Eigen's LLT decides it
+// (fails when a pivot is <= 0; a NaN pivot passes), evaluated as an LDL^T
+// factorisation with reciprocal pivots: the pivots D_j are LLT's L_jj^2, so
+// the decision is the same up to rounding, with one division per pivot and
+// no square roots (LLT: one division per entry and a square root per pivot).
+// Row i: e_j = A_ij - sum_k e_k L_jk (k < j) is L_ij D_j, L_ij = e_j / D_j;
+// D_i = A_ii - sum_k e_k L_ik.
 template <int N>
-__device__ __forceinline__ bool chol_ok(const double* A) {
-  double L[N * N];
+__device__ __forceinline__ bool ldlt_factor(const double* A, double* L, double* iD, bool nan_passes) {
 #pragma unroll
   for (int i = 0; i < N; ++i) {
+    double e[N];
 #pragma unroll
-    for (int j = 0; j <= i; ++j) {
+    for (int j = 0; j < i; ++j) {
       double acc = A[N * i + j];
 #pragma unroll
-      for (int k = 0; k < j; ++k) acc = fmad(-L[N * i + k], L[N * j + k], acc);
-      if (i == j) {
-        if (acc <= 0.0) return false;
-        L[N * i + i] = sqrtd(acc);
-      } else {
-        L[N * i + j] = dvd(acc, L[N * j + j]);
-      }
+      for (int k = 0; k < j; ++k) acc = fmad(-e[k], L[N * j + k], acc);
+      e[j] = acc;
+      L[N * i + j] = mul(acc, iD[j]);
     }
+    double acc = A[N * i + i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) acc = fmad(-e[k], L[N * i + k], acc);
+    if (nan_passes ? (acc <= 0.0) : !(acc > 0.0)) return false;
+    iD[i] = dvd(1.0, acc);
   }
   return true;
 }
-// x^T A^-1 x: Cholesky solve, Gaussian elimination with partial pivoting when
-// a pivot is <= 0 or NaN.
+template <int N>
+__device__ __forceinline__ bool chol_ok(const double* A) {
+  double L[N * N], iD[N];
+  return ldlt_factor<N>(A, L, iD, true);
+}
+// x^T A^-1 x: from the LDL^T factors (z = L^-1 x, sum of z_i^2 / D_i); when a
+// pivot is <= 0 or NaN, Gaussian elimination with partial pivoting.
 template <int N>
 __device__ __forceinline__ double quad_inv(const double* A, const double* x) {
-  double L[N * N];
-  bool ok = true;
+  {
+    double L[N * N], iD[N];
+    if (ldlt_factor<N>(A, L, iD, false)) {
+      double z[N];
+      double d2 = 0.0;
 #pragma unroll
-  for (int i = 0; i < N; ++i) {
+      for (int i = 0; i < N; ++i) {
+        double acc = x[i];
 #pragma unroll
-    for (int j = 0; j <= i; ++j) {
-      if (!ok) continue;
-      double acc = A[N * i + j];
-#pragma unroll
-      for (int k = 0; k < j; ++k) acc = fmad(-L[N * i + k], L[N * j + k], acc);
-      if (i == j) {
-        if (!(acc > 0.0)) ok = false;
-        else L[N * i + i] = sqrtd(acc);
-      } else {
-        L[N * i + j] = dvd(acc, L[N * j + j]);
+        for (int k = 0; k < i; ++k) acc = fmad(-L[N * i + k], z[k], acc);
+        z[i] = acc;
+        const double t = mul(acc, iD[i]);
+        d2 = (i == 0) ? mul(t, acc) : fmad(t, acc, d2);
       }
+      return d2;
     }
-  }
-  if (ok) {
-    double y[N];
-    double d2 = 0.0;
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      double acc = x[i];
-#pragma unroll
-      for (int k = 0; k < i; ++k) acc = fmad(-L[N * i + k], y[k], acc);
-      y[i] = dvd(acc, L[N * i + i]);
-      d2 = (i == 0) ? mul(y[0], y[0]) : fmad(y[i], y[i], d2);
-    }
-    return d2;
   }
   double M[N * N], b[N], z[N];
   for (int i = 0; i < N * N; ++i) M[i] = A[i];

@@ -303,50 +303,49 @@ static inline void p2_logmap(const P2& T, double xi[3]) {
 }
 
 // ---------------------------------------------------------------- dense SPD helpers
-// Cholesky (lower, row oriented). Fails exactly when a pivot is <= 0 (a NaN
-// pivot passes, as in Eigen's LLT).
-static inline bool chol_lower(const double* A, int n, double* L) {
+// Positive-definiteness test of a symmetric matrix as Eigen's LLT decides it
+// (fails when a pivot is <= 0; a NaN pivot passes), evaluated as an LDL^T
+// factorisation with reciprocal pivots (the pivots D_j are LLT's L_jj^2):
+// row i: e_j = A_ij - sum_k e_k L_jk (k < j), L_ij = e_j * (1 / D_j);
+// D_i = A_ii - sum_k e_k L_ik. The GPU kernels evaluate the same sequence.
+static inline bool ldlt_factor(const double* A, int n, double* L, double* iD, bool nan_passes) {
   for (int i = 0; i < n; ++i) {
-    for (int j = 0; j <= i; ++j) {
+    double e[6];
+    for (int j = 0; j < i; ++j) {
       double acc = A[n * i + j];
-      for (int k = 0; k < j; ++k) acc = fmad(-L[n * i + k], L[n * j + k], acc);
-      if (i == j) {
-        if (acc <= 0.0) return false;
-        L[n * i + i] = std::sqrt(acc);
-      } else {
-        L[n * i + j] = acc / L[n * j + j];
-      }
+      for (int k = 0; k < j; ++k) acc = fmad(-e[k], L[n * j + k], acc);
+      e[j] = acc;
+      L[n * i + j] = acc * iD[j];
     }
+    double acc = A[n * i + i];
+    for (int k = 0; k < i; ++k) acc = fmad(-e[k], L[n * i + k], acc);
+    if (nan_passes ? (acc <= 0.0) : !(acc > 0.0)) return false;
+    iD[i] = 1.0 / acc;
   }
   return true;
 }
-// x^T A^-1 x for symmetric A: Cholesky solve; if a pivot is <= 0 or NaN,
-// Gaussian elimination with partial pivoting.
+static inline bool llt_ok(const double* A, int n) {
+  double L[36], iD[6];
+  return ldlt_factor(A, n, L, iD, true);
+}
+// x^T A^-1 x for symmetric A: from the LDL^T factors (z = L^-1 x, sum of
+// z_i^2 / D_i); if a pivot is <= 0 or NaN, Gaussian elimination with partial
+// pivoting.
 static inline double quad_inv(const double* A, int n, const double* x) {
-  double L[36];
-  bool ok = true;
-  for (int i = 0; i < n && ok; ++i) {
-    for (int j = 0; j <= i; ++j) {
-      double acc = A[n * i + j];
-      for (int k = 0; k < j; ++k) acc = fmad(-L[n * i + k], L[n * j + k], acc);
-      if (i == j) {
-        if (!(acc > 0.0)) { ok = false; break; }
-        L[n * i + i] = std::sqrt(acc);
-      } else {
-        L[n * i + j] = acc / L[n * j + j];
+  {
+    double L[36], iD[6];
+    if (ldlt_factor(A, n, L, iD, false)) {
+      double z[6];
+      double d2 = 0.0;
+      for (int i = 0; i < n; ++i) {
+        double acc = x[i];
+        for (int k = 0; k < i; ++k) acc = fmad(-L[n * i + k], z[k], acc);
+        z[i] = acc;
+        const double t = acc * iD[i];
+        d2 = (i == 0) ? t * acc : fmad(t, acc, d2);
       }
+      return d2;
     }
-  }
-  if (ok) {
-    double y[6];
-    double d2 = 0.0;
-    for (int i = 0; i < n; ++i) {
-      double acc = x[i];
-      for (int k = 0; k < i; ++k) acc = fmad(-L[n * i + k], y[k], acc);
-      y[i] = acc / L[n * i + i];
-      d2 = (i == 0) ? (y[0] * y[0]) : fmad(y[i], y[i], d2);
-    }
-    return d2;
   }
   double M[36], b[6], z[6];
   for (int i = 0; i < n * n; ++i) M[i] = A[i];

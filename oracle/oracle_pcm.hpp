@@ -116,7 +116,7 @@ struct PWC {
     constexpr int n = L::dim;
     const typename L::Pose res = L::between(pose, other.pose);
     out.pose = res;
-    double C[n * n], Lf[n * n];
+    double C[n * n];
     L::congruence(L::inverse(res), cov, C);
     for (int i = 0; i < n; ++i)
       for (int j = 0; j <= i; ++j) {
@@ -124,7 +124,7 @@ struct PWC {
         out.cov[n * i + j] = v;
         out.cov[n * j + i] = v;
       }
-    if (!chol_lower(out.cov, n, Lf)) {
+    if (!llt_ok(out.cov, n)) {
       const typename L::Pose res2 = L::between(other.pose, pose);
       L::congruence(L::inverse(res2), other.cov, C);
       for (int i = 0; i < n; ++i)
