@@ -450,10 +450,12 @@ int rpgo_max_clique_heu_dev(int32_t n, const uint32_t* adj, int32_t words, int32
  * one file-scope __device__ array of RPGO_CLIQUE_NOALLOC_SCRATCH_BYTES, held
  * by every device that loads the library until the process exits. The first
  * call on a device (with that device current) looks up the array's address
- * with cudaGetSymbolAddress; make that first call before any stream capture.
- * The address is kept for the process: do not call this entry point again
- * after a cudaDeviceReset of that device. Every call shares the one array: calls that overlap on the GPU (from
- * several host threads, or on several streams) race and give wrong results. */
+ * with cudaGetSymbolAddress. Every call synchronises `stream` once per
+ * candidate window (it reads the window's scores back), so it cannot be
+ * captured into a CUDA graph. The address is kept for the process: do not
+ * call this entry point again after a cudaDeviceReset of that device. Every
+ * call shares the one array: calls that overlap on the GPU (from several host
+ * threads, or on several streams) race and give wrong results. */
 #define RPGO_CLIQUE_NOALLOC_MAX_N 4096
 #define RPGO_CLIQUE_NOALLOC_MAX_WORDS 128
 #define RPGO_CLIQUE_NOALLOC_SCRATCH_BYTES 2245632

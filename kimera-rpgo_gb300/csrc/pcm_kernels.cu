@@ -13,6 +13,8 @@
 //                       warp ballot; a second kernel mirrors the lower
 //                       triangle into the upper one with warp bit transposes.
 // All arithmetic is the exact FP64 sequence of pcm_math.cuh.
+#include <type_traits>
+
 #include "pcm_kernels.hpp"
 #include "pcm_math.cuh"
 
@@ -81,6 +83,22 @@ struct PWC {
     L::inverse(other.pose, inv);
     double C[d * d];
     L::congruence(inv, cov, C);
+#pragma unroll
+    for (int i = 0; i < d; ++i)
+#pragma unroll
+      for (int j = 0; j <= i; ++j) {
+        const double v = add(C[d * i + j], other.cov[d * i + j]);
+        out.cov[d * i + j] = v;
+        out.cov[d * j + i] = v;
+      }
+    out.rot = rot && other.rot;
+  }
+  // the same composition with the inverse of other's pose given as its
+  // rotation and the K block of its adjoint (per-closure constants, 3D)
+  __device__ void compose_pre(const PWC& other, const double* pre, PWC& out) const {
+    L::compose(pose, other.pose, out.pose);
+    double C[d * d];
+    pm::p3_congruence_RK(pre, pre + 9, cov, C);
 #pragma unroll
     for (int i = 0; i < d; ++i)
 #pragma unroll
@@ -615,11 +633,30 @@ __global__ void k_odom_check(int64_t count, const int32_t* __restrict__ si, cons
 }
 
 // ------------------------------------------------------------------ K2
+// Per-closure constants of the 3D PoseWithCovariance test: the rotation of
+// the inverse of each measured pose and the K block of that inverse's adjoint
+// (what each composition with the closure computes first), 18 doubles per
+// closure. The pairwise test uses them instead of recomputing them per pair:
+// the same operations, so the same bits.
+constexpr int kClosurePre = 18;
+__global__ void k_closure_pre3(int n, const double* __restrict__ zp, double* __restrict__ pre) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  pm::P3 Z, inv;
+  pm::p3_load(zp + (size_t)k * 12, Z);
+  pm::p3_inverse(Z, inv);
+  double* o = pre + (size_t)k * kClosurePre;
+#pragma unroll
+  for (int e = 0; e < 9; ++e) o[e] = inv.R[e];
+  pm::p3_adjoint_K(inv, o + 9);
+}
+
 template <int DIM, class U>
 __device__ __forceinline__ bool pair_consistent(int i, int j, const int32_t* __restrict__ sa,
                                                 const int32_t* __restrict__ sb, const uint8_t* __restrict__ flip,
                                                 const double* __restrict__ zp, const double* __restrict__ zc,
-                                                const TrajView& tr, double th0, double th1) {
+                                                const TrajView& tr, double th0, double th1,
+                                                const double* __restrict__ pre) {
   using L = Lie<DIM>;
   int a = sa[i], b = sb[i], c = sa[j], dd = sb[j];
   if (flip[i] != flip[j]) {
@@ -635,10 +672,16 @@ __device__ __forceinline__ bool pair_consistent(int i, int j, const int32_t* __r
   Tc.from_traj(tr, dd);
   Ta.between(Tc, B);
   Zj.from_factor(zp + (size_t)j * L::stride, zc + (size_t)j * L::d * L::d);
-  A.compose(Zj, P);
-  P.inverse_inplace();
   Zi.from_factor(zp + (size_t)i * L::stride, zc + (size_t)i * L::d * L::d);
-  P.compose(Zi, Q);
+  if constexpr (std::is_same<U, PWC<3>>::value) {
+    A.compose_pre(Zj, pre + (size_t)j * kClosurePre, P);
+    P.inverse_inplace();
+    P.compose_pre(Zi, pre + (size_t)i * kClosurePre, Q);
+  } else {
+    A.compose(Zj, P);
+    P.inverse_inplace();
+    P.compose(Zi, Q);
+  }
   Q.compose(B, loop);
   return check_u<DIM>(loop, th0, th1);
 }
@@ -696,14 +739,15 @@ __global__ void __launch_bounds__(32 * ROWS) k_pairwise(int n, int row_begin, co
                                                         const uint8_t* __restrict__ flip,
                                                         const double* __restrict__ zp,
                                                         const double* __restrict__ zc, TrajView tr, double th0,
-                                                        double th1, uint32_t* __restrict__ lower, int words) {
+                                                        double th1, uint32_t* __restrict__ lower, int words,
+                                                        const double* __restrict__ pre) {
   const int lane = threadIdx.x;
   const int j = row_begin + ROWS * blockIdx.y + threadIdx.y;
   const int i0 = 32 * blockIdx.x;
   if (j >= n || i0 >= j) return;  // whole warp: tile above the diagonal or past the end
   const int i = i0 + lane;
   bool ok = false;
-  if (i < j) ok = pair_consistent<DIM, U>(i, j, sa, sb, flip, zp, zc, tr, th0, th1);
+  if (i < j) ok = pair_consistent<DIM, U>(i, j, sa, sb, flip, zp, zc, tr, th0, th1, pre);
   const unsigned bits = __ballot_sync(0xffffffffu, ok);
   if (lane == 0) lower[(size_t)(j - row_begin) * words + blockIdx.x] = bits;
 }
@@ -808,21 +852,27 @@ void launch_pairwise(int dim, int mode, int n, int row_begin, const int32_t* sa,
   const int rows = n - row_begin;
   dim3 block(32, ROWS), grid(div_up(n, 32), div_up(rows, ROWS));
   if (n > 1) {
+    DeviceBuffer<double> pre;
+    if (dim == 3 && mode == 0) {
+      pre.resize((size_t)n * kClosurePre);
+      k_closure_pre3<<<div_up(n, 128), 128, 0, st>>>(n, zp, pre.get());
+      RPGO_LAUNCHED();
+    }
     EventTimer timer(st);
     if (dim == 3) {
       if (mode == 0)
         k_pairwise<3, PWC<3>, ROWS><<<grid, block, 0, st>>>(n, row_begin, sa, sb, flip, zp, zc, tr, th0, th1,
-                                                            lower_scratch, words);
+                                                            lower_scratch, words, pre.get());
       else
         k_pairwise<3, PWN<3>, ROWS><<<grid, block, 0, st>>>(n, row_begin, sa, sb, flip, zp, zc, tr, th0, th1,
-                                                            lower_scratch, words);
+                                                            lower_scratch, words, nullptr);
     } else {
       if (mode == 0)
         k_pairwise<2, PWC<2>, ROWS><<<grid, block, 0, st>>>(n, row_begin, sa, sb, flip, zp, zc, tr, th0, th1,
-                                                            lower_scratch, words);
+                                                            lower_scratch, words, nullptr);
       else
         k_pairwise<2, PWN<2>, ROWS><<<grid, block, 0, st>>>(n, row_begin, sa, sb, flip, zp, zc, tr, th0, th1,
-                                                            lower_scratch, words);
+                                                            lower_scratch, words, nullptr);
     }
     RPGO_LAUNCHED();
     kernel_times().pair_ms += timer.elapsed_ms();

@@ -194,8 +194,10 @@ double device_sum(const double* in, int n, DeviceBuffer<double>& red, cudaStream
 // Linearisation of every factor at x (weights w): whitened residual
 // r = sqrt(w) R e, Jacobians (between: J_i = -D Ad(h^-1), J_j = D; prior:
 // J = I), gradient blocks A^T r and Hessian blocks Hii, Hjj, Hij in FP64 and
-// an FP32 copy. Two phases, the Jacobian products spread over d lanes per
-// factor. Phase A, one thread per factor: the
+// an FP32 copy. A between factor forms only A_j = sqrt(w) R D: since
+// A_i = -A_j Ad, its blocks follow as Hjj = A_j^T A_j, Hij = -Ad^T Hjj,
+// Hii = -Hij Ad and gi = -Ad^T gj (156 instead of 228 FMAs per lane). Two
+// phases, the Jacobian products spread over d lanes per factor. Phase A, one thread per factor: the
 // whitened residual r (times sqrt(w)), D = LogmapDerivative(e) and
 // Ad(h^-1) into a per-factor record [r (d), D (dd), Ad (dd), sqrt(w)];
 // for priors D and Ad are unused. Phase B, d lanes per factor (lane a owns
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __res
   constexpr int d = (DIM == 3) ? 6 : 3, dd = d * d, RS = d + 2 * dd + 1;
   constexpr int per_warp = 32 / d;  // factors per warp
   constexpr int warps = 4;
-  __shared__ double sJ[warps][per_warp][dd], sA[warps][per_warp][dd], sB[warps][per_warp][dd];
+  __shared__ double sA[warps][per_warp][dd], sH[warps][per_warp][dd], sg[warps][per_warp][d];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int slot = lane / d, a = lane % d;
   const int f = (blockIdx.x * warps + warp) * per_warp + slot;
@@ -276,76 +278,89 @@ __global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __res
   const double* rc = rec + (size_t)(active ? f : 0) * RS;
   const double* Rf = R + (size_t)(active ? f : 0) * dd;
   const bool between = active && kind[f] == 0;
-  double* Ji = sJ[warp][active ? slot : 0];
-  double* Ai = sA[warp][active ? slot : 0];
-  double* Aj = sB[warp][active ? slot : 0];
+  double* Aj = sA[warp][active ? slot : 0];  // between: Aj = sqrt(w) R D; prior: Ai = sqrt(w) R
+  double* Hs = sH[warp][active ? slot : 0];
+  double* gs = sg[warp][active ? slot : 0];
   const double sw = active ? rc[d + 2 * dd] : 0.0;
-  if (between) {
+  const double* r = rc;
+  float* out = fH ? fH + (size_t)(active ? f : 0) * 3 * dd : nullptr;
+  double* out64 = fH64 + (size_t)(active ? f : 0) * 3 * dd;
+  double* og = fg + (size_t)(active ? f : 0) * 2 * d;
+  // row a of A (Aj for a between factor, Ai for a prior)
+  if (active) {
     const double* D = rc + d;
-    const double* Ad = rc + d + dd;
 #pragma unroll
     for (int j = 0; j < d; ++j) {
       double acc = 0.0;
+      if (between) {
 #pragma unroll
-      for (int k = 0; k < d; ++k) acc += D[d * a + k] * Ad[d * k + j];
-      Ji[d * a + j] = -acc;
+        for (int k = 0; k < d; ++k) acc += Rf[d * a + k] * D[d * k + j];
+      } else {
+        acc = Rf[d * a + j];
+      }
+      Aj[d * a + j] = sw * acc;
     }
   }
   __syncwarp();
+  // H = A^T A (row a), g = A^T r (entry a): Hjj and gj of a between factor,
+  // Hii and gi of a prior
+  double h[d];
+  double ga = 0.0;
   if (active) {
-    if (between) {
-      const double* D = rc + d;
 #pragma unroll
-      for (int j = 0; j < d; ++j) {
-        double ai = 0.0, aj = 0.0;
+    for (int i = 0; i < d; ++i) ga += Aj[d * i + a] * r[i];
 #pragma unroll
-        for (int k = 0; k < d; ++k) {
-          ai += Rf[d * a + k] * Ji[d * k + j];
-          aj += Rf[d * a + k] * D[d * k + j];
-        }
-        Ai[d * a + j] = sw * ai;
-        Aj[d * a + j] = sw * aj;
-      }
-    } else {
+    for (int b = 0; b < d; ++b) {
+      double acc = 0.0;
 #pragma unroll
-      for (int j = 0; j < d; ++j) {
-        Ai[d * a + j] = sw * Rf[d * a + j];
-        Aj[d * a + j] = 0.0;
-      }
+      for (int q = 0; q < d; ++q) acc += Aj[d * q + a] * Aj[d * q + b];
+      h[b] = acc;
+      Hs[d * a + b] = acc;
     }
+    gs[a] = ga;
   }
   __syncwarp();
   if (!active) return;
-  const double* r = rc;
-  double gi = 0.0, gj = 0.0;
+  auto put = [&](int blk, int b, double v) {
+    out64[blk * dd + d * a + b] = v;
+    if (out) out[blk * dd + d * a + b] = (float)v;  // the FP32 copy feeds only the PCG path
+  };
+  if (!between) {
 #pragma unroll
-  for (int i = 0; i < d; ++i) {
-    gi += Ai[d * i + a] * r[i];
-    gj += Aj[d * i + a] * r[i];
+    for (int b = 0; b < d; ++b) {
+      put(0, b, h[b]);
+      put(1, b, 0.0);
+      put(2, b, 0.0);
+    }
+    og[a] = ga;
+    og[d + a] = 0.0;
+    return;
   }
-  double* og = fg + (size_t)f * 2 * d;
-  og[a] = gi;
-  og[d + a] = gj;
-  float* out = fH ? fH + (size_t)f * 3 * dd : nullptr;
-  double* out64 = fH64 + (size_t)f * 3 * dd;
+  // between: J_i = -D Ad, so A_i = -A_j Ad and Hij = A_i^T A_j = -Ad^T Hjj,
+  // Hii = A_i^T A_i = -Hij Ad, gi = A_i^T r = -Ad^T gj
+  const double* Ad = rc + d + dd;
+  double hij[d];
+  double gi = 0.0;
+#pragma unroll
+  for (int k = 0; k < d; ++k) gi += Ad[d * k + a] * gs[k];
 #pragma unroll
   for (int b = 0; b < d; ++b) {
-    double hii = 0.0, hjj = 0.0, hij = 0.0;
+    double acc = 0.0;
 #pragma unroll
-    for (int q = 0; q < d; ++q) {
-      hii += Ai[d * q + a] * Ai[d * q + b];
-      hjj += Aj[d * q + a] * Aj[d * q + b];
-      hij += Ai[d * q + a] * Aj[d * q + b];
-    }
-    out64[d * a + b] = hii;
-    out64[dd + d * a + b] = hjj;
-    out64[2 * dd + d * a + b] = hij;
-    if (fH) {  // the FP32 copy feeds only the PCG path's preconditioner and SpMV
-      out[d * a + b] = (float)hii;
-      out[dd + d * a + b] = (float)hjj;
-      out[2 * dd + d * a + b] = (float)hij;
-    }
+    for (int k = 0; k < d; ++k) acc += Ad[d * k + a] * Hs[d * k + b];
+    hij[b] = -acc;
   }
+#pragma unroll
+  for (int b = 0; b < d; ++b) {
+    double acc = 0.0;
+#pragma unroll
+    for (int l = 0; l < d; ++l) acc += hij[l] * Ad[d * l + b];
+    put(0, b, -acc);
+    put(1, b, h[b]);
+    put(2, b, hij[b]);
+  }
+  og[a] = -gi;
+  og[d + a] = ga;
 }
 
 template <int D>
