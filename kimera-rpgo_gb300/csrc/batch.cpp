@@ -35,6 +35,8 @@ namespace {
 constexpr int kDefaultWorkers = 16;
 // concurrent lock-step groups of the joint batch
 constexpr int kDefaultJointStreams = 4;
+// host threads of the joint batch's per-graph stages (PCM, outputs)
+constexpr int kJointHostThreads = 32;
 // co-resident CTAs of the direct solve per SM (256 threads x 128 registers)
 constexpr int kCholCtasPerSm = 2;
 
@@ -154,7 +156,9 @@ extern "C" int rpgo_solve_batch_joint(const rpgo_params* p, int32_t n, const rpg
     voff[g + 1] = voff[g] + values[g].count;
     foff[g + 1] = foff[g] + factors[g].count;
   }
-  const int threads = kDefaultWorkers;
+  // host threads of the per-graph stages: they mostly wait on their own
+  // streams' short kernels, so more threads than cores keep the GPU busier
+  const int threads = std::min<int>(n, kJointHostThreads);
   // 1. every graph's PCM (and classification) on its own solver, concurrently
   std::vector<rpgo_solver*> sv((size_t)n, nullptr);
   std::vector<int> rc((size_t)n, RPGO_OK), kind((size_t)n, rpgo::kJointNone);

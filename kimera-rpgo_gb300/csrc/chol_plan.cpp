@@ -721,40 +721,55 @@ CholPlan merge_chol_plans(const std::vector<CholPlan>& plans, const std::vector<
   }
   // levels: every plan's level l, then the level's columns by descending
   // block count and its tasks by descending work (as make_chol_plan orders a
-  // level); independent items, so the order changes no result
+  // level; a stable counting sort, the keys being small); independent items,
+  // so the order changes no result
   u.lvl_col_ptr.assign(L + 1, 0);
   u.lvl_task_ptr.assign(L + 1, 0);
   u.lvl_cols.reserve(u.N);
+  std::vector<int32_t> cols_l, cnt;
+  std::vector<std::array<int32_t, 4>> tasks_l;
+  auto task_work = [](const std::array<int32_t, 4>& x) {
+    const int kind = x[3] & 3, n = x[2] - x[1];
+    return kind == 2 ? n : 3 * n + (kind == 1 ? 1 : 0);
+  };
   for (int l = 0; l < L; ++l) {
-    const size_t c_begin = u.lvl_cols.size(), t_begin = u.tasks.size() / 4;
+    cols_l.clear();
+    tasks_l.clear();
     for (int g = 0; g < G; ++g) {
       const CholPlan& p = plans[g];
       if (l >= p.levels()) continue;
       const int v0 = voff[g], b0 = boff[g], s0 = soff[g], u0 = uoff[g], r0 = roff[g];
-      for (int w = p.lvl_col_ptr[l]; w < p.lvl_col_ptr[l + 1]; ++w) u.lvl_cols.push_back(p.lvl_cols[w] + v0);
+      for (int w = p.lvl_col_ptr[l]; w < p.lvl_col_ptr[l + 1]; ++w) cols_l.push_back(p.lvl_cols[w] + v0);
       for (int t = p.lvl_task_ptr[l]; t < p.lvl_task_ptr[l + 1]; ++t) {
         const int32_t* tk = &p.tasks[4 * (size_t)t];
         const int kind = tk[3] & 3, low = tk[3] & 15, slot = tk[3] >> 4;
-        if (kind < 2) u.tasks.insert(u.tasks.end(), {tk[0] + b0, tk[1] + u0, tk[2] + u0, low | (slot + s0) << 4});
-        else u.tasks.insert(u.tasks.end(), {tk[0] + v0, tk[1] + r0, tk[2] + r0, low | (slot + s0) << 4});
+        if (kind < 2) tasks_l.push_back({tk[0] + b0, tk[1] + u0, tk[2] + u0, low | (slot + s0) << 4});
+        else tasks_l.push_back({tk[0] + v0, tk[1] + r0, tk[2] + r0, low | (slot + s0) << 4});
       }
     }
-    std::stable_sort(u.lvl_cols.begin() + c_begin, u.lvl_cols.end(), [&](int32_t a, int32_t b) {
-      return u.col_ptr[a + 1] - u.col_ptr[a] > u.col_ptr[b + 1] - u.col_ptr[b];
-    });
-    const size_t t_end = u.tasks.size() / 4;
-    std::vector<std::array<int32_t, 4>> lt(t_end - t_begin);
-    for (size_t t = t_begin; t < t_end; ++t)
-      lt[t - t_begin] = {u.tasks[4 * t], u.tasks[4 * t + 1], u.tasks[4 * t + 2], u.tasks[4 * t + 3]};
-    auto work = [](const std::array<int32_t, 4>& x) {
-      const int kind = x[3] & 3, n = x[2] - x[1];
-      return kind == 2 ? n : 3 * n + (kind == 1 ? 1 : 0);
-    };
-    std::stable_sort(lt.begin(), lt.end(), [&](const auto& a, const auto& b) { return work(a) > work(b); });
-    for (size_t t = t_begin; t < t_end; ++t)
-      for (int k = 0; k < 4; ++k) u.tasks[4 * t + k] = lt[t - t_begin][k];
+    // columns by descending block count
+    int kmax = 0;
+    for (int32_t c : cols_l) kmax = std::max(kmax, u.col_ptr[c + 1] - u.col_ptr[c]);
+    cnt.assign(kmax + 2, 0);
+    for (int32_t c : cols_l) cnt[kmax - (u.col_ptr[c + 1] - u.col_ptr[c]) + 1]++;
+    for (int k = 1; k <= kmax + 1; ++k) cnt[k] += cnt[k - 1];
+    const size_t c_begin = u.lvl_cols.size();
+    u.lvl_cols.resize(c_begin + cols_l.size());
+    for (int32_t c : cols_l) u.lvl_cols[c_begin + cnt[kmax - (u.col_ptr[c + 1] - u.col_ptr[c])]++] = c;
+    // tasks by descending work
+    int wmax = 0;
+    for (const auto& x : tasks_l) wmax = std::max(wmax, task_work(x));
+    cnt.assign(wmax + 2, 0);
+    for (const auto& x : tasks_l) cnt[wmax - task_work(x) + 1]++;
+    for (int k = 1; k <= wmax + 1; ++k) cnt[k] += cnt[k - 1];
+    const size_t t_begin = u.tasks.size() / 4;
+    u.tasks.resize(u.tasks.size() + 4 * tasks_l.size());
+    for (const auto& x : tasks_l) {
+      const size_t t = t_begin + cnt[wmax - task_work(x)]++;
+      for (int k = 0; k < 4; ++k) u.tasks[4 * t + k] = x[k];
+    }
     u.lvl_col_ptr[l + 1] = (int32_t)u.lvl_cols.size();
-    u.lvl_task_ptr[l + 1] = (int32_t)t_end;
+    u.lvl_task_ptr[l + 1] = (int32_t)(u.tasks.size() / 4);
   }
   u.tupd_ptr.assign(1, 0);
   u.ta_ptr.assign(1, 0);

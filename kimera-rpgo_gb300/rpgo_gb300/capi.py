@@ -168,7 +168,9 @@ def params_struct(p) -> Params:
 
 
 class Batch:
-    """Keeps the numpy arrays alive while the C structs point into them."""
+    """A graph in the C ABI's host layout (rpgo_factor_batch / rpgo_value_batch);
+    keeps the numpy arrays alive while the C structs point into them. Every
+    call that takes a graph also takes a Batch (converted once, reused)."""
 
     def __init__(self, g):
         self.a = g.arrays()
@@ -176,6 +178,10 @@ class Batch:
         self.f = FactorBatch(len(a["kind"]), _ptr(a["kind"]), _ptr(a["key1"]), _ptr(a["key2"]), _ptr(a["measured"]),
                              _ptr(a["cov"]), _ptr(a["sqrt_info"]))
         self.v = ValueBatch(len(a["value_keys"]), _ptr(a["value_keys"]), _ptr(a["value_poses"]))
+
+
+def as_batch(g) -> Batch:
+    return g if isinstance(g, Batch) else Batch(g)
 
 
 class DeviceBatch:
@@ -221,22 +227,22 @@ class RobustSolver:
 
     # ---- reference API
     def update(self, graph, optimize_graph: bool = True) -> int:
-        b = Batch(graph)
+        b = as_batch(graph)
         return load().rpgo_update(self.h, C.byref(b.f), C.byref(b.v), int(optimize_graph))
 
     def update_dev(self, dbatch: "DeviceBatch", optimize_graph: bool = True) -> int:
         return load().rpgo_update_dev(self.h, C.byref(dbatch.f), C.byref(dbatch.v), int(optimize_graph))
 
     def forceUpdate(self, graph) -> int:
-        b = Batch(graph)
+        b = as_batch(graph)
         return load().rpgo_force_update(self.h, C.byref(b.f), C.byref(b.v))
 
     def loadGraph(self, graph, prior) -> int:
-        b, p = Batch(graph), Batch(prior)
+        b, p = as_batch(graph), as_batch(prior)
         return load().rpgo_load_graph(self.h, C.byref(b.f), C.byref(b.v), C.byref(p.f))
 
     def addGraph(self, graph, between) -> int:
-        b, p = Batch(graph), Batch(between)
+        b, p = as_batch(graph), as_batch(between)
         return load().rpgo_add_graph(self.h, C.byref(b.f), C.byref(b.v), C.byref(p.f))
 
     def counts(self) -> Counts:
@@ -277,11 +283,11 @@ class RobustSolver:
 
     # temporary factors and values (GenericSolver.h:46-65)
     def updateTempFactorsValues(self, graph) -> int:
-        b = Batch(graph)
+        b = as_batch(graph)
         return load().rpgo_update_temp_factors_values(self.h, C.byref(b.f), C.byref(b.v))
 
     def replaceTempFactorsValues(self, graph) -> int:
-        b = Batch(graph)
+        b = as_batch(graph)
         return load().rpgo_replace_temp_factors_values(self.h, C.byref(b.f), C.byref(b.v))
 
     def clearTempFactorsValues(self) -> int:
@@ -440,7 +446,7 @@ def solve_batch(params, graphs, workers: int = 0, coop_ctas: int = 0, joint: boo
     Returns a list of (status, keys, poses, gnc_weights, timing) per graph,
     the poses in ascending key order as calculateEstimate() gives them."""
     n = len(graphs)
-    batches = [Batch(g) for g in graphs]
+    batches = [as_batch(g) for g in graphs]
     fb = (FactorBatch * max(n, 1))(*[b.f for b in batches])
     vb = (ValueBatch * max(n, 1))(*[b.v for b in batches])
     dim = 2 if params.outlier_removal in (1, 3) or (params.outlier_removal == 0 and params.dim == 2) else 3
