@@ -195,8 +195,9 @@ int solve_joint(int dim, std::vector<JointProblem*>& probs, cudaStream_t st, int
   double* res = hres.get((size_t)4 * G);  // err (2G), then out (2G)
   const double eps = std::numeric_limits<double>::epsilon();
 
-  // an LM run from the initial values (or the previous estimate) starts in
-  // the next round: reset (unless continuing), error at x, speculative solve
+  // an LM run from the initial values starts in the next round: x <- x0, the
+  // error at x0, and a solve with the initial lambda (used unless the error
+  // at x0 already ends the run)
   auto lm_begin = [&](Graph& x) {
     x.phase = Graph::kLmStart;
     x.lambda = x.p->lm.gauss_newton ? 0.0 : x.p->lm.lambda_initial;
