@@ -286,7 +286,10 @@ __global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __res
   float* out = fH ? fH + (size_t)(active ? f : 0) * 3 * dd : nullptr;
   double* out64 = fH64 + (size_t)(active ? f : 0) * 3 * dd;
   double* og = fg + (size_t)(active ? f : 0) * 2 * d;
-  // row a of A (Aj for a between factor, Ai for a prior)
+  // row a of A (Aj for a between factor, Ai for a prior); in 3D the log-map
+  // derivative D and the adjoint have a zero upper-right 3x3 block, whose
+  // terms are skipped (they add exact zeros)
+  constexpr int zb = DIM == 3 ? 3 : 0;
   if (active) {
     const double* D = rc + d;
 #pragma unroll
@@ -294,7 +297,7 @@ __global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __res
       double acc = 0.0;
       if (between) {
 #pragma unroll
-        for (int k = 0; k < d; ++k) acc += Rf[d * a + k] * D[d * k + j];
+        for (int k = (j >= zb && zb) ? zb : 0; k < d; ++k) acc += Rf[d * a + k] * D[d * k + j];
       } else {
         acc = Rf[d * a + j];
       }
@@ -354,7 +357,7 @@ __global__ void __launch_bounds__(128) k_linearize_b(int F, const int32_t* __res
   for (int b = 0; b < d; ++b) {
     double acc = 0.0;
 #pragma unroll
-    for (int l = 0; l < d; ++l) acc += hij[l] * Ad[d * l + b];
+    for (int l = (b >= zb && zb) ? zb : 0; l < d; ++l) acc += hij[l] * Ad[d * l + b];
     put(0, b, -acc);
     put(1, b, h[b]);
     put(2, b, hij[b]);
