@@ -12,7 +12,7 @@ import pytest
 
 from oracle import rpgo_oracle as O
 from rpgo_gb300 import capi, synth
-from rpgo_gb300.params import GN, QUIET, RobustSolverParams
+from rpgo_gb300.params import GN, LINEAR_PCG, QUIET, RobustSolverParams
 
 ATE_TOL = 1e-4
 SIZES = [(200, 30, 10, 41), (350, 60, 20, 42), (500, 80, 30, 43), (300, 40, 0, 44), (450, 70, 35, 45),
@@ -55,7 +55,7 @@ def test_batch_equals_individual_solves(workers, ctas):
         assert t.gnc_iterations > 0 and t.kernel_launches > 0
 
 
-def _check_against_oracle(params, graphs, res):
+def _check_against_oracle(params, graphs, res, dim=3):
     for s, (status, keys, poses, w, t) in zip(graphs, res):
         assert status == 0
         o = O.OracleSolver(params)
@@ -63,7 +63,7 @@ def _check_against_oracle(params, graphs, res):
         ko, po = o.estimate()
         assert np.array_equal(keys, ko)
         assert np.array_equal(np.round(w), np.round(o.gnc_weights()))
-        assert synth.ate(poses, po, 3) <= ATE_TOL
+        assert synth.ate(poses, po, dim) <= ATE_TOL
 
 
 @pytest.mark.gpu
@@ -102,10 +102,11 @@ def test_joint_batch_matches_oracle_and_individual_solves(group, streams):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("mode", ["gn", "lm_only", "bias_odom", "no_closures"])
+@pytest.mark.parametrize("mode", ["gn", "lm_only", "bias_odom", "no_closures", "pcg"])
 def test_joint_batch_modes_match_oracle(mode):
     # Gauss-Newton under GNC, plain LM without GNC, GNC with odometry-biased
-    # first weights, and graphs whose closures PCM rejects entirely
+    # first weights, graphs whose closures PCM rejects entirely, and the PCG
+    # solver (each graph then solved on its solver's own path)
     from rpgo_gb300 import build
 
     build()
@@ -117,6 +118,8 @@ def test_joint_batch_modes_match_oracle(mode):
         p = RobustSolverParams().setPcm3DParams(10.0, 5.0, QUIET)
     elif mode == "bias_odom":
         p.gnc_bias_odom = 1
+    elif mode == "pcg":
+        p.setLinearSolver(LINEAR_PCG)
     else:
         p = RobustSolverParams().setPcm3DParams(0.0, 0.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
     graphs = [synth.walk3d(n, ni, no, seed=s) for n, ni, no, s in sizes]
@@ -146,3 +149,16 @@ def test_joint_batch_graph_replay_equals_stage_launches():
         assert a[0] == 0 and b[0] == 0
         assert np.array_equal(a[2], b[2]) and np.array_equal(a[3], b[3])
         assert a[4].linear_solves == b[4].linear_solves
+
+
+@pytest.mark.gpu
+def test_joint_batch_2d_matches_oracle():
+    # SE(2) graphs (PCM2D, 3x3 blocks) through the lock-step batch
+    from rpgo_gb300 import build
+
+    build()
+    p = RobustSolverParams().setPcm2DParams(3.0, 3.0, QUIET).setGncInlierCostThresholdsAtProbability(0.9)
+    graphs = [synth.grid2d(n, ni, no, seed=s) for n, ni, no, s in [(300, 60, 12, 61), (500, 100, 20, 62),
+                                                                 (200, 30, 6, 63)]]
+    res = capi.solve_batch(p, [s.graph for s in graphs], joint=True, streams=2)
+    _check_against_oracle(p, graphs, res, dim=2)
