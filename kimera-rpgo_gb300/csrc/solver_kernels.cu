@@ -204,62 +204,82 @@ double device_sum(const double* in, int n, DeviceBuffer<double>& red, cudaStream
 // row a): Ji = -D Ad, Ai = sqrt(w) R Ji, Aj = sqrt(w) R D through shared
 // memory, then gradient entry a and row a of Hii, Hjj, Hij.
 template <int DIM>
-__global__ void k_linearize_a(int F, const int32_t* __restrict__ kind, const int32_t* __restrict__ vi,
-                              const int32_t* __restrict__ vj, const double* __restrict__ z,
-                              const double* __restrict__ R, const double* __restrict__ x,
-                              const double* __restrict__ w, double* __restrict__ rec,
-                              const uint8_t* __restrict__ mask) {
+__global__ void __launch_bounds__(128) k_linearize_a(int F, const int32_t* __restrict__ kind,
+                                                     const int32_t* __restrict__ vi, const int32_t* __restrict__ vj,
+                                                     const double* __restrict__ z, const double* __restrict__ R,
+                                                     const double* __restrict__ x, const double* __restrict__ w,
+                                                     double* __restrict__ rec, const uint8_t* __restrict__ mask) {
   using L = SLie<DIM>;
   constexpr int d = L::d, st = L::stride, dd = d * d, RS = d + 2 * dd + 1;
-  // two threads per factor (the FP64 chain of one thread is the cost, and
+  // Two warps per 32 factors (the FP64 chain of one thread is the cost, and
   // one thread per factor fills only about a quarter of the SM
-  // sub-partitions): both form the residual; role 1 then the log-map
-  // Jacobian, role 0 the whitened residual and the adjoint
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int f = t >> 1, role = t & 1;
-  if (f >= F || (mask && !(mask[f] & 1))) return;
-  const bool between = kind[f] == 0;
-  typename L::Pose Xi, Z, rel, h;
-  L::load(x + (size_t)vi[f] * st, Xi);
-  L::load(z + (size_t)f * st, Z);
-  double e[d];
-  double* out = rec + (size_t)f * RS;
-  if (between) {
-    typename L::Pose Xj;
-    L::load(x + (size_t)vj[f] * st, Xj);
-    L::between(Xi, Xj, h);
-    L::between(Z, h, rel);
-    L::logmap(rel, e);
-    if (role == 1) {
-      double D[dd];
-      L::dlog(e, D);
+  // sub-partitions; roles split by warp, not by lane, so that neither
+  // role's instructions run with half the lanes idle): the role-0 warp forms
+  // the residual, hands its log map to the role-1 warp through shared memory,
+  // then forms the adjoint and the whitened residual; the role-1 warp forms
+  // the log-map Jacobian.
+  __shared__ double sh_e[2][32][d];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int pair = warp >> 1, role = warp & 1;
+  const int f = (blockIdx.x * 2 + pair) * 32 + lane;
+  const bool valid = f < F && (!mask || (mask[f] & 1));
+  const bool between = valid && kind[f] == 0;
+  double* out = rec + (size_t)(valid ? f : 0) * RS;
+  if (role == 0) {
+    typename L::Pose h;
+    double e[d];
 #pragma unroll
-      for (int i = 0; i < dd; ++i) out[d + i] = D[i];
-      return;
+    for (int i = 0; i < d; ++i) e[i] = 0.0;
+    if (valid) {
+      typename L::Pose Xi, Z, rel;
+      L::load(x + (size_t)vi[f] * st, Xi);
+      L::load(z + (size_t)f * st, Z);
+      if (between) {
+        typename L::Pose Xj;
+        L::load(x + (size_t)vj[f] * st, Xj);
+        L::between(Xi, Xj, h);
+        L::between(Z, h, rel);
+      } else {
+        L::between(Xi, Z, rel);
+      }
+      L::logmap(rel, e);
     }
-    typename L::Pose hinv;
-    double Ad[dd];
-    L::inverse(h, hinv);
-    L::adjoint(hinv, Ad);
 #pragma unroll
-    for (int i = 0; i < dd; ++i) out[d + dd + i] = Ad[i];
+    for (int i = 0; i < d; ++i) sh_e[pair][lane][i] = e[i];
+    // (named barrier 1 + pair of the warp pair: role 0 arrives, role 1 waits)
+    asm volatile("bar.arrive %0, 64;" ::"r"(1 + pair) : "memory");
+    if (!valid) return;
+    if (between) {
+      typename L::Pose hinv;
+      double Ad[dd];
+      L::inverse(h, hinv);
+      L::adjoint(hinv, Ad);
+#pragma unroll
+      for (int i = 0; i < dd; ++i) out[d + dd + i] = Ad[i];
+    } else {
+#pragma unroll
+      for (int i = 0; i < d; ++i) e[i] = -e[i];
+    }
+    const double sw = sqrt(w[f]);
+    const double* Rf = R + (size_t)f * dd;
+#pragma unroll
+    for (int i = 0; i < d; ++i) {
+      double acc = 0.0;
+#pragma unroll
+      for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * e[k];
+      out[i] = sw * acc;
+    }
+    out[d + 2 * dd] = sw;
   } else {
-    if (role == 1) return;
-    L::between(Xi, Z, rel);
-    L::logmap(rel, e);
+    asm volatile("bar.sync %0, 64;" ::"r"(1 + pair) : "memory");
+    if (!between) return;
+    double e[d], D[dd];
 #pragma unroll
-    for (int i = 0; i < d; ++i) e[i] = -e[i];
+    for (int i = 0; i < d; ++i) e[i] = sh_e[pair][lane][i];
+    L::dlog(e, D);
+#pragma unroll
+    for (int i = 0; i < dd; ++i) out[d + i] = D[i];
   }
-  const double sw = sqrt(w[f]);
-  const double* Rf = R + (size_t)f * dd;
-#pragma unroll
-  for (int i = 0; i < d; ++i) {
-    double acc = 0.0;
-#pragma unroll
-    for (int k = 0; k < d; ++k) acc += Rf[d * i + k] * e[k];
-    out[i] = sw * acc;
-  }
-  out[d + 2 * dd] = sw;
 }
 
 template <int DIM>
@@ -825,14 +845,14 @@ void solver_linearize(SolverDev& s, bool diagonal_damping, cudaStream_t st) {
     s.lin_rec.resize((size_t)s.F * rs);
     const int per_block = 4 * (32 / d);  // k_linearize_b: 4 warps of 32/d factors
     if (s.dim == 3) {
-      k_linearize_a<3><<<div_up(2 * (int64_t)s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+      k_linearize_a<3><<<div_up(s.F, 64), 128, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                        s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get(), nullptr);
       RPGO_LAUNCHED();
       k_linearize_b<3><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
                                                                need_pcg(s) ? s.fH.get() : nullptr, s.fH64.get(),
                                                                s.fg.get(), nullptr);
     } else {
-      k_linearize_a<2><<<div_up(2 * (int64_t)s.F, tb), tb, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+      k_linearize_a<2><<<div_up(s.F, 64), 128, 0, st>>>(s.F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                        s.sqrt_info.get(), s.x.get(), s.weights.get(), s.lin_rec.get(), nullptr);
       RPGO_LAUNCHED();
       k_linearize_b<2><<<div_up(s.F, per_block), 128, 0, st>>>(s.F, s.kind.get(), s.sqrt_info.get(), s.lin_rec.get(),
@@ -1407,7 +1427,7 @@ static void batch_pre_t(SolverDev& s, BatchDev& b, bool diagonal_damping, bool a
   // linearise, solve, retract, error at xnew: the active graphs
   const int rs = d + 2 * d * d + 1;
   s.lin_rec.resize((size_t)F * rs);
-  k_linearize_a<DIM><<<div_up(2 * (int64_t)F, tb), tb, 0, st>>>(F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
+  k_linearize_a<DIM><<<div_up(F, 64), 128, 0, st>>>(F, s.kind.get(), s.vi.get(), s.vj.get(), s.z.get(),
                                                                 s.sqrt_info.get(), s.x.get(), s.weights.get(),
                                                                 s.lin_rec.get(), b.fmask.get());
   RPGO_LAUNCHED();
