@@ -26,6 +26,13 @@
 // Each round waits on one adjacency row (that of m); the row of B's
 // second-highest element, the next round's m whenever it is adjacent to m
 // (most rounds on dense matrices), is fetched one round ahead.
+// Clean runs: a round whose m is adjacent to every element of B below it
+// only removes m, so the next round's m is B's next element, known before
+// the round. Rounds are therefore taken in batches: the rows of B's 32
+// highest elements u_0 > u_1 > ... are checked against B (independent loads,
+// four rows at a time) and the leading run of clean ones is committed at
+// once (B loses those elements; each goes to the slot of its round); the
+// first element that is not clean takes an ordinary round.
 #include <mutex>
 
 #include "../../include/rpgo_gb300.h"
@@ -61,6 +68,8 @@ __device__ __forceinline__ int warp_max(int v) {
 }
 
 constexpr int kRowRegs = 24;  // register words per lane of a prefetched adjacency row (n <= 24,576)
+constexpr int kWindowThreads = 256;  // block of k_clique_window: 8 candidates
+constexpr int kCleanGroup = 4;       // rows checked together in a clean-run batch
 
 // One warp per candidate of the window [v0, v0 + count).
 // result[s]: -1 pruned (deg < best), -2 cannot beat best, else icc.
@@ -68,8 +77,10 @@ constexpr int kRowRegs = 24;  // register words per lane of a prefetched adjacen
 __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int words, const int32_t* __restrict__ deg,
                                 int v0, int count, int best, int32_t* __restrict__ result,
                                 uint32_t* __restrict__ sets, int32_t* __restrict__ bufs, int buf_len) {
+  __shared__ int sh_top[kWindowThreads / 32][32];
   const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (slot >= count) return;
+  int* const top32 = sh_top[threadIdx.x >> 5];
   const int v = v0 + slot;
   if (best > deg[v]) {
     if (lane == 0) result[slot] = -1;
@@ -98,10 +109,15 @@ __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int wor
   if (lane == 0) buf[0] = v;
   int r = 0;
   // rows of at most 32 * kRowRegs words are held in registers: the row of
-  // this round's m and the prefetched row of the likely next one
-  const bool regs = words <= 32 * kRowRegs;
+  // this round's m and the prefetched row of the likely next one. Only the
+  // first ceil(n / 32) words of a row can hold bits (the row stride `words`
+  // may be a larger capacity)
+  const bool regs = (n + 31) / 32 <= 32 * kRowRegs;
   uint32_t row[kRowRegs], pf[kRowRegs];
   int pf_m = -1;
+  // clean-run batches are tried from round try_at on; after a batch whose
+  // first element was not clean, the next try waits 2, 4, ... 64 rounds
+  int try_at = 0, misses = 0;
   __syncwarp();
   while (true) {
     if (nr == 0) {
@@ -111,6 +127,90 @@ __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int wor
     if (r + nr + 1 <= best) {
       if (lane == 0) result[slot] = -2;
       return;
+    }
+    if (regs && r >= try_at) {
+      // B's (up to) 32 highest elements, descending, into top32
+      int n_top = 0;
+      for (int base = top; base >= 0 && n_top < 32; base -= 32) {
+        const int w = base - lane;  // lane 0 takes the highest word of the chunk
+        const uint32_t x = (w >= 0) ? cur[w] : 0u;
+        const int pc = __popc(x);
+        int incl = pc;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, o);
+          if (lane >= o) incl += y;
+        }
+        uint32_t y = x;
+        int q = n_top + incl - pc;
+        while (y && q < 32) {
+          const int b = 31 - __clz(y);
+          y &= ~(1u << b);
+          top32[q++] = 32 * w + b;
+        }
+        n_top += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      n_top = min(n_top, 32);
+      __syncwarp();
+      // B's words; u_l is clean when B's elements below u_l are all in N(u_l)
+      // (the rounds before it, clean, removed exactly the elements above it)
+      uint32_t bw[kRowRegs];
+#pragma unroll
+      for (int q = 0; q < kRowRegs; ++q) {
+        const int w = lane + 32 * q;
+        bw[q] = (w <= top) ? cur[w] : 0u;
+      }
+      int k = 0;  // leading clean elements
+      while (k < n_top) {
+        const int g = min(kCleanGroup, n_top - k);
+        int uj[kCleanGroup];
+        uint32_t viol[kCleanGroup];
+#pragma unroll
+        for (int j = 0; j < kCleanGroup; ++j) {
+          uj[j] = j < g ? top32[k + j] : -1;
+          viol[j] = 0u;
+        }
+#pragma unroll
+        for (int q = 0; q < kRowRegs; ++q) {
+          const int w = lane + 32 * q;
+#pragma unroll
+          for (int j = 0; j < kCleanGroup; ++j) {
+            const int wl = uj[j] >> 5;  // -1 for an empty entry: no word
+            if (w <= wl) {
+              uint32_t b = bw[q];
+              if (w == wl) b &= (1u << (uj[j] & 31)) - 1u;
+              viol[j] |= b & ~__ldg(adj + (size_t)uj[j] * words + w);
+            }
+          }
+        }
+        unsigned bad = 1u << g;  // the group's leading clean elements: the first bad one's index
+#pragma unroll
+        for (int j = 0; j < kCleanGroup; ++j)
+          if (__any_sync(0xffffffffu, viol[j] != 0u)) bad |= 1u << j;
+        const int clean = __ffs(bad) - 1;
+        k += clean;
+        if (clean < g) break;
+      }
+      if (k > 0) {
+        // rounds r .. r+k-1: B shrinks by its highest element, which goes to
+        // the slot of the round (B's size then)
+        for (int l = lane; l < k; l += 32) buf[nr - l] = top32[l];
+        const int ul = top32[k - 1];
+        __syncwarp();
+        if (lane == 0) cur[ul >> 5] &= (1u << (ul & 31)) - 1u;  // words above top are never read
+        top = ul >> 5;
+        nr -= k;
+        r += k;
+        pf_m = -1;
+        misses = 0;
+        // a batch that stopped early stopped at an element that is not clean:
+        // the next round is an ordinary one
+        try_at = k < n_top ? r + 1 : r;
+        __syncwarp();
+        continue;
+      }
+      misses = min(misses + 1, 6);
+      try_at = r + (1 << misses);
     }
     // m = highest element of B: top word's highest bit
     int m;
@@ -258,7 +358,7 @@ int max_clique_heu(int n, const uint32_t* adj, int words, int first, int seed, s
   int v = std::max(first, 0);
   while (v < n) {
     const int count = std::min(W, n - v);
-    const int tb = 256;
+    const int tb = kWindowThreads;
     k_clique_window<<<div_up((int64_t)count * 32, tb), tb, 0, st>>>(n, adj, words, ws.deg.get(), v, count, best,
                                                                     ws.result.get(), ws.sets.get(),
                                                                     ws.buffers.get(), buf_len);
@@ -365,7 +465,7 @@ int max_clique_heu_noalloc(int n, const uint32_t* adj, int words, int first, int
     int v = std::max(first, 0);
     while (v < n) {
       const int count = std::min(kNoAllocWindow, n - v);
-      const int tb = 256;
+      const int tb = kWindowThreads;
       k_clique_window<<<div_up((int64_t)count * 32, tb), tb, 0, st>>>(n, adj, words, deg, v, count, best, result,
                                                                       sets, bufs, buf_len);
       RPGO_LAUNCHED();
