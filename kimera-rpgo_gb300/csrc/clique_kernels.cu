@@ -29,8 +29,8 @@
 // Clean runs: a round whose m is adjacent to every element of B below it
 // only removes m, so the next round's m is B's next element, known before
 // the round. Rounds are therefore taken in batches: the rows of B's 32
-// highest elements u_0 > u_1 > ... are checked against B (independent loads,
-// four rows at a time) and the leading run of clean ones is committed at
+// highest elements u_0 > u_1 > ... are checked against B (one row per lane,
+// all 32 in flight) and the leading run of clean ones is committed at
 // once (B loses those elements; each goes to the slot of its round); the
 // first element that is not clean takes an ordinary round.
 #include <mutex>
@@ -69,7 +69,6 @@ __device__ __forceinline__ int warp_max(int v) {
 
 constexpr int kRowRegs = 24;  // register words per lane of a prefetched adjacency row (n <= 24,576)
 constexpr int kWindowThreads = 256;  // block of k_clique_window: 8 candidates
-constexpr int kCleanGroup = 4;       // rows checked together in a clean-run batch
 
 // One warp per candidate of the window [v0, v0 + count).
 // result[s]: -1 pruned (deg < best), -2 cannot beat best, else icc.
@@ -113,6 +112,7 @@ __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int wor
   // first ceil(n / 32) words of a row can hold bits (the row stride `words`
   // may be a larger capacity)
   const bool regs = (n + 31) / 32 <= 32 * kRowRegs;
+  const bool vec = (words & 3) == 0 && (reinterpret_cast<uintptr_t>(adj) & 15) == 0;
   uint32_t row[kRowRegs], pf[kRowRegs];
   int pf_m = -1;
   // clean-run batches are tried from round try_at on; after a batch whose
@@ -160,37 +160,61 @@ __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int wor
         const int w = lane + 32 * q;
         bw[q] = (w <= top) ? cur[w] : 0u;
       }
-      int k = 0;  // leading clean elements
-      while (k < n_top) {
-        const int g = min(kCleanGroup, n_top - k);
-        int uj[kCleanGroup];
-        uint32_t viol[kCleanGroup];
-#pragma unroll
-        for (int j = 0; j < kCleanGroup; ++j) {
-          uj[j] = j < g ? top32[k + j] : -1;
-          viol[j] = 0u;
-        }
+      // lane l checks u_l on its own row, 32 words (one line) per step, the
+      // lines two steps ahead prefetched into L1; B's words reach every lane
+      // by shuffles. Loads past u_l's word are clamped to it and masked out:
+      // no divergent branch. Rows whose starts are 16-byte aligned are read
+      // as 4-word vectors.
+      const int u = lane < n_top ? top32[lane] : -1;
+      const int wl = u >> 5;  // -1 for an empty lane: every word masked
+      const uint32_t low = (1u << (u & 31)) - 1u;
+      const uint32_t* const rp = adj + (size_t)(u >= 0 ? u : top32[0]) * words;
+      const int wc = wl >= 0 ? wl : 0;
+      const int wmax = top32[0] >> 5;
+      uint32_t viol = 0u;
+      if (vec) {
 #pragma unroll
         for (int q = 0; q < kRowRegs; ++q) {
-          const int w = lane + 32 * q;
+          if (32 * q > wmax) break;
+          if (32 * q + 64 <= wc) asm volatile("prefetch.global.L1 [%0];" ::"l"(rp + 32 * q + 64));
+          uint4 rw[8];
 #pragma unroll
-          for (int j = 0; j < kCleanGroup; ++j) {
-            const int wl = uj[j] >> 5;  // -1 for an empty entry: no word
-            if (w <= wl) {
-              uint32_t b = bw[q];
-              if (w == wl) b &= (1u << (uj[j] & 31)) - 1u;
-              viol[j] |= b & ~__ldg(adj + (size_t)uj[j] * words + w);
+          for (int j = 0; j < 8; ++j)
+            rw[j] = __ldg(reinterpret_cast<const uint4*>(rp + min(32 * q + 4 * j, wc & ~3)));
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const uint32_t e[4] = {rw[j].x, rw[j].y, rw[j].z, rw[j].w};
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+              const int w = 32 * q + 4 * j + t;
+              const uint32_t b = __shfl_sync(0xffffffffu, bw[q], 4 * j + t);
+              const uint32_t msk = w < wl ? 0xffffffffu : (w == wl ? low : 0u);
+              viol |= b & msk & ~e[t];
             }
           }
+          // u_0 not clean: nothing to commit, the next round is an ordinary one
+          if (__shfl_sync(0xffffffffu, viol, 0) != 0u) break;
         }
-        unsigned bad = 1u << g;  // the group's leading clean elements: the first bad one's index
+      } else {
 #pragma unroll
-        for (int j = 0; j < kCleanGroup; ++j)
-          if (__any_sync(0xffffffffu, viol[j] != 0u)) bad |= 1u << j;
-        const int clean = __ffs(bad) - 1;
-        k += clean;
-        if (clean < g) break;
+        for (int q = 0; q < kRowRegs; ++q) {
+          if (32 * q > wmax) break;
+          if (32 * q + 64 <= wc) asm volatile("prefetch.global.L1 [%0];" ::"l"(rp + 32 * q + 64));
+          uint32_t rw[32];
+#pragma unroll
+          for (int j = 0; j < 32; ++j) rw[j] = __ldg(rp + min(32 * q + j, wc));
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const int w = 32 * q + j;
+            const uint32_t b = __shfl_sync(0xffffffffu, bw[q], j);
+            const uint32_t msk = w < wl ? 0xffffffffu : (w == wl ? low : 0u);
+            viol |= b & msk & ~rw[j];
+          }
+          if (__shfl_sync(0xffffffffu, viol, 0) != 0u) break;
+        }
       }
+      const unsigned bad = __ballot_sync(0xffffffffu, u < 0 || viol != 0u);
+      const int k = bad ? __ffs(bad) - 1 : 32;  // leading clean elements
       if (k > 0) {
         // rounds r .. r+k-1: B shrinks by its highest element, which goes to
         // the slot of the round (B's size then)

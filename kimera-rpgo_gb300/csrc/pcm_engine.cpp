@@ -94,12 +94,15 @@ void PcmEngine::flush_slots() {
   pending_init_.clear();
 }
 
-// adjacency capacity: row_cap rows of row_cap/32 words, zero padded
+// adjacency capacity: row_cap rows of row_cap/32 + 4 words, zero padded. The
+// 16 extra bytes put consecutive row starts in different 128-byte line
+// offsets (the clique kernel reads 32 rows side by side; with a power-of-two
+// stride they all fall into the same L1 sets) and keep rows 16-byte aligned.
 void PcmEngine::grow_adjacency(Group& g, int n) {
   if (n <= g.row_cap) return;
   int cap = g.row_cap ? g.row_cap : 64;
   while (cap < n) cap *= 2;
-  const int words = cap / 32;
+  const int words = cap / 32 + 4;
   DeviceBuffer<uint32_t> nb((size_t)cap * words);
   nb.zero(st_);
   if (g.n > 0)
