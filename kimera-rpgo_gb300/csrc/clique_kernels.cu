@@ -77,9 +77,11 @@ __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int wor
                                 int v0, int count, int best, int32_t* __restrict__ result,
                                 uint32_t* __restrict__ sets, int32_t* __restrict__ bufs, int buf_len) {
   __shared__ int sh_top[kWindowThreads / 32][32];
+  __shared__ __align__(16) uint32_t sh_b[kWindowThreads / 32][32 * kRowRegs];
   const int slot = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (slot >= count) return;
   int* const top32 = sh_top[threadIdx.x >> 5];
+  uint32_t* const bsh = sh_b[threadIdx.x >> 5];
   const int v = v0 + slot;
   if (best > deg[v]) {
     if (lane == 0) result[slot] = -1;
@@ -152,44 +154,53 @@ __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int wor
       }
       n_top = min(n_top, 32);
       __syncwarp();
-      // B's words; u_l is clean when B's elements below u_l are all in N(u_l)
-      // (the rounds before it, clean, removed exactly the elements above it)
-      uint32_t bw[kRowRegs];
-#pragma unroll
-      for (int q = 0; q < kRowRegs; ++q) {
-        const int w = lane + 32 * q;
-        bw[q] = (w <= top) ? cur[w] : 0u;
-      }
+      // B's words into shared memory; u_l is clean when B's elements below
+      // u_l are all in N(u_l) (the rounds before it, clean, removed exactly
+      // the elements above it)
+      const int u0 = top32[0];
+      const int wmax = u0 >> 5;
+      for (int w = lane; w <= wmax; w += 32) bsh[w] = cur[w];
+      __syncwarp();
       // lane l checks u_l on its own row, 32 words (one line) per step, the
-      // lines two steps ahead prefetched into L1; B's words reach every lane
-      // by shuffles. Loads past u_l's word are clamped to it and masked out:
-      // no divergent branch. Rows whose starts are 16-byte aligned are read
-      // as 4-word vectors.
+      // lines two steps ahead prefetched into L1; every lane reads B's words
+      // from shared memory (broadcast). Steps below every lane's last word
+      // need no mask; in the others, loads past u_l's word are clamped to it
+      // and masked out. An empty lane checks u_0's row (its verdict is unused).
       const int u = lane < n_top ? top32[lane] : -1;
-      const int wl = u >> 5;  // -1 for an empty lane: every word masked
-      const uint32_t low = (1u << (u & 31)) - 1u;
-      const uint32_t* const rp = adj + (size_t)(u >= 0 ? u : top32[0]) * words;
-      const int wc = wl >= 0 ? wl : 0;
-      const int wmax = top32[0] >> 5;
+      const int ue = u >= 0 ? u : u0;
+      const int wl = ue >> 5;
+      const uint32_t low = (1u << (ue & 31)) - 1u;
+      const uint32_t* const rp = adj + (size_t)ue * words;
       uint32_t viol = 0u;
       if (vec) {
+        const uint4* const rp4 = reinterpret_cast<const uint4*>(rp);
+        const uint4* const b4 = reinterpret_cast<const uint4*>(bsh);
 #pragma unroll
         for (int q = 0; q < kRowRegs; ++q) {
           if (32 * q > wmax) break;
-          if (32 * q + 64 <= wc) asm volatile("prefetch.global.L1 [%0];" ::"l"(rp + 32 * q + 64));
-          uint4 rw[8];
+          if (32 * q + 64 <= wl) asm volatile("prefetch.global.L1 [%0];" ::"l"(rp + 32 * q + 64));
+          if (__all_sync(0xffffffffu, 32 * q + 31 < wl)) {
 #pragma unroll
-          for (int j = 0; j < 8; ++j)
-            rw[j] = __ldg(reinterpret_cast<const uint4*>(rp + min(32 * q + 4 * j, wc & ~3)));
+            for (int j = 0; j < 8; ++j) {
+              const uint4 r4 = __ldg(rp4 + 8 * q + j);
+              const uint4 bb = b4[8 * q + j];
+              viol |= (bb.x & ~r4.x) | (bb.y & ~r4.y) | (bb.z & ~r4.z) | (bb.w & ~r4.w);
+            }
+          } else {
+            uint4 rw[8];
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const uint32_t e[4] = {rw[j].x, rw[j].y, rw[j].z, rw[j].w};
+            for (int j = 0; j < 8; ++j) rw[j] = __ldg(rp4 + (min(32 * q + 4 * j, wl & ~3) >> 2));
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
-              const int w = 32 * q + 4 * j + t;
-              const uint32_t b = __shfl_sync(0xffffffffu, bw[q], 4 * j + t);
-              const uint32_t msk = w < wl ? 0xffffffffu : (w == wl ? low : 0u);
-              viol |= b & msk & ~e[t];
+            for (int j = 0; j < 8; ++j) {
+              const uint4 bb = b4[8 * q + j];
+              const uint32_t e[4] = {rw[j].x, rw[j].y, rw[j].z, rw[j].w};
+              const uint32_t f[4] = {bb.x, bb.y, bb.z, bb.w};
+#pragma unroll
+              for (int t = 0; t < 4; ++t) {
+                const int w = 32 * q + 4 * j + t;
+                const uint32_t msk = w < wl ? 0xffffffffu : (w == wl ? low : 0u);
+                viol |= f[t] & msk & ~e[t];
+              }
             }
           }
           // u_0 not clean: nothing to commit, the next round is an ordinary one
@@ -199,16 +210,15 @@ __global__ void k_clique_window(int n, const uint32_t* __restrict__ adj, int wor
 #pragma unroll
         for (int q = 0; q < kRowRegs; ++q) {
           if (32 * q > wmax) break;
-          if (32 * q + 64 <= wc) asm volatile("prefetch.global.L1 [%0];" ::"l"(rp + 32 * q + 64));
+          if (32 * q + 64 <= wl) asm volatile("prefetch.global.L1 [%0];" ::"l"(rp + 32 * q + 64));
           uint32_t rw[32];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) rw[j] = __ldg(rp + min(32 * q + j, wc));
+          for (int j = 0; j < 32; ++j) rw[j] = __ldg(rp + min(32 * q + j, wl));
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int w = 32 * q + j;
-            const uint32_t b = __shfl_sync(0xffffffffu, bw[q], j);
             const uint32_t msk = w < wl ? 0xffffffffu : (w == wl ? low : 0u);
-            viol |= b & msk & ~rw[j];
+            viol |= bsh[w] & msk & ~rw[j];
           }
           if (__shfl_sync(0xffffffffu, viol, 0) != 0u) break;
         }
