@@ -283,12 +283,45 @@ struct NestedDissection {
   }
 };
 
-// Symbolic elimination in a given order.
-void eliminate_in_order(std::vector<std::vector<int32_t>>& adj, const std::vector<int32_t>& order,
-                        std::vector<std::vector<int32_t>>* col_vars) {
-  Elimination el(adj);
-  for (int u : order) el.eliminate(u, [](int) {});
-  *col_vars = std::move(el.col_vars);
+// Symbolic elimination in a given order: the same column structures as the
+// elimination game (the neighbours of each variable when it is eliminated),
+// from the elimination tree in time linear in the factor's size. Column j's
+// structure is its later neighbours together with its children's structures
+// less j itself (a child c's parent is the first variable of c's structure).
+// Output: column j (elimination position) holds positions
+// idx[ptr[j] .. ptr[j + 1]), unsorted.
+void eliminate_in_order(const std::vector<std::vector<int32_t>>& adj, const std::vector<int32_t>& order,
+                        std::vector<int32_t>* ptr, std::vector<int32_t>* idx) {
+  const int N = (int)order.size();
+  std::vector<int32_t> pos(adj.size(), -1), mark(N, -1), first_child(N, -1), next_sibling(N, -1);
+  for (int j = 0; j < N; ++j) pos[order[j]] = j;
+  ptr->assign(N + 1, 0);
+  idx->clear();
+  idx->reserve((size_t)8 * N);
+  for (int j = 0; j < N; ++j) {
+    const size_t b = idx->size();
+    for (int w : adj[order[j]]) {
+      const int x = pos[w];
+      if (x > j && mark[x] != j) {
+        mark[x] = j;
+        idx->push_back(x);
+      }
+    }
+    for (int ch = first_child[j]; ch >= 0; ch = next_sibling[ch])
+      for (int q = (*ptr)[ch]; q < (*ptr)[ch + 1]; ++q) {
+        const int x = (*idx)[q];
+        if (x != j && mark[x] != j) {
+          mark[x] = j;
+          idx->push_back(x);
+        }
+      }
+    (*ptr)[j + 1] = (int32_t)idx->size();
+    if (idx->size() > b) {
+      const int parent = *std::min_element(idx->begin() + b, idx->end());
+      next_sibling[j] = first_child[parent];
+      first_child[parent] = j;
+    }
+  }
 }
 
 int find_block(const CholPlan& p, int col, int row) {
@@ -324,30 +357,30 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
   // about kPhaseUs, every FP64 flop of the factorisation kUsPerFlop.
   struct Candidate {
     std::vector<int32_t> perm, pos;
-    std::vector<std::vector<int32_t>> cols;
+    std::vector<int32_t> cptr, cidx;  // column j's rows (positions), ascending
     int T = 0;
     double cost = 0.0;
   };
-  auto make_candidate = [&](std::vector<int32_t>&& perm, const std::vector<std::vector<int32_t>>& col_vars) {
+  // cptr / cidx: column structures by elimination position, unsorted
+  auto make_candidate = [&](std::vector<int32_t>&& perm, std::vector<int32_t>&& cptr, std::vector<int32_t>&& cidx) {
     Candidate c;
     c.perm = std::move(perm);
     c.pos.assign(N, 0);
     for (int j = 0; j < N; ++j) c.pos[c.perm[j]] = j;
-    c.cols.assign(N, {});
-    for (int j = 0; j < N; ++j) {
-      for (int v : col_vars[c.perm[j]]) c.cols[j].push_back(c.pos[v]);
-      std::sort(c.cols[j].begin(), c.cols[j].end());
-    }
+    c.cptr = std::move(cptr);
+    c.cidx = std::move(cidx);
+    for (int j = 0; j < N; ++j) std::sort(c.cidx.begin() + c.cptr[j], c.cidx.begin() + c.cptr[j + 1]);
+    auto size = [&](int j) { return c.cptr[j + 1] - c.cptr[j]; };
     // dense tail: the trailing columns whose structure is complete
-    while (dense_tail && c.T < N && (int)c.cols[N - 1 - c.T].size() == c.T) ++c.T;
+    while (dense_tail && c.T < N && size(N - 1 - c.T) == c.T) ++c.T;
     const int ns = N - c.T;
     std::vector<int32_t> lvl(ns, 0);
     int L = 0;
     double pairs = 0.0;
     for (int j = 0; j < ns; ++j) {
       L = std::max(L, lvl[j] + 1);
-      if (!c.cols[j].empty() && c.cols[j][0] < ns) lvl[c.cols[j][0]] = std::max(lvl[c.cols[j][0]], lvl[j] + 1);
-      const double m = (double)c.cols[j].size();
+      if (size(j) > 0 && c.cidx[c.cptr[j]] < ns) lvl[c.cidx[c.cptr[j]]] = std::max(lvl[c.cidx[c.cptr[j]]], lvl[j] + 1);
+      const double m = (double)size(j);
       pairs += m * (m + 1) / 2;
     }
     const double nt = (double)c.T * d, dd3 = (double)d * d * d;
@@ -365,7 +398,13 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
       std::vector<std::vector<int32_t>> a = adj, col_vars;
       std::vector<int32_t> perm;
       order_variables(N, a, &perm, &col_vars);
-      cands[0] = make_candidate(std::move(perm), col_vars);
+      std::vector<int32_t> pos(N), cptr(N + 1, 0), cidx;
+      for (int j = 0; j < N; ++j) pos[perm[j]] = j;
+      for (int j = 0; j < N; ++j) cptr[j + 1] = cptr[j] + (int32_t)col_vars[perm[j]].size();
+      cidx.reserve(cptr[N]);
+      for (int j = 0; j < N; ++j)
+        for (int v : col_vars[perm[j]]) cidx.push_back(pos[v]);
+      cands[0] = make_candidate(std::move(perm), std::move(cptr), std::move(cidx));
     } catch (...) {
       err[0] = std::current_exception();
     }
@@ -383,17 +422,17 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
     }
     std::thread t_nd([&] {
       try {
-        std::vector<std::vector<int32_t>> a = adj, col_vars;
-        eliminate_in_order(a, nd.out2, &col_vars);
-        cands[2] = make_candidate(std::move(nd.out2), col_vars);
+        std::vector<int32_t> cptr, cidx;
+        eliminate_in_order(adj, nd.out2, &cptr, &cidx);
+        cands[2] = make_candidate(std::move(nd.out2), std::move(cptr), std::move(cidx));
       } catch (...) {
         err[1] = std::current_exception();
       }
     });
     try {
-      std::vector<std::vector<int32_t>> a = adj, col_vars;
-      eliminate_in_order(a, nd.out, &col_vars);
-      cands[1] = make_candidate(std::move(nd.out), col_vars);
+      std::vector<int32_t> cptr, cidx;
+      eliminate_in_order(adj, nd.out, &cptr, &cidx);
+      cands[1] = make_candidate(std::move(nd.out), std::move(cptr), std::move(cidx));
     } catch (...) {
       t_nd.join();
       t_md.join();
@@ -409,7 +448,7 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
     if (cands[c].cost < cands[best].cost) best = c;
   p.perm = std::move(cands[best].perm);
   p.pos = std::move(cands[best].pos);
-  std::vector<std::vector<int32_t>> cols = std::move(cands[best].cols);
+  const std::vector<int32_t> cptr = std::move(cands[best].cptr), cidx = std::move(cands[best].cidx);
   const int T = cands[best].T;
   p.T = T;
   p.n_sparse = N - T;
@@ -418,14 +457,15 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
 
   // sparse blocks
   p.col_ptr.assign(ns + 1, 0);
-  for (int j = 0; j < ns; ++j) p.col_ptr[j + 1] = p.col_ptr[j] + 1 + (int)cols[j].size();
+  for (int j = 0; j < ns; ++j) p.col_ptr[j + 1] = p.col_ptr[j] + 1 + (cptr[j + 1] - cptr[j]);
   p.blk_row.resize(p.col_ptr[ns]);
   p.blk_col.resize(p.col_ptr[ns]);
   for (int j = 0; j < ns; ++j) {
     int q = p.col_ptr[j];
     p.blk_row[q] = j;
     p.blk_col[q] = j;
-    for (int r : cols[j]) {
+    for (int e = cptr[j]; e < cptr[j + 1]; ++e) {
+      const int r = cidx[e];
       ++q;
       p.blk_row[q] = r;
       p.blk_col[q] = j;
@@ -436,7 +476,7 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
   int L = 0;
   for (int j = 0; j < ns; ++j) {
     L = std::max(L, lvl[j] + 1);
-    if (!cols[j].empty() && cols[j][0] < ns) lvl[cols[j][0]] = std::max(lvl[cols[j][0]], lvl[j] + 1);
+    if (cptr[j + 1] > cptr[j] && cidx[cptr[j]] < ns) lvl[cidx[cptr[j]]] = std::max(lvl[cidx[cptr[j]]], lvl[j] + 1);
   }
   p.lvl_col_ptr.assign(L + 1, 0);
   for (int j = 0; j < ns; ++j) p.lvl_col_ptr[lvl[j] + 1] += 1;
@@ -575,6 +615,13 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
   p.tasks.clear();
   {
     const int halves = d == 6 ? 2 : 1;
+    {
+      size_t n = 0;  // tasks, for the reservation
+      for (int q = 0; q < nblk; ++q) n += (size_t)halves * ((p.upd_ptr[q + 1] - p.upd_ptr[q] + p.chunk - 1) / p.chunk);
+      for (int j = 0; j < ns; ++j) n += (size_t)((p.row_ptr[j + 1] - p.row_ptr[j] + p.row_chunk - 1) / p.row_chunk);
+      p.tasks.reserve(4 * n);
+    }
+    std::vector<int32_t> lt;
     int slot = 0;
     for (int l = 0; l < L; ++l) {
       for (int w = p.lvl_col_ptr[l]; w < p.lvl_col_ptr[l + 1]; ++w) {
@@ -610,16 +657,24 @@ CholPlan make_chol_plan(int N, int d, const std::vector<int32_t>& kind, const st
       // that the lane groups of a warp, which take consecutive tasks on wide
       // levels, get similar loops; the order of independent tasks changes no
       // result
+      // (a stable counting sort: the weights are small integers)
       const int t0 = p.lvl_task_ptr[l], t1 = (int)p.tasks.size() / 4;
-      std::vector<std::array<int32_t, 4>> lt((size_t)(t1 - t0));
-      for (int t = t0; t < t1; ++t) lt[t - t0] = {p.tasks[4 * t], p.tasks[4 * t + 1], p.tasks[4 * t + 2], p.tasks[4 * t + 3]};
-      auto work = [](const std::array<int32_t, 4>& x) {
-        const int kind = x[3] & 3, n = x[2] - x[1];
+      auto work = [&](int t) {
+        const int kind = p.tasks[4 * t + 3] & 3, n = p.tasks[4 * t + 2] - p.tasks[4 * t + 1];
         return kind == 2 ? n : 3 * n + (kind == 1 ? 1 : 0);
       };
-      std::stable_sort(lt.begin(), lt.end(), [&](const auto& a, const auto& b) { return work(a) > work(b); });
-      for (int t = t0; t < t1; ++t)
-        for (int k = 0; k < 4; ++k) p.tasks[4 * t + k] = lt[t - t0][k];
+      int wmax = 0;
+      for (int t = t0; t < t1; ++t) wmax = std::max(wmax, work(t));
+      std::vector<int32_t> at((size_t)wmax + 2, 0);  // at[wmax - w + 1]: tasks of weight w
+      for (int t = t0; t < t1; ++t) at[(size_t)(wmax - work(t)) + 1]++;
+      for (int w = 1; w <= wmax + 1; ++w) at[w] += at[w - 1];
+      lt.assign(p.tasks.begin() + 4 * (size_t)t0, p.tasks.begin() + 4 * (size_t)t1);
+      for (int t = 0; t < t1 - t0; ++t) {
+        const int x = lt[4 * t + 3] & 3, n = lt[4 * t + 2] - lt[4 * t + 1];
+        const int w = x == 2 ? n : 3 * n + (x == 1 ? 1 : 0);
+        const int dst = t0 + at[wmax - w]++;
+        for (int k = 0; k < 4; ++k) p.tasks[4 * (size_t)dst + k] = lt[4 * t + k];
+      }
       p.lvl_task_ptr[l + 1] = t1;
     }
     p.n_slots = slot;
