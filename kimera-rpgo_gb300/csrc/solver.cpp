@@ -6,6 +6,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <unordered_map>
 
 namespace rpgo {
 
@@ -13,7 +14,8 @@ GpuNls::GpuNls(int dim, const std::vector<FactorRec>& graph, const FactorStore& 
                cudaStream_t st, bool direct)
     : dim_(dim), st_(st) {
   const int stride = dim == 3 ? 12 : 4, d = dim == 3 ? 6 : 3;
-  std::map<uint64_t, int> index;
+  std::unordered_map<uint64_t, int> index;
+  index.reserve(values.size());
   std::vector<int64_t> vrows;
   vrows.reserve(values.size());
   for (const auto& kv : values.rows()) {

@@ -27,6 +27,8 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <exception>
+#include <thread>
 
 #include "chol.hpp"
 #include "solver_kernels.hpp"
@@ -680,6 +682,24 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   s.N = N;
   s.F = (int)kind.size();
   const int d = s.d, dd = d * d, F = s.F;
+  // the direct solve's plan (host work only) is built on its own thread while
+  // the lists below are built and uploaded
+  CholPlan plan;
+  std::exception_ptr plan_err;
+  struct Joiner {
+    std::thread t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  } planner;
+  if (direct && N > 0 && !given)
+    planner.t = std::thread([&] {
+      try {
+        plan = make_chol_plan(N, d, kind, vi, vj);
+      } catch (...) {
+        plan_err = std::current_exception();
+      }
+    });
   std::vector<uint8_t> tree(F, 0), has_tree(N, 0);
   std::vector<int32_t> deg(N + 1, 0);
   for (int f = 0; f < F; ++f) {
@@ -780,7 +800,9 @@ void solver_upload(SolverDev& s, int dim, const std::vector<int32_t>& kind, cons
   s.out.resize(8);
   s.chol.reset();
   if (direct && N > 0) {
-    CholPlan plan = given ? std::move(*given) : make_chol_plan(N, d, kind, vi, vj);
+    if (planner.t.joinable()) planner.t.join();
+    if (plan_err) std::rethrow_exception(plan_err);
+    if (given) plan = std::move(*given);
     const double ntp = (double)plan.n_tiles * plan.tile;
     const double bytes = 8.0 * dd * (plan.n_blocks() + plan.n_sparse) + 8.0 * ntp * ntp +
                          4.0 * (plan.upd_src.size() + plan.tupd_src.size());
