@@ -170,8 +170,8 @@ struct NestedDissection {
   // two: the set is still above leaf2 for the second order; the two halves
   // of a large set in the first kParDepth splits are ordered concurrently
   // (a second instance on its own thread, its orders inserted before the
-  // other half's: the same orders as one thread's)
-  static constexpr int kParDepth = 2, kParMin = 2048;
+  // other half's: the same orders as one thread's); up to 16 threads
+  static constexpr int kParDepth = 4, kParMin = 2048;
   void run(std::vector<int32_t> nodes, bool two, int split = 0) {
     if (two && (int)nodes.size() <= leaf2) {
       std::vector<int32_t> sorted = nodes;
